@@ -1,0 +1,129 @@
+"""ctypes binding of the C ABI in include/sph_gb300.h (libsph_gb300.so).
+
+The product path has no CPU fallback: if the library is missing or no CUDA device is
+present, every entry point raises.  Torch tensors are passed as raw device pointers
+(`tensor.data_ptr()`), and work is issued on torch's current CUDA stream so that torch
+allocations, CUDA graphs and the library's kernels share one ordering.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import threading
+
+import torch
+
+from . import build as _build
+
+_P = ctypes.c_void_p
+_I64 = ctypes.c_int64
+_I32 = ctypes.c_int32
+_F32 = ctypes.c_float
+_SZ = ctypes.c_size_t
+
+# name -> (restype, argtypes); mirrors include/sph_gb300.h
+SIGNATURES = {
+    "sph_abi_version": (_I32, []),
+    "sph_last_error": (ctypes.c_char_p, []),
+    "sph_status_string": (ctypes.c_char_p, [_I32]),
+    "sph_scan_scratch_bytes": (_SZ, [_I64]),
+    "sph_exclusive_scan_i32": (_I32, [_P, _P, _I64, _P, _SZ, _P]),
+    "sph_exclusive_scan_i32_to_i64": (_I32, [_P, _P, _I64, _P, _SZ, _P]),
+    "sph_radix_sort_scratch_bytes": (_SZ, [_I64, _I32]),
+    "sph_radix_sort_pairs": (_I32, [_P, _P, _I64, _I32, _I32, _P, _SZ, _P]),
+    "sph_grid_scratch_bytes": (_SZ, [_I64]),
+    "sph_grid_build": (_I32, [_P, _P, _I64, _P, _P, _I32, _P, _P, _P, _SZ, _P]),
+    "sph_cell_keys": (_I32, [_P, _I64, _P, _I32, _P, _P, _P, _P]),
+    "sph_key_bits": (_I32, [_I32]),
+    "sph_cell_starts": (_I32, [_P, _I64, _I32, _P, _P]),
+    "sph_gather_packed": (_I32, [_P, _I64, _P, _P, _P, _P, _P]),
+    "sph_hash_map_scratch_bytes": (_SZ, [_I64, _I32]),
+    "sph_hash_map_build": (_I32, [_P, _I64, _I32, _I32, _P, _P, _P, _P, _P, _P, _SZ, _P]),
+    "sph_nl_count": (_I32, [_P, _I64, _P, _P, _P, _I32, _I32, _F32, _P, _P, _P]),
+    "sph_nl_fill": (_I32, [_P, _I64, _P, _P, _P, _I32, _I32, _P, _I64, _P, _P, _P]),
+    "sph_scatter_f32": (_I32, [_P, _P, _I64, _P, _P]),
+    "sph_nl_to_coo": (_I32, [_P, _I64, _P, _P, _P, _P, _P, _F32, _F32, _P, _I64, _P, _P, _P]),
+    "sph_scatter_counts": (_I32, [_P, _P, _I64, _P, _P]),
+    "sph_invert_permutation": (_I32, [_P, _I64, _P, _P]),
+    "sph_nl_query_count": (_I32, [_P, _P, _I64, _P, _P, _P, _I32, _I32, _P, _P]),
+    "sph_nl_query_fill": (_I32, [_P, _P, _I64, _P, _P, _P, _I32, _I32, _P, _P, _P, _P, _P]),
+    "sph_nl_hashed_query_count": (_I32, [_P, _P, _I64, _P, _P, _P, _P, _P, _P, _F32, _I32, _I32, _I32, _P, _P]),
+    "sph_nl_hashed_query_fill": (_I32, [_P, _P, _I64, _P, _P, _P, _P, _P, _P, _P, _F32, _I32, _I32, _I32, _P,
+                                        _P, _P, _P]),
+    "sph_nl_hashed_cells_count": (_I32, [_P, _P, _P, _P, _P, _P, _I64, _I32, _I32, _I32, _P, _P]),
+    "sph_nl_hashed_cells_fill": (_I32, [_P, _P, _P, _P, _P, _P, _P, _I64, _I32, _I32, _I32, _P, _P, _P, _P]),
+    "sph_nl_hashed_asym_count": (_I32, [_P, _P, _P, _P, _P, _P, _I64, _P, _P, _P, _P, _P, _I32, _I32, _P, _P]),
+    "sph_nl_hashed_asym_fill": (_I32, [_P, _P, _P, _P, _P, _P, _P, _I64, _P, _P, _P, _P, _P, _P, _I32, _I32, _P,
+                                       _P, _P, _P]),
+}
+
+SPH_FLAG_OUT_OF_GRID = 1
+SPH_FLAG_NONFINITE = 2
+SPH_FLAG_PAIR_CAPACITY = 4
+SPH_FLAG_CELL_CAPACITY = 8
+SPH_FLAG_ITERATION_CAP = 16
+
+FLAG_NAMES = {
+    SPH_FLAG_OUT_OF_GRID: "a particle lies outside the search grid",
+    SPH_FLAG_NONFINITE: "non-finite value (NaN/Inf) in positions or results",
+    SPH_FLAG_PAIR_CAPACITY: "neighbor pair buffer too small",
+    SPH_FLAG_CELL_CAPACITY: "search grid has more cells than the cell table holds",
+    SPH_FLAG_ITERATION_CAP: "an iterative solve stopped at its maximum iteration count",
+}
+
+_lib = None
+_lock = threading.Lock()
+
+
+class SPHError(RuntimeError):
+    """Raised when a GB300 kernel reports a failure (the reference raises RuntimeError too)."""
+
+
+def library_path() -> str:
+    return _build.LIB_PATH
+
+
+def load(require_cuda: bool = True):
+    """Load libsph_gb300.so; raises if it is missing (no CPU fallback exists)."""
+    global _lib
+    if require_cuda and not torch.cuda.is_available():
+        raise SPHError("pytorchsph_gb300 needs a CUDA device (GB300, sm_103a); there is no CPU path")
+    with _lock:
+        if _lib is None:
+            path = library_path()
+            if not os.path.exists(path):
+                raise SPHError(f"GB300 library not built: {path} is missing; run pytorchsph_gb300.build.build()")
+            lib = ctypes.CDLL(path)
+            for name, (res, args) in SIGNATURES.items():
+                fn = getattr(lib, name)
+                fn.restype = res
+                fn.argtypes = args
+            _lib = lib
+    return _lib
+
+
+def check(status: int, what: str = ""):
+    if status != 0:
+        lib = load(require_cuda=False)
+        msg = lib.sph_last_error().decode(errors="replace")
+        kind = lib.sph_status_string(status).decode()
+        raise SPHError(f"{what}: {kind}: {msg}")
+
+
+def call(name: str, *args):
+    fn = getattr(load(), name)
+    check(fn(*args), name)
+
+
+def ptr(t) -> int | None:
+    if t is None:
+        return None
+    return t.data_ptr()
+
+
+def stream_ptr() -> int:
+    return torch.cuda.current_stream().cuda_stream
+
+
+def decode_flags(flags: int) -> str:
+    return "; ".join(msg for bit, msg in FLAG_NAMES.items() if flags & bit) or "ok"

@@ -1,0 +1,335 @@
+// Device-wide exclusive scan and stable LSD radix sort (sm_103a), plus the C-ABI error
+// plumbing.  Both primitives are reduce-then-scan designs: no block ever waits on
+// another block, so there is no inter-block spin and nothing can hang.
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+
+#include "sph_common.cuh"
+
+namespace sph {
+
+static thread_local char g_err[512] = "";
+
+void set_error(const char* where, cudaError_t err) {
+  snprintf(g_err, sizeof(g_err), "%s: %s", where, cudaGetErrorString(err));
+}
+void set_error_text(const char* text) { snprintf(g_err, sizeof(g_err), "%s", text); }
+
+// ------------------------------------------------------------------ scan
+constexpr int kScanThreads = 256;
+constexpr int kScanItems = 16;
+constexpr int kScanTile = kScanThreads * kScanItems;  // 4096
+
+template <typename T>
+__device__ __forceinline__ T warp_incl_scan(T v) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    T t = __shfl_up_sync(0xffffffffu, v, o);
+    if (lane >= o) v += t;
+  }
+  return v;
+}
+
+// Block-wide exclusive scan of one value per thread; returns the block total via *total.
+template <typename T>
+__device__ __forceinline__ T block_excl_scan(T v, T* smem_warp, T* total) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int nwarps = blockDim.x >> 5;
+  T incl = warp_incl_scan(v);
+  if (lane == 31) smem_warp[warp] = incl;
+  __syncthreads();
+  if (warp == 0) {
+    T w = lane < nwarps ? smem_warp[lane] : T(0);
+    T wi = warp_incl_scan(w);
+    if (lane < nwarps) smem_warp[lane] = wi - w;
+    if (lane == nwarps - 1) smem_warp[32] = wi;
+  }
+  __syncthreads();
+  T res = incl - v + smem_warp[warp];
+  *total = smem_warp[32];
+  __syncthreads();
+  return res;
+}
+
+template <typename TOut>
+__global__ void __launch_bounds__(kScanThreads) k_scan_reduce(const int32_t* __restrict__ in, int64_t n,
+                                                              TOut* __restrict__ block_sums) {
+  __shared__ TOut sw[33];
+  const int64_t base = (int64_t)blockIdx.x * kScanTile;
+  TOut s = 0;
+#pragma unroll
+  for (int k = 0; k < kScanItems; ++k) {
+    int64_t idx = base + (int64_t)k * kScanThreads + threadIdx.x;
+    if (idx < n) s += (TOut)in[idx];
+  }
+  TOut total;
+  block_excl_scan<TOut>(s, sw, &total);
+  if (threadIdx.x == 0) block_sums[blockIdx.x] = total;
+}
+
+// Single block: exclusive scan of block_sums in place (any count, chunked).
+template <typename TOut>
+__global__ void __launch_bounds__(1024) k_scan_sums(TOut* __restrict__ sums, int64_t nb) {
+  __shared__ TOut sw[33];
+  TOut carry = 0;
+  for (int64_t base = 0; base < nb; base += blockDim.x) {
+    int64_t idx = base + threadIdx.x;
+    TOut v = idx < nb ? sums[idx] : TOut(0);
+    TOut total;
+    TOut ex = block_excl_scan<TOut>(v, sw, &total);
+    if (idx < nb) sums[idx] = ex + carry;
+    carry += total;
+  }
+  if (threadIdx.x == 0) sums[nb] = carry;
+}
+
+// Each thread owns kScanItems consecutive items (blocked layout), so a tile is read in
+// two coalesced sweeps through shared memory.
+template <typename TOut>
+__global__ void __launch_bounds__(kScanThreads) k_scan_down(const int32_t* __restrict__ in, TOut* __restrict__ out,
+                                                            int64_t n, const TOut* __restrict__ block_offsets) {
+  __shared__ TOut sw[33];
+  __shared__ int32_t tile[kScanTile];
+  const int64_t base = (int64_t)blockIdx.x * kScanTile;
+#pragma unroll
+  for (int k = 0; k < kScanItems; ++k) {
+    int64_t idx = base + (int64_t)k * kScanThreads + threadIdx.x;
+    tile[k * kScanThreads + threadIdx.x] = idx < n ? in[idx] : 0;
+  }
+  __syncthreads();
+  TOut local[kScanItems];
+  TOut s = 0;
+#pragma unroll
+  for (int k = 0; k < kScanItems; ++k) {
+    local[k] = s;
+    s += (TOut)tile[threadIdx.x * kScanItems + k];
+  }
+  TOut total;
+  TOut ex = block_excl_scan<TOut>(s, sw, &total) + block_offsets[blockIdx.x];
+  __syncthreads();
+  TOut* otile = reinterpret_cast<TOut*>(tile);  // reuse only when sizeof(TOut)==4
+  if (sizeof(TOut) == 4) {
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) otile[threadIdx.x * kScanItems + k] = ex + local[k];
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+      int64_t idx = base + (int64_t)k * kScanThreads + threadIdx.x;
+      if (idx < n) out[idx] = otile[k * kScanThreads + threadIdx.x];
+    }
+  } else {
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+      int64_t idx = base + (int64_t)threadIdx.x * kScanItems + k;
+      if (idx < n) out[idx] = ex + local[k];
+    }
+  }
+  if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) out[n] = block_offsets[gridDim.x];
+}
+
+static int64_t scan_blocks(int64_t n) { return (n + kScanTile - 1) / kScanTile; }
+
+template <typename TOut>
+static sph_status_t scan_impl(const int32_t* in, TOut* out, int64_t n, void* scratch, size_t scratch_bytes,
+                              void* stream) {
+  SPH_REQUIRE(n >= 0 && out != nullptr, "scan: bad arguments");
+  cudaStream_t st = as_stream(stream);
+  if (n == 0) {
+    cudaMemsetAsync(out, 0, sizeof(TOut), st);
+    SPH_CHECK_LAUNCH("scan(memset)");
+    return SPH_OK;
+  }
+  int64_t nb = scan_blocks(n);
+  if (scratch_bytes < (size_t)(nb + 1) * sizeof(int64_t) || scratch == nullptr) {
+    set_error_text("scan: scratch too small");
+    return SPH_ERR_SCRATCH_TOO_SMALL;
+  }
+  TOut* sums = reinterpret_cast<TOut*>(scratch);
+  k_scan_reduce<TOut><<<(unsigned)nb, kScanThreads, 0, st>>>(in, n, sums);
+  k_scan_sums<TOut><<<1, 1024, 0, st>>>(sums, nb);
+  k_scan_down<TOut><<<(unsigned)nb, kScanThreads, 0, st>>>(in, out, n, sums);
+  SPH_CHECK_LAUNCH("scan");
+  return SPH_OK;
+}
+
+// ------------------------------------------------------------------ radix sort
+constexpr int kRsThreads = 256;
+constexpr int kRsWarps = kRsThreads / 32;
+constexpr int kRsRounds = 8;
+constexpr int kRsTile = kRsThreads * kRsRounds;  // 2048 keys per block
+
+__global__ void __launch_bounds__(kRsThreads) k_radix_hist(const uint32_t* __restrict__ keys, int64_t n, int shift,
+                                                           int digit_bits, int32_t* __restrict__ hist, int ntiles) {
+  __shared__ int32_t cnt[256];
+  const int nd = 1 << digit_bits;
+  const uint32_t mask = (uint32_t)nd - 1u;
+  for (int d = threadIdx.x; d < nd; d += kRsThreads) cnt[d] = 0;
+  __syncthreads();
+  const int64_t base = (int64_t)blockIdx.x * kRsTile;
+#pragma unroll
+  for (int r = 0; r < kRsRounds; ++r) {
+    int64_t idx = base + (int64_t)r * kRsThreads + threadIdx.x;
+    if (idx < n) atomicAdd(&cnt[(keys[idx] >> shift) & mask], 1);
+  }
+  __syncthreads();
+  for (int d = threadIdx.x; d < nd; d += kRsThreads) hist[(int64_t)d * ntiles + blockIdx.x] = cnt[d];
+}
+
+// Stable scatter: tile order = (round, warp, lane); the rank of an item among equal
+// digits is (count in earlier rounds) + (count in earlier warps of this round) +
+// (count among earlier lanes, from __match_any_sync).
+__global__ void __launch_bounds__(kRsThreads) k_radix_scatter(const uint32_t* __restrict__ keys_in,
+                                                              const uint32_t* __restrict__ vals_in,
+                                                              uint32_t* __restrict__ keys_out,
+                                                              uint32_t* __restrict__ vals_out, int64_t n, int shift,
+                                                              int digit_bits, const int32_t* __restrict__ offsets,
+                                                              int ntiles) {
+  __shared__ int32_t s_wc[kRsWarps][256];
+  __shared__ int32_t s_run[256];
+  __shared__ int32_t s_goff[256];
+  const int nd = 1 << digit_bits;
+  const uint32_t mask = (uint32_t)nd - 1u;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int d = threadIdx.x; d < nd; d += kRsThreads) {
+    s_run[d] = 0;
+    s_goff[d] = offsets[(int64_t)d * ntiles + blockIdx.x];
+#pragma unroll
+    for (int w = 0; w < kRsWarps; ++w) s_wc[w][d] = 0;
+  }
+  __syncthreads();
+  const int64_t base = (int64_t)blockIdx.x * kRsTile;
+  const unsigned lt_mask = (1u << lane) - 1u;
+  for (int r = 0; r < kRsRounds; ++r) {
+    int64_t idx = base + (int64_t)r * kRsThreads + threadIdx.x;
+    bool valid = idx < n;
+    uint32_t key = valid ? keys_in[idx] : 0u;
+    uint32_t val = valid ? vals_in[idx] : 0u;
+    uint32_t d = (key >> shift) & mask;
+    unsigned match_key = valid ? d : 0xffffffffu;
+    unsigned peers = __match_any_sync(0xffffffffu, match_key);
+    int rank = __popc(peers & lt_mask);
+    bool leader = valid && (rank == 0);
+    if (leader) s_wc[warp][d] = __popc(peers);
+    __syncthreads();
+    for (int dd = threadIdx.x; dd < nd; dd += kRsThreads) {
+      int run = s_run[dd];
+#pragma unroll
+      for (int w = 0; w < kRsWarps; ++w) {
+        int c = s_wc[w][dd];
+        s_wc[w][dd] = run;
+        run += c;
+      }
+      s_run[dd] = run;
+    }
+    __syncthreads();
+    if (valid) {
+      int dst = s_goff[d] + s_wc[warp][d] + rank;
+      keys_out[dst] = key;
+      vals_out[dst] = val;
+    }
+    __syncthreads();
+    for (int dd = threadIdx.x; dd < nd; dd += kRsThreads) {
+#pragma unroll
+      for (int w = 0; w < kRsWarps; ++w) s_wc[w][dd] = 0;
+    }
+    __syncthreads();
+  }
+}
+
+static int64_t rs_tiles(int64_t n) { return (n + kRsTile - 1) / kRsTile; }
+
+}  // namespace sph
+
+using namespace sph;
+
+extern "C" {
+
+int32_t sph_abi_version(void) { return 1; }
+
+const char* sph_last_error(void) { return sph::g_err; }
+
+const char* sph_status_string(sph_status_t s) {
+  switch (s) {
+    case SPH_OK: return "ok";
+    case SPH_ERR_INVALID_ARGUMENT: return "invalid argument";
+    case SPH_ERR_CUDA: return "CUDA error";
+    case SPH_ERR_SCRATCH_TOO_SMALL: return "scratch buffer too small";
+    default: return "unknown status";
+  }
+}
+
+size_t sph_scan_scratch_bytes(int64_t n) { return (size_t)(scan_blocks(n < 1 ? 1 : n) + 1) * sizeof(int64_t); }
+
+sph_status_t sph_exclusive_scan_i32(const int32_t* in, int32_t* out, int64_t n, void* scratch, size_t scratch_bytes,
+                                    void* stream) {
+  SPH_REQUIRE(n < (int64_t)1 << 31, "scan: n must be < 2^31 for int32 offsets");
+  return scan_impl<int32_t>(in, out, n, scratch, scratch_bytes, stream);
+}
+
+sph_status_t sph_exclusive_scan_i32_to_i64(const int32_t* in, int64_t* out, int64_t n, void* scratch,
+                                           size_t scratch_bytes, void* stream) {
+  return scan_impl<int64_t>(in, out, n, scratch, scratch_bytes, stream);
+}
+
+size_t sph_radix_sort_scratch_bytes(int64_t n, int32_t digit_bits) {
+  if (digit_bits < 1) digit_bits = 1;
+  if (digit_bits > 8) digit_bits = 8;
+  int64_t nt = rs_tiles(n < 1 ? 1 : n);
+  size_t hist = (size_t)(nt << digit_bits) + 1;
+  size_t bytes = 2 * (size_t)n * sizeof(uint32_t);  // ping-pong keys + vals
+  bytes += 2 * hist * sizeof(int32_t);              // histogram + scanned offsets
+  bytes += sph_scan_scratch_bytes((int64_t)hist);
+  return bytes + 256;
+}
+
+sph_status_t sph_radix_sort_pairs(uint32_t* keys, uint32_t* vals, int64_t n, int32_t key_bits, int32_t digit_bits,
+                                  void* scratch, size_t scratch_bytes, void* stream) {
+  SPH_REQUIRE(n >= 0 && n < ((int64_t)1 << 31), "radix sort: n out of range");
+  SPH_REQUIRE(digit_bits >= 1 && digit_bits <= 8, "radix sort: digit_bits must be 1..8");
+  SPH_REQUIRE(key_bits >= 0 && key_bits <= 32, "radix sort: key_bits must be 0..32");
+  if (n <= 1 || key_bits == 0) return SPH_OK;
+  if (scratch == nullptr || scratch_bytes < sph_radix_sort_scratch_bytes(n, digit_bits)) {
+    set_error_text("radix sort: scratch too small");
+    return SPH_ERR_SCRATCH_TOO_SMALL;
+  }
+  cudaStream_t st = as_stream(stream);
+  int64_t nt = rs_tiles(n);
+  size_t hist_n = (size_t)(nt << digit_bits);
+  char* p = reinterpret_cast<char*>(scratch);
+  uint32_t* k_alt = reinterpret_cast<uint32_t*>(p);
+  p += (size_t)n * sizeof(uint32_t);
+  uint32_t* v_alt = reinterpret_cast<uint32_t*>(p);
+  p += (size_t)n * sizeof(uint32_t);
+  int32_t* hist = reinterpret_cast<int32_t*>(p);
+  p += (hist_n + 1) * sizeof(int32_t);
+  int32_t* offs = reinterpret_cast<int32_t*>(p);
+  p += (hist_n + 1) * sizeof(int32_t);
+  p = reinterpret_cast<char*>(((uintptr_t)p + 15) & ~(uintptr_t)15);
+  void* scan_scratch = p;
+  size_t scan_bytes = sph_scan_scratch_bytes((int64_t)hist_n + 1);
+
+  int passes = (key_bits + digit_bits - 1) / digit_bits;
+  uint32_t *kin = keys, *vin = vals, *kout = k_alt, *vout = v_alt;
+  for (int pass = 0; pass < passes; ++pass) {
+    int shift = pass * digit_bits;
+    int bits = digit_bits;
+    if (shift + bits > key_bits) bits = key_bits - shift;
+    k_radix_hist<<<(unsigned)nt, kRsThreads, 0, st>>>(kin, n, shift, bits, hist, (int)nt);
+    sph_status_t s = scan_impl<int32_t>(hist, offs, (int64_t)(nt << bits), scan_scratch, scan_bytes, stream);
+    if (s != SPH_OK) return s;
+    k_radix_scatter<<<(unsigned)nt, kRsThreads, 0, st>>>(kin, vin, kout, vout, n, shift, bits, offs, (int)nt);
+    SPH_CHECK_LAUNCH("radix sort pass");
+    uint32_t* t = kin; kin = kout; kout = t;
+    t = vin; vin = vout; vout = t;
+  }
+  if (kin != keys) {
+    cudaMemcpyAsync(keys, kin, (size_t)n * sizeof(uint32_t), cudaMemcpyDeviceToDevice, st);
+    cudaMemcpyAsync(vals, vin, (size_t)n * sizeof(uint32_t), cudaMemcpyDeviceToDevice, st);
+    SPH_CHECK_LAUNCH("radix sort copy-back");
+  }
+  return SPH_OK;
+}
+
+}  // extern "C"
