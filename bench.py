@@ -41,6 +41,8 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="search_density_A")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--sort", default="counting", choices=["counting", "radix"])
+    ap.add_argument("--digit-bits", type=int, default=8)
     return ap.parse_args()
 
 
@@ -160,13 +162,24 @@ def run_reference(args):
 # ----------------------------------------------------------------------------- GPU arm
 # algorithmic bytes per particle of each kernel of the step (measurement)
 def algorithmic_bytes(kernel, n, P, cells):
-    if kernel == "nl_count":   # packed (16) + key (4) read, count (4) + rho (4) written, cell table once
-        return n * 28 + 4 * (cells + 1)
-    if kernel == "nl_fill":    # packed (16) + key (4) + offsets (4) read, cols written (4 per pair)
-        return n * 24 + 4 * P + 4 * (cells + 1)
+    if kernel == "nl_count":   # xy (8) + h (4) + A (4) + key (4) read, count (4) + rho (4) written, cell table once
+        return n * 28 + 4 * (cells + 2)
+    if kernel == "nl_fill":    # xy (8) + h (4) + key (4) + offsets (4) read, cols written (4 per pair)
+        return n * 20 + 4 * P + 4 * (cells + 2)
     if kernel == "radix_sort": # per pass: keys+vals read twice (hist + scatter), written once
         return n * 24
     return n * 16
+
+
+def make_event():
+    import torch
+    try:  # an event recorded inside a captured graph becomes a timed node only when external
+        return torch.cuda.Event(enable_timing=True, external=True)
+    except TypeError:
+        return torch.cuda.Event(enable_timing=True)
+
+
+PHASES = ["start", "keys", "sort", "gather", "count", "scan", "fill", "end"]
 
 
 def run_ours(args):
@@ -180,7 +193,7 @@ def run_ours(args):
     from pytorchsph_gb300 import build as B
     B.build()
     from pytorchsph_gb300 import _native as N
-    from pytorchsph_gb300.search import GridSearch, grid_from_bytes
+    from pytorchsph_gb300.search import GridSearch
     N.load()
 
     pos, h, area, vmin, vmax, L = load_workload(args.workload)
@@ -189,24 +202,35 @@ def run_ours(args):
     h_pos, h_h, h_a = pin(pos), pin(h), pin(area)
     d_pos, d_h, d_a = h_pos.to(dev), h_h.to(dev), h_a.to(dev)
     support = float(h[0])
-    gs = GridSearch(dev)
+    gs = GridSearch(dev, sort=args.sort, digit_bits=args.digit_bits)
     first = gs.run(d_pos, d_h, d_a, kernel_support=support, min_coord=vmin, max_coord=vmax)
     cells = first.cell_capacity
     P = first.num_pairs
     pair_cap = int(P * 1.05) + 1024
     rho_out = torch.empty(n, dtype=torch.float32, device=dev)
+    events = {}
+
+    def marks(name):
+        e = events.get(name)
+        if e is None:
+            e = events[name] = make_event()
+        e.record()
 
     def step():
         r = gs.run(d_pos, d_h, d_a, kernel_support=support, min_coord=vmin, max_coord=vmax,
-                   cell_capacity=cells, pair_capacity=pair_cap, sync=False)
+                   cell_capacity=cells, pair_capacity=pair_cap, sync=False, marks=marks)
         N.call("sph_scatter_f32", N.ptr(r.order), N.ptr(r.rho), n, N.ptr(rho_out), N.stream_ptr())
+        marks("end")
         return r
 
-    # kernel launches per step (library calls -> kernels): grid 2, keys 1, radix sort
-    # passes x (hist 1 + scan 3 + scatter 1), gather 1, cell starts 1, count 1, scan 3,
-    # fill 1, scatter 1; plus one torch fill of the status word
-    passes = (N.load().sph_key_bits(cells) + 7) // 8
-    launches_per_step = 2 + 1 + passes * 5 + 1 + 1 + 1 + 3 + 1 + 1
+    # kernels per step: grid 2, keys 1, sort (counting: scan 3 + scatter + fix + fix_large = 6,
+    # plus one memset; radix: passes x 5 + cell starts), gather 1, count 1, scan 3, fill 1,
+    # scatter 1 (and one torch fill of the status word)
+    if args.sort == "counting":
+        sort_launches = 6
+    else:
+        sort_launches = ((N.load().sph_key_bits(cells) + args.digit_bits - 1) // args.digit_bits) * 5 + 1
+    launches_per_step = 2 + 1 + sort_launches + 1 + 1 + 3 + 1 + 1
 
     s = torch.cuda.Stream(dev)
     s.wait_stream(torch.cuda.current_stream())
@@ -227,6 +251,8 @@ def run_ours(args):
 
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    phase_acc = {k: 0.0 for k in PHASES[1:]}
+    phase_ok = True
     if world > 1:
         dist.barrier()
     torch.cuda.synchronize()
@@ -237,6 +263,12 @@ def run_ours(args):
             starts[k].record()
             g.replay()
             ends[k].record()
+            ends[k].synchronize()
+            try:
+                for a_, b_ in zip(PHASES[:-1], PHASES[1:]):
+                    phase_acc[b_] += events[a_].elapsed_time(events[b_])
+            except Exception:
+                phase_ok = False
         torch.cuda.synchronize()
         t_wall = time.perf_counter() - t_wall0
     if world > 1:
@@ -247,63 +279,27 @@ def run_ours(args):
         dist.all_reduce(ms_t, op=dist.ReduceOp.MAX)
     ms = float(ms_t.item())
     value = n * world / (ms / 1e3)
-
-    # per-kernel durations of one un-captured step (events between the library calls)
-    phases = {}
-    lib = N.load()
-    st = N.stream_ptr()
-    ev = lambda: torch.cuda.Event(enable_timing=True)
-    reps = 10
-    acc = {}
-    for _ in range(reps):
-        flush.zero_()
-        r = first
-        e = [ev() for _ in range(7)]
-        e[0].record()
-        gs.grid(d_pos, d_h, vmin, vmax, cells)
-        N.call("sph_cell_keys", N.ptr(d_pos), n, N.ptr(r.grid), cells, N.ptr(r.keys), N.ptr(r.order),
-               N.ptr(r.status), st)
-        e[1].record()
-        rs = gs.ws.bytes("rs_scratch", lib.sph_radix_sort_scratch_bytes(n, 8))
-        N.call("sph_radix_sort_pairs", N.ptr(r.keys), N.ptr(r.order), n, lib.sph_key_bits(cells), 8, N.ptr(rs),
-               rs.numel() * 8, st)
-        e[2].record()
-        N.call("sph_gather_packed", N.ptr(r.order), n, N.ptr(d_pos), N.ptr(d_h), N.ptr(d_a), N.ptr(r.packed), st)
-        N.call("sph_cell_starts", N.ptr(r.keys), n, cells, N.ptr(r.cell_start), st)
-        e[3].record()
-        N.call("sph_nl_count", N.ptr(r.packed), n, N.ptr(r.keys), N.ptr(r.cell_start), N.ptr(r.grid), cells, 1,
-               support, N.ptr(r.counts), N.ptr(r.rho), st)
-        e[4].record()
-        sc = gs.ws.bytes("scan_scratch", lib.sph_scan_scratch_bytes(n))
-        N.call("sph_exclusive_scan_i32", N.ptr(r.counts), N.ptr(r.offsets), n, N.ptr(sc), sc.numel() * 8, st)
-        e[5].record()
-        N.call("sph_nl_fill", N.ptr(r.packed), n, N.ptr(r.keys), N.ptr(r.cell_start), N.ptr(r.grid), cells, 1,
-               N.ptr(r.offsets), pair_cap, N.ptr(r.cols), N.ptr(r.status), st)
-        e[6].record()
-        torch.cuda.synchronize()
-        names = ["grid+keys", "radix_sort", "gather+cell_starts", "nl_count", "scan", "nl_fill"]
-        for k, nm in enumerate(names):
-            acc[nm] = acc.get(nm, 0.0) + e[k].elapsed_time(e[k + 1]) / reps
-    phases = acc
-    dom = max(["nl_count", "nl_fill"], key=lambda k: phases[k])
-    alg = algorithmic_bytes(dom, n, P, cells)
+    phases = {k: v / args.steps for k, v in phase_acc.items()} if phase_ok else {}
+    dom = max(["count", "fill"], key=lambda k: phases.get(k, 0.0)) if phases else "fill"
+    dom_kernel = {"count": "nl_count", "fill": "nl_fill"}[dom]
+    alg = algorithmic_bytes(dom_kernel, n, P, cells)
     peaks = {}
     try:
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
     except Exception:
         pass
     peak = float(peaks.get("hbm_gbs", 6800.0))
-    achieved = alg / (phases[dom] / 1e3) / 1e9
+    achieved = alg / (phases[dom] / 1e3) / 1e9 if phases else None
     traffic = None
     try:
         prof = json.load(open(os.path.join(ROOT, "profiles", "traffic.json")))
-        traffic = prof.get(args.workload, {}).get(dom)
+        traffic = prof.get(args.workload, {}).get(dom_kernel)
     except Exception:
         pass
 
     # end to end through the public API from pinned host memory
     e2e_ms = []
-    h2d = 3 * 0 + h_pos.numel() * 4 + h_h.numel() * 4 + h_a.numel() * 4
+    h2d = h_pos.numel() * 4 + h_h.numel() * 4 + h_a.numel() * 4
     d2h = n * 4 + 4
     rho_host = torch.empty(n, dtype=torch.float32).pin_memory()
     cnt_host = torch.empty(1, dtype=torch.int32).pin_memory()
@@ -334,11 +330,13 @@ def run_ours(args):
                 "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f32", "data": "synthetic",
                 "config": {"workload": args.workload, "particles": n, "pairs": P, "cells": cells,
-                           "support": "3dx", "l2": "flushed between timed steps (flush not timed)",
+                           "support": "3dx", "sort": args.sort,
+                           "l2": "flushed between timed steps (flush not timed)",
                            "graph": "one CUDA graph per step", "parallelism": f"replicas{world}"},
                 "phases_ms": {k: round(v, 5) for k, v in phases.items()},
-                "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                             "frac": achieved / peak, "traffic": traffic, "algorithmic_bytes": alg,
+                "roofline": {"bound": "hbm", "kernel": dom_kernel, "achieved": achieved, "peak": peak,
+                             "unit": "GB/s", "frac": (achieved / peak) if achieved else None, "traffic": traffic,
+                             "algorithmic_bytes": alg,
                              "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback"},
                 "e2e": {"value": e2e_value, "unit": "particles/s", "h2d_bytes_per_step": h2d,
                         "d2h_bytes_per_step": d2h},

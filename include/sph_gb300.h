@@ -36,6 +36,8 @@ typedef int32_t sph_status_t;
 #define SPH_FLAG_PAIR_CAPACITY 4    /* pair count exceeded the pair buffer */
 #define SPH_FLAG_CELL_CAPACITY 8    /* grid has more cells than the cell table holds */
 #define SPH_FLAG_ITERATION_CAP 16   /* an iterative solve stopped at its maximum iteration count */
+#define SPH_FLAG_CELL_ORDER 32      /* a cell held > 2048 particles: their order inside the cell is
+                                       not reproducible (the pair set is unaffected) */
 
 /* Uniform search grid, the device-side form of what sortPositions computes
  * (src/modules/neighborSearch.py:30-55): cell size hmax, origin qmin,
@@ -85,21 +87,36 @@ size_t sph_grid_scratch_bytes(int64_t n);
 sph_status_t sph_grid_build(const float* pos, const float* support, int64_t n, const float* min_coord,
                             const float* max_coord, int32_t cell_capacity, sph_grid* grid,
                             int32_t* status, void* scratch, size_t scratch_bytes, void* stream);
-/* keys[i] = linear cell id of pos[i] (the linearIndices of neighborSearch.py:46-47), vals[i] = i.
+/* keys[i] = linear cell id of pos[i] (the linearIndices of neighborSearch.py:46-47);
+ * vals[i] = i when vals != NULL; cell_count[key] += 1 when cell_count != NULL (a zeroed
+ * int32 [cell_capacity+1] histogram for sph_counting_sort).
  * A particle outside the grid (or any particle when the grid does not fit cell_capacity)
  * gets the sentinel key cell_capacity, is never searched, and flags SPH_FLAG_OUT_OF_GRID. */
 sph_status_t sph_cell_keys(const float* pos, int64_t n, const sph_grid* grid, int32_t cell_capacity,
-                           uint32_t* keys, uint32_t* vals, int32_t* status, void* stream);
+                           uint32_t* keys, uint32_t* vals, int32_t* cell_count, int32_t* status, void* stream);
 /* Number of key bits the radix sort needs for keys 0..cell_capacity (the sentinel included). */
 int32_t sph_key_bits(int32_t cell_capacity);
-/* cell_start[c] = first sorted index whose key >= c, for c = 0..cell_capacity (a cell
- * begin/end table: cell c holds [cell_start[c], cell_start[c+1])). */
+/* Counting sort of particles by cell key (a one-pass radix sort whose digit is the whole
+ * key; replaces the argsort of neighborSearch.py:49): cell_start [cell_capacity+2] =
+ * exclusive scan of cell_count, which is the cell begin table (cell c holds
+ * [cell_start[c], cell_start[c+1])); order[s] = original index of sorted particle s,
+ * ordered by (key, index) exactly as a stable sort; sorted_keys[s] = its key.  Leaves
+ * cell_count zeroed.  Cells of more than 2048 particles keep an unreproducible inner
+ * order and flag SPH_FLAG_CELL_ORDER. */
+size_t sph_counting_sort_scratch_bytes(int64_t n, int32_t cell_capacity);
+sph_status_t sph_counting_sort(const uint32_t* keys, int64_t n, int32_t cell_capacity, int32_t* cell_count,
+                               int32_t* cell_start, uint32_t* order, uint32_t* sorted_keys, int32_t* status,
+                               void* scratch, size_t scratch_bytes, void* stream);
+/* cell_start[c] = first sorted index whose key >= c, for c = 0..cell_capacity+1 (the cell
+ * begin table after sph_radix_sort_pairs). */
 sph_status_t sph_cell_starts(const uint32_t* sorted_keys, int64_t n, int32_t cell_capacity,
                              int32_t* cell_start, void* stream);
-/* Reorder into sorted SoA: packed[s] = (x, y, support, area) of particle order[s]; any
- * of support/area may be NULL (then 0).  Replaces the gathers of neighborSearch.py:51-53. */
-sph_status_t sph_gather_packed(const uint32_t* order, int64_t n, const float* pos, const float* support,
-                               const float* area, float* packed /* float4 [n] */, void* stream);
+/* Reorder into sorted SoA (the gathers of neighborSearch.py:51-53): xy[s] = pos[order[s]]
+ * (float2), sorted_support[s] = support[order[s]], sorted_area[s] = area[order[s]]; the
+ * last two may be NULL. */
+sph_status_t sph_gather_sorted(const uint32_t* order, int64_t n, const float* pos, const float* support,
+                               const float* area, float* xy, float* sorted_support, float* sorted_area,
+                               void* stream);
 
 /* constructHashMap (src/modules/neighborSearch.py:58-88) on the GPU from the sorted keys:
  * writes cell_indices/cum_cell(counts)/cell_span(begins) [C] in hash order and
@@ -118,14 +135,14 @@ sph_status_t sph_hash_map_build(const uint32_t* sorted_keys, int64_t n, int32_t 
  * the reference's predicate sqrtf(fmaf(dx,dx,dy*dy)) < h_s, dx = x_s - x_j.
  * If rho != NULL also rho[s] = sum_j W(|x_s-x_j| / kernel_support) * area_j (Wendland C2,
  * src/modules/density.py:26-30) — the fused search + density. */
-sph_status_t sph_nl_count(const float* packed, int64_t n, const uint32_t* sorted_keys,
-                          const int32_t* cell_start, const sph_grid* grid, int32_t cell_capacity,
-                          int32_t search_radius,
-                          float kernel_support, int32_t* counts, float* rho, void* stream);
+sph_status_t sph_nl_count(const float* xy, const float* sorted_support, const float* sorted_area, int64_t n,
+                          const uint32_t* sorted_keys, const int32_t* cell_start, const sph_grid* grid,
+                          int32_t cell_capacity, int32_t search_radius, float kernel_support,
+                          int32_t* counts, float* rho, void* stream);
 /* Pass 2: cols[offsets[s] + k] = sorted index of the k-th neighbor of s (cell order).
  * offsets = exclusive scan of counts (n+1 entries).  A row that would end beyond
  * pair_capacity is not written and flags SPH_FLAG_PAIR_CAPACITY. */
-sph_status_t sph_nl_fill(const float* packed, int64_t n, const uint32_t* sorted_keys,
+sph_status_t sph_nl_fill(const float* xy, const float* sorted_support, int64_t n, const uint32_t* sorted_keys,
                          const int32_t* cell_start, const sph_grid* grid, int32_t cell_capacity,
                          int32_t search_radius, const int32_t* offsets, int64_t pair_capacity,
                          int32_t* cols, int32_t* status, void* stream);
@@ -136,7 +153,7 @@ sph_status_t sph_scatter_f32(const uint32_t* order, const float* in, int64_t n, 
  * (i, j) like the CUDA finalize (:153-157).  order[s] = original index of sorted s,
  * rank[i] = sorted index of original i, orig_offsets = exclusive scan of counts by
  * original index.  dist/radial may be NULL. */
-sph_status_t sph_nl_to_coo(const float* packed, int64_t n, const uint32_t* order, const uint32_t* rank,
+sph_status_t sph_nl_to_coo(const float* xy, int64_t n, const uint32_t* order, const uint32_t* rank,
                            const int32_t* offsets, const int32_t* cols, const int64_t* orig_offsets,
                            float grad_threshold, float kernel_support, int64_t* pairs /* [2, P] */,
                            int64_t num_pairs, float* dist /* [P,2] */, float* radial /* [P] */,
@@ -154,10 +171,10 @@ sph_status_t sph_invert_permutation(const uint32_t* order, int64_t n, uint32_t* 
  * Two passes like sph_nl_count/sph_nl_fill; offsets are int64 [m+1]; cols are original
  * particle indices when order != NULL, sorted indices otherwise. */
 sph_status_t sph_nl_query_count(const float* query_pos, const float* query_support, int64_t m,
-                                const float* packed, const int32_t* cell_start, const sph_grid* grid,
+                                const float* xy, const int32_t* cell_start, const sph_grid* grid,
                                 int32_t cell_capacity, int32_t search_radius, int32_t* counts, void* stream);
 sph_status_t sph_nl_query_fill(const float* query_pos, const float* query_support, int64_t m,
-                               const float* packed, const int32_t* cell_start, const sph_grid* grid,
+                               const float* xy, const int32_t* cell_start, const sph_grid* grid,
                                int32_t cell_capacity, int32_t search_radius, const uint32_t* order,
                                const int64_t* offsets, int32_t* rows, int32_t* cols, void* stream);
 

@@ -33,14 +33,16 @@ SIGNATURES = {
     "sph_radix_sort_pairs": (_I32, [_P, _P, _I64, _I32, _I32, _P, _SZ, _P]),
     "sph_grid_scratch_bytes": (_SZ, [_I64]),
     "sph_grid_build": (_I32, [_P, _P, _I64, _P, _P, _I32, _P, _P, _P, _SZ, _P]),
-    "sph_cell_keys": (_I32, [_P, _I64, _P, _I32, _P, _P, _P, _P]),
+    "sph_cell_keys": (_I32, [_P, _I64, _P, _I32, _P, _P, _P, _P, _P]),
+    "sph_counting_sort_scratch_bytes": (_SZ, [_I64, _I32]),
+    "sph_counting_sort": (_I32, [_P, _I64, _I32, _P, _P, _P, _P, _P, _P, _SZ, _P]),
     "sph_key_bits": (_I32, [_I32]),
     "sph_cell_starts": (_I32, [_P, _I64, _I32, _P, _P]),
-    "sph_gather_packed": (_I32, [_P, _I64, _P, _P, _P, _P, _P]),
+    "sph_gather_sorted": (_I32, [_P, _I64, _P, _P, _P, _P, _P, _P, _P]),
     "sph_hash_map_scratch_bytes": (_SZ, [_I64, _I32]),
     "sph_hash_map_build": (_I32, [_P, _I64, _I32, _I32, _P, _P, _P, _P, _P, _P, _SZ, _P]),
-    "sph_nl_count": (_I32, [_P, _I64, _P, _P, _P, _I32, _I32, _F32, _P, _P, _P]),
-    "sph_nl_fill": (_I32, [_P, _I64, _P, _P, _P, _I32, _I32, _P, _I64, _P, _P, _P]),
+    "sph_nl_count": (_I32, [_P, _P, _P, _I64, _P, _P, _P, _I32, _I32, _F32, _P, _P, _P]),
+    "sph_nl_fill": (_I32, [_P, _P, _I64, _P, _P, _P, _I32, _I32, _P, _I64, _P, _P, _P]),
     "sph_scatter_f32": (_I32, [_P, _P, _I64, _P, _P]),
     "sph_nl_to_coo": (_I32, [_P, _I64, _P, _P, _P, _P, _P, _F32, _F32, _P, _I64, _P, _P, _P]),
     "sph_scatter_counts": (_I32, [_P, _P, _I64, _P, _P]),

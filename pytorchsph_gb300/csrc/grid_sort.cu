@@ -1,0 +1,525 @@
+// Search grid, cell keys and the sort of particles by cell key (sm_103a).
+//
+// Two sorts are provided; both order particles by (cell key, original index), which is
+// what a stable sort of the keys gives:
+//   * sph_counting_sort — single-digit radix (counting) sort where the digit is the whole
+//     cell key: a global per-cell histogram (atomics, filled by sph_cell_keys), one
+//     exclusive scan that is directly the cell begin table, an atomic scatter, and a
+//     per-cell fix-up that restores index order inside each cell.  ~6 launches.
+//   * sph_radix_sort_pairs (scan_sort.cu) — multi-pass LSD radix sort with 1..8-bit
+//     digits; its cell table comes from sph_cell_starts (binary search per cell).
+#include <cstdio>
+
+#include "sph_common.cuh"
+
+namespace sph {
+
+constexpr int kRedThreads = 256;
+
+struct Bounds {
+  float hmax, mnx, mny, mxx, mxy;
+  int nonfinite;
+};
+
+__global__ void __launch_bounds__(kRedThreads) k_bounds_partial(const float2* __restrict__ pos,
+                                                                const float* __restrict__ h, int64_t n,
+                                                                Bounds* __restrict__ part) {
+  float hm = -INFINITY, mnx = INFINITY, mny = INFINITY, mxx = -INFINITY, mxy = -INFINITY;
+  int bad = 0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    float2 p = pos[i];
+    float hv = h[i];
+    if (!isfinite(p.x) || !isfinite(p.y) || !isfinite(hv)) bad = 1;
+    hm = fmaxf(hm, hv);
+    mnx = fminf(mnx, p.x);
+    mny = fminf(mny, p.y);
+    mxx = fmaxf(mxx, p.x);
+    mxy = fmaxf(mxy, p.y);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    hm = fmaxf(hm, __shfl_xor_sync(0xffffffffu, hm, o));
+    mnx = fminf(mnx, __shfl_xor_sync(0xffffffffu, mnx, o));
+    mny = fminf(mny, __shfl_xor_sync(0xffffffffu, mny, o));
+    mxx = fmaxf(mxx, __shfl_xor_sync(0xffffffffu, mxx, o));
+    mxy = fmaxf(mxy, __shfl_xor_sync(0xffffffffu, mxy, o));
+    bad |= __shfl_xor_sync(0xffffffffu, bad, o);
+  }
+  __shared__ Bounds sb[kRedThreads / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) sb[warp] = Bounds{hm, mnx, mny, mxx, mxy, bad};
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    Bounds b = sb[0];
+    for (int w = 1; w < kRedThreads / 32; ++w) {
+      b.hmax = fmaxf(b.hmax, sb[w].hmax);
+      b.mnx = fminf(b.mnx, sb[w].mnx);
+      b.mny = fminf(b.mny, sb[w].mny);
+      b.mxx = fmaxf(b.mxx, sb[w].mxx);
+      b.mxy = fmaxf(b.mxy, sb[w].mxy);
+      b.nonfinite |= sb[w].nonfinite;
+    }
+    part[blockIdx.x] = b;
+  }
+}
+
+// Grid of sortPositions, src/modules/neighborSearch.py:34-46, all in float32:
+// qMin = minCoord - hMax*1.0, qMax = maxCoord + 2*hMax*1.0, cells = ceil((qMax-qMin)/hMax).
+__global__ void k_bounds_final(const Bounds* __restrict__ part, int nparts, int has_min, float min_x, float min_y,
+                               int has_max, float max_x, float max_y, int32_t cell_capacity, sph_grid* grid,
+                               int32_t* status) {
+  __shared__ Bounds sb[32];
+  Bounds b{-INFINITY, INFINITY, INFINITY, -INFINITY, -INFINITY, 0};
+  for (int k = threadIdx.x; k < nparts; k += 32) {
+    Bounds p = part[k];
+    b.hmax = fmaxf(b.hmax, p.hmax);
+    b.mnx = fminf(b.mnx, p.mnx);
+    b.mny = fminf(b.mny, p.mny);
+    b.mxx = fmaxf(b.mxx, p.mxx);
+    b.mxy = fmaxf(b.mxy, p.mxy);
+    b.nonfinite |= p.nonfinite;
+  }
+  sb[threadIdx.x] = b;
+  __syncwarp();
+  if (threadIdx.x != 0) return;
+  for (int k = 1; k < 32; ++k) {
+    b.hmax = fmaxf(b.hmax, sb[k].hmax);
+    b.mnx = fminf(b.mnx, sb[k].mnx);
+    b.mny = fminf(b.mny, sb[k].mny);
+    b.mxx = fmaxf(b.mxx, sb[k].mxx);
+    b.mxy = fmaxf(b.mxy, sb[k].mxy);
+    b.nonfinite |= sb[k].nonfinite;
+  }
+  float hs = __fmul_rn(b.hmax, 1.0f);
+  float two_hs = __fmul_rn(__fmul_rn(2.0f, b.hmax), 1.0f);
+  float qmin_x = __fsub_rn(has_min ? min_x : b.mnx, hs);
+  float qmin_y = __fsub_rn(has_min ? min_y : b.mny, hs);
+  float qmax_x = __fadd_rn(has_max ? max_x : b.mxx, two_hs);
+  float qmax_y = __fadd_rn(has_max ? max_y : b.mxy, two_hs);
+  float ex = __fdiv_rn(__fsub_rn(qmax_x, qmin_x), hs);
+  float ey = __fdiv_rn(__fsub_rn(qmax_y, qmin_y), hs);
+  sph_grid g;
+  g.qmin[0] = qmin_x;
+  g.qmin[1] = qmin_y;
+  g.hmax = b.hmax;
+  g.reserved = 0.f;
+  g.reserved2 = 0;
+  bool ok = b.nonfinite == 0 && b.hmax > 0.f && isfinite(ex) && isfinite(ey) && ex < 2.0e9f && ey < 2.0e9f;
+  int cx = ok ? (int)ceilf(ex) : 0;
+  int cy = ok ? (int)ceilf(ey) : 0;
+  long long nc = (long long)cx * (long long)cy;
+  if (!ok) flag(status, SPH_FLAG_NONFINITE);
+  if (nc > (long long)cell_capacity) flag(status, SPH_FLAG_CELL_CAPACITY);
+  g.cells_x = cx;
+  g.cells_y = cy;
+  g.num_cells = nc > (long long)cell_capacity ? cell_capacity + 1 : (int)nc;
+  *grid = g;
+}
+
+__global__ void k_cell_keys(const float2* __restrict__ pos, int64_t n, const sph_grid* __restrict__ gp,
+                            int32_t cell_capacity, uint32_t* __restrict__ keys, uint32_t* __restrict__ vals,
+                            int32_t* __restrict__ cell_count, int32_t* status) {
+  const sph_grid g = *gp;
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float2 p = pos[i];
+  uint32_t key = (uint32_t)cell_capacity;  // sentinel: sorts last, never searched
+  if (!isfinite(p.x) || !isfinite(p.y)) {
+    flag(status, SPH_FLAG_NONFINITE);
+  } else if (grid_ok(g, cell_capacity)) {
+    int ix = cell_coord(p.x, g.qmin[0], g.hmax);
+    int iy = cell_coord(p.y, g.qmin[1], g.hmax);
+    if (ix >= 0 && iy >= 0 && ix < g.cells_x && iy < g.cells_y)
+      key = (uint32_t)(ix + g.cells_x * iy);
+    else
+      flag(status, SPH_FLAG_OUT_OF_GRID);
+  }
+  keys[i] = key;
+  if (vals) vals[i] = (uint32_t)i;
+  if (cell_count) atomicAdd(cell_count + key, 1);
+}
+
+// Counting-sort scatter: slot = cell_start[key] + (remaining count of the cell) - 1.
+// Decrementing the histogram leaves it all zero for the next sort.
+__global__ void k_count_scatter(const uint32_t* __restrict__ keys, int64_t n, const int32_t* __restrict__ cell_start,
+                                int32_t* __restrict__ cell_count, uint32_t* __restrict__ tmp) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  uint32_t k = keys[i];
+  int slot = cell_start[k] + atomicSub(cell_count + k, 1) - 1;
+  tmp[slot] = (uint32_t)i;
+}
+
+constexpr int kSmallCell = 48;    // cells up to this size are sorted by one thread in registers
+constexpr int kBlockSortMax = 2048;  // larger cells: one block, bitonic sort in shared memory
+
+// Per-cell fix-up: restore ascending original index inside every cell, write the sorted
+// keys.  Cells larger than kSmallCell are queued for k_cell_fix_large.
+__global__ void __launch_bounds__(128) k_cell_fix(const int32_t* __restrict__ cell_start, int32_t ncell_slots,
+                                                  const uint32_t* __restrict__ tmp, uint32_t* __restrict__ order,
+                                                  uint32_t* __restrict__ sorted_keys, int32_t* __restrict__ big_list,
+                                                  int32_t* __restrict__ big_count) {
+  int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= ncell_slots) return;
+  const int b = cell_start[c], e = cell_start[c + 1];
+  const int k = e - b;
+  if (k == 0) return;
+  for (int t = b; t < e; ++t) sorted_keys[t] = (uint32_t)c;
+  if (k <= kSmallCell) {
+    uint32_t v[kSmallCell];
+#pragma unroll 1
+    for (int t = 0; t < k; ++t) {
+      uint32_t x = tmp[b + t];
+      int u = t;
+      while (u > 0 && v[u - 1] > x) {
+        v[u] = v[u - 1];
+        --u;
+      }
+      v[u] = x;
+    }
+#pragma unroll 1
+    for (int t = 0; t < k; ++t) order[b + t] = v[t];
+  } else {
+    int q = atomicAdd(big_count, 1);
+    big_list[q] = c;
+  }
+}
+
+// One block per large cell: bitonic sort of up to kBlockSortMax indices in shared memory.
+// Bigger cells keep the atomic scatter order (their pair set is unchanged; only the
+// order inside that cell is not reproducible) and flag SPH_FLAG_CELL_ORDER.
+__global__ void __launch_bounds__(512) k_cell_fix_large(const int32_t* __restrict__ cell_start,
+                                                        const uint32_t* __restrict__ tmp,
+                                                        uint32_t* __restrict__ order,
+                                                        const int32_t* __restrict__ big_list,
+                                                        const int32_t* __restrict__ big_count, int32_t* status) {
+  __shared__ uint32_t s[kBlockSortMax];
+  const int nbig = *big_count;
+  for (int q = blockIdx.x; q < nbig; q += gridDim.x) {
+    const int c = big_list[q];
+    const int b = cell_start[c], e = cell_start[c + 1];
+    const int k = e - b;
+    if (k > kBlockSortMax) {
+      for (int t = threadIdx.x; t < k; t += blockDim.x) order[b + t] = tmp[b + t];
+      if (threadIdx.x == 0) flag(status, SPH_FLAG_CELL_ORDER);
+      continue;
+    }
+    int p2 = 1;
+    while (p2 < k) p2 <<= 1;
+    for (int t = threadIdx.x; t < p2; t += blockDim.x) s[t] = t < k ? tmp[b + t] : 0xffffffffu;
+    __syncthreads();
+    for (int size = 2; size <= p2; size <<= 1) {
+      for (int stride = size >> 1; stride > 0; stride >>= 1) {
+        for (int t = threadIdx.x; t < p2; t += blockDim.x) {
+          int u = t ^ stride;
+          if (u > t) {
+            bool up = (t & size) == 0;
+            uint32_t a = s[t], bb = s[u];
+            if ((a > bb) == up) {
+              s[t] = bb;
+              s[u] = a;
+            }
+          }
+        }
+        __syncthreads();
+      }
+    }
+    for (int t = threadIdx.x; t < k; t += blockDim.x) order[b + t] = s[t];
+    __syncthreads();
+  }
+}
+
+// cell_start[c] = lower_bound(sorted_keys, c) for c = 0..cap+1 (used after the LSD radix sort).
+__global__ void k_cell_starts(const uint32_t* __restrict__ keys, int64_t n, int32_t cap,
+                              int32_t* __restrict__ cell_start) {
+  int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c > (int64_t)cap + 1) return;
+  int64_t lo = 0, hi = n;
+  while (lo < hi) {
+    int64_t mid = (lo + hi) >> 1;
+    if ((int64_t)keys[mid] < c) lo = mid + 1; else hi = mid;
+  }
+  cell_start[c] = (int32_t)lo;
+}
+
+__global__ void k_gather_sorted(const uint32_t* __restrict__ order, int64_t n, const float2* __restrict__ pos,
+                                const float* __restrict__ h, const float* __restrict__ a, float2* __restrict__ xy,
+                                float* __restrict__ sh, float* __restrict__ sa) {
+  int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  uint32_t o = order[s];
+  xy[s] = pos[o];
+  if (sh) sh[s] = h[o];
+  if (sa) sa[s] = a[o];
+}
+
+__global__ void k_scatter_f32(const uint32_t* __restrict__ order, const float* __restrict__ in, int64_t n,
+                              float* __restrict__ out) {
+  int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s < n) out[order[s]] = in[s];
+}
+
+__global__ void k_scatter_counts(const uint32_t* __restrict__ order, const int32_t* __restrict__ counts, int64_t n,
+                                 int32_t* __restrict__ out) {
+  int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s < n) out[order[s]] = counts[s];
+}
+
+__global__ void k_invert_perm(const uint32_t* __restrict__ order, int64_t n, uint32_t* __restrict__ rank) {
+  int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s < n) rank[order[s]] = (uint32_t)s;
+}
+
+// ------------------------------------------------------------------ constructHashMap
+__global__ void k_cell_heads(const uint32_t* __restrict__ keys, int64_t n, int32_t* __restrict__ head) {
+  int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s < n) head[s] = (s == 0 || keys[s] != keys[s - 1]) ? 1 : 0;
+}
+
+__global__ void k_cell_compact(const uint32_t* __restrict__ keys, int64_t n, const int32_t* __restrict__ head,
+                               const int32_t* __restrict__ slot, int32_t cells_x, int32_t L,
+                               int32_t* __restrict__ c_lin, int32_t* __restrict__ c_begin,
+                               uint32_t* __restrict__ c_hash, uint32_t* __restrict__ c_id) {
+  int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n || !head[s]) return;
+  int32_t c = slot[s];
+  int32_t lin = (int32_t)keys[s];
+  c_lin[c] = lin;
+  c_begin[c] = (int32_t)s;
+  long long x = lin % cells_x, y = lin / cells_x;
+  c_hash[c] = (uint32_t)((x * 3 + y * 5) % L);
+  c_id[c] = (uint32_t)c;
+}
+
+__global__ void k_cell_emit(int64_t C, int64_t n, const uint32_t* __restrict__ c_id, const int32_t* __restrict__ c_lin,
+                            const int32_t* __restrict__ c_begin, int32_t* __restrict__ cell_indices,
+                            int32_t* __restrict__ cum_cell, int32_t* __restrict__ cell_span) {
+  int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= C) return;
+  uint32_t c = c_id[k];
+  int32_t b = c_begin[c];
+  int32_t e = (int64_t)c + 1 < C ? c_begin[c + 1] : (int32_t)n;
+  cell_indices[k] = c_lin[c];
+  cum_cell[k] = e - b;
+  cell_span[k] = b;
+}
+
+__global__ void k_table_init(int32_t* __restrict__ table, int32_t L) {
+  int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (b < L) {
+    table[2 * b] = -1;
+    table[2 * b + 1] = 0;
+  }
+}
+
+__global__ void k_table_fill(const uint32_t* __restrict__ sorted_hash, int64_t C, int32_t* __restrict__ table) {
+  int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= C) return;
+  uint32_t hv = sorted_hash[k];
+  if (k > 0 && sorted_hash[k - 1] == hv) return;
+  int64_t e = k + 1;
+  while (e < C && sorted_hash[e] == hv) ++e;
+  table[2 * (int64_t)hv] = (int32_t)k;
+  table[2 * (int64_t)hv + 1] = (int32_t)(e - k);
+}
+
+static int key_bits_for(int64_t v) {
+  int b = 0;
+  while (b < 32 && (((int64_t)1 << b) <= v)) ++b;
+  return b;
+}
+
+}  // namespace sph
+
+using namespace sph;
+
+extern "C" {
+
+size_t sph_grid_scratch_bytes(int64_t) { return (size_t)(2 * kNumSMs) * sizeof(Bounds) + 64; }
+
+sph_status_t sph_grid_build(const float* pos, const float* support, int64_t n, const float* min_coord,
+                            const float* max_coord, int32_t cell_capacity, sph_grid* grid, int32_t* status,
+                            void* scratch, size_t scratch_bytes, void* stream) {
+  SPH_REQUIRE(n > 0 && pos && support && grid && cell_capacity > 0 && cell_capacity < 0x7ffffffe,
+              "grid_build: bad arguments");
+  if (!scratch || scratch_bytes < sph_grid_scratch_bytes(n)) {
+    set_error_text("grid_build: scratch too small");
+    return SPH_ERR_SCRATCH_TOO_SMALL;
+  }
+  cudaStream_t st = as_stream(stream);
+  int nparts = (int)std::min<int64_t>(2 * kNumSMs, (n + kRedThreads - 1) / kRedThreads);
+  Bounds* part = reinterpret_cast<Bounds*>(scratch);
+  k_bounds_partial<<<nparts, kRedThreads, 0, st>>>(reinterpret_cast<const float2*>(pos), support, n, part);
+  k_bounds_final<<<1, 32, 0, st>>>(part, nparts, min_coord != nullptr, min_coord ? min_coord[0] : 0.f,
+                                   min_coord ? min_coord[1] : 0.f, max_coord != nullptr,
+                                   max_coord ? max_coord[0] : 0.f, max_coord ? max_coord[1] : 0.f, cell_capacity,
+                                   grid, status);
+  SPH_CHECK_LAUNCH("grid_build");
+  return SPH_OK;
+}
+
+sph_status_t sph_cell_keys(const float* pos, int64_t n, const sph_grid* grid, int32_t cell_capacity, uint32_t* keys,
+                           uint32_t* vals, int32_t* cell_count, int32_t* status, void* stream) {
+  SPH_REQUIRE(n >= 0 && pos && grid && keys && cell_capacity > 0, "cell_keys: bad arguments");
+  if (n == 0) return SPH_OK;
+  k_cell_keys<<<grid_for(n, 256), 256, 0, as_stream(stream)>>>(reinterpret_cast<const float2*>(pos), n, grid,
+                                                               cell_capacity, keys, vals, cell_count, status);
+  SPH_CHECK_LAUNCH("cell_keys");
+  return SPH_OK;
+}
+
+int32_t sph_key_bits(int32_t cell_capacity) { return key_bits_for(cell_capacity); }
+
+size_t sph_counting_sort_scratch_bytes(int64_t n, int32_t cell_capacity) {
+  size_t b = (size_t)(n < 1 ? 1 : n) * sizeof(uint32_t) + 256;          // scatter target
+  b += ((size_t)cell_capacity + 1) * sizeof(int32_t) + 256;              // large-cell list
+  b += 256;                                                               // large-cell count
+  b += sph_scan_scratch_bytes((int64_t)cell_capacity + 1) + 256;
+  return b;
+}
+
+sph_status_t sph_counting_sort(const uint32_t* keys, int64_t n, int32_t cell_capacity, int32_t* cell_count,
+                               int32_t* cell_start, uint32_t* order, uint32_t* sorted_keys, int32_t* status,
+                               void* scratch, size_t scratch_bytes, void* stream) {
+  SPH_REQUIRE(n >= 0 && n < ((int64_t)1 << 31) && keys && cell_count && cell_start && order && sorted_keys &&
+                  cell_capacity > 0,
+              "counting_sort: bad arguments");
+  if (!scratch || scratch_bytes < sph_counting_sort_scratch_bytes(n, cell_capacity)) {
+    set_error_text("counting_sort: scratch too small");
+    return SPH_ERR_SCRATCH_TOO_SMALL;
+  }
+  cudaStream_t st = as_stream(stream);
+  char* p = reinterpret_cast<char*>(scratch);
+  auto take = [&](size_t bytes) {
+    char* r = p;
+    p += (bytes + 255) & ~(size_t)255;
+    return r;
+  };
+  uint32_t* tmp = reinterpret_cast<uint32_t*>(take((size_t)(n < 1 ? 1 : n) * sizeof(uint32_t)));
+  int32_t* big_list = reinterpret_cast<int32_t*>(take(((size_t)cell_capacity + 1) * sizeof(int32_t)));
+  int32_t* big_count = reinterpret_cast<int32_t*>(take(sizeof(int32_t)));
+  size_t scan_b = sph_scan_scratch_bytes((int64_t)cell_capacity + 1);
+  void* scan_s = take(scan_b);
+  const int64_t slots = (int64_t)cell_capacity + 1;  // cells 0..cap-1 and the sentinel cap
+  sph_status_t s = sph_exclusive_scan_i32(cell_count, cell_start, slots, scan_s, scan_b, stream);
+  if (s != SPH_OK) return s;
+  if (n == 0) return SPH_OK;
+  cudaMemsetAsync(big_count, 0, sizeof(int32_t), st);
+  k_count_scatter<<<grid_for(n, 256), 256, 0, st>>>(keys, n, cell_start, cell_count, tmp);
+  k_cell_fix<<<grid_for(slots, 128), 128, 0, st>>>(cell_start, (int32_t)slots, tmp, order, sorted_keys, big_list,
+                                                   big_count);
+  k_cell_fix_large<<<kNumSMs, 512, 0, st>>>(cell_start, tmp, order, big_list, big_count, status);
+  SPH_CHECK_LAUNCH("counting_sort");
+  return SPH_OK;
+}
+
+sph_status_t sph_cell_starts(const uint32_t* sorted_keys, int64_t n, int32_t cell_capacity, int32_t* cell_start,
+                             void* stream) {
+  SPH_REQUIRE(n >= 0 && cell_capacity > 0 && cell_start && (n == 0 || sorted_keys), "cell_starts: bad arguments");
+  k_cell_starts<<<grid_for((int64_t)cell_capacity + 2, 256), 256, 0, as_stream(stream)>>>(sorted_keys, n,
+                                                                                           cell_capacity, cell_start);
+  SPH_CHECK_LAUNCH("cell_starts");
+  return SPH_OK;
+}
+
+sph_status_t sph_gather_sorted(const uint32_t* order, int64_t n, const float* pos, const float* support,
+                               const float* area, float* xy, float* sorted_support, float* sorted_area,
+                               void* stream) {
+  SPH_REQUIRE(n >= 0 && order && pos && xy, "gather_sorted: bad arguments");
+  SPH_REQUIRE(!sorted_support || support, "gather_sorted: sorted_support needs support");
+  SPH_REQUIRE(!sorted_area || area, "gather_sorted: sorted_area needs area");
+  if (n == 0) return SPH_OK;
+  k_gather_sorted<<<grid_for(n, 256), 256, 0, as_stream(stream)>>>(order, n, reinterpret_cast<const float2*>(pos),
+                                                                    support, area, reinterpret_cast<float2*>(xy),
+                                                                    sorted_support, sorted_area);
+  SPH_CHECK_LAUNCH("gather_sorted");
+  return SPH_OK;
+}
+
+sph_status_t sph_scatter_f32(const uint32_t* order, const float* in, int64_t n, float* out, void* stream) {
+  SPH_REQUIRE(n >= 0 && order && in && out, "scatter_f32: bad arguments");
+  if (n == 0) return SPH_OK;
+  k_scatter_f32<<<grid_for(n, 256), 256, 0, as_stream(stream)>>>(order, in, n, out);
+  SPH_CHECK_LAUNCH("scatter_f32");
+  return SPH_OK;
+}
+
+sph_status_t sph_scatter_counts(const uint32_t* order, const int32_t* counts, int64_t n, int32_t* out, void* stream) {
+  SPH_REQUIRE(n >= 0 && order && counts && out, "scatter_counts: bad arguments");
+  if (n == 0) return SPH_OK;
+  k_scatter_counts<<<grid_for(n, 256), 256, 0, as_stream(stream)>>>(order, counts, n, out);
+  SPH_CHECK_LAUNCH("scatter_counts");
+  return SPH_OK;
+}
+
+sph_status_t sph_invert_permutation(const uint32_t* order, int64_t n, uint32_t* rank, void* stream) {
+  SPH_REQUIRE(n >= 0 && order && rank, "invert_permutation: bad arguments");
+  if (n == 0) return SPH_OK;
+  k_invert_perm<<<grid_for(n, 256), 256, 0, as_stream(stream)>>>(order, n, rank);
+  SPH_CHECK_LAUNCH("invert_permutation");
+  return SPH_OK;
+}
+
+size_t sph_hash_map_scratch_bytes(int64_t n, int32_t hash_len) {
+  size_t nn = (size_t)(n < 1 ? 1 : n) + 1;
+  size_t b = 6 * (nn * sizeof(int32_t) + 256);
+  b += sph_scan_scratch_bytes(n) + 256;
+  b += sph_radix_sort_scratch_bytes(n, 8) + 256;
+  (void)hash_len;
+  return b + 1024;
+}
+
+sph_status_t sph_hash_map_build(const uint32_t* sorted_keys, int64_t n, int32_t cells_x, int32_t hash_len,
+                                int32_t* hash_table, int32_t* cell_indices, int32_t* cum_cell, int32_t* cell_span,
+                                int64_t* num_cells_out, void* scratch, size_t scratch_bytes, void* stream) {
+  SPH_REQUIRE(n > 0 && n < ((int64_t)1 << 31) && sorted_keys && cells_x > 0 && hash_len > 0 && hash_table &&
+                  cell_indices && cum_cell && cell_span && num_cells_out,
+              "hash_map_build: bad arguments");
+  if (!scratch || scratch_bytes < sph_hash_map_scratch_bytes(n, hash_len)) {
+    set_error_text("hash_map_build: scratch too small");
+    return SPH_ERR_SCRATCH_TOO_SMALL;
+  }
+  cudaStream_t st = as_stream(stream);
+  size_t nn = (size_t)n + 1;
+  char* p = reinterpret_cast<char*>(scratch);
+  auto take = [&](size_t bytes) {
+    char* r = p;
+    p += (bytes + 255) & ~(size_t)255;
+    return r;
+  };
+  int32_t* head = reinterpret_cast<int32_t*>(take(nn * 4));
+  int32_t* slot = reinterpret_cast<int32_t*>(take(nn * 4));
+  int32_t* c_lin = reinterpret_cast<int32_t*>(take(nn * 4));
+  int32_t* c_begin = reinterpret_cast<int32_t*>(take(nn * 4));
+  uint32_t* c_hash = reinterpret_cast<uint32_t*>(take(nn * 4));
+  uint32_t* c_id = reinterpret_cast<uint32_t*>(take(nn * 4));
+  size_t scan_b = sph_scan_scratch_bytes(n);
+  void* scan_s = take(scan_b);
+  size_t rs_b = sph_radix_sort_scratch_bytes(n, 8);
+  void* rs_s = take(rs_b);
+
+  k_cell_heads<<<grid_for(n, 256), 256, 0, st>>>(sorted_keys, n, head);
+  sph_status_t s = sph_exclusive_scan_i32(head, slot, n, scan_s, scan_b, stream);
+  if (s != SPH_OK) return s;
+  int32_t C32 = 0;
+  cudaMemcpyAsync(&C32, slot + n, sizeof(int32_t), cudaMemcpyDeviceToHost, st);
+  k_cell_compact<<<grid_for(n, 256), 256, 0, st>>>(sorted_keys, n, head, slot, cells_x, hash_len, c_lin, c_begin,
+                                                   c_hash, c_id);
+  SPH_CHECK_LAUNCH("hash_map_build(compact)");
+  cudaError_t e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) {
+    set_error("hash_map_build(sync)", e);
+    return SPH_ERR_CUDA;
+  }
+  int64_t C = C32;
+  s = sph_radix_sort_pairs(c_hash, c_id, C, key_bits_for(hash_len > 1 ? hash_len - 1 : 1), 8, rs_s, rs_b, stream);
+  if (s != SPH_OK) return s;
+  k_cell_emit<<<grid_for(C, 256), 256, 0, st>>>(C, n, c_id, c_lin, c_begin, cell_indices, cum_cell, cell_span);
+  k_table_init<<<grid_for(hash_len, 256), 256, 0, st>>>(hash_table, hash_len);
+  k_table_fill<<<grid_for(C, 256), 256, 0, st>>>(c_hash, C, hash_table);
+  SPH_CHECK_LAUNCH("hash_map_build");
+  *num_cells_out = C;
+  return SPH_OK;
+}
+
+}  // extern "C"

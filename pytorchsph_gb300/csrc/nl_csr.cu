@@ -1,0 +1,245 @@
+// Two-pass CSR neighbor list over particles in cell-sorted order (sm_103a).
+//
+// Layout: xy (float2, sorted), sorted support h, sorted area A, sorted cell keys, and the
+// cell begin table cell_start[c] (cell c = [cell_start[c], cell_start[c+1])).  With the
+// linear cell id ix + cells_x*iy, the cells (cx-r .. cx+r, yy) of one grid row are
+// contiguous in the sorted order, so a particle scans 2r+1 contiguous index ranges.
+//
+// The pair test is the reference's sqrtf(fmaf(dx,dx,dy*dy)) < h_i in its square-root-free
+// exact form v <= F_i (sq_threshold); the square root is taken only for accepted pairs
+// that need the distance (density).
+#include "sph_common.cuh"
+
+namespace sph {
+
+template <typename F>
+__device__ __forceinline__ void scan_candidates(const float2* __restrict__ xy, const int32_t* __restrict__ cell_start,
+                                                const sph_grid& g, int r, int cx, int cy, float xi, float yi,
+                                                float thr, F&& f) {
+  const int x0 = max(cx - r, 0), x1 = min(cx + r, g.cells_x - 1);
+  if (x0 > x1) return;
+  const int y0 = max(cy - r, 0), y1 = min(cy + r, g.cells_y - 1);
+  for (int yy = y0; yy <= y1; ++yy) {
+    const int row = yy * g.cells_x;
+    const int b = __ldg(cell_start + row + x0);
+    const int e = __ldg(cell_start + row + x1 + 1);
+    for (int j = b; j < e; ++j) {
+      const float2 pj = __ldg(xy + j);
+      const float v = dist2_ref(xi, yi, pj.x, pj.y);
+      if (v <= thr) f(j, v);
+    }
+  }
+}
+
+__global__ void __launch_bounds__(256) k_nl_count(const float2* __restrict__ xy, const float* __restrict__ sh,
+                                                  const float* __restrict__ sa, int64_t n,
+                                                  const uint32_t* __restrict__ keys,
+                                                  const int32_t* __restrict__ cell_start,
+                                                  const sph_grid* __restrict__ gp, int32_t cap, int r,
+                                                  float inv_support, float c_w, int32_t* __restrict__ counts,
+                                                  float* __restrict__ rho) {
+  int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  const sph_grid g = *gp;
+  const uint32_t key = keys[s];
+  int cnt = 0;
+  float acc = 0.f;
+  if (grid_ok(g, cap) && key < (uint32_t)g.num_cells) {
+    const float2 pi = xy[s];
+    const float thr = sq_threshold(sh[s]);
+    const int cx = (int)(key % (uint32_t)g.cells_x), cy = (int)(key / (uint32_t)g.cells_x);
+    if (rho) {
+      scan_candidates(xy, cell_start, g, r, cx, cy, pi.x, pi.y, thr, [&](int j, float v) {
+        ++cnt;
+        acc += wendland(__fsqrt_rn(v) * inv_support, c_w) * __ldg(sa + j);
+      });
+    } else {
+      scan_candidates(xy, cell_start, g, r, cx, cy, pi.x, pi.y, thr, [&](int, float) { ++cnt; });
+    }
+  }
+  counts[s] = cnt;
+  if (rho) rho[s] = acc;
+}
+
+__global__ void __launch_bounds__(256) k_nl_fill(const float2* __restrict__ xy, const float* __restrict__ sh, int64_t n,
+                                                 const uint32_t* __restrict__ keys,
+                                                 const int32_t* __restrict__ cell_start,
+                                                 const sph_grid* __restrict__ gp, int32_t cap, int r,
+                                                 const int32_t* __restrict__ offsets, int64_t pair_capacity,
+                                                 int32_t* __restrict__ cols, int32_t* status) {
+  int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  const sph_grid g = *gp;
+  const uint32_t key = keys[s];
+  if (!(grid_ok(g, cap) && key < (uint32_t)g.num_cells)) return;
+  if ((int64_t)offsets[s + 1] > pair_capacity) {  // the row does not fit: write nothing
+    flag(status, SPH_FLAG_PAIR_CAPACITY);
+    return;
+  }
+  const float2 pi = xy[s];
+  const float thr = sq_threshold(sh[s]);
+  const int cx = (int)(key % (uint32_t)g.cells_x), cy = (int)(key / (uint32_t)g.cells_x);
+  int32_t o = offsets[s];
+  scan_candidates(xy, cell_start, g, r, cx, cy, pi.x, pi.y, thr, [&](int j, float) { cols[o++] = j; });
+}
+
+// Query points (any order, e.g. wall or ghost particles) against the sorted grid, with
+// the query's own support in the predicate (dx = x_query - x_j): the pair set of
+// buildNeighborListUnsortedPerParticle, cppSrc/neighSearch.cpp:261-331.
+__device__ __forceinline__ bool query_cell(float x, float qmin, float hmax, int* c) {
+  float v = ceilf(__fdiv_rn(__fsub_rn(x, qmin), hmax));
+  if (!(v > -1.0e9f && v < 1.0e9f)) return false;
+  *c = (int)v;
+  return true;
+}
+
+template <bool kFill>
+__global__ void __launch_bounds__(128) k_nl_query(const float2* __restrict__ qpos, const float* __restrict__ qh, int64_t m,
+                                                  const float2* __restrict__ xy,
+                                                  const int32_t* __restrict__ cell_start,
+                                                  const sph_grid* __restrict__ gp, int32_t cap, int r,
+                                                  const uint32_t* __restrict__ order, int32_t* __restrict__ counts,
+                                                  const int64_t* __restrict__ offsets, int32_t* __restrict__ rows,
+                                                  int32_t* __restrict__ cols) {
+  int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= m) return;
+  const sph_grid g = *gp;
+  int cnt = 0;
+  int64_t o = kFill ? offsets[b] : 0;
+  const float2 xi = qpos[b];
+  const float thr = sq_threshold(qh[b]);
+  int qx, qy;
+  if (grid_ok(g, cap) && query_cell(xi.x, g.qmin[0], g.hmax, &qx) && query_cell(xi.y, g.qmin[1], g.hmax, &qy)) {
+    scan_candidates(xy, cell_start, g, r, qx, qy, xi.x, xi.y, thr, [&](int j, float) {
+      if (kFill) {
+        rows[o + cnt] = (int32_t)b;
+        cols[o + cnt] = order ? (int32_t)order[j] : j;
+      }
+      ++cnt;
+    });
+  }
+  if (!kFill) counts[b] = cnt;
+}
+
+// One thread per original particle i: its row of the (i, j)-ordered COO list, plus the
+// reference's fluidDistances / fluidRadialDistances (src/modules/neighborSearch.py:218-223).
+__global__ void k_nl_to_coo(const float2* __restrict__ xy, int64_t n, const uint32_t* __restrict__ order,
+                            const uint32_t* __restrict__ rank, const int32_t* __restrict__ offsets,
+                            const int32_t* __restrict__ cols, const int64_t* __restrict__ orig_offsets,
+                            float thr, float support, int64_t* __restrict__ pairs, int64_t P,
+                            float* __restrict__ dist, float* __restrict__ radial) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const uint32_t s = rank[i];
+  const int32_t b = offsets[s], e = offsets[s + 1];
+  const int64_t o = orig_offsets[i];
+  int64_t* prow = pairs;
+  int64_t* pcol = pairs + P;
+  for (int k = b; k < e; ++k) {  // insertion sort by original column index
+    int64_t jo = (int64_t)order[cols[k]];
+    int64_t t = o + (k - b);
+    while (t > o && pcol[t - 1] > jo) {
+      pcol[t] = pcol[t - 1];
+      --t;
+    }
+    pcol[t] = jo;
+  }
+  const float2 pi = xy[s];
+  for (int k = 0; k < e - b; ++k) {
+    prow[o + k] = i;
+    if (dist || radial) {
+      float2 pj = xy[rank[pcol[o + k]]];
+      float dx = pi.x - pj.x, dy = pi.y - pj.y;
+      float rr = sqrtf(dx * dx + dy * dy);
+      if (dist) {
+        if (rr < thr) {
+          dist[2 * (o + k)] = 0.f;
+          dist[2 * (o + k) + 1] = 0.f;
+        } else {
+          dist[2 * (o + k)] = dx / rr;
+          dist[2 * (o + k) + 1] = dy / rr;
+        }
+      }
+      if (radial) radial[o + k] = rr / support;
+    }
+  }
+}
+
+}  // namespace sph
+
+using namespace sph;
+
+extern "C" {
+
+sph_status_t sph_nl_count(const float* xy, const float* sorted_support, const float* sorted_area, int64_t n,
+                          const uint32_t* sorted_keys, const int32_t* cell_start, const sph_grid* grid,
+                          int32_t cell_capacity, int32_t search_radius, float kernel_support, int32_t* counts,
+                          float* rho, void* stream) {
+  SPH_REQUIRE(n >= 0 && xy && sorted_support && sorted_keys && cell_start && grid && counts && search_radius >= 0,
+              "nl_count: bad arguments");
+  SPH_REQUIRE(!rho || (kernel_support > 0.f && sorted_area), "nl_count: density needs kernel_support > 0 and areas");
+  if (n == 0) return SPH_OK;
+  float inv = rho ? 1.0f / kernel_support : 0.f;
+  float cw = rho ? (float)(7.0 / 3.14159265358979323846) / (kernel_support * kernel_support) : 0.f;
+  k_nl_count<<<grid_for(n, 256), 256, 0, as_stream(stream)>>>(reinterpret_cast<const float2*>(xy), sorted_support,
+                                                               sorted_area, n, sorted_keys, cell_start, grid,
+                                                               cell_capacity, search_radius, inv, cw, counts, rho);
+  SPH_CHECK_LAUNCH("nl_count");
+  return SPH_OK;
+}
+
+sph_status_t sph_nl_fill(const float* xy, const float* sorted_support, int64_t n, const uint32_t* sorted_keys,
+                         const int32_t* cell_start, const sph_grid* grid, int32_t cell_capacity, int32_t search_radius,
+                         const int32_t* offsets, int64_t pair_capacity, int32_t* cols, int32_t* status, void* stream) {
+  SPH_REQUIRE(n >= 0 && xy && sorted_support && sorted_keys && cell_start && grid && offsets && cols,
+              "nl_fill: bad arguments");
+  if (n == 0) return SPH_OK;
+  k_nl_fill<<<grid_for(n, 256), 256, 0, as_stream(stream)>>>(reinterpret_cast<const float2*>(xy), sorted_support, n,
+                                                              sorted_keys, cell_start, grid, cell_capacity,
+                                                              search_radius, offsets, pair_capacity, cols, status);
+  SPH_CHECK_LAUNCH("nl_fill");
+  return SPH_OK;
+}
+
+sph_status_t sph_nl_to_coo(const float* xy, int64_t n, const uint32_t* order, const uint32_t* rank,
+                           const int32_t* offsets, const int32_t* cols, const int64_t* orig_offsets,
+                           float grad_threshold, float kernel_support, int64_t* pairs, int64_t num_pairs, float* dist,
+                           float* radial, void* stream) {
+  SPH_REQUIRE(n >= 0 && xy && order && rank && offsets && cols && orig_offsets && pairs, "nl_to_coo: bad arguments");
+  if (n == 0) return SPH_OK;
+  k_nl_to_coo<<<grid_for(n, 128), 128, 0, as_stream(stream)>>>(reinterpret_cast<const float2*>(xy), n, order, rank,
+                                                                offsets, cols, orig_offsets, grad_threshold,
+                                                                kernel_support, pairs, num_pairs, dist, radial);
+  SPH_CHECK_LAUNCH("nl_to_coo");
+  return SPH_OK;
+}
+
+sph_status_t sph_nl_query_count(const float* query_pos, const float* query_support, int64_t m, const float* xy,
+                                const int32_t* cell_start, const sph_grid* grid, int32_t cell_capacity,
+                                int32_t search_radius, int32_t* counts, void* stream) {
+  SPH_REQUIRE(m >= 0 && query_pos && query_support && xy && cell_start && grid && counts && search_radius >= 0,
+              "nl_query: bad arguments");
+  if (m == 0) return SPH_OK;
+  k_nl_query<false><<<grid_for(m, 128), 128, 0, as_stream(stream)>>>(
+      reinterpret_cast<const float2*>(query_pos), query_support, m, reinterpret_cast<const float2*>(xy), cell_start,
+      grid, cell_capacity, search_radius, nullptr, counts, nullptr, nullptr, nullptr);
+  SPH_CHECK_LAUNCH("nl_query_count");
+  return SPH_OK;
+}
+
+sph_status_t sph_nl_query_fill(const float* query_pos, const float* query_support, int64_t m, const float* xy,
+                               const int32_t* cell_start, const sph_grid* grid, int32_t cell_capacity,
+                               int32_t search_radius, const uint32_t* order, const int64_t* offsets, int32_t* rows,
+                               int32_t* cols, void* stream) {
+  SPH_REQUIRE(m >= 0 && query_pos && query_support && xy && cell_start && grid && offsets && rows && cols &&
+                  search_radius >= 0,
+              "nl_query: bad arguments");
+  if (m == 0) return SPH_OK;
+  k_nl_query<true><<<grid_for(m, 128), 128, 0, as_stream(stream)>>>(
+      reinterpret_cast<const float2*>(query_pos), query_support, m, reinterpret_cast<const float2*>(xy), cell_start,
+      grid, cell_capacity, search_radius, order, nullptr, offsets, rows, cols);
+  SPH_CHECK_LAUNCH("nl_query_fill");
+  return SPH_OK;
+}
+
+}  // extern "C"

@@ -42,11 +42,34 @@ inline int grid_for(int64_t n, int threads) {
 // reference's flags (GCC contracts dx*dx + dy*dy into fmaf(dx, dx, dy*dy)):
 //   sqrtf(fmaf(dx, dx, dy*dy)) < h_i,  dx = x_i - x_j (i = query).
 // Every operation is spelled as a round-to-nearest intrinsic so nvcc can neither
-// contract nor approximate it.  Returns the distance through *dist.
-__device__ __forceinline__ bool pair_pred(float xi, float yi, float xj, float yj, float hi, float* dist) {
+// contract nor approximate it.
+__device__ __forceinline__ float dist2_ref(float xi, float yi, float xj, float yj) {
   float dx = __fsub_rn(xi, xj);
   float dy = __fsub_rn(yi, yj);
-  float d = __fsqrt_rn(__fmaf_rn(dx, dx, __fmul_rn(dy, dy)));
+  return __fmaf_rn(dx, dx, __fmul_rn(dy, dy));
+}
+
+// Square-root-free form of the same predicate.  For a float v >= 0 and a float h > 0,
+// with IEEE round-to-nearest sqrt:  RN(sqrt(v)) < h  <=>  sqrt(v) < m, where m is the
+// midpoint between h and its float predecessor (RN(x) <= pred(h) exactly when x < m; a tie
+// x = m cannot occur because m^2 has an odd ~50-bit significand while v has 24 bits).
+// m^2 is exact in double, so the predicate is  v <= F  with F the largest float below
+// m^2.  F is computed once per query particle; the candidate loop then needs no sqrt.
+__device__ __forceinline__ float sq_threshold(float h) {
+  if (!(h > 0.f)) return -1.0f;          // sqrt(v) >= 0 >= h: nothing passes (NaN h too)
+  if (isinf(h)) return 3.40282347e38f;   // every finite v passes
+  float p = nextafterf(h, 0.0f);
+  double m = ((double)p + (double)h) * 0.5;
+  double m2 = m * m;
+  float f = __double2float_rn(m2);
+  if ((double)f >= m2) f = nextafterf(f, 0.0f);
+  return f;
+}
+
+// Reference predicate with the distance: true iff sqrtf(fmaf(dx,dx,dy*dy)) < h_i.
+__device__ __forceinline__ bool pair_pred(float xi, float yi, float xj, float yj, float hi, float* dist) {
+  float v = dist2_ref(xi, yi, xj, yj);
+  float d = __fsqrt_rn(v);
   *dist = d;
   return d < hi;
 }
@@ -63,6 +86,11 @@ __device__ __forceinline__ float wendland(float q, float c_w) {
   float a = 1.0f - q;
   float a2 = a * a;
   return a2 * a2 * (1.0f + 4.0f * q) * c_w;
+}
+
+// A grid is usable only if its cells fit the cell table.
+__device__ __forceinline__ bool grid_ok(const sph_grid& g, int32_t cap) {
+  return g.num_cells <= cap && g.cells_x > 0 && g.cells_y > 0;
 }
 
 __device__ __forceinline__ void flag(int32_t* status, int32_t f) {

@@ -1,5 +1,5 @@
-"""Native GB300 neighbor search: cell keys -> radix sort -> sorted SoA -> cell table ->
-two-pass CSR (count with fused density, scan, fill).
+"""Native GB300 neighbor search: cell keys -> sort by cell key -> sorted SoA -> cell table
+-> two-pass CSR (count with fused density, scan, fill).
 
 This replaces the reference's search path (src/modules/neighborSearch.py:30-171 and
 cppSrc/neighSearch*.{cpp,cu}).  Pairs are kept as CSR over the particles in cell-sorted
@@ -13,12 +13,12 @@ through the device status word (`CSRNeighbors.check()`).
 """
 from __future__ import annotations
 
+import ctypes
 import math
 
 import torch
 
 from . import _native as N
-
 
 MAX_CELLS = 1 << 28  # dense cell table limit (1 GiB of int32 starts)
 
@@ -38,41 +38,44 @@ class Workspace:
             self._bufs[name] = b
         return b[:numel]
 
+    def zeros(self, name, numel, dtype=torch.int32):
+        """Like get(), but zero-filled the first time the buffer is created."""
+        b = self._bufs.get(name)
+        fresh = b is None or b.numel() < max(int(numel), 1) or b.dtype != dtype
+        t = self.get(name, numel, dtype)
+        if fresh:
+            t.zero_()
+        return t
+
     def bytes(self, name, nbytes):
         return self.get(name, (int(nbytes) + 7) // 8, torch.int64)
 
 
 def grid_from_bytes(t: torch.Tensor) -> dict:
     """Decode an sph_grid struct read back to the host."""
-    raw = t.detach().cpu()
-    f = raw[:4].view(torch.float32) if raw.dtype == torch.int32 else None
-    f = raw.view(torch.int32)[:4].view(torch.float32)
-    i = raw.view(torch.int32)[4:8]
+    raw = t.detach().cpu().view(torch.int32)
+    f = raw[:4].view(torch.float32)
+    i = raw[4:8]
     return {"qmin": (float(f[0]), float(f[1])), "hmax": float(f[2]), "cells_x": int(i[0]),
             "cells_y": int(i[1]), "num_cells": int(i[2])}
+
+
+def _f2(v):
+    if v is None:
+        return None
+    arr = (ctypes.c_float * 2)(float(v[0]), float(v[1]))
+    return ctypes.cast(arr, ctypes.c_void_p)
 
 
 class CSRNeighbors:
     """Result of one search: sorted SoA, cell table and CSR pairs (all on the device)."""
 
-    def __init__(self, n, order, keys, packed, cell_start, counts, offsets, cols, rho, grid, status,
-                 cell_capacity, pair_capacity, kernel_support, search_radius):
-        self.n = n
-        self.order = order          # int32 [n]: original index of sorted particle s
-        self.keys = keys            # int32 [n]: sorted cell keys
-        self.packed = packed        # float32 [n, 4]: (x, y, support, area) in sorted order
-        self.cell_start = cell_start
-        self.counts = counts        # int32 [n]
-        self.offsets = offsets      # int32 [n+1]
-        self.cols = cols            # int32 [pair_capacity]
-        self.rho = rho              # float32 [n] (sorted order) or None
-        self.grid = grid            # int32 [8] device bytes of sph_grid
-        self.status = status        # int32 [1] device status word
-        self.cell_capacity = cell_capacity
-        self.pair_capacity = pair_capacity
-        self.kernel_support = kernel_support
-        self.search_radius = search_radius
+    def __init__(self, **kw):
+        self.__dict__.update(kw)
         self._rank = None
+
+    # n, order, keys, xy, sh, sa, cell_start, counts, offsets, cols, rho, grid, status,
+    # cell_capacity, pair_capacity, kernel_support, search_radius
 
     @property
     def num_pairs(self) -> int:
@@ -98,11 +101,15 @@ class CSRNeighbors:
             N.call("sph_invert_permutation", N.ptr(self.order), self.n, N.ptr(self._rank), N.stream_ptr())
         return self._rank
 
+    def to_original(self, field: torch.Tensor) -> torch.Tensor:
+        """A sorted-order float32 field back in original particle order."""
+        out = torch.empty(self.n, dtype=torch.float32, device=self.order.device)
+        N.call("sph_scatter_f32", N.ptr(self.order), N.ptr(field), self.n, N.ptr(out), N.stream_ptr())
+        return out
+
     def density(self) -> torch.Tensor:
         """rho in original particle order."""
-        out = torch.empty(self.n, dtype=torch.float32, device=self.order.device)
-        N.call("sph_scatter_f32", N.ptr(self.order), N.ptr(self.rho), self.n, N.ptr(out), N.stream_ptr())
-        return out
+        return self.to_original(self.rho)
 
     def to_coo(self, grad_threshold: float = 1e-7, distances: bool = True):
         """(fluidNeighbors int64 [2,P], fluidDistances [P,2], fluidRadialDistances [P]) in the
@@ -120,102 +127,160 @@ class CSRNeighbors:
         pairs = torch.empty((2, P), dtype=torch.int64, device=dev)
         dist = torch.empty((P, 2), dtype=torch.float32, device=dev) if distances else None
         radial = torch.empty(P, dtype=torch.float32, device=dev) if distances else None
-        N.call("sph_nl_to_coo", N.ptr(self.packed), self.n, N.ptr(self.order), N.ptr(self.rank),
+        N.call("sph_nl_to_coo", N.ptr(self.xy), self.n, N.ptr(self.order), N.ptr(self.rank),
                N.ptr(self.offsets), N.ptr(self.cols), N.ptr(orig_off), float(grad_threshold),
                float(self.kernel_support or 1.0), N.ptr(pairs), P, N.ptr(dist), N.ptr(radial), st)
         return pairs, dist, radial
 
+    def query(self, qpos: torch.Tensor, qsupport: torch.Tensor, search_radius: int | None = None,
+              original_indices: bool = True):
+        """Pairs of arbitrary query points against this grid (searchExisting,
+        src/modules/neighborSearch.py:231-252): rows = query index, cols = particle index
+        (original order by default), predicate |x_q - x_j| < support_q."""
+        r = self.search_radius if search_radius is None else int(search_radius)
+        m = qpos.shape[0]
+        dev = self.order.device
+        st = N.stream_ptr()
+        qpos = qpos.contiguous()
+        qsupport = qsupport.contiguous()
+        counts = torch.empty(max(m, 1), dtype=torch.int32, device=dev)
+        if m == 0:
+            e = torch.empty(0, dtype=torch.int32, device=dev)
+            return e, e.clone()
+        N.call("sph_nl_query_count", N.ptr(qpos), N.ptr(qsupport), m, N.ptr(self.xy), N.ptr(self.cell_start),
+               N.ptr(self.grid), self.cell_capacity, r, N.ptr(counts), st)
+        off = torch.empty(m + 1, dtype=torch.int64, device=dev)
+        scratch = torch.empty((N.load().sph_scan_scratch_bytes(m) + 7) // 8, dtype=torch.int64, device=dev)
+        N.call("sph_exclusive_scan_i32_to_i64", N.ptr(counts), N.ptr(off), m, N.ptr(scratch), scratch.numel() * 8, st)
+        P = int(off[m].item())
+        rows = torch.empty(P, dtype=torch.int32, device=dev)
+        cols = torch.empty(P, dtype=torch.int32, device=dev)
+        if P:
+            N.call("sph_nl_query_fill", N.ptr(qpos), N.ptr(qsupport), m, N.ptr(self.xy), N.ptr(self.cell_start),
+                   N.ptr(self.grid), self.cell_capacity, r, N.ptr(self.order) if original_indices else None,
+                   N.ptr(off), N.ptr(rows), N.ptr(cols), st)
+        return rows, cols
+
 
 class GridSearch:
-    """Hashed-grid neighbor search with CSR output, reusing its device workspace."""
+    """Hashed-grid neighbor search with CSR output, reusing its device workspace.
 
-    def __init__(self, device=None, digit_bits: int = 8, threads_per_particle: int = 1):
+    sort = "counting" (one pass, the digit is the whole cell key) or "radix" (LSD radix
+    with `digit_bits` per pass); both give the (key, index) order of a stable sort."""
+
+    def __init__(self, device=None, sort: str = "counting", digit_bits: int = 8):
         if device is None:
             device = torch.device("cuda", torch.cuda.current_device())
         self.device = torch.device(device)
         self.ws = Workspace(self.device)
+        if sort not in ("counting", "radix"):
+            raise ValueError(sort)
+        self.sort = sort
         self.digit_bits = int(digit_bits)
-        self.threads_per_particle = int(threads_per_particle)
 
-    def grid(self, pos, support, min_coord=None, max_coord=None, cell_capacity=(1 << 31) - 2):
+    def grid(self, pos, support, min_coord=None, max_coord=None, cell_capacity=MAX_CELLS):
         """Compute the search grid on the device; returns the device grid bytes."""
         lib = N.load()
         n = pos.shape[0]
         grid = self.ws.get("grid", 8, torch.int32)
         status = self.ws.get("status", 1, torch.int32)
-        scratch_b = lib.sph_grid_scratch_bytes(n)
-        scratch = self.ws.bytes("grid_scratch", scratch_b)
-        mn = (ctypes_f2(min_coord) if min_coord is not None else None)
-        mx = (ctypes_f2(max_coord) if max_coord is not None else None)
-        N.call("sph_grid_build", N.ptr(pos), N.ptr(support), n, mn, mx, int(cell_capacity), N.ptr(grid),
-               N.ptr(status), N.ptr(scratch), scratch.numel() * 8, N.stream_ptr())
+        scratch = self.ws.bytes("grid_scratch", lib.sph_grid_scratch_bytes(n))
+        N.call("sph_grid_build", N.ptr(pos), N.ptr(support), n, _f2(min_coord), _f2(max_coord), int(cell_capacity),
+               N.ptr(grid), N.ptr(status), N.ptr(scratch), scratch.numel() * 8, N.stream_ptr())
         return grid
+
+    def auto_cell_capacity(self, pos, support, min_coord=None, max_coord=None) -> int:
+        """Number of grid cells (one host synchronisation)."""
+        status = self.ws.get("status", 1, torch.int32)
+        status.zero_()
+        g = self.grid(pos, support, min_coord, max_coord, MAX_CELLS)
+        info = grid_from_bytes(g)
+        flags = int(status.item())
+        status.zero_()
+        if flags & N.SPH_FLAG_NONFINITE:
+            raise N.SPHError("neighbor search: non-finite positions or supports")
+        if flags & N.SPH_FLAG_CELL_CAPACITY:
+            raise N.SPHError(f"neighbor search: the grid needs more than {MAX_CELLS} cells "
+                             f"(domain / support ratio too large for the dense cell table)")
+        return max(info["num_cells"], 1)
 
     def run(self, pos, support, area=None, kernel_support=None, min_coord=None, max_coord=None,
             search_radius: int = 1, cell_capacity: int | None = None, pair_capacity: int | None = None,
-            density: bool = True, sync: bool = True) -> CSRNeighbors:
+            density: bool = True, sync: bool = True, marks=None) -> CSRNeighbors:
+        """One search.  `marks(name)` (optional) is called at each phase boundary, e.g. to
+        record CUDA events: "start", "keys", "sort", "gather", "count", "scan", "fill"."""
         lib = N.load()
-        assert pos.is_cuda and pos.dtype == torch.float32 and pos.dim() == 2 and pos.shape[1] == 2
+        mark = marks or (lambda name: None)
+        if not (pos.is_cuda and pos.dtype == torch.float32 and pos.dim() == 2 and pos.shape[1] == 2):
+            raise N.SPHError("positions must be a float32 CUDA tensor of shape [N, 2]")
         pos = pos.contiguous()
         support = support.contiguous()
+        if area is not None:
+            area = area.contiguous()
         n = pos.shape[0]
         if n >= (1 << 31) - 1:
             raise N.SPHError("neighbor search: at most 2^31-2 particles")
         st = N.stream_ptr()
         ws = self.ws
+        if cell_capacity is None:
+            cell_capacity = self.auto_cell_capacity(pos, support, min_coord, max_coord)
+        cap = int(cell_capacity)
         status = ws.get("status", 1, torch.int32)
         status.zero_()
-        if cell_capacity is None:
-            g = self.grid(pos, support, min_coord, max_coord, MAX_CELLS)
-            info = grid_from_bytes(g)
-            flags = int(status.item())
-            if flags & N.SPH_FLAG_NONFINITE:
-                raise N.SPHError("neighbor search: non-finite positions or supports")
-            if flags & N.SPH_FLAG_CELL_CAPACITY:
-                raise N.SPHError(f"neighbor search: the grid needs more than {MAX_CELLS} cells "
-                                 f"(domain / support ratio too large for the dense cell table)")
-            cell_capacity = max(info["num_cells"], 1)
-            status.zero_()
-        grid = self.grid(pos, support, min_coord, max_coord, cell_capacity)
+        mark("start")
+        grid = self.grid(pos, support, min_coord, max_coord, cap)
         keys = ws.get("keys", n)
         order = ws.get("order", n)
-        N.call("sph_cell_keys", N.ptr(pos), n, N.ptr(grid), int(cell_capacity), N.ptr(keys), N.ptr(order),
-               N.ptr(status), st)
-        kb = lib.sph_key_bits(int(cell_capacity))
-        rs_b = lib.sph_radix_sort_scratch_bytes(n, self.digit_bits)
-        rs = ws.bytes("rs_scratch", rs_b)
-        N.call("sph_radix_sort_pairs", N.ptr(keys), N.ptr(order), n, kb, self.digit_bits, N.ptr(rs), rs.numel() * 8, st)
-        packed = ws.get("packed", 4 * n, torch.float32).view(n, 4)
-        N.call("sph_gather_packed", N.ptr(order), n, N.ptr(pos), N.ptr(support), N.ptr(area), N.ptr(packed), st)
-        cell_start = ws.get("cell_start", cell_capacity + 1)
-        N.call("sph_cell_starts", N.ptr(keys), n, int(cell_capacity), N.ptr(cell_start), st)
+        skeys = ws.get("sorted_keys", n)
+        cell_start = ws.get("cell_start", cap + 2)
+        if self.sort == "counting":
+            cell_count = ws.zeros("cell_count", cap + 1)  # left zeroed by every sort
+            N.call("sph_cell_keys", N.ptr(pos), n, N.ptr(grid), cap, N.ptr(keys), None, N.ptr(cell_count),
+                   N.ptr(status), st)
+            mark("keys")
+            cs = ws.bytes("cs_scratch", lib.sph_counting_sort_scratch_bytes(n, cap))
+            N.call("sph_counting_sort", N.ptr(keys), n, cap, N.ptr(cell_count), N.ptr(cell_start), N.ptr(order),
+                   N.ptr(skeys), N.ptr(status), N.ptr(cs), cs.numel() * 8, st)
+        else:
+            N.call("sph_cell_keys", N.ptr(pos), n, N.ptr(grid), cap, N.ptr(skeys), N.ptr(order), None,
+                   N.ptr(status), st)
+            mark("keys")
+            rs = ws.bytes("rs_scratch", lib.sph_radix_sort_scratch_bytes(n, self.digit_bits))
+            N.call("sph_radix_sort_pairs", N.ptr(skeys), N.ptr(order), n, lib.sph_key_bits(cap), self.digit_bits,
+                   N.ptr(rs), rs.numel() * 8, st)
+            N.call("sph_cell_starts", N.ptr(skeys), n, cap, N.ptr(cell_start), st)
+        mark("sort")
+        xy = ws.get("xy", 2 * n, torch.float32).view(n, 2)
+        sh = ws.get("sorted_support", n, torch.float32)
+        sa = ws.get("sorted_area", n, torch.float32) if area is not None else None
+        N.call("sph_gather_sorted", N.ptr(order), n, N.ptr(pos), N.ptr(support), N.ptr(area), N.ptr(xy), N.ptr(sh),
+               N.ptr(sa), st)
+        mark("gather")
         counts = ws.get("counts", n)
         rho = ws.get("rho", n, torch.float32) if density else None
         ks = float(kernel_support) if kernel_support is not None else 0.0
-        if density and ks <= 0:
-            raise N.SPHError("neighbor search: density needs kernel_support > 0")
-        N.call("sph_nl_count", N.ptr(packed), n, N.ptr(keys), N.ptr(cell_start), N.ptr(grid), int(cell_capacity),
+        if density and (ks <= 0 or area is None):
+            raise N.SPHError("neighbor search: density needs kernel_support > 0 and areas")
+        N.call("sph_nl_count", N.ptr(xy), N.ptr(sh), N.ptr(sa), n, N.ptr(skeys), N.ptr(cell_start), N.ptr(grid), cap,
                int(search_radius), ks, N.ptr(counts), N.ptr(rho), st)
+        mark("count")
         offsets = ws.get("offsets", n + 1)
-        sc_b = lib.sph_scan_scratch_bytes(n)
-        sc = ws.bytes("scan_scratch", sc_b)
+        sc = ws.bytes("scan_scratch", lib.sph_scan_scratch_bytes(n))
         N.call("sph_exclusive_scan_i32", N.ptr(counts), N.ptr(offsets), n, N.ptr(sc), sc.numel() * 8, st)
+        mark("scan")
         if pair_capacity is None:
             pair_capacity = int(offsets[n].item())
         cols = ws.get("cols", pair_capacity)
-        N.call("sph_nl_fill", N.ptr(packed), n, N.ptr(keys), N.ptr(cell_start), N.ptr(grid), int(cell_capacity),
+        N.call("sph_nl_fill", N.ptr(xy), N.ptr(sh), n, N.ptr(skeys), N.ptr(cell_start), N.ptr(grid), cap,
                int(search_radius), N.ptr(offsets), int(pair_capacity), N.ptr(cols), N.ptr(status), st)
-        res = CSRNeighbors(n, order, keys, packed, cell_start, counts, offsets, cols, rho, grid, status,
-                           cell_capacity, pair_capacity, kernel_support, search_radius)
+        mark("fill")
+        res = CSRNeighbors(n=n, order=order, keys=skeys, xy=xy, sh=sh, sa=sa, cell_start=cell_start, counts=counts,
+                           offsets=offsets, cols=cols, rho=rho, grid=grid, status=status, cell_capacity=cap,
+                           pair_capacity=int(pair_capacity), kernel_support=kernel_support,
+                           search_radius=int(search_radius))
         if sync:
             res.check()
         return res
-
-
-def ctypes_f2(v):
-    import ctypes
-    arr = (ctypes.c_float * 2)(float(v[0]), float(v[1]))
-    return ctypes.cast(arr, ctypes.c_void_p)
 
 
 def next_prime(n: int) -> int:

@@ -28,19 +28,19 @@ def dom(g, c):
 def run_native(pos, h, area, support, vmin, vmax, **kw):
     from pytorchsph_gb300.search import GridSearch
     dev = torch.device("cuda")
-    gs = GridSearch(dev, **{k: v for k, v in kw.items() if k in ("digit_bits",)})
+    gs = GridSearch(dev, **{k: v for k, v in kw.items() if k in ("digit_bits", "sort")})
     res = gs.run(torch.from_numpy(pos).to(dev), torch.from_numpy(h).to(dev), torch.from_numpy(area).to(dev),
                  kernel_support=float(support), min_coord=vmin, max_coord=vmax)
     return res
 
 
 @pytest.mark.parametrize("case", CASES)
-@pytest.mark.parametrize("digit_bits", [8, 5])
-def test_native_csr_pairs_bit_exact(cuda, golden, case, digit_bits):
+@pytest.mark.parametrize("sort,digit_bits", [("counting", 8), ("radix", 8), ("radix", 5)])
+def test_native_csr_pairs_bit_exact(cuda, golden, case, sort, digit_bits):
     g = golden
     vmin, vmax = dom(g, case)
     res = run_native(g[f"{case}/pos"], g[f"{case}/h"], g[f"{case}/area"], g[f"{case}/support"], vmin, vmax,
-                     digit_bits=digit_bits)
+                     digit_bits=digit_bits, sort=sort)
     pairs, dist, radial = res.to_coo()
     got = pairs_key(pairs[0].cpu().numpy(), pairs[1].cpu().numpy())
     assert np.array_equal(got, csr_key(g[f"{case}/offsets"], g[f"{case}/cols"]))
@@ -177,6 +177,46 @@ def test_full_size_search_density(cuda, variant):
         pytest.fail("variant A input generation is not bit-reproducible on this machine")
 
 
+def test_sort_variants_agree(cuda):
+    """Counting sort and LSD radix sort give the same (key, index) order."""
+    from pytorchsph_gb300.search import GridSearch
+    from pytorchsph_gb300 import workloads
+    dev = torch.device("cuda")
+    pos = torch.from_numpy(workloads.gaussian_uniform_mix(50000, 0.05, (0.5, 0.5), 7)).to(dev)
+    h = torch.full((50000,), 0.01, device=dev)
+    a = GridSearch(dev, sort="counting").run(pos, h, None, min_coord=[0, 0], max_coord=[1, 1], density=False)
+    b = GridSearch(dev, sort="radix", digit_bits=6).run(pos, h, None, min_coord=[0, 0], max_coord=[1, 1],
+                                                        density=False)
+    assert torch.equal(a.order, b.order)
+    assert torch.equal(a.keys, b.keys)
+    assert torch.equal(a.cell_start[:a.cell_capacity + 2], b.cell_start[:b.cell_capacity + 2])
+    assert torch.equal(a.cols[:a.num_pairs], b.cols[:b.num_pairs])
+
+
+def test_counting_sort_large_cells(cuda):
+    """Cells above the per-thread sort limit (48) and the block limit (2048): the pair count
+    stays exact, cells up to 2048 keep (key, index) order, bigger ones flag CELL_ORDER."""
+    from pytorchsph_gb300.search import GridSearch
+    from pytorchsph_gb300 import _native as N
+    dev = torch.device("cuda")
+    rng = np.random.default_rng(5)
+    pos = np.concatenate([np.full((3000, 2), 0.505) + rng.normal(0, 1e-4, (3000, 2)),
+                          np.full((300, 2), 0.205) + rng.normal(0, 1e-4, (300, 2)),
+                          rng.uniform(0, 1, (2000, 2))]).astype(np.float32)
+    h = np.full(len(pos), 0.01, np.float32)
+    res = GridSearch(dev).run(torch.from_numpy(pos).to(dev), torch.from_numpy(h).to(dev), None,
+                              min_coord=[0, 0], max_coord=[1, 1], density=False, sync=False)
+    assert res.flags() == N.SPH_FLAG_CELL_ORDER
+    order = res.order.cpu().numpy()
+    cs = res.cell_start[:res.cell_capacity + 2].cpu().numpy()
+    sizes = np.diff(cs)
+    assert sizes.max() > 2048 and np.sort(sizes)[-2] > 48
+    for c in np.flatnonzero((sizes > 1) & (sizes <= 2048)):
+        assert np.all(np.diff(order[cs[c]:cs[c + 1]].astype(np.int64)) > 0)
+    si, off, cols = ns.search(pos, h, np.zeros(2, np.float32), np.ones(2, np.float32))
+    assert res.num_pairs == int(off[-1])
+
+
 def test_status_flags(cuda):
     from pytorchsph_gb300.search import GridSearch
     from pytorchsph_gb300 import _native as N
@@ -189,10 +229,14 @@ def test_status_flags(cuda):
     pos2[0] = torch.tensor([5.0, 5.0])
     res = gs.run(pos2, h, None, min_coord=[0, 0], max_coord=[1, 1], density=False, sync=False)
     assert res.flags() & N.SPH_FLAG_OUT_OF_GRID
-    # NaN positions flag NONFINITE
+    # NaN positions: the automatic grid sizing refuses them; with a given cell table the
+    # particle is flagged NONFINITE and left out of the search
     pos3 = pos.clone()
     pos3[3, 0] = float("nan")
-    res = gs.run(pos3, h, None, min_coord=[0, 0], max_coord=[1, 1], density=False, sync=False)
+    with pytest.raises(N.SPHError, match="non-finite"):
+        gs.run(pos3, h, None, min_coord=[0, 0], max_coord=[1, 1], density=False)
+    res = gs.run(pos3, h, None, min_coord=[0, 0], max_coord=[1, 1], density=False, cell_capacity=4096,
+                 sync=False)
     assert res.flags() & N.SPH_FLAG_NONFINITE
     with pytest.raises(N.SPHError):
         res.check()

@@ -112,3 +112,25 @@ def test_oracle_against_compiled_reference(seed):
     ref = np.sort(rr.numpy().astype(np.int64) * (1 << 32) + rc.numpy())
     got = np.sort(r.astype(np.int64) * (1 << 32) + c)
     assert np.array_equal(got, ref)
+
+
+def test_square_root_free_predicate_is_exact():
+    """The GPU tests v <= F(h) instead of sqrtf(v) < h (csrc/sph_common.cuh, sq_threshold).
+    Restated here with numpy float32/float64 and checked against IEEE sqrtf on random and
+    adversarial (v within a few ulps of h^2) inputs."""
+    rng = np.random.default_rng(0)
+    h = np.concatenate([rng.uniform(1e-4, 10, 200000), np.float32(3 / 1024) * np.ones(1000),
+                        2.0 ** rng.integers(-20, 20, 1000)]).astype(np.float32)
+    p = np.nextafter(h, np.float32(0))
+    m = (p.astype(np.float64) + h.astype(np.float64)) * 0.5
+    m2 = m * m
+    F = m2.astype(np.float32)
+    F = np.where(F.astype(np.float64) >= m2, np.nextafter(F, np.float32(0)), F)
+    base = (h.astype(np.float64) ** 2).astype(np.float32)
+    for k in range(-6, 7):
+        v = base.view(np.int32) + np.int32(k)
+        v = v.view(np.float32)
+        ref = np.sqrt(v) < h
+        assert np.array_equal(v <= F, ref), k
+    v = rng.uniform(0, 100, h.shape).astype(np.float32)
+    assert np.array_equal(v <= F, np.sqrt(v) < h)
