@@ -64,6 +64,7 @@ SPH_FLAG_NONFINITE = 2
 SPH_FLAG_PAIR_CAPACITY = 4
 SPH_FLAG_CELL_CAPACITY = 8
 SPH_FLAG_ITERATION_CAP = 16
+SPH_FLAG_CELL_ORDER = 32
 
 FLAG_NAMES = {
     SPH_FLAG_OUT_OF_GRID: "a particle lies outside the search grid",
@@ -71,6 +72,7 @@ FLAG_NAMES = {
     SPH_FLAG_PAIR_CAPACITY: "neighbor pair buffer too small",
     SPH_FLAG_CELL_CAPACITY: "search grid has more cells than the cell table holds",
     SPH_FLAG_ITERATION_CAP: "an iterative solve stopped at its maximum iteration count",
+    SPH_FLAG_CELL_ORDER: "a cell held more than 2048 particles; their order inside the cell is not reproducible",
 }
 
 _lib = None
