@@ -68,6 +68,20 @@ sph_status_t sph_exclusive_scan_i32(const int32_t* in, int32_t* out, int64_t n, 
 sph_status_t sph_exclusive_scan_i32_to_i64(const int32_t* in, int64_t* out, int64_t n, void* scratch,
                                            size_t scratch_bytes, void* stream);
 
+/* Allocation-free variant of sph_exclusive_scan_i32.  It has no counterpart in the
+ * reference; it exists for callers that cannot allocate device memory: a host runtime
+ * bound through this C ABI that only receives device pointers from another owner of
+ * GPU memory, or code recording a CUDA graph, where cudaMalloc is not permitted.  The
+ * scan's block sums live in a fixed 64 KiB array in the library's device memory (one per
+ * GPU, held until the process exits), so n is limited to
+ * sph_exclusive_scan_i32_static_max_items() = 33,550,336; larger n is rejected with
+ * SPH_ERR_INVALID_ARGUMENT.  Nothing in the array needs to start at zero.  The first call
+ * on a device looks up the array's device address (cudaGetSymbolAddress) and should come
+ * before any stream capture.  All calls share the one array: calls whose work overlaps on
+ * the GPU (different streams, or different host threads) race and corrupt each other. */
+int64_t sph_exclusive_scan_i32_static_max_items(void);
+sph_status_t sph_exclusive_scan_i32_static(const int32_t* in, int32_t* out, int64_t n, void* stream);
+
 /* Scratch bytes sph_radix_sort_pairs needs. */
 size_t sph_radix_sort_scratch_bytes(int64_t n, int32_t digit_bits);
 /* Stable LSD radix sort of (keys, vals) by the low key_bits bits of keys, digit_bits

@@ -154,6 +154,44 @@ static sph_status_t scan_impl(const int32_t* in, TOut* out, int64_t n, void* scr
   return SPH_OK;
 }
 
+// ------------------------------------------------------------------ allocation-free scan
+// Scratch for sph_exclusive_scan_i32_static: one int64 block sum per 4096-item tile plus
+// the total.  64 KiB of device memory in every GPU that loads this library, held until
+// the process exits.  It caps n at (kStaticScanSlots - 1) * kScanTile = 33,550,336 items.
+constexpr int kStaticScanSlots = 8192;
+static __device__ __align__(256) int64_t g_static_scan_scratch[kStaticScanSlots];
+
+constexpr int kMaxDevices = 64;
+static void* g_static_scan_ptr[kMaxDevices] = {nullptr};
+static std::mutex g_static_scan_mu;
+
+// Device address of g_static_scan_scratch for the current device.  The host-side symbol
+// is only a stand-in: kernels must be given this address.  Looked up once per device.
+static sph_status_t static_scan_scratch(void** out) {
+  int dev = -1;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) {
+    set_error("static scan: cudaGetDevice", e);
+    return SPH_ERR_CUDA;
+  }
+  if (dev < 0 || dev >= kMaxDevices) {
+    set_error_text("static scan: device index out of range");
+    return SPH_ERR_INVALID_ARGUMENT;
+  }
+  std::lock_guard<std::mutex> lock(g_static_scan_mu);
+  if (g_static_scan_ptr[dev] == nullptr) {
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_static_scan_scratch);
+    if (e != cudaSuccess || p == nullptr) {
+      set_error("static scan: cudaGetSymbolAddress", e);
+      return SPH_ERR_CUDA;
+    }
+    g_static_scan_ptr[dev] = p;
+  }
+  *out = g_static_scan_ptr[dev];
+  return SPH_OK;
+}
+
 // ------------------------------------------------------------------ radix sort
 constexpr int kRsThreads = 256;
 constexpr int kRsWarps = kRsThreads / 32;
@@ -271,6 +309,23 @@ sph_status_t sph_exclusive_scan_i32(const int32_t* in, int32_t* out, int64_t n, 
 sph_status_t sph_exclusive_scan_i32_to_i64(const int32_t* in, int64_t* out, int64_t n, void* scratch,
                                            size_t scratch_bytes, void* stream) {
   return scan_impl<int64_t>(in, out, n, scratch, scratch_bytes, stream);
+}
+
+int64_t sph_exclusive_scan_i32_static_max_items(void) {
+  return (int64_t)(kStaticScanSlots - 1) * kScanTile;
+}
+
+sph_status_t sph_exclusive_scan_i32_static(const int32_t* in, int32_t* out, int64_t n, void* stream) {
+  SPH_REQUIRE(n >= 0 && out != nullptr && (n == 0 || in != nullptr), "static scan: bad arguments");
+  if (n > sph_exclusive_scan_i32_static_max_items()) {
+    set_error_text("static scan: n exceeds the fixed scratch (at most 33,550,336 items); "
+                   "use sph_exclusive_scan_i32 with caller-provided scratch");
+    return SPH_ERR_INVALID_ARGUMENT;
+  }
+  void* scratch = nullptr;
+  sph_status_t s = static_scan_scratch(&scratch);
+  if (s != SPH_OK) return s;
+  return scan_impl<int32_t>(in, out, n, scratch, sizeof(int64_t) * kStaticScanSlots, stream);
 }
 
 size_t sph_radix_sort_scratch_bytes(int64_t n, int32_t digit_bits) {
