@@ -58,3 +58,74 @@ def search_density_case(variant: str = "A", n_side: int = 1024):
     area = np.full(n, np.float32(dx * dx), np.float32)
     hash_len = 1 << 22 if n == 1 << 20 else -1
     return pos, h, area, np.array([0.0, 0.0], np.float32), np.array([1.0, 1.0], np.float32), hash_len
+
+
+def tank_walls(width: float, height: float, dx: float, layers: int = 3):
+    """Ghost-particle walls of a rectangular tank [0, width] x [0, height].
+
+    Layer k lies at distance (k + 1/2) dx outside the tank walls (the offsets
+    (2k+1) * packing/2 of src/modules/solidBoundary.py:142-146), sampled every dx along the
+    offset rectangle.  Each wall particle's ghost is its mirror image inside the tank (the
+    `mirrored` samples of src/ghostParticles.py:132-135), reflected through the corner at
+    corners.  Returns (wall_positions, ghost_positions), float32 [Nb, 2]."""
+    pts = []
+    for k in range(layers):
+        d = (k + 0.5) * dx
+        x0, x1, y0, y1 = -d, width + d, -d, height + d
+        nxs = int(round((x1 - x0) / dx)) + 1
+        nys = int(round((y1 - y0) / dx)) + 1
+        xs = x0 + np.arange(nxs) * dx
+        ys = y0 + np.arange(nys) * dx
+        pts.append(np.stack([xs, np.full(nxs, y0)], 1))
+        pts.append(np.stack([xs, np.full(nxs, y1)], 1))
+        pts.append(np.stack([np.full(nys - 2, x0), ys[1:-1]], 1))
+        pts.append(np.stack([np.full(nys - 2, x1), ys[1:-1]], 1))
+    w = np.concatenate(pts)
+    g = w.copy()
+    g[:, 0] = np.where(w[:, 0] < 0, -w[:, 0], np.where(w[:, 0] > width, 2 * width - w[:, 0], w[:, 0]))
+    g[:, 1] = np.where(w[:, 1] < 0, -w[:, 1], np.where(w[:, 1] > height, 2 * height - w[:, 1], w[:, 1]))
+    return w.astype(np.float32), g.astype(np.float32)
+
+
+def dam_break(nx: int = 64, ny: int = 128, dx: float = 0.01, tank=(4.0, 2.0), layers: int = 3):
+    """Dam-break scene: an nx x ny lattice fluid block (spacing dx) at the lower-left corner
+    of the tank, at rest, relative density 1, with ghost-particle walls.  Support h = 3 dx and
+    particle area A = dx^2 (particle radius dx / sqrt(pi)).  The search domain is the tank
+    widened by 2 h on every side (virtualMin/Max with buffer 2, src/simulationBase.py:968-969)."""
+    i, j = np.meshgrid(np.arange(nx, dtype=np.float64), np.arange(ny, dtype=np.float64), indexing="ij")
+    pos = np.stack([(i.ravel() + 0.5) * dx, (j.ravel() + 0.5) * dx], 1).astype(np.float32)
+    n = len(pos)
+    h = np.float32(3 * dx)
+    wall, ghost = tank_walls(tank[0], tank[1], dx, layers)
+    return {
+        "pos": pos, "vel": np.zeros((n, 2), np.float32), "rho": np.ones(n, np.float32),
+        "area": np.full(n, np.float32(dx * dx), np.float32), "support": np.full(n, h, np.float32),
+        "wall_pos": wall, "ghost_pos": ghost, "wall_area": np.full(len(wall), np.float32(dx * dx), np.float32),
+        "h": float(h), "dx": float(dx), "tank": (float(tank[0]), float(tank[1])),
+        "vmin": np.array([-2 * h, -2 * h], np.float32),
+        "vmax": np.array([tank[0] + 2 * h, tank[1] + 2 * h], np.float32),
+        "column_height": float(ny * dx),
+    }
+
+
+def oscillating_drop(n_target: int = 16384, radius: float = 0.5, amplitude: float = 1.0):
+    """Oscillating drop: lattice particles inside a circle of `radius` centred at the origin,
+    initial velocity v = A (x, -y) (the velocity idea of the reference notebook), no walls.
+    The spacing dx is chosen so that about n_target particles fall inside the circle."""
+    dx = float(np.sqrt(np.pi * radius * radius / n_target))
+    m = int(np.ceil(radius / dx)) + 1
+    k = np.arange(-m, m + 1, dtype=np.float64)
+    gx, gy = np.meshgrid(k * dx, k * dx, indexing="ij")
+    p = np.stack([gx.ravel(), gy.ravel()], 1)
+    p = p[np.linalg.norm(p, axis=1) <= radius - 0.5 * dx]
+    pos = p.astype(np.float32)
+    n = len(pos)
+    vel = (amplitude * np.stack([pos[:, 0], -pos[:, 1]], 1)).astype(np.float32)
+    h = np.float32(3 * dx)
+    ext = radius * 3
+    return {
+        "pos": pos, "vel": vel, "rho": np.ones(n, np.float32), "area": np.full(n, np.float32(dx * dx), np.float32),
+        "support": np.full(n, h, np.float32), "wall_pos": np.zeros((0, 2), np.float32),
+        "ghost_pos": np.zeros((0, 2), np.float32), "wall_area": np.zeros(0, np.float32), "h": float(h), "dx": dx,
+        "vmin": np.array([-ext, -ext], np.float32), "vmax": np.array([ext, ext], np.float32),
+    }
