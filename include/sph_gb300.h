@@ -52,6 +52,55 @@ typedef struct sph_grid {
   int32_t reserved2;
 } sph_grid;
 
+/* Physical and numerical parameters of the summations (one scene). */
+typedef struct sph_params {
+  float support;            /* kernel support h (config particle.support) */
+  float rest_density;       /* rho0 (fluid.restDensity) */
+  float c0;                 /* speed of sound (fluid.c0) */
+  float gamma;              /* Tait exponent (pressure.gamma) */
+  float alpha;              /* artificial viscosity (diffusion.alpha) */
+  float delta;              /* density diffusion (diffusion.delta) */
+  float kinematic;          /* laminar viscosity (diffusion.kinematic) */
+  float gravity[2];         /* constant body force (gravity.magnitude * gravity.direction) */
+  int32_t point_source;     /* 1: gravity = -g (x - c) (gravity.pointSource with potentialField) */
+  float point_magnitude;
+  float point_center[2];
+  int32_t density_diffusion;   /* 0 none, 1 MOG, 2 deltaSPH (diffusion.densityScheme) */
+  int32_t boundary_diffusion;  /* diffusion.boundaryDiffusion */
+  int32_t search_radius;       /* cells searched around a particle (1) */
+  int32_t cell_capacity;       /* size of the cell tables */
+  /* DFSPH (dfsph.*) */
+  int32_t min_density_iters, max_density_iters, min_divergence_iters, max_divergence_iters;
+  float density_threshold, divergence_threshold;
+  float omega_boundary;        /* wall relaxed-Jacobi weight (dfsph.relaxedJacobiOmega) */
+  float omega_fluid;           /* fluid relaxed-Jacobi weight (0.3 in the reference, src/modules/dfsph.py:175) */
+} sph_params;
+
+/* Fluid particles in cell-sorted order (device arrays) and their CSR neighbor list. */
+typedef struct sph_fluid_view {
+  const float* x;           /* float2 [n] positions */
+  const float* v;           /* float2 [n] velocities */
+  const float* rho;         /* [n] relative density rho~ (absolute = rho~ * rest_density) */
+  const float* area;        /* [n] particle area A */
+  const uint32_t* keys;     /* [n] cell keys of the sorted particles */
+  const int32_t* offsets;   /* [n+1] CSR row offsets */
+  const int32_t* cols;      /* [P] CSR columns (sorted indices) */
+  const int32_t* cell_start;/* [cells+2] fluid cell table */
+  int64_t n;
+} sph_fluid_view;
+
+/* Wall (ghost-particle boundary) particles sorted by their cell in the fluid grid. */
+typedef struct sph_wall_view {
+  const float* x;           /* float2 [nb] wall positions */
+  const float* ghost;       /* float2 [nb] mirrored ghost positions */
+  const float* area;        /* [nb] boundaryVolume = pi r^2 */
+  const int32_t* cell_start;/* [cells+2] wall cell table in the fluid grid */
+  int64_t n;
+  float* rho;               /* [nb] wall relative density (written) */
+  float* volume;            /* [nb] A_b / rho_b (written) */
+  float* pressure;          /* [nb] wall pressure (written) */
+} sph_wall_view;
+
 int32_t sph_abi_version(void);
 const char* sph_last_error(void);
 const char* sph_status_string(sph_status_t status);
@@ -191,6 +240,99 @@ sph_status_t sph_nl_query_fill(const float* query_pos, const float* query_suppor
                                const float* xy, const int32_t* cell_start, const sph_grid* grid,
                                int32_t cell_capacity, int32_t search_radius, const uint32_t* order,
                                const int64_t* offsets, int32_t* rows, int32_t* cols, void* stream);
+
+/* ---------------------------------------------------------------- deltaSPH summations (a8-a19) */
+
+/* mDBC wall density (computeBoundaryDensitymDBC, src/modules/solidBoundary.py:561-617):
+ * per wall particle, Shepard and first-order MLS sums over the fluid within h of its ghost,
+ * a 3x3 pseudo-inverse solve, rho_b = max(result, 1); writes walls->rho, ->volume
+ * (A_b / rho_b) and ->pressure (Tait, solidBoundary.py:802-804). */
+sph_status_t sph_mdbc_wall_density(const sph_fluid_view* fluid, const sph_wall_view* walls, const sph_grid* grid,
+                                   const sph_params* params, void* stream);
+/* The deltaSPH right-hand side (deltaSPHSimulation.timestep steps 6-12, src/deltaSPH.py:146-200):
+ * dpdt [n] = continuity (src/modules/momentum.py:13-19) + density diffusion (MOG
+ * densityDiffusion.py:56-63, or the renormalized deltaSPH scheme :12-52 when
+ * density_diffusion = 2, which needs L float4 [n] and grad_rho float2 [n] scratch);
+ * acc float2 [n] = gravity + pressure (pressure.py:13-19) + artificial viscosity
+ * (diffusion.py:12-25) + laminar viscosity (laminar.py:12-27), each with its wall part
+ * (solidBoundary.py:746-890).  Wall quantities must come from sph_mdbc_wall_density. */
+sph_status_t sph_deltasph_forces(const sph_fluid_view* fluid, const sph_wall_view* walls, const sph_grid* grid,
+                                 const sph_params* params, float* dpdt, float* acc, float* L, float* grad_rho,
+                                 void* stream);
+/* semiImplicitEuler (src/simulationBase.py:647-652): v' = v + dt a, x' = x + dt (v + dt a),
+ * rho' = rho + dt dpdt / rest_density when continuum_density.  dt is a device float. */
+sph_status_t sph_integrate_semi_implicit_euler(int64_t n, const float* x, const float* v, const float* rho,
+                                               const float* acc, const float* dpdt, const float* dt,
+                                               float rest_density, int32_t continuum_density, float* x_out,
+                                               float* v_out, float* rho_out, int32_t* status, void* stream);
+/* RK4 stage / combination (src/simulationBase.py:679-705): out = base + c*dt*(ku, ka, kd/rest_density). */
+sph_status_t sph_rk_axpy(int64_t n, const float* x0, const float* v0, const float* rho0_field, const float* ku,
+                         const float* ka, const float* kd, const float* dt, float c, float rest_density, float* x_out,
+                         float* v_out, float* rho_out, int32_t* status, void* stream);
+/* s = w*k (init) or s += w*k for the RK4 sums of (velocity, acceleration, dpdt). */
+sph_status_t sph_rk_accumulate(int64_t n, const float* ku, const float* ka, const float* kd, float w, int32_t init,
+                               float* su, float* sa, float* sd, void* stream);
+/* out[s] = in[order[s]] for 4-, 8- or 16-byte elements (re-sorting per-particle state). */
+sph_status_t sph_permute(const uint32_t* order, int64_t n, int32_t elem_bytes, const void* in, void* out, void* stream);
+
+/* ---------------------------------------------------------------- DFSPH (a20-a25) */
+
+/* Device work arrays of one DFSPH solve (fluid arrays [n] in sorted order, wall arrays [nb]). */
+typedef struct sph_dfsph_buffers {
+  float* rho;               /* relative density incl. the wall contribution */
+  float* volume;            /* A / fluid-only density (fluidVolume) */
+  float* actual_area;       /* A / rho (fluidActualArea) */
+  float* vstar;             /* float2 predicted velocity */
+  float* alpha;
+  float* source;
+  float* pressure;          /* fluidPressure2 */
+  float* pred_accel;        /* float2 fluidPredAccel */
+  float* residual;
+  float* wall_rho;          /* wall density (summation, <= 1) */
+  float* wall_actual_area;
+  float* wall_alpha;
+  float* wall_source;
+  float* wall_pressure;
+  float* wall_residual;
+  const float* wall_density_term;  /* static wall-wall kernel sum (sph_dfsph_wall_wall_term) */
+  double* partials;         /* [sph_dfsph_partials_count()] */
+  float* errors;            /* [max iterations + 1] error of every iteration */
+  int32_t* iters;           /* [1] iterations run */
+} sph_dfsph_buffers;
+
+size_t sph_dfsph_partials_count(void);
+/* Static wall-wall density term sum_b' W(|x_b - x_b'| / h) A_b' (solidBoundary.py:180-200). */
+sph_status_t sph_dfsph_wall_wall_term(const sph_wall_view* walls, const sph_grid* grid, const sph_params* params,
+                                      float* term, void* stream);
+/* Summation density with walls (density.py:26-34 + evalBoundaryDensitySummation,
+ * solidBoundary.py:522-549): bufs->rho = rho_fluid + sum_b W A_b, ->volume = A / rho_fluid,
+ * ->actual_area = A / rho; wall_rho = min(term + sum_f W A_f, 1), wall_actual_area. */
+sph_status_t sph_dfsph_densities(const sph_fluid_view* fluid, const sph_wall_view* walls, const sph_grid* grid,
+                                 const sph_params* params, const float* rho_fluid, const sph_dfsph_buffers* bufs,
+                                 void* stream);
+/* One DFSPH pressure solve (DFSPH(), src/modules/dfsph.py:263-311): predicted velocity
+ * v* = v + dt acc_in, alpha and source (with PBSPH wall terms when density != 0), then the
+ * relaxed-Jacobi loop of densitySolve / divergenceSolve (:195-260) as a single cooperative
+ * kernel with an in-kernel reduction of the mean error, bounded by the maximum iteration
+ * count; leaves the final predicted acceleration in bufs->pred_accel and the iteration
+ * count in bufs->iters.  A non-finite pressure flags SPH_FLAG_NONFINITE (the reference
+ * raises 'Pressure solver became unstable!'). */
+sph_status_t sph_dfsph_solve(const sph_fluid_view* fluid, const sph_wall_view* walls, const sph_grid* grid,
+                             const sph_params* params, const sph_dfsph_buffers* bufs, const float* acc_in,
+                             const float* dt, int32_t density, int32_t* status, void* stream);
+/* DFSPH steps 11-12 (src/dfsph.py:187-194): acc += artificial viscosity (with walls) +
+ * laminar viscosity, with V = A / fluid-only density and rho incl. walls. */
+sph_status_t sph_dfsph_viscosity(const sph_fluid_view* fluid, const sph_wall_view* walls, const sph_grid* grid,
+                                 const sph_params* params, const sph_dfsph_buffers* bufs, float* acc, void* stream);
+/* a += b (float2 [n]); a = (x, y) (float2 [n]). */
+sph_status_t sph_add_float2(int64_t n, const float* b, float* a, void* stream);
+sph_status_t sph_fill_float2(int64_t n, float x, float y, float* a, void* stream);
+/* Adaptive time step (adaptiveTimeSteppingModule.updateTimestep, src/modules/adaptiveDT.py:59-95)
+ * entirely on the device: dt <- min(max(target, dt/2), 1.05 dt). */
+size_t sph_dt_scratch_bytes(void);
+sph_status_t sph_update_dt(int64_t n, const float* v, const float* acc, float support, float kinematic, float cfl,
+                           float c0, int32_t acoustic_from_c0, float dt_min, float dt_max, float* dt, void* scratch,
+                           size_t scratch_bytes, void* stream);
 
 /* ---------------------------------------------------------------- drop-in hashed-table search */
 

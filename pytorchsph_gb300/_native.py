@@ -61,6 +61,30 @@ SIGNATURES = {
                                        _P, _P, _P]),
 }
 
+SIGNATURES.update({  # simulation kernels
+    "sph_mdbc_wall_density": (_I32, [_P] * 5),
+    "sph_deltasph_forces": (_I32, [_P] * 9),
+    "sph_integrate_semi_implicit_euler": (_I32, [_I64] + [_P] * 6 +
+                                          [_F32, _I32] + [_P] * 5),
+    "sph_rk_axpy": (_I32, [_I64] + [_P] * 7 + [_F32, _F32] +
+                    [_P] * 5),
+    "sph_rk_accumulate": (_I32, [_I64] + [_P] * 3 + [_F32, _I32] +
+                          [_P] * 4),
+    "sph_permute": (_I32, [_P, _I64, _I32] + [_P] * 3),
+    "sph_dfsph_partials_count": (_SZ, []),
+    "sph_dfsph_wall_wall_term": (_I32, [_P] * 5),
+    "sph_dfsph_densities": (_I32, [_P] * 7),
+    "sph_dfsph_solve": (_I32, [_P] * 7 + [_I32] + [_P] * 2),
+    "sph_dfsph_viscosity": (_I32, [_P] * 7),
+    "sph_add_float2": (_I32, [_I64, _P, _P, _P]),
+    "sph_fill_float2": (_I32, [_I64, _F32, _F32, _P,
+                                         _P]),
+    "sph_dt_scratch_bytes": (_SZ, []),
+    "sph_update_dt": (_I32, [_I64] + [_P] * 2 + [_F32] * 4 +
+                      [_I32, _F32, _F32] + [_P] * 2 +
+                      [_SZ, _P]),
+})
+
 SPH_FLAG_OUT_OF_GRID = 1
 SPH_FLAG_NONFINITE = 2
 SPH_FLAG_PAIR_CAPACITY = 4

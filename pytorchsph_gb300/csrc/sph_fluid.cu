@@ -1,0 +1,452 @@
+// deltaSPH right-hand side on sm_103a: one thread per fluid particle (cell-sorted order),
+// gathering over its CSR row and over the wall particles of the neighboring cells.  Every
+// sum is a gather into registers — no atomics, deterministic order: fluid neighbors in CSR
+// order, then walls, added to the fluid sum the way the reference adds its wall module's
+// result (`x += simulation.boundaryModule...`).
+//
+// Reference formulas (relative density rho~, absolute rho = rho~ rho0, V = A / rho~):
+//   continuity     src/modules/momentum.py:13-19 (+ wall solidBoundary.py:746-770)
+//   MOG diffusion  src/modules/densityDiffusion.py:56-63
+//   deltaSPH diff. src/modules/densityDiffusion.py:12-52 (+ wall L / grad parts,
+//                  solidBoundary.py:676-717), pinv2x2 src/util.py:386-433
+//   Tait EOS       src/modules/pressure.py:82-83 (wall: solidBoundary.py:802-804)
+//   pressure acc.  src/modules/pressure.py:13-19 (+ wall solidBoundary.py:846-890)
+//   art. viscosity src/modules/diffusion.py:12-25 (+ wall solidBoundary.py:820-844)
+//   laminar visc.  src/modules/laminar.py:12-27 (index choices kept: r = x_j - x_i, mu_j = rho_i nu)
+//   gravity        src/modules/gravity.py:46-57
+//   mDBC density   src/modules/solidBoundary.py:561-617
+#include "sph_math.cuh"
+
+namespace sph {
+
+// ---------------------------------------------------------------------------- mDBC
+// One thread per wall particle: Shepard and first-order MLS sums over the fluid particles
+// within h of its ghost (accumulated in double), the 3x3 pseudo-inverse solve, then the
+// wall density, volume and Tait pressure.
+__global__ void __launch_bounds__(128) k_mdbc(FluidView F, WallView W, const sph_grid* __restrict__ gp, SphParams P) {
+  int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= W.n) return;
+  const sph_grid g = *gp;
+  const float2 xg = W.xg[b];
+  const float thr = sq_threshold(P.h);
+  double nom = 0, den = 0, gx = 0, gy = 0, vgx = 0, vgy = 0, px = 0, py = 0;
+  double m00 = 0, m01 = 0, m10 = 0, m11 = 0;
+  int cnt = 0;
+  if (grid_ok(g, P.cell_capacity)) {
+    float fcx = ceilf(__fdiv_rn(__fsub_rn(xg.x, g.qmin[0]), g.hmax));
+    float fcy = ceilf(__fdiv_rn(__fsub_rn(xg.y, g.qmin[1]), g.hmax));
+    if (fcx > -1e9f && fcx < 1e9f && fcy > -1e9f && fcy < 1e9f) {
+      const int cx = (int)fcx, cy = (int)fcy, r = P.search_radius;
+      const int x0 = max(cx - r, 0), x1 = min(cx + r, g.cells_x - 1);
+      const int y0 = max(cy - r, 0), y1 = min(cy + r, g.cells_y - 1);
+      if (x0 <= x1) {
+        for (int yy = y0; yy <= y1; ++yy) {
+          const int row = yy * g.cells_x;
+          const int j0 = F.cell_start[row + x0], j1 = F.cell_start[row + x1 + 1];
+          for (int j = j0; j < j1; ++j) {
+            const float2 xj = F.x[j];
+            if (!(dist2_ref(xg.x, xg.y, xj.x, xj.y) <= thr)) continue;
+            const Geo e = geo(xg.x, xg.y, xj.x, xj.y, P.inv_h);   // e = (x_g - x_j)/r
+            const double k = kW(e.q, P.c_w);
+            const double gw = kGW(e.q, P.c_g);
+            const double ggx = gw * e.ex, ggy = gw * e.ey;
+            const double Aj = F.area[j];
+            const double mass = Aj * P.rho0;
+            const double Vj = Aj / (double)F.rho[j];
+            const double xx = (double)xj.x - xg.x, xy = (double)xj.y - xg.y;
+            nom += mass * k;
+            den += Vj * k;
+            gx += mass * ggx;
+            gy += mass * ggy;
+            vgx += Vj * ggx;
+            vgy += Vj * ggy;
+            px += Vj * k * xx;
+            py += Vj * k * xy;
+            m00 += Vj * xx * ggx;
+            m01 += Vj * xx * ggy;
+            m10 += Vj * xy * ggx;
+            m11 += Vj * xy * ggy;
+            ++cnt;
+          }
+        }
+      }
+    }
+  }
+  double rho_b = 1.0;
+  if (cnt > 0) rho_b = (nom / den) / P.rho0;
+  if (cnt > 10) {
+    const double A[3][3] = {{den, px, py}, {vgx, m00, m01}, {vgy, m10, m11}};
+    const double bb[3] = {nom, gx, gy};
+    double res[3];
+    pinv3_solve(A, bb, res);
+    const float2 xb = W.x[b];
+    rho_b = (res[0] + ((double)xb.x - xg.x) * res[1] + ((double)xb.y - xg.y) * res[2]) / P.rho0;
+  }
+  float rb = (float)fmax(rho_b, 1.0);
+  W.rho[b] = rb;
+  W.vol[b] = W.area[b] / rb;
+  W.p[b] = tait(rb, P);
+}
+
+// ---------------------------------------------------------------------------- pass 1
+// dpdt (continuity + MOG), acceleration (gravity, pressure, artificial and laminar
+// viscosity) and, for the deltaSPH scheme, the normalization matrix L.
+__global__ void __launch_bounds__(128) k_dsph_pass1(FluidView F, WallView W, const sph_grid* __restrict__ gp,
+                                                    SphParams P, float* __restrict__ dpdt, float2* __restrict__ acc,
+                                                    float4* __restrict__ Lout) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= F.n) return;
+  const float2 xi = F.x[i], vi = F.v[i];
+  const float rti = F.rho[i];
+  const float rhoi = rti * P.rho0;
+  const float pi = tait(rti, P);
+  float dp_f = 0.f, mog = 0.f;
+  float pax = 0.f, pay = 0.f, vax = 0.f, vay = 0.f, lax = 0.f, lay = 0.f;
+  float l00 = 0.f, l01 = 0.f, l10 = 0.f, l11 = 0.f;
+  const bool want_L = P.diffusion == 2;
+  const int k0 = F.offsets[i], k1 = F.offsets[i + 1];
+  for (int k = k0; k < k1; ++k) {
+    const int j = __ldg(F.cols + k);
+    const float2 xj = __ldg(F.x + j), vj = __ldg(F.v + j);
+    const float rtj = __ldg(F.rho + j), Aj = __ldg(F.area + j);
+    const float Vj = Aj / rtj, rhoj = rtj * P.rho0;
+    const Geo e = geo(xi.x, xi.y, xj.x, xj.y, P.inv_h);
+    const float gw = kGW(e.q, P.c_g);
+    const float gx = gw * e.ex, gy = gw * e.ey;
+    const float ux = vj.x - vi.x, uy = vj.y - vi.y;   // u_j - u_i
+    const float rx = -e.dx, ry = -e.dy;               // x_j - x_i
+    const float r2 = rx * rx + ry * ry + P.eps;
+    dp_f -= (ux * gx + uy * gy) * Vj * rhoj;
+    if (P.diffusion == 1) {
+      const float s = 2.0f * (rhoj - rhoi) / r2;
+      mog += (s * rx * gx + s * ry * gy) * Vj;
+    }
+    const float pj = tait(rtj, P);
+    const float pf = (pi + pj) * Vj;
+    pax += pf * gx;
+    pay += pf * gy;
+    float pij = ux * rx + uy * ry;
+    pij = fminf(pij, 0.f) / r2;
+    const float vf = pij * Vj * rhoj / (rhoi + rhoj);
+    vax += vf * gx;
+    vay += vf * gy;
+    const float mj = rhoj * Vj;
+    const float mu2 = 2.0f * rhoi * P.kinematic;
+    const float rs = rhoi + rhoj;
+    const float term = 4.0f * mj * mu2 * (rx * gx + ry * gy) / (rs * rs * r2);
+    lax -= term * (vi.x - vj.x);
+    lay -= term * (vi.y - vj.y);
+    if (want_L) {
+      l00 += Vj * rx * gx;
+      l01 += Vj * rx * gy;
+      l10 += Vj * ry * gx;
+      l11 += Vj * ry * gy;
+    }
+  }
+  float dp_w = 0.f, pwx = 0.f, pwy = 0.f, vwx = 0.f, vwy = 0.f;
+  float w00 = 0.f, w01 = 0.f, w10 = 0.f, w11 = 0.f;
+  if (W.n > 0) {
+    const sph_grid g = *gp;
+    int cx, cy;
+    cell_of(F.keys[i], g, &cx, &cy);
+    const float thr = sq_threshold(P.h);
+    for_each_wall(W, g, P.search_radius, cx, cy, xi.x, xi.y, thr, [&](int b, float2 xb) {
+      const Geo e = geo(xi.x, xi.y, xb.x, xb.y, P.inv_h);   // fluid side: e = (x_f - x_b)/r
+      const float gw = kGW(e.q, P.c_g);
+      const float gx = gw * e.ex, gy = gw * e.ey;
+      const float Vb = W.vol[b], rhob = W.rho[b] * P.rho0, pb = W.p[b];
+      const float ux = -vi.x, uy = -vi.y;               // u_b - u_f, walls at rest
+      dp_w -= (ux * gx + uy * gy) * Vb * rhob;
+      const float pf = (pi + pb) * Vb;
+      pwx += pf * gx;
+      pwy += pf * gy;
+      const float rx = -e.dx, ry = -e.dy;               // x_b - x_f
+      if (P.boundary_diffusion) {
+        const float r2 = rx * rx + ry * ry + P.eps;
+        float pij = fminf(ux * rx + uy * ry, 0.f) / r2;
+        const float vf = pij * Vb * rhob / (rhoi + rhob);
+        vwx += vf * gx;
+        vwy += vf * gy;
+      }
+      if (want_L) {
+        w00 += Vb * rx * gx;
+        w01 += Vb * rx * gy;
+        w10 += Vb * ry * gx;
+        w11 += Vb * ry * gy;
+      }
+    });
+  }
+  float d = dp_f + dp_w;
+  if (P.diffusion == 1) d += P.diff_k * mog;
+  dpdt[i] = d;
+  float ax, ay;
+  if (P.point_source) {
+    float dx = xi.x - P.point_cx, dy = xi.y - P.point_cy;
+    float dist = sqrtf(dx * dx + dy * dy);
+    if (dist > 1e-7f) {
+      dx /= dist;
+      dy /= dist;
+    }
+    ax = -P.point_mag * dx * dist;
+    ay = -P.point_mag * dy * dist;
+  } else {
+    ax = P.gx;
+    ay = P.gy;
+  }
+  const float ir = -1.0f / rhoi;
+  ax += ir * pax + ir * pwx;
+  ay += ir * pay + ir * pwy;
+  ax += P.visc_k * vax + P.visc_k * vwx;
+  ay += P.visc_k * vay + P.visc_k * vwy;
+  ax += lax;
+  ay += lay;
+  acc[i] = make_float2(ax, ay);
+  if (want_L) Lout[i] = make_float4(l00 + w00, l01 + w01, l10 + w10, l11 + w11);
+}
+
+// ---------------------------------------------------------------------------- pass 2 (deltaSPH)
+// <grad rho>_i = -sum_j 2 (rho_j - rho_i) V_j L_i^+ gradW_ij  (+ walls)
+__global__ void __launch_bounds__(128) k_dsph_gradrho(FluidView F, WallView W, const sph_grid* __restrict__ gp,
+                                                      SphParams P, const float4* __restrict__ L,
+                                                      float2* __restrict__ grad_rho) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= F.n) return;
+  const float4 m = L[i];
+  const float4 Li = pinv2x2(m.x, m.y, m.z, m.w);
+  const float2 xi = F.x[i];
+  const float rhoi = F.rho[i] * P.rho0;
+  float fx = 0.f, fy = 0.f;
+  const int k0 = F.offsets[i], k1 = F.offsets[i + 1];
+  for (int k = k0; k < k1; ++k) {
+    const int j = __ldg(F.cols + k);
+    const float2 xj = __ldg(F.x + j);
+    const float rtj = __ldg(F.rho + j);
+    const float Vj = __ldg(F.area + j) / rtj, rhoj = rtj * P.rho0;
+    const Geo e = geo(xi.x, xi.y, xj.x, xj.y, P.inv_h);
+    const float gw = kGW(e.q, P.c_g);
+    const float gx = gw * e.ex, gy = gw * e.ey;
+    const float rx = Li.x * gx + Li.y * gy, ry = Li.z * gx + Li.w * gy;
+    const float s = (rhoj - rhoi) * Vj * 2.0f;
+    fx += s * rx;
+    fy += s * ry;
+  }
+  float wx = 0.f, wy = 0.f;
+  if (W.n > 0) {
+    const sph_grid g = *gp;
+    int cx, cy;
+    cell_of(F.keys[i], g, &cx, &cy);
+    const float thr = sq_threshold(P.h);
+    for_each_wall(W, g, P.search_radius, cx, cy, xi.x, xi.y, thr, [&](int b, float2 xb) {
+      const Geo e = geo(xi.x, xi.y, xb.x, xb.y, P.inv_h);
+      const float gw = kGW(e.q, P.c_g);
+      const float gx = gw * e.ex, gy = gw * e.ey;
+      const float rx = Li.x * gx + Li.y * gy, ry = Li.z * gx + Li.w * gy;
+      const float s = (W.rho[b] * P.rho0 - rhoi) * W.vol[b] * 2.0f;
+      wx += s * rx;
+      wy += s * ry;
+    });
+  }
+  grad_rho[i] = make_float2(-fx - wx, -fy - wy);
+}
+
+// ---------------------------------------------------------------------------- pass 3 (deltaSPH)
+// D_i = h delta c0 sum_j [2 (rho_j - rho_i)/(|x_ji|^2 + eps) x_ji - (<grad rho>_i + <grad rho>_j)] . gradW_ij V_j
+__global__ void __launch_bounds__(128) k_dsph_diffusion(FluidView F, SphParams P, const float2* __restrict__ grad_rho,
+                                                        float* __restrict__ dpdt) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= F.n) return;
+  const float2 xi = F.x[i], gi = grad_rho[i];
+  const float rhoi = F.rho[i] * P.rho0;
+  float acc = 0.f;
+  const int k0 = F.offsets[i], k1 = F.offsets[i + 1];
+  for (int k = k0; k < k1; ++k) {
+    const int j = __ldg(F.cols + k);
+    const float2 xj = __ldg(F.x + j), gj = __ldg(grad_rho + j);
+    const float rtj = __ldg(F.rho + j);
+    const float Vj = __ldg(F.area + j) / rtj, rhoj = rtj * P.rho0;
+    const Geo e = geo(xi.x, xi.y, xj.x, xj.y, P.inv_h);
+    const float gw = kGW(e.q, P.c_g);
+    const float gx = gw * e.ex, gy = gw * e.ey;
+    const float rx = -e.dx, ry = -e.dy;
+    const float r2 = rx * rx + ry * ry + P.eps;
+    const float s = 2.0f * (rhoj - rhoi) / r2;
+    const float psx = s * rx - (gi.x + gj.x), psy = s * ry - (gi.y + gj.y);
+    acc += (psx * gx + psy * gy) * Vj;
+  }
+  dpdt[i] += P.diff_k * acc;
+}
+
+// ---------------------------------------------------------------------------- integration
+// semiImplicitEuler, src/simulationBase.py:647-652 with integrateValues :564-569:
+// v' = v + dt a, x' = x + dt (v + dt a), rho~' = rho~ + dt dpdt / rho0 (continuum density).
+__global__ void k_sie(int n, const float2* __restrict__ x, const float2* __restrict__ v,
+                      const float* __restrict__ rho, const float2* __restrict__ a, const float* __restrict__ dpdt,
+                      const float* __restrict__ dt_ptr, float rho0, int continuum, float2* __restrict__ xo,
+                      float2* __restrict__ vo, float* __restrict__ ro, int32_t* status) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float dt = *dt_ptr;
+  const float2 ai = a[i], vi = v[i], xi = x[i];
+  const float2 vn = make_float2(vi.x + dt * ai.x, vi.y + dt * ai.y);
+  const float2 xn = make_float2(xi.x + dt * (vi.x + dt * ai.x), xi.y + dt * (vi.y + dt * ai.y));
+  xo[i] = xn;
+  vo[i] = vn;
+  float rn = continuum ? rho[i] + dt * dpdt[i] / rho0 : rho[i];
+  ro[i] = rn;
+  if (!isfinite(xn.x) || !isfinite(xn.y) || !isfinite(vn.x) || !isfinite(vn.y) || !isfinite(rn))
+    flag(status, SPH_FLAG_NONFINITE);
+}
+
+// RK4 stage / combination, src/simulationBase.py:679-705: out = base + c * (k_u, k_a, k_d / rho0).
+__global__ void k_rk_axpy(int n, const float2* __restrict__ x0, const float2* __restrict__ v0,
+                          const float* __restrict__ r0, const float2* __restrict__ ku, const float2* __restrict__ ka,
+                          const float* __restrict__ kd, const float* __restrict__ dt_ptr, float c, float rho0,
+                          float2* __restrict__ xo, float2* __restrict__ vo, float* __restrict__ ro, int32_t* status) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float h = c * *dt_ptr;
+  const float2 u = ku[i], a = ka[i], x = x0[i], v = v0[i];
+  const float2 xn = make_float2(x.x + h * u.x, x.y + h * u.y);
+  const float2 vn = make_float2(v.x + h * a.x, v.y + h * a.y);
+  const float rn = r0[i] + h * kd[i] / rho0;
+  xo[i] = xn;
+  vo[i] = vn;
+  ro[i] = rn;
+  if (!isfinite(xn.x) || !isfinite(xn.y) || !isfinite(vn.x) || !isfinite(vn.y) || !isfinite(rn))
+    flag(status, SPH_FLAG_NONFINITE);
+}
+
+// s (+)= w * k for the RK4 sums; init = 1 overwrites.
+__global__ void k_rk_accum(int n, const float2* __restrict__ ku, const float2* __restrict__ ka,
+                           const float* __restrict__ kd, float w, int init, float2* __restrict__ su,
+                           float2* __restrict__ sa, float* __restrict__ sd) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float2 u = ku[i], a = ka[i];
+  float d = kd[i];
+  if (init) {
+    su[i] = make_float2(w * u.x, w * u.y);
+    sa[i] = make_float2(w * a.x, w * a.y);
+    sd[i] = w * d;
+  } else {
+    float2 s = su[i], t = sa[i];
+    su[i] = make_float2(s.x + w * u.x, s.y + w * u.y);
+    sa[i] = make_float2(t.x + w * a.x, t.y + w * a.y);
+    sd[i] += w * d;
+  }
+}
+
+// Permute per-particle arrays into a new order: out[s] = in[order[s]] (4-, 8- and 16-byte elements).
+template <typename T>
+__global__ void k_permute(const uint32_t* __restrict__ order, int n, const T* __restrict__ in, T* __restrict__ out) {
+  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s < n) out[s] = in[order[s]];
+}
+
+}  // namespace sph
+
+using namespace sph;
+
+
+extern "C" {
+
+sph_status_t sph_mdbc_wall_density(const sph_fluid_view* fluid, const sph_wall_view* walls, const sph_grid* grid,
+                                   const sph_params* params, void* stream) {
+  SPH_VIEW_CHECK(fluid);
+  SPH_VIEW_CHECK(walls);
+  SPH_REQUIRE(grid && params && params->support > 0.f, "mdbc: bad arguments");
+  if (walls->n == 0) return SPH_OK;
+  k_mdbc<<<grid_for(walls->n, 128), 128, 0, as_stream(stream)>>>(to_fluid(fluid), to_walls(walls), grid,
+                                                                 to_params(params));
+  SPH_CHECK_LAUNCH("mdbc_wall_density");
+  return SPH_OK;
+}
+
+sph_status_t sph_deltasph_forces(const sph_fluid_view* fluid, const sph_wall_view* walls, const sph_grid* grid,
+                                 const sph_params* params, float* dpdt, float* acc, float* L, float* grad_rho,
+                                 void* stream) {
+  SPH_VIEW_CHECK(fluid);
+  SPH_VIEW_CHECK(walls);
+  SPH_REQUIRE(grid && params && dpdt && acc && params->support > 0.f, "deltasph_forces: bad arguments");
+  SPH_REQUIRE(params->density_diffusion != 2 || (L && grad_rho), "deltasph_forces: deltaSPH diffusion needs L, grad_rho");
+  if (fluid->n == 0) return SPH_OK;
+  cudaStream_t st = as_stream(stream);
+  const FluidView F = to_fluid(fluid);
+  const WallView W = to_walls(walls);
+  const SphParams P = to_params(params);
+  const int nb = grid_for(fluid->n, 128);
+  k_dsph_pass1<<<nb, 128, 0, st>>>(F, W, grid, P, dpdt, reinterpret_cast<float2*>(acc), reinterpret_cast<float4*>(L));
+  if (P.diffusion == 2) {
+    k_dsph_gradrho<<<nb, 128, 0, st>>>(F, W, grid, P, reinterpret_cast<const float4*>(L),
+                                       reinterpret_cast<float2*>(grad_rho));
+    k_dsph_diffusion<<<nb, 128, 0, st>>>(F, P, reinterpret_cast<const float2*>(grad_rho), dpdt);
+  }
+  SPH_CHECK_LAUNCH("deltasph_forces");
+  return SPH_OK;
+}
+
+sph_status_t sph_integrate_semi_implicit_euler(int64_t n, const float* x, const float* v, const float* rho,
+                                               const float* acc, const float* dpdt, const float* dt,
+                                               float rest_density, int32_t continuum_density, float* x_out,
+                                               float* v_out, float* rho_out, int32_t* status, void* stream) {
+  SPH_REQUIRE(n >= 0 && n < (1LL << 31) && x && v && rho && acc && dt && x_out && v_out && rho_out,
+              "integrate_semi_implicit_euler: bad arguments");
+  SPH_REQUIRE(!continuum_density || dpdt, "integrate_semi_implicit_euler: continuum density needs dpdt");
+  if (n == 0) return SPH_OK;
+  k_sie<<<grid_for(n, 256), 256, 0, as_stream(stream)>>>(
+      (int)n, reinterpret_cast<const float2*>(x), reinterpret_cast<const float2*>(v), rho,
+      reinterpret_cast<const float2*>(acc), dpdt, dt, rest_density, continuum_density, reinterpret_cast<float2*>(x_out),
+      reinterpret_cast<float2*>(v_out), rho_out, status);
+  SPH_CHECK_LAUNCH("integrate_semi_implicit_euler");
+  return SPH_OK;
+}
+
+sph_status_t sph_rk_axpy(int64_t n, const float* x0, const float* v0, const float* rho0_field, const float* ku,
+                         const float* ka, const float* kd, const float* dt, float c, float rest_density, float* x_out,
+                         float* v_out, float* rho_out, int32_t* status, void* stream) {
+  SPH_REQUIRE(n >= 0 && n < (1LL << 31) && x0 && v0 && rho0_field && ku && ka && kd && dt && x_out && v_out && rho_out,
+              "rk_axpy: bad arguments");
+  if (n == 0) return SPH_OK;
+  k_rk_axpy<<<grid_for(n, 256), 256, 0, as_stream(stream)>>>(
+      (int)n, reinterpret_cast<const float2*>(x0), reinterpret_cast<const float2*>(v0), rho0_field,
+      reinterpret_cast<const float2*>(ku), reinterpret_cast<const float2*>(ka), kd, dt, c, rest_density,
+      reinterpret_cast<float2*>(x_out), reinterpret_cast<float2*>(v_out), rho_out, status);
+  SPH_CHECK_LAUNCH("rk_axpy");
+  return SPH_OK;
+}
+
+sph_status_t sph_rk_accumulate(int64_t n, const float* ku, const float* ka, const float* kd, float w, int32_t init,
+                               float* su, float* sa, float* sd, void* stream) {
+  SPH_REQUIRE(n >= 0 && n < (1LL << 31) && ku && ka && kd && su && sa && sd, "rk_accumulate: bad arguments");
+  if (n == 0) return SPH_OK;
+  k_rk_accum<<<grid_for(n, 256), 256, 0, as_stream(stream)>>>(
+      (int)n, reinterpret_cast<const float2*>(ku), reinterpret_cast<const float2*>(ka), kd, w, init,
+      reinterpret_cast<float2*>(su), reinterpret_cast<float2*>(sa), sd);
+  SPH_CHECK_LAUNCH("rk_accumulate");
+  return SPH_OK;
+}
+
+sph_status_t sph_permute(const uint32_t* order, int64_t n, int32_t elem_bytes, const void* in, void* out, void* stream) {
+  SPH_REQUIRE(n >= 0 && n < (1LL << 31) && order && in && out, "permute: bad arguments");
+  if (n == 0) return SPH_OK;
+  cudaStream_t st = as_stream(stream);
+  const int nb = grid_for(n, 256);
+  switch (elem_bytes) {
+    case 4:
+      k_permute<uint32_t><<<nb, 256, 0, st>>>(order, (int)n, static_cast<const uint32_t*>(in), static_cast<uint32_t*>(out));
+      break;
+    case 8:
+      k_permute<uint2><<<nb, 256, 0, st>>>(order, (int)n, static_cast<const uint2*>(in), static_cast<uint2*>(out));
+      break;
+    case 16:
+      k_permute<uint4><<<nb, 256, 0, st>>>(order, (int)n, static_cast<const uint4*>(in), static_cast<uint4*>(out));
+      break;
+    default:
+      set_error_text("permute: elem_bytes must be 4, 8 or 16");
+      return SPH_ERR_INVALID_ARGUMENT;
+  }
+  SPH_CHECK_LAUNCH("permute");
+  return SPH_OK;
+}
+
+}  // extern "C"

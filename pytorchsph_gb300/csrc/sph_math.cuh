@@ -1,0 +1,269 @@
+// Device math of the SPH summations: Wendland C2 / spiky kernels (src/kernels.py:20-33),
+// pair geometry (src/modules/neighborSearch.py:218-223), the reference's closed-form 2x2
+// pseudo-inverse (src/util.py:386-433) and a 3x3 pseudo-inverse for mDBC.
+#pragma once
+
+#include "sph_common.cuh"
+
+namespace sph {
+
+// Parameters shared by every summation kernel (by value in the launch).
+struct SphParams {
+  float h, inv_h;
+  float c_w;        // 7 / (pi h^2)           Wendland W
+  float c_g;        // 7 / (pi h^3)           Wendland gradient (times 20 q (1-q)^3)
+  float c_s;        // 30 / (pi h^3)          spiky gradient
+  float eps;        // 0.1 h^2
+  float rho0, c0, gamma;
+  float tait_k;     // rho0 c0^2 / gamma
+  float visc_k;     // h alpha c0
+  float diff_k;     // h delta c0
+  float kinematic;
+  float gx, gy;     // constant gravity
+  int point_source; // gravity = -g (x - c)  (potential field)
+  float point_mag, point_cx, point_cy;
+  int diffusion;    // 0 none, 1 MOG, 2 deltaSPH
+  int boundary_diffusion;
+  int search_radius;
+  int cell_capacity;
+};
+
+// Wall particles, sorted by their cell in the fluid grid; quantities per sorted wall.
+struct WallView {
+  const float2* x;         // wall positions
+  const float2* xg;        // ghost positions
+  const float* area;       // boundaryVolume (pi r^2)
+  const int32_t* cell_start;  // wall cell table in the fluid grid (cells+2)
+  int n;
+  float* rho;              // relative wall density
+  float* vol;              // A_b / rho_b
+  float* p;                // wall pressure
+};
+
+__device__ __forceinline__ float kW(float q, float c_w) {
+  float a = 1.0f - q;
+  float a2 = a * a;
+  return a2 * a2 * (1.0f + 4.0f * q) * c_w;
+}
+
+// gradW = e * kGW(q): Wendland gradient magnitude factor -C/h^3 * 20 q (1-q)^3.
+__device__ __forceinline__ float kGW(float q, float c_g) {
+  float a = 1.0f - q;
+  return -c_g * 20.0f * q * a * a * a;
+}
+
+// spikyGrad = e * kGS(q): -30/(pi h^3) (1-q)^2.
+__device__ __forceinline__ float kGS(float q, float c_s) {
+  float a = 1.0f - q;
+  return -c_s * a * a;
+}
+
+struct Geo {
+  float dx, dy;   // x_row - x_col
+  float r, q;
+  float ex, ey;   // unit vector, 0 when r < 1e-7
+};
+
+__device__ __forceinline__ Geo geo(float xi, float yi, float xj, float yj, float inv_h) {
+  Geo g;
+  g.dx = xi - xj;
+  g.dy = yi - yj;
+  g.r = sqrtf(g.dx * g.dx + g.dy * g.dy);
+  if (g.r >= 1e-7f) {
+    float ir = 1.0f / g.r;
+    g.ex = g.dx * ir;
+    g.ey = g.dy * ir;
+  } else {
+    g.ex = 0.f;
+    g.ey = 0.f;
+  }
+  g.q = g.r * inv_h;
+  return g;
+}
+
+__device__ __forceinline__ float tait(float rho_rel, const SphParams& P) {
+  float r7;
+  if (P.gamma == 7.0f) {
+    float r2 = rho_rel * rho_rel;
+    float r4 = r2 * r2;
+    r7 = r4 * r2 * rho_rel;
+  } else {
+    r7 = powf(rho_rel, P.gamma);
+  }
+  return P.tait_k * (r7 - 1.0f);
+}
+
+// pinv2x2, src/util.py:386-433: closed-form SVD pseudo-inverse, singular values <= 1e-5
+// dropped.  M = [[a, b], [c, d]]; returns [[o00, o01], [o10, o11]] in a float4 (row major).
+__device__ __forceinline__ float4 pinv2x2(float a, float b, float c, float d) {
+  float theta = 0.5f * atan2f(2 * a * c + 2 * b * d, a * a + b * b - c * c - d * d);
+  float ct = cosf(theta), st = sinf(theta);
+  float S1 = a * a + b * b + c * c + d * d;
+  float t = a * a + b * b - c * c - d * d;
+  float u = a * c + b * d;
+  float S2 = sqrtf(t * t + 4 * u * u);
+  float o1 = sqrtf((S1 + S2) * 0.5f);
+  float o2 = sqrtf((S1 - S2) * 0.5f);
+  float phi = 0.5f * atan2f(2 * a * b + 2 * c * d, a * a - b * b + c * c - d * d);
+  float cp = cosf(phi), sp = sinf(phi);
+  float v1 = (a * ct + c * st) * cp + (b * ct + d * st) * sp;
+  float v2 = (a * st - c * ct) * sp + (-b * st + d * ct) * cp;
+  float s11 = (v1 > 0.f) ? 1.f : ((v1 < 0.f) ? -1.f : 0.f);
+  float s22 = (v2 > 0.f) ? 1.f : ((v2 < 0.f) ? -1.f : 0.f);
+  // V = [[cp s11, -sp s22], [sp s11, cp s22]]; U = [[ct, -st], [st, ct]]
+  float i1 = fabsf(o1) > 1e-5f ? 1.0f / o1 : 0.f;
+  float i2 = fabsf(o2) > 1e-5f ? 1.0f / o2 : 0.f;
+  // V S^-1 = [[cp s11 i1, -sp s22 i2], [sp s11 i1, cp s22 i2]]; times U^T = [[ct, st], [-st, ct]]
+  float m00 = cp * s11 * i1, m01 = -sp * s22 * i2, m10 = sp * s11 * i1, m11 = cp * s22 * i2;
+  return make_float4(m00 * ct - m01 * st, m00 * st + m01 * ct, m10 * ct - m11 * st, m10 * st + m11 * ct);
+}
+
+// x = pinv(A) b for a 3x3 A in double (torch.linalg.pinv semantics: singular values below
+// 3 * FLT_EPSILON * sigma_max are dropped).  Eigen-decomposition of A^T A by cyclic Jacobi
+// rotations (at most 16 sweeps), then pinv(A) b = sum_k v_k ((A v_k) . b) / sigma_k^2.
+__device__ inline void pinv3_solve(const double A[3][3], const double b[3], double x[3]) {
+  double S[3][3];
+  for (int r = 0; r < 3; ++r)
+    for (int c = 0; c < 3; ++c) S[r][c] = A[0][r] * A[0][c] + A[1][r] * A[1][c] + A[2][r] * A[2][c];
+  double V[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+  for (int sweep = 0; sweep < 16; ++sweep) {
+    double off = fabs(S[0][1]) + fabs(S[0][2]) + fabs(S[1][2]);
+    double diag = fabs(S[0][0]) + fabs(S[1][1]) + fabs(S[2][2]);
+    if (off <= 1e-300 || off <= 1e-17 * diag) break;
+    for (int p = 0; p < 2; ++p)
+      for (int q = p + 1; q < 3; ++q) {
+        double apq = S[p][q];
+        if (fabs(apq) <= 1e-300) continue;
+        double tau = (S[q][q] - S[p][p]) / (2.0 * apq);
+        double t = (tau >= 0 ? 1.0 : -1.0) / (fabs(tau) + sqrt(1.0 + tau * tau));
+        double c = 1.0 / sqrt(1.0 + t * t), s = t * c;
+        for (int k = 0; k < 3; ++k) {  // S = J^T S J
+          double skp = S[k][p], skq = S[k][q];
+          S[k][p] = c * skp - s * skq;
+          S[k][q] = s * skp + c * skq;
+        }
+        for (int k = 0; k < 3; ++k) {
+          double spk = S[p][k], sqk = S[q][k];
+          S[p][k] = c * spk - s * sqk;
+          S[q][k] = s * spk + c * sqk;
+        }
+        for (int k = 0; k < 3; ++k) {
+          double vkp = V[k][p], vkq = V[k][q];
+          V[k][p] = c * vkp - s * vkq;
+          V[k][q] = s * vkp + c * vkq;
+        }
+      }
+  }
+  double lmax = fmax(fmax(S[0][0], S[1][1]), S[2][2]);
+  double smax = sqrt(fmax(lmax, 0.0));
+  double tol = 3.0 * 1.1920928955078125e-07 * smax;
+  x[0] = x[1] = x[2] = 0.0;
+  for (int k = 0; k < 3; ++k) {
+    double sig = sqrt(fmax(S[k][k], 0.0));
+    if (!(sig > tol)) continue;
+    double av[3];
+    for (int r = 0; r < 3; ++r) av[r] = A[r][0] * V[0][k] + A[r][1] * V[1][k] + A[r][2] * V[2][k];
+    double coef = (av[0] * b[0] + av[1] * b[1] + av[2] * b[2]) / (sig * sig);
+    for (int r = 0; r < 3; ++r) x[r] += V[r][k] * coef;
+  }
+}
+
+// Iterate the wall particles whose cell is within +-r of fluid cell (cx, cy) and that pass
+// the wall-side predicate sqrtf(fmaf(dx,dx,dy*dy)) < h_b with dx = x_b - x_f: exactly the
+// wall->fluid pairs of searchExisting (src/modules/neighborSearch.py:231-252).
+template <typename F>
+__device__ __forceinline__ void for_each_wall(const WallView& W, const sph_grid& g, int r, int cx, int cy, float xf,
+                                              float yf, float thr_b, F&& f) {
+  const int x0 = max(cx - r, 0), x1 = min(cx + r, g.cells_x - 1);
+  if (x0 > x1) return;
+  const int y0 = max(cy - r, 0), y1 = min(cy + r, g.cells_y - 1);
+  for (int yy = y0; yy <= y1; ++yy) {
+    const int row = yy * g.cells_x;
+    const int b0 = __ldg(W.cell_start + row + x0), b1 = __ldg(W.cell_start + row + x1 + 1);
+    for (int b = b0; b < b1; ++b) {
+      const float2 xb = __ldg(W.x + b);
+      if (dist2_ref(xb.x, xb.y, xf, yf) <= thr_b) f(b, xb);
+    }
+  }
+}
+
+struct FluidView {
+  const float2* x;
+  const float2* v;
+  const float* rho;
+  const float* area;
+  const uint32_t* keys;
+  const int32_t* offsets;
+  const int32_t* cols;
+  const int32_t* cell_start;
+  int n;
+};
+
+__device__ __forceinline__ void cell_of(uint32_t key, const sph_grid& g, int* cx, int* cy) {
+  *cx = (int)(key % (uint32_t)g.cells_x);
+  *cy = (int)(key / (uint32_t)g.cells_x);
+}
+
+}  // namespace sph
+
+// Host-side conversions of the C-ABI views into the kernels' views.
+namespace sph {
+static inline SphParams to_params(const sph_params* p) {
+  SphParams P;
+  P.h = p->support;
+  P.inv_h = 1.0f / p->support;
+  const double h = p->support;
+  P.c_w = (float)(7.0 / 3.14159265358979323846 / (h * h));
+  P.c_g = (float)(7.0 / 3.14159265358979323846 / (h * h * h));
+  P.c_s = (float)(30.0 / 3.14159265358979323846 / (h * h * h));
+  P.eps = (float)(h * h * 0.1);
+  P.rho0 = p->rest_density;
+  P.c0 = p->c0;
+  P.gamma = p->gamma;
+  P.tait_k = (float)((double)p->rest_density * p->c0 * p->c0 / p->gamma);
+  P.visc_k = (float)(h * p->alpha * p->c0);
+  P.diff_k = (float)(h * p->delta * p->c0);
+  P.kinematic = p->kinematic;
+  P.gx = p->gravity[0];
+  P.gy = p->gravity[1];
+  P.point_source = p->point_source;
+  P.point_mag = p->point_magnitude;
+  P.point_cx = p->point_center[0];
+  P.point_cy = p->point_center[1];
+  P.diffusion = p->density_diffusion;
+  P.boundary_diffusion = p->boundary_diffusion;
+  P.search_radius = p->search_radius;
+  P.cell_capacity = p->cell_capacity;
+  return P;
+}
+
+static inline FluidView to_fluid(const sph_fluid_view* f) {
+  FluidView F;
+  F.x = reinterpret_cast<const float2*>(f->x);
+  F.v = reinterpret_cast<const float2*>(f->v);
+  F.rho = f->rho;
+  F.area = f->area;
+  F.keys = f->keys;
+  F.offsets = f->offsets;
+  F.cols = f->cols;
+  F.cell_start = f->cell_start;
+  F.n = (int)f->n;
+  return F;
+}
+
+static inline WallView to_walls(const sph_wall_view* w) {
+  WallView W;
+  W.x = reinterpret_cast<const float2*>(w->x);
+  W.xg = reinterpret_cast<const float2*>(w->ghost);
+  W.area = w->area;
+  W.cell_start = w->cell_start;
+  W.n = (int)w->n;
+  W.rho = w->rho;
+  W.vol = w->volume;
+  W.p = w->pressure;
+  return W;
+}
+
+}  // namespace sph
+
+#define SPH_VIEW_CHECK(f) SPH_REQUIRE((f) && (f)->n >= 0 && (f)->n < (1LL << 31), "bad particle view")
