@@ -170,6 +170,11 @@ size_t sph_counting_sort_scratch_bytes(int64_t n, int32_t cell_capacity);
 sph_status_t sph_counting_sort(const uint32_t* keys, int64_t n, int32_t cell_capacity, int32_t* cell_count,
                                int32_t* cell_start, uint32_t* order, uint32_t* sorted_keys, int32_t* status,
                                void* scratch, size_t scratch_bytes, void* stream);
+/* As sph_counting_sort, ordering each cell by (tie[i], i) instead of i: with a particle id as
+ * tie key the sorted order no longer depends on the order the particles arrived in. */
+sph_status_t sph_counting_sort_tie(const uint32_t* keys, int64_t n, int32_t cell_capacity, int32_t* cell_count,
+                                   int32_t* cell_start, const uint32_t* tie, uint32_t* order, uint32_t* sorted_keys,
+                                   int32_t* status, void* scratch, size_t scratch_bytes, void* stream);
 /* cell_start[c] = first sorted index whose key >= c, for c = 0..cell_capacity+1 (the cell
  * begin table after sph_radix_sort_pairs). */
 sph_status_t sph_cell_starts(const uint32_t* sorted_keys, int64_t n, int32_t cell_capacity,
@@ -274,6 +279,37 @@ sph_status_t sph_rk_accumulate(int64_t n, const float* ku, const float* ka, cons
                                float* su, float* sa, float* sd, void* stream);
 /* out[s] = in[order[s]] for 4-, 8- or 16-byte elements (re-sorting per-particle state). */
 sph_status_t sph_permute(const uint32_t* order, int64_t n, int32_t elem_bytes, const void* in, void* out, void* stream);
+
+/* ---------------------------------------------------------------- batch of independent scenes */
+/* Many scenes stepped together: their particles are concatenated in one array with a
+ * per-particle scene index `sid`; scene s owns cells [cell_offset_s, cell_offset_s +
+ * num_cells_s) of the shared cell tables, so (scene, cell) keys sort every scene into its
+ * own contiguous range and scenes never interact.  The scene table is an array of opaque
+ * records of sph_scene_bytes() bytes each, filled with sph_scene_encode and copied to the
+ * device. */
+size_t sph_scene_bytes(void);
+/* Encode one scene record on the host: parameters, its grid (host copy of the sph_grid
+ * from sph_grid_build), its cell-table offset and its time step. */
+sph_status_t sph_scene_encode(const sph_params* params, const sph_grid* grid_host, int32_t cell_offset, float dt,
+                              void* out_host);
+/* (scene, cell) keys + per-cell histogram for sph_counting_sort; cell_capacity = total cells. */
+sph_status_t sph_batch_cell_keys(const float* pos, int64_t n, const int32_t* sid, const void* scenes,
+                                 int32_t cell_capacity, uint32_t* keys, int32_t* cell_count, int32_t* status,
+                                 void* stream);
+/* Two-pass CSR over a sorted batch (each particle searches its own scene's cells). */
+sph_status_t sph_batch_nl_count(const float* xy, const float* sorted_support, int64_t n, const uint32_t* sorted_keys,
+                                const int32_t* cell_start, const void* scenes, const int32_t* sid, int32_t* counts,
+                                void* stream);
+sph_status_t sph_batch_nl_fill(const float* xy, const float* sorted_support, int64_t n, const uint32_t* sorted_keys,
+                               const int32_t* cell_start, const void* scenes, const int32_t* sid, const int32_t* offsets,
+                               int64_t pair_capacity, int32_t* cols, int32_t* status, void* stream);
+/* One semi-implicit-Euler deltaSPH step of every scene of the batch: mDBC wall densities,
+ * the right-hand side (as sph_deltasph_forces, each particle with its scene's parameters)
+ * and the update with each scene's own dt, written to x_out / v_out / rho_out. */
+sph_status_t sph_batch_deltasph_step(const sph_fluid_view* fluid, const sph_wall_view* walls, const void* scenes,
+                                     const int32_t* sid, const int32_t* wall_sid, float* dpdt, float* acc, float* L,
+                                     float* grad_rho, int32_t any_renormalized, float* x_out, float* v_out,
+                                     float* rho_out, int32_t* status, void* stream);
 
 /* ---------------------------------------------------------------- DFSPH (a20-a25) */
 

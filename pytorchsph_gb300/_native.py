@@ -61,6 +61,16 @@ SIGNATURES = {
                                        _P, _P, _P]),
 }
 
+SIGNATURES.update({  # batch of scenes
+    "sph_counting_sort_tie": (_I32, [_P, _I64, _I32, _P, _P, _P, _P, _P, _P, _P, _SZ, _P]),
+    "sph_scene_bytes": (_SZ, []),
+    "sph_scene_encode": (_I32, [_P, _P, _I32, _F32, _P]),
+    "sph_batch_cell_keys": (_I32, [_P, _I64, _P, _P, _I32, _P, _P, _P, _P]),
+    "sph_batch_nl_count": (_I32, [_P, _P, _I64, _P, _P, _P, _P, _P, _P]),
+    "sph_batch_nl_fill": (_I32, [_P, _P, _I64, _P, _P, _P, _P, _P, _I64, _P, _P, _P]),
+    "sph_batch_deltasph_step": (_I32, [_P] * 9 + [_I32] + [_P] * 5),
+})
+
 SIGNATURES.update({  # simulation kernels
     "sph_mdbc_wall_density": (_I32, [_P] * 5),
     "sph_deltasph_forces": (_I32, [_P] * 9),

@@ -10,7 +10,7 @@
 //     digits; its cell table comes from sph_cell_starts (binary search per cell).
 #include <cstdio>
 
-#include "sph_common.cuh"
+#include "sph_math.cuh"
 
 namespace sph {
 
@@ -139,6 +139,31 @@ __global__ void k_cell_keys(const float2* __restrict__ pos, int64_t n, const sph
   if (cell_count) atomicAdd(cell_count + key, 1);
 }
 
+// Batch of scenes: key = coff_s + ix + cells_x_s * iy with scene s's own grid; particles
+// outside their scene's grid get the sentinel cell_capacity (the batch's total cell count).
+__global__ void k_batch_cell_keys(const float2* __restrict__ pos, int64_t n, const int32_t* __restrict__ sid,
+                                  const SceneDev* __restrict__ scenes, int32_t cell_capacity,
+                                  uint32_t* __restrict__ keys, int32_t* __restrict__ cell_count, int32_t* status) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const SceneDev& S = scenes[sid[i]];
+  const sph_grid& g = S.g;
+  float2 p = pos[i];
+  uint32_t key = (uint32_t)cell_capacity;
+  if (!isfinite(p.x) || !isfinite(p.y)) {
+    flag(status, SPH_FLAG_NONFINITE);
+  } else {
+    int ix = cell_coord(p.x, g.qmin[0], g.hmax);
+    int iy = cell_coord(p.y, g.qmin[1], g.hmax);
+    if (ix >= 0 && iy >= 0 && ix < g.cells_x && iy < g.cells_y && S.coff + g.num_cells <= cell_capacity)
+      key = (uint32_t)(S.coff + ix + g.cells_x * iy);
+    else
+      flag(status, SPH_FLAG_OUT_OF_GRID);
+  }
+  keys[i] = key;
+  atomicAdd(cell_count + key, 1);
+}
+
 // Counting-sort scatter: slot = cell_start[key] + (remaining count of the cell) - 1.
 // Decrementing the histogram leaves it all zero for the next sort.
 __global__ void k_count_scatter(const uint32_t* __restrict__ keys, int64_t n, const int32_t* __restrict__ cell_start,
@@ -153,12 +178,18 @@ __global__ void k_count_scatter(const uint32_t* __restrict__ keys, int64_t n, co
 constexpr int kSmallCell = 48;    // cells up to this size are sorted by one thread in registers
 constexpr int kBlockSortMax = 2048;  // larger cells: one block, bitonic sort in shared memory
 
-// Per-cell fix-up: restore ascending original index inside every cell, write the sorted
+// Sort key inside a cell: the particle's index, or (tie[index], index) when a tie key is
+// given (e.g. a particle id, which makes the order independent of the previous order).
+__device__ __forceinline__ uint64_t cell_rank(uint32_t x, const uint32_t* __restrict__ tie) {
+  return tie ? (((uint64_t)__ldg(tie + x)) << 32) | x : (uint64_t)x;
+}
+
+// Per-cell fix-up: restore ascending (tie, index) order inside every cell, write the sorted
 // keys.  Cells larger than kSmallCell are queued for k_cell_fix_large.
 __global__ void __launch_bounds__(128) k_cell_fix(const int32_t* __restrict__ cell_start, int32_t ncell_slots,
-                                                  const uint32_t* __restrict__ tmp, uint32_t* __restrict__ order,
-                                                  uint32_t* __restrict__ sorted_keys, int32_t* __restrict__ big_list,
-                                                  int32_t* __restrict__ big_count) {
+                                                  const uint32_t* __restrict__ tmp, const uint32_t* __restrict__ tie,
+                                                  uint32_t* __restrict__ order, uint32_t* __restrict__ sorted_keys,
+                                                  int32_t* __restrict__ big_list, int32_t* __restrict__ big_count) {
   int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= ncell_slots) return;
   const int b = cell_start[c], e = cell_start[c + 1];
@@ -166,10 +197,10 @@ __global__ void __launch_bounds__(128) k_cell_fix(const int32_t* __restrict__ ce
   if (k == 0) return;
   for (int t = b; t < e; ++t) sorted_keys[t] = (uint32_t)c;
   if (k <= kSmallCell) {
-    uint32_t v[kSmallCell];
+    uint64_t v[kSmallCell];
 #pragma unroll 1
     for (int t = 0; t < k; ++t) {
-      uint32_t x = tmp[b + t];
+      uint64_t x = cell_rank(tmp[b + t], tie);
       int u = t;
       while (u > 0 && v[u - 1] > x) {
         v[u] = v[u - 1];
@@ -178,22 +209,23 @@ __global__ void __launch_bounds__(128) k_cell_fix(const int32_t* __restrict__ ce
       v[u] = x;
     }
 #pragma unroll 1
-    for (int t = 0; t < k; ++t) order[b + t] = v[t];
+    for (int t = 0; t < k; ++t) order[b + t] = (uint32_t)(v[t] & 0xffffffffu);
   } else {
     int q = atomicAdd(big_count, 1);
     big_list[q] = c;
   }
 }
 
-// One block per large cell: bitonic sort of up to kBlockSortMax indices in shared memory.
+// One block per large cell: bitonic sort of up to kBlockSortMax entries in shared memory.
 // Bigger cells keep the atomic scatter order (their pair set is unchanged; only the
 // order inside that cell is not reproducible) and flag SPH_FLAG_CELL_ORDER.
 __global__ void __launch_bounds__(512) k_cell_fix_large(const int32_t* __restrict__ cell_start,
                                                         const uint32_t* __restrict__ tmp,
+                                                        const uint32_t* __restrict__ tie,
                                                         uint32_t* __restrict__ order,
                                                         const int32_t* __restrict__ big_list,
                                                         const int32_t* __restrict__ big_count, int32_t* status) {
-  __shared__ uint32_t s[kBlockSortMax];
+  __shared__ uint64_t s[kBlockSortMax];
   const int nbig = *big_count;
   for (int q = blockIdx.x; q < nbig; q += gridDim.x) {
     const int c = big_list[q];
@@ -206,7 +238,7 @@ __global__ void __launch_bounds__(512) k_cell_fix_large(const int32_t* __restric
     }
     int p2 = 1;
     while (p2 < k) p2 <<= 1;
-    for (int t = threadIdx.x; t < p2; t += blockDim.x) s[t] = t < k ? tmp[b + t] : 0xffffffffu;
+    for (int t = threadIdx.x; t < p2; t += blockDim.x) s[t] = t < k ? cell_rank(tmp[b + t], tie) : ~0ull;
     __syncthreads();
     for (int size = 2; size <= p2; size <<= 1) {
       for (int stride = size >> 1; stride > 0; stride >>= 1) {
@@ -214,7 +246,7 @@ __global__ void __launch_bounds__(512) k_cell_fix_large(const int32_t* __restric
           int u = t ^ stride;
           if (u > t) {
             bool up = (t & size) == 0;
-            uint32_t a = s[t], bb = s[u];
+            uint64_t a = s[t], bb = s[u];
             if ((a > bb) == up) {
               s[t] = bb;
               s[u] = a;
@@ -224,7 +256,7 @@ __global__ void __launch_bounds__(512) k_cell_fix_large(const int32_t* __restric
         __syncthreads();
       }
     }
-    for (int t = threadIdx.x; t < k; t += blockDim.x) order[b + t] = s[t];
+    for (int t = threadIdx.x; t < k; t += blockDim.x) order[b + t] = (uint32_t)(s[t] & 0xffffffffu);
     __syncthreads();
   }
 }
@@ -370,6 +402,19 @@ sph_status_t sph_cell_keys(const float* pos, int64_t n, const sph_grid* grid, in
 
 int32_t sph_key_bits(int32_t cell_capacity) { return key_bits_for(cell_capacity); }
 
+sph_status_t sph_batch_cell_keys(const float* pos, int64_t n, const int32_t* sid, const void* scenes,
+                                 int32_t cell_capacity, uint32_t* keys, int32_t* cell_count, int32_t* status,
+                                 void* stream) {
+  SPH_REQUIRE(n >= 0 && pos && sid && scenes && keys && cell_count && cell_capacity > 0,
+              "batch_cell_keys: bad arguments");
+  if (n == 0) return SPH_OK;
+  k_batch_cell_keys<<<grid_for(n, 256), 256, 0, as_stream(stream)>>>(reinterpret_cast<const float2*>(pos), n, sid,
+                                                                     static_cast<const SceneDev*>(scenes),
+                                                                     cell_capacity, keys, cell_count, status);
+  SPH_CHECK_LAUNCH("batch_cell_keys");
+  return SPH_OK;
+}
+
 size_t sph_counting_sort_scratch_bytes(int64_t n, int32_t cell_capacity) {
   size_t b = (size_t)(n < 1 ? 1 : n) * sizeof(uint32_t) + 256;          // scatter target
   b += ((size_t)cell_capacity + 1) * sizeof(int32_t) + 256;              // large-cell list
@@ -381,6 +426,13 @@ size_t sph_counting_sort_scratch_bytes(int64_t n, int32_t cell_capacity) {
 sph_status_t sph_counting_sort(const uint32_t* keys, int64_t n, int32_t cell_capacity, int32_t* cell_count,
                                int32_t* cell_start, uint32_t* order, uint32_t* sorted_keys, int32_t* status,
                                void* scratch, size_t scratch_bytes, void* stream) {
+  return sph_counting_sort_tie(keys, n, cell_capacity, cell_count, cell_start, nullptr, order, sorted_keys, status,
+                               scratch, scratch_bytes, stream);
+}
+
+sph_status_t sph_counting_sort_tie(const uint32_t* keys, int64_t n, int32_t cell_capacity, int32_t* cell_count,
+                                   int32_t* cell_start, const uint32_t* tie, uint32_t* order, uint32_t* sorted_keys,
+                                   int32_t* status, void* scratch, size_t scratch_bytes, void* stream) {
   SPH_REQUIRE(n >= 0 && n < ((int64_t)1 << 31) && keys && cell_count && cell_start && order && sorted_keys &&
                   cell_capacity > 0,
               "counting_sort: bad arguments");
@@ -406,9 +458,9 @@ sph_status_t sph_counting_sort(const uint32_t* keys, int64_t n, int32_t cell_cap
   if (n == 0) return SPH_OK;
   cudaMemsetAsync(big_count, 0, sizeof(int32_t), st);
   k_count_scatter<<<grid_for(n, 256), 256, 0, st>>>(keys, n, cell_start, cell_count, tmp);
-  k_cell_fix<<<grid_for(slots, 128), 128, 0, st>>>(cell_start, (int32_t)slots, tmp, order, sorted_keys, big_list,
-                                                   big_count);
-  k_cell_fix_large<<<kNumSMs, 512, 0, st>>>(cell_start, tmp, order, big_list, big_count, status);
+  k_cell_fix<<<grid_for(slots, 128), 128, 0, st>>>(cell_start, (int32_t)slots, tmp, tie, order, sorted_keys,
+                                                   big_list, big_count);
+  k_cell_fix_large<<<kNumSMs, 512, 0, st>>>(cell_start, tmp, tie, order, big_list, big_count, status);
   SPH_CHECK_LAUNCH("counting_sort");
   return SPH_OK;
 }

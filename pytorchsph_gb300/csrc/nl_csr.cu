@@ -8,7 +8,7 @@
 // The pair test is the reference's sqrtf(fmaf(dx,dx,dy*dy)) < h_i in its square-root-free
 // exact form v <= F_i (sq_threshold); the square root is taken only for accepted pairs
 // that need the distance (density).
-#include "sph_common.cuh"
+#include "sph_math.cuh"
 
 namespace sph {
 
@@ -165,11 +165,83 @@ __global__ void k_nl_to_coo(const float2* __restrict__ xy, int64_t n, const uint
   }
 }
 
+// ---------------------------------------------------------------------------- batch of scenes
+// Keys are global: scene s's cells occupy [coff_s, coff_s + num_cells_s) of the cell table.
+__global__ void __launch_bounds__(256) k_batch_nl_count(const float2* __restrict__ xy, const float* __restrict__ sh,
+                                                        int64_t n, const uint32_t* __restrict__ keys,
+                                                        const int32_t* __restrict__ cell_start,
+                                                        const SceneDev* __restrict__ scenes,
+                                                        const int32_t* __restrict__ sid, int32_t* __restrict__ counts) {
+  int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  const SceneDev& S = scenes[sid[s]];
+  const uint32_t key = keys[s] - (uint32_t)S.coff;
+  int cnt = 0;
+  if (keys[s] >= (uint32_t)S.coff && key < (uint32_t)S.g.num_cells) {
+    const float2 pi = xy[s];
+    const float thr = sq_threshold(sh[s]);
+    const int cx = (int)(key % (uint32_t)S.g.cells_x), cy = (int)(key / (uint32_t)S.g.cells_x);
+    scan_candidates(xy, cell_start + S.coff, S.g, S.P.search_radius, cx, cy, pi.x, pi.y, thr,
+                    [&](int, float) { ++cnt; });
+  }
+  counts[s] = cnt;
+}
+
+__global__ void __launch_bounds__(256) k_batch_nl_fill(const float2* __restrict__ xy, const float* __restrict__ sh,
+                                                       int64_t n, const uint32_t* __restrict__ keys,
+                                                       const int32_t* __restrict__ cell_start,
+                                                       const SceneDev* __restrict__ scenes,
+                                                       const int32_t* __restrict__ sid,
+                                                       const int32_t* __restrict__ offsets, int64_t pair_capacity,
+                                                       int32_t* __restrict__ cols, int32_t* status) {
+  int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  const SceneDev& S = scenes[sid[s]];
+  const uint32_t key = keys[s] - (uint32_t)S.coff;
+  if (!(keys[s] >= (uint32_t)S.coff && key < (uint32_t)S.g.num_cells)) return;
+  if ((int64_t)offsets[s + 1] > pair_capacity) {
+    flag(status, SPH_FLAG_PAIR_CAPACITY);
+    return;
+  }
+  const float2 pi = xy[s];
+  const float thr = sq_threshold(sh[s]);
+  const int cx = (int)(key % (uint32_t)S.g.cells_x), cy = (int)(key / (uint32_t)S.g.cells_x);
+  int32_t o = offsets[s];
+  scan_candidates(xy, cell_start + S.coff, S.g, S.P.search_radius, cx, cy, pi.x, pi.y, thr,
+                  [&](int j, float) { cols[o++] = j; });
+}
+
 }  // namespace sph
 
 using namespace sph;
 
 extern "C" {
+
+sph_status_t sph_batch_nl_count(const float* xy, const float* sorted_support, int64_t n, const uint32_t* sorted_keys,
+                                const int32_t* cell_start, const void* scenes, const int32_t* sid, int32_t* counts,
+                                void* stream) {
+  SPH_REQUIRE(n >= 0 && xy && sorted_support && sorted_keys && cell_start && scenes && sid && counts,
+              "batch_nl_count: bad arguments");
+  if (n == 0) return SPH_OK;
+  k_batch_nl_count<<<grid_for(n, 256), 256, 0, as_stream(stream)>>>(
+      reinterpret_cast<const float2*>(xy), sorted_support, n, sorted_keys, cell_start,
+      static_cast<const SceneDev*>(scenes), sid, counts);
+  SPH_CHECK_LAUNCH("batch_nl_count");
+  return SPH_OK;
+}
+
+sph_status_t sph_batch_nl_fill(const float* xy, const float* sorted_support, int64_t n, const uint32_t* sorted_keys,
+                               const int32_t* cell_start, const void* scenes, const int32_t* sid, const int32_t* offsets,
+                               int64_t pair_capacity, int32_t* cols, int32_t* status, void* stream) {
+  SPH_REQUIRE(n >= 0 && xy && sorted_support && sorted_keys && cell_start && scenes && sid && offsets && cols,
+              "batch_nl_fill: bad arguments");
+  if (n == 0) return SPH_OK;
+  k_batch_nl_fill<<<grid_for(n, 256), 256, 0, as_stream(stream)>>>(
+      reinterpret_cast<const float2*>(xy), sorted_support, n, sorted_keys, cell_start,
+      static_cast<const SceneDev*>(scenes), sid, offsets, pair_capacity, cols, status);
+  SPH_CHECK_LAUNCH("batch_nl_fill");
+  return SPH_OK;
+}
 
 sph_status_t sph_nl_count(const float* xy, const float* sorted_support, const float* sorted_area, int64_t n,
                           const uint32_t* sorted_keys, const int32_t* cell_start, const sph_grid* grid,

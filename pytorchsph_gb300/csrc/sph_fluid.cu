@@ -4,6 +4,11 @@
 // order, then walls, added to the fluid sum the way the reference adds its wall module's
 // result (`x += simulation.boundaryModule...`).
 //
+// Each kernel body takes its scene's grid, parameters and cell-table offset explicitly, so
+// the same code serves one scene (sph_* entry points) and a batch of independent scenes
+// concatenated in one particle array (sph_batch_* entry points, scene table + per-particle
+// scene index).
+//
 // Reference formulas (relative density rho~, absolute rho = rho~ rho0, V = A / rho~):
 //   continuity     src/modules/momentum.py:13-19 (+ wall solidBoundary.py:746-770)
 //   MOG diffusion  src/modules/densityDiffusion.py:56-63
@@ -15,23 +20,24 @@
 //   laminar visc.  src/modules/laminar.py:12-27 (index choices kept: r = x_j - x_i, mu_j = rho_i nu)
 //   gravity        src/modules/gravity.py:46-57
 //   mDBC density   src/modules/solidBoundary.py:561-617
+#include <cstring>
+
 #include "sph_math.cuh"
 
 namespace sph {
 
 // ---------------------------------------------------------------------------- mDBC
-// One thread per wall particle: Shepard and first-order MLS sums over the fluid particles
-// within h of its ghost (accumulated in double), the 3x3 pseudo-inverse solve, then the
-// wall density, volume and Tait pressure.
-__global__ void __launch_bounds__(128) k_mdbc(FluidView F, WallView W, const sph_grid* __restrict__ gp, SphParams P) {
-  int b = blockIdx.x * blockDim.x + threadIdx.x;
-  if (b >= W.n) return;
-  const sph_grid g = *gp;
+// Shepard and first-order MLS sums over the fluid particles within h of wall b's ghost
+// (accumulated in double), the 3x3 pseudo-inverse solve, then wall density, volume and
+// Tait pressure.
+__device__ __forceinline__ void mdbc_body(int b, const FluidView& F, const WallView& W, const sph_grid& g,
+                                          const SphParams& P, int coff) {
   const float2 xg = W.xg[b];
   const float thr = sq_threshold(P.h);
   double nom = 0, den = 0, gx = 0, gy = 0, vgx = 0, vgy = 0, px = 0, py = 0;
   double m00 = 0, m01 = 0, m10 = 0, m11 = 0;
   int cnt = 0;
+  const int32_t* cs = F.cell_start + coff;
   if (grid_ok(g, P.cell_capacity)) {
     float fcx = ceilf(__fdiv_rn(__fsub_rn(xg.x, g.qmin[0]), g.hmax));
     float fcy = ceilf(__fdiv_rn(__fsub_rn(xg.y, g.qmin[1]), g.hmax));
@@ -42,7 +48,7 @@ __global__ void __launch_bounds__(128) k_mdbc(FluidView F, WallView W, const sph
       if (x0 <= x1) {
         for (int yy = y0; yy <= y1; ++yy) {
           const int row = yy * g.cells_x;
-          const int j0 = F.cell_start[row + x0], j1 = F.cell_start[row + x1 + 1];
+          const int j0 = cs[row + x0], j1 = cs[row + x1 + 1];
           for (int j = j0; j < j1; ++j) {
             const float2 xj = F.x[j];
             if (!(dist2_ref(xg.x, xg.y, xj.x, xj.y) <= thr)) continue;
@@ -91,11 +97,9 @@ __global__ void __launch_bounds__(128) k_mdbc(FluidView F, WallView W, const sph
 // ---------------------------------------------------------------------------- pass 1
 // dpdt (continuity + MOG), acceleration (gravity, pressure, artificial and laminar
 // viscosity) and, for the deltaSPH scheme, the normalization matrix L.
-__global__ void __launch_bounds__(128) k_dsph_pass1(FluidView F, WallView W, const sph_grid* __restrict__ gp,
-                                                    SphParams P, float* __restrict__ dpdt, float2* __restrict__ acc,
-                                                    float4* __restrict__ Lout) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= F.n) return;
+__device__ __forceinline__ void pass1_body(int i, const FluidView& F, const WallView& W, const sph_grid& g,
+                                           const SphParams& P, int coff, float* __restrict__ dpdt,
+                                           float2* __restrict__ acc, float4* __restrict__ Lout) {
   const float2 xi = F.x[i], vi = F.v[i];
   const float rti = F.rho[i];
   const float rhoi = rti * P.rho0;
@@ -146,35 +150,37 @@ __global__ void __launch_bounds__(128) k_dsph_pass1(FluidView F, WallView W, con
   float dp_w = 0.f, pwx = 0.f, pwy = 0.f, vwx = 0.f, vwy = 0.f;
   float w00 = 0.f, w01 = 0.f, w10 = 0.f, w11 = 0.f;
   if (W.n > 0) {
-    const sph_grid g = *gp;
     int cx, cy;
-    cell_of(F.keys[i], g, &cx, &cy);
+    cell_of(F.keys[i] - (uint32_t)coff, g, &cx, &cy);
     const float thr = sq_threshold(P.h);
-    for_each_wall(W, g, P.search_radius, cx, cy, xi.x, xi.y, thr, [&](int b, float2 xb) {
-      const Geo e = geo(xi.x, xi.y, xb.x, xb.y, P.inv_h);   // fluid side: e = (x_f - x_b)/r
-      const float gw = kGW(e.q, P.c_g);
-      const float gx = gw * e.ex, gy = gw * e.ey;
-      const float Vb = W.vol[b], rhob = W.rho[b] * P.rho0, pb = W.p[b];
-      const float ux = -vi.x, uy = -vi.y;               // u_b - u_f, walls at rest
-      dp_w -= (ux * gx + uy * gy) * Vb * rhob;
-      const float pf = (pi + pb) * Vb;
-      pwx += pf * gx;
-      pwy += pf * gy;
-      const float rx = -e.dx, ry = -e.dy;               // x_b - x_f
-      if (P.boundary_diffusion) {
-        const float r2 = rx * rx + ry * ry + P.eps;
-        float pij = fminf(ux * rx + uy * ry, 0.f) / r2;
-        const float vf = pij * Vb * rhob / (rhoi + rhob);
-        vwx += vf * gx;
-        vwy += vf * gy;
-      }
-      if (want_L) {
-        w00 += Vb * rx * gx;
-        w01 += Vb * rx * gy;
-        w10 += Vb * ry * gx;
-        w11 += Vb * ry * gy;
-      }
-    });
+    for_each_wall(
+        W, g, P.search_radius, cx, cy, xi.x, xi.y, thr,
+        [&](int b, float2 xb) {
+          const Geo e = geo(xi.x, xi.y, xb.x, xb.y, P.inv_h);   // fluid side: e = (x_f - x_b)/r
+          const float gw = kGW(e.q, P.c_g);
+          const float gx = gw * e.ex, gy = gw * e.ey;
+          const float Vb = W.vol[b], rhob = W.rho[b] * P.rho0, pb = W.p[b];
+          const float ux = -vi.x, uy = -vi.y;               // u_b - u_f, walls at rest
+          dp_w -= (ux * gx + uy * gy) * Vb * rhob;
+          const float pf = (pi + pb) * Vb;
+          pwx += pf * gx;
+          pwy += pf * gy;
+          const float rx = -e.dx, ry = -e.dy;               // x_b - x_f
+          if (P.boundary_diffusion) {
+            const float r2 = rx * rx + ry * ry + P.eps;
+            float pij = fminf(ux * rx + uy * ry, 0.f) / r2;
+            const float vf = pij * Vb * rhob / (rhoi + rhob);
+            vwx += vf * gx;
+            vwy += vf * gy;
+          }
+          if (want_L) {
+            w00 += Vb * rx * gx;
+            w01 += Vb * rx * gy;
+            w10 += Vb * ry * gx;
+            w11 += Vb * ry * gy;
+          }
+        },
+        coff);
   }
   float d = dp_f + dp_w;
   if (P.diffusion == 1) d += P.diff_k * mog;
@@ -204,13 +210,10 @@ __global__ void __launch_bounds__(128) k_dsph_pass1(FluidView F, WallView W, con
   if (want_L) Lout[i] = make_float4(l00 + w00, l01 + w01, l10 + w10, l11 + w11);
 }
 
-// ---------------------------------------------------------------------------- pass 2 (deltaSPH)
 // <grad rho>_i = -sum_j 2 (rho_j - rho_i) V_j L_i^+ gradW_ij  (+ walls)
-__global__ void __launch_bounds__(128) k_dsph_gradrho(FluidView F, WallView W, const sph_grid* __restrict__ gp,
-                                                      SphParams P, const float4* __restrict__ L,
-                                                      float2* __restrict__ grad_rho) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= F.n) return;
+__device__ __forceinline__ void gradrho_body(int i, const FluidView& F, const WallView& W, const sph_grid& g,
+                                             const SphParams& P, int coff, const float4* __restrict__ L,
+                                             float2* __restrict__ grad_rho) {
   const float4 m = L[i];
   const float4 Li = pinv2x2(m.x, m.y, m.z, m.w);
   const float2 xi = F.x[i];
@@ -232,29 +235,28 @@ __global__ void __launch_bounds__(128) k_dsph_gradrho(FluidView F, WallView W, c
   }
   float wx = 0.f, wy = 0.f;
   if (W.n > 0) {
-    const sph_grid g = *gp;
     int cx, cy;
-    cell_of(F.keys[i], g, &cx, &cy);
+    cell_of(F.keys[i] - (uint32_t)coff, g, &cx, &cy);
     const float thr = sq_threshold(P.h);
-    for_each_wall(W, g, P.search_radius, cx, cy, xi.x, xi.y, thr, [&](int b, float2 xb) {
-      const Geo e = geo(xi.x, xi.y, xb.x, xb.y, P.inv_h);
-      const float gw = kGW(e.q, P.c_g);
-      const float gx = gw * e.ex, gy = gw * e.ey;
-      const float rx = Li.x * gx + Li.y * gy, ry = Li.z * gx + Li.w * gy;
-      const float s = (W.rho[b] * P.rho0 - rhoi) * W.vol[b] * 2.0f;
-      wx += s * rx;
-      wy += s * ry;
-    });
+    for_each_wall(
+        W, g, P.search_radius, cx, cy, xi.x, xi.y, thr,
+        [&](int b, float2 xb) {
+          const Geo e = geo(xi.x, xi.y, xb.x, xb.y, P.inv_h);
+          const float gw = kGW(e.q, P.c_g);
+          const float gx = gw * e.ex, gy = gw * e.ey;
+          const float rx = Li.x * gx + Li.y * gy, ry = Li.z * gx + Li.w * gy;
+          const float s = (W.rho[b] * P.rho0 - rhoi) * W.vol[b] * 2.0f;
+          wx += s * rx;
+          wy += s * ry;
+        },
+        coff);
   }
   grad_rho[i] = make_float2(-fx - wx, -fy - wy);
 }
 
-// ---------------------------------------------------------------------------- pass 3 (deltaSPH)
 // D_i = h delta c0 sum_j [2 (rho_j - rho_i)/(|x_ji|^2 + eps) x_ji - (<grad rho>_i + <grad rho>_j)] . gradW_ij V_j
-__global__ void __launch_bounds__(128) k_dsph_diffusion(FluidView F, SphParams P, const float2* __restrict__ grad_rho,
-                                                        float* __restrict__ dpdt) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= F.n) return;
+__device__ __forceinline__ void diffusion_body(int i, const FluidView& F, const SphParams& P,
+                                               const float2* __restrict__ grad_rho, float* __restrict__ dpdt) {
   const float2 xi = F.x[i], gi = grad_rho[i];
   const float rhoi = F.rho[i] * P.rho0;
   float acc = 0.f;
@@ -276,16 +278,12 @@ __global__ void __launch_bounds__(128) k_dsph_diffusion(FluidView F, SphParams P
   dpdt[i] += P.diff_k * acc;
 }
 
-// ---------------------------------------------------------------------------- integration
-// semiImplicitEuler, src/simulationBase.py:647-652 with integrateValues :564-569:
-// v' = v + dt a, x' = x + dt (v + dt a), rho~' = rho~ + dt dpdt / rho0 (continuum density).
-__global__ void k_sie(int n, const float2* __restrict__ x, const float2* __restrict__ v,
-                      const float* __restrict__ rho, const float2* __restrict__ a, const float* __restrict__ dpdt,
-                      const float* __restrict__ dt_ptr, float rho0, int continuum, float2* __restrict__ xo,
-                      float2* __restrict__ vo, float* __restrict__ ro, int32_t* status) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const float dt = *dt_ptr;
+// semiImplicitEuler, src/simulationBase.py:647-652 with integrateValues :564-569.
+__device__ __forceinline__ void sie_body(int i, const float2* __restrict__ x, const float2* __restrict__ v,
+                                         const float* __restrict__ rho, const float2* __restrict__ a,
+                                         const float* __restrict__ dpdt, float dt, float rho0, int continuum,
+                                         float2* __restrict__ xo, float2* __restrict__ vo, float* __restrict__ ro,
+                                         int32_t* status) {
   const float2 ai = a[i], vi = v[i], xi = x[i];
   const float2 vn = make_float2(vi.x + dt * ai.x, vi.y + dt * ai.y);
   const float2 xn = make_float2(xi.x + dt * (vi.x + dt * ai.x), xi.y + dt * (vi.y + dt * ai.y));
@@ -297,6 +295,95 @@ __global__ void k_sie(int n, const float2* __restrict__ x, const float2* __restr
     flag(status, SPH_FLAG_NONFINITE);
 }
 
+// ---------------------------------------------------------------------------- one scene
+__global__ void __launch_bounds__(128) k_mdbc(FluidView F, WallView W, const sph_grid* __restrict__ gp, SphParams P) {
+  int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= W.n) return;
+  mdbc_body(b, F, W, *gp, P, 0);
+}
+
+__global__ void __launch_bounds__(128) k_dsph_pass1(FluidView F, WallView W, const sph_grid* __restrict__ gp,
+                                                    SphParams P, float* __restrict__ dpdt, float2* __restrict__ acc,
+                                                    float4* __restrict__ Lout) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= F.n) return;
+  pass1_body(i, F, W, *gp, P, 0, dpdt, acc, Lout);
+}
+
+__global__ void __launch_bounds__(128) k_dsph_gradrho(FluidView F, WallView W, const sph_grid* __restrict__ gp,
+                                                      SphParams P, const float4* __restrict__ L,
+                                                      float2* __restrict__ grad_rho) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= F.n) return;
+  gradrho_body(i, F, W, *gp, P, 0, L, grad_rho);
+}
+
+__global__ void __launch_bounds__(128) k_dsph_diffusion(FluidView F, SphParams P, const float2* __restrict__ grad_rho,
+                                                        float* __restrict__ dpdt) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= F.n) return;
+  diffusion_body(i, F, P, grad_rho, dpdt);
+}
+
+__global__ void k_sie(int n, const float2* __restrict__ x, const float2* __restrict__ v,
+                      const float* __restrict__ rho, const float2* __restrict__ a, const float* __restrict__ dpdt,
+                      const float* __restrict__ dt_ptr, float rho0, int continuum, float2* __restrict__ xo,
+                      float2* __restrict__ vo, float* __restrict__ ro, int32_t* status) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  sie_body(i, x, v, rho, a, dpdt, *dt_ptr, rho0, continuum, xo, vo, ro, status);
+}
+
+// ---------------------------------------------------------------------------- batch of scenes
+// scenes[sid[i]] gives particle i's grid, parameters, cell-table offset and time step.
+__global__ void __launch_bounds__(128) k_batch_mdbc(FluidView F, WallView W, const SceneDev* __restrict__ scenes,
+                                                    const int32_t* __restrict__ wsid) {
+  int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= W.n) return;
+  const SceneDev& S = scenes[wsid[b]];
+  mdbc_body(b, F, W, S.g, S.P, S.coff);
+}
+
+__global__ void __launch_bounds__(128) k_batch_pass1(FluidView F, WallView W, const SceneDev* __restrict__ scenes,
+                                                     const int32_t* __restrict__ sid, float* __restrict__ dpdt,
+                                                     float2* __restrict__ acc, float4* __restrict__ Lout) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= F.n) return;
+  const SceneDev& S = scenes[sid[i]];
+  pass1_body(i, F, W, S.g, S.P, S.coff, dpdt, acc, Lout);
+}
+
+__global__ void __launch_bounds__(128) k_batch_gradrho(FluidView F, WallView W, const SceneDev* __restrict__ scenes,
+                                                       const int32_t* __restrict__ sid, const float4* __restrict__ L,
+                                                       float2* __restrict__ grad_rho) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= F.n) return;
+  const SceneDev& S = scenes[sid[i]];
+  if (S.P.diffusion != 2) return;
+  gradrho_body(i, F, W, S.g, S.P, S.coff, L, grad_rho);
+}
+
+__global__ void __launch_bounds__(128) k_batch_diffusion(FluidView F, const SceneDev* __restrict__ scenes,
+                                                         const int32_t* __restrict__ sid,
+                                                         const float2* __restrict__ grad_rho, float* __restrict__ dpdt) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= F.n) return;
+  const SceneDev& S = scenes[sid[i]];
+  if (S.P.diffusion != 2) return;
+  diffusion_body(i, F, S.P, grad_rho, dpdt);
+}
+
+__global__ void k_batch_sie(int n, const int32_t* __restrict__ sid, const SceneDev* __restrict__ scenes,
+                            const float2* __restrict__ x, const float2* __restrict__ v, const float* __restrict__ rho,
+                            const float2* __restrict__ a, const float* __restrict__ dpdt, float2* __restrict__ xo,
+                            float2* __restrict__ vo, float* __restrict__ ro, int32_t* status) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const SceneDev& S = scenes[sid[i]];
+  sie_body(i, x, v, rho, a, dpdt, S.dt, S.P.rho0, 1, xo, vo, ro, status);
+}
+
+// ---------------------------------------------------------------------------- RK4 helpers
 // RK4 stage / combination, src/simulationBase.py:679-705: out = base + c * (k_u, k_a, k_d / rho0).
 __global__ void k_rk_axpy(int n, const float2* __restrict__ x0, const float2* __restrict__ v0,
                           const float* __restrict__ r0, const float2* __restrict__ ku, const float2* __restrict__ ka,
@@ -346,7 +433,6 @@ __global__ void k_permute(const uint32_t* __restrict__ order, int n, const T* __
 }  // namespace sph
 
 using namespace sph;
-
 
 extern "C" {
 
@@ -398,6 +484,50 @@ sph_status_t sph_integrate_semi_implicit_euler(int64_t n, const float* x, const 
       reinterpret_cast<const float2*>(acc), dpdt, dt, rest_density, continuum_density, reinterpret_cast<float2*>(x_out),
       reinterpret_cast<float2*>(v_out), rho_out, status);
   SPH_CHECK_LAUNCH("integrate_semi_implicit_euler");
+  return SPH_OK;
+}
+
+sph_status_t sph_batch_deltasph_step(const sph_fluid_view* fluid, const sph_wall_view* walls, const void* scenes,
+                                     const int32_t* sid, const int32_t* wall_sid, float* dpdt, float* acc, float* L,
+                                     float* grad_rho, int32_t any_renormalized, float* x_out, float* v_out,
+                                     float* rho_out, int32_t* status, void* stream) {
+  SPH_VIEW_CHECK(fluid);
+  SPH_VIEW_CHECK(walls);
+  SPH_REQUIRE(scenes && sid && dpdt && acc && x_out && v_out && rho_out, "batch_deltasph_step: bad arguments");
+  SPH_REQUIRE(walls->n == 0 || wall_sid, "batch_deltasph_step: walls need wall_sid");
+  SPH_REQUIRE(!any_renormalized || (L && grad_rho), "batch_deltasph_step: deltaSPH diffusion needs L, grad_rho");
+  const int n = (int)fluid->n;
+  if (n == 0) return SPH_OK;
+  cudaStream_t st = as_stream(stream);
+  const FluidView F = to_fluid(fluid);
+  const WallView W = to_walls(walls);
+  const SceneDev* S = static_cast<const SceneDev*>(scenes);
+  if (W.n > 0) k_batch_mdbc<<<grid_for(W.n, 128), 128, 0, st>>>(F, W, S, wall_sid);
+  const int nb = grid_for(n, 128);
+  k_batch_pass1<<<nb, 128, 0, st>>>(F, W, S, sid, dpdt, reinterpret_cast<float2*>(acc), reinterpret_cast<float4*>(L));
+  if (any_renormalized) {
+    k_batch_gradrho<<<nb, 128, 0, st>>>(F, W, S, sid, reinterpret_cast<const float4*>(L),
+                                        reinterpret_cast<float2*>(grad_rho));
+    k_batch_diffusion<<<nb, 128, 0, st>>>(F, S, sid, reinterpret_cast<const float2*>(grad_rho), dpdt);
+  }
+  k_batch_sie<<<grid_for(n, 256), 256, 0, st>>>(n, sid, S, F.x, F.v, F.rho, reinterpret_cast<const float2*>(acc), dpdt,
+                                                 reinterpret_cast<float2*>(x_out), reinterpret_cast<float2*>(v_out),
+                                                 rho_out, status);
+  SPH_CHECK_LAUNCH("batch_deltasph_step");
+  return SPH_OK;
+}
+
+size_t sph_scene_bytes(void) { return sizeof(SceneDev); }
+
+sph_status_t sph_scene_encode(const sph_params* params, const sph_grid* grid_host, int32_t cell_offset, float dt,
+                              void* out_host) {
+  SPH_REQUIRE(params && grid_host && out_host && params->support > 0.f, "scene_encode: bad arguments");
+  SceneDev s;
+  s.P = to_params(params);
+  s.g = *grid_host;
+  s.coff = cell_offset;
+  s.dt = dt;
+  memcpy(out_host, &s, sizeof(s));
   return SPH_OK;
 }
 

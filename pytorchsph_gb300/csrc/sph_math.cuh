@@ -171,15 +171,17 @@ __device__ inline void pinv3_solve(const double A[3][3], const double b[3], doub
 // Iterate the wall particles whose cell is within +-r of fluid cell (cx, cy) and that pass
 // the wall-side predicate sqrtf(fmaf(dx,dx,dy*dy)) < h_b with dx = x_b - x_f: exactly the
 // wall->fluid pairs of searchExisting (src/modules/neighborSearch.py:231-252).
+// `coff` is the scene's first slot in the (batched) cell tables; 0 for a single scene.
 template <typename F>
 __device__ __forceinline__ void for_each_wall(const WallView& W, const sph_grid& g, int r, int cx, int cy, float xf,
-                                              float yf, float thr_b, F&& f) {
+                                              float yf, float thr_b, F&& f, int coff = 0) {
   const int x0 = max(cx - r, 0), x1 = min(cx + r, g.cells_x - 1);
   if (x0 > x1) return;
   const int y0 = max(cy - r, 0), y1 = min(cy + r, g.cells_y - 1);
+  const int32_t* cs = W.cell_start + coff;
   for (int yy = y0; yy <= y1; ++yy) {
     const int row = yy * g.cells_x;
-    const int b0 = __ldg(W.cell_start + row + x0), b1 = __ldg(W.cell_start + row + x1 + 1);
+    const int b0 = __ldg(cs + row + x0), b1 = __ldg(cs + row + x1 + 1);
     for (int b = b0; b < b1; ++b) {
       const float2 xb = __ldg(W.x + b);
       if (dist2_ref(xb.x, xb.y, xf, yf) <= thr_b) f(b, xb);
@@ -208,6 +210,15 @@ __device__ __forceinline__ void cell_of(uint32_t key, const sph_grid& g, int* cx
 
 // Host-side conversions of the C-ABI views into the kernels' views.
 namespace sph {
+// One scene of a batch as the kernels see it: derived parameters, its search grid, its
+// first slot in the concatenated cell tables and its time step.
+struct SceneDev {
+  SphParams P;
+  sph_grid g;
+  int coff;
+  float dt;
+};
+
 static inline SphParams to_params(const sph_params* p) {
   SphParams P;
   P.h = p->support;

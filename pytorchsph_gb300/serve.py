@@ -1,0 +1,426 @@
+"""Batched serving of many deltaSPH scenes on one GB300.
+
+`SceneBatch` holds any number of independent scenes in one concatenated particle array
+(per-particle scene index, per-scene grid / parameters / dt in a device scene table,
+(scene, cell) sort keys) and advances all of them with one fixed sequence of kernels:
+keys -> counting sort -> permute -> CSR count / scan / fill -> mDBC + forces + update.
+Buffers are static, so one batch step can be captured once in a CUDA graph and replayed.
+Scenes never interact: each scene's particles sort into their own cell range and every
+kernel reads only its own scene's cells, so a scene gives the same bits alone and in any
+mix.
+
+`Server` is the request loop: requests arrive (a trace with arrival times), are admitted
+while the device memory budget allows, step together with every other live scene, and
+retire after their step count.  Admission / retirement rebuild the batch between steps;
+steps in between replay the captured graph.  It records per-scene step latency and
+time-to-completion.
+"""
+from __future__ import annotations
+
+import ctypes
+import time
+from dataclasses import dataclass, field
+
+import numpy as np
+import torch
+
+from . import _native as N
+from .search import MAX_CELLS, Workspace, grid_from_bytes, _f2
+from .sim import SimConfig, SphParamsC, FluidViewC, WallViewC, DIFFUSION
+
+
+def _params_for(cfg: SimConfig, h: float, cells: int) -> SphParamsC:
+    P = SphParamsC()
+    P.support = h
+    P.rest_density = cfg.rest_density
+    P.c0 = cfg.c0
+    P.gamma = cfg.gamma
+    P.alpha = cfg.alpha
+    P.delta = cfg.delta
+    P.kinematic = cfg.kinematic
+    P.gravity[0], P.gravity[1] = cfg.gravity
+    P.point_source = int(cfg.point_source)
+    P.point_magnitude = cfg.point_magnitude
+    P.point_center[0], P.point_center[1] = cfg.point_center
+    P.density_diffusion = DIFFUSION[cfg.density_diffusion]
+    P.boundary_diffusion = int(bool(cfg.boundary_diffusion))
+    P.search_radius = cfg.search_radius
+    P.cell_capacity = cells
+    return P
+
+
+class _Grid(ctypes.Structure):
+    _fields_ = [("qmin", ctypes.c_float * 2), ("hmax", ctypes.c_float), ("reserved", ctypes.c_float),
+                ("cells_x", ctypes.c_int32), ("cells_y", ctypes.c_int32), ("num_cells", ctypes.c_int32),
+                ("reserved2", ctypes.c_int32)]
+
+
+def scene_grid(scene, device) -> _Grid:
+    """The scene's search grid (sortPositions bounds with the scene's virtual domain)."""
+    lib = N.load()
+    x = torch.as_tensor(np.ascontiguousarray(scene["pos"], np.float32), device=device)
+    h = torch.as_tensor(np.ascontiguousarray(scene["support"], np.float32), device=device)
+    n = x.shape[0]
+    g = torch.empty(8, dtype=torch.int32, device=device)
+    status = torch.zeros(1, dtype=torch.int32, device=device)
+    scratch = torch.empty((lib.sph_grid_scratch_bytes(n) + 7) // 8, dtype=torch.int64, device=device)
+    N.call("sph_grid_build", N.ptr(x), N.ptr(h), n, _f2(scene["vmin"]), _f2(scene["vmax"]), MAX_CELLS, N.ptr(g),
+           N.ptr(status), N.ptr(scratch), scratch.numel() * 8, N.stream_ptr())
+    if int(status.item()):
+        raise N.SPHError(f"scene grid: {N.decode_flags(int(status.item()))}")
+    raw = g.cpu().numpy().tobytes()
+    return _Grid.from_buffer_copy(raw)
+
+
+@dataclass
+class SceneSpec:
+    scene: dict
+    cfg: SimConfig
+    steps: int = 1000
+    name: str = ""
+
+
+class SceneBatch:
+    """A fixed set of scenes stepped together (deltaSPH, semi-implicit Euler)."""
+
+    def __init__(self, specs, device=None, states=None, pair_headroom: float = 1.3):
+        self.lib = N.load()
+        self.device = torch.device(device or torch.device("cuda", torch.cuda.current_device()))
+        dev = self.device
+        self.specs = list(specs)
+        S = len(self.specs)
+        rec = self.lib.sph_scene_bytes()
+        table = bytearray(rec * max(S, 1))
+        self.grids, self.coff = [], []
+        pos, vel, rho, area, sup, sid, uid = [], [], [], [], [], [], []
+        wpos, wgh, war, wsid = [], [], [], []
+        self.p_off = [0]
+        total_cells = 0
+        self.any_renorm = False
+        for s, spec in enumerate(self.specs):
+            sc, cfg = spec.scene, spec.cfg
+            if cfg.solver != "deltaSPH" or cfg.integration != "semiImplicitEuler":
+                raise N.SPHError("batched serving runs deltaSPH with semi-implicit Euler")
+            g = scene_grid(sc, dev)
+            h = float(np.float32(sc["support"][0]))
+            P = _params_for(cfg, h, g.num_cells)
+            buf = ctypes.create_string_buffer(rec)
+            N.check(self.lib.sph_scene_encode(ctypes.byref(P), ctypes.byref(g), total_cells, cfg.dt, buf),
+                    "scene_encode")
+            table[s * rec:(s + 1) * rec] = buf.raw
+            self.grids.append(g)
+            self.coff.append(total_cells)
+            total_cells += g.num_cells
+            self.any_renorm |= cfg.density_diffusion == "deltaSPH"
+            st = states[s] if states is not None else None
+            n = len(sc["pos"])
+            pos.append(st["x"] if st else sc["pos"])
+            vel.append(st["v"] if st else sc["vel"])
+            rho.append(st["rho"] if st else sc["rho"])
+            area.append(sc["area"])
+            sup.append(sc["support"])
+            sid.append(np.full(n, s, np.int32))
+            uid.append(np.arange(n, dtype=np.int32))
+            self.p_off.append(self.p_off[-1] + n)
+            nb = len(sc.get("wall_pos", ()))
+            if nb:
+                wpos.append(sc["wall_pos"])
+                wgh.append(sc["ghost_pos"])
+                war.append(sc["wall_area"])
+                wsid.append(np.full(nb, s, np.int32))
+        if total_cells >= MAX_CELLS:
+            raise N.SPHError("batch cell tables too large")
+        self.cap = max(total_cells, 1)
+        self.scenes = torch.frombuffer(bytearray(table), dtype=torch.uint8).to(dev)
+        self.n = self.p_off[-1]
+        n = self.n
+        cat = lambda xs, dt_: torch.as_tensor(np.ascontiguousarray(np.concatenate(xs), dt_), device=dev)
+        self.a = {"x": cat(pos, np.float32).reshape(n, 2), "v": cat(vel, np.float32).reshape(n, 2),
+                  "rho": cat(rho, np.float32), "area": cat(area, np.float32), "sup": cat(sup, np.float32),
+                  "sid": cat(sid, np.int32), "uid": cat(uid, np.int32)}
+        self.b = {k: torch.empty_like(v) for k, v in self.a.items()}
+        self.ws = Workspace(dev)
+        self.status = torch.zeros(1, dtype=torch.int32, device=dev)
+        self.keys = torch.empty(n, dtype=torch.int32, device=dev)
+        self.order = torch.empty(n, dtype=torch.int32, device=dev)
+        self.skeys = torch.empty(n, dtype=torch.int32, device=dev)
+        self.cell_start = torch.empty(self.cap + 2, dtype=torch.int32, device=dev)
+        self.hist = torch.zeros(self.cap + 1, dtype=torch.int32, device=dev)
+        self.cs_scratch = torch.empty((self.lib.sph_counting_sort_scratch_bytes(n, self.cap) + 7) // 8,
+                                      dtype=torch.int64, device=dev)
+        self.counts = torch.empty(n, dtype=torch.int32, device=dev)
+        self.offsets = torch.empty(n + 1, dtype=torch.int32, device=dev)
+        self.scan_scratch = torch.empty((self.lib.sph_scan_scratch_bytes(n) + 7) // 8, dtype=torch.int64, device=dev)
+        self.dpdt = torch.empty(n, dtype=torch.float32, device=dev)
+        self.acc = torch.empty((n, 2), dtype=torch.float32, device=dev)
+        self.L = torch.empty((n, 4), dtype=torch.float32, device=dev) if self.any_renorm else None
+        self.grad_rho = torch.empty((n, 2), dtype=torch.float32, device=dev) if self.any_renorm else None
+        # walls: concatenated, sorted once by (scene, cell)
+        self.nb = sum(len(w) for w in wpos)
+        self._setup_walls(wpos, wgh, war, wsid)
+        # pair capacity from a first count
+        self._sort_permute()
+        self._count()
+        P = int(self.offsets[n].item())
+        self.pair_cap = int(P * pair_headroom) + 1024
+        self.cols = torch.empty(self.pair_cap, dtype=torch.int32, device=dev)
+        self.graph = None
+        self.steps_done = 0
+
+    def _setup_walls(self, wpos, wgh, war, wsid):
+        dev = self.device
+        nb = self.nb
+        if nb == 0:
+            z = torch.zeros(1, dtype=torch.float32, device=dev)
+            self.w = {"x": torch.zeros((1, 2), device=dev), "ghost": torch.zeros((1, 2), device=dev), "area": z,
+                      "rho": z.clone(), "vol": z.clone(), "p": z.clone(), "sid": torch.zeros(1, dtype=torch.int32, device=dev),
+                      "cell_start": torch.zeros(self.cap + 2, dtype=torch.int32, device=dev), "order": None}
+        else:
+            cat = lambda xs, dt_: torch.as_tensor(np.ascontiguousarray(np.concatenate(xs), dt_), device=dev)
+            x = cat(wpos, np.float32).reshape(nb, 2)
+            sid = cat(wsid, np.int32)
+            keys = torch.empty(nb, dtype=torch.int32, device=dev)
+            order = torch.empty(nb, dtype=torch.int32, device=dev)
+            skeys = torch.empty(nb, dtype=torch.int32, device=dev)
+            cs = torch.empty(self.cap + 2, dtype=torch.int32, device=dev)
+            hist = torch.zeros(self.cap + 1, dtype=torch.int32, device=dev)
+            st = N.stream_ptr()
+            N.call("sph_batch_cell_keys", N.ptr(x), nb, N.ptr(sid), N.ptr(self.scenes), self.cap, N.ptr(keys),
+                   N.ptr(hist), N.ptr(self.status), st)
+            scr = torch.empty((self.lib.sph_counting_sort_scratch_bytes(nb, self.cap) + 7) // 8, dtype=torch.int64,
+                              device=dev)
+            N.call("sph_counting_sort", N.ptr(keys), nb, self.cap, N.ptr(hist), N.ptr(cs), N.ptr(order), N.ptr(skeys),
+                   N.ptr(self.status), N.ptr(scr), scr.numel() * 8, st)
+            perm = lambda t: self._perm(order, t)
+            self.w = {"x": perm(x), "ghost": perm(cat(wgh, np.float32).reshape(nb, 2)), "area": perm(cat(war, np.float32)),
+                      "sid": perm(sid), "cell_start": cs, "rho": torch.ones(nb, device=dev),
+                      "vol": torch.zeros(nb, device=dev), "p": torch.zeros(nb, device=dev), "order": order}
+        self.wall_view = WallViewC(N.ptr(self.w["x"]), N.ptr(self.w["ghost"]), N.ptr(self.w["area"]),
+                                   N.ptr(self.w["cell_start"]), nb, N.ptr(self.w["rho"]), N.ptr(self.w["vol"]),
+                                   N.ptr(self.w["p"]))
+
+    def _perm(self, order, t, out=None):
+        if out is None:
+            out = torch.empty_like(t)
+        eb = t.element_size() * (t.shape[1] if t.dim() == 2 else 1)
+        N.call("sph_permute", N.ptr(order), t.shape[0], eb, N.ptr(t), N.ptr(out), N.stream_ptr())
+        return out
+
+    # ------------------------------------------------------------------ one batch step
+    def _sort_permute(self):
+        st = N.stream_ptr()
+        n = self.n
+        N.call("sph_batch_cell_keys", N.ptr(self.a["x"]), n, N.ptr(self.a["sid"]), N.ptr(self.scenes), self.cap,
+               N.ptr(self.keys), N.ptr(self.hist), N.ptr(self.status), st)
+        # inside a cell, order by particle id: a scene's order never depends on its history
+        # or on the other scenes of the batch
+        N.call("sph_counting_sort_tie", N.ptr(self.keys), n, self.cap, N.ptr(self.hist), N.ptr(self.cell_start),
+               N.ptr(self.a["uid"]), N.ptr(self.order), N.ptr(self.skeys), N.ptr(self.status),
+               N.ptr(self.cs_scratch), self.cs_scratch.numel() * 8, st)
+        for k in self.a:
+            self._perm(self.order, self.a[k], self.b[k])
+
+    def _count(self):
+        st = N.stream_ptr()
+        n = self.n
+        b = self.b
+        N.call("sph_batch_nl_count", N.ptr(b["x"]), N.ptr(b["sup"]), n, N.ptr(self.skeys), N.ptr(self.cell_start),
+               N.ptr(self.scenes), N.ptr(b["sid"]), N.ptr(self.counts), st)
+        N.call("sph_exclusive_scan_i32", N.ptr(self.counts), N.ptr(self.offsets), n, N.ptr(self.scan_scratch),
+               self.scan_scratch.numel() * 8, st)
+
+    def step_kernels(self):
+        """The batch step as a fixed kernel sequence (no host synchronisation)."""
+        st = N.stream_ptr()
+        n = self.n
+        a, b = self.a, self.b
+        self._sort_permute()
+        self._count()
+        N.call("sph_batch_nl_fill", N.ptr(b["x"]), N.ptr(b["sup"]), n, N.ptr(self.skeys), N.ptr(self.cell_start),
+               N.ptr(self.scenes), N.ptr(b["sid"]), N.ptr(self.offsets), self.pair_cap, N.ptr(self.cols),
+               N.ptr(self.status), st)
+        fv = FluidViewC(N.ptr(b["x"]), N.ptr(b["v"]), N.ptr(b["rho"]), N.ptr(b["area"]), N.ptr(self.skeys),
+                        N.ptr(self.offsets), N.ptr(self.cols), N.ptr(self.cell_start), n)
+        N.call("sph_batch_deltasph_step", ctypes.byref(fv), ctypes.byref(self.wall_view), N.ptr(self.scenes),
+               N.ptr(b["sid"]), N.ptr(self.w["sid"]), N.ptr(self.dpdt), N.ptr(self.acc), N.ptr(self.L),
+               N.ptr(self.grad_rho), int(self.any_renorm), N.ptr(a["x"]), N.ptr(a["v"]), N.ptr(a["rho"]),
+               N.ptr(self.status), st)
+        for k in ("area", "sup", "sid", "uid"):
+            a[k].copy_(b[k])
+
+    # kernels launched by one batch step (for the bench's launch count): keys 1, counting sort
+    # (scan 3 + scatter + fix + fix_large) 6, permutes 7, count 1, scan 3, fill 1, mdbc 1,
+    # pass1 1 (+2 renormalized), update 1
+    def launches_per_step(self):
+        return 1 + 6 + 7 + 1 + 3 + 1 + (1 if self.nb else 0) + 1 + (2 if self.any_renorm else 0) + 1
+
+    def capture(self):
+        """Capture one batch step into a CUDA graph (after a warm-up step)."""
+        s = torch.cuda.Stream(self.device)
+        s.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(s):
+            self.step_kernels()
+        torch.cuda.current_stream().wait_stream(s)
+        torch.cuda.synchronize()
+        self.graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(self.graph):
+            self.step_kernels()
+        torch.cuda.synchronize()
+        self.steps_done += 1
+
+    def step(self):
+        if self.graph is not None:
+            self.graph.replay()
+        else:
+            self.step_kernels()
+        self.steps_done += 1
+
+    def check(self):
+        f = int(self.status.item())
+        if f:
+            raise N.SPHError(f"batch step: {N.decode_flags(f)}")
+        if int(self.offsets[self.n].item()) > self.pair_cap:
+            raise N.SPHError("batch step: neighbor pair buffer too small")
+
+    # ------------------------------------------------------------------ output
+    def scene_state(self, s: int):
+        """Positions, velocities and densities of scene s in its original particle order."""
+        lo, hi = self.p_off[s], self.p_off[s + 1]
+        uid = self.a["uid"][lo:hi].long()
+        out = {}
+        for k in ("x", "v", "rho"):
+            t = self.a[k][lo:hi]
+            o = torch.empty_like(t)
+            o[uid] = t
+            out[k] = o.cpu().numpy()
+        return out
+
+    def device_bytes(self):
+        tot = 0
+        for d in (self.a, self.b):
+            tot += sum(t.numel() * t.element_size() for t in d.values())
+        tot += self.cols.numel() * 4 + (self.cap + 2) * 8 + self.n * 40
+        return tot
+
+
+def estimate_bytes(scene) -> int:
+    """Device bytes one scene needs in a batch (state x2, sort, CSR at ~30 pairs/particle)."""
+    n = len(scene["pos"])
+    nb = len(scene.get("wall_pos", ()))
+    return n * (2 * 36 + 60 + 30 * 4 * 1.3) + nb * 60 + 4096
+
+
+# ----------------------------------------------------------------------------- continuous batching
+@dataclass
+class Request:
+    rid: int
+    arrival: float           # seconds from the start of the trace
+    spec: SceneSpec
+    admitted: float = -1.0
+    finished: float = -1.0
+    steps_done: int = 0
+    final: dict | None = None
+
+
+class Server:
+    """Continuous batching: admit arrived requests while the memory budget allows, step all
+    live scenes together, retire each scene exactly when it reaches its step count (its
+    final state is kept in `Request.final`).  Membership changes rebuild the batch (and its
+    CUDA graph) between steps; new arrivals wait at most `rebuild_every` batch steps."""
+
+    def __init__(self, device=None, budget_bytes: float = 60e9, rebuild_every: int = 20, use_graph: bool = True,
+                 keep_final: bool = True):
+        self.device = torch.device(device or torch.device("cuda", torch.cuda.current_device()))
+        self.budget = budget_bytes
+        self.rebuild_every = rebuild_every
+        self.use_graph = use_graph
+        self.keep_final = keep_final
+        self.live: list[Request] = []
+        self.batch: SceneBatch | None = None
+        self.particle_steps = 0
+        self.batch_steps = 0
+        self.rebuilds = 0
+        self.step_latency = []      # (batch step seconds, live scenes) per batch step
+        self.rebuild_seconds = 0.0
+
+    def _rebuild(self, queue, now):
+        t = time.perf_counter()
+        states, keep = [], []
+        if self.batch is not None:
+            for s, r in enumerate(self.live):
+                st = self.batch.scene_state(s)
+                if r.steps_done >= r.spec.steps:
+                    r.finished = now
+                    if self.keep_final:
+                        r.final = st
+                else:
+                    keep.append(r)
+                    states.append(st)
+        used = sum(estimate_bytes(r.spec.scene) for r in keep)
+        while queue and queue[0].arrival <= now:
+            need = estimate_bytes(queue[0].spec.scene)
+            if used + need > self.budget and keep:
+                break
+            r = queue.pop(0)
+            r.admitted = now
+            keep.append(r)
+            states.append(None)
+            used += need
+        self.live = keep
+        self.batch = None
+        if keep:
+            self.batch = SceneBatch([r.spec for r in keep], self.device, states=states)
+            if self.use_graph:
+                self.batch.capture()          # runs one step eagerly, then records it
+                self._count_step(0.0)
+            self.rebuilds += 1
+        self.rebuild_seconds += time.perf_counter() - t
+
+    def _count_step(self, seconds):
+        for r in self.live:
+            r.steps_done += 1
+        self.particle_steps += self.batch.n
+        self.batch_steps += 1
+        if seconds > 0:
+            self.step_latency.append((seconds, len(self.live)))
+
+    def run(self, requests, time_scale: float = 1.0, max_wall: float = 600.0):
+        """Serve `requests` (arrival times scaled by time_scale); returns the wall seconds."""
+        queue = sorted(requests, key=lambda r: r.arrival)
+        for r in queue:
+            r.arrival *= time_scale
+        t0 = time.perf_counter()
+        since = 0
+        while queue or self.live:
+            now = time.perf_counter() - t0
+            if now > max_wall:
+                break
+            done = any(r.steps_done >= r.spec.steps for r in self.live)
+            arrived = bool(queue) and queue[0].arrival <= now
+            if self.batch is None or done or (arrived and since >= self.rebuild_every):
+                self._rebuild(queue, now)
+                since = 0
+                if self.batch is None:
+                    if queue:
+                        time.sleep(max(0.0, min(queue[0].arrival - (time.perf_counter() - t0), 0.01)))
+                    continue
+                if any(r.steps_done >= r.spec.steps for r in self.live):
+                    continue
+            t = time.perf_counter()
+            self.batch.step()
+            torch.cuda.current_stream().synchronize()
+            self._count_step(time.perf_counter() - t)
+            since += 1
+        if self.batch is not None:
+            self.batch.check()
+        return time.perf_counter() - t0
+
+    def latency_percentiles(self, qs=(50, 99)):
+        """Per-scene step latency percentiles (each batch step counts once per live scene)."""
+        if not self.step_latency:
+            return {q: None for q in qs}
+        sec = np.array([s for s, _ in self.step_latency])
+        w = np.array([k for _, k in self.step_latency], np.float64)
+        o = np.argsort(sec)
+        cw = np.cumsum(w[o]) / w.sum()
+        return {q: float(sec[o][min(np.searchsorted(cw, q / 100.0), len(o) - 1)]) for q in qs}

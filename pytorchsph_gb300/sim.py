@@ -189,8 +189,9 @@ class Simulation:
         P.omega_fluid = c.omega_fluid
         return P
 
-    def _sort_keys(self, x, n, prefix):
-        """Counting sort of `n` positions by cell key; returns (order, sorted_keys, cell_start)."""
+    def _sort_keys(self, x, n, prefix, tie=None):
+        """Counting sort of `n` positions by cell key (inside a cell by `tie`, e.g. the
+        particle id, then index); returns (order, sorted_keys, cell_start)."""
         st = N.stream_ptr()
         ws = self.ws
         keys = ws.get(prefix + "keys", n)
@@ -201,8 +202,8 @@ class Simulation:
         N.call("sph_cell_keys", N.ptr(x), n, N.ptr(self.grid), self.cap, N.ptr(keys), None, N.ptr(hist),
                N.ptr(self.status), st)
         scratch = ws.bytes(prefix + "cs_scratch", self.lib.sph_counting_sort_scratch_bytes(n, self.cap))
-        N.call("sph_counting_sort", N.ptr(keys), n, self.cap, N.ptr(hist), N.ptr(cs), N.ptr(order), N.ptr(skeys),
-               N.ptr(self.status), N.ptr(scratch), scratch.numel() * 8, st)
+        N.call("sph_counting_sort_tie", N.ptr(keys), n, self.cap, N.ptr(hist), N.ptr(cs), N.ptr(tie), N.ptr(order),
+               N.ptr(skeys), N.ptr(self.status), N.ptr(scratch), scratch.numel() * 8, st)
         return order, skeys, cs
 
     def _permute(self, order, t):
@@ -241,7 +242,7 @@ class Simulation:
         """Re-sort every particle array by cell key and build the CSR neighbor list."""
         st = N.stream_ptr()
         n = self.n
-        order, skeys, cs = self._sort_keys(self.arr["x"], n, "f_")
+        order, skeys, cs = self._sort_keys(self.arr["x"], n, "f_", tie=self.arr["uid"])
         for k in list(self.arr):
             self.arr[k] = self._permute(order, self.arr[k])
         for k in list(self.extra):

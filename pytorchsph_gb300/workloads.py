@@ -129,3 +129,50 @@ def oscillating_drop(n_target: int = 16384, radius: float = 0.5, amplitude: floa
         "ghost_pos": np.zeros((0, 2), np.float32), "wall_area": np.zeros(0, np.float32), "h": float(h), "dx": dx,
         "vmin": np.array([-ext, -ext], np.float32), "vmax": np.array([ext, ext], np.float32),
     }
+
+
+def dam_break_scene(n_target: int, aspect: float, tank=(4.0, 2.0)):
+    """Dam break with about n_target fluid particles in a block of width/height `aspect`
+    whose area is a quarter of the tank's (dx = sqrt(area / n)), with 3-layer walls."""
+    W, H = tank
+    area = 0.25 * W * H
+    dx = float(np.sqrt(area / n_target))
+    nx = max(2, int(round(np.sqrt(n_target * aspect))))
+    ny = max(2, int(round(n_target / nx)))
+    while ny * dx > H - dx:
+        ny -= 1
+    return dam_break(nx, ny, dx, tank)
+
+
+def serving_trace(n_requests: int = 1024, rate: float = 50.0, n_min: int = 2048, n_max: int = 131072,
+                  steps: int = 1000, seed: int = 0):
+    """The serving workload: Poisson arrivals (mean `rate` per second), sizes log-uniform in
+    [n_min, n_max], half dam breaks with block width/height ~ U[0.5, 2], half oscillating
+    drops (radius 0.5, v = A (x, -y), A ~ U[0.5, 2]).  Everything derives from one master
+    seed through numpy SeedSequence.  Returns a list of dicts with the arrival time and the
+    scene parameters; `make_request_scene` builds the arrays when a request is admitted."""
+    ss = np.random.SeedSequence(seed)
+    rng = np.random.default_rng(ss)
+    gaps = rng.exponential(1.0 / rate, n_requests)
+    arrivals = np.cumsum(gaps) - gaps[0]
+    sizes = np.exp(rng.uniform(np.log(n_min), np.log(n_max), n_requests)).astype(np.int64)
+    kinds = rng.integers(0, 2, n_requests)
+    shape = rng.uniform(0.5, 2.0, n_requests)
+    out = []
+    for k in range(n_requests):
+        out.append({"rid": k, "arrival": float(arrivals[k]), "n": int(sizes[k]),
+                    "kind": "dam_break" if kinds[k] == 0 else "drop", "shape": float(shape[k]), "steps": steps})
+    return out
+
+
+def make_request_scene(req):
+    """(scene arrays, deltaSPH parameters) of one serving request."""
+    if req["kind"] == "dam_break":
+        sc = dam_break_scene(req["n"], req["shape"])
+        c0 = float(10.0 * np.sqrt(2 * 9.81 * sc["column_height"]))
+        params = {"c0": c0, "dt": 0.25 * sc["h"] / c0, "gravity": (0.0, -9.81), "point_source": False}
+    else:
+        sc = oscillating_drop(req["n"], 0.5, req["shape"])
+        c0 = 10.0
+        params = {"c0": c0, "dt": 0.25 * sc["h"] / c0, "gravity": (0.0, 0.0), "point_source": True}
+    return sc, params
