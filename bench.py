@@ -1,18 +1,23 @@
-"""Benchmark of the GB300 SPH hot path (one JSON line on rank 0).
+"""Benchmarks of the GB300 SPH hot path; rank 0 prints one JSON line.
 
-Workload `search_density_A` (default) / `search_density_B`: one step = the full hashed-grid
-neighbor search plus the density summation over N = 2^20 particles in [0,1]^2 (h = 3 dx,
-A = dx^2, domain [0,1]^2): grid bounds -> cell keys -> radix sort -> sorted SoA -> cell
-table -> CSR count with fused density -> scan -> CSR fill -> density back to particle order.
+Workloads (--workload):
+  serving (default)   1024 deltaSPH scene requests (Poisson arrivals at 50/s, 2,048-131,072
+                      particles log-uniform, half random-aspect dam breaks, half oscillating
+                      drops, 1000 steps each, 60 GB budget), served by continuous batching.
+                      value = particle-steps/s of the device-resident batch of all requests
+                      (K timed batch steps); e2e = the whole trace through the Server (scene
+                      upload, admission, batch rebuilds, final states read back) with every
+                      request queued at t=0; `serving` adds the real-time trace's p50/p99
+                      step latency and time-to-completion and the one-scene-at-a-time GPU path.
+  search_density_A/B  neighbor search + density over N = 2^20 particles.
+  dambreak_deltasph   8,192-particle dam break, renormalized deltaSPH, 3-layer walls.
+  dambreak_dfsph      262,144-particle dam break, DFSPH with walls, adaptive dt.
 
-  python bench.py [--steps K] [--warmup W] [--workload search_density_A|search_density_B]
+  python bench.py [--workload W] [--steps K] [--warmup W]
   python bench.py --impl reference ...   # the reference algorithm on the host cores
 
-`value` (particles searched per second) is timed on the device with the inputs resident
-in HBM, L2 flushed between steps; `e2e` times the same step through the public API from
-pinned host buffers (H2D of positions/supports/areas, D2H of the density and pair count).
-With torchrun (N>1) every rank runs an independent replica (the path has no exchange
-step) and `value` sums over ranks.
+With torchrun (N>1) every rank runs an independent replica (no exchange step exists on
+this path) and `value` sums over ranks.
 """
 from __future__ import annotations
 
@@ -39,10 +44,13 @@ def parse():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="search_density_A")
+    ap.add_argument("--workload", default="serving")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--sort", default="counting", choices=["counting", "radix"])
     ap.add_argument("--digit-bits", type=int, default=8)
+    ap.add_argument("--requests", type=int, default=1024)
+    ap.add_argument("--trace-steps", type=int, default=1000)
+    ap.add_argument("--no-trace", action="store_true", help="serving: skip the e2e and real-time trace runs")
     return ap.parse_args()
 
 
@@ -84,8 +92,9 @@ class ClockSampler:
     def summary(self):
         if not self.samples:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"], "samples": 0}
-        sm = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
-        mx = [float(s[2]) for s in self.samples if s[2].replace(".", "").isdigit()]
+        num = lambda s: s.replace(".", "", 1).isdigit()
+        sm = [float(s[1]) for s in self.samples if num(s[1])]
+        mx = [float(s[2]) for s in self.samples if num(s[2])]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         reasons = sorted({names[k] for s in self.samples for k in range(4) if len(s) > 5 + k and s[5 + k] == "Active"})
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
@@ -93,82 +102,15 @@ class ClockSampler:
 
 
 def dist_env():
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return rank, world, local
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
 
 
-# ----------------------------------------------------------------------------- CPU arm
-def cpu_search_density(pos, h, area, vmin, vmax, L, threads):
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import nsearch as ns
-    si = ns.SortInfo(pos, h, vmin, vmax, L)
-    rows, cols = ns.nl_cells(si, threads=threads)
-    off, c = ns.canonical_csr(rows, cols, si.n)
-    rho = ns.density(off, c, pos, area, float(h[0]))
-    return len(rows), rho
-
-
-def time_cpu(pos, h, area, vmin, vmax, L, budget_s=20.0, max_reps=10):
-    threads = os.cpu_count() or 1
-    reps, t_total = 0, 0.0
-    while reps < max_reps and (reps < 1 or t_total < budget_s):
-        t0 = time.perf_counter()
-        cpu_search_density(pos, h, area, vmin, vmax, L, threads)
-        t_total += time.perf_counter() - t0
-        reps += 1
-    return len(pos) * reps / t_total, threads, reps
-
-
-def load_workload(name):
-    from pytorchsph_gb300 import workloads
-    if name.startswith("search_density_"):
-        v = name.rsplit("_", 1)[1]
-        return workloads.search_density_case(v)
-    raise SystemExit(f"unknown workload {name}")
-
-
-def run_reference(args):
-    rank, world, _ = dist_env()
-    if rank != 0:
-        return
-    pos, h, area, vmin, vmax, L = load_workload(args.workload)
-    # the reference compiles only where its checkout exists; elsewhere the oracle port
-    # (oracle/nsearch_oracle.c, the same algorithm) stands in for it
-    kind = "port"
-    cpu_search_density(pos[:4096], h[:4096], area[:4096], vmin, vmax, -1, 1)  # build + warm
-    threads = os.cpu_count() or 1
-    times = []
-    for _ in range(args.warmup):
-        cpu_search_density(pos, h, area, vmin, vmax, L, threads)
-    for _ in range(args.steps):
-        t0 = time.perf_counter()
-        cpu_search_density(pos, h, area, vmin, vmax, L, threads)
-        times.append(time.perf_counter() - t0)
-    ms = 1e3 * sum(times) / len(times)
-    value = len(pos) / (ms / 1e3)
-    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "particles/s", "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": args.workload, "particles": len(pos), "support": "3dx", "hash_len": L},
-            "cpu_baseline": {"value": value, "unit": "particles/s", "cores": threads, "kind": kind,
-                             "sample": f"full {args.workload} step x {args.steps} (sort + hash map + "
-                                       f"buildNeighborList + density)"},
-            "e2e": {"value": value, "unit": "particles/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
-    print(json.dumps(line), flush=True)
-
-
-# ----------------------------------------------------------------------------- GPU arm
-# algorithmic bytes per particle of each kernel of the step (measurement)
-def algorithmic_bytes(kernel, n, P, cells):
-    if kernel == "nl_count":   # xy (8) + h (4) + A (4) + key (4) read, count (4) + rho (4) written, cell table once
-        return n * 28 + 4 * (cells + 2)
-    if kernel == "nl_fill":    # xy (8) + h (4) + key (4) + offsets (4) read, cols written (4 per pair)
-        return n * 20 + 4 * P + 4 * (cells + 2)
-    if kernel == "radix_sort": # per pass: keys+vals read twice (hist + scatter), written once
-        return n * 24
-    return n * 16
+def hbm_peak():
+    try:
+        p = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+        return float(p["hbm_gbs"]), "MEASURED_PEAKS.json hbm_gbs"
+    except Exception:
+        return 6800.0, "fallback 6.8 TB/s"
 
 
 def make_event():
@@ -179,24 +121,279 @@ def make_event():
         return torch.cuda.Event(enable_timing=True)
 
 
-PHASES = ["start", "keys", "sort", "gather", "count", "scan", "fill", "end"]
+def traffic_from_profiles(workload, kernel):
+    try:
+        prof = json.load(open(os.path.join(ROOT, "profiles", "traffic.json")))
+        return prof.get(workload, {}).get(kernel)
+    except Exception:
+        return None
 
 
-def run_ours(args):
+def base_line(args, world, value, ms, unit, config):
+    return {"metric": METRIC, "value": value, "unit": unit, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": config}
+
+
+# ----------------------------------------------------------------------------- CPU (oracle port) arms
+def cpu_search_density(pos, h, area, vmin, vmax, L, threads):
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import nsearch as ns
+    si = ns.SortInfo(pos, h, vmin, vmax, L)
+    rows, cols = ns.nl_cells(si, threads=threads)
+    off, c = ns.canonical_csr(rows, cols, si.n)
+    ns.density(off, c, pos, area, float(h[0]))
+    return len(rows)
+
+
+def cpu_deltasph_steps(scene, params, steps, diffusion="MOG"):
+    """Seconds for `steps` of the restated reference step (oracle/sph_torch.py, float32, torch CPU)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import torch
-    import torch.distributed as dist
-    rank, world, local = dist_env()
-    if world > 1:
-        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
-    torch.cuda.set_device(local)
-    dev = torch.device("cuda", local)
-    from pytorchsph_gb300 import build as B
-    B.build()
-    from pytorchsph_gb300 import _native as N
-    from pytorchsph_gb300.search import GridSearch
-    N.load()
+    import sph_torch as S
+    p = S.Params(h=scene["h"], c0=params["c0"], diffusion=diffusion, vmin=scene["vmin"], vmax=scene["vmax"],
+                 gravity=params.get("gravity", (0.0, -9.81)), point_source=params.get("point_source", False))
+    walls = S.Walls(torch.from_numpy(scene["wall_pos"]), torch.from_numpy(scene["ghost_pos"]),
+                    torch.from_numpy(scene["wall_area"])) if len(scene["wall_pos"]) else None
+    st = {"x": torch.from_numpy(scene["pos"]), "v": torch.from_numpy(scene["vel"]),
+          "rho": torch.from_numpy(scene["rho"]), "area": torch.from_numpy(scene["area"])}
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        new, _ = S.step(st, walls, p, params["dt"], "semiImplicitEuler", "deltaSPH", torch.float32)
+        st = {"x": new["x"].float(), "v": new["v"], "rho": new["rho"], "area": st["area"]}
+    return time.perf_counter() - t0
 
-    pos, h, area, vmin, vmax, L = load_workload(args.workload)
+
+def cpu_baseline_serving(steps=3):
+    import torch
+    from pytorchsph_gb300 import workloads
+    sc, p = workloads.make_request_scene({"kind": "dam_break", "n": 2048, "shape": 1.0})
+    cpu_deltasph_steps(sc, p, 1)
+    t = cpu_deltasph_steps(sc, p, steps)
+    n = len(sc["pos"])
+    return {"value": n * steps / t, "unit": "particle-steps/s", "cores": torch.get_num_threads(), "kind": "port",
+            "sample": f"{steps} semi-implicit-Euler deltaSPH steps of a {n}-particle dam-break request with the "
+                      f"restated reference step (oracle/sph_torch.py, float32, torch CPU)"}
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    if args.workload.startswith("search_density_"):
+        from pytorchsph_gb300 import workloads
+        pos, h, area, vmin, vmax, L = workloads.search_density_case(args.workload.rsplit("_", 1)[1])
+        cpu_search_density(pos[:4096], h[:4096], area[:4096], vmin, vmax, -1, 1)
+        for _ in range(args.warmup):
+            cpu_search_density(pos, h, area, vmin, vmax, L, threads)
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            cpu_search_density(pos, h, area, vmin, vmax, L, threads)
+        ms = 1e3 * (time.perf_counter() - t0) / args.steps
+        value = len(pos) / (ms / 1e3)
+        sample = f"full {args.workload} step x {args.steps} (sort + hash map + buildNeighborList + density)"
+        unit, cores = "particles/s", threads
+        config = {"workload": args.workload, "particles": len(pos)}
+    else:
+        import torch
+        torch.set_num_threads(threads)
+        cb = cpu_baseline_serving(steps=max(1, min(args.steps, 5)))
+        value, unit, sample, cores = cb["value"], cb["unit"], cb["sample"], cb["cores"]
+        ms = 2048 / value * 1e3
+        config = {"workload": args.workload}
+    line = base_line(args, world, value, ms, unit, config)
+    line["impl"] = "reference"
+    line["cpu_baseline"] = {"value": value, "unit": unit, "cores": cores, "kind": "port", "sample": sample}
+    line["e2e"] = {"value": value, "unit": unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
+    print(json.dumps(line), flush=True)
+
+
+# ----------------------------------------------------------------------------- GPU: serving
+def serving_specs(n_requests, steps):
+    from pytorchsph_gb300 import workloads
+    from pytorchsph_gb300.serve import SceneSpec
+    from pytorchsph_gb300.sim import SimConfig
+    trace = workloads.serving_trace(n_requests, 50.0, 2048, 131072, steps, seed=0)
+    specs = []
+    for t in trace:
+        sc, p = workloads.make_request_scene(t)
+        cfg = SimConfig(solver="deltaSPH", integration="semiImplicitEuler", dt=p["dt"], c0=p["c0"],
+                        gravity=p["gravity"], point_source=p["point_source"], density_diffusion="MOG")
+        specs.append(SceneSpec(sc, cfg, t["steps"], name=f"r{t['rid']}"))
+    return trace, specs
+
+
+def forces_alg_bytes(batch):
+    """Algorithmic HBM bytes of one forces launch: per particle x 8 + v 8 + rho 4 + area 4 +
+    key 4 + offsets 4 + sid 4 read, dpdt 4 + acc 8 written (52), 4 per CSR column read
+    (neighbor gathers are L1/L2 hits), per wall x 8 + vol/rho/p 12."""
+    P = int(batch.offsets[batch.n].item())
+    return batch.n * 52 + 4 * P + batch.nb * 20
+
+
+def phase_times(batch, reps=5):
+    """Mean milliseconds of each phase of one batch step (eager, events between the calls;
+    the step is run into scratch outputs so the batch state does not advance)."""
+    import ctypes
+    import torch
+    from pytorchsph_gb300 import _native as N
+    from pytorchsph_gb300.sim import FluidViewC
+    acc = {}
+    xo = torch.empty_like(batch.a["x"])
+    vo = torch.empty_like(batch.a["v"])
+    ro = torch.empty_like(batch.a["rho"])
+    for _ in range(reps):
+        e = [torch.cuda.Event(enable_timing=True) for _ in range(5)]
+        torch.cuda.synchronize()
+        e[0].record()
+        batch._sort_permute()
+        e[1].record()
+        batch._count()
+        e[2].record()
+        st = N.stream_ptr()
+        b = batch.b
+        N.call("sph_batch_nl_fill", N.ptr(b["x"]), N.ptr(b["sup"]), batch.n, N.ptr(batch.skeys),
+               N.ptr(batch.cell_start), N.ptr(batch.scenes), N.ptr(b["sid"]), N.ptr(batch.offsets), batch.pair_cap,
+               N.ptr(batch.cols), N.ptr(batch.status), st)
+        e[3].record()
+        fv = FluidViewC(N.ptr(b["x"]), N.ptr(b["v"]), N.ptr(b["rho"]), N.ptr(b["area"]), N.ptr(batch.skeys),
+                        N.ptr(batch.offsets), N.ptr(batch.cols), N.ptr(batch.cell_start), batch.n)
+        N.call("sph_batch_deltasph_step", ctypes.byref(fv), ctypes.byref(batch.wall_view), N.ptr(batch.scenes),
+               N.ptr(b["sid"]), N.ptr(batch.w["sid"]), N.ptr(batch.dpdt), N.ptr(batch.acc), N.ptr(batch.L),
+               N.ptr(batch.grad_rho), int(batch.any_renorm), N.ptr(xo), N.ptr(vo), N.ptr(ro), N.ptr(batch.status), st)
+        e[4].record()
+        torch.cuda.synchronize()
+        for k, name in enumerate(["sort+permute", "count+scan", "fill", "forces"]):
+            acc[name] = acc.get(name, 0.0) + e[k].elapsed_time(e[k + 1]) / reps
+    return acc
+
+
+def run_serving(args, dev, world, rank):
+    import torch
+    from pytorchsph_gb300.serve import SceneBatch, Server, Request
+    t_gen = time.perf_counter()
+    trace, specs = serving_specs(args.requests, args.trace_steps)
+    gen_s = time.perf_counter() - t_gen
+    total_p = sum(len(s.scene["pos"]) for s in specs)
+    budget = 60e9
+
+    # (a) device-resident batch of every request: W warm-up + K timed batch steps
+    batch = SceneBatch(specs, dev)
+    batch.capture()
+    for _ in range(max(args.warmup, 3)):
+        batch.step()
+    torch.cuda.synchronize()
+    batch.check()
+    st, en = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(dev.index or 0) as clk:
+        torch.cuda.synchronize()
+        st.record()
+        for _ in range(args.steps):
+            batch.step()
+        en.record()
+        torch.cuda.synchronize()
+    ms = st.elapsed_time(en) / args.steps
+    batch.check()
+    value = total_p * world / (ms / 1e3)
+    phases = phase_times(batch)
+    alg = forces_alg_bytes(batch)
+    peak, peak_src = hbm_peak()
+    achieved = alg / (phases["forces"] / 1e3) / 1e9 if phases.get("forces") else None
+    launches = batch.launches_per_step()
+    batch_bytes = batch.device_bytes()
+    del batch
+    for s in specs:
+        s.dev = None
+    torch.cuda.empty_cache()
+
+    # (b) one-scene-at-a-time GPU path on 16 requests spread over the sizes
+    order = sorted(range(len(specs)), key=lambda k: len(specs[k].scene["pos"]))
+    pick = sorted(set(order[int(q * (len(order) - 1))] for q in np.linspace(0, 1, 16)))
+    one = []
+    for k in pick:
+        b1 = SceneBatch([specs[k]], dev)
+        b1.capture()
+        for _ in range(3):
+            b1.step()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(20):
+            b1.step()
+        torch.cuda.synchronize()
+        one.append((len(specs[k].scene["pos"]), (time.perf_counter() - t0) / 20))
+        del b1
+        specs[k].dev = None
+    ln = np.log([n for n, _ in one])
+    lt = np.log([t for _, t in one])
+    t_of = lambda n: float(np.exp(np.interp(np.log(n), ln, lt)))
+    one_scene_time = sum(t_of(len(s.scene["pos"])) * s.steps for s in specs)
+    total_work = sum(len(s.scene["pos"]) * s.steps for s in specs)
+    one_scene_value = total_work / one_scene_time
+
+    e2e, realtime = None, None
+    if not args.no_trace:
+        # (c) end to end: every request queued at t = 0, continuous batching to completion
+        reqs = [Request(t["rid"], 0.0, specs[k]) for k, t in enumerate(trace)]
+        torch.cuda.synchronize()
+        srv = Server(dev, budget_bytes=budget, rebuild_every=50, keep_final=False)
+        wall = srv.run(reqs, time_scale=0.0, max_wall=600)
+        done = sum(r.steps_done >= r.spec.steps for r in reqs)
+        h2d = sum(s.scene["pos"].nbytes * 2 + s.scene["rho"].nbytes * 3 + s.scene["wall_pos"].nbytes * 2 +
+                  s.scene["wall_area"].nbytes for s in specs)
+        d2h = sum(s.scene["pos"].nbytes * 2 + s.scene["rho"].nbytes for s in specs)
+        e2e = {"value": srv.particle_steps / wall, "unit": "particle-steps/s",
+               "h2d_bytes_per_step": h2d / max(srv.batch_steps, 1), "d2h_bytes_per_step": d2h / max(srv.batch_steps, 1),
+               "wall_s": wall, "requests_completed": done, "batch_steps": srv.batch_steps, "rebuilds": srv.rebuilds,
+               "rebuild_s": srv.rebuild_seconds}
+        for s in specs:
+            s.dev = None
+        # (d) real-time trace: Poisson arrivals at 50 / s
+        reqs = [Request(t["rid"], t["arrival"], specs[k]) for k, t in enumerate(trace)]
+        srv = Server(dev, budget_bytes=budget, rebuild_every=20, keep_final=False)
+        wall = srv.run(reqs, time_scale=1.0, max_wall=600)
+        lat = srv.latency_percentiles((50, 99))
+        ttc = [r.finished - r.arrival for r in reqs if r.finished >= 0]
+        realtime = {"wall_s": wall, "particle_steps_per_s": srv.particle_steps / wall,
+                    "step_latency_ms_p50": lat[50] * 1e3 if lat[50] else None,
+                    "step_latency_ms_p99": lat[99] * 1e3 if lat[99] else None,
+                    "time_to_completion_s_p50": float(np.percentile(ttc, 50)) if ttc else None,
+                    "time_to_completion_s_p99": float(np.percentile(ttc, 99)) if ttc else None,
+                    "requests_completed": len(ttc), "rebuilds": srv.rebuilds, "rebuild_s": srv.rebuild_seconds}
+
+    cpu = cpu_baseline_serving() if rank == 0 and not args.no_cpu_baseline else None
+    if rank == 0:
+        line = base_line(args, world, value, ms, "particle-steps/s", {
+            "workload": "serving", "requests": len(specs), "trace_steps": args.trace_steps,
+            "particles_resident": total_p, "arrivals": "Poisson 50/s", "sizes": "log-uniform 2048-131072",
+            "mix": "50% dam break (aspect U[0.5,2]) / 50% oscillating drop (A U[0.5,2])",
+            "solver": "deltaSPH MOG, semi-implicit Euler, 3-layer walls", "budget_gb": budget / 1e9,
+            "batch_bytes": batch_bytes, "l2": f"state of {total_p} particles >> L2 (no flush needed)",
+            "graph": "one CUDA graph per batch step", "parallelism": f"replicas{world}",
+            "scene_generation_s": gen_s})
+        line["phases_ms"] = {k: round(v, 4) for k, v in phases.items()}
+        line["roofline"] = {"bound": "hbm", "kernel": "deltaSPH forces (k_batch_pass1)", "achieved": achieved,
+                            "peak": peak, "unit": "GB/s", "frac": achieved / peak if achieved else None,
+                            "traffic": traffic_from_profiles("serving", "k_batch_pass1"), "algorithmic_bytes": alg,
+                            "peak_source": peak_src}
+        line["serving"] = {"one_scene_gpu_path": {"value": one_scene_value, "unit": "particle-steps/s",
+                                                  "sample": [{"n": n, "ms_per_step": t * 1e3} for n, t in one]},
+                           "batched_over_one_scene": value / one_scene_value, "realtime_trace": realtime}
+        line["e2e"] = e2e or {"value": None, "unit": "particle-steps/s", "h2d_bytes_per_step": None,
+                              "d2h_bytes_per_step": None}
+        line["gpu_launches"] = launches * args.steps
+        line["clocks"] = clk.summary()
+        line["cpu_baseline"] = cpu
+        print(json.dumps(line), flush=True)
+
+
+# ----------------------------------------------------------------------------- GPU: search + density
+def run_search_density(args, dev, world, rank):
+    import torch
+    from pytorchsph_gb300 import _native as N
+    from pytorchsph_gb300 import workloads
+    from pytorchsph_gb300.search import GridSearch
+    pos, h, area, vmin, vmax, L = workloads.search_density_case(args.workload.rsplit("_", 1)[1])
     n = len(pos)
     pin = lambda a: torch.from_numpy(a).pin_memory()
     h_pos, h_h, h_a = pin(pos), pin(h), pin(area)
@@ -204,8 +401,7 @@ def run_ours(args):
     support = float(h[0])
     gs = GridSearch(dev, sort=args.sort, digit_bits=args.digit_bits)
     first = gs.run(d_pos, d_h, d_a, kernel_support=support, min_coord=vmin, max_coord=vmax)
-    cells = first.cell_capacity
-    P = first.num_pairs
+    cells, P = first.cell_capacity, first.num_pairs
     pair_cap = int(P * 1.05) + 1024
     rho_out = torch.empty(n, dtype=torch.float32, device=dev)
     events = {}
@@ -217,21 +413,17 @@ def run_ours(args):
         e.record()
 
     def step():
-        r = gs.run(d_pos, d_h, d_a, kernel_support=support, min_coord=vmin, max_coord=vmax,
-                   cell_capacity=cells, pair_capacity=pair_cap, sync=False, marks=marks)
+        r = gs.run(d_pos, d_h, d_a, kernel_support=support, min_coord=vmin, max_coord=vmax, cell_capacity=cells,
+                   pair_capacity=pair_cap, sync=False, marks=marks)
         N.call("sph_scatter_f32", N.ptr(r.order), N.ptr(r.rho), n, N.ptr(rho_out), N.stream_ptr())
         marks("end")
         return r
 
-    # kernels per step: grid 2, keys 1, sort (counting: scan 3 + scatter + fix + fix_large = 6,
-    # plus one memset; radix: passes x 5 + cell starts), gather 1, count 1, scan 3, fill 1,
-    # scatter 1 (and one torch fill of the status word)
     if args.sort == "counting":
         sort_launches = 6
     else:
         sort_launches = ((N.load().sph_key_bits(cells) + args.digit_bits - 1) // args.digit_bits) * 5 + 1
     launches_per_step = 2 + 1 + sort_launches + 1 + 1 + 3 + 1 + 1
-
     s = torch.cuda.Stream(dev)
     s.wait_stream(torch.cuda.current_stream())
     with torch.cuda.stream(s):
@@ -242,22 +434,17 @@ def run_ours(args):
     g = torch.cuda.CUDAGraph()
     with torch.cuda.graph(g):
         res = step()
-    flush = torch.empty(2 * 129 * 1024 * 1024 // 4 * 2, dtype=torch.float32, device=dev)  # 2x L2
+    flush = torch.empty(2 * 129 * 1024 * 1024 // 4 * 2, dtype=torch.float32, device=dev)
     for _ in range(max(args.warmup, 3)):
         g.replay()
     torch.cuda.synchronize()
     res.check()
-    assert res.num_pairs == P
-
+    names = ["start", "keys", "sort", "gather", "count", "scan", "fill", "end"]
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    phase_acc = {k: 0.0 for k in PHASES[1:]}
-    phase_ok = True
-    if world > 1:
-        dist.barrier()
-    torch.cuda.synchronize()
-    with ClockSampler(local) as clk:
-        t_wall0 = time.perf_counter()
+    phase_acc = {k: 0.0 for k in names[1:]}
+    ok = True
+    with ClockSampler(dev.index or 0) as clk:
         for k in range(args.steps):
             flush.zero_()
             starts[k].record()
@@ -265,42 +452,19 @@ def run_ours(args):
             ends[k].record()
             ends[k].synchronize()
             try:
-                for a_, b_ in zip(PHASES[:-1], PHASES[1:]):
+                for a_, b_ in zip(names[:-1], names[1:]):
                     phase_acc[b_] += events[a_].elapsed_time(events[b_])
             except Exception:
-                phase_ok = False
-        torch.cuda.synchronize()
-        t_wall = time.perf_counter() - t_wall0
-    if world > 1:
-        dist.barrier()
+                ok = False
     ms = sum(a.elapsed_time(b) for a, b in zip(starts, ends)) / args.steps
-    ms_t = torch.tensor([ms], dtype=torch.float64, device=dev)
-    if world > 1:
-        dist.all_reduce(ms_t, op=dist.ReduceOp.MAX)
-    ms = float(ms_t.item())
     value = n * world / (ms / 1e3)
-    phases = {k: v / args.steps for k, v in phase_acc.items()} if phase_ok else {}
+    phases = {k: v / args.steps for k, v in phase_acc.items()} if ok else {}
     dom = max(["count", "fill"], key=lambda k: phases.get(k, 0.0)) if phases else "fill"
-    dom_kernel = {"count": "nl_count", "fill": "nl_fill"}[dom]
-    alg = algorithmic_bytes(dom_kernel, n, P, cells)
-    peaks = {}
-    try:
-        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
-    except Exception:
-        pass
-    peak = float(peaks.get("hbm_gbs", 6800.0))
+    kern = {"count": "nl_count", "fill": "nl_fill"}[dom]
+    alg = n * 28 + 4 * (cells + 2) if kern == "nl_count" else n * 20 + 4 * P + 4 * (cells + 2)
+    peak, peak_src = hbm_peak()
     achieved = alg / (phases[dom] / 1e3) / 1e9 if phases else None
-    traffic = None
-    try:
-        prof = json.load(open(os.path.join(ROOT, "profiles", "traffic.json")))
-        traffic = prof.get(args.workload, {}).get(dom_kernel)
-    except Exception:
-        pass
-
-    # end to end through the public API from pinned host memory
     e2e_ms = []
-    h2d = h_pos.numel() * 4 + h_h.numel() * 4 + h_a.numel() * 4
-    d2h = n * 4 + 4
     rho_host = torch.empty(n, dtype=torch.float32).pin_memory()
     cnt_host = torch.empty(1, dtype=torch.int32).pin_memory()
     for k in range(args.steps + 2):
@@ -316,35 +480,127 @@ def run_ours(args):
         if k >= 2:
             e2e_ms.append((time.perf_counter() - t0) * 1e3)
     assert int(cnt_host[0]) == P
-    e2e_value = n * world / (statistics.mean(e2e_ms) / 1e3)
-
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
-        v, cores, reps_cpu = time_cpu(pos, h, area, vmin, vmax, L)
-        cpu = {"value": v, "unit": "particles/s", "cores": cores, "kind": "port",
-               "sample": f"{reps_cpu} full steps of {args.workload} (N={n}) with the oracle port "
-                         f"(oracle/nsearch_oracle.c, OpenMP)"}
-
+        threads = os.cpu_count() or 1
+        reps, tt = 0, 0.0
+        while reps < 10 and (reps < 1 or tt < 20.0):
+            t0 = time.perf_counter()
+            cpu_search_density(pos, h, area, vmin, vmax, L, threads)
+            tt += time.perf_counter() - t0
+            reps += 1
+        cpu = {"value": n * reps / tt, "unit": "particles/s", "cores": threads, "kind": "port",
+               "sample": f"{reps} full steps of {args.workload} (N={n}) with the oracle port (OpenMP)"}
     if rank == 0:
-        line = {"metric": METRIC, "value": value, "unit": "particles/s", "n_gpus": world, "steps": args.steps,
-                "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-                "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-                "config": {"workload": args.workload, "particles": n, "pairs": P, "cells": cells,
-                           "support": "3dx", "sort": args.sort,
-                           "l2": "flushed between timed steps (flush not timed)",
-                           "graph": "one CUDA graph per step", "parallelism": f"replicas{world}"},
-                "phases_ms": {k: round(v, 5) for k, v in phases.items()},
-                "roofline": {"bound": "hbm", "kernel": dom_kernel, "achieved": achieved, "peak": peak,
-                             "unit": "GB/s", "frac": (achieved / peak) if achieved else None, "traffic": traffic,
-                             "algorithmic_bytes": alg,
-                             "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback"},
-                "e2e": {"value": e2e_value, "unit": "particles/s", "h2d_bytes_per_step": h2d,
-                        "d2h_bytes_per_step": d2h},
-                "gpu_launches": launches_per_step * args.steps,
-                "clocks": clk.summary(), "wall_s_timed_loop": t_wall,
-                "cpu_baseline": cpu}
+        line = base_line(args, world, value, ms, "particles/s", {
+            "workload": args.workload, "particles": n, "pairs": P, "cells": cells, "support": "3dx", "sort": args.sort,
+            "l2": "flushed between timed steps (flush not timed)", "graph": "one CUDA graph per step",
+            "parallelism": f"replicas{world}"})
+        line["phases_ms"] = {k: round(v, 5) for k, v in phases.items()}
+        line["roofline"] = {"bound": "hbm", "kernel": kern, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                            "frac": achieved / peak if achieved else None,
+                            "traffic": traffic_from_profiles(args.workload, kern), "algorithmic_bytes": alg,
+                            "peak_source": peak_src}
+        line["e2e"] = {"value": n * world / (statistics.mean(e2e_ms) / 1e3), "unit": "particles/s",
+                       "h2d_bytes_per_step": 16 * n, "d2h_bytes_per_step": 4 * n + 4}
+        line["gpu_launches"] = launches_per_step * args.steps
+        line["clocks"] = clk.summary()
+        line["cpu_baseline"] = cpu
         print(json.dumps(line), flush=True)
+
+
+# ----------------------------------------------------------------------------- GPU: single dam breaks
+def run_dambreak(args, dev, world, rank):
+    import torch
+    from pytorchsph_gb300 import workloads
+    from pytorchsph_gb300.sim import SimConfig, Simulation
+    from pytorchsph_gb300.serve import SceneBatch, SceneSpec
+    cpu = None
+    if args.workload == "dambreak_deltasph":
+        sc = workloads.dam_break(64, 128, 0.01, (4.0, 2.0))
+        c0 = float(10 * np.sqrt(2 * 9.81 * sc["column_height"]))
+        cfg = SimConfig(solver="deltaSPH", integration="semiImplicitEuler", dt=0.25 * sc["h"] / c0, c0=c0,
+                        density_diffusion="deltaSPH")
+        b = SceneBatch([SceneSpec(sc, cfg, 500)], dev)
+        b.capture()
+        for _ in range(max(args.warmup, 3)):
+            b.step()
+        torch.cuda.synchronize()
+        with ClockSampler(dev.index or 0) as clk:
+            st, en = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            st.record()
+            for _ in range(args.steps):
+                b.step()
+            en.record()
+            torch.cuda.synchronize()
+        b.check()
+        ms = st.elapsed_time(en) / args.steps
+        n, launches = b.n, b.launches_per_step()
+        config = {"workload": args.workload, "particles": n, "walls": b.nb,
+                  "solver": "deltaSPH renormalized, semi-implicit Euler", "c0": c0, "graph": "one CUDA graph per step"}
+        if rank == 0 and not args.no_cpu_baseline:
+            t = cpu_deltasph_steps(sc, {"c0": c0, "dt": cfg.dt}, 2, "deltaSPH")
+            cpu = {"value": n * 2 / t, "unit": "particle-steps/s", "cores": torch.get_num_threads(), "kind": "port",
+                   "sample": "2 steps of the same scene with the restated reference step (float32, torch CPU)"}
+    else:
+        sc = workloads.dam_break(512, 512, 0.002, (4.096, 2.048))
+        cfg = SimConfig(solver="dfsph", integration="semiImplicitEuler", dt=2e-4, c0=float(10 * np.sqrt(2 * 9.81 * 1.024)),
+                        kinematic=0.01, fixed_dt=False, dt_min=1e-6, dt_max=1e-3, density_threshold=1e-4,
+                        divergence_threshold=1e-3, max_density_iters=100, max_divergence_iters=100)
+        sim = Simulation(sc, cfg, dev)
+        for _ in range(max(args.warmup, 3)):
+            sim.step(sync=False)
+        torch.cuda.synchronize()
+        with ClockSampler(dev.index or 0) as clk:
+            st, en = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            st.record()
+            for _ in range(args.steps):
+                sim.step(sync=False)
+            en.record()
+            torch.cuda.synchronize()
+        sim.check()
+        ms = st.elapsed_time(en) / args.steps
+        n, launches = sim.n, 40
+        config = {"workload": args.workload, "particles": n, "walls": sim.nb,
+                  "solver": "DFSPH, divergence + density solves, semi-implicit Euler, adaptive dt",
+                  "density_iters_last": int(sim.last["density_iters"].item())}
+    value = n * world / (ms / 1e3)
+    if rank == 0:
+        line = base_line(args, world, value, ms, "particle-steps/s", config)
+        peak, peak_src = hbm_peak()
+        line["roofline"] = {"bound": "hbm", "kernel": "step", "achieved": None, "peak": peak, "unit": "GB/s",
+                            "frac": None, "traffic": None, "peak_source": peak_src}
+        line["e2e"] = {"value": None, "unit": "particle-steps/s", "h2d_bytes_per_step": None, "d2h_bytes_per_step": None}
+        line["gpu_launches"] = launches * args.steps
+        line["clocks"] = clk.summary()
+        line["cpu_baseline"] = cpu
+        print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import torch
+    import torch.distributed as dist
+    rank, world, local = dist_env()
     if world > 1:
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    from pytorchsph_gb300 import build as B
+    B.build()
+    from pytorchsph_gb300 import _native as N
+    N.load()
+    if world > 1:
+        dist.barrier()
+    if args.workload == "serving":
+        run_serving(args, dev, world, rank)
+    elif args.workload.startswith("search_density_"):
+        run_search_density(args, dev, world, rank)
+    elif args.workload in ("dambreak_deltasph", "dambreak_dfsph"):
+        run_dambreak(args, dev, world, rank)
+    else:
+        raise SystemExit(f"unknown workload {args.workload}")
+    if world > 1:
+        dist.barrier()
         dist.destroy_process_group()
 
 

@@ -78,6 +78,22 @@ class SceneSpec:
     cfg: SimConfig
     steps: int = 1000
     name: str = ""
+    dev: dict | None = field(default=None, repr=False)   # device copies + grid, made once
+
+    def on_device(self, device):
+        """The scene's arrays on `device` and its grid (host copies of the sph_grid), cached."""
+        if self.dev is None or self.dev["device"] != device:
+            sc = self.scene
+            t = lambda a: torch.as_tensor(np.ascontiguousarray(a, np.float32), device=device)
+            n = len(sc["pos"])
+            nb = len(sc.get("wall_pos", ()))
+            self.dev = {"device": device, "n": n, "nb": nb, "pos": t(sc["pos"]).reshape(n, 2),
+                        "vel": t(sc["vel"]).reshape(n, 2), "rho": t(sc["rho"]), "area": t(sc["area"]),
+                        "sup": t(sc["support"]), "grid": scene_grid(sc, device)}
+            if nb:
+                self.dev.update({"wall_pos": t(sc["wall_pos"]).reshape(nb, 2),
+                                 "ghost_pos": t(sc["ghost_pos"]).reshape(nb, 2), "wall_area": t(sc["wall_area"])})
+        return self.dev
 
 
 class SceneBatch:
@@ -97,12 +113,14 @@ class SceneBatch:
         self.p_off = [0]
         total_cells = 0
         self.any_renorm = False
+        as_dev = lambda a: torch.as_tensor(a, device=dev, dtype=torch.float32)
         for s, spec in enumerate(self.specs):
-            sc, cfg = spec.scene, spec.cfg
+            cfg = spec.cfg
             if cfg.solver != "deltaSPH" or cfg.integration != "semiImplicitEuler":
                 raise N.SPHError("batched serving runs deltaSPH with semi-implicit Euler")
-            g = scene_grid(sc, dev)
-            h = float(np.float32(sc["support"][0]))
+            d = spec.on_device(dev)
+            g = d["grid"]
+            h = float(np.float32(spec.scene["support"][0]))
             P = _params_for(cfg, h, g.num_cells)
             buf = ctypes.create_string_buffer(rec)
             N.check(self.lib.sph_scene_encode(ctypes.byref(P), ctypes.byref(g), total_cells, cfg.dt, buf),
@@ -113,31 +131,28 @@ class SceneBatch:
             total_cells += g.num_cells
             self.any_renorm |= cfg.density_diffusion == "deltaSPH"
             st = states[s] if states is not None else None
-            n = len(sc["pos"])
-            pos.append(st["x"] if st else sc["pos"])
-            vel.append(st["v"] if st else sc["vel"])
-            rho.append(st["rho"] if st else sc["rho"])
-            area.append(sc["area"])
-            sup.append(sc["support"])
-            sid.append(np.full(n, s, np.int32))
-            uid.append(np.arange(n, dtype=np.int32))
+            n = d["n"]
+            pos.append(as_dev(st["x"]).reshape(n, 2) if st else d["pos"])
+            vel.append(as_dev(st["v"]).reshape(n, 2) if st else d["vel"])
+            rho.append(as_dev(st["rho"]) if st else d["rho"])
+            area.append(d["area"])
+            sup.append(d["sup"])
+            sid.append(torch.full((n,), s, dtype=torch.int32, device=dev))
+            uid.append(torch.arange(n, dtype=torch.int32, device=dev))
             self.p_off.append(self.p_off[-1] + n)
-            nb = len(sc.get("wall_pos", ()))
-            if nb:
-                wpos.append(sc["wall_pos"])
-                wgh.append(sc["ghost_pos"])
-                war.append(sc["wall_area"])
-                wsid.append(np.full(nb, s, np.int32))
+            if d["nb"]:
+                wpos.append(d["wall_pos"])
+                wgh.append(d["ghost_pos"])
+                war.append(d["wall_area"])
+                wsid.append(torch.full((d["nb"],), s, dtype=torch.int32, device=dev))
         if total_cells >= MAX_CELLS:
             raise N.SPHError("batch cell tables too large")
         self.cap = max(total_cells, 1)
         self.scenes = torch.frombuffer(bytearray(table), dtype=torch.uint8).to(dev)
         self.n = self.p_off[-1]
         n = self.n
-        cat = lambda xs, dt_: torch.as_tensor(np.ascontiguousarray(np.concatenate(xs), dt_), device=dev)
-        self.a = {"x": cat(pos, np.float32).reshape(n, 2), "v": cat(vel, np.float32).reshape(n, 2),
-                  "rho": cat(rho, np.float32), "area": cat(area, np.float32), "sup": cat(sup, np.float32),
-                  "sid": cat(sid, np.int32), "uid": cat(uid, np.int32)}
+        self.a = {"x": torch.cat(pos), "v": torch.cat(vel), "rho": torch.cat(rho), "area": torch.cat(area),
+                  "sup": torch.cat(sup), "sid": torch.cat(sid), "uid": torch.cat(uid)}
         self.b = {k: torch.empty_like(v) for k, v in self.a.items()}
         self.ws = Workspace(dev)
         self.status = torch.zeros(1, dtype=torch.int32, device=dev)
@@ -176,9 +191,8 @@ class SceneBatch:
                       "rho": z.clone(), "vol": z.clone(), "p": z.clone(), "sid": torch.zeros(1, dtype=torch.int32, device=dev),
                       "cell_start": torch.zeros(self.cap + 2, dtype=torch.int32, device=dev), "order": None}
         else:
-            cat = lambda xs, dt_: torch.as_tensor(np.ascontiguousarray(np.concatenate(xs), dt_), device=dev)
-            x = cat(wpos, np.float32).reshape(nb, 2)
-            sid = cat(wsid, np.int32)
+            x = torch.cat(wpos)
+            sid = torch.cat(wsid)
             keys = torch.empty(nb, dtype=torch.int32, device=dev)
             order = torch.empty(nb, dtype=torch.int32, device=dev)
             skeys = torch.empty(nb, dtype=torch.int32, device=dev)
@@ -192,7 +206,7 @@ class SceneBatch:
             N.call("sph_counting_sort", N.ptr(keys), nb, self.cap, N.ptr(hist), N.ptr(cs), N.ptr(order), N.ptr(skeys),
                    N.ptr(self.status), N.ptr(scr), scr.numel() * 8, st)
             perm = lambda t: self._perm(order, t)
-            self.w = {"x": perm(x), "ghost": perm(cat(wgh, np.float32).reshape(nb, 2)), "area": perm(cat(war, np.float32)),
+            self.w = {"x": perm(x), "ghost": perm(torch.cat(wgh)), "area": perm(torch.cat(war)),
                       "sid": perm(sid), "cell_start": cs, "rho": torch.ones(nb, device=dev),
                       "vol": torch.zeros(nb, device=dev), "p": torch.zeros(nb, device=dev), "order": order}
         self.wall_view = WallViewC(N.ptr(self.w["x"]), N.ptr(self.w["ghost"]), N.ptr(self.w["area"]),
@@ -283,8 +297,8 @@ class SceneBatch:
             raise N.SPHError("batch step: neighbor pair buffer too small")
 
     # ------------------------------------------------------------------ output
-    def scene_state(self, s: int):
-        """Positions, velocities and densities of scene s in its original particle order."""
+    def scene_state_device(self, s: int):
+        """Positions, velocities and densities of scene s in its original particle order (device)."""
         lo, hi = self.p_off[s], self.p_off[s + 1]
         uid = self.a["uid"][lo:hi].long()
         out = {}
@@ -292,8 +306,12 @@ class SceneBatch:
             t = self.a[k][lo:hi]
             o = torch.empty_like(t)
             o[uid] = t
-            out[k] = o.cpu().numpy()
+            out[k] = o
         return out
+
+    def scene_state(self, s: int):
+        """Positions, velocities and densities of scene s in its original particle order (numpy)."""
+        return {k: v.cpu().numpy() for k, v in self.scene_state_device(s).items()}
 
     def device_bytes(self):
         tot = 0
@@ -348,11 +366,12 @@ class Server:
         states, keep = [], []
         if self.batch is not None:
             for s, r in enumerate(self.live):
-                st = self.batch.scene_state(s)
+                st = self.batch.scene_state_device(s)
                 if r.steps_done >= r.spec.steps:
                     r.finished = now
                     if self.keep_final:
-                        r.final = st
+                        r.final = {k: v.cpu().numpy() for k, v in st.items()}
+                    r.spec.dev = None          # release the scene's device copies
                 else:
                     keep.append(r)
                     states.append(st)
