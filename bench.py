@@ -168,8 +168,8 @@ def cpu_baseline_serving(steps=3):
     import torch
     from pytorchsph_gb300 import workloads
     sc, p = workloads.make_request_scene({"kind": "dam_break", "n": 2048, "shape": 1.0})
-    cpu_deltasph_steps(sc, p, 1)
-    t = cpu_deltasph_steps(sc, p, steps)
+    cpu_deltasph_steps(sc, p, 1, p["diffusion"])
+    t = cpu_deltasph_steps(sc, p, steps, p["diffusion"])
     n = len(sc["pos"])
     return {"value": n * steps / t, "unit": "particle-steps/s", "cores": torch.get_num_threads(), "kind": "port",
             "sample": f"{steps} semi-implicit-Euler deltaSPH steps of a {n}-particle dam-break request with the "
@@ -219,7 +219,7 @@ def serving_specs(n_requests, steps):
     for t in trace:
         sc, p = workloads.make_request_scene(t)
         cfg = SimConfig(solver="deltaSPH", integration="semiImplicitEuler", dt=p["dt"], c0=p["c0"],
-                        gravity=p["gravity"], point_source=p["point_source"], density_diffusion="MOG")
+                        gravity=p["gravity"], point_source=p["point_source"], density_diffusion=p["diffusion"])
         specs.append(SceneSpec(sc, cfg, t["steps"], name=f"r{t['rid']}"))
     return trace, specs
 
@@ -258,7 +258,7 @@ def phase_times(batch, reps=5):
                N.ptr(batch.cols), N.ptr(batch.status), st)
         e[3].record()
         fv = FluidViewC(N.ptr(b["x"]), N.ptr(b["v"]), N.ptr(b["rho"]), N.ptr(b["area"]), N.ptr(batch.skeys),
-                        N.ptr(batch.offsets), N.ptr(batch.cols), N.ptr(batch.cell_start), batch.n)
+                        N.ptr(batch.offsets), N.ptr(batch.cols), N.ptr(batch.cell_start), batch.n, batch.pair_cap)
         N.call("sph_batch_deltasph_step", ctypes.byref(fv), ctypes.byref(batch.wall_view), N.ptr(batch.scenes),
                N.ptr(b["sid"]), N.ptr(batch.w["sid"]), N.ptr(batch.dpdt), N.ptr(batch.acc), N.ptr(batch.L),
                N.ptr(batch.grad_rho), int(batch.any_renorm), N.ptr(xo), N.ptr(vo), N.ptr(ro), N.ptr(batch.status), st)
@@ -338,14 +338,15 @@ def run_serving(args, dev, world, rank):
         torch.cuda.synchronize()
         srv = Server(dev, budget_bytes=budget, rebuild_every=50, keep_final=False)
         wall = srv.run(reqs, time_scale=0.0, max_wall=600)
-        done = sum(r.steps_done >= r.spec.steps for r in reqs)
+        done = sum(r.steps_done >= r.spec.steps and r.error is None for r in reqs)
         h2d = sum(s.scene["pos"].nbytes * 2 + s.scene["rho"].nbytes * 3 + s.scene["wall_pos"].nbytes * 2 +
                   s.scene["wall_area"].nbytes for s in specs)
         d2h = sum(s.scene["pos"].nbytes * 2 + s.scene["rho"].nbytes for s in specs)
         e2e = {"value": srv.particle_steps / wall, "unit": "particle-steps/s",
                "h2d_bytes_per_step": h2d / max(srv.batch_steps, 1), "d2h_bytes_per_step": d2h / max(srv.batch_steps, 1),
                "wall_s": wall, "requests_completed": done, "batch_steps": srv.batch_steps, "rebuilds": srv.rebuilds,
-               "rebuild_s": srv.rebuild_seconds}
+               "rebuild_s": srv.rebuild_seconds, "requests_failed": len(srv.failed),
+               "pair_overflows": srv.pair_overflows, "particles_escaped": int(sum(r.escaped for r in reqs))}
         for s in specs:
             s.dev = None
         # (d) real-time trace: Poisson arrivals at 50 / s
@@ -353,13 +354,14 @@ def run_serving(args, dev, world, rank):
         srv = Server(dev, budget_bytes=budget, rebuild_every=20, keep_final=False)
         wall = srv.run(reqs, time_scale=1.0, max_wall=600)
         lat = srv.latency_percentiles((50, 99))
-        ttc = [r.finished - r.arrival for r in reqs if r.finished >= 0]
+        ttc = [r.finished - r.arrival for r in reqs if r.finished >= 0 and r.error is None]
         realtime = {"wall_s": wall, "particle_steps_per_s": srv.particle_steps / wall,
                     "step_latency_ms_p50": lat[50] * 1e3 if lat[50] else None,
                     "step_latency_ms_p99": lat[99] * 1e3 if lat[99] else None,
                     "time_to_completion_s_p50": float(np.percentile(ttc, 50)) if ttc else None,
                     "time_to_completion_s_p99": float(np.percentile(ttc, 99)) if ttc else None,
-                    "requests_completed": len(ttc), "rebuilds": srv.rebuilds, "rebuild_s": srv.rebuild_seconds}
+                    "requests_completed": len(ttc), "requests_failed": len(srv.failed),
+                    "rebuilds": srv.rebuilds, "rebuild_s": srv.rebuild_seconds}
 
     cpu = cpu_baseline_serving() if rank == 0 and not args.no_cpu_baseline else None
     if rank == 0:
@@ -367,7 +369,8 @@ def run_serving(args, dev, world, rank):
             "workload": "serving", "requests": len(specs), "trace_steps": args.trace_steps,
             "particles_resident": total_p, "arrivals": "Poisson 50/s", "sizes": "log-uniform 2048-131072",
             "mix": "50% dam break (aspect U[0.5,2]) / 50% oscillating drop (A U[0.5,2])",
-            "solver": "deltaSPH MOG, semi-implicit Euler, 3-layer walls", "budget_gb": budget / 1e9,
+            "solver": "deltaSPH (renormalized density diffusion), semi-implicit Euler, dt = 0.1 h / c0, "
+                      "3-layer walls", "budget_gb": budget / 1e9,
             "batch_bytes": batch_bytes, "l2": f"state of {total_p} particles >> L2 (no flush needed)",
             "graph": "one CUDA graph per batch step", "parallelism": f"replicas{world}",
             "scene_generation_s": gen_s})

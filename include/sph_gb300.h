@@ -87,6 +87,9 @@ typedef struct sph_fluid_view {
   const int32_t* cols;      /* [P] CSR columns (sorted indices) */
   const int32_t* cell_start;/* [cells+2] fluid cell table */
   int64_t n;
+  int64_t pair_capacity;    /* length of cols; a row ending past it was not filled (the fill
+                               flagged SPH_FLAG_PAIR_CAPACITY) and reads as empty; 0 = cols
+                               holds every row */
 } sph_fluid_view;
 
 /* Wall (ghost-particle boundary) particles sorted by their cell in the fluid grid. */
@@ -282,9 +285,10 @@ sph_status_t sph_permute(const uint32_t* order, int64_t n, int32_t elem_bytes, c
 
 /* ---------------------------------------------------------------- batch of independent scenes */
 /* Many scenes stepped together: their particles are concatenated in one array with a
- * per-particle scene index `sid`; scene s owns cells [cell_offset_s, cell_offset_s +
- * num_cells_s) of the shared cell tables, so (scene, cell) keys sort every scene into its
- * own contiguous range and scenes never interact.  The scene table is an array of opaque
+ * per-particle scene index `sid`; scene s owns the slots [cell_offset_s, cell_offset_s +
+ * num_cells_s] of the shared cell tables (its cells, then one outside slot for particles
+ * that left its grid or became non-finite: no neighbors, body forces only), so (scene,
+ * cell) keys sort every scene into its own contiguous range and scenes never interact.  The scene table is an array of opaque
  * records of sph_scene_bytes() bytes each, filled with sph_scene_encode and copied to the
  * device. */
 size_t sph_scene_bytes(void);
@@ -292,7 +296,9 @@ size_t sph_scene_bytes(void);
  * from sph_grid_build), its cell-table offset and its time step. */
 sph_status_t sph_scene_encode(const sph_params* params, const sph_grid* grid_host, int32_t cell_offset, float dt,
                               void* out_host);
-/* (scene, cell) keys + per-cell histogram for sph_counting_sort; cell_capacity = total cells. */
+/* (scene, cell) keys + per-cell histogram for sph_counting_sort; cell_capacity = the total
+ * slot count, sum over scenes of num_cells_s + 1.  Sets SPH_FLAG_OUT_OF_GRID /
+ * SPH_FLAG_NONFINITE for particles put in their scene's outside slot. */
 sph_status_t sph_batch_cell_keys(const float* pos, int64_t n, const int32_t* sid, const void* scenes,
                                  int32_t cell_capacity, uint32_t* keys, int32_t* cell_count, int32_t* status,
                                  void* stream);
@@ -305,7 +311,9 @@ sph_status_t sph_batch_nl_fill(const float* xy, const float* sorted_support, int
                                int64_t pair_capacity, int32_t* cols, int32_t* status, void* stream);
 /* One semi-implicit-Euler deltaSPH step of every scene of the batch: mDBC wall densities,
  * the right-hand side (as sph_deltasph_forces, each particle with its scene's parameters)
- * and the update with each scene's own dt, written to x_out / v_out / rho_out. */
+ * and the update with each scene's own dt, written to x_out / v_out / rho_out.  If
+ * SPH_FLAG_PAIR_CAPACITY is set in *status when the update runs (the fill overflowed),
+ * the step is not applied: the outputs are the sorted inputs unchanged. */
 sph_status_t sph_batch_deltasph_step(const sph_fluid_view* fluid, const sph_wall_view* walls, const void* scenes,
                                      const int32_t* sid, const int32_t* wall_sid, float* dpdt, float* acc, float* L,
                                      float* grad_rho, int32_t any_renormalized, float* x_out, float* v_out,

@@ -139,8 +139,11 @@ __global__ void k_cell_keys(const float2* __restrict__ pos, int64_t n, const sph
   if (cell_count) atomicAdd(cell_count + key, 1);
 }
 
-// Batch of scenes: key = coff_s + ix + cells_x_s * iy with scene s's own grid; particles
-// outside their scene's grid get the sentinel cell_capacity (the batch's total cell count).
+// Batch of scenes: key = coff_s + ix + cells_x_s * iy with scene s's own grid.  Scene s owns
+// the slots coff_s .. coff_s + num_cells_s: its cells, then one outside slot for particles
+// that left its grid (or became non-finite).  Those particles have no neighbors and move
+// under body forces only, and every scene stays one contiguous range of the sorted order.
+// A scene whose slots do not fit the table gets the sentinel cell_capacity.
 __global__ void k_batch_cell_keys(const float2* __restrict__ pos, int64_t n, const int32_t* __restrict__ sid,
                                   const SceneDev* __restrict__ scenes, int32_t cell_capacity,
                                   uint32_t* __restrict__ keys, int32_t* __restrict__ cell_count, int32_t* status) {
@@ -149,13 +152,14 @@ __global__ void k_batch_cell_keys(const float2* __restrict__ pos, int64_t n, con
   const SceneDev& S = scenes[sid[i]];
   const sph_grid& g = S.g;
   float2 p = pos[i];
-  uint32_t key = (uint32_t)cell_capacity;
+  const bool fits = S.coff >= 0 && S.coff + g.num_cells < cell_capacity;
+  uint32_t key = fits ? (uint32_t)(S.coff + g.num_cells) : (uint32_t)cell_capacity;
   if (!isfinite(p.x) || !isfinite(p.y)) {
     flag(status, SPH_FLAG_NONFINITE);
   } else {
     int ix = cell_coord(p.x, g.qmin[0], g.hmax);
     int iy = cell_coord(p.y, g.qmin[1], g.hmax);
-    if (ix >= 0 && iy >= 0 && ix < g.cells_x && iy < g.cells_y && S.coff + g.num_cells <= cell_capacity)
+    if (ix >= 0 && iy >= 0 && ix < g.cells_x && iy < g.cells_y && fits)
       key = (uint32_t)(S.coff + ix + g.cells_x * iy);
     else
       flag(status, SPH_FLAG_OUT_OF_GRID);

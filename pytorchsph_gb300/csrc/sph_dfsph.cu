@@ -142,7 +142,7 @@ __global__ void __launch_bounds__(128) k_dfsph_prepare(FluidView F, WallView W, 
   const float2 xi = F.x[i];
   const float2 vi = B.vstar[i];
   float k1x = 0.f, k1y = 0.f, k2 = 0.f, src = 0.f;
-  const int k0 = F.offsets[i], kn = F.offsets[i + 1];
+  const int k0 = F.offsets[i], kn = row_end(F, i, k0);
   for (int k = k0; k < kn; ++k) {
     const int j = __ldg(F.cols + k);
     const float2 xj = __ldg(F.x + j), vj = __ldg(B.vstar + j);
@@ -231,7 +231,7 @@ __device__ __forceinline__ float2 pressure_accel(const FluidView& F, const WallV
   const float ri = B.rho[i] * P.rho0;
   const float ppi = B.p[i] / (ri * ri);
   float ax = 0.f, ay = 0.f;
-  const int k0 = F.offsets[i], kn = F.offsets[i + 1];
+  const int k0 = F.offsets[i], kn = row_end(F, i, k0);
   for (int k = k0; k < kn; ++k) {
     const int j = __ldg(F.cols + k);
     const float2 xj = __ldg(F.x + j);
@@ -286,7 +286,7 @@ __global__ void __launch_bounds__(256) k_dfsph_solve(FluidView F, WallView W, co
     for (int i = tid; i < F.n; i += nthreads) {
       const float2 xi = F.x[i], pai = B.pa[i];
       float ks = 0.f;
-      const int k0 = F.offsets[i], kn = F.offsets[i + 1];
+      const int k0 = F.offsets[i], kn = row_end(F, i, k0);
       for (int k = k0; k < kn; ++k) {
         const int j = __ldg(F.cols + k);
         const float2 xj = __ldg(F.x + j), paj = B.pa[j];
@@ -378,7 +378,7 @@ __global__ void __launch_bounds__(128) k_dfsph_viscosity(FluidView F, WallView W
   const float2 xi = F.x[i], vi = F.v[i];
   const float rhoi = B.rho[i] * P.rho0;
   float vax = 0.f, vay = 0.f, lax = 0.f, lay = 0.f;
-  const int k0 = F.offsets[i], kn = F.offsets[i + 1];
+  const int k0 = F.offsets[i], kn = row_end(F, i, k0);
   for (int k = k0; k < kn; ++k) {
     const int j = __ldg(F.cols + k);
     const float2 xj = __ldg(F.x + j), vj = __ldg(F.v + j);

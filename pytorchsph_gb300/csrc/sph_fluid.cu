@@ -108,7 +108,7 @@ __device__ __forceinline__ void pass1_body(int i, const FluidView& F, const Wall
   float pax = 0.f, pay = 0.f, vax = 0.f, vay = 0.f, lax = 0.f, lay = 0.f;
   float l00 = 0.f, l01 = 0.f, l10 = 0.f, l11 = 0.f;
   const bool want_L = P.diffusion == 2;
-  const int k0 = F.offsets[i], k1 = F.offsets[i + 1];
+  const int k0 = F.offsets[i], k1 = row_end(F, i, k0);
   for (int k = k0; k < k1; ++k) {
     const int j = __ldg(F.cols + k);
     const float2 xj = __ldg(F.x + j), vj = __ldg(F.v + j);
@@ -219,7 +219,7 @@ __device__ __forceinline__ void gradrho_body(int i, const FluidView& F, const Wa
   const float2 xi = F.x[i];
   const float rhoi = F.rho[i] * P.rho0;
   float fx = 0.f, fy = 0.f;
-  const int k0 = F.offsets[i], k1 = F.offsets[i + 1];
+  const int k0 = F.offsets[i], k1 = row_end(F, i, k0);
   for (int k = k0; k < k1; ++k) {
     const int j = __ldg(F.cols + k);
     const float2 xj = __ldg(F.x + j);
@@ -260,7 +260,7 @@ __device__ __forceinline__ void diffusion_body(int i, const FluidView& F, const 
   const float2 xi = F.x[i], gi = grad_rho[i];
   const float rhoi = F.rho[i] * P.rho0;
   float acc = 0.f;
-  const int k0 = F.offsets[i], k1 = F.offsets[i + 1];
+  const int k0 = F.offsets[i], k1 = row_end(F, i, k0);
   for (int k = k0; k < k1; ++k) {
     const int j = __ldg(F.cols + k);
     const float2 xj = __ldg(F.x + j), gj = __ldg(grad_rho + j);
@@ -379,6 +379,12 @@ __global__ void k_batch_sie(int n, const int32_t* __restrict__ sid, const SceneD
                             float2* __restrict__ vo, float* __restrict__ ro, int32_t* status) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
+  if (*status & SPH_FLAG_PAIR_CAPACITY) {  // the neighbor list overflowed: the step is not applied
+    xo[i] = x[i];
+    vo[i] = v[i];
+    ro[i] = rho[i];
+    return;
+  }
   const SceneDev& S = scenes[sid[i]];
   sie_body(i, x, v, rho, a, dpdt, S.dt, S.P.rho0, 1, xo, vo, ro, status);
 }
@@ -493,7 +499,8 @@ sph_status_t sph_batch_deltasph_step(const sph_fluid_view* fluid, const sph_wall
                                      float* rho_out, int32_t* status, void* stream) {
   SPH_VIEW_CHECK(fluid);
   SPH_VIEW_CHECK(walls);
-  SPH_REQUIRE(scenes && sid && dpdt && acc && x_out && v_out && rho_out, "batch_deltasph_step: bad arguments");
+  SPH_REQUIRE(scenes && sid && dpdt && acc && x_out && v_out && rho_out && status,
+              "batch_deltasph_step: bad arguments");
   SPH_REQUIRE(walls->n == 0 || wall_sid, "batch_deltasph_step: walls need wall_sid");
   SPH_REQUIRE(!any_renormalized || (L && grad_rho), "batch_deltasph_step: deltaSPH diffusion needs L, grad_rho");
   const int n = (int)fluid->n;

@@ -199,9 +199,24 @@ struct FluidView {
   const int32_t* cols;
   const int32_t* cell_start;
   int n;
+  int pair_cap;  // 0: cols holds every row
 };
 
+// End of particle i's CSR row [offsets[i], end): a row that ends past the column buffer was
+// not filled and reads as empty, so no kernel reads a column that was never written.
+__device__ __forceinline__ int row_end(const FluidView& F, int i, int k0) {
+  const int k1 = F.offsets[i + 1];
+  return (F.pair_cap > 0 && k1 > F.pair_cap) ? k0 : k1;
+}
+
+// Cell coordinates of a grid key.  A key past the grid (a particle outside its grid) gives a
+// row far below the grid, so that every +-r cell window around it is empty.
 __device__ __forceinline__ void cell_of(uint32_t key, const sph_grid& g, int* cx, int* cy) {
+  if (key >= (uint32_t)g.num_cells) {
+    *cx = 0;
+    *cy = -(1 << 20);
+    return;
+  }
   *cx = (int)(key % (uint32_t)g.cells_x);
   *cy = (int)(key / (uint32_t)g.cells_x);
 }
@@ -259,6 +274,7 @@ static inline FluidView to_fluid(const sph_fluid_view* f) {
   F.cols = f->cols;
   F.cell_start = f->cell_start;
   F.n = (int)f->n;
+  F.pair_cap = f->pair_capacity > 0x7fffffff ? 0x7fffffff : (int)f->pair_capacity;
   return F;
 }
 

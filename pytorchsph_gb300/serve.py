@@ -128,7 +128,7 @@ class SceneBatch:
             table[s * rec:(s + 1) * rec] = buf.raw
             self.grids.append(g)
             self.coff.append(total_cells)
-            total_cells += g.num_cells
+            total_cells += g.num_cells + 1      # the scene's cells and its outside slot
             self.any_renorm |= cfg.density_diffusion == "deltaSPH"
             st = states[s] if states is not None else None
             n = d["n"]
@@ -149,6 +149,9 @@ class SceneBatch:
             raise N.SPHError("batch cell tables too large")
         self.cap = max(total_cells, 1)
         self.scenes = torch.frombuffer(bytearray(table), dtype=torch.uint8).to(dev)
+        # slot of each scene that holds its particles outside its grid
+        self.outside_slot = torch.tensor([c + g.num_cells for c, g in zip(self.coff, self.grids)] or [0],
+                                         dtype=torch.int64, device=dev)
         self.n = self.p_off[-1]
         n = self.n
         self.a = {"x": torch.cat(pos), "v": torch.cat(vel), "rho": torch.cat(rho), "area": torch.cat(area),
@@ -254,7 +257,7 @@ class SceneBatch:
                N.ptr(self.scenes), N.ptr(b["sid"]), N.ptr(self.offsets), self.pair_cap, N.ptr(self.cols),
                N.ptr(self.status), st)
         fv = FluidViewC(N.ptr(b["x"]), N.ptr(b["v"]), N.ptr(b["rho"]), N.ptr(b["area"]), N.ptr(self.skeys),
-                        N.ptr(self.offsets), N.ptr(self.cols), N.ptr(self.cell_start), n)
+                        N.ptr(self.offsets), N.ptr(self.cols), N.ptr(self.cell_start), n, self.pair_cap)
         N.call("sph_batch_deltasph_step", ctypes.byref(fv), ctypes.byref(self.wall_view), N.ptr(self.scenes),
                N.ptr(b["sid"]), N.ptr(self.w["sid"]), N.ptr(self.dpdt), N.ptr(self.acc), N.ptr(self.L),
                N.ptr(self.grad_rho), int(self.any_renorm), N.ptr(a["x"]), N.ptr(a["v"]), N.ptr(a["rho"]),
@@ -289,12 +292,32 @@ class SceneBatch:
             self.step_kernels()
         self.steps_done += 1
 
-    def check(self):
-        f = int(self.status.item())
+    # flags that leave every scene's result valid: particles that left their scene's grid
+    # (they move under body forces only, see escaped()), and a cell too large for the
+    # reproducible in-cell order (summation order only)
+    BENIGN = N.SPH_FLAG_OUT_OF_GRID | N.SPH_FLAG_CELL_ORDER
+
+    def flags(self) -> int:
+        return int(self.status.item())
+
+    def check(self, allow: int = BENIGN):
+        f = self.flags() & ~allow
         if f:
             raise N.SPHError(f"batch step: {N.decode_flags(f)}")
         if int(self.offsets[self.n].item()) > self.pair_cap:
             raise N.SPHError("batch step: neighbor pair buffer too small")
+
+    def escaped(self):
+        """Per scene, how many of its particles were outside its grid at the last sort."""
+        if not self.specs:
+            return np.zeros(0, np.int64)
+        cs = self.cell_start.long()
+        return (cs[self.outside_slot + 1] - cs[self.outside_slot]).cpu().numpy()
+
+    def scene_finite(self, s: int) -> bool:
+        lo, hi = self.p_off[s], self.p_off[s + 1]
+        return bool(torch.isfinite(self.a["x"][lo:hi]).all() and torch.isfinite(self.a["v"][lo:hi]).all()
+                    and torch.isfinite(self.a["rho"][lo:hi]).all())
 
     # ------------------------------------------------------------------ output
     def scene_state_device(self, s: int):
@@ -338,34 +361,62 @@ class Request:
     finished: float = -1.0
     steps_done: int = 0
     final: dict | None = None
+    escaped: int = 0            # particles outside the scene's grid at its last step
+    error: str | None = None    # set when the request was retired without completing
 
 
 class Server:
     """Continuous batching: admit arrived requests while the memory budget allows, step all
     live scenes together, retire each scene exactly when it reaches its step count (its
     final state is kept in `Request.final`).  Membership changes rebuild the batch (and its
-    CUDA graph) between steps; new arrivals wait at most `rebuild_every` batch steps."""
+    CUDA graph) between steps; new arrivals wait at most `rebuild_every` batch steps.
+
+    The batch status word is read after every step.  A step whose neighbor list overflowed
+    was not applied by the device: the batch is rebuilt with a fresh pair count (and more
+    headroom) and the step runs again.  A scene whose state became non-finite is retired
+    with `Request.error` set; the other scenes, which share no data with it, carry on."""
 
     def __init__(self, device=None, budget_bytes: float = 60e9, rebuild_every: int = 20, use_graph: bool = True,
-                 keep_final: bool = True):
+                 keep_final: bool = True, pair_headroom: float = 1.3):
         self.device = torch.device(device or torch.device("cuda", torch.cuda.current_device()))
         self.budget = budget_bytes
         self.rebuild_every = rebuild_every
         self.use_graph = use_graph
         self.keep_final = keep_final
+        self.pair_headroom = pair_headroom
         self.live: list[Request] = []
         self.batch: SceneBatch | None = None
         self.particle_steps = 0
         self.batch_steps = 0
         self.rebuilds = 0
+        self.pair_overflows = 0
+        self.failed: list[Request] = []
         self.step_latency = []      # (batch step seconds, live scenes) per batch step
         self.rebuild_seconds = 0.0
+        self._flags = torch.zeros(1, dtype=torch.int32, pin_memory=True)
+        self._last_flags = 0
+
+    def _read_flags(self) -> int:
+        """Wait for the batch's work and read its status word (4 bytes over a pinned buffer)."""
+        self._flags.copy_(self.batch.status, non_blocking=True)
+        torch.cuda.current_stream().synchronize()
+        self._last_flags = int(self._flags[0])
+        return self._last_flags
 
     def _rebuild(self, queue, now):
         t = time.perf_counter()
         states, keep = [], []
         if self.batch is not None:
+            nonfinite = bool(self._read_flags() & N.SPH_FLAG_NONFINITE)
+            escaped = self.batch.escaped()
             for s, r in enumerate(self.live):
+                r.escaped = int(escaped[s])
+                if nonfinite and not self.batch.scene_finite(s):
+                    r.error = "non-finite state"
+                    r.finished = now
+                    r.spec.dev = None
+                    self.failed.append(r)
+                    continue
                 st = self.batch.scene_state_device(s)
                 if r.steps_done >= r.spec.steps:
                     r.finished = now
@@ -387,21 +438,34 @@ class Server:
             used += need
         self.live = keep
         self.batch = None
+        self._last_flags = 0
         if keep:
-            self.batch = SceneBatch([r.spec for r in keep], self.device, states=states)
+            self.batch = SceneBatch([r.spec for r in keep], self.device, states=states,
+                                    pair_headroom=self.pair_headroom)
+            self.rebuilds += 1
             if self.use_graph:
                 self.batch.capture()          # runs one step eagerly, then records it
-                self._count_step(0.0)
-            self.rebuilds += 1
+                self._after_step(0.0, self._read_flags())
         self.rebuild_seconds += time.perf_counter() - t
 
-    def _count_step(self, seconds):
+    def _after_step(self, seconds, flags) -> bool:
+        """Book one batch step; False if the device did not apply it (neighbor list overflow)."""
+        if flags & N.SPH_FLAG_PAIR_CAPACITY:
+            self.pair_overflows += 1
+            self.pair_headroom *= 1.5
+            return False
         for r in self.live:
             r.steps_done += 1
         self.particle_steps += self.batch.n
         self.batch_steps += 1
         if seconds > 0:
             self.step_latency.append((seconds, len(self.live)))
+        return True
+
+    def _must_rebuild(self) -> bool:
+        f = self._last_flags
+        return bool(f & (N.SPH_FLAG_PAIR_CAPACITY | N.SPH_FLAG_NONFINITE)) or \
+            any(r.steps_done >= r.spec.steps for r in self.live)
 
     def run(self, requests, time_scale: float = 1.0, max_wall: float = 600.0):
         """Serve `requests` (arrival times scaled by time_scale); returns the wall seconds."""
@@ -414,22 +478,20 @@ class Server:
             now = time.perf_counter() - t0
             if now > max_wall:
                 break
-            done = any(r.steps_done >= r.spec.steps for r in self.live)
             arrived = bool(queue) and queue[0].arrival <= now
-            if self.batch is None or done or (arrived and since >= self.rebuild_every):
+            if self.batch is None or self._must_rebuild() or (arrived and since >= self.rebuild_every):
                 self._rebuild(queue, now)
                 since = 0
                 if self.batch is None:
                     if queue:
                         time.sleep(max(0.0, min(queue[0].arrival - (time.perf_counter() - t0), 0.01)))
                     continue
-                if any(r.steps_done >= r.spec.steps for r in self.live):
+                if self._must_rebuild():
                     continue
             t = time.perf_counter()
             self.batch.step()
-            torch.cuda.current_stream().synchronize()
-            self._count_step(time.perf_counter() - t)
-            since += 1
+            flags = self._read_flags()          # waits for the step
+            since += self._after_step(time.perf_counter() - t, flags)
         if self.batch is not None:
             self.batch.check()
         return time.perf_counter() - t0

@@ -40,7 +40,7 @@ class SphParamsC(ctypes.Structure):
 class FluidViewC(ctypes.Structure):
     _fields_ = [("x", ctypes.c_void_p), ("v", ctypes.c_void_p), ("rho", ctypes.c_void_p), ("area", ctypes.c_void_p),
                 ("keys", ctypes.c_void_p), ("offsets", ctypes.c_void_p), ("cols", ctypes.c_void_p),
-                ("cell_start", ctypes.c_void_p), ("n", ctypes.c_int64)]
+                ("cell_start", ctypes.c_void_p), ("n", ctypes.c_int64), ("pair_capacity", ctypes.c_int64)]
 
 
 class WallViewC(ctypes.Structure):
@@ -267,7 +267,8 @@ class Simulation:
         self.offsets = offsets
         self.rho_fluid = rho_fluid
         self.fluid_view = FluidViewC(N.ptr(self.arr["x"]), N.ptr(self.arr["v"]), N.ptr(self.arr["rho"]),
-                                     N.ptr(self.arr["area"]), N.ptr(skeys), N.ptr(offsets), N.ptr(self.cols), N.ptr(cs), n)
+                                     N.ptr(self.arr["area"]), N.ptr(skeys), N.ptr(offsets), N.ptr(self.cols), N.ptr(cs), n,
+                                     self.pair_cap)
 
     def rhs(self, sync=True):
         """Evaluate one timestep() at the current state; returns (acc, vel, dpdt or None)."""

@@ -15,7 +15,7 @@ def spec(kind, n, shape, steps=5):
     from pytorchsph_gb300.sim import SimConfig
     sc, p = workloads.make_request_scene({"kind": kind, "n": n, "shape": shape})
     cfg = SimConfig(solver="deltaSPH", integration="semiImplicitEuler", dt=p["dt"], c0=p["c0"], gravity=p["gravity"],
-                    point_source=p["point_source"], density_diffusion="MOG")
+                    point_source=p["point_source"], density_diffusion=p["diffusion"])
     return SceneSpec(sc, cfg, steps)
 
 
@@ -95,3 +95,61 @@ def test_server_completes_small_trace(cuda):
     r = reqs[2]
     alone = run_batch([r.spec], r.spec.steps, cuda)[0]
     assert r.final is not None and same(alone, r.final)
+
+
+def test_particle_leaving_its_grid_keeps_scenes_apart(cuda):
+    """A particle thrown out of its scene's grid goes to that scene's outside slot: the scene
+    keeps its own particle range, the particle has no neighbors, and the scene's result is
+    still the same alone and in a mix."""
+    from pytorchsph_gb300 import _native as N
+    from pytorchsph_gb300.serve import SceneBatch, SceneSpec
+    A = spec("dam_break", 3000, 0.7)
+    B = spec("drop", 2500, 1.5)
+    sc = dict(B.scene)
+    pos, vel = sc["pos"].copy(), sc["vel"].copy()
+    pos[7] = (1.45, 0.0)                       # alone near the edge of the grid (domain +-1.5)
+    vel[7] = (200.0, 0.0)                      # ~0.1 m per step: outside after two steps
+    sc["pos"], sc["vel"] = pos, vel
+    Bx = SceneSpec(sc, B.cfg, B.steps)
+    b = SceneBatch([Bx, A], cuda)
+    for _ in range(6):
+        b.step()
+    b.check()                                  # leaving the grid is reported, not an error
+    assert b.flags() & N.SPH_FLAG_OUT_OF_GRID
+    esc = b.escaped()
+    assert list(esc) == [1, 0]
+    mix = [b.scene_state(0), b.scene_state(1)]
+    g = b.grids[0]
+    hi = g.qmin[0] + g.cells_x * g.hmax
+    assert mix[0]["x"][7, 0] > hi and np.isfinite(mix[0]["x"]).all()
+    assert same(run_batch([A], 6, cuda)[0], mix[1])
+    assert same(run_batch([Bx], 6, cuda)[0], mix[0])
+
+
+def test_pair_overflow_holds_the_step(cuda):
+    """With a column buffer too small for the neighbor list the fill writes only whole rows
+    that fit, no kernel reads past it, and the update leaves the state unchanged."""
+    from pytorchsph_gb300 import _native as N
+    from pytorchsph_gb300.serve import SceneBatch
+    A = spec("dam_break", 3000, 1.0)
+    b = SceneBatch([A], cuda, pair_headroom=0.5)
+    before = b.scene_state(0)
+    b.step()
+    assert b.flags() & N.SPH_FLAG_PAIR_CAPACITY
+    assert same(before, b.scene_state(0))
+    with pytest.raises(N.SPHError):
+        b.check()
+
+
+def test_server_recovers_from_pair_overflow(cuda):
+    """The request loop reruns a step the device did not apply, after a rebuild with more
+    pair headroom; results equal the scenes run alone."""
+    from pytorchsph_gb300.serve import Request, Server
+    A, B = spec("dam_break", 3000, 1.2, steps=5), spec("drop", 2600, 0.9, steps=7)
+    reqs = [Request(0, 0.0, A), Request(1, 0.0, B)]
+    srv = Server(cuda, rebuild_every=4, pair_headroom=0.5)
+    srv.run(reqs, time_scale=1.0, max_wall=120)
+    assert srv.pair_overflows >= 1
+    assert all(r.steps_done == r.spec.steps and r.error is None for r in reqs)
+    for r in reqs:
+        assert same(run_batch([r.spec], r.spec.steps, cuda)[0], r.final)
