@@ -260,8 +260,9 @@ def phase_times(batch, reps=5):
         fv = FluidViewC(N.ptr(b["x"]), N.ptr(b["v"]), N.ptr(b["rho"]), N.ptr(b["area"]), N.ptr(batch.skeys),
                         N.ptr(batch.offsets), N.ptr(batch.cols), N.ptr(batch.cell_start), batch.n, batch.pair_cap)
         N.call("sph_batch_deltasph_step", ctypes.byref(fv), ctypes.byref(batch.wall_view), N.ptr(batch.scenes),
-               N.ptr(b["sid"]), N.ptr(batch.w["sid"]), N.ptr(batch.dpdt), N.ptr(batch.acc), N.ptr(batch.L),
-               N.ptr(batch.grad_rho), int(batch.any_renorm), N.ptr(xo), N.ptr(vo), N.ptr(ro), N.ptr(batch.status), st)
+               N.ptr(b["sid"]), N.ptr(batch.w["sid"]), N.ptr(batch.dpdt), N.ptr(batch.acc), N.ptr(batch.grad_rho),
+               int(batch.any_renorm), N.ptr(xo), N.ptr(vo), N.ptr(ro), N.ptr(batch.status),
+               N.ptr(batch.forces_scratch), batch.forces_scratch.numel() * 8, st)
         e[4].record()
         torch.cuda.synchronize()
         for k, name in enumerate(["sort+permute", "count+scan", "fill", "forces"]):

@@ -260,13 +260,16 @@ sph_status_t sph_mdbc_wall_density(const sph_fluid_view* fluid, const sph_wall_v
 /* The deltaSPH right-hand side (deltaSPHSimulation.timestep steps 6-12, src/deltaSPH.py:146-200):
  * dpdt [n] = continuity (src/modules/momentum.py:13-19) + density diffusion (MOG
  * densityDiffusion.py:56-63, or the renormalized deltaSPH scheme :12-52 when
- * density_diffusion = 2, which needs L float4 [n] and grad_rho float2 [n] scratch);
- * acc float2 [n] = gravity + pressure (pressure.py:13-19) + artificial viscosity
- * (diffusion.py:12-25) + laminar viscosity (laminar.py:12-27), each with its wall part
- * (solidBoundary.py:746-890).  Wall quantities must come from sph_mdbc_wall_density. */
+ * density_diffusion = 2, which needs grad_rho float2 [n]; L float4 [n], optional, receives
+ * the renormalization matrix); acc float2 [n] = gravity + pressure (pressure.py:13-19) +
+ * artificial viscosity (diffusion.py:12-25) + laminar viscosity (laminar.py:12-27), each
+ * with its wall part (solidBoundary.py:746-890).  Wall quantities must come from
+ * sph_mdbc_wall_density.  scratch: sph_deltasph_scratch_bytes(n) bytes of device memory
+ * (per-particle neighbor records). */
+size_t sph_deltasph_scratch_bytes(int64_t n);
 sph_status_t sph_deltasph_forces(const sph_fluid_view* fluid, const sph_wall_view* walls, const sph_grid* grid,
                                  const sph_params* params, float* dpdt, float* acc, float* L, float* grad_rho,
-                                 void* stream);
+                                 void* scratch, size_t scratch_bytes, void* stream);
 /* semiImplicitEuler (src/simulationBase.py:647-652): v' = v + dt a, x' = x + dt (v + dt a),
  * rho' = rho + dt dpdt / rest_density when continuum_density.  dt is a device float. */
 sph_status_t sph_integrate_semi_implicit_euler(int64_t n, const float* x, const float* v, const float* rho,
@@ -313,11 +316,14 @@ sph_status_t sph_batch_nl_fill(const float* xy, const float* sorted_support, int
  * the right-hand side (as sph_deltasph_forces, each particle with its scene's parameters)
  * and the update with each scene's own dt, written to x_out / v_out / rho_out.  If
  * SPH_FLAG_PAIR_CAPACITY is set in *status when the update runs (the fill overflowed),
- * the step is not applied: the outputs are the sorted inputs unchanged. */
+ * the step is not applied: the outputs are the sorted inputs unchanged.  dpdt [n], acc
+ * float2 [n] and grad_rho float2 [n] carry the renormalized scenes' first pass to their
+ * diffusion pass (needed when any_renormalized); scratch as for sph_deltasph_forces. */
 sph_status_t sph_batch_deltasph_step(const sph_fluid_view* fluid, const sph_wall_view* walls, const void* scenes,
-                                     const int32_t* sid, const int32_t* wall_sid, float* dpdt, float* acc, float* L,
+                                     const int32_t* sid, const int32_t* wall_sid, float* dpdt, float* acc,
                                      float* grad_rho, int32_t any_renormalized, float* x_out, float* v_out,
-                                     float* rho_out, int32_t* status, void* stream);
+                                     float* rho_out, int32_t* status, void* scratch, size_t scratch_bytes,
+                                     void* stream);
 
 /* ---------------------------------------------------------------- DFSPH (a20-a25) */
 

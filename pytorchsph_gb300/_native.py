@@ -68,12 +68,13 @@ SIGNATURES.update({  # batch of scenes
     "sph_batch_cell_keys": (_I32, [_P, _I64, _P, _P, _I32, _P, _P, _P, _P]),
     "sph_batch_nl_count": (_I32, [_P, _P, _I64, _P, _P, _P, _P, _P, _P]),
     "sph_batch_nl_fill": (_I32, [_P, _P, _I64, _P, _P, _P, _P, _P, _I64, _P, _P, _P]),
-    "sph_batch_deltasph_step": (_I32, [_P] * 9 + [_I32] + [_P] * 5),
+    "sph_batch_deltasph_step": (_I32, [_P] * 8 + [_I32] + [_P] * 5 + [_SZ, _P]),
 })
 
 SIGNATURES.update({  # simulation kernels
     "sph_mdbc_wall_density": (_I32, [_P] * 5),
-    "sph_deltasph_forces": (_I32, [_P] * 9),
+    "sph_deltasph_scratch_bytes": (_SZ, [_I64]),
+    "sph_deltasph_forces": (_I32, [_P] * 8 + [_P, _SZ, _P]),
     "sph_integrate_semi_implicit_euler": (_I32, [_I64] + [_P] * 6 +
                                           [_F32, _I32] + [_P] * 5),
     "sph_rk_axpy": (_I32, [_I64] + [_P] * 7 + [_F32, _F32] +

@@ -94,100 +94,137 @@ __device__ __forceinline__ void mdbc_body(int b, const FluidView& F, const WallV
   W.p[b] = tait(rb, P);
 }
 
+// ---------------------------------------------------------------------------- neighbor records
+// What neighbor j brings to every pair term, computed once per particle instead of once
+// per pair: xv = (x, y, vx, vy) and q = (rho_j, V_j = A_j / rho~_j, p_j = Tait(rho~_j),
+// m_j = rho_j V_j).  Two 16-byte loads per pair replace four scalar loads, a division and
+// the Tait power.
+__device__ __forceinline__ void prep_body(int i, const FluidView& F, const SphParams& P, float4* __restrict__ xv,
+                                          float4* __restrict__ qv) {
+  const float2 x = F.x[i], v = F.v[i];
+  const float rt = F.rho[i];
+  const float V = F.area[i] / rt, rho = rt * P.rho0;
+  xv[i] = make_float4(x.x, x.y, v.x, v.y);
+  qv[i] = make_float4(rho, V, tait(rt, P), rho * V);
+}
+
+// Pair geometry with one reciprocal square root: d = x_i - x_j, e = d / r (0 when r < 1e-7),
+// q = r / h, r2 = |d|^2.
+struct PairGeo {
+  float dx, dy, ex, ey, q, r2;
+};
+
+__device__ __forceinline__ PairGeo pair_geo(float xi, float yi, float xj, float yj, float inv_h) {
+  PairGeo g;
+  g.dx = xi - xj;
+  g.dy = yi - yj;
+  g.r2 = g.dx * g.dx + g.dy * g.dy;
+  const float ir = g.r2 >= 1e-14f ? rsqrtf(g.r2) : 0.f;
+  g.ex = g.dx * ir;
+  g.ey = g.dy * ir;
+  g.q = g.r2 * ir * inv_h;
+  return g;
+}
+
 // ---------------------------------------------------------------------------- pass 1
 // dpdt (continuity + MOG), acceleration (gravity, pressure, artificial and laminar
-// viscosity) and, for the deltaSPH scheme, the normalization matrix L.
-__device__ __forceinline__ void pass1_body(int i, const FluidView& F, const WallView& W, const sph_grid& g,
-                                           const SphParams& P, int coff, float* __restrict__ dpdt,
-                                           float2* __restrict__ acc, float4* __restrict__ Lout) {
-  const float2 xi = F.x[i], vi = F.v[i];
-  const float rti = F.rho[i];
-  const float rhoi = rti * P.rho0;
-  const float pi = tait(rti, P);
+// viscosity) and, for the deltaSPH scheme, the renormalization matrix L_i and the density
+// gradient <grad rho>_i = -L_i^+ sum_j 2 (rho_j - rho_i) V_j gradW_ij (+ walls), all in one
+// sweep over the row: L_i^+ is applied to the summed vector once instead of to every term.
+struct Pass1 {
+  float dpdt, ax, ay;
+  float4 L;        // renormalization matrix, fluid + walls
+  float2 grad_rho;
+};
+
+__device__ __forceinline__ Pass1 pass1_body(int i, const FluidView& F, const float4* __restrict__ xv,
+                                            const float4* __restrict__ qv, const WallView& W, const sph_grid& g,
+                                            const SphParams& P, int coff) {
+  const float4 si = xv[i];
+  const float4 qi = qv[i];
+  const float rhoi = qi.x, pi = qi.z;
+  const bool renorm = P.diffusion == 2;
+  const float mu2 = 2.0f * rhoi * P.kinematic;
   float dp_f = 0.f, mog = 0.f;
   float pax = 0.f, pay = 0.f, vax = 0.f, vay = 0.f, lax = 0.f, lay = 0.f;
-  float l00 = 0.f, l01 = 0.f, l10 = 0.f, l11 = 0.f;
-  const bool want_L = P.diffusion == 2;
+  float l00 = 0.f, l01 = 0.f, l10 = 0.f, l11 = 0.f, gfx = 0.f, gfy = 0.f;
   const int k0 = F.offsets[i], k1 = row_end(F, i, k0);
   for (int k = k0; k < k1; ++k) {
     const int j = __ldg(F.cols + k);
-    const float2 xj = __ldg(F.x + j), vj = __ldg(F.v + j);
-    const float rtj = __ldg(F.rho + j), Aj = __ldg(F.area + j);
-    const float Vj = Aj / rtj, rhoj = rtj * P.rho0;
-    const Geo e = geo(xi.x, xi.y, xj.x, xj.y, P.inv_h);
+    const float4 sj = __ldg(xv + j), qj = __ldg(qv + j);
+    const float rhoj = qj.x, Vj = qj.y, pj = qj.z, mj = qj.w;
+    const PairGeo e = pair_geo(si.x, si.y, sj.x, sj.y, P.inv_h);
     const float gw = kGW(e.q, P.c_g);
     const float gx = gw * e.ex, gy = gw * e.ey;
-    const float ux = vj.x - vi.x, uy = vj.y - vi.y;   // u_j - u_i
+    const float ux = sj.z - si.z, uy = sj.w - si.w;   // u_j - u_i
     const float rx = -e.dx, ry = -e.dy;               // x_j - x_i
-    const float r2 = rx * rx + ry * ry + P.eps;
-    dp_f -= (ux * gx + uy * gy) * Vj * rhoj;
-    if (P.diffusion == 1) {
-      const float s = 2.0f * (rhoj - rhoi) / r2;
-      mog += (s * rx * gx + s * ry * gy) * Vj;
-    }
-    const float pj = tait(rtj, P);
+    const float ir2 = __fdividef(1.0f, e.r2 + P.eps);
+    const float rg = rx * gx + ry * gy;
+    dp_f -= (ux * gx + uy * gy) * mj;
+    if (P.diffusion == 1) mog += 2.0f * (rhoj - rhoi) * ir2 * rg * Vj;
     const float pf = (pi + pj) * Vj;
     pax += pf * gx;
     pay += pf * gy;
-    float pij = ux * rx + uy * ry;
-    pij = fminf(pij, 0.f) / r2;
-    const float vf = pij * Vj * rhoj / (rhoi + rhoj);
+    const float irs = __fdividef(1.0f, rhoi + rhoj);
+    const float vf = fminf(ux * rx + uy * ry, 0.f) * ir2 * mj * irs;
     vax += vf * gx;
     vay += vf * gy;
-    const float mj = rhoj * Vj;
-    const float mu2 = 2.0f * rhoi * P.kinematic;
-    const float rs = rhoi + rhoj;
-    const float term = 4.0f * mj * mu2 * (rx * gx + ry * gy) / (rs * rs * r2);
-    lax -= term * (vi.x - vj.x);
-    lay -= term * (vi.y - vj.y);
-    if (want_L) {
+    const float term = 4.0f * mj * mu2 * rg * irs * irs * ir2;   // laminar: -term (u_i - u_j)
+    lax += term * ux;
+    lay += term * uy;
+    if (renorm) {
       l00 += Vj * rx * gx;
       l01 += Vj * rx * gy;
       l10 += Vj * ry * gx;
       l11 += Vj * ry * gy;
+      const float s = 2.0f * (rhoj - rhoi) * Vj;
+      gfx += s * gx;
+      gfy += s * gy;
     }
   }
   float dp_w = 0.f, pwx = 0.f, pwy = 0.f, vwx = 0.f, vwy = 0.f;
-  float w00 = 0.f, w01 = 0.f, w10 = 0.f, w11 = 0.f;
+  float w00 = 0.f, w01 = 0.f, w10 = 0.f, w11 = 0.f, gwx = 0.f, gwy = 0.f;
   if (W.n > 0) {
     int cx, cy;
     cell_of(F.keys[i] - (uint32_t)coff, g, &cx, &cy);
     const float thr = sq_threshold(P.h);
     for_each_wall(
-        W, g, P.search_radius, cx, cy, xi.x, xi.y, thr,
+        W, g, P.search_radius, cx, cy, si.x, si.y, thr,
         [&](int b, float2 xb) {
-          const Geo e = geo(xi.x, xi.y, xb.x, xb.y, P.inv_h);   // fluid side: e = (x_f - x_b)/r
+          const PairGeo e = pair_geo(si.x, si.y, xb.x, xb.y, P.inv_h);   // fluid side: e = (x_f - x_b)/r
           const float gw = kGW(e.q, P.c_g);
           const float gx = gw * e.ex, gy = gw * e.ey;
           const float Vb = W.vol[b], rhob = W.rho[b] * P.rho0, pb = W.p[b];
-          const float ux = -vi.x, uy = -vi.y;               // u_b - u_f, walls at rest
+          const float ux = -si.z, uy = -si.w;               // u_b - u_f, walls at rest
           dp_w -= (ux * gx + uy * gy) * Vb * rhob;
           const float pf = (pi + pb) * Vb;
           pwx += pf * gx;
           pwy += pf * gy;
           const float rx = -e.dx, ry = -e.dy;               // x_b - x_f
           if (P.boundary_diffusion) {
-            const float r2 = rx * rx + ry * ry + P.eps;
-            float pij = fminf(ux * rx + uy * ry, 0.f) / r2;
-            const float vf = pij * Vb * rhob / (rhoi + rhob);
+            const float vf = fminf(ux * rx + uy * ry, 0.f) * __fdividef(1.0f, e.r2 + P.eps) * Vb * rhob *
+                             __fdividef(1.0f, rhoi + rhob);
             vwx += vf * gx;
             vwy += vf * gy;
           }
-          if (want_L) {
+          if (renorm) {
             w00 += Vb * rx * gx;
             w01 += Vb * rx * gy;
             w10 += Vb * ry * gx;
             w11 += Vb * ry * gy;
+            const float s = (rhob - rhoi) * Vb * 2.0f;
+            gwx += s * gx;
+            gwy += s * gy;
           }
         },
         coff);
   }
-  float d = dp_f + dp_w;
-  if (P.diffusion == 1) d += P.diff_k * mog;
-  dpdt[i] = d;
+  Pass1 o;
+  o.dpdt = dp_f + dp_w;
+  if (P.diffusion == 1) o.dpdt += P.diff_k * mog;
   float ax, ay;
   if (P.point_source) {
-    float dx = xi.x - P.point_cx, dy = xi.y - P.point_cy;
+    float dx = si.x - P.point_cx, dy = si.y - P.point_cy;
     float dist = sqrtf(dx * dx + dy * dy);
     if (dist > 1e-7f) {
       dx /= dist;
@@ -204,92 +241,51 @@ __device__ __forceinline__ void pass1_body(int i, const FluidView& F, const Wall
   ay += ir * pay + ir * pwy;
   ax += P.visc_k * vax + P.visc_k * vwx;
   ay += P.visc_k * vay + P.visc_k * vwy;
-  ax += lax;
-  ay += lay;
-  acc[i] = make_float2(ax, ay);
-  if (want_L) Lout[i] = make_float4(l00 + w00, l01 + w01, l10 + w10, l11 + w11);
+  o.ax = ax + lax;
+  o.ay = ay + lay;
+  o.L = make_float4(l00 + w00, l01 + w01, l10 + w10, l11 + w11);
+  o.grad_rho = make_float2(0.f, 0.f);
+  if (renorm) {
+    const float4 Li = pinv2x2(o.L.x, o.L.y, o.L.z, o.L.w);
+    const float fx = Li.x * gfx + Li.y * gfy, fy = Li.z * gfx + Li.w * gfy;
+    const float wx = Li.x * gwx + Li.y * gwy, wy = Li.z * gwx + Li.w * gwy;
+    o.grad_rho = make_float2(-fx - wx, -fy - wy);
+  }
+  return o;
 }
 
-// <grad rho>_i = -sum_j 2 (rho_j - rho_i) V_j L_i^+ gradW_ij  (+ walls)
-__device__ __forceinline__ void gradrho_body(int i, const FluidView& F, const WallView& W, const sph_grid& g,
-                                             const SphParams& P, int coff, const float4* __restrict__ L,
-                                             float2* __restrict__ grad_rho) {
-  const float4 m = L[i];
-  const float4 Li = pinv2x2(m.x, m.y, m.z, m.w);
-  const float2 xi = F.x[i];
-  const float rhoi = F.rho[i] * P.rho0;
-  float fx = 0.f, fy = 0.f;
-  const int k0 = F.offsets[i], k1 = row_end(F, i, k0);
-  for (int k = k0; k < k1; ++k) {
-    const int j = __ldg(F.cols + k);
-    const float2 xj = __ldg(F.x + j);
-    const float rtj = __ldg(F.rho + j);
-    const float Vj = __ldg(F.area + j) / rtj, rhoj = rtj * P.rho0;
-    const Geo e = geo(xi.x, xi.y, xj.x, xj.y, P.inv_h);
-    const float gw = kGW(e.q, P.c_g);
-    const float gx = gw * e.ex, gy = gw * e.ey;
-    const float rx = Li.x * gx + Li.y * gy, ry = Li.z * gx + Li.w * gy;
-    const float s = (rhoj - rhoi) * Vj * 2.0f;
-    fx += s * rx;
-    fy += s * ry;
-  }
-  float wx = 0.f, wy = 0.f;
-  if (W.n > 0) {
-    int cx, cy;
-    cell_of(F.keys[i] - (uint32_t)coff, g, &cx, &cy);
-    const float thr = sq_threshold(P.h);
-    for_each_wall(
-        W, g, P.search_radius, cx, cy, xi.x, xi.y, thr,
-        [&](int b, float2 xb) {
-          const Geo e = geo(xi.x, xi.y, xb.x, xb.y, P.inv_h);
-          const float gw = kGW(e.q, P.c_g);
-          const float gx = gw * e.ex, gy = gw * e.ey;
-          const float rx = Li.x * gx + Li.y * gy, ry = Li.z * gx + Li.w * gy;
-          const float s = (W.rho[b] * P.rho0 - rhoi) * W.vol[b] * 2.0f;
-          wx += s * rx;
-          wy += s * ry;
-        },
-        coff);
-  }
-  grad_rho[i] = make_float2(-fx - wx, -fy - wy);
-}
-
-// D_i = h delta c0 sum_j [2 (rho_j - rho_i)/(|x_ji|^2 + eps) x_ji - (<grad rho>_i + <grad rho>_j)] . gradW_ij V_j
-__device__ __forceinline__ void diffusion_body(int i, const FluidView& F, const SphParams& P,
-                                               const float2* __restrict__ grad_rho, float* __restrict__ dpdt) {
+// D_i = sum_j [2 (rho_j - rho_i)/(|x_ji|^2 + eps) x_ji - (<grad rho>_i + <grad rho>_j)] . gradW_ij V_j
+// (the deltaSPH density diffusion before its h delta c0 factor).
+__device__ __forceinline__ float diffusion_sum(int i, const FluidView& F, const float4* __restrict__ qv,
+                                               const SphParams& P, const float2* __restrict__ grad_rho) {
   const float2 xi = F.x[i], gi = grad_rho[i];
-  const float rhoi = F.rho[i] * P.rho0;
+  const float rhoi = qv[i].x;
   float acc = 0.f;
   const int k0 = F.offsets[i], k1 = row_end(F, i, k0);
   for (int k = k0; k < k1; ++k) {
     const int j = __ldg(F.cols + k);
     const float2 xj = __ldg(F.x + j), gj = __ldg(grad_rho + j);
-    const float rtj = __ldg(F.rho + j);
-    const float Vj = __ldg(F.area + j) / rtj, rhoj = rtj * P.rho0;
-    const Geo e = geo(xi.x, xi.y, xj.x, xj.y, P.inv_h);
+    const float4 qj = __ldg(qv + j);
+    const PairGeo e = pair_geo(xi.x, xi.y, xj.x, xj.y, P.inv_h);
     const float gw = kGW(e.q, P.c_g);
     const float gx = gw * e.ex, gy = gw * e.ey;
-    const float rx = -e.dx, ry = -e.dy;
-    const float r2 = rx * rx + ry * ry + P.eps;
-    const float s = 2.0f * (rhoj - rhoi) / r2;
-    const float psx = s * rx - (gi.x + gj.x), psy = s * ry - (gi.y + gj.y);
-    acc += (psx * gx + psy * gy) * Vj;
+    const float s = 2.0f * (qj.x - rhoi) * __fdividef(1.0f, e.r2 + P.eps);
+    const float psx = -s * e.dx - (gi.x + gj.x), psy = -s * e.dy - (gi.y + gj.y);
+    acc += (psx * gx + psy * gy) * qj.y;
   }
-  dpdt[i] += P.diff_k * acc;
+  return acc;
 }
 
-// semiImplicitEuler, src/simulationBase.py:647-652 with integrateValues :564-569.
-__device__ __forceinline__ void sie_body(int i, const float2* __restrict__ x, const float2* __restrict__ v,
-                                         const float* __restrict__ rho, const float2* __restrict__ a,
-                                         const float* __restrict__ dpdt, float dt, float rho0, int continuum,
-                                         float2* __restrict__ xo, float2* __restrict__ vo, float* __restrict__ ro,
-                                         int32_t* status) {
-  const float2 ai = a[i], vi = v[i], xi = x[i];
+// semiImplicitEuler, src/simulationBase.py:647-652 with integrateValues :564-569, for one
+// particle with its own values.
+__device__ __forceinline__ void sie_apply(int i, float2 xi, float2 vi, float rti, float2 ai, float dpi, float dt,
+                                          float rho0, int continuum, float2* __restrict__ xo,
+                                          float2* __restrict__ vo, float* __restrict__ ro, int32_t* status) {
   const float2 vn = make_float2(vi.x + dt * ai.x, vi.y + dt * ai.y);
   const float2 xn = make_float2(xi.x + dt * (vi.x + dt * ai.x), xi.y + dt * (vi.y + dt * ai.y));
   xo[i] = xn;
   vo[i] = vn;
-  float rn = continuum ? rho[i] + dt * dpdt[i] / rho0 : rho[i];
+  const float rn = continuum ? rti + dt * dpi / rho0 : rti;
   ro[i] = rn;
   if (!isfinite(xn.x) || !isfinite(xn.y) || !isfinite(vn.x) || !isfinite(vn.y) || !isfinite(rn))
     flag(status, SPH_FLAG_NONFINITE);
@@ -302,27 +298,32 @@ __global__ void __launch_bounds__(128) k_mdbc(FluidView F, WallView W, const sph
   mdbc_body(b, F, W, *gp, P, 0);
 }
 
-__global__ void __launch_bounds__(128) k_dsph_pass1(FluidView F, WallView W, const sph_grid* __restrict__ gp,
-                                                    SphParams P, float* __restrict__ dpdt, float2* __restrict__ acc,
-                                                    float4* __restrict__ Lout) {
+__global__ void __launch_bounds__(256) k_prep(FluidView F, SphParams P, float4* __restrict__ xv,
+                                              float4* __restrict__ qv) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= F.n) return;
-  pass1_body(i, F, W, *gp, P, 0, dpdt, acc, Lout);
+  prep_body(i, F, P, xv, qv);
 }
 
-__global__ void __launch_bounds__(128) k_dsph_gradrho(FluidView F, WallView W, const sph_grid* __restrict__ gp,
-                                                      SphParams P, const float4* __restrict__ L,
-                                                      float2* __restrict__ grad_rho) {
+__global__ void __launch_bounds__(128) k_dsph_pass1(FluidView F, const float4* __restrict__ xv,
+                                                    const float4* __restrict__ qv, WallView W,
+                                                    const sph_grid* __restrict__ gp, SphParams P,
+                                                    float* __restrict__ dpdt, float2* __restrict__ acc,
+                                                    float4* __restrict__ Lout, float2* __restrict__ grad_rho) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= F.n) return;
-  gradrho_body(i, F, W, *gp, P, 0, L, grad_rho);
+  const Pass1 o = pass1_body(i, F, xv, qv, W, *gp, P, 0);
+  dpdt[i] = o.dpdt;
+  acc[i] = make_float2(o.ax, o.ay);
+  if (Lout) Lout[i] = o.L;
+  if (grad_rho) grad_rho[i] = o.grad_rho;
 }
 
-__global__ void __launch_bounds__(128) k_dsph_diffusion(FluidView F, SphParams P, const float2* __restrict__ grad_rho,
-                                                        float* __restrict__ dpdt) {
+__global__ void __launch_bounds__(128) k_dsph_diffusion(FluidView F, const float4* __restrict__ qv, SphParams P,
+                                                        const float2* __restrict__ grad_rho, float* __restrict__ dpdt) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= F.n) return;
-  diffusion_body(i, F, P, grad_rho, dpdt);
+  dpdt[i] += P.diff_k * diffusion_sum(i, F, qv, P, grad_rho);
 }
 
 __global__ void k_sie(int n, const float2* __restrict__ x, const float2* __restrict__ v,
@@ -331,7 +332,7 @@ __global__ void k_sie(int n, const float2* __restrict__ x, const float2* __restr
                       float2* __restrict__ vo, float* __restrict__ ro, int32_t* status) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  sie_body(i, x, v, rho, a, dpdt, *dt_ptr, rho0, continuum, xo, vo, ro, status);
+  sie_apply(i, x[i], v[i], rho[i], a[i], continuum ? dpdt[i] : 0.f, *dt_ptr, rho0, continuum, xo, vo, ro, status);
 }
 
 // ---------------------------------------------------------------------------- batch of scenes
@@ -344,49 +345,67 @@ __global__ void __launch_bounds__(128) k_batch_mdbc(FluidView F, WallView W, con
   mdbc_body(b, F, W, S.g, S.P, S.coff);
 }
 
-__global__ void __launch_bounds__(128) k_batch_pass1(FluidView F, WallView W, const SceneDev* __restrict__ scenes,
-                                                     const int32_t* __restrict__ sid, float* __restrict__ dpdt,
-                                                     float2* __restrict__ acc, float4* __restrict__ Lout) {
+__global__ void __launch_bounds__(256) k_batch_prep(FluidView F, const SceneDev* __restrict__ scenes,
+                                                    const int32_t* __restrict__ sid, float4* __restrict__ xv,
+                                                    float4* __restrict__ qv) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= F.n) return;
-  const SceneDev& S = scenes[sid[i]];
-  pass1_body(i, F, W, S.g, S.P, S.coff, dpdt, acc, Lout);
+  prep_body(i, F, scenes[sid[i]].P, xv, qv);
 }
 
-__global__ void __launch_bounds__(128) k_batch_gradrho(FluidView F, WallView W, const SceneDev* __restrict__ scenes,
-                                                       const int32_t* __restrict__ sid, const float4* __restrict__ L,
-                                                       float2* __restrict__ grad_rho) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= F.n) return;
-  const SceneDev& S = scenes[sid[i]];
-  if (S.P.diffusion != 2) return;
-  gradrho_body(i, F, W, S.g, S.P, S.coff, L, grad_rho);
-}
-
-__global__ void __launch_bounds__(128) k_batch_diffusion(FluidView F, const SceneDev* __restrict__ scenes,
-                                                         const int32_t* __restrict__ sid,
-                                                         const float2* __restrict__ grad_rho, float* __restrict__ dpdt) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= F.n) return;
-  const SceneDev& S = scenes[sid[i]];
-  if (S.P.diffusion != 2) return;
-  diffusion_body(i, F, S.P, grad_rho, dpdt);
-}
-
-__global__ void k_batch_sie(int n, const int32_t* __restrict__ sid, const SceneDev* __restrict__ scenes,
-                            const float2* __restrict__ x, const float2* __restrict__ v, const float* __restrict__ rho,
-                            const float2* __restrict__ a, const float* __restrict__ dpdt, float2* __restrict__ xo,
-                            float2* __restrict__ vo, float* __restrict__ ro, int32_t* status) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  if (*status & SPH_FLAG_PAIR_CAPACITY) {  // the neighbor list overflowed: the step is not applied
-    xo[i] = x[i];
-    vo[i] = v[i];
-    ro[i] = rho[i];
+// The update of one particle of a batch with its scene's dt.  If the neighbor list
+// overflowed (the fill set SPH_FLAG_PAIR_CAPACITY) the step is not applied: the sorted
+// inputs are copied unchanged.
+__device__ __forceinline__ void batch_update(int i, const FluidView& F, float ax, float ay, float dpdt,
+                                             const SceneDev& S, float2* __restrict__ xo, float2* __restrict__ vo,
+                                             float* __restrict__ ro, int32_t* status) {
+  if (*status & SPH_FLAG_PAIR_CAPACITY) {
+    xo[i] = F.x[i];
+    vo[i] = F.v[i];
+    ro[i] = F.rho[i];
     return;
   }
+  sie_apply(i, F.x[i], F.v[i], F.rho[i], make_float2(ax, ay), dpdt, S.dt, S.P.rho0, 1, xo, vo, ro, status);
+}
+
+// Pass 1 of every particle.  Particles of scenes without the deltaSPH density diffusion are
+// complete after it and are updated here; the others hand dpdt, acc and <grad rho> to
+// k_batch_diffusion, which finishes and updates them.
+__global__ void __launch_bounds__(128) k_batch_pass1(FluidView F, const float4* __restrict__ xv,
+                                                     const float4* __restrict__ qv, WallView W,
+                                                     const SceneDev* __restrict__ scenes,
+                                                     const int32_t* __restrict__ sid, float* __restrict__ dpdt,
+                                                     float2* __restrict__ acc, float2* __restrict__ grad_rho,
+                                                     float2* __restrict__ xo, float2* __restrict__ vo,
+                                                     float* __restrict__ ro, int32_t* status) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= F.n) return;
   const SceneDev& S = scenes[sid[i]];
-  sie_body(i, x, v, rho, a, dpdt, S.dt, S.P.rho0, 1, xo, vo, ro, status);
+  const Pass1 o = pass1_body(i, F, xv, qv, W, S.g, S.P, S.coff);
+  if (S.P.diffusion == 2) {
+    dpdt[i] = o.dpdt;
+    acc[i] = make_float2(o.ax, o.ay);
+    grad_rho[i] = o.grad_rho;
+    return;
+  }
+  batch_update(i, F, o.ax, o.ay, o.dpdt, S, xo, vo, ro, status);
+}
+
+__global__ void __launch_bounds__(128) k_batch_diffusion(FluidView F, const float4* __restrict__ qv,
+                                                         const SceneDev* __restrict__ scenes,
+                                                         const int32_t* __restrict__ sid,
+                                                         const float2* __restrict__ grad_rho,
+                                                         const float* __restrict__ dpdt,
+                                                         const float2* __restrict__ acc, float2* __restrict__ xo,
+                                                         float2* __restrict__ vo, float* __restrict__ ro,
+                                                         int32_t* status) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= F.n) return;
+  const SceneDev& S = scenes[sid[i]];
+  if (S.P.diffusion != 2) return;
+  const float d = dpdt[i] + S.P.diff_k * diffusion_sum(i, F, qv, S.P, grad_rho);
+  const float2 a = acc[i];
+  batch_update(i, F, a.x, a.y, d, S, xo, vo, ro, status);
 }
 
 // ---------------------------------------------------------------------------- RK4 helpers
@@ -454,25 +473,44 @@ sph_status_t sph_mdbc_wall_density(const sph_fluid_view* fluid, const sph_wall_v
   return SPH_OK;
 }
 
+size_t sph_deltasph_scratch_bytes(int64_t n) { return (size_t)(n > 0 ? n : 0) * 2 * sizeof(float4) + 256; }
+
+}  // extern "C"
+
+// The neighbor records (xv, q) in caller scratch, 16-byte aligned.
+static bool records_from_scratch(void* scratch, size_t bytes, int64_t n, float4** xv, float4** qv) {
+  if (!scratch) return false;
+  const uintptr_t base = reinterpret_cast<uintptr_t>(scratch);
+  const uintptr_t p = (base + 15) & ~(uintptr_t)15;
+  if ((p - base) + (size_t)n * 2 * sizeof(float4) > bytes) return false;
+  *xv = reinterpret_cast<float4*>(p);
+  *qv = *xv + n;
+  return true;
+}
+
+extern "C" {
+
 sph_status_t sph_deltasph_forces(const sph_fluid_view* fluid, const sph_wall_view* walls, const sph_grid* grid,
                                  const sph_params* params, float* dpdt, float* acc, float* L, float* grad_rho,
-                                 void* stream) {
+                                 void* scratch, size_t scratch_bytes, void* stream) {
   SPH_VIEW_CHECK(fluid);
   SPH_VIEW_CHECK(walls);
   SPH_REQUIRE(grid && params && dpdt && acc && params->support > 0.f, "deltasph_forces: bad arguments");
-  SPH_REQUIRE(params->density_diffusion != 2 || (L && grad_rho), "deltasph_forces: deltaSPH diffusion needs L, grad_rho");
+  SPH_REQUIRE(params->density_diffusion != 2 || grad_rho, "deltasph_forces: deltaSPH diffusion needs grad_rho");
   if (fluid->n == 0) return SPH_OK;
+  float4 *xv, *qv;
+  SPH_REQUIRE(records_from_scratch(scratch, scratch_bytes, fluid->n, &xv, &qv),
+              "deltasph_forces: scratch smaller than sph_deltasph_scratch_bytes(n)");
   cudaStream_t st = as_stream(stream);
   const FluidView F = to_fluid(fluid);
   const WallView W = to_walls(walls);
   const SphParams P = to_params(params);
   const int nb = grid_for(fluid->n, 128);
-  k_dsph_pass1<<<nb, 128, 0, st>>>(F, W, grid, P, dpdt, reinterpret_cast<float2*>(acc), reinterpret_cast<float4*>(L));
-  if (P.diffusion == 2) {
-    k_dsph_gradrho<<<nb, 128, 0, st>>>(F, W, grid, P, reinterpret_cast<const float4*>(L),
-                                       reinterpret_cast<float2*>(grad_rho));
-    k_dsph_diffusion<<<nb, 128, 0, st>>>(F, P, reinterpret_cast<const float2*>(grad_rho), dpdt);
-  }
+  k_prep<<<grid_for(fluid->n, 256), 256, 0, st>>>(F, P, xv, qv);
+  k_dsph_pass1<<<nb, 128, 0, st>>>(F, xv, qv, W, grid, P, dpdt, reinterpret_cast<float2*>(acc),
+                                   reinterpret_cast<float4*>(L), reinterpret_cast<float2*>(grad_rho));
+  if (P.diffusion == 2)
+    k_dsph_diffusion<<<nb, 128, 0, st>>>(F, qv, P, reinterpret_cast<const float2*>(grad_rho), dpdt);
   SPH_CHECK_LAUNCH("deltasph_forces");
   return SPH_OK;
 }
@@ -494,32 +532,35 @@ sph_status_t sph_integrate_semi_implicit_euler(int64_t n, const float* x, const 
 }
 
 sph_status_t sph_batch_deltasph_step(const sph_fluid_view* fluid, const sph_wall_view* walls, const void* scenes,
-                                     const int32_t* sid, const int32_t* wall_sid, float* dpdt, float* acc, float* L,
+                                     const int32_t* sid, const int32_t* wall_sid, float* dpdt, float* acc,
                                      float* grad_rho, int32_t any_renormalized, float* x_out, float* v_out,
-                                     float* rho_out, int32_t* status, void* stream) {
+                                     float* rho_out, int32_t* status, void* scratch, size_t scratch_bytes,
+                                     void* stream) {
   SPH_VIEW_CHECK(fluid);
   SPH_VIEW_CHECK(walls);
-  SPH_REQUIRE(scenes && sid && dpdt && acc && x_out && v_out && rho_out && status,
-              "batch_deltasph_step: bad arguments");
+  SPH_REQUIRE(scenes && sid && x_out && v_out && rho_out && status, "batch_deltasph_step: bad arguments");
   SPH_REQUIRE(walls->n == 0 || wall_sid, "batch_deltasph_step: walls need wall_sid");
-  SPH_REQUIRE(!any_renormalized || (L && grad_rho), "batch_deltasph_step: deltaSPH diffusion needs L, grad_rho");
+  SPH_REQUIRE(!any_renormalized || (dpdt && acc && grad_rho),
+              "batch_deltasph_step: deltaSPH diffusion needs dpdt, acc, grad_rho");
   const int n = (int)fluid->n;
   if (n == 0) return SPH_OK;
+  float4 *xv, *qv;
+  SPH_REQUIRE(records_from_scratch(scratch, scratch_bytes, n, &xv, &qv),
+              "batch_deltasph_step: scratch smaller than sph_deltasph_scratch_bytes(n)");
   cudaStream_t st = as_stream(stream);
   const FluidView F = to_fluid(fluid);
   const WallView W = to_walls(walls);
   const SceneDev* S = static_cast<const SceneDev*>(scenes);
   if (W.n > 0) k_batch_mdbc<<<grid_for(W.n, 128), 128, 0, st>>>(F, W, S, wall_sid);
+  k_batch_prep<<<grid_for(n, 256), 256, 0, st>>>(F, S, sid, xv, qv);
   const int nb = grid_for(n, 128);
-  k_batch_pass1<<<nb, 128, 0, st>>>(F, W, S, sid, dpdt, reinterpret_cast<float2*>(acc), reinterpret_cast<float4*>(L));
-  if (any_renormalized) {
-    k_batch_gradrho<<<nb, 128, 0, st>>>(F, W, S, sid, reinterpret_cast<const float4*>(L),
-                                        reinterpret_cast<float2*>(grad_rho));
-    k_batch_diffusion<<<nb, 128, 0, st>>>(F, S, sid, reinterpret_cast<const float2*>(grad_rho), dpdt);
-  }
-  k_batch_sie<<<grid_for(n, 256), 256, 0, st>>>(n, sid, S, F.x, F.v, F.rho, reinterpret_cast<const float2*>(acc), dpdt,
-                                                 reinterpret_cast<float2*>(x_out), reinterpret_cast<float2*>(v_out),
-                                                 rho_out, status);
+  float2* xo = reinterpret_cast<float2*>(x_out);
+  float2* vo = reinterpret_cast<float2*>(v_out);
+  k_batch_pass1<<<nb, 128, 0, st>>>(F, xv, qv, W, S, sid, dpdt, reinterpret_cast<float2*>(acc),
+                                    reinterpret_cast<float2*>(grad_rho), xo, vo, rho_out, status);
+  if (any_renormalized)
+    k_batch_diffusion<<<nb, 128, 0, st>>>(F, qv, S, sid, reinterpret_cast<const float2*>(grad_rho), dpdt,
+                                          reinterpret_cast<const float2*>(acc), xo, vo, rho_out, status);
   SPH_CHECK_LAUNCH("batch_deltasph_step");
   return SPH_OK;
 }

@@ -122,6 +122,32 @@ __device__ __forceinline__ float4 pinv2x2(float a, float b, float c, float d) {
 // 3 * FLT_EPSILON * sigma_max are dropped).  Eigen-decomposition of A^T A by cyclic Jacobi
 // rotations (at most 16 sweeps), then pinv(A) b = sum_k v_k ((A v_k) . b) / sigma_k^2.
 __device__ inline void pinv3_solve(const double A[3][3], const double b[3], double x[3]) {
+  // Well-conditioned A (Frobenius condition bound ||A|| ||A^-1|| below 1e5, far under the
+  // 1/(3 FLT_EPSILON) at which a singular value would be dropped): pinv(A) = A^-1, applied
+  // through the adjugate.  This is the common case and costs ~100 double operations instead
+  // of the Jacobi sweeps (GB300's FP64 rate is low).
+  {
+    const double c00 = A[1][1] * A[2][2] - A[1][2] * A[2][1], c01 = A[1][2] * A[2][0] - A[1][0] * A[2][2],
+                 c02 = A[1][0] * A[2][1] - A[1][1] * A[2][0];
+    const double c10 = A[0][2] * A[2][1] - A[0][1] * A[2][2], c11 = A[0][0] * A[2][2] - A[0][2] * A[2][0],
+                 c12 = A[0][1] * A[2][0] - A[0][0] * A[2][1];
+    const double c20 = A[0][1] * A[1][2] - A[0][2] * A[1][1], c21 = A[0][2] * A[1][0] - A[0][0] * A[1][2],
+                 c22 = A[0][0] * A[1][1] - A[0][1] * A[1][0];
+    const double det = A[0][0] * c00 + A[0][1] * c01 + A[0][2] * c02;
+    double na = 0.0;
+    for (int r = 0; r < 3; ++r)
+      for (int c = 0; c < 3; ++c) na += A[r][c] * A[r][c];
+    const double nc = c00 * c00 + c01 * c01 + c02 * c02 + c10 * c10 + c11 * c11 + c12 * c12 + c20 * c20 +
+                      c21 * c21 + c22 * c22;
+    // ||A^-1||_F = ||adj A||_F / |det|
+    if (det != 0.0 && na * nc < 1e10 * det * det) {
+      const double id = 1.0 / det;  // A^-1 = adj(A) / det, adj(A)[r][c] = cofactor c_cr
+      x[0] = (c00 * b[0] + c10 * b[1] + c20 * b[2]) * id;
+      x[1] = (c01 * b[0] + c11 * b[1] + c21 * b[2]) * id;
+      x[2] = (c02 * b[0] + c12 * b[1] + c22 * b[2]) * id;
+      return;
+    }
+  }
   double S[3][3];
   for (int r = 0; r < 3; ++r)
     for (int c = 0; c < 3; ++c) S[r][c] = A[0][r] * A[0][c] + A[1][r] * A[1][c] + A[2][r] * A[2][c];

@@ -171,8 +171,9 @@ class SceneBatch:
         self.scan_scratch = torch.empty((self.lib.sph_scan_scratch_bytes(n) + 7) // 8, dtype=torch.int64, device=dev)
         self.dpdt = torch.empty(n, dtype=torch.float32, device=dev)
         self.acc = torch.empty((n, 2), dtype=torch.float32, device=dev)
-        self.L = torch.empty((n, 4), dtype=torch.float32, device=dev) if self.any_renorm else None
         self.grad_rho = torch.empty((n, 2), dtype=torch.float32, device=dev) if self.any_renorm else None
+        self.forces_scratch = torch.empty((self.lib.sph_deltasph_scratch_bytes(n) + 7) // 8, dtype=torch.int64,
+                                          device=dev)
         # walls: concatenated, sorted once by (scene, cell)
         self.nb = sum(len(w) for w in wpos)
         self._setup_walls(wpos, wgh, war, wsid)
@@ -259,17 +260,17 @@ class SceneBatch:
         fv = FluidViewC(N.ptr(b["x"]), N.ptr(b["v"]), N.ptr(b["rho"]), N.ptr(b["area"]), N.ptr(self.skeys),
                         N.ptr(self.offsets), N.ptr(self.cols), N.ptr(self.cell_start), n, self.pair_cap)
         N.call("sph_batch_deltasph_step", ctypes.byref(fv), ctypes.byref(self.wall_view), N.ptr(self.scenes),
-               N.ptr(b["sid"]), N.ptr(self.w["sid"]), N.ptr(self.dpdt), N.ptr(self.acc), N.ptr(self.L),
-               N.ptr(self.grad_rho), int(self.any_renorm), N.ptr(a["x"]), N.ptr(a["v"]), N.ptr(a["rho"]),
-               N.ptr(self.status), st)
+               N.ptr(b["sid"]), N.ptr(self.w["sid"]), N.ptr(self.dpdt), N.ptr(self.acc), N.ptr(self.grad_rho),
+               int(self.any_renorm), N.ptr(a["x"]), N.ptr(a["v"]), N.ptr(a["rho"]), N.ptr(self.status),
+               N.ptr(self.forces_scratch), self.forces_scratch.numel() * 8, st)
         for k in ("area", "sup", "sid", "uid"):
             a[k].copy_(b[k])
 
-    # kernels launched by one batch step (for the bench's launch count): keys 1, counting sort
-    # (scan 3 + scatter + fix + fix_large) 6, permutes 7, count 1, scan 3, fill 1, mdbc 1,
-    # pass1 1 (+2 renormalized), update 1
+    # kernels of this library launched by one batch step (for the bench's launch count): keys 1,
+    # counting sort (scan 3 + scatter + fix + fix_large) 6, permutes 7, count 1, scan 3, fill 1,
+    # mdbc 1, records 1, pass1 + update 1 (+ diffusion + update 1 when renormalized)
     def launches_per_step(self):
-        return 1 + 6 + 7 + 1 + 3 + 1 + (1 if self.nb else 0) + 1 + (2 if self.any_renorm else 0) + 1
+        return 1 + 6 + 7 + 1 + 3 + 1 + (1 if self.nb else 0) + 1 + 1 + (1 if self.any_renorm else 0)
 
     def capture(self):
         """Capture one batch step into a CUDA graph (after a warm-up step)."""

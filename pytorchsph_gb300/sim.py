@@ -282,10 +282,10 @@ class Simulation:
         if self.nb:
             N.call("sph_mdbc_wall_density", _ref(self.fluid_view), _ref(self.wall_view), N.ptr(self.grid),
                    _ref(self.params), st)
-        L = self.ws.get("L", 4 * n, torch.float32) if self.cfg.density_diffusion == "deltaSPH" else None
         gr = self.ws.get("grad_rho", 2 * n, torch.float32) if self.cfg.density_diffusion == "deltaSPH" else None
+        scr = self.ws.bytes("forces_scratch", self.lib.sph_deltasph_scratch_bytes(n))
         N.call("sph_deltasph_forces", _ref(self.fluid_view), _ref(self.wall_view), N.ptr(self.grid), _ref(self.params),
-               N.ptr(dpdt), N.ptr(acc), N.ptr(L), N.ptr(gr), st)
+               N.ptr(dpdt), N.ptr(acc), None, N.ptr(gr), N.ptr(scr), scr.numel() * 8, st)
         self.last = {"acc": acc, "dpdt": dpdt}
         return acc, self.arr["v"], dpdt
 
