@@ -121,10 +121,15 @@ def make_event():
         return torch.cuda.Event(enable_timing=True)
 
 
-def traffic_from_profiles(workload, kernel):
+def traffic_from_profiles(workload, kernel, units):
+    """DRAM bytes (ncu dram__bytes_read.sum + dram__bytes_write.sum) of one launch of `kernel`
+    scaled to `units` particles: profiles/traffic.json holds the bytes per particle of a
+    smaller captured case of the same kernel (its traffic grows in proportion to the
+    particles processed)."""
     try:
         prof = json.load(open(os.path.join(ROOT, "profiles", "traffic.json")))
-        return prof.get(workload, {}).get(kernel)
+        e = prof[workload][kernel]
+        return e["dram_bytes"] / e["particles"] * units
     except Exception:
         return None
 
@@ -224,12 +229,13 @@ def serving_specs(n_requests, steps):
     return trace, specs
 
 
-def forces_alg_bytes(batch):
-    """Algorithmic HBM bytes of one forces launch: per particle x 8 + v 8 + rho 4 + area 4 +
-    key 4 + offsets 4 + sid 4 read, dpdt 4 + acc 8 written (52), 4 per CSR column read
-    (neighbor gathers are L1/L2 hits), per wall x 8 + vol/rho/p 12."""
+def pass1_alg_bytes(batch):
+    """Algorithmic HBM bytes of one k_batch_pass1 launch: per particle its two 16-byte
+    neighbor records (read once; the other 27-odd reads of them are L1/L2 hits), key 4,
+    offsets 4, scene index 4 read, dpdt 4 + acc 8 + <grad rho> 8 written (64); 4 per CSR
+    column read; per wall position 8 + volume, density, pressure 12."""
     P = int(batch.offsets[batch.n].item())
-    return batch.n * 52 + 4 * P + batch.nb * 20
+    return batch.n * 64 + 4 * P + batch.nb * 20
 
 
 def phase_times(batch, reps=5):
@@ -244,7 +250,7 @@ def phase_times(batch, reps=5):
     vo = torch.empty_like(batch.a["v"])
     ro = torch.empty_like(batch.a["rho"])
     for _ in range(reps):
-        e = [torch.cuda.Event(enable_timing=True) for _ in range(5)]
+        e = [torch.cuda.Event(enable_timing=True) for _ in range(7)]
         torch.cuda.synchronize()
         e[0].record()
         batch._sort_permute()
@@ -259,13 +265,15 @@ def phase_times(batch, reps=5):
         e[3].record()
         fv = FluidViewC(N.ptr(b["x"]), N.ptr(b["v"]), N.ptr(b["rho"]), N.ptr(b["area"]), N.ptr(batch.skeys),
                         N.ptr(batch.offsets), N.ptr(batch.cols), N.ptr(batch.cell_start), batch.n, batch.pair_cap)
-        N.call("sph_batch_deltasph_step", ctypes.byref(fv), ctypes.byref(batch.wall_view), N.ptr(batch.scenes),
-               N.ptr(b["sid"]), N.ptr(batch.w["sid"]), N.ptr(batch.dpdt), N.ptr(batch.acc), N.ptr(batch.grad_rho),
-               int(batch.any_renorm), N.ptr(xo), N.ptr(vo), N.ptr(ro), N.ptr(batch.status),
-               N.ptr(batch.forces_scratch), batch.forces_scratch.numel() * 8, st)
-        e[4].record()
+        for k, mask in enumerate([N.SPH_PHASE_WALLS | N.SPH_PHASE_RECORDS, N.SPH_PHASE_PASS1,
+                                  N.SPH_PHASE_DIFFUSION]):
+            N.call("sph_batch_deltasph_step", ctypes.byref(fv), ctypes.byref(batch.wall_view), N.ptr(batch.scenes),
+                   N.ptr(b["sid"]), N.ptr(batch.w["sid"]), N.ptr(batch.dpdt), N.ptr(batch.acc),
+                   N.ptr(batch.grad_rho), int(batch.any_renorm), N.ptr(xo), N.ptr(vo), N.ptr(ro),
+                   N.ptr(batch.status), mask, N.ptr(batch.forces_scratch), batch.forces_scratch.numel() * 8, st)
+            e[4 + k].record()
         torch.cuda.synchronize()
-        for k, name in enumerate(["sort+permute", "count+scan", "fill", "forces"]):
+        for k, name in enumerate(["sort+permute", "count+scan", "fill", "walls+records", "pass1", "diffusion"]):
             acc[name] = acc.get(name, 0.0) + e[k].elapsed_time(e[k + 1]) / reps
     return acc
 
@@ -298,9 +306,9 @@ def run_serving(args, dev, world, rank):
     batch.check()
     value = total_p * world / (ms / 1e3)
     phases = phase_times(batch)
-    alg = forces_alg_bytes(batch)
+    alg = pass1_alg_bytes(batch)
     peak, peak_src = hbm_peak()
-    achieved = alg / (phases["forces"] / 1e3) / 1e9 if phases.get("forces") else None
+    achieved = alg / (phases["pass1"] / 1e3) / 1e9 if phases.get("pass1") else None
     launches = batch.launches_per_step()
     batch_bytes = batch.device_bytes()
     del batch
@@ -378,7 +386,7 @@ def run_serving(args, dev, world, rank):
         line["phases_ms"] = {k: round(v, 4) for k, v in phases.items()}
         line["roofline"] = {"bound": "hbm", "kernel": "deltaSPH forces (k_batch_pass1)", "achieved": achieved,
                             "peak": peak, "unit": "GB/s", "frac": achieved / peak if achieved else None,
-                            "traffic": traffic_from_profiles("serving", "k_batch_pass1"), "algorithmic_bytes": alg,
+                            "traffic": traffic_from_profiles("serving", "k_batch_pass1", total_p), "algorithmic_bytes": alg,
                             "peak_source": peak_src}
         line["serving"] = {"one_scene_gpu_path": {"value": one_scene_value, "unit": "particle-steps/s",
                                                   "sample": [{"n": n, "ms_per_step": t * 1e3} for n, t in one]},
@@ -503,7 +511,7 @@ def run_search_density(args, dev, world, rank):
         line["phases_ms"] = {k: round(v, 5) for k, v in phases.items()}
         line["roofline"] = {"bound": "hbm", "kernel": kern, "achieved": achieved, "peak": peak, "unit": "GB/s",
                             "frac": achieved / peak if achieved else None,
-                            "traffic": traffic_from_profiles(args.workload, kern), "algorithmic_bytes": alg,
+                            "traffic": traffic_from_profiles(args.workload, kern, n), "algorithmic_bytes": alg,
                             "peak_source": peak_src}
         line["e2e"] = {"value": n * world / (statistics.mean(e2e_ms) / 1e3), "unit": "particles/s",
                        "h2d_bytes_per_step": 16 * n, "d2h_bytes_per_step": 4 * n + 4}

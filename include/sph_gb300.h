@@ -45,7 +45,8 @@ typedef int32_t sph_status_t;
 typedef struct sph_grid {
   float qmin[2];
   float hmax;
-  float reserved;
+  float hmax_threshold;  /* set by sph_grid_build: the pair test's square-root-free threshold
+                            for support hmax (0 = not set) */
   int32_t cells_x;
   int32_t cells_y;
   int32_t num_cells;
@@ -285,6 +286,11 @@ sph_status_t sph_rk_accumulate(int64_t n, const float* ku, const float* ka, cons
                                float* su, float* sa, float* sd, void* stream);
 /* out[s] = in[order[s]] for 4-, 8- or 16-byte elements (re-sorting per-particle state). */
 sph_status_t sph_permute(const uint32_t* order, int64_t n, int32_t elem_bytes, const void* in, void* out, void* stream);
+/* The same for `count` (at most 8) arrays in one pass: out[k][s] = in[k][order[s]], or a
+ * plain copy when order is NULL.  elem_bytes, in and out are host arrays of `count` entries;
+ * in[k] and out[k] must not overlap. */
+sph_status_t sph_permute_arrays(const uint32_t* order, int64_t n, int32_t count, const int32_t* elem_bytes,
+                                const void* const* in, void* const* out, void* stream);
 
 /* ---------------------------------------------------------------- batch of independent scenes */
 /* Many scenes stepped together: their particles are concatenated in one array with a
@@ -318,12 +324,21 @@ sph_status_t sph_batch_nl_fill(const float* xy, const float* sorted_support, int
  * SPH_FLAG_PAIR_CAPACITY is set in *status when the update runs (the fill overflowed),
  * the step is not applied: the outputs are the sorted inputs unchanged.  dpdt [n], acc
  * float2 [n] and grad_rho float2 [n] carry the renormalized scenes' first pass to their
- * diffusion pass (needed when any_renormalized); scratch as for sph_deltasph_forces. */
+ * diffusion pass (needed when any_renormalized); scratch as for sph_deltasph_forces.
+ * `phases` selects the launches (SPH_PHASE_ALL for a step; single phases, in order, let a
+ * caller time each kernel): walls = mDBC wall densities, records = per-particle neighbor
+ * records, pass1 = first pair pass (+ update of scenes without deltaSPH diffusion),
+ * diffusion = deltaSPH diffusion pass (+ update of the other scenes). */
+#define SPH_PHASE_WALLS 1
+#define SPH_PHASE_RECORDS 2
+#define SPH_PHASE_PASS1 4
+#define SPH_PHASE_DIFFUSION 8
+#define SPH_PHASE_ALL 15
 sph_status_t sph_batch_deltasph_step(const sph_fluid_view* fluid, const sph_wall_view* walls, const void* scenes,
                                      const int32_t* sid, const int32_t* wall_sid, float* dpdt, float* acc,
                                      float* grad_rho, int32_t any_renormalized, float* x_out, float* v_out,
-                                     float* rho_out, int32_t* status, void* scratch, size_t scratch_bytes,
-                                     void* stream);
+                                     float* rho_out, int32_t* status, int32_t phases, void* scratch,
+                                     size_t scratch_bytes, void* stream);
 
 /* ---------------------------------------------------------------- DFSPH (a20-a25) */
 

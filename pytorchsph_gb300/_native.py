@@ -68,7 +68,7 @@ SIGNATURES.update({  # batch of scenes
     "sph_batch_cell_keys": (_I32, [_P, _I64, _P, _P, _I32, _P, _P, _P, _P]),
     "sph_batch_nl_count": (_I32, [_P, _P, _I64, _P, _P, _P, _P, _P, _P]),
     "sph_batch_nl_fill": (_I32, [_P, _P, _I64, _P, _P, _P, _P, _P, _I64, _P, _P, _P]),
-    "sph_batch_deltasph_step": (_I32, [_P] * 8 + [_I32] + [_P] * 5 + [_SZ, _P]),
+    "sph_batch_deltasph_step": (_I32, [_P] * 8 + [_I32] + [_P] * 4 + [_I32, _P, _SZ, _P]),
 })
 
 SIGNATURES.update({  # simulation kernels
@@ -82,6 +82,7 @@ SIGNATURES.update({  # simulation kernels
     "sph_rk_accumulate": (_I32, [_I64] + [_P] * 3 + [_F32, _I32] +
                           [_P] * 4),
     "sph_permute": (_I32, [_P, _I64, _I32] + [_P] * 3),
+    "sph_permute_arrays": (_I32, [_P, _I64, _I32, _P, _P, _P, _P]),
     "sph_dfsph_partials_count": (_SZ, []),
     "sph_dfsph_wall_wall_term": (_I32, [_P] * 5),
     "sph_dfsph_densities": (_I32, [_P] * 7),
@@ -95,6 +96,8 @@ SIGNATURES.update({  # simulation kernels
                       [_I32, _F32, _F32] + [_P] * 2 +
                       [_SZ, _P]),
 })
+
+SPH_PHASE_WALLS, SPH_PHASE_RECORDS, SPH_PHASE_PASS1, SPH_PHASE_DIFFUSION, SPH_PHASE_ALL = 1, 2, 4, 8, 15
 
 SPH_FLAG_OUT_OF_GRID = 1
 SPH_FLAG_NONFINITE = 2
@@ -164,6 +167,18 @@ def ptr(t) -> int | None:
 
 def stream_ptr() -> int:
     return torch.cuda.current_stream().cuda_stream
+
+
+def permute_arrays(order, pairs):
+    """out[s] = in[order[s]] (a copy when order is None) for up to 8 (in, out) tensor pairs
+    of per-particle rows, in one kernel (sph_permute_arrays)."""
+    k = len(pairs)
+    n = pairs[0][0].shape[0] if k else 0
+    row = lambda t: t.element_size() * (t.shape[1] if t.dim() == 2 else 1)
+    eb = (ctypes.c_int32 * k)(*[row(t) for t, _ in pairs])
+    ins = (ctypes.c_void_p * k)(*[t.data_ptr() for t, _ in pairs])
+    outs = (ctypes.c_void_p * k)(*[o.data_ptr() for _, o in pairs])
+    call("sph_permute_arrays", ptr(order), n, k, eb, ins, outs, stream_ptr())
 
 
 def decode_flags(flags: int) -> str:

@@ -102,7 +102,7 @@ __global__ void k_bounds_final(const Bounds* __restrict__ part, int nparts, int 
   g.qmin[0] = qmin_x;
   g.qmin[1] = qmin_y;
   g.hmax = b.hmax;
-  g.reserved = 0.f;
+  g.hmax_threshold = sq_threshold(b.hmax);
   g.reserved2 = 0;
   bool ok = b.nonfinite == 0 && b.hmax > 0.f && isfinite(ex) && isfinite(ey) && ex < 2.0e9f && ey < 2.0e9f;
   int cx = ok ? (int)ceilf(ex) : 0;

@@ -46,7 +46,7 @@ __global__ void __launch_bounds__(256) k_nl_count(const float2* __restrict__ xy,
   float acc = 0.f;
   if (grid_ok(g, cap) && key < (uint32_t)g.num_cells) {
     const float2 pi = xy[s];
-    const float thr = sq_threshold(sh[s]);
+    const float thr = grid_threshold(sh[s], g);
     const int cx = (int)(key % (uint32_t)g.cells_x), cy = (int)(key / (uint32_t)g.cells_x);
     if (rho) {
       scan_candidates(xy, cell_start, g, r, cx, cy, pi.x, pi.y, thr, [&](int j, float v) {
@@ -61,26 +61,68 @@ __global__ void __launch_bounds__(256) k_nl_count(const float2* __restrict__ xy,
   if (rho) rho[s] = acc;
 }
 
+constexpr int kFillStage = 8192;  // CSR columns one 256-thread block builds in shared memory (32 KiB)
+
+// Writes the row [offsets[s], offsets[s+1]) of particle s with the columns `scan` emits.
+// The rows of one block are one contiguous span of cols.  When that span fits the stage
+// buffer (and the column buffer), the block builds it in shared memory and writes it out
+// with coalesced stores; otherwise every row is written in place, and a row that does not
+// fit the column buffer is skipped with SPH_FLAG_PAIR_CAPACITY set.  Every thread of the
+// block must call this (inactive ones with active = false): it holds a block barrier.
+template <typename Scan>
+__device__ __forceinline__ void staged_fill(int64_t s, int64_t n, bool active, const int32_t* __restrict__ offsets,
+                                            int64_t pair_capacity, int32_t* __restrict__ cols, int32_t* status,
+                                            Scan&& scan) {
+  __shared__ int32_t stage[kFillStage];
+  const int64_t b0 = (int64_t)blockIdx.x * blockDim.x;
+  const int64_t b1 = min(b0 + (int64_t)blockDim.x, n);
+  const int32_t span0 = offsets[b0], span1 = offsets[b1];
+  const bool staged = span0 >= 0 && span1 >= span0 && span1 - span0 <= kFillStage &&
+                      (int64_t)span1 <= pair_capacity;  // the same in the whole block
+  if (active) {
+    // writes stay inside the row even if offsets disagree with the scan
+    if (staged) {
+      int32_t o = offsets[s] - span0;
+      const int32_t e = offsets[s + 1] - span0;
+      if (o >= 0) scan([&](int j) {
+        if (o < e) stage[o++] = j;
+      });
+    } else if ((int64_t)offsets[s + 1] <= pair_capacity) {
+      int32_t o = offsets[s];
+      const int32_t e = offsets[s + 1];
+      if (o >= 0) scan([&](int j) {
+        if (o < e) cols[o++] = j;
+      });
+    } else {
+      flag(status, SPH_FLAG_PAIR_CAPACITY);
+    }
+  }
+  if (staged) {
+    __syncthreads();
+    for (int k = threadIdx.x; k < span1 - span0; k += blockDim.x) cols[span0 + k] = stage[k];
+  }
+}
+
 __global__ void __launch_bounds__(256) k_nl_fill(const float2* __restrict__ xy, const float* __restrict__ sh, int64_t n,
                                                  const uint32_t* __restrict__ keys,
                                                  const int32_t* __restrict__ cell_start,
                                                  const sph_grid* __restrict__ gp, int32_t cap, int r,
                                                  const int32_t* __restrict__ offsets, int64_t pair_capacity,
                                                  int32_t* __restrict__ cols, int32_t* status) {
-  int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= n) return;
+  const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const sph_grid g = *gp;
-  const uint32_t key = keys[s];
-  if (!(grid_ok(g, cap) && key < (uint32_t)g.num_cells)) return;
-  if ((int64_t)offsets[s + 1] > pair_capacity) {  // the row does not fit: write nothing
-    flag(status, SPH_FLAG_PAIR_CAPACITY);
-    return;
+  const uint32_t key = s < n ? keys[s] : 0xffffffffu;
+  const bool active = s < n && grid_ok(g, cap) && key < (uint32_t)g.num_cells;
+  float2 pi = make_float2(0.f, 0.f);
+  float thr = 0.f;
+  if (active) {
+    pi = xy[s];
+    thr = grid_threshold(sh[s], g);
   }
-  const float2 pi = xy[s];
-  const float thr = sq_threshold(sh[s]);
-  const int cx = (int)(key % (uint32_t)g.cells_x), cy = (int)(key / (uint32_t)g.cells_x);
-  int32_t o = offsets[s];
-  scan_candidates(xy, cell_start, g, r, cx, cy, pi.x, pi.y, thr, [&](int j, float) { cols[o++] = j; });
+  const int cx = active ? (int)(key % (uint32_t)g.cells_x) : 0, cy = active ? (int)(key / (uint32_t)g.cells_x) : 0;
+  staged_fill(s, n, active, offsets, pair_capacity, cols, status, [&](auto&& emit) {
+    scan_candidates(xy, cell_start, g, r, cx, cy, pi.x, pi.y, thr, [&](int j, float) { emit(j); });
+  });
 }
 
 // Query points (any order, e.g. wall or ghost particles) against the sorted grid, with
@@ -107,7 +149,7 @@ __global__ void __launch_bounds__(128) k_nl_query(const float2* __restrict__ qpo
   int cnt = 0;
   int64_t o = kFill ? offsets[b] : 0;
   const float2 xi = qpos[b];
-  const float thr = sq_threshold(qh[b]);
+  const float thr = grid_threshold(qh[b], g);
   int qx, qy;
   if (grid_ok(g, cap) && query_cell(xi.x, g.qmin[0], g.hmax, &qx) && query_cell(xi.y, g.qmin[1], g.hmax, &qy)) {
     scan_candidates(xy, cell_start, g, r, qx, qy, xi.x, xi.y, thr, [&](int j, float) {
@@ -179,7 +221,7 @@ __global__ void __launch_bounds__(256) k_batch_nl_count(const float2* __restrict
   int cnt = 0;
   if (keys[s] >= (uint32_t)S.coff && key < (uint32_t)S.g.num_cells) {
     const float2 pi = xy[s];
-    const float thr = sq_threshold(sh[s]);
+    const float thr = grid_threshold(sh[s], S.g);
     const int cx = (int)(key % (uint32_t)S.g.cells_x), cy = (int)(key / (uint32_t)S.g.cells_x);
     scan_candidates(xy, cell_start + S.coff, S.g, S.P.search_radius, cx, cy, pi.x, pi.y, thr,
                     [&](int, float) { ++cnt; });
@@ -194,21 +236,23 @@ __global__ void __launch_bounds__(256) k_batch_nl_fill(const float2* __restrict_
                                                        const int32_t* __restrict__ sid,
                                                        const int32_t* __restrict__ offsets, int64_t pair_capacity,
                                                        int32_t* __restrict__ cols, int32_t* status) {
-  int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= n) return;
-  const SceneDev& S = scenes[sid[s]];
-  const uint32_t key = keys[s] - (uint32_t)S.coff;
-  if (!(keys[s] >= (uint32_t)S.coff && key < (uint32_t)S.g.num_cells)) return;
-  if ((int64_t)offsets[s + 1] > pair_capacity) {
-    flag(status, SPH_FLAG_PAIR_CAPACITY);
-    return;
+  const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const SceneDev* S = s < n ? scenes + sid[s] : scenes;
+  const uint32_t key = s < n ? keys[s] - (uint32_t)S->coff : 0xffffffffu;
+  const bool active = s < n && keys[s] >= (uint32_t)S->coff && key < (uint32_t)S->g.num_cells;
+  float2 pi = make_float2(0.f, 0.f);
+  float thr = 0.f;
+  int cx = 0, cy = 0;
+  if (active) {
+    pi = xy[s];
+    thr = grid_threshold(sh[s], S->g);
+    cx = (int)(key % (uint32_t)S->g.cells_x);
+    cy = (int)(key / (uint32_t)S->g.cells_x);
   }
-  const float2 pi = xy[s];
-  const float thr = sq_threshold(sh[s]);
-  const int cx = (int)(key % (uint32_t)S.g.cells_x), cy = (int)(key / (uint32_t)S.g.cells_x);
-  int32_t o = offsets[s];
-  scan_candidates(xy, cell_start + S.coff, S.g, S.P.search_radius, cx, cy, pi.x, pi.y, thr,
-                  [&](int j, float) { cols[o++] = j; });
+  staged_fill(s, n, active, offsets, pair_capacity, cols, status, [&](auto&& emit) {
+    scan_candidates(xy, cell_start + S->coff, S->g, S->P.search_radius, cx, cy, pi.x, pi.y, thr,
+                    [&](int j, float) { emit(j); });
+  });
 }
 
 }  // namespace sph

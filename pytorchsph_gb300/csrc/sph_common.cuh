@@ -55,15 +55,27 @@ __device__ __forceinline__ float dist2_ref(float xi, float yi, float xj, float y
 // x = m cannot occur because m^2 has an odd ~50-bit significand while v has 24 bits).
 // m^2 is exact in double, so the predicate is  v <= F  with F the largest float below
 // m^2.  F is computed once per query particle; the candidate loop then needs no sqrt.
-__device__ __forceinline__ float sq_threshold(float h) {
+// The double arithmetic is slow on GB300, so kernels take F from a table computed once
+// (grid_threshold, SphParams::thr) whenever the support is the common one.
+__host__ __device__ __forceinline__ float sq_threshold(float h) {
   if (!(h > 0.f)) return -1.0f;          // sqrt(v) >= 0 >= h: nothing passes (NaN h too)
   if (isinf(h)) return 3.40282347e38f;   // every finite v passes
   float p = nextafterf(h, 0.0f);
   double m = ((double)p + (double)h) * 0.5;
   double m2 = m * m;
+#ifdef __CUDA_ARCH__
   float f = __double2float_rn(m2);
+#else
+  float f = (float)m2;                   // round to nearest, as on the device
+#endif
   if ((double)f >= m2) f = nextafterf(f, 0.0f);
   return f;
+}
+
+// sq_threshold(h) for a query of support h in grid g: the grid carries the value for its
+// cell size hmax (the common support), computed once by sph_grid_build.
+__device__ __forceinline__ float grid_threshold(float h, const sph_grid& g) {
+  return (h == g.hmax && g.hmax_threshold > 0.f) ? g.hmax_threshold : sq_threshold(h);
 }
 
 // Reference predicate with the distance: true iff sqrtf(fmaf(dx,dx,dy*dy)) < h_i.

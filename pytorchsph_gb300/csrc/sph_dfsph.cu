@@ -54,7 +54,7 @@ __global__ void __launch_bounds__(128) k_dfsph_fluid_density(FluidView F, WallVi
     int cx, cy;
     cell_of(F.keys[i], g, &cx, &cy);
     const float2 xi = F.x[i];
-    const float thr = sq_threshold(P.h);
+    const float thr = P.thr;
     for_each_wall(W, g, P.search_radius, cx, cy, xi.x, xi.y, thr, [&](int b, float2 xb) {
       const Geo e = geo(xb.x, xb.y, xi.x, xi.y, P.inv_h);
       rw += kW(e.q, P.c_w) * W.area[b];
@@ -74,7 +74,7 @@ __global__ void __launch_bounds__(128) k_dfsph_wall_density(FluidView F, WallVie
   if (b >= W.n) return;
   const sph_grid g = *gp;
   const float2 xb = W.x[b];
-  const float thr = sq_threshold(P.h);
+  const float thr = P.thr;
   float s = 0.f;
   int qx, qy;
   float fcx = ceilf(__fdiv_rn(__fsub_rn(xb.x, g.qmin[0]), g.hmax));
@@ -112,7 +112,7 @@ __global__ void __launch_bounds__(128) k_wall_wall_term(WallView W, const sph_gr
   float fcy = ceilf(__fdiv_rn(__fsub_rn(xb.y, g.qmin[1]), g.hmax));
   float s = 0.f;
   if (grid_ok(g, P.cell_capacity) && fcx > -1e9f && fcx < 1e9f && fcy > -1e9f && fcy < 1e9f) {
-    const float thr = sq_threshold(P.h);
+    const float thr = P.thr;
     for_each_wall(W, g, P.search_radius, (int)fcx, (int)fcy, xb.x, xb.y, thr, [&](int c, float2 xc) {
       const Geo e = geo(xb.x, xb.y, xc.x, xc.y, P.inv_h);
       s += kW(e.q, P.c_w) * W.area[c];
@@ -160,7 +160,7 @@ __global__ void __launch_bounds__(128) k_dfsph_prepare(FluidView F, WallView W, 
     const sph_grid g = *gp;
     int cx, cy;
     cell_of(F.keys[i], g, &cx, &cy);
-    const float thr = sq_threshold(P.h);
+    const float thr = P.thr;
     for_each_wall(W, g, P.search_radius, cx, cy, xi.x, xi.y, thr, [&](int b, float2 xb) {
       const Geo e = geo(xb.x, xb.y, xi.x, xi.y, P.inv_h);   // e = (x_b - x_f)/r
       const float gs = kGS(e.q, P.c_s);
@@ -193,7 +193,7 @@ __global__ void __launch_bounds__(128) k_dfsph_wall_prepare(FluidView F, WallVie
   const float dt = *dt_ptr;
   const sph_grid g = *gp;
   const float2 xb = W.x[b];
-  const float thr = sq_threshold(P.h);
+  const float thr = P.thr;
   float t = 0.f, s = 0.f;
   float fcx = ceilf(__fdiv_rn(__fsub_rn(xb.x, g.qmin[0]), g.hmax));
   float fcy = ceilf(__fdiv_rn(__fsub_rn(xb.y, g.qmin[1]), g.hmax));
@@ -247,7 +247,7 @@ __device__ __forceinline__ float2 pressure_accel(const FluidView& F, const WallV
     float wx = 0.f, wy = 0.f;
     int cx, cy;
     cell_of(F.keys[i], g, &cx, &cy);
-    const float thr = sq_threshold(P.h);
+    const float thr = P.thr;
     for_each_wall(W, g, P.search_radius, cx, cy, xi.x, xi.y, thr, [&](int b, float2 xb) {
       const Geo e = geo(xb.x, xb.y, xi.x, xi.y, P.inv_h);   // spiky(e_bf), used negated
       const float gs = kGS(e.q, P.c_s);
@@ -299,7 +299,7 @@ __global__ void __launch_bounds__(256) k_dfsph_solve(FluidView F, WallView W, co
         float wks = 0.f;
         int cx, cy;
         cell_of(F.keys[i], g, &cx, &cy);
-        const float thr = sq_threshold(P.h);
+        const float thr = P.thr;
         for_each_wall(W, g, P.search_radius, cx, cy, xi.x, xi.y, thr, [&](int b, float2 xb) {
           const Geo e = geo(xb.x, xb.y, xi.x, xi.y, P.inv_h);
           const float gs = kGS(e.q, P.c_s);
@@ -325,7 +325,7 @@ __global__ void __launch_bounds__(256) k_dfsph_solve(FluidView F, WallView W, co
           const int qx = (int)fcx, qy = (int)fcy, rr = P.search_radius;
           const int x0 = max(qx - rr, 0), x1 = min(qx + rr, g.cells_x - 1);
           const int y0 = max(qy - rr, 0), y1 = min(qy + rr, g.cells_y - 1);
-          const float thr = sq_threshold(P.h);
+          const float thr = P.thr;
           if (x0 <= x1)
             for (int yy = y0; yy <= y1; ++yy) {
               const int row = yy * g.cells_x;
@@ -404,7 +404,7 @@ __global__ void __launch_bounds__(128) k_dfsph_viscosity(FluidView F, WallView W
     const sph_grid g = *gp;
     int cx, cy;
     cell_of(F.keys[i], g, &cx, &cy);
-    const float thr = sq_threshold(P.h);
+    const float thr = P.thr;
     for_each_wall(W, g, P.search_radius, cx, cy, xi.x, xi.y, thr, [&](int b, float2 xb) {
       const Geo e = geo(xi.x, xi.y, xb.x, xb.y, P.inv_h);
       const float gw = kGW(e.q, P.c_g);

@@ -33,9 +33,10 @@ namespace sph {
 __device__ __forceinline__ void mdbc_body(int b, const FluidView& F, const WallView& W, const sph_grid& g,
                                           const SphParams& P, int coff) {
   const float2 xg = W.xg[b];
-  const float thr = sq_threshold(P.h);
-  double nom = 0, den = 0, gx = 0, gy = 0, vgx = 0, vgy = 0, px = 0, py = 0;
-  double m00 = 0, m01 = 0, m10 = 0, m11 = 0;
+  const float thr = P.thr;
+  // float sums (GB300's FP64 rate is low); the 3x3 solve below runs in double
+  float nom = 0, den = 0, gx = 0, gy = 0, vgx = 0, vgy = 0, px = 0, py = 0;
+  float m00 = 0, m01 = 0, m10 = 0, m11 = 0;
   int cnt = 0;
   const int32_t* cs = F.cell_start + coff;
   if (grid_ok(g, P.cell_capacity)) {
@@ -53,13 +54,13 @@ __device__ __forceinline__ void mdbc_body(int b, const FluidView& F, const WallV
             const float2 xj = F.x[j];
             if (!(dist2_ref(xg.x, xg.y, xj.x, xj.y) <= thr)) continue;
             const Geo e = geo(xg.x, xg.y, xj.x, xj.y, P.inv_h);   // e = (x_g - x_j)/r
-            const double k = kW(e.q, P.c_w);
-            const double gw = kGW(e.q, P.c_g);
-            const double ggx = gw * e.ex, ggy = gw * e.ey;
-            const double Aj = F.area[j];
-            const double mass = Aj * P.rho0;
-            const double Vj = Aj / (double)F.rho[j];
-            const double xx = (double)xj.x - xg.x, xy = (double)xj.y - xg.y;
+            const float k = kW(e.q, P.c_w);
+            const float gw = kGW(e.q, P.c_g);
+            const float ggx = gw * e.ex, ggy = gw * e.ey;
+            const float Aj = F.area[j];
+            const float mass = Aj * P.rho0;
+            const float Vj = Aj / F.rho[j];
+            const float xx = xj.x - xg.x, xy = xj.y - xg.y;
             nom += mass * k;
             den += Vj * k;
             gx += mass * ggx;
@@ -79,7 +80,7 @@ __device__ __forceinline__ void mdbc_body(int b, const FluidView& F, const WallV
     }
   }
   double rho_b = 1.0;
-  if (cnt > 0) rho_b = (nom / den) / P.rho0;
+  if (cnt > 0) rho_b = ((double)nom / (double)den) / P.rho0;
   if (cnt > 10) {
     const double A[3][3] = {{den, px, py}, {vgx, m00, m01}, {vgy, m10, m11}};
     const double bb[3] = {nom, gx, gy};
@@ -187,7 +188,7 @@ __device__ __forceinline__ Pass1 pass1_body(int i, const FluidView& F, const flo
   if (W.n > 0) {
     int cx, cy;
     cell_of(F.keys[i] - (uint32_t)coff, g, &cx, &cy);
-    const float thr = sq_threshold(P.h);
+    const float thr = P.thr;
     for_each_wall(
         W, g, P.search_radius, cx, cy, si.x, si.y, thr,
         [&](int b, float2 xb) {
@@ -455,6 +456,37 @@ __global__ void k_permute(const uint32_t* __restrict__ order, int n, const T* __
   if (s < n) out[s] = in[order[s]];
 }
 
+// Up to kMaxArrays per-particle arrays gathered in one pass: out_k[s] = in_k[order[s]], or
+// a plain copy when order is null.  One launch reads order once instead of once per array.
+constexpr int kMaxArrays = 8;
+struct ArraySet {
+  const void* in[kMaxArrays];
+  void* out[kMaxArrays];
+  int32_t bytes[kMaxArrays];
+  int32_t count;
+};
+
+__global__ void __launch_bounds__(256) k_permute_arrays(const uint32_t* __restrict__ order, int n, ArraySet a) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  const int src = order ? (int)order[s] : s;
+#pragma unroll
+  for (int k = 0; k < kMaxArrays; ++k) {
+    if (k >= a.count) break;
+    switch (a.bytes[k]) {
+      case 4:
+        static_cast<uint32_t*>(a.out[k])[s] = static_cast<const uint32_t*>(a.in[k])[src];
+        break;
+      case 8:
+        static_cast<uint2*>(a.out[k])[s] = static_cast<const uint2*>(a.in[k])[src];
+        break;
+      default:
+        static_cast<uint4*>(a.out[k])[s] = static_cast<const uint4*>(a.in[k])[src];
+        break;
+    }
+  }
+}
+
 }  // namespace sph
 
 using namespace sph;
@@ -534,8 +566,8 @@ sph_status_t sph_integrate_semi_implicit_euler(int64_t n, const float* x, const 
 sph_status_t sph_batch_deltasph_step(const sph_fluid_view* fluid, const sph_wall_view* walls, const void* scenes,
                                      const int32_t* sid, const int32_t* wall_sid, float* dpdt, float* acc,
                                      float* grad_rho, int32_t any_renormalized, float* x_out, float* v_out,
-                                     float* rho_out, int32_t* status, void* scratch, size_t scratch_bytes,
-                                     void* stream) {
+                                     float* rho_out, int32_t* status, int32_t phases, void* scratch,
+                                     size_t scratch_bytes, void* stream) {
   SPH_VIEW_CHECK(fluid);
   SPH_VIEW_CHECK(walls);
   SPH_REQUIRE(scenes && sid && x_out && v_out && rho_out && status, "batch_deltasph_step: bad arguments");
@@ -551,14 +583,15 @@ sph_status_t sph_batch_deltasph_step(const sph_fluid_view* fluid, const sph_wall
   const FluidView F = to_fluid(fluid);
   const WallView W = to_walls(walls);
   const SceneDev* S = static_cast<const SceneDev*>(scenes);
-  if (W.n > 0) k_batch_mdbc<<<grid_for(W.n, 128), 128, 0, st>>>(F, W, S, wall_sid);
-  k_batch_prep<<<grid_for(n, 256), 256, 0, st>>>(F, S, sid, xv, qv);
+  if (W.n > 0 && (phases & SPH_PHASE_WALLS)) k_batch_mdbc<<<grid_for(W.n, 128), 128, 0, st>>>(F, W, S, wall_sid);
+  if (phases & SPH_PHASE_RECORDS) k_batch_prep<<<grid_for(n, 256), 256, 0, st>>>(F, S, sid, xv, qv);
   const int nb = grid_for(n, 128);
   float2* xo = reinterpret_cast<float2*>(x_out);
   float2* vo = reinterpret_cast<float2*>(v_out);
-  k_batch_pass1<<<nb, 128, 0, st>>>(F, xv, qv, W, S, sid, dpdt, reinterpret_cast<float2*>(acc),
-                                    reinterpret_cast<float2*>(grad_rho), xo, vo, rho_out, status);
-  if (any_renormalized)
+  if (phases & SPH_PHASE_PASS1)
+    k_batch_pass1<<<nb, 128, 0, st>>>(F, xv, qv, W, S, sid, dpdt, reinterpret_cast<float2*>(acc),
+                                      reinterpret_cast<float2*>(grad_rho), xo, vo, rho_out, status);
+  if (any_renormalized && (phases & SPH_PHASE_DIFFUSION))
     k_batch_diffusion<<<nb, 128, 0, st>>>(F, qv, S, sid, reinterpret_cast<const float2*>(grad_rho), dpdt,
                                           reinterpret_cast<const float2*>(acc), xo, vo, rho_out, status);
   SPH_CHECK_LAUNCH("batch_deltasph_step");
@@ -601,6 +634,31 @@ sph_status_t sph_rk_accumulate(int64_t n, const float* ku, const float* ka, cons
       (int)n, reinterpret_cast<const float2*>(ku), reinterpret_cast<const float2*>(ka), kd, w, init,
       reinterpret_cast<float2*>(su), reinterpret_cast<float2*>(sa), sd);
   SPH_CHECK_LAUNCH("rk_accumulate");
+  return SPH_OK;
+}
+
+sph_status_t sph_permute_arrays(const uint32_t* order, int64_t n, int32_t count, const int32_t* elem_bytes,
+                                const void* const* in, void* const* out, void* stream) {
+  SPH_REQUIRE(n >= 0 && n < (1LL << 31) && count >= 0 && count <= kMaxArrays && (count == 0 || (elem_bytes && in && out)),
+              "permute_arrays: bad arguments");
+  if (n == 0 || count == 0) return SPH_OK;
+  ArraySet a;
+  a.count = count;
+  for (int k = 0; k < kMaxArrays; ++k) {
+    a.in[k] = nullptr;
+    a.out[k] = nullptr;
+    a.bytes[k] = 4;
+  }
+  for (int k = 0; k < count; ++k) {
+    SPH_REQUIRE(in[k] && out[k] && in[k] != out[k] &&
+                    (elem_bytes[k] == 4 || elem_bytes[k] == 8 || elem_bytes[k] == 16),
+                "permute_arrays: each array needs distinct in/out and 4, 8 or 16-byte elements");
+    a.in[k] = in[k];
+    a.out[k] = out[k];
+    a.bytes[k] = elem_bytes[k];
+  }
+  k_permute_arrays<<<grid_for(n, 256), 256, 0, as_stream(stream)>>>(order, (int)n, a);
+  SPH_CHECK_LAUNCH("permute_arrays");
   return SPH_OK;
 }
 

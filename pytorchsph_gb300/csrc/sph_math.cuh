@@ -10,6 +10,7 @@ namespace sph {
 // Parameters shared by every summation kernel (by value in the launch).
 struct SphParams {
   float h, inv_h;
+  float thr;        // sq_threshold(h): the pair test v <= thr for support h
   float c_w;        // 7 / (pi h^2)           Wendland W
   float c_g;        // 7 / (pi h^3)           Wendland gradient (times 20 q (1-q)^3)
   float c_s;        // 30 / (pi h^3)          spiky gradient
@@ -264,6 +265,7 @@ static inline SphParams to_params(const sph_params* p) {
   SphParams P;
   P.h = p->support;
   P.inv_h = 1.0f / p->support;
+  P.thr = sq_threshold(p->support);
   const double h = p->support;
   P.c_w = (float)(7.0 / 3.14159265358979323846 / (h * h));
   P.c_g = (float)(7.0 / 3.14159265358979323846 / (h * h * h));

@@ -50,7 +50,7 @@ def _params_for(cfg: SimConfig, h: float, cells: int) -> SphParamsC:
 
 
 class _Grid(ctypes.Structure):
-    _fields_ = [("qmin", ctypes.c_float * 2), ("hmax", ctypes.c_float), ("reserved", ctypes.c_float),
+    _fields_ = [("qmin", ctypes.c_float * 2), ("hmax", ctypes.c_float), ("hmax_threshold", ctypes.c_float),
                 ("cells_x", ctypes.c_int32), ("cells_y", ctypes.c_int32), ("num_cells", ctypes.c_int32),
                 ("reserved2", ctypes.c_int32)]
 
@@ -235,8 +235,7 @@ class SceneBatch:
         N.call("sph_counting_sort_tie", N.ptr(self.keys), n, self.cap, N.ptr(self.hist), N.ptr(self.cell_start),
                N.ptr(self.a["uid"]), N.ptr(self.order), N.ptr(self.skeys), N.ptr(self.status),
                N.ptr(self.cs_scratch), self.cs_scratch.numel() * 8, st)
-        for k in self.a:
-            self._perm(self.order, self.a[k], self.b[k])
+        N.permute_arrays(self.order, [(self.a[k], self.b[k]) for k in self.a])
 
     def _count(self):
         st = N.stream_ptr()
@@ -262,15 +261,14 @@ class SceneBatch:
         N.call("sph_batch_deltasph_step", ctypes.byref(fv), ctypes.byref(self.wall_view), N.ptr(self.scenes),
                N.ptr(b["sid"]), N.ptr(self.w["sid"]), N.ptr(self.dpdt), N.ptr(self.acc), N.ptr(self.grad_rho),
                int(self.any_renorm), N.ptr(a["x"]), N.ptr(a["v"]), N.ptr(a["rho"]), N.ptr(self.status),
-               N.ptr(self.forces_scratch), self.forces_scratch.numel() * 8, st)
-        for k in ("area", "sup", "sid", "uid"):
-            a[k].copy_(b[k])
+               N.SPH_PHASE_ALL, N.ptr(self.forces_scratch), self.forces_scratch.numel() * 8, st)
+        N.permute_arrays(None, [(b[k], a[k]) for k in ("area", "sup", "sid", "uid")])
 
     # kernels of this library launched by one batch step (for the bench's launch count): keys 1,
-    # counting sort (scan 3 + scatter + fix + fix_large) 6, permutes 7, count 1, scan 3, fill 1,
-    # mdbc 1, records 1, pass1 + update 1 (+ diffusion + update 1 when renormalized)
+    # counting sort (scan 3 + scatter + fix + fix_large) 6, permute 1, count 1, scan 3, fill 1,
+    # mdbc 1, records 1, pass1 + update 1 (+ diffusion + update 1 when renormalized), copy 1
     def launches_per_step(self):
-        return 1 + 6 + 7 + 1 + 3 + 1 + (1 if self.nb else 0) + 1 + 1 + (1 if self.any_renorm else 0)
+        return 1 + 6 + 1 + 1 + 3 + 1 + (1 if self.nb else 0) + 1 + 1 + (1 if self.any_renorm else 0) + 1
 
     def capture(self):
         """Capture one batch step into a CUDA graph (after a warm-up step)."""
