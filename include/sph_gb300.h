@@ -145,6 +145,13 @@ sph_status_t sph_radix_sort_pairs(uint32_t* keys, uint32_t* vals, int64_t n, int
 
 /* ---------------------------------------------------------------- grid + sort (a1, a2) */
 
+/* The grids of nseg particle sets in one launch: set s is particles [seg_offsets[s],
+ * seg_offsets[s+1]) of pos / support; min_coords / max_coords are device float[2*nseg] (set
+ * s's domain) or NULL; grids device sph_grid[nseg].  Same arithmetic as sph_grid_build.
+ * An empty set flags SPH_FLAG_NONFINITE. */
+sph_status_t sph_grid_build_segments(const float* pos, const float* support, const int64_t* seg_offsets,
+                                     int32_t nseg, const float* min_coords, const float* max_coords,
+                                     int32_t cell_capacity, sph_grid* grids, int32_t* status, void* stream);
 /* Scratch bytes sph_grid_build needs. */
 size_t sph_grid_scratch_bytes(int64_t n);
 /* Grid of sortPositions (src/modules/neighborSearch.py:34-46): hmax = max(support),

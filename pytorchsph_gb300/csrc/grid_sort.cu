@@ -63,6 +63,9 @@ __global__ void __launch_bounds__(kRedThreads) k_bounds_partial(const float2* __
   }
 }
 
+__device__ sph_grid make_grid(const Bounds& b, int has_min, float min_x, float min_y, int has_max, float max_x,
+                              float max_y, int32_t cell_capacity, int32_t* status);
+
 // Grid of sortPositions, src/modules/neighborSearch.py:34-46, all in float32:
 // qMin = minCoord - hMax*1.0, qMax = maxCoord + 2*hMax*1.0, cells = ceil((qMax-qMin)/hMax).
 __global__ void k_bounds_final(const Bounds* __restrict__ part, int nparts, int has_min, float min_x, float min_y,
@@ -90,6 +93,12 @@ __global__ void k_bounds_final(const Bounds* __restrict__ part, int nparts, int 
     b.mxy = fmaxf(b.mxy, sb[k].mxy);
     b.nonfinite |= sb[k].nonfinite;
   }
+  *grid = make_grid(b, has_min, min_x, min_y, has_max, max_x, max_y, cell_capacity, status);
+}
+
+// The grid of one particle set from its bounds (thread-local).
+__device__ sph_grid make_grid(const Bounds& b, int has_min, float min_x, float min_y, int has_max, float max_x,
+                              float max_y, int32_t cell_capacity, int32_t* status) {
   float hs = __fmul_rn(b.hmax, 1.0f);
   float two_hs = __fmul_rn(__fmul_rn(2.0f, b.hmax), 1.0f);
   float qmin_x = __fsub_rn(has_min ? min_x : b.mnx, hs);
@@ -113,7 +122,60 @@ __global__ void k_bounds_final(const Bounds* __restrict__ part, int nparts, int 
   g.cells_x = cx;
   g.cells_y = cy;
   g.num_cells = nc > (long long)cell_capacity ? cell_capacity + 1 : (int)nc;
-  *grid = g;
+  return g;
+}
+
+// Grids of many particle sets at once (one block per set): set s is the particles
+// [seg[s], seg[s+1]) of the concatenated arrays, with its own optional domain
+// min_coords[2s..2s+1] / max_coords[2s..2s+1].  Same arithmetic as sph_grid_build.
+__global__ void __launch_bounds__(kRedThreads) k_grid_segments(const float2* __restrict__ pos,
+                                                               const float* __restrict__ h,
+                                                               const int64_t* __restrict__ seg, int nseg,
+                                                               const float* __restrict__ min_coords,
+                                                               const float* __restrict__ max_coords,
+                                                               int32_t cell_capacity, sph_grid* __restrict__ grids,
+                                                               int32_t* status) {
+  const int s = blockIdx.x;
+  if (s >= nseg) return;
+  float hm = -INFINITY, mnx = INFINITY, mny = INFINITY, mxx = -INFINITY, mxy = -INFINITY;
+  int bad = 0;
+  for (int64_t i = seg[s] + threadIdx.x; i < seg[s + 1]; i += blockDim.x) {
+    float2 p = pos[i];
+    float hv = h[i];
+    if (!isfinite(p.x) || !isfinite(p.y) || !isfinite(hv)) bad = 1;
+    hm = fmaxf(hm, hv);
+    mnx = fminf(mnx, p.x);
+    mny = fminf(mny, p.y);
+    mxx = fmaxf(mxx, p.x);
+    mxy = fmaxf(mxy, p.y);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    hm = fmaxf(hm, __shfl_xor_sync(0xffffffffu, hm, o));
+    mnx = fminf(mnx, __shfl_xor_sync(0xffffffffu, mnx, o));
+    mny = fminf(mny, __shfl_xor_sync(0xffffffffu, mny, o));
+    mxx = fmaxf(mxx, __shfl_xor_sync(0xffffffffu, mxx, o));
+    mxy = fmaxf(mxy, __shfl_xor_sync(0xffffffffu, mxy, o));
+    bad |= __shfl_xor_sync(0xffffffffu, bad, o);
+  }
+  __shared__ Bounds sb[kRedThreads / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) sb[warp] = Bounds{hm, mnx, mny, mxx, mxy, bad};
+  __syncthreads();
+  if (threadIdx.x != 0) return;
+  Bounds b = sb[0];
+  for (int w = 1; w < kRedThreads / 32; ++w) {
+    b.hmax = fmaxf(b.hmax, sb[w].hmax);
+    b.mnx = fminf(b.mnx, sb[w].mnx);
+    b.mny = fminf(b.mny, sb[w].mny);
+    b.mxx = fmaxf(b.mxx, sb[w].mxx);
+    b.mxy = fmaxf(b.mxy, sb[w].mxy);
+    b.nonfinite |= sb[w].nonfinite;
+  }
+  grids[s] = make_grid(b, min_coords != nullptr, min_coords ? min_coords[2 * s] : 0.f,
+                       min_coords ? min_coords[2 * s + 1] : 0.f, max_coords != nullptr,
+                       max_coords ? max_coords[2 * s] : 0.f, max_coords ? max_coords[2 * s + 1] : 0.f,
+                       cell_capacity, status);
 }
 
 __global__ void k_cell_keys(const float2* __restrict__ pos, int64_t n, const sph_grid* __restrict__ gp,
@@ -391,6 +453,20 @@ sph_status_t sph_grid_build(const float* pos, const float* support, int64_t n, c
                                    max_coord ? max_coord[0] : 0.f, max_coord ? max_coord[1] : 0.f, cell_capacity,
                                    grid, status);
   SPH_CHECK_LAUNCH("grid_build");
+  return SPH_OK;
+}
+
+sph_status_t sph_grid_build_segments(const float* pos, const float* support, const int64_t* seg_offsets,
+                                     int32_t nseg, const float* min_coords, const float* max_coords,
+                                     int32_t cell_capacity, sph_grid* grids, int32_t* status, void* stream) {
+  SPH_REQUIRE(nseg >= 0 && (nseg == 0 || (pos && support && seg_offsets && grids && status)) && cell_capacity > 0 &&
+                  cell_capacity < 0x7ffffffe,
+              "grid_build_segments: bad arguments");
+  if (nseg == 0) return SPH_OK;
+  k_grid_segments<<<nseg, kRedThreads, 0, as_stream(stream)>>>(reinterpret_cast<const float2*>(pos), support,
+                                                               seg_offsets, nseg, min_coords, max_coords,
+                                                               cell_capacity, grids, status);
+  SPH_CHECK_LAUNCH("grid_build_segments");
   return SPH_OK;
 }
 

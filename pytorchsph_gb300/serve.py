@@ -25,7 +25,7 @@ import numpy as np
 import torch
 
 from . import _native as N
-from .search import MAX_CELLS, Workspace, grid_from_bytes, _f2
+from .search import MAX_CELLS, Workspace
 from .sim import SimConfig, SphParamsC, FluidViewC, WallViewC, DIFFUSION
 
 
@@ -55,23 +55,6 @@ class _Grid(ctypes.Structure):
                 ("reserved2", ctypes.c_int32)]
 
 
-def scene_grid(scene, device) -> _Grid:
-    """The scene's search grid (sortPositions bounds with the scene's virtual domain)."""
-    lib = N.load()
-    x = torch.as_tensor(np.ascontiguousarray(scene["pos"], np.float32), device=device)
-    h = torch.as_tensor(np.ascontiguousarray(scene["support"], np.float32), device=device)
-    n = x.shape[0]
-    g = torch.empty(8, dtype=torch.int32, device=device)
-    status = torch.zeros(1, dtype=torch.int32, device=device)
-    scratch = torch.empty((lib.sph_grid_scratch_bytes(n) + 7) // 8, dtype=torch.int64, device=device)
-    N.call("sph_grid_build", N.ptr(x), N.ptr(h), n, _f2(scene["vmin"]), _f2(scene["vmax"]), MAX_CELLS, N.ptr(g),
-           N.ptr(status), N.ptr(scratch), scratch.numel() * 8, N.stream_ptr())
-    if int(status.item()):
-        raise N.SPHError(f"scene grid: {N.decode_flags(int(status.item()))}")
-    raw = g.cpu().numpy().tobytes()
-    return _Grid.from_buffer_copy(raw)
-
-
 @dataclass
 class SceneSpec:
     scene: dict
@@ -82,18 +65,60 @@ class SceneSpec:
 
     def on_device(self, device):
         """The scene's arrays on `device` and its grid (host copies of the sph_grid), cached."""
-        if self.dev is None or self.dev["device"] != device:
-            sc = self.scene
-            t = lambda a: torch.as_tensor(np.ascontiguousarray(a, np.float32), device=device)
-            n = len(sc["pos"])
-            nb = len(sc.get("wall_pos", ()))
-            self.dev = {"device": device, "n": n, "nb": nb, "pos": t(sc["pos"]).reshape(n, 2),
-                        "vel": t(sc["vel"]).reshape(n, 2), "rho": t(sc["rho"]), "area": t(sc["area"]),
-                        "sup": t(sc["support"]), "grid": scene_grid(sc, device)}
-            if nb:
-                self.dev.update({"wall_pos": t(sc["wall_pos"]).reshape(nb, 2),
-                                 "ghost_pos": t(sc["ghost_pos"]).reshape(nb, 2), "wall_area": t(sc["wall_area"])})
+        upload_scenes([self], device)
         return self.dev
+
+
+_FIELDS = (("pos", "pos", 2, "n"), ("vel", "vel", 2, "n"), ("rho", "rho", 1, "n"), ("area", "area", 1, "n"),
+           ("sup", "support", 1, "n"), ("wall_pos", "wall_pos", 2, "nb"), ("ghost_pos", "ghost_pos", 2, "nb"),
+           ("wall_area", "wall_area", 1, "nb"))
+
+
+def upload_scenes(specs, device):
+    """Device copies and grids of every spec not yet on `device`: one copy per field for all
+    of them (from pinned host memory) and one grid launch (sph_grid_build_segments)."""
+    device = torch.device(device)
+    todo = [sp for sp in specs if sp.dev is None or sp.dev["device"] != device]
+    if not todo:
+        return
+    lib = N.load()
+    counts = {"n": [len(sp.scene["pos"]) for sp in todo],
+              "nb": [len(sp.scene.get("wall_pos", ())) for sp in todo]}
+    dev_fields = {}
+    for name, key, width, cnt in _FIELDS:
+        c = counts[cnt]
+        total = sum(c)
+        if total == 0:
+            continue
+        host = torch.empty((total, width) if width > 1 else (total,), dtype=torch.float32, pin_memory=True)
+        hv = host.numpy()
+        o = 0
+        for sp, k in zip(todo, c):
+            if k:
+                hv[o:o + k] = np.asarray(sp.scene[key], np.float32).reshape(hv[o:o + k].shape)
+                o += k
+        dev_fields[name] = (host.to(device, non_blocking=True), c)
+    S = len(todo)
+    seg = torch.tensor(np.concatenate([[0], np.cumsum(counts["n"])]), dtype=torch.int64).to(device)
+    vmin = torch.tensor(np.array([sp.scene["vmin"] for sp in todo], np.float32)).to(device)
+    vmax = torch.tensor(np.array([sp.scene["vmax"] for sp in todo], np.float32)).to(device)
+    grids = torch.empty(S * 8, dtype=torch.int32, device=device)
+    status = torch.zeros(1, dtype=torch.int32, device=device)
+    N.call("sph_grid_build_segments", N.ptr(dev_fields["pos"][0]), N.ptr(dev_fields["sup"][0]), N.ptr(seg), S,
+           N.ptr(vmin), N.ptr(vmax), MAX_CELLS, N.ptr(grids), N.ptr(status), N.stream_ptr())
+    flags = int(status.item())
+    if flags:
+        raise N.SPHError(f"scene grids: {N.decode_flags(flags)}")
+    raw = grids.cpu().numpy().tobytes()
+    offs = {name: np.concatenate([[0], np.cumsum(c)]) for name, (_, c) in dev_fields.items()}
+    for s, sp in enumerate(todo):
+        d = {"device": device, "n": counts["n"][s], "nb": counts["nb"][s],
+             "grid": _Grid.from_buffer_copy(raw[32 * s:32 * (s + 1)])}
+        for name, (t, _) in dev_fields.items():
+            lo, hi = offs[name][s], offs[name][s + 1]
+            if hi > lo:
+                d[name] = t[lo:hi]
+        sp.dev = d
 
 
 class SceneBatch:
@@ -105,11 +130,12 @@ class SceneBatch:
         dev = self.device
         self.specs = list(specs)
         S = len(self.specs)
+        upload_scenes(self.specs, dev)
         rec = self.lib.sph_scene_bytes()
         table = bytearray(rec * max(S, 1))
         self.grids, self.coff = [], []
-        pos, vel, rho, area, sup, sid, uid = [], [], [], [], [], [], []
-        wpos, wgh, war, wsid = [], [], [], []
+        pos, vel, rho, area, sup = [], [], [], [], []
+        wpos, wgh, war, nbs = [], [], [], []
         self.p_off = [0]
         total_cells = 0
         self.any_renorm = False
@@ -137,14 +163,12 @@ class SceneBatch:
             rho.append(as_dev(st["rho"]) if st else d["rho"])
             area.append(d["area"])
             sup.append(d["sup"])
-            sid.append(torch.full((n,), s, dtype=torch.int32, device=dev))
-            uid.append(torch.arange(n, dtype=torch.int32, device=dev))
             self.p_off.append(self.p_off[-1] + n)
+            nbs.append(d["nb"])
             if d["nb"]:
                 wpos.append(d["wall_pos"])
                 wgh.append(d["ghost_pos"])
                 war.append(d["wall_area"])
-                wsid.append(torch.full((d["nb"],), s, dtype=torch.int32, device=dev))
         if total_cells >= MAX_CELLS:
             raise N.SPHError("batch cell tables too large")
         self.cap = max(total_cells, 1)
@@ -154,9 +178,18 @@ class SceneBatch:
                                          dtype=torch.int64, device=dev)
         self.n = self.p_off[-1]
         n = self.n
+        # scene index and particle id of every particle; p_off_dev[sid] + uid is its slot in the
+        # concatenation of the scenes in their own particle order
+        counts = torch.tensor(np.diff(self.p_off), dtype=torch.int64, device=dev)
+        self.p_off_dev = torch.tensor(self.p_off[:-1] or [0], dtype=torch.int64, device=dev)
+        sid = torch.repeat_interleave(torch.arange(S, dtype=torch.int32, device=dev), counts)
+        uid = (torch.arange(n, dtype=torch.int64, device=dev) - self.p_off_dev[sid.long()]).to(torch.int32)
+        wsid = [torch.repeat_interleave(torch.arange(S, dtype=torch.int32, device=dev),
+                                        torch.tensor(nbs, dtype=torch.int64, device=dev))] if sum(nbs) else []
         self.a = {"x": torch.cat(pos), "v": torch.cat(vel), "rho": torch.cat(rho), "area": torch.cat(area),
-                  "sup": torch.cat(sup), "sid": torch.cat(sid), "uid": torch.cat(uid)}
+                  "sup": torch.cat(sup), "sid": sid, "uid": uid}
         self.b = {k: torch.empty_like(v) for k, v in self.a.items()}
+        self._inv = torch.empty(n, dtype=torch.int32, device=dev)
         self.ws = Workspace(dev)
         self.status = torch.zeros(1, dtype=torch.int32, device=dev)
         self.keys = torch.empty(n, dtype=torch.int32, device=dev)
@@ -319,17 +352,20 @@ class SceneBatch:
                     and torch.isfinite(self.a["rho"][lo:hi]).all())
 
     # ------------------------------------------------------------------ output
-    def scene_state_device(self, s: int):
-        """Positions, velocities and densities of scene s in its original particle order (device)."""
-        lo, hi = self.p_off[s], self.p_off[s + 1]
-        uid = self.a["uid"][lo:hi].long()
-        out = {}
-        for k in ("x", "v", "rho"):
-            t = self.a[k][lo:hi]
-            o = torch.empty_like(t)
-            o[uid] = t
-            out[k] = o
+    def states_device(self):
+        """Positions, velocities and densities of every scene in its original particle order,
+        concatenated scene after scene (device; scene s is rows p_off[s]:p_off[s+1])."""
+        dst = (self.p_off_dev[self.a["sid"].long()] + self.a["uid"].long()).to(torch.int32)
+        out = {k: torch.empty_like(self.a[k]) for k in ("x", "v", "rho")}
+        N.call("sph_invert_permutation", N.ptr(dst), self.n, N.ptr(self._inv), N.stream_ptr())
+        N.permute_arrays(self._inv, [(self.a[k], out[k]) for k in ("x", "v", "rho")])
         return out
+
+    def scene_state_device(self, s: int, states=None):
+        """Positions, velocities and densities of scene s in its original particle order (device)."""
+        states = states or self.states_device()
+        lo, hi = self.p_off[s], self.p_off[s + 1]
+        return {k: v[lo:hi] for k, v in states.items()}
 
     def scene_state(self, s: int):
         """Positions, velocities and densities of scene s in its original particle order (numpy)."""
@@ -408,6 +444,7 @@ class Server:
         if self.batch is not None:
             nonfinite = bool(self._read_flags() & N.SPH_FLAG_NONFINITE)
             escaped = self.batch.escaped()
+            all_states = self.batch.states_device()
             for s, r in enumerate(self.live):
                 r.escaped = int(escaped[s])
                 if nonfinite and not self.batch.scene_finite(s):
@@ -416,7 +453,7 @@ class Server:
                     r.spec.dev = None
                     self.failed.append(r)
                     continue
-                st = self.batch.scene_state_device(s)
+                st = self.batch.scene_state_device(s, all_states)
                 if r.steps_done >= r.spec.steps:
                     r.finished = now
                     if self.keep_final:
