@@ -347,6 +347,62 @@ sph_status_t sph_batch_deltasph_step(const sph_fluid_view* fluid, const sph_wall
                                      float* rho_out, int32_t* status, int32_t phases, void* scratch,
                                      size_t scratch_bytes, void* stream);
 
+/* ---------------------------------------------------------------- Module terms (a9-a17) */
+
+/* One summation term over the reference's own pair list, for callers that drive the
+ * reference's Module interface (densityModule.evaluate, momentumModule.computeDpDt,
+ * densityDiffusionModule.*, pressureModule.computePressureAcceleration,
+ * diffusionModule.evaluate, laminarViscosityModule.computeLaminarViscosity).  Arrays are
+ * in original particle order: the simulationState fields.  Pairs are fluidNeighbors
+ * ordered by row i (offsets from sph_row_offsets), fluidDistances e_ij and
+ * fluidRadialDistances q_ij as neighborSearchModule.search writes them
+ * (src/modules/neighborSearch.py:216-227). */
+typedef struct sph_pair_terms_in {
+  const int32_t* offsets;   /* [n+1] first pair of each row */
+  const int64_t* cols;      /* [P] j = fluidNeighbors[1] */
+  const float* dist;        /* float2 [P] fluidDistances */
+  const float* radial;      /* [P] fluidRadialDistances */
+  const float* pos;         /* float2 [n] fluidPosition */
+  const float* vel;         /* float2 [n] fluidVelocity */
+  const float* rho;         /* [n] fluidDensity (relative) */
+  const float* volume;      /* [n] fluidVolume */
+  const float* area;        /* [n] fluidArea */
+  const float* pressure;    /* [n] fluidPressure */
+  const float* L;           /* float4 [n] pseudo-inverted normalization matrix (fluidL) */
+  const float* grad_rho;    /* float2 [n] renormalized density gradient */
+  int64_t n;
+} sph_pair_terms_in;
+
+#define SPH_TERM_DENSITY 0                 /* [n]   density.py:26-30 */
+#define SPH_TERM_DIVERGENCE 1              /* [n]   momentum.py:31-38 */
+#define SPH_TERM_MOG_DIFFUSION 2           /* [n]   densityDiffusion.py:74-82 */
+#define SPH_TERM_NORMALIZATION 3           /* [n,4] densityDiffusion.py:30-44 */
+#define SPH_TERM_RENORMALIZED_GRADIENT 4   /* [n,2] densityDiffusion.py:45-61 */
+#define SPH_TERM_DELTA_DIFFUSION 5         /* [n]   densityDiffusion.py:63-71 */
+#define SPH_TERM_PRESSURE_ACCEL 6          /* [n,2] pressure.py:31-38 */
+#define SPH_TERM_VELOCITY_DIFFUSION 7      /* [n,2] diffusion.py:30-44 */
+#define SPH_TERM_LAMINAR 8                 /* [n,2] laminar.py:30-46 */
+/* out (=, or += when accumulate) one term per particle; params gives h, rest_density, c0,
+ * alpha, delta, kinematic. */
+sph_status_t sph_pair_term(int32_t term, const sph_pair_terms_in* in, const sph_params* params, float* out,
+                           int32_t accumulate, void* stream);
+
+#define SPH_OP_TAIT 0       /* out = rho0 c0^2/gamma (a^gamma - 1), a = fluidDensity (pressure.py:103) */
+#define SPH_OP_VOLUME 1     /* out = a / b: fluidArea / fluidDensity (density.py:54) */
+#define SPH_OP_PINV2X2 2    /* out float4 = pinv2x2(a float4) (util.py:386-433) */
+#define SPH_OP_GRAVITY 3    /* out float2 += gravity at positions a (gravity.py:46-57) */
+/* Per-particle operations of the same modules over n particles. */
+sph_status_t sph_particle_op(int32_t op, int64_t n, const float* a, const float* b, const sph_params* params,
+                             float* out, int32_t accumulate, void* stream);
+/* offsets[i] = first index of row i in rows (int64, ascending), offsets[n] = num_pairs. */
+sph_status_t sph_row_offsets(const int64_t* rows, int64_t num_pairs, int64_t n, int32_t* offsets, void* stream);
+/* Distances of query pairs (searchExisting, src/modules/neighborSearch.py:244-251):
+ * d = query_pos[row] - pos[col], r = |d|; dist float2 = d / r (0 when r < threshold),
+ * radial = r / query_support[row]. */
+sph_status_t sph_pair_geometry(const int32_t* rows, const int32_t* cols, int64_t num_pairs, const float* query_pos,
+                               const float* pos, const float* query_support, float threshold, float* dist,
+                               float* radial, void* stream);
+
 /* ---------------------------------------------------------------- DFSPH (a20-a25) */
 
 /* Device work arrays of one DFSPH solve (fluid arrays [n] in sorted order, wall arrays [nb]). */

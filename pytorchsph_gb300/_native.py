@@ -72,6 +72,13 @@ SIGNATURES.update({  # batch of scenes
     "sph_batch_deltasph_step": (_I32, [_P] * 8 + [_I32] + [_P] * 4 + [_I32, _P, _SZ, _P]),
 })
 
+SIGNATURES.update({  # Module-interface terms
+    "sph_pair_term": (_I32, [_I32, _P, _P, _P, _I32, _P]),
+    "sph_particle_op": (_I32, [_I32, _I64, _P, _P, _P, _P, _I32, _P]),
+    "sph_row_offsets": (_I32, [_P, _I64, _I64, _P, _P]),
+    "sph_pair_geometry": (_I32, [_P, _P, _I64, _P, _P, _P, _F32, _P, _P, _P]),
+})
+
 SIGNATURES.update({  # simulation kernels
     "sph_mdbc_wall_density": (_I32, [_P] * 5),
     "sph_deltasph_scratch_bytes": (_SZ, [_I64]),

@@ -1,0 +1,489 @@
+"""The reference's Module interface (src/module.py) for the neighbor search and the deltaSPH
+summations, computed by the GB300 kernels.
+
+Each class has the reference module's name, constructor, `getParameters`, `initialize`
+(reading the same configuration keys), `resetState` (dropping the same state keys) and hot
+methods with the same signatures and the same simulationState reads and writes, so a
+reference driver (`deltaSPHSimulation.timestep`, src/deltaSPH.py:146-200) runs unchanged
+with these modules in place of its own.  Wall contributions still come from
+`simulation.boundaryModule`, as in the reference.
+
+The arrays stay torch CUDA tensors in original particle order; every summation is one
+kernel launch over the (i, j)-ordered pair list (`sph_pair_term`), with no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _native as N
+from .search import GridSearch
+from .sim import SphParamsC
+
+
+class Parameter:
+    """A configuration parameter (src/parameter.py:3-22)."""
+
+    def __init__(self, namespace, name, datatype, defaultValue, required=False, hint='', export=True):
+        self.namespace = namespace
+        self.name = name
+        self.datatype = datatype
+        self.defaultValue = defaultValue
+        self.required = required
+        self.hint = hint
+        self.export = export
+
+    def parseConfig(self, config):
+        if self.required and self.namespace not in config:
+            raise Exception('Parameter Namespace %s missing for required parameter %s.%s' %
+                            (self.namespace, self.namespace, self.name))
+        config.setdefault(self.namespace, {})
+        if self.required and self.name not in config[self.namespace]:
+            raise Exception('Required parameter %s.%s is missing' % (self.namespace, self.name))
+        config[self.namespace].setdefault(self.name, self.defaultValue)
+
+
+class Module:
+    """Base class of all modules (src/module.py:4-24): every hook is a no-op by default."""
+
+    def getParameters(self):
+        return None
+
+    def initialize(self, config, state):
+        return
+
+    def finalize(self):
+        return
+
+    def resetState(self, simulationState):
+        return
+
+    def saveState(self, perennialState, copy):
+        return
+
+    def exportState(self, simulationState, simulation, group, mask):
+        return
+
+    def setupSimulationState(self, perennialState):
+        return
+
+    def __init__(self, identifier, moduleDescription):
+        self.description = moduleDescription
+        self.name = identifier
+
+
+class BoundaryModule(Module):
+    """Boundary hooks the solvers require (src/module.py:27-56); unimplemented ones raise."""
+
+    def __init__(self, identifier, moduleDescription):
+        super().__init__(identifier, moduleDescription)
+
+    def _missing(self, what):
+        raise Exception('Operation %s not implemented for ' % what, self.name)
+
+    def dfsphPrepareSolver(self, simulationState, simulation, density):
+        self._missing('dfsphPrepareSolver')
+
+    def dfsphBoundaryAccelTerm(self, simulationState, simulation, density):
+        self._missing('dfsphBoundaryAccelTerm')
+
+    def dfsphBoundaryPressureSum(self, simulationState, simulation, density):
+        self._missing('dfsphBoundaryPressureSum')
+
+    def dfsphBoundaryAlphaTerm(self, simulationState, simulation, density):
+        self._missing('dfsphBoundaryAlphaTerm')
+
+    def dfsphBoundarySourceTerm(self, simulationState, simulation, density):
+        self._missing('dfsphBoundarySourceTerm')
+
+    def evalBoundaryPressure(self, simulationState, simulation, density):
+        self._missing('boundaryPressure')
+
+    def evalBoundaryDensity(self, simulationState, simulation):
+        self._missing('boundaryDensity')
+
+    def evalBoundaryFriction(self, simulationState, simulation):
+        self._missing('boundaryFriction')
+
+    def boundaryNeighborhoodSearch(self, simulationState, simulation):
+        self._missing('boundaryNeighborsearch')
+
+    def boundaryFilterNeighborhoods(self, simulationState, simulation):
+        return
+
+
+# ----------------------------------------------------------------------------- kernel plumbing
+class PairTermsC(ctypes.Structure):
+    _fields_ = [(k, ctypes.c_void_p) for k in ("offsets", "cols", "dist", "radial", "pos", "vel", "rho", "volume",
+                                                "area", "pressure", "L", "grad_rho")] + [("n", ctypes.c_int64)]
+
+
+TERM = {"density": 0, "divergence": 1, "mog": 2, "normalization": 3, "renormalized_gradient": 4,
+        "delta_diffusion": 5, "pressure_accel": 6, "velocity_diffusion": 7, "laminar": 8}
+OP = {"tait": 0, "volume": 1, "pinv2x2": 2, "gravity": 3}
+WIDTH = {"density": 1, "divergence": 1, "mog": 1, "normalization": 4, "renormalized_gradient": 2,
+         "delta_diffusion": 1, "pressure_accel": 2, "velocity_diffusion": 2, "laminar": 2}
+
+
+def _f32(t):
+    if t is None:
+        return None
+    if not (t.is_cuda and t.dtype == torch.float32):
+        raise N.SPHError("module state arrays must be float32 CUDA tensors")
+    return t.contiguous()
+
+
+def _params(support, restDensity=1000.0, c0=10.0, gamma=7.0, alpha=0.01, delta=0.1, kinematic=0.01,
+            gravity=(0.0, 0.0), pointSource=False, magnitude=1.0, center=(0.0, 0.0)):
+    P = SphParamsC()
+    P.support = float(support)
+    P.rest_density = float(restDensity)
+    P.c0 = float(c0)
+    P.gamma = float(gamma)
+    P.alpha = float(alpha)
+    P.delta = float(delta)
+    P.kinematic = float(kinematic)
+    P.gravity[0], P.gravity[1] = float(gravity[0]), float(gravity[1])
+    P.point_source = int(bool(pointSource))
+    P.point_magnitude = float(magnitude)
+    P.point_center[0], P.point_center[1] = float(center[0]), float(center[1])
+    P.search_radius = 1
+    return P
+
+
+def row_offsets(simulationState):
+    """int32 [n+1] row offsets of fluidNeighbors (kept in the state beside the pairs)."""
+    nb = simulationState['fluidNeighbors']
+    n = simulationState['fluidPosition'].shape[0]
+    cached = simulationState.get('fluidNeighborOffsets')
+    if cached is not None and cached.shape[0] == n + 1:
+        return cached
+    rows = nb[0].contiguous()
+    off = torch.empty(n + 1, dtype=torch.int32, device=rows.device)
+    N.call("sph_row_offsets", N.ptr(rows), rows.shape[0], n, N.ptr(off), N.stream_ptr())
+    simulationState['fluidNeighborOffsets'] = off
+    return off
+
+
+def pair_term(term, simulationState, P, pressure=None, L=None, grad_rho=None, out=None, accumulate=False):
+    """One summation of `term` over the state's pairs; returns [n], [n,2] or [n,2,2]."""
+    st = simulationState
+    n = st['fluidPosition'].shape[0]
+    off = row_offsets(st)
+    nb = st['fluidNeighbors']
+    cols = nb[1].contiguous()
+    vol = st.get('fluidVolume')
+    keep = [off, cols]
+    arrays = {"dist": st.get('fluidDistances'), "radial": st.get('fluidRadialDistances'),
+              "pos": st.get('fluidPosition'), "vel": st.get('fluidVelocity'), "rho": st.get('fluidDensity'),
+              "volume": vol, "area": st.get('fluidArea'), "pressure": pressure, "L": L, "grad_rho": grad_rho}
+    ptrs = {}
+    for k, t in arrays.items():
+        t = _f32(t)
+        keep.append(t)
+        ptrs[k] = N.ptr(t)
+    inp = PairTermsC(N.ptr(off), N.ptr(cols), ptrs["dist"], ptrs["radial"], ptrs["pos"], ptrs["vel"], ptrs["rho"],
+                     ptrs["volume"], ptrs["area"], ptrs["pressure"], ptrs["L"], ptrs["grad_rho"], n)
+    w = WIDTH[term]
+    if out is None:
+        out = torch.zeros((n,) if w == 1 else (n, w), dtype=torch.float32, device=st['fluidPosition'].device)
+    N.call("sph_pair_term", TERM[term], ctypes.byref(inp), ctypes.byref(P), N.ptr(out), int(accumulate),
+           N.stream_ptr())
+    return out.view(n, 2, 2) if w == 4 else out
+
+
+def particle_op(op, a, b, P, out, accumulate=False):
+    a = _f32(a)
+    b = _f32(b)
+    N.call("sph_particle_op", OP[op], a.shape[0], N.ptr(a), N.ptr(b), ctypes.byref(P), N.ptr(out), int(accumulate),
+           N.stream_ptr())
+    return out
+
+
+def _c0(cfg):
+    """The c0 default every deltaSPH module applies (e.g. src/modules/momentum.py:62-67)."""
+    if cfg['fluid']['c0'] < 0:
+        cfg['fluid']['c0'] = 10.0 * np.sqrt(2.0 * 9.81 * 0.3)
+    return cfg['fluid']['c0']
+
+
+class _SummationModule(Module):
+    """Shared configuration of the summation modules (the keys their initialize reads)."""
+
+    def __init__(self):
+        super().__init__('densityInterpolation', 'Evaluates density at the current timestep')
+
+    def initialize(self, simulationConfig, simulationState):
+        cfg = simulationConfig
+        self.support = cfg['particle']['support']
+        self.restDensity = cfg['fluid']['restDensity']
+        self.gamma = cfg['pressure']['gamma']
+        self.dtype = cfg['compute']['precision']
+        self.device = cfg['compute']['device']
+        self.alpha = cfg['diffusion']['alpha']
+        self.delta = cfg['diffusion']['delta']
+        self.c0 = _c0(cfg)
+        self.eps = self.support ** 2 * 0.1
+        self.kinematic = cfg['diffusion'].get('kinematic', 0.01)
+        self.P = _params(self.support, self.restDensity, self.c0, self.gamma, self.alpha, self.delta, self.kinematic)
+
+
+# ----------------------------------------------------------------------------- neighbor search
+class neighborSearchModule(Module):
+    """src/modules/neighborSearch.py:174-252 on the GB300 search (sorted SoA + CSR inside)."""
+
+    def __init__(self):
+        super().__init__('densityInterpolation', 'Evaluates density at the current timestep')
+
+    def getParameters(self):
+        return [
+            Parameter('neighborSearch', 'gradientThreshold', 'float', 1e-7, required=False, export=True, hint=''),
+            Parameter('neighborSearch', 'supportScale', 'float', 1.0, required=False, export=True, hint=''),
+            Parameter('neighborSearch', 'sortNeighborhoods', 'bool', True, required=False, export=True, hint=''),
+        ]
+
+    def initialize(self, simulationConfig, simulationState):
+        self.support = simulationConfig['particle']['support']
+        self.maxNeighbors = simulationConfig['compute']['maxNeighbors']
+        self.threshold = simulationConfig['neighborSearch']['gradientThreshold']
+        self.supportScale = simulationConfig['neighborSearch']['supportScale']
+        self.sortNeighborhoods = simulationConfig['neighborSearch']['sortNeighborhoods']
+        self.dtype = simulationConfig['compute']['precision']
+        self.device = simulationConfig['compute']['device']
+        self.minDomain = simulationConfig['domain']['virtualMin']
+        self.maxDomain = simulationConfig['domain']['virtualMax']
+        self.engine = None
+        self.csr = None
+
+    def resetState(self, simulationState):
+        simulationState.pop('fluidNeighbors', None)
+        simulationState.pop('fluidDistances', None)
+        simulationState.pop('fluidRadialDistances', None)
+        simulationState.pop('fluidNeighborOffsets', None)
+
+    def search(self, simulationState, simulation):
+        pos = _f32(simulationState['fluidPosition'])
+        sup = _f32(simulationState['fluidSupport'])
+        if self.engine is None:
+            self.engine = GridSearch(pos.device)
+        self.csr = self.engine.run(pos, sup, kernel_support=float(self.support), density=False,
+                                   min_coord=np.asarray(self.minDomain, np.float32),
+                                   max_coord=np.asarray(self.maxDomain, np.float32))
+        fluidNeighbors, fluidDistances, fluidRadialDistances = self.csr.to_coo(self.threshold)
+        simulationState['fluidNeighbors'] = fluidNeighbors
+        simulationState['fluidDistances'] = fluidDistances
+        simulationState['fluidRadialDistances'] = fluidRadialDistances
+        simulationState.pop('fluidNeighborOffsets', None)
+        row_offsets(simulationState)
+        return fluidNeighbors, fluidDistances, fluidRadialDistances
+
+    def searchExisting(self, queryPositions, querySupports, simulationState, simulation, searchRadius: int = 1):
+        if self.csr is None:
+            raise N.SPHError("searchExisting needs a prior search() of the fluid")
+        q = _f32(queryPositions)
+        hq = _f32(querySupports)
+        rows, cols = self.csr.query(q, hq, searchRadius)
+        P = rows.shape[0]
+        dist = torch.empty((P, 2), dtype=torch.float32, device=q.device)
+        radial = torch.empty(P, dtype=torch.float32, device=q.device)
+        N.call("sph_pair_geometry", N.ptr(rows), N.ptr(cols), P, N.ptr(q),
+               N.ptr(_f32(simulationState['fluidPosition'])), N.ptr(hq), float(self.threshold), N.ptr(dist),
+               N.ptr(radial), N.stream_ptr())
+        fluidNeighbors = torch.stack([rows.long(), cols.long()], dim=0)
+        return fluidNeighbors, dist, radial
+
+
+# ----------------------------------------------------------------------------- summations
+class densityModule(Module):
+    """src/modules/density.py:33-55."""
+
+    def __init__(self):
+        super().__init__('densityInterpolation', 'Evaluates density at the current timestep')
+
+    def initialize(self, simulationConfig, simulationState):
+        self.support = simulationConfig['particle']['support']
+        self.scheme = simulationConfig['simulation']['densityScheme']
+        self.P = _params(self.support)
+
+    def resetState(self, simulationState):
+        simulationState.pop('fluidVolume', None)
+
+    def evaluate(self, simulationState, simulation):
+        if self.scheme == 'summation':
+            simulationState['fluidDensity'] = pair_term("density", simulationState, self.P)
+        area = simulationState['fluidArea']
+        vol = torch.empty_like(area)
+        simulationState['fluidVolume'] = particle_op("volume", area, simulationState['fluidDensity'], self.P, vol)
+
+
+class momentumModule(_SummationModule):
+    """src/modules/momentum.py:41-90: dpdt = continuity (+ walls)."""
+
+    def resetState(self, simulationState):
+        self.divergenceTerm = None
+        self.dpdt = None
+        simulationState.pop('dpdt', None)
+
+    def computeDpDt(self, simulationState, simulation):
+        self.divergenceTerm = pair_term("divergence", simulationState, self.P)
+        self.divergenceTerm += simulation.boundaryModule.computeDpDt(simulationState, simulation)
+        self.dpdt = self.divergenceTerm
+        simulationState['dpdt'] = self.dpdt
+        simulation.sync(simulationState['dpdt'])
+
+
+class densityDiffusionModule(_SummationModule):
+    """src/modules/densityDiffusion.py:86-180: MOG or renormalized deltaSPH density diffusion."""
+
+    def getParameters(self):
+        return [Parameter('deltaSPH', 'HughesGrahamCorrection', 'bool', True, required=False, export=True, hint='')]
+
+    def initialize(self, simulationConfig, simulationState):
+        super().initialize(simulationConfig, simulationState)
+        self.scheme = simulationConfig['diffusion']['densityScheme']
+
+    def resetState(self, simulationState):
+        self.normalizationMatrix = None
+        self.fluidL = None
+        self.eigVals = None
+        self.densityDiffusion = None
+
+    def computeNormalizationMatrices(self, simulationState, simulation):
+        self.normalizationMatrix = pair_term("normalization", simulationState, self.P)
+        self.normalizationMatrix += simulation.boundaryModule.computeNormalizationMatrices(simulationState, simulation)
+        n = self.normalizationMatrix.shape[0]
+        L = torch.empty((n, 4), dtype=torch.float32, device=self.normalizationMatrix.device)
+        particle_op("pinv2x2", self.normalizationMatrix.reshape(n, 4), None, self.P, L)
+        self.fluidL = L.view(n, 2, 2)
+        self.eigVals = None   # the singular values are not computed (nothing on the path reads them)
+
+    def computeRenormalizedDensityGradient(self, simulationState, simulation):
+        n = self.fluidL.shape[0]
+        self.renormalizedGrad = None   # per-pair L_i gradW is folded into the row sums
+        self.renormalizedDensityGradient = pair_term("renormalized_gradient", simulationState, self.P,
+                                                     L=self.fluidL.reshape(n, 4))
+        self.renormalizedDensityGradient += simulation.boundaryModule.computeRenormalizedDensityGradient(
+            simulationState, simulation)
+
+    def computeDensityDiffusion(self, simulationState, simulation):
+        if self.scheme == 'deltaSPH':
+            if 'fluidL' in simulationState:
+                self.normalizationMatrix = simulationState['normalizationMatrix']
+                self.fluidL = simulationState['fluidL']
+                self.eigVals = simulationState['eigVals']
+            else:
+                self.computeNormalizationMatrices(simulationState, simulation)
+            self.computeRenormalizedDensityGradient(simulationState, simulation)
+            self.densityDiffusion = pair_term("delta_diffusion", simulationState, self.P,
+                                              grad_rho=self.renormalizedDensityGradient)
+            simulationState['dpdt'] += self.densityDiffusion
+        elif self.scheme == 'MOG':
+            self.densityDiffusion = pair_term("mog", simulationState, self.P)
+            simulationState['dpdt'] += self.densityDiffusion
+        simulation.sync(simulationState['dpdt'])
+
+
+class pressureModule(_SummationModule):
+    """src/modules/pressure.py:54-140: Tait pressure and the pressure acceleration."""
+
+    def getParameters(self):
+        return [Parameter('pressure', 'HughesGrahamCorrection', 'bool', True, required=False, export=True, hint='')]
+
+    def initialize(self, simulationConfig, simulationState):
+        super().initialize(simulationConfig, simulationState)
+        self.kappa = simulationConfig['pressure']['kappa']
+        self.simulationScheme = simulationConfig['simulation']['scheme']
+        self.fluidPressureScheme = simulationConfig['pressure']['fluidPressureTerm']
+
+    def resetState(self, simulationState):
+        self.pressure = None
+        self.pressureAccel = None
+
+    def computePressure(self, simulationState, simulation):
+        if self.fluidPressureScheme != "TaitEOS":
+            raise N.SPHError("pressureModule: only the TaitEOS pressure term runs on this path")
+        rho = simulationState['fluidDensity']
+        self.pressure = particle_op("tait", rho, None, self.P, torch.empty_like(rho))
+        simulation.boundaryModule.computePressure(simulationState, simulation)
+        simulationState['fluidPressure'] = self.pressure
+        simulation.sync(simulationState['fluidPressure'])
+        return self.pressure
+
+    def computePressureAcceleration(self, simulationState, simulation):
+        if self.simulationScheme == 'deltaPlus':
+            raise N.SPHError("pressureModule: the deltaPlus pressure term is not on this path")
+        self.pressureAccel = pair_term("pressure_accel", simulationState, self.P, pressure=self.pressure)
+        self.pressureAccel += simulation.boundaryModule.computePressureAcceleration(simulationState, simulation)
+        simulationState['fluidAcceleration'] += self.pressureAccel
+        simulation.sync(simulationState['fluidAcceleration'])
+
+
+class diffusionModule(_SummationModule):
+    """src/modules/diffusion.py:47-93: artificial viscosity (+ walls when boundaryDiffusion)."""
+
+    def initialize(self, simulationConfig, simulationState):
+        super().initialize(simulationConfig, simulationState)
+        self.boundaryDiffusion = simulationConfig['diffusion']['boundaryDiffusion']
+
+    def resetState(self, simulationState):
+        self.velocityDiffusion = None
+
+    def evaluate(self, simulationState, simulation):
+        self.velocityDiffusion = pair_term("velocity_diffusion", simulationState, self.P)
+        if self.boundaryDiffusion:
+            self.velocityDiffusion += simulation.boundaryModule.computeVelocityDiffusion(simulationState, simulation)
+        simulationState['fluidAcceleration'] += self.velocityDiffusion
+        simulation.sync(simulationState['fluidAcceleration'])
+
+
+class laminarViscosityModule(_SummationModule):
+    """src/modules/laminar.py:49-100."""
+
+    def initialize(self, simulationConfig, simulationState):
+        super().initialize(simulationConfig, simulationState)
+        self.boundaryDiffusion = simulationConfig['diffusion']['boundaryDiffusion']
+        self.kinematic = simulationConfig['diffusion']['kinematic']
+        self.P = _params(self.support, self.restDensity, self.c0, self.gamma, self.alpha, self.delta, self.kinematic)
+
+    def resetState(self, simulationState):
+        self.laminarViscosity = None
+
+    def computeLaminarViscosity(self, simulationState, simulation):
+        self.laminarViscosity = pair_term("laminar", simulationState, self.P)
+        simulationState['fluidAcceleration'] += self.laminarViscosity
+        simulation.sync(simulationState['fluidAcceleration'])
+
+
+class gravityModule(Module):
+    """src/modules/gravity.py:23-57: constant gravity or the point source (potential field)."""
+
+    def __init__(self):
+        super().__init__('densityInterpolation', 'Evaluates density at the current timestep')
+
+    def getParameters(self):
+        return [
+            Parameter('gravity', 'magnitude', 'float', 9.81, required=False, export=True, hint=''),
+            Parameter('gravity', 'direction', 'float array', [0, -1], required=False, export=True, hint=''),
+            Parameter('gravity', 'pointSource', 'bool', False, required=False, export=True, hint=''),
+            Parameter('gravity', 'potentialField', 'bool', True, required=False, export=True, hint=''),
+            Parameter('gravity', 'center', 'float array', [0, 0], required=False, export=True, hint=''),
+        ]
+
+    def initialize(self, simulationConfig, simulationState):
+        g = simulationConfig['gravity']
+        self.magnitude = g['magnitude']
+        self.direction = g['direction']
+        self.pointSource = g['pointSource']
+        self.potentialField = g['potentialField']
+        self.center = g['center']
+        self.dtype = simulationConfig['compute']['precision']
+        self.device = simulationConfig['compute']['device']
+        if self.pointSource and not self.potentialField:
+            raise N.SPHError("gravityModule: the point source runs as a potential field on this path")
+        self.P = _params(1.0, gravity=(self.magnitude * self.direction[0], self.magnitude * self.direction[1]),
+                         pointSource=self.pointSource, magnitude=self.magnitude, center=self.center)
+
+    def evaluate(self, simulationState, simulation):
+        particle_op("gravity", simulationState['fluidPosition'], None, self.P, simulationState['fluidAcceleration'])
