@@ -12,6 +12,8 @@ Workloads (--workload):
   search_density_A/B  neighbor search + density over N = 2^20 particles.
   dambreak_deltasph   8,192-particle dam break, renormalized deltaSPH, 3-layer walls.
   dambreak_dfsph      262,144-particle dam break, DFSPH with walls, adaptive dt.
+  diff_drop           16,384-particle oscillating drop, 200 float64 steps: forward + adjoint
+                      (gradients w.r.t. v0 and alpha) checked against finite differences.
 
   python bench.py [--workload W] [--steps K] [--warmup W]
   python bench.py --impl reference ...   # the reference algorithm on the host cores
@@ -589,6 +591,107 @@ def run_dambreak(args, dev, world, rank):
         print(json.dumps(line), flush=True)
 
 
+def cpu_autograd_drop(sc, dt, steps):
+    """Seconds for forward + torch autograd backward of `steps` restated reference steps
+    (oracle/sph_torch.py, float64, torch CPU) with respect to v0 and alpha."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import torch
+    import sph_torch as S
+    alpha = torch.tensor(0.01, dtype=torch.float64, requires_grad=True)
+    p = S.Params(h=sc["h"], c0=10.0, diffusion="MOG", vmin=sc["vmin"], vmax=sc["vmax"], gravity=(0.0, 0.0),
+                 point_source=True, alpha=alpha, kinematic=0.001)
+    v0 = torch.from_numpy(sc["vel"]).double().requires_grad_(True)
+    t0 = time.perf_counter()
+    st = {"x": torch.from_numpy(sc["pos"]).double(), "v": v0, "rho": torch.from_numpy(sc["rho"]).double(),
+          "area": torch.from_numpy(sc["area"]).double()}
+    for _ in range(steps):
+        new, _ = S.step(st, None, p, dt, "semiImplicitEuler", "deltaSPH", torch.float64)
+        st = {"x": new["x"], "v": new["v"], "rho": new["rho"], "area": st["area"]}
+    ((st["x"] - torch.from_numpy(sc["pos"]).double()) ** 2).sum().backward()
+    return time.perf_counter() - t0
+
+
+def run_diff_drop(args, dev, world, rank):
+    """Differentiable drop: 16,384-particle disc, 200 float64 steps, loss against a target
+    rollout (A = 1.0, alpha = 0.02) from A = 0.8, alpha = 0.01; gradient with respect to v0 and
+    alpha by the GPU adjoint with checkpoints every 20 steps, checked against central finite
+    differences (float64, eps 1e-4) on 64 seeded velocity components and on alpha."""
+    import torch
+    from pytorchsph_gb300 import workloads
+    from pytorchsph_gb300.adjoint import DropRollout
+    steps = 200
+    start = workloads.oscillating_drop(16384, 0.5, 0.8)
+    tgt = workloads.oscillating_drop(16384, 0.5, 1.0)
+    dt = 0.1 * start["h"] / 10.0
+    r = DropRollout(start, 10.0, dt, checkpoint_every=20, device=dev)
+    target, _ = r.rollout(torch.as_tensor(tgt["vel"], dtype=torch.float64, device=dev), 0.02, steps)
+    v0 = torch.as_tensor(start["vel"], dtype=torch.float64, device=dev)
+    for _ in range(max(args.warmup, 3)):
+        r.loss_and_grad(v0, 0.01, target, steps)
+    torch.cuda.synchronize()
+    reps = max(1, args.steps)
+    with ClockSampler(dev.index or 0) as clk:
+        st, en = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        st.record()
+        for _ in range(reps):
+            loss, gv, ga = r.loss_and_grad(v0, 0.01, target, steps)
+        en.record()
+        torch.cuda.synchronize()
+    ms = st.elapsed_time(en) / reps
+    t0 = time.perf_counter()
+    r.loss(v0, 0.01, target, steps)
+    torch.cuda.synchronize()
+    fwd_ms = (time.perf_counter() - t0) * 1e3
+    # finite differences
+    rng = np.random.default_rng(0)
+    idx = rng.choice(v0.numel(), 64, replace=False)
+    eps = 1e-4
+    fd, ad = [], []
+    for k in idx:
+        e = torch.zeros(v0.numel(), dtype=torch.float64, device=dev)
+        e[int(k)] = eps
+        e = e.reshape(v0.shape)
+        fd.append((r.loss(v0 + e, 0.01, target, steps) - r.loss(v0 - e, 0.01, target, steps)) / (2 * eps))
+        ad.append(float(gv.reshape(-1)[int(k)]))
+    fd, ad = np.array(fd), np.array(ad)
+    fa = (r.loss(v0, 0.01 + eps, target, steps) - r.loss(v0, 0.01 - eps, target, steps)) / (2 * eps)
+    n = r.n
+    value = n * steps * world / (ms / 1e3)
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cpu_steps = 3
+        cpu_autograd_drop(start, dt, 1)
+        t = cpu_autograd_drop(start, dt, cpu_steps)
+        cpu = {"value": n * cpu_steps / t, "unit": "particle-steps/s", "cores": torch.get_num_threads(),
+               "kind": "port", "sample": f"forward + torch autograd backward of {cpu_steps} float64 steps of the "
+                                         f"same {n}-particle drop through the restated reference step "
+                                         f"(oracle/sph_torch.py)"}
+    if rank == 0:
+        line = base_line(args, world, value, ms, "particle-steps/s", {
+            "workload": "diff_drop", "particles": n, "rollout_steps": steps, "checkpoint_every": 20,
+            "dtype": "f64", "loss": "mean |x_T - x*_T|^2", "target": "A = 1.0, alpha = 0.02",
+            "start": "A = 0.8, alpha = 0.01", "dt": "0.1 h / c0", "density_diffusion": "MOG",
+            "unit_of_work": "one forward + adjoint of the 200-step rollout per timed step"})
+        line["dtype"] = "f64"
+        line["gradient_check"] = {
+            "components": 64, "eps": eps,
+            "max_abs_err_over_max_fd": float(np.abs(ad - fd).max() / max(np.abs(fd).max(), 1e-300)),
+            "median_rel_err": float(np.median(np.abs(ad - fd) / np.maximum(np.abs(fd), 1e-300))),
+            "alpha_adjoint": ga, "alpha_fd": fa, "alpha_rel_err": abs(ga - fa) / max(abs(fa), 1e-300),
+            "loss": loss}
+        line["forward_ms"] = fwd_ms
+        peak, peak_src = hbm_peak()
+        line["roofline"] = {"bound": "hbm", "kernel": "k_drop_adjoint (float64)", "achieved": None, "peak": peak,
+                            "unit": "GB/s", "frac": None, "traffic": None, "peak_source": peak_src,
+                            "note": "the float64 dual-number pair products bound this kernel, not HBM"}
+        line["e2e"] = {"value": None, "unit": "particle-steps/s", "h2d_bytes_per_step": None,
+                       "d2h_bytes_per_step": None}
+        line["gpu_launches"] = None
+        line["clocks"] = clk.summary()
+        line["cpu_baseline"] = cpu
+        print(json.dumps(line), flush=True)
+
+
 def run_ours(args):
     import torch
     import torch.distributed as dist
@@ -609,6 +712,8 @@ def run_ours(args):
         run_search_density(args, dev, world, rank)
     elif args.workload in ("dambreak_deltasph", "dambreak_dfsph"):
         run_dambreak(args, dev, world, rank)
+    elif args.workload == "diff_drop":
+        run_diff_drop(args, dev, world, rank)
     else:
         raise SystemExit(f"unknown workload {args.workload}")
     if world > 1:

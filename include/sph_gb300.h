@@ -403,6 +403,30 @@ sph_status_t sph_pair_geometry(const int32_t* rows, const int32_t* cols, int64_t
                                const float* pos, const float* query_support, float threshold, float* dist,
                                float* radial, void* stream);
 
+/* ---------------------------------------------------------------- differentiable rollouts */
+
+/* A free fluid (no walls) stepped by the deltaSPH right-hand side (src/deltaSPH.py:146-200:
+ * gravity or point source, continuity, MOG density diffusion when density_diffusion = 1,
+ * Tait pressure with gamma 7, artificial and laminar viscosity) and semi-implicit Euler, in
+ * float (fp64 = 0) or double (fp64 = 1): x, v, acc are 2-vectors, rho relative density.
+ * Pairs: the (i, j)-ordered reference list in original order as row offsets + int64
+ * columns (sph_row_offsets of fluidNeighbors), symmetric (one support for all particles). */
+sph_status_t sph_drop_rhs(int32_t fp64, int64_t n, const int32_t* offsets, const int64_t* cols, const void* x,
+                          const void* v, const void* rho, const void* area, const sph_params* params, void* acc,
+                          void* dpdt, void* stream);
+/* In place: v += dt acc, x += dt v (new v), rho += dt dpdt / rest_density. */
+sph_status_t sph_drop_integrate(int32_t fp64, int64_t n, void* x, void* v, void* rho, const void* acc,
+                                const void* dpdt, double dt, double rest_density, void* stream);
+/* Discrete adjoint of one step at state (x, v, rho) with the pairs of that state: from the
+ * adjoint (lx1, lv1, lr1) of the next state, the adjoint (lx0, lv0, lr0) of this one and
+ * dalpha[i] = particle i's share of dLoss/d(params->alpha) for this step.  Vector-Jacobian
+ * products by forward-mode dual numbers per pair; each particle gathers over its own row
+ * (no atomics). */
+sph_status_t sph_drop_adjoint(int32_t fp64, int64_t n, const int32_t* offsets, const int64_t* cols, const void* x,
+                              const void* v, const void* rho, const void* area, const sph_params* params, double dt,
+                              const void* lx1, const void* lv1, const void* lr1, void* lx0, void* lv0, void* lr0,
+                              void* dalpha, void* stream);
+
 /* ---------------------------------------------------------------- DFSPH (a20-a25) */
 
 /* Device work arrays of one DFSPH solve (fluid arrays [n] in sorted order, wall arrays [nb]). */

@@ -247,10 +247,11 @@ def deltasph_rhs(st, walls, nb: Neighbors, p: Params, dtype):
     acc = torch.zeros((n, 2), dtype=dtype)
     # 7 gravity (gravity.py:46-57)
     if p.point_source:
-        diff = x.clone()
-        dist = torch.linalg.norm(diff, axis=1)
+        dist = torch.linalg.norm(x, axis=1)
         m = dist > 1e-7
-        diff[m] = diff[m] / dist[m, None]
+        # the reference normalises in place where dist > 1e-7; torch.where keeps it
+        # differentiable (same values)
+        diff = torch.where(m[:, None], x / torch.where(m, dist, torch.ones_like(dist))[:, None], x)
         acc = acc - p.point_magnitude * diff * dist[:, None]
     else:
         acc = acc + torch.tensor(p.gravity, dtype=dtype)

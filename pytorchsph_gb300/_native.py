@@ -79,6 +79,13 @@ SIGNATURES.update({  # Module-interface terms
     "sph_pair_geometry": (_I32, [_P, _P, _I64, _P, _P, _P, _F32, _P, _P, _P]),
 })
 
+_D = ctypes.c_double
+SIGNATURES.update({  # differentiable rollouts
+    "sph_drop_rhs": (_I32, [_I32, _I64] + [_P] * 9 + [_P]),
+    "sph_drop_integrate": (_I32, [_I32, _I64] + [_P] * 5 + [_D, _D, _P]),
+    "sph_drop_adjoint": (_I32, [_I32, _I64] + [_P] * 7 + [_D] + [_P] * 8),
+})
+
 SIGNATURES.update({  # simulation kernels
     "sph_mdbc_wall_density": (_I32, [_P] * 5),
     "sph_deltasph_scratch_bytes": (_SZ, [_I64]),
