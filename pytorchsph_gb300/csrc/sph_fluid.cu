@@ -109,21 +109,23 @@ __device__ __forceinline__ void prep_body(int i, const FluidView& F, const SphPa
   qv[i] = make_float4(rho, V, tait(rt, P), rho * V);
 }
 
-// Pair geometry with one reciprocal square root: d = x_i - x_j, e = d / r (0 when r < 1e-7),
-// q = r / h, r2 = |d|^2.
-struct PairGeo {
-  float dx, dy, ex, ey, q, r2;
+// Pair geometry in the form the sums need: d = x_i - x_j, r2 = |d|^2 and the Wendland
+// gradient as gradW_ij = gd * d, gd = kGW(q) / r = -20 c_g (1 - q)^3 / h (zero when
+// r < 1e-7, where the reference's e_ij is zero).  Every dot product with gradW then folds
+// into gd: (x_j - x_i) . gradW = -gd r2, u . gradW = gd (u . d).
+struct PairG {
+  float dx, dy, r2, gd;
 };
 
-__device__ __forceinline__ PairGeo pair_geo(float xi, float yi, float xj, float yj, float inv_h) {
-  PairGeo g;
+__device__ __forceinline__ PairG pair_g(float xi, float yi, float xj, float yj, const SphParams& P) {
+  PairG g;
   g.dx = xi - xj;
   g.dy = yi - yj;
   g.r2 = g.dx * g.dx + g.dy * g.dy;
-  const float ir = g.r2 >= 1e-14f ? rsqrtf(g.r2) : 0.f;
-  g.ex = g.dx * ir;
-  g.ey = g.dy * ir;
-  g.q = g.r2 * ir * inv_h;
+  const bool apart = g.r2 >= 1e-14f;
+  const float r = apart ? g.r2 * rsqrtf(g.r2) : 0.f;
+  const float a = 1.0f - r * P.inv_h;
+  g.gd = apart ? P.gk * (a * a * a) : 0.f;
   return g;
 }
 
@@ -154,33 +156,33 @@ __device__ __forceinline__ Pass1 pass1_body(int i, const FluidView& F, const flo
     const int j = __ldg(F.cols + k);
     const float4 sj = __ldg(xv + j), qj = __ldg(qv + j);
     const float rhoj = qj.x, Vj = qj.y, pj = qj.z, mj = qj.w;
-    const PairGeo e = pair_geo(si.x, si.y, sj.x, sj.y, P.inv_h);
-    const float gw = kGW(e.q, P.c_g);
-    const float gx = gw * e.ex, gy = gw * e.ey;
-    const float ux = sj.z - si.z, uy = sj.w - si.w;   // u_j - u_i
-    const float rx = -e.dx, ry = -e.dy;               // x_j - x_i
+    const PairG e = pair_g(si.x, si.y, sj.x, sj.y, P);   // gradW = e.gd * d
+    const float ux = sj.z - si.z, uy = sj.w - si.w;       // u_j - u_i
+    const float ud = ux * e.dx + uy * e.dy;               // (u_j - u_i) . d
     const float ir2 = __fdividef(1.0f, e.r2 + P.eps);
-    const float rg = rx * gx + ry * gy;
-    dp_f -= (ux * gx + uy * gy) * mj;
+    const float rg = -e.gd * e.r2;                        // (x_j - x_i) . gradW
+    dp_f -= e.gd * ud * mj;
     if (P.diffusion == 1) mog += 2.0f * (rhoj - rhoi) * ir2 * rg * Vj;
-    const float pf = (pi + pj) * Vj;
-    pax += pf * gx;
-    pay += pf * gy;
+    const float pf = (pi + pj) * Vj * e.gd;
+    pax += pf * e.dx;
+    pay += pf * e.dy;
     const float irs = __fdividef(1.0f, rhoi + rhoj);
-    const float vf = fminf(ux * rx + uy * ry, 0.f) * ir2 * mj * irs;
-    vax += vf * gx;
-    vay += vf * gy;
+    const float vf = fminf(-ud, 0.f) * ir2 * mj * irs * e.gd;   // pi_ij, (u_j - u_i) . (x_j - x_i) = -ud
+    vax += vf * e.dx;
+    vay += vf * e.dy;
     const float term = 4.0f * mj * mu2 * rg * irs * irs * ir2;   // laminar: -term (u_i - u_j)
     lax += term * ux;
     lay += term * uy;
     if (renorm) {
-      l00 += Vj * rx * gx;
-      l01 += Vj * rx * gy;
-      l10 += Vj * ry * gx;
-      l11 += Vj * ry * gy;
-      const float s = 2.0f * (rhoj - rhoi) * Vj;
-      gfx += s * gx;
-      gfy += s * gy;
+      const float t = Vj * e.gd;                          // V_j (x_j - x_i) (x) gradW = -t d (x) d
+      const float tx = t * e.dx, ty = t * e.dy;
+      l00 -= tx * e.dx;
+      l01 -= tx * e.dy;
+      l10 -= ty * e.dx;
+      l11 -= ty * e.dy;
+      const float s = 2.0f * (rhoj - rhoi) * t;
+      gfx += s * e.dx;
+      gfy += s * e.dy;
     }
   }
   float dp_w = 0.f, pwx = 0.f, pwy = 0.f, vwx = 0.f, vwy = 0.f;
@@ -192,30 +194,29 @@ __device__ __forceinline__ Pass1 pass1_body(int i, const FluidView& F, const flo
     for_each_wall(
         W, g, P.search_radius, cx, cy, si.x, si.y, thr,
         [&](int b, float2 xb) {
-          const PairGeo e = pair_geo(si.x, si.y, xb.x, xb.y, P.inv_h);   // fluid side: e = (x_f - x_b)/r
-          const float gw = kGW(e.q, P.c_g);
-          const float gx = gw * e.ex, gy = gw * e.ey;
+          const PairG e = pair_g(si.x, si.y, xb.x, xb.y, P);   // fluid side: d = x_f - x_b
           const float Vb = W.vol[b], rhob = W.rho[b] * P.rho0, pb = W.p[b];
-          const float ux = -si.z, uy = -si.w;               // u_b - u_f, walls at rest
-          dp_w -= (ux * gx + uy * gy) * Vb * rhob;
-          const float pf = (pi + pb) * Vb;
-          pwx += pf * gx;
-          pwy += pf * gy;
-          const float rx = -e.dx, ry = -e.dy;               // x_b - x_f
+          const float ud = -(si.z * e.dx + si.w * e.dy);       // (u_b - u_f) . d, walls at rest
+          dp_w -= e.gd * ud * Vb * rhob;
+          const float pf = (pi + pb) * Vb * e.gd;
+          pwx += pf * e.dx;
+          pwy += pf * e.dy;
           if (P.boundary_diffusion) {
-            const float vf = fminf(ux * rx + uy * ry, 0.f) * __fdividef(1.0f, e.r2 + P.eps) * Vb * rhob *
-                             __fdividef(1.0f, rhoi + rhob);
-            vwx += vf * gx;
-            vwy += vf * gy;
+            const float vf = fminf(-ud, 0.f) * __fdividef(1.0f, e.r2 + P.eps) * Vb * rhob *
+                             __fdividef(1.0f, rhoi + rhob) * e.gd;
+            vwx += vf * e.dx;
+            vwy += vf * e.dy;
           }
           if (renorm) {
-            w00 += Vb * rx * gx;
-            w01 += Vb * rx * gy;
-            w10 += Vb * ry * gx;
-            w11 += Vb * ry * gy;
-            const float s = (rhob - rhoi) * Vb * 2.0f;
-            gwx += s * gx;
-            gwy += s * gy;
+            const float t = Vb * e.gd;
+            const float tx = t * e.dx, ty = t * e.dy;
+            w00 -= tx * e.dx;
+            w01 -= tx * e.dy;
+            w10 -= ty * e.dx;
+            w11 -= ty * e.dy;
+            const float s = (rhob - rhoi) * 2.0f * t;
+            gwx += s * e.dx;
+            gwy += s * e.dy;
           }
         },
         coff);
@@ -267,12 +268,11 @@ __device__ __forceinline__ float diffusion_sum(int i, const FluidView& F, const 
     const int j = __ldg(F.cols + k);
     const float2 xj = __ldg(F.x + j), gj = __ldg(grad_rho + j);
     const float4 qj = __ldg(qv + j);
-    const PairGeo e = pair_geo(xi.x, xi.y, xj.x, xj.y, P.inv_h);
-    const float gw = kGW(e.q, P.c_g);
-    const float gx = gw * e.ex, gy = gw * e.ey;
+    const PairG e = pair_g(xi.x, xi.y, xj.x, xj.y, P);
     const float s = 2.0f * (qj.x - rhoi) * __fdividef(1.0f, e.r2 + P.eps);
-    const float psx = -s * e.dx - (gi.x + gj.x), psy = -s * e.dy - (gi.y + gj.y);
-    acc += (psx * gx + psy * gy) * qj.y;
+    // psi . gradW with psi = s (x_j - x_i) - (g_i + g_j) and gradW = gd d
+    const float pd = -s * e.r2 - ((gi.x + gj.x) * e.dx + (gi.y + gj.y) * e.dy);
+    acc += e.gd * pd * qj.y;
   }
   return acc;
 }
@@ -372,7 +372,7 @@ __device__ __forceinline__ void batch_update(int i, const FluidView& F, float ax
 // Pass 1 of every particle.  Particles of scenes without the deltaSPH density diffusion are
 // complete after it and are updated here; the others hand dpdt, acc and <grad rho> to
 // k_batch_diffusion, which finishes and updates them.
-__global__ void __launch_bounds__(128) k_batch_pass1(FluidView F, const float4* __restrict__ xv,
+__global__ void __launch_bounds__(128, 8) k_batch_pass1(FluidView F, const float4* __restrict__ xv,
                                                      const float4* __restrict__ qv, WallView W,
                                                      const SceneDev* __restrict__ scenes,
                                                      const int32_t* __restrict__ sid, float* __restrict__ dpdt,

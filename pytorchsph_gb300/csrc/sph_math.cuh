@@ -14,6 +14,7 @@ struct SphParams {
   float c_w;        // 7 / (pi h^2)           Wendland W
   float c_g;        // 7 / (pi h^3)           Wendland gradient (times 20 q (1-q)^3)
   float c_s;        // 30 / (pi h^3)          spiky gradient
+  float gk;         // -20 c_g / h: gradW = gk (1 - q)^3 (x_i - x_j)
   float eps;        // 0.1 h^2
   float rho0, c0, gamma;
   float tait_k;     // rho0 c0^2 / gamma
@@ -270,6 +271,7 @@ static inline SphParams to_params(const sph_params* p) {
   P.c_w = (float)(7.0 / 3.14159265358979323846 / (h * h));
   P.c_g = (float)(7.0 / 3.14159265358979323846 / (h * h * h));
   P.c_s = (float)(30.0 / 3.14159265358979323846 / (h * h * h));
+  P.gk = (float)(-20.0 * 7.0 / 3.14159265358979323846 / (h * h * h * h));
   P.eps = (float)(h * h * 0.1);
   P.rho0 = p->rest_density;
   P.c0 = p->c0;
