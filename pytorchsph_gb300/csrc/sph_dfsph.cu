@@ -355,9 +355,16 @@ __global__ void __launch_bounds__(256) k_dfsph_solve(FluidView F, WallView W, co
       B.partials[blockIdx.x] = t;
     }
     grid.sync();
-    // phase C: every block forms the same mean error in the same order
+    // phase C: every block forms the same mean error in the same order (a strided sum per
+    // thread, then a fixed tree over the block: identical arithmetic in every block)
     double tot = 0.0;
-    for (int k = 0; k < (int)gridDim.x; ++k) tot += B.partials[k];
+    for (int k = threadIdx.x; k < (int)gridDim.x; k += blockDim.x) tot += B.partials[k];
+    for (int o = 16; o > 0; o >>= 1) tot += __shfl_xor_sync(0xffffffffu, tot, o);
+    __syncthreads();  // s_part is reused
+    if ((threadIdx.x & 31) == 0) s_part[threadIdx.x >> 5] = tot;
+    __syncthreads();
+    tot = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) tot += s_part[w];
     err = tot / count;
     if (tid == 0) B.errors[it] = (float)err;
     ++it;
