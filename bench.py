@@ -107,6 +107,28 @@ def dist_env():
     return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
 
 
+def sync_ranks(world):
+    """Device synchronisation and, with several ranks, a barrier: brackets every timed region."""
+    import torch
+    import torch.distributed as dist
+    if torch.cuda.is_available():
+        torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+
+
+def max_over_ranks(x, world):
+    """The maximum of x over all ranks (the slowest replica sets the whole job's time)."""
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(x)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def hbm_peak():
     try:
         p = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
@@ -298,13 +320,13 @@ def run_serving(args, dev, world, rank):
     batch.check()
     st, en = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(dev.index or 0) as clk:
-        torch.cuda.synchronize()
+        sync_ranks(world)
         st.record()
         for _ in range(args.steps):
             batch.step()
         en.record()
-        torch.cuda.synchronize()
-    ms = st.elapsed_time(en) / args.steps
+        sync_ranks(world)
+    ms = max_over_ranks(st.elapsed_time(en) / args.steps, world)
     batch.check()
     value = total_p * world / (ms / 1e3)
     phases = phase_times(batch)
@@ -346,14 +368,18 @@ def run_serving(args, dev, world, rank):
     if not args.no_trace:
         # (c) end to end: every request queued at t = 0, continuous batching to completion
         reqs = [Request(t["rid"], 0.0, specs[k]) for k, t in enumerate(trace)]
-        torch.cuda.synchronize()
-        srv = Server(dev, budget_bytes=budget, rebuild_every=50, keep_final=False)
+        sync_ranks(world)
+        srv = Server(dev, budget_bytes=budget, rebuild_every=50, keep_final=True)   # final states to host
         wall = srv.run(reqs, time_scale=0.0, max_wall=600)
-        done = sum(r.steps_done >= r.spec.steps and r.error is None for r in reqs)
+        sync_ranks(world)
+        wall = max_over_ranks(wall, world)
+        done = sum(r.steps_done >= r.spec.steps and r.error is None and r.final is not None for r in reqs)
+        for r in reqs:
+            r.final = None
         h2d = sum(s.scene["pos"].nbytes * 2 + s.scene["rho"].nbytes * 3 + s.scene["wall_pos"].nbytes * 2 +
                   s.scene["wall_area"].nbytes for s in specs)
-        d2h = sum(s.scene["pos"].nbytes * 2 + s.scene["rho"].nbytes for s in specs)
-        e2e = {"value": srv.particle_steps / wall, "unit": "particle-steps/s",
+        d2h = sum(s.scene["pos"].nbytes * 2 + s.scene["rho"].nbytes for s in specs) + 4 * srv.batch_steps
+        e2e = {"value": srv.particle_steps * world / wall, "unit": "particle-steps/s",
                "h2d_bytes_per_step": h2d / max(srv.batch_steps, 1), "d2h_bytes_per_step": d2h / max(srv.batch_steps, 1),
                "wall_s": wall, "requests_completed": done, "batch_steps": srv.batch_steps, "rebuilds": srv.rebuilds,
                "rebuild_s": srv.rebuild_seconds, "requests_failed": len(srv.failed),
@@ -459,6 +485,7 @@ def run_search_density(args, dev, world, rank):
     phase_acc = {k: 0.0 for k in names[1:]}
     ok = True
     with ClockSampler(dev.index or 0) as clk:
+        sync_ranks(world)
         for k in range(args.steps):
             flush.zero_()
             starts[k].record()
@@ -470,7 +497,8 @@ def run_search_density(args, dev, world, rank):
                     phase_acc[b_] += events[a_].elapsed_time(events[b_])
             except Exception:
                 ok = False
-    ms = sum(a.elapsed_time(b) for a, b in zip(starts, ends)) / args.steps
+        sync_ranks(world)
+    ms = max_over_ranks(sum(a.elapsed_time(b) for a, b in zip(starts, ends)) / args.steps, world)
     value = n * world / (ms / 1e3)
     phases = {k: v / args.steps for k, v in phase_acc.items()} if ok else {}
     dom = max(["count", "fill"], key=lambda k: phases.get(k, 0.0)) if phases else "fill"
@@ -542,13 +570,14 @@ def run_dambreak(args, dev, world, rank):
         torch.cuda.synchronize()
         with ClockSampler(dev.index or 0) as clk:
             st, en = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            sync_ranks(world)
             st.record()
             for _ in range(args.steps):
                 b.step()
             en.record()
-            torch.cuda.synchronize()
+            sync_ranks(world)
         b.check()
-        ms = st.elapsed_time(en) / args.steps
+        ms = max_over_ranks(st.elapsed_time(en) / args.steps, world)
         n, launches = b.n, b.launches_per_step()
         config = {"workload": args.workload, "particles": n, "walls": b.nb,
                   "solver": "deltaSPH renormalized, semi-implicit Euler", "c0": c0, "graph": "one CUDA graph per step"}
@@ -567,13 +596,14 @@ def run_dambreak(args, dev, world, rank):
         torch.cuda.synchronize()
         with ClockSampler(dev.index or 0) as clk:
             st, en = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            sync_ranks(world)
             st.record()
             for _ in range(args.steps):
                 sim.step(sync=False)
             en.record()
-            torch.cuda.synchronize()
+            sync_ranks(world)
         sim.check()
-        ms = st.elapsed_time(en) / args.steps
+        ms = max_over_ranks(st.elapsed_time(en) / args.steps, world)
         n, launches = sim.n, 40
         config = {"workload": args.workload, "particles": n, "walls": sim.nb,
                   "solver": "DFSPH, divergence + density solves, semi-implicit Euler, adaptive dt",
@@ -632,12 +662,13 @@ def run_diff_drop(args, dev, world, rank):
     reps = max(1, args.steps)
     with ClockSampler(dev.index or 0) as clk:
         st, en = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        sync_ranks(world)
         st.record()
         for _ in range(reps):
             loss, gv, ga = r.loss_and_grad(v0, 0.01, target, steps)
         en.record()
-        torch.cuda.synchronize()
-    ms = st.elapsed_time(en) / reps
+        sync_ranks(world)
+    ms = max_over_ranks(st.elapsed_time(en) / reps, world)
     t0 = time.perf_counter()
     r.loss(v0, 0.01, target, steps)
     torch.cuda.synchronize()
