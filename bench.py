@@ -159,7 +159,10 @@ def traffic_from_profiles(workload, kernel, units):
 
 
 def base_line(args, world, value, ms, unit, config):
-    return {"metric": METRIC, "value": value, "unit": unit, "n_gpus": world, "steps": args.steps,
+    # the solver workloads report the serving metric (particle-steps/s); the search
+    # workloads count particles searched (with density) per second
+    return {"metric": METRIC if unit == METRIC else unit, "value": value, "unit": unit, "n_gpus": world,
+            "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": config}
 
