@@ -370,6 +370,10 @@ typedef struct sph_pair_terms_in {
   const float* pressure;    /* [n] fluidPressure */
   const float* L;           /* float4 [n] pseudo-inverted normalization matrix (fluidL) */
   const float* grad_rho;    /* float2 [n] renormalized density gradient */
+  const float* actual_area; /* [n] fluidActualArea (DFSPH) */
+  const float* pred_accel;  /* float2 [n] fluidPredAccel (DFSPH) */
+  const float* pred_vel;    /* float2 [n] fluidPredictedVelocity (DFSPH) */
+  double dt;                /* time step (DFSPH terms) */
   int64_t n;
 } sph_pair_terms_in;
 
@@ -382,6 +386,11 @@ typedef struct sph_pair_terms_in {
 #define SPH_TERM_PRESSURE_ACCEL 6          /* [n,2] pressure.py:31-38 */
 #define SPH_TERM_VELOCITY_DIFFUSION 7      /* [n,2] diffusion.py:30-44 */
 #define SPH_TERM_LAMINAR 8                 /* [n,2] laminar.py:30-46 */
+/* DFSPH (src/modules/dfsph.py), spiky gradient S_ij = e_ij kGS(q_ij), rho = fluidDensity: */
+#define SPH_TERM_DFSPH_ALPHA 9             /* [n,4] (kSum1 x, y, kSum2, 0), dfsph.py:58-72 */
+#define SPH_TERM_DFSPH_SOURCE 10           /* [n]   -dt sum A^act_j (v*_i - v*_j) . S_ij, dfsph.py:85-100 */
+#define SPH_TERM_DFSPH_PRESSURE_SUM 11     /* [n]   dt^2 sum A^act_j (a_i - a_j) . S_ij, dfsph.py:43-57 */
+#define SPH_TERM_DFSPH_ACCEL 12            /* [n,2] -sum A_j rho0 (p_i/(rho_i rho0)^2 + p_j/(rho_j rho0)^2) S_ij, dfsph.py:25-42 */
 /* out (=, or += when accumulate) one term per particle; params gives h, rest_density, c0,
  * alpha, delta, kinematic. */
 sph_status_t sph_pair_term(int32_t term, const sph_pair_terms_in* in, const sph_params* params, float* out,
@@ -402,6 +411,68 @@ sph_status_t sph_row_offsets(const int64_t* rows, int64_t num_pairs, int64_t n, 
 sph_status_t sph_pair_geometry(const int32_t* rows, const int32_t* cols, int64_t num_pairs, const float* query_pos,
                                const float* pos, const float* query_support, float threshold, float* dist,
                                float* radial, void* stream);
+
+/* ---------------------------------------------------------------- Boundary-module wall terms (a18) */
+
+/* The solid-wall terms of src/modules/solidBoundary.py for callers of its BoundaryModule
+ * interface, over the reference's own wall pair lists: pairs (b, f) of wall (or ghost) b
+ * and fluid particle f in wall order (boundaryToFluidNeighbors / ghostToFluidNeighbors of
+ * searchExisting) with e = (x_b - x_f) / r and q = r / h, and the same pairs grouped by
+ * fluid particle (sph_transpose_pairs).  Fluid arrays in original order. */
+typedef struct sph_wall_terms_in {
+  const int32_t* wall_offsets;   /* [nb+1] first pair of each wall (sph_row_offsets of rows) */
+  const int64_t* rows;           /* [P] wall of each pair */
+  const int64_t* cols;           /* [P] fluid particle of each pair */
+  const float* dist;             /* float2 [P] e = (x_b - x_f) / r */
+  const float* radial;           /* [P] q = r / h */
+  const int32_t* fluid_offsets;  /* [n+1] first grouped pair of each fluid particle */
+  const int32_t* fluid_pairs;    /* [P] pair indices grouped by fluid particle, ascending */
+  const float* pos;              /* float2 [n] fluid positions */
+  const float* vel;              /* float2 [n] */
+  const float* rho;              /* [n] fluidDensity (relative) */
+  const float* area;             /* [n] fluidArea */
+  const float* volume;           /* [n] fluidVolume */
+  const float* pressure;         /* [n] fluidPressure (deltaSPH) / fluidPressure2 (DFSPH) */
+  const float* L;                /* float4 [n] pseudo-inverted fluid normalization matrix */
+  const float* actual_area;      /* [n] fluidActualArea */
+  const float* pred_accel;       /* float2 [n] fluidPredAccel */
+  const float* pred_vel;         /* float2 [n] fluidPredictedVelocity */
+  const float* wall_pos;         /* float2 [nb] boundaryPositions */
+  const float* wall_ghost;       /* float2 [nb] boundaryGhostPositions */
+  const float* wall_area;        /* [nb] boundaryVolume (the wall particle's area) */
+  const float* wall_rho;         /* [nb] boundaryDensity (relative) */
+  const float* wall_volume;      /* [nb] boundaryVolume / boundaryDensity */
+  const float* wall_pressure;    /* [nb] boundaryPressure */
+  const float* wall_actual_area; /* [nb] boundaryActualArea */
+  const float* wall_term;        /* [nb] static wall-wall density term */
+  double dt;
+  int64_t n, nb;
+} sph_wall_terms_in;
+
+/* fluid-side sums, out per fluid particle (=, or += when accumulate) */
+#define SPH_WALL_DENSITY 0                 /* [n]   sum W A_b (:522-549) */
+#define SPH_WALL_DPDT 1                    /* [n]   continuity wall part (:746-770) */
+#define SPH_WALL_NORMALIZATION 2           /* [n,4] L wall part (:676-694) */
+#define SPH_WALL_RENORMALIZED_GRADIENT 3   /* [n,2] <grad rho> wall part (:695-717) */
+#define SPH_WALL_PRESSURE_ACCEL 4          /* [n,2] (:846-896) */
+#define SPH_WALL_VELOCITY_DIFFUSION 5      /* [n,2] (:820-844) */
+#define SPH_WALL_DFSPH_ALPHA 6             /* [n,4] (kSum1 x, y, kSum2, 0) PBSPH (:443-479) */
+#define SPH_WALL_DFSPH_SOURCE 7            /* [n]   (:481-520) */
+#define SPH_WALL_DFSPH_PRESSURE_SUM 8      /* [n]   (:405-441) */
+#define SPH_WALL_DFSPH_ACCEL 9             /* [n,2] PBSPH (:310-403) */
+/* wall-side sums, out per wall (=) */
+#define SPH_BWALL_DENSITY 20               /* [nb]  min(term + sum W A_f, 1) (:522-549) */
+#define SPH_BWALL_MDBC 21                  /* [nb]  mDBC density from ghost pairs (:561-617) */
+#define SPH_BWALL_DFSPH_ALPHA 22           /* [nb]  boundaryAlpha (:443-479) */
+#define SPH_BWALL_DFSPH_SOURCE 23          /* [nb]  boundarySource, density solve (:481-520) */
+#define SPH_BWALL_DFSPH_PRESSURE_SUM 24    /* [nb]  boundary kernel sum (:405-441) */
+sph_status_t sph_wall_term(int32_t term, const sph_wall_terms_in* in, const sph_params* params, float* out,
+                           int32_t accumulate, void* stream);
+/* Pairs grouped by column (fluid particle): col_offsets [n+1], pairs [num_pairs] = pair
+ * indices, ascending inside each column. */
+size_t sph_transpose_pairs_scratch_bytes(int64_t n);
+sph_status_t sph_transpose_pairs(const int64_t* cols, int64_t num_pairs, int64_t n, int32_t* col_offsets,
+                                 int32_t* pairs, void* scratch, size_t scratch_bytes, void* stream);
 
 /* ---------------------------------------------------------------- differentiable rollouts */
 

@@ -76,6 +76,9 @@ SIGNATURES.update({  # Module-interface terms
     "sph_pair_term": (_I32, [_I32, _P, _P, _P, _I32, _P]),
     "sph_particle_op": (_I32, [_I32, _I64, _P, _P, _P, _P, _I32, _P]),
     "sph_row_offsets": (_I32, [_P, _I64, _I64, _P, _P]),
+    "sph_wall_term": (_I32, [_I32, _P, _P, _P, _I32, _P]),
+    "sph_transpose_pairs_scratch_bytes": (_SZ, [_I64]),
+    "sph_transpose_pairs": (_I32, [_P, _I64, _I64, _P, _P, _P, _SZ, _P]),
     "sph_pair_geometry": (_I32, [_P, _P, _I64, _P, _P, _P, _F32, _P, _P, _P]),
 })
 

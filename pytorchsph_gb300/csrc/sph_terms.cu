@@ -33,8 +33,73 @@ struct TermIn {
   const float* pressure;
   const float4* L;
   const float2* grad_rho;
+  const float* aact;
+  const float2* pred_accel;
+  const float2* pred_vel;
+  float dt;
   int n;
 };
+
+// DFSPH terms of src/modules/dfsph.py over the pair list (spiky gradient S_ij = e_ij kGS(q)).
+template <int kTerm>
+__global__ void __launch_bounds__(128) k_dfsph_term(TermIn in, SphParams P, float* __restrict__ out, int accumulate) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= in.n) return;
+  const int k0 = in.offsets[i], k1 = in.offsets[i + 1];
+  const float dt = in.dt;
+  float s0 = 0.f, s1 = 0.f, s2 = 0.f;
+  const float2 vi = kTerm == SPH_TERM_DFSPH_SOURCE ? in.pred_vel[i] : make_float2(0.f, 0.f);
+  const float2 ai = kTerm == SPH_TERM_DFSPH_PRESSURE_SUM ? in.pred_accel[i] : make_float2(0.f, 0.f);
+  float ppi = 0.f;
+  if (kTerm == SPH_TERM_DFSPH_ACCEL) {
+    const float ri = in.rho[i] * P.rho0;
+    ppi = in.pressure[i] / (ri * ri);
+  }
+  for (int k = k0; k < k1; ++k) {
+    const int j = (int)__ldg(in.cols + k);
+    const float2 e = __ldg(in.dist + k);
+    const float gs = kGS(__ldg(in.radial + k), P.c_s);
+    const float sx = e.x * gs, sy = e.y * gs;
+    if (kTerm == SPH_TERM_DFSPH_ALPHA) {
+      const float aj = __ldg(in.aact + j);
+      s0 += aj * sx;
+      s1 += aj * sy;
+      s2 += aj * aj / (__ldg(in.area + j) * P.rho0) * (sx * sx + sy * sy);
+    } else if (kTerm == SPH_TERM_DFSPH_SOURCE) {
+      const float2 vj = __ldg(in.pred_vel + j);
+      s0 += -dt * __ldg(in.aact + j) * ((vi.x - vj.x) * sx + (vi.y - vj.y) * sy);
+    } else if (kTerm == SPH_TERM_DFSPH_PRESSURE_SUM) {
+      const float2 aj = __ldg(in.pred_accel + j);
+      const float f = dt * dt * __ldg(in.aact + j);
+      s0 += f * (ai.x - aj.x) * sx + f * (ai.y - aj.y) * sy;
+    } else if (kTerm == SPH_TERM_DFSPH_ACCEL) {
+      const float rj = __ldg(in.rho + j) * P.rho0;
+      const float ppj = __ldg(in.pressure + j) / (rj * rj);
+      const float f = -(__ldg(in.area + j) * P.rho0) * (ppi + ppj);
+      s0 += f * sx;
+      s1 += f * sy;
+    }
+  }
+  if (kTerm == SPH_TERM_DFSPH_ALPHA) {
+    float4* o = reinterpret_cast<float4*>(out) + i;
+    float4 v = make_float4(s0, s1, s2, 0.f);
+    if (accumulate) {
+      const float4 a = *o;
+      v = make_float4(a.x + v.x, a.y + v.y, a.z + v.z, a.w);
+    }
+    *o = v;
+  } else if (kTerm == SPH_TERM_DFSPH_ACCEL) {
+    float2* o = reinterpret_cast<float2*>(out) + i;
+    if (accumulate) {
+      const float2 a = *o;
+      s0 += a.x;
+      s1 += a.y;
+    }
+    *o = make_float2(s0, s1);
+  } else {
+    out[i] = accumulate ? out[i] + s0 : s0;
+  }
+}
 
 template <int kTerm>
 __global__ void __launch_bounds__(128) k_pair_term(TermIn in, SphParams P, float* __restrict__ out, int accumulate) {
@@ -242,9 +307,17 @@ sph_status_t sph_pair_term(int32_t term, const sph_pair_terms_in* in, const sph_
   SPH_REQUIRE(in && params && out && params->support > 0.f && in->n >= 0 && in->n < (1LL << 31),
               "pair_term: bad arguments");
   SPH_REQUIRE(in->n == 0 || (in->offsets && in->cols && in->radial), "pair_term: needs offsets, cols, radial");
-  const bool needs_geo = term != SPH_TERM_DENSITY;
+  const bool dfsph = term >= SPH_TERM_DFSPH_ALPHA && term <= SPH_TERM_DFSPH_ACCEL;
+  const bool needs_geo = term != SPH_TERM_DENSITY && !dfsph;
   SPH_REQUIRE(!needs_geo || (in->dist && in->pos && in->volume), "pair_term: needs distances, positions, volumes");
-  SPH_REQUIRE(term == SPH_TERM_DENSITY || term == SPH_TERM_NORMALIZATION || in->rho, "pair_term: needs densities");
+  SPH_REQUIRE(!dfsph || in->dist, "pair_term: needs distances");
+  SPH_REQUIRE(!dfsph || term == SPH_TERM_DFSPH_ACCEL || in->actual_area, "pair_term: needs actual areas");
+  SPH_REQUIRE((term != SPH_TERM_DFSPH_ALPHA && term != SPH_TERM_DFSPH_ACCEL) || in->area, "pair_term: needs areas");
+  SPH_REQUIRE(term != SPH_TERM_DFSPH_SOURCE || in->pred_vel, "pair_term: needs predicted velocities");
+  SPH_REQUIRE(term != SPH_TERM_DFSPH_PRESSURE_SUM || in->pred_accel, "pair_term: needs predicted accelerations");
+  SPH_REQUIRE(term != SPH_TERM_DFSPH_ACCEL || (in->rho && in->pressure), "pair_term: needs densities, pressures");
+  SPH_REQUIRE(term == SPH_TERM_DENSITY || term == SPH_TERM_NORMALIZATION || dfsph || in->rho,
+              "pair_term: needs densities");
   SPH_REQUIRE(term != SPH_TERM_DENSITY || in->area, "pair_term: density needs areas");
   SPH_REQUIRE((term != SPH_TERM_DIVERGENCE && term != SPH_TERM_VELOCITY_DIFFUSION && term != SPH_TERM_LAMINAR) ||
                   in->vel,
@@ -266,6 +339,10 @@ sph_status_t sph_pair_term(int32_t term, const sph_pair_terms_in* in, const sph_
   t.pressure = in->pressure;
   t.L = reinterpret_cast<const float4*>(in->L);
   t.grad_rho = reinterpret_cast<const float2*>(in->grad_rho);
+  t.aact = in->actual_area;
+  t.pred_accel = reinterpret_cast<const float2*>(in->pred_accel);
+  t.pred_vel = reinterpret_cast<const float2*>(in->pred_vel);
+  t.dt = (float)in->dt;
   t.n = (int)in->n;
   const SphParams P = to_params(params);
   const int nb = grid_for(in->n, 128);
@@ -285,6 +362,15 @@ sph_status_t sph_pair_term(int32_t term, const sph_pair_terms_in* in, const sph_
     SPH_TERM_CASE(SPH_TERM_VELOCITY_DIFFUSION)
     SPH_TERM_CASE(SPH_TERM_LAMINAR)
 #undef SPH_TERM_CASE
+#define SPH_DFSPH_CASE(T)                                             \
+  case T:                                                             \
+    k_dfsph_term<T><<<nb, 128, 0, st>>>(t, P, out, accumulate);       \
+    break;
+    SPH_DFSPH_CASE(SPH_TERM_DFSPH_ALPHA)
+    SPH_DFSPH_CASE(SPH_TERM_DFSPH_SOURCE)
+    SPH_DFSPH_CASE(SPH_TERM_DFSPH_PRESSURE_SUM)
+    SPH_DFSPH_CASE(SPH_TERM_DFSPH_ACCEL)
+#undef SPH_DFSPH_CASE
     default:
       set_error_text("pair_term: unknown term");
       return SPH_ERR_INVALID_ARGUMENT;

@@ -117,14 +117,31 @@ class BoundaryModule(Module):
 # ----------------------------------------------------------------------------- kernel plumbing
 class PairTermsC(ctypes.Structure):
     _fields_ = [(k, ctypes.c_void_p) for k in ("offsets", "cols", "dist", "radial", "pos", "vel", "rho", "volume",
-                                                "area", "pressure", "L", "grad_rho")] + [("n", ctypes.c_int64)]
+                                                "area", "pressure", "L", "grad_rho", "actual_area", "pred_accel",
+                                                "pred_vel")] + [("dt", ctypes.c_double), ("n", ctypes.c_int64)]
+
+
+class WallTermsC(ctypes.Structure):
+    _fields_ = [(k, ctypes.c_void_p) for k in (
+        "wall_offsets", "rows", "cols", "dist", "radial", "fluid_offsets", "fluid_pairs", "pos", "vel", "rho", "area",
+        "volume", "pressure", "L", "actual_area", "pred_accel", "pred_vel", "wall_pos", "wall_ghost", "wall_area",
+        "wall_rho", "wall_volume", "wall_pressure", "wall_actual_area", "wall_term")] + [
+        ("dt", ctypes.c_double), ("n", ctypes.c_int64), ("nb", ctypes.c_int64)]
 
 
 TERM = {"density": 0, "divergence": 1, "mog": 2, "normalization": 3, "renormalized_gradient": 4,
-        "delta_diffusion": 5, "pressure_accel": 6, "velocity_diffusion": 7, "laminar": 8}
+        "delta_diffusion": 5, "pressure_accel": 6, "velocity_diffusion": 7, "laminar": 8, "dfsph_alpha": 9,
+        "dfsph_source": 10, "dfsph_pressure_sum": 11, "dfsph_accel": 12}
+WALL = {"density": 0, "dpdt": 1, "normalization": 2, "renormalized_gradient": 3, "pressure_accel": 4,
+        "velocity_diffusion": 5, "dfsph_alpha": 6, "dfsph_source": 7, "dfsph_pressure_sum": 8, "dfsph_accel": 9,
+        "b_density": 20, "b_mdbc": 21, "b_dfsph_alpha": 22, "b_dfsph_source": 23, "b_dfsph_pressure_sum": 24}
+WALL_WIDTH = {"density": 1, "dpdt": 1, "normalization": 4, "renormalized_gradient": 2, "pressure_accel": 2,
+              "velocity_diffusion": 2, "dfsph_alpha": 4, "dfsph_source": 1, "dfsph_pressure_sum": 1,
+              "dfsph_accel": 2}
 OP = {"tait": 0, "volume": 1, "pinv2x2": 2, "gravity": 3}
 WIDTH = {"density": 1, "divergence": 1, "mog": 1, "normalization": 4, "renormalized_gradient": 2,
-         "delta_diffusion": 1, "pressure_accel": 2, "velocity_diffusion": 2, "laminar": 2}
+         "delta_diffusion": 1, "pressure_accel": 2, "velocity_diffusion": 2, "laminar": 2, "dfsph_alpha": 4,
+         "dfsph_source": 1, "dfsph_pressure_sum": 1, "dfsph_accel": 2}
 
 
 def _f32(t):
@@ -167,7 +184,8 @@ def row_offsets(simulationState):
     return off
 
 
-def pair_term(term, simulationState, P, pressure=None, L=None, grad_rho=None, out=None, accumulate=False):
+def pair_term(term, simulationState, P, pressure=None, L=None, grad_rho=None, out=None, accumulate=False,
+              actual_area=None, pred_accel=None, pred_vel=None, dt=0.0):
     """One summation of `term` over the state's pairs; returns [n], [n,2] or [n,2,2]."""
     st = simulationState
     n = st['fluidPosition'].shape[0]
@@ -178,20 +196,22 @@ def pair_term(term, simulationState, P, pressure=None, L=None, grad_rho=None, ou
     keep = [off, cols]
     arrays = {"dist": st.get('fluidDistances'), "radial": st.get('fluidRadialDistances'),
               "pos": st.get('fluidPosition'), "vel": st.get('fluidVelocity'), "rho": st.get('fluidDensity'),
-              "volume": vol, "area": st.get('fluidArea'), "pressure": pressure, "L": L, "grad_rho": grad_rho}
+              "volume": vol, "area": st.get('fluidArea'), "pressure": pressure, "L": L, "grad_rho": grad_rho,
+              "actual_area": actual_area, "pred_accel": pred_accel, "pred_vel": pred_vel}
     ptrs = {}
     for k, t in arrays.items():
         t = _f32(t)
         keep.append(t)
         ptrs[k] = N.ptr(t)
-    inp = PairTermsC(N.ptr(off), N.ptr(cols), ptrs["dist"], ptrs["radial"], ptrs["pos"], ptrs["vel"], ptrs["rho"],
-                     ptrs["volume"], ptrs["area"], ptrs["pressure"], ptrs["L"], ptrs["grad_rho"], n)
+    inp = PairTermsC(N.ptr(off), N.ptr(cols), *[ptrs[k] for k in (
+        "dist", "radial", "pos", "vel", "rho", "volume", "area", "pressure", "L", "grad_rho", "actual_area",
+        "pred_accel", "pred_vel")], float(dt), n)
     w = WIDTH[term]
     if out is None:
         out = torch.zeros((n,) if w == 1 else (n, w), dtype=torch.float32, device=st['fluidPosition'].device)
     N.call("sph_pair_term", TERM[term], ctypes.byref(inp), ctypes.byref(P), N.ptr(out), int(accumulate),
            N.stream_ptr())
-    return out.view(n, 2, 2) if w == 4 else out
+    return out.view(n, 2, 2) if term == "normalization" else out
 
 
 def particle_op(op, a, b, P, out, accumulate=False):
@@ -487,3 +507,408 @@ class gravityModule(Module):
 
     def evaluate(self, simulationState, simulation):
         particle_op("gravity", simulationState['fluidPosition'], None, self.P, simulationState['fluidAcceleration'])
+
+
+# ----------------------------------------------------------------------------- solid walls
+class _WallPairs:
+    """A wall -> fluid pair list of searchExisting (rows = wall, cols = fluid particle) with
+    its grouping by wall (row offsets) and by fluid particle (sph_transpose_pairs)."""
+
+    def __init__(self, neighbors, dist, radial, nb, n):
+        self.rows = neighbors[0].contiguous()
+        self.cols = neighbors[1].contiguous()
+        self.dist = _f32(dist)
+        self.radial = _f32(radial)
+        P = self.rows.shape[0]
+        dev = self.rows.device
+        st = N.stream_ptr()
+        self.woff = torch.empty(nb + 1, dtype=torch.int32, device=dev)
+        N.call("sph_row_offsets", N.ptr(self.rows), P, nb, N.ptr(self.woff), st)
+        self.foff = torch.empty(n + 1, dtype=torch.int32, device=dev)
+        self.fpairs = torch.empty(max(P, 1), dtype=torch.int32, device=dev)
+        scr = torch.empty((N.load().sph_transpose_pairs_scratch_bytes(n) + 7) // 8, dtype=torch.int64, device=dev)
+        N.call("sph_transpose_pairs", N.ptr(self.cols), P, n, N.ptr(self.foff), N.ptr(self.fpairs), N.ptr(scr),
+               scr.numel() * 8, st)
+
+
+def wall_term(term, pairs, P, n, nb, out=None, accumulate=False, dt=0.0, **arrays):
+    """One wall sum (sph_wall_term): fluid side -> [n], [n,2] or [n,4]; wall side -> [nb]."""
+    keep = {k: _f32(v) for k, v in arrays.items()}
+    names = ("pos", "vel", "rho", "area", "volume", "pressure", "L", "actual_area", "pred_accel", "pred_vel",
+             "wall_pos", "wall_ghost", "wall_area", "wall_rho", "wall_volume", "wall_pressure", "wall_actual_area",
+             "wall_term")
+    unknown = set(keep) - set(names)
+    if unknown:
+        raise N.SPHError(f"wall_term: unknown arrays {sorted(unknown)}")
+    inp = WallTermsC(N.ptr(pairs.woff), N.ptr(pairs.rows), N.ptr(pairs.cols), N.ptr(pairs.dist),
+                     N.ptr(pairs.radial), N.ptr(pairs.foff), N.ptr(pairs.fpairs),
+                     *[N.ptr(keep.get(k)) for k in names], float(dt), n, nb)
+    if out is None:
+        dev = pairs.rows.device
+        if WALL[term] >= 20:
+            out = torch.zeros(nb, dtype=torch.float32, device=dev)
+        else:
+            w = WALL_WIDTH[term]
+            out = torch.zeros((n,) if w == 1 else (n, w), dtype=torch.float32, device=dev)
+    N.call("sph_wall_term", WALL[term], ctypes.byref(inp), ctypes.byref(P), N.ptr(out), int(accumulate),
+           N.stream_ptr())
+    return out
+
+
+class solidBoundaryModule(BoundaryModule):
+    """src/modules/solidBoundary.py on GPU kernels: ghost-particle solid walls with mDBC wall
+    densities and the PBSPH pressure scheme (deltaSPH: continuity, L, <grad rho>, pressure
+    acceleration and velocity diffusion wall parts; DFSPH: summation wall density and the
+    alpha, source, pressure-sum and acceleration wall parts with the walls' own relaxed-Jacobi
+    pressures).  The wall particles come as arrays through `setWalls` (positions, mirrored
+    ghost positions, areas); sampling them from SDF or polygon descriptions
+    (solidBoundary.py:113-211) is scene set-up, outside this path."""
+
+    MLSscale = 1
+
+    def __init__(self):
+        super().__init__('densityInterpolation', 'Evaluates density at the current timestep')
+        self.active = False
+        self.boundaryToFluidNeighbors = None
+        self.ghostToFluidNeighbors = None
+
+    def getParameters(self):
+        return [
+            Parameter('solidBoundary', 'recomputeBoundary', 'bool', False, required=False, export=True, hint=''),
+            Parameter('solidBoundary', 'layers', 'int', 3, required=False, export=True, hint=''),
+        ]
+
+    def initialize(self, simulationConfig, simulationState):
+        cfg = simulationConfig
+        self.support = cfg['particle']['support']
+        self.threshold = cfg['neighborSearch']['gradientThreshold']
+        self.dtype = cfg['compute']['precision']
+        self.device = cfg['compute']['device']
+        self.layers = cfg['solidBoundary']['layers']
+        self.recomputeBoundary = cfg['solidBoundary']['recomputeBoundary']
+        self.boundaryPressureScheme = cfg['pressure']['boundaryPressureTerm']
+        self.fluidPressureScheme = cfg['pressure']['fluidPressureTerm']
+        self.relaxedJacobiOmega = cfg['dfsph']['relaxedJacobiOmega'] if 'dfsph' in cfg else 0.5
+        self.backgroundPressure = cfg['fluid']['backgroundPressure']
+        self.alpha = cfg['diffusion']['alpha']
+        self.delta = cfg['diffusion']['delta']
+        self.simulationDensityScheme = cfg['simulation']['densityScheme']
+        self.simulationScheme = cfg['simulation']['scheme']
+        self.gamma = cfg['pressure']['gamma']
+        self.c0 = _c0(cfg)
+        self.eps = self.support ** 2 * 0.1
+        self.restDensity = cfg['fluid']['restDensity']
+        if self.boundaryPressureScheme != 'PBSPH' or self.fluidPressureScheme != 'TaitEOS':
+            raise N.SPHError("solidBoundaryModule: the PBSPH boundary pressure with TaitEOS runs on this path")
+        self.P = _params(self.support, self.restDensity, self.c0, self.gamma, self.alpha, self.delta)
+
+    def setWalls(self, positions, ghostPositions, volumes):
+        """Wall particles (float32 CUDA [nb, 2], [nb, 2], [nb]); the walls are static."""
+        self.boundaryPositions = _f32(positions)
+        self.boundaryGhostPositions = _f32(ghostPositions)
+        self.boundaryVolume = _f32(volumes)
+        self.numPtcls = self.boundaryPositions.shape[0]
+        dev = self.boundaryPositions.device
+        self.boundarySupport = torch.full((self.numPtcls,), float(self.support), dtype=torch.float32, device=dev)
+        self.boundaryDensity = torch.ones(self.numPtcls, dtype=torch.float32, device=dev)
+        self.boundaryVelocity = torch.zeros((self.numPtcls, 2), dtype=torch.float32, device=dev)
+        self.boundaryAcceleration = torch.zeros((self.numPtcls, 2), dtype=torch.float32, device=dev)
+        self.boundaryRestDensity = torch.full((self.numPtcls,), float(self.restDensity), dtype=torch.float32,
+                                              device=dev)
+        self.staticBoundary = True
+        self.active = True
+        # static wall-wall density term sum_b' W A_b' (solidBoundary.py:180-200): a search of the
+        # walls among themselves with the density sum fused
+        res = GridSearch(dev).run(self.boundaryPositions, self.boundarySupport, self.boundaryVolume,
+                                  kernel_support=float(self.support))
+        self.boundaryDensityTerm = res.density()
+
+    def resetState(self, simulationState):
+        for k in ("boundaryPressure", "boundaryPressure2", "boundaryActualArea", "boundaryPredictedVelocity",
+                  "boundaryResidual", "boundaryAlpha", "boundarySource", "boundaryDensityContribution",
+                  "boundaryToFluidNeighbors", "boundaryToFluidNeighborDistances",
+                  "boundaryToFluidNeighborRadialDistances", "ghostToFluidNeighbors", "ghostToFluidNeighborDistances",
+                  "ghostToFluidNeighborRadialDistances", "fluidVolume", "pressure", "divergenceTerm", "dpdt"):
+            setattr(self, k, None)
+
+    # ------------------------------------------------------------------ neighborhoods
+    def boundaryNeighborhoodSearch(self, simulationState, simulation):
+        if not self.active:
+            return
+        n = simulationState['fluidPosition'].shape[0]
+        ns = simulation.neighborSearch
+        (self.boundaryToFluidNeighbors, self.boundaryToFluidNeighborDistances,
+         self.boundaryToFluidNeighborRadialDistances) = ns.searchExisting(
+            self.boundaryPositions, self.boundarySupport, simulationState, simulation)
+        (self.ghostToFluidNeighbors, self.ghostToFluidNeighborDistances,
+         self.ghostToFluidNeighborRadialDistances) = ns.searchExisting(
+            self.boundaryGhostPositions, self.boundarySupport * self.MLSscale, simulationState, simulation,
+            searchRadius=self.MLSscale)
+        self._bf = _WallPairs(self.boundaryToFluidNeighbors, self.boundaryToFluidNeighborDistances,
+                              self.boundaryToFluidNeighborRadialDistances, self.numPtcls, n)
+        self._gf = _WallPairs(self.ghostToFluidNeighbors, self.ghostToFluidNeighborDistances,
+                              self.ghostToFluidNeighborRadialDistances, self.numPtcls, n)
+
+    def _wall_volume(self):
+        out = torch.empty_like(self.boundaryVolume)
+        return particle_op("volume", self.boundaryVolume, self.boundaryDensity, self.P, out)
+
+    def _sum(self, term, st, pairs=None, out=None, **arrays):
+        n = st['fluidPosition'].shape[0]
+        return wall_term(term, pairs or self._bf, self.P, n, self.numPtcls, out=out,
+                         dt=float(st.get('dt', 0.0)), **arrays)
+
+    # ------------------------------------------------------------------ densities
+    def evalBoundaryDensity(self, simulationState, simulation):
+        if self.simulationDensityScheme == 'summation':
+            self.evalBoundaryDensitySummation(simulationState, simulation)
+        elif self.simulationDensityScheme == 'continuum':
+            self.computeBoundaryDensitymDBC(simulationState, simulation)
+
+    def evalBoundaryDensitySummation(self, simulationState, simulation):
+        st = simulationState
+        if self.boundaryToFluidNeighbors is None:
+            return torch.zeros_like(st['fluidDensity'])
+        self.boundaryDensityContribution = self._sum("density", st, wall_area=self.boundaryVolume)
+        self.boundaryDensity = self._sum("b_density", st, area=st['fluidArea'], wall_term=self.boundaryDensityTerm)
+        self.fluidVolume = self._wall_volume()
+        st['fluidDensity'] += self.boundaryDensityContribution
+
+    def computeBoundaryDensitymDBC(self, simulationState, simulation):
+        st = simulationState
+        self.boundaryDensity = self._sum("b_mdbc", st, pairs=self._gf, pos=st['fluidPosition'],
+                                         area=st['fluidArea'], volume=st['fluidVolume'],
+                                         wall_pos=self.boundaryPositions, wall_ghost=self.boundaryGhostPositions)
+
+    # ------------------------------------------------------------------ deltaSPH wall parts
+    def computeDpDt(self, simulationState, simulation):
+        st = simulationState
+        self.fluidVolume = self._wall_volume()
+        return self._sum("dpdt", st, vel=st['fluidVelocity'], wall_volume=self.fluidVolume,
+                         wall_rho=self.boundaryDensity)
+
+    def computeNormalizationMatrices(self, simulationState, simulation):
+        st = simulationState
+        n = st['fluidPosition'].shape[0]
+        self.fluidVolume = self._wall_volume()
+        out = self._sum("normalization", st, pos=st['fluidPosition'], wall_pos=self.boundaryPositions,
+                        wall_volume=self.fluidVolume)
+        return out.view(n, 2, 2)
+
+    def computeRenormalizedDensityGradient(self, simulationState, simulation):
+        st = simulationState
+        n = st['fluidPosition'].shape[0]
+        L = simulation.densityDiffusionModule.fluidL.reshape(n, 4)
+        return self._sum("renormalized_gradient", st, L=L, rho=st['fluidDensity'], wall_rho=self.boundaryDensity,
+                         wall_volume=self._wall_volume())
+
+    def computePressure(self, simulationState, simulation):
+        self.pressure = particle_op("tait", self.boundaryDensity, None, self.P, torch.empty_like(self.boundaryDensity))
+        return self.pressure
+
+    def computeVelocityDiffusion(self, simulationState, simulation):
+        st = simulationState
+        return self._sum("velocity_diffusion", st, pos=st['fluidPosition'], vel=st['fluidVelocity'],
+                         rho=st['fluidDensity'], wall_pos=self.boundaryPositions, wall_volume=self._wall_volume(),
+                         wall_rho=self.boundaryDensity)
+
+    def computePressureAcceleration(self, simulationState, simulation):
+        st = simulationState
+        self.fluidVolume = self._wall_volume()
+        return self._sum("pressure_accel", st, rho=st['fluidDensity'], pressure=st['fluidPressure'],
+                         wall_pressure=self.pressure, wall_volume=self.fluidVolume)
+
+    # ------------------------------------------------------------------ DFSPH wall parts (PBSPH)
+    def dfsphPrepareSolver(self, simulationState, simulation, density=True):
+        if not density or self.boundaryToFluidNeighbors is None:
+            return
+        self.boundaryPressure = torch.zeros_like(self.boundaryVolume)
+        self.boundaryPressure2 = torch.zeros_like(self.boundaryVolume)
+        self.boundaryActualArea = self._wall_volume()
+        self.boundaryPredictedVelocity = torch.zeros_like(self.boundaryPositions)   # static walls
+
+    def dfsphBoundaryAccelTerm(self, simulationState, simulation, density):
+        st = simulationState
+        if not density or self.boundaryToFluidNeighbors is None:
+            return torch.zeros_like(st['fluidPosition'])
+        return self._sum("dfsph_accel", st, rho=st['fluidDensity'], pressure=st['fluidPressure2'],
+                         wall_area=self.boundaryVolume, wall_rho=self.boundaryDensity,
+                         wall_pressure=self.boundaryPressure)
+
+    def dfsphBoundaryPressureSum(self, simulationState, simulation, density):
+        st = simulationState
+        if not density or self.boundaryToFluidNeighbors is None:
+            return torch.zeros_like(st['fluidDensity'])
+        ksum = self._sum("b_dfsph_pressure_sum", st, actual_area=st['fluidActualArea'], pred_accel=st['fluidPredAccel'])
+        self.boundaryResidual = ksum - self.boundarySource
+        p = self.boundaryPressure - self.relaxedJacobiOmega * self.boundaryResidual / self.boundaryAlpha
+        p = torch.clamp(p, min=0.)
+        if self.backgroundPressure:
+            p = torch.clamp(p, min=(5 ** 2) * self.restDensity)
+        self.boundaryPressure = p
+        return self._sum("dfsph_pressure_sum", st, pred_accel=st['fluidPredAccel'],
+                         wall_actual_area=self.boundaryActualArea)
+
+    def dfsphBoundaryAlphaTerm(self, simulationState, simulation, density):
+        st = simulationState
+        n = st['fluidPosition'].shape[0]
+        if not density or self.boundaryToFluidNeighbors is None:
+            return (torch.zeros((n, 2), dtype=torch.float32, device=st['fluidPosition'].device),
+                    torch.zeros(n, dtype=torch.float32, device=st['fluidPosition'].device))
+        k = self._sum("dfsph_alpha", st, wall_actual_area=self.boundaryActualArea, wall_area=self.boundaryVolume)
+        self.boundaryAlpha = self._sum("b_dfsph_alpha", st, actual_area=st['fluidActualArea'], area=st['fluidArea'],
+                                       wall_actual_area=self.boundaryActualArea)
+        return k[:, 0:2], k[:, 2]
+
+    def dfsphBoundarySourceTerm(self, simulationState, simulation, density):
+        st = simulationState
+        if not density or self.boundaryToFluidNeighbors is None:
+            return torch.zeros_like(st['fluidDensity'])
+        self.boundarySource = self._sum("b_dfsph_source", st, actual_area=st['fluidActualArea'],
+                                        pred_vel=st['fluidPredictedVelocity'], wall_rho=self.boundaryDensity)
+        return self._sum("dfsph_source", st, pred_vel=st['fluidPredictedVelocity'],
+                         wall_actual_area=self.boundaryActualArea)
+
+
+# ----------------------------------------------------------------------------- DFSPH
+class dfsphModule(Module):
+    """src/modules/dfsph.py:102-320: the divergence-free and constant-density solves of DFSPH,
+    each relaxed-Jacobi sweep one kernel per fluid term plus the boundary module's hooks, with
+    the reference's loop, error and iteration-count rules (the fused cooperative solver of
+    `pytorchsph_gb300.sim.Simulation` is the fast path)."""
+
+    def getParameters(self):
+        return [
+            Parameter('dfsph', 'minDensitySolverIterations', 'int', 2, required=False, export=True, hint=''),
+            Parameter('dfsph', 'minDivergenceSolverIterations', 'int', 2, required=False, export=True, hint=''),
+            Parameter('dfsph', 'maxDensitySolverIterations', 'int', 256, required=False, export=True, hint=''),
+            Parameter('dfsph', 'maxDivergenceSolverIterations', 'int', 8, required=False, export=True, hint=''),
+            Parameter('dfsph', 'densityThreshold', 'float', 1e-3, required=False, export=True, hint=''),
+            Parameter('dfsph', 'divergenceThreshold', 'float', 1e-2, required=False, export=True, hint=''),
+            Parameter('dfsph', 'divergenceSolver', 'bool', True, required=False, export=True, hint=''),
+            Parameter('dfsph', 'relaxedJacobiOmega', 'float', 0.5, required=False, export=True, hint=''),
+        ]
+
+    def __init__(self):
+        super().__init__('densityInterpolation', 'Evaluates density at the current timestep')
+
+    def initialize(self, simulationConfig, simulationState):
+        cfg = simulationConfig
+        self.support = cfg['particle']['support']
+        d = cfg['dfsph']
+        self.minDensitySolverIterations = d['minDensitySolverIterations']
+        self.minDivergenceSolverIterations = d['minDivergenceSolverIterations']
+        self.maxDensitySolverIterations = d['maxDensitySolverIterations']
+        self.maxDivergenceSolverIterations = d['maxDivergenceSolverIterations']
+        self.densityThreshold = d['densityThreshold']
+        self.divergenceThreshold = d['divergenceThreshold']
+        self.relaxedJacobiOmega = d['relaxedJacobiOmega'] if 'dfsph' in cfg else 0.5
+        self.backgroundPressure = cfg['fluid']['backgroundPressure']
+        self.pressureScheme = cfg['pressure']['boundaryPressureTerm']
+        self.P = _params(self.support, cfg['fluid']['restDensity'])
+
+    def _dt(self, st):
+        return float(st['dt'])
+
+    def computeAlpha(self, simulationState, simulation, density=True):
+        st = simulationState
+        k = pair_term("dfsph_alpha", st, self.P, actual_area=st['fluidActualArea'])
+        bk1, bk2 = simulation.boundaryModule.dfsphBoundaryAlphaTerm(st, simulation, density)
+        kSum1 = k[:, 0:2] + bk1
+        kSum2 = k[:, 2] + bk2
+        dt = self._dt(st)
+        fac = -dt ** 2 * st['fluidActualArea']
+        mass = st['fluidArea'] * st['fluidRestDensity']
+        alpha = fac / mass * torch.einsum('nd, nd -> n', kSum1, kSum1) + fac * kSum2
+        return torch.clamp(alpha, -1, -1e-7)
+
+    def computeSourceTerm(self, simulationState, simulation, density=True):
+        st = simulationState
+        source = pair_term("dfsph_source", st, self.P, actual_area=st['fluidActualArea'],
+                           pred_vel=st['fluidPredictedVelocity'], dt=self._dt(st))
+        source = source + simulation.boundaryModule.dfsphBoundarySourceTerm(st, simulation, density)
+        return 1. - st['fluidDensity'] + source if density else source
+
+    def computeUpdatedPressure(self, simulationState, simulation, density=True):
+        st = simulationState
+        kernelSum = pair_term("dfsph_pressure_sum", st, self.P, actual_area=st['fluidActualArea'],
+                              pred_accel=st['fluidPredAccel'], dt=self._dt(st))
+        kernelSum += simulation.boundaryModule.dfsphBoundaryPressureSum(st, simulation, density)
+        residual = kernelSum - st['fluidSourceTerm']
+        pressure = st['fluidPressure'] - 0.3 * residual / st['fluidAlpha']
+        pressure = torch.clamp(pressure, min=0.) if density else pressure
+        if density and self.backgroundPressure:
+            pressure = torch.clamp(pressure, min=(5 ** 2) * st['fluidRestDensity'])
+        if not bool(torch.isfinite(pressure).all()):
+            raise Exception('Pressure solver became unstable!')
+        return pressure, residual
+
+    def computeAcceleration(self, simulationState, simulation, density=True):
+        st = simulationState
+        a = pair_term("dfsph_accel", st, self.P, pressure=st['fluidPressure2'])
+        return a + simulation.boundaryModule.dfsphBoundaryAccelTerm(st, simulation, density)
+
+    def _solve(self, st, simulation, density):
+        errors = []
+        i = 0
+        error = 0.
+        if density:
+            minIters, maxIters, thr = (self.minDensitySolverIterations, self.maxDensitySolverIterations,
+                                       self.densityThreshold)
+            if 'densityErrors' in st:
+                minIters = max(minIters, len(st['densityErrors']) * 0.75)
+        else:
+            minIters, maxIters, thr = (self.minDivergenceSolverIterations, self.maxDivergenceSolverIterations,
+                                       self.divergenceThreshold)
+        while (i < minIters or error > thr) and i <= maxIters:
+            st['fluidPredAccel'] = self.computeAcceleration(st, simulation, density)
+            st['fluidPressure'][:] = st['fluidPressure2'][:]
+            st['fluidPressure2'], st['residual'] = self.computeUpdatedPressure(st, simulation, density)
+            if density and self.pressureScheme == 'PBSPH':
+                bm = simulation.boundaryModule
+                fluidError = torch.sum(torch.clamp(st['residual'], min=-thr))
+                boundaryError = torch.sum(torch.clamp(bm.boundaryResidual, min=-thr)) \
+                    if getattr(bm, 'boundaryResidual', None) is not None else 0.
+                error = (fluidError + boundaryError) / (getattr(bm, 'numPtcls', 0) + st['residual'].shape[0])
+            else:
+                error = torch.mean(torch.clamp(st['residual'], min=-thr))
+            errors.append(float(error))
+            error = float(error)
+            i += 1
+        return errors
+
+    def densitySolve(self, simulationState, simulation):
+        errors = self._solve(simulationState, simulation, True)
+        simulationState['densityErrors'] = errors
+        simulationState['densitySolverPressure'] = simulationState['fluidPressure']
+        return errors
+
+    def divergenceSolve(self, simulationState, simulation):
+        errors = self._solve(simulationState, simulation, False)
+        simulationState['divergenceErrors'] = errors
+        simulationState['divergenceSolverPressure'] = simulationState['fluidPressure']
+        return errors
+
+    def DFSPH(self, simulationState, simulation, density=True):
+        st = simulationState
+        x = st['fluidPosition']
+        st['fluidPredAccel'] = torch.zeros_like(x)
+        st['fluidPredictedVelocity'] = st['fluidVelocity'] + float(st['dt']) * st['fluidAcceleration']
+        st['fluidActualArea'] = st['fluidArea'] / st['fluidDensity']
+        simulation.boundaryModule.dfsphPrepareSolver(st, simulation, density)
+        st['fluidAlpha'] = self.computeAlpha(st, simulation, density)
+        st['fluidSourceTerm'] = self.computeSourceTerm(st, simulation, density)
+        n = st['numParticles']
+        st['fluidPressure2'] = torch.zeros(n, dtype=x.dtype, device=x.device)
+        st['fluidPressure'] = torch.zeros(n, dtype=x.dtype, device=x.device)
+        errors = self.densitySolve(st, simulation) if density else self.divergenceSolve(st, simulation)
+        st['fluidPredAccel'] = self.computeAcceleration(st, simulation, density)
+        st['fluidPressure'][:] = st['fluidPressure2'][:]
+        st['fluidPredictedVelocity'] += float(st['dt']) * st['fluidPredAccel']
+        return errors
+
+    def incompressibleSolver(self, simulationState, simulation):
+        return self.DFSPH(simulationState, simulation, True)
+
+    def divergenceSolver(self, simulationState, simulation):
+        return self.DFSPH(simulationState, simulation, False)

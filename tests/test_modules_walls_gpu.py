@@ -1,0 +1,158 @@
+"""The Module interface with solid walls (pytorchsph_gb300.modules.solidBoundaryModule) and the
+DFSPH solver module (dfsphModule), driven in the reference drivers' timestep order
+(src/deltaSPH.py:146-200, src/dfsph.py:134-202), against the restated reference step in
+float64 (oracle/sph_torch.py) on a dam break with three wall layers.
+
+Tolerances are relative to each field's maximum: acceleration and dpdt within 5e-3 (the
+float32 bar of the solver tests), wall densities within 1e-5; the DFSPH solves must take
+the same number of iterations as the float64 restatement."""
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-30))
+
+
+class Driver:
+    """The attributes of a reference simulation object that modules read."""
+
+    def sync(self, t):
+        return
+
+
+def config(sc, c0, density_scheme, diffusion="deltaSPH"):
+    return {
+        "particle": {"support": sc["h"], "packing": 0.4},
+        "fluid": {"restDensity": 1000.0, "c0": c0, "backgroundPressure": False},
+        "pressure": {"gamma": 7.0, "kappa": 1.0, "fluidPressureTerm": "TaitEOS", "boundaryPressureTerm": "PBSPH"},
+        "diffusion": {"alpha": 0.01, "delta": 0.1, "kinematic": 0.01, "boundaryDiffusion": True,
+                      "densityScheme": diffusion},
+        "compute": {"precision": torch.float32, "device": "cuda", "maxNeighbors": 256},
+        "neighborSearch": {"gradientThreshold": 1e-7, "supportScale": 1.0, "sortNeighborhoods": True},
+        "domain": {"virtualMin": [float(v) for v in sc["vmin"]], "virtualMax": [float(v) for v in sc["vmax"]]},
+        "simulation": {"densityScheme": density_scheme, "scheme": "deltaSPH", "boundaryScheme": "solid",
+                       "bodyForces": True},
+        "gravity": {"magnitude": 9.81, "direction": [0.0, -1.0], "pointSource": False, "potentialField": True,
+                    "center": [0.0, 0.0]},
+        "solidBoundary": {"recomputeBoundary": False, "layers": 3},
+        "dfsph": {"minDensitySolverIterations": 2, "minDivergenceSolverIterations": 2,
+                  "maxDensitySolverIterations": 100, "maxDivergenceSolverIterations": 100,
+                  "densityThreshold": 1e-4, "divergenceThreshold": 1e-3, "divergenceSolver": True,
+                  "relaxedJacobiOmega": 0.5},
+    }
+
+
+def setup(mods, cfg, st):
+    for m in mods:
+        for p in m.getParameters() or []:
+            p.parseConfig(cfg)
+        m.initialize(cfg, st)
+        m.resetState(st)
+
+
+def state(sc, dev, rho):
+    t = lambda a: torch.as_tensor(np.asarray(a, np.float32), device=dev).contiguous()
+    n = len(sc["pos"])
+    return {"fluidPosition": t(sc["pos"]), "fluidVelocity": t(sc["vel"]), "fluidDensity": t(rho),
+            "fluidArea": t(sc["area"]), "fluidSupport": t(sc["support"]), "numParticles": n,
+            "fluidRestDensity": t(np.full(n, 1000.0, np.float32))}
+
+
+def oracle_walls(sc):
+    import sph_torch as S
+    return S.Walls(torch.from_numpy(sc["wall_pos"]), torch.from_numpy(sc["ghost_pos"]),
+                   torch.from_numpy(sc["wall_area"]))
+
+
+def test_deltasph_timestep_with_walls_matches_reference_step(cuda):
+    import sph_torch as S
+    from pytorchsph_gb300 import modules as M
+    from pytorchsph_gb300 import workloads
+    sc = workloads.dam_break(30, 40, 0.01, (4.0, 2.0))
+    c0 = float(10 * np.sqrt(2 * 9.81 * sc["column_height"]))
+    rng = np.random.default_rng(7)
+    rho = (1.0 + 2e-3 * rng.random(len(sc["pos"]))).astype(np.float32)
+    st = state(sc, cuda, rho)
+    cfg = config(sc, c0, "continuum")
+    sim = Driver()
+    sim.neighborSearch = M.neighborSearchModule()
+    sim.boundaryModule = M.solidBoundaryModule()
+    sim.densityDiffusionModule = M.densityDiffusionModule()
+    dens, grav, mom, pres, visc, lam = (M.densityModule(), M.gravityModule(), M.momentumModule(),
+                                        M.pressureModule(), M.diffusionModule(), M.laminarViscosityModule())
+    setup([sim.neighborSearch, sim.boundaryModule, sim.densityDiffusionModule, dens, grav, mom, pres, visc, lam],
+          cfg, st)
+    t = lambda a: torch.as_tensor(np.asarray(a, np.float32), device=cuda).contiguous()
+    sim.boundaryModule.setWalls(t(sc["wall_pos"]), t(sc["ghost_pos"]), t(sc["wall_area"]))
+    sim.neighborSearch.search(st, sim)                                   # 2
+    sim.boundaryModule.boundaryNeighborhoodSearch(st, sim)               # 3
+    dens.evaluate(st, sim)                                               # 4
+    sim.boundaryModule.evalBoundaryDensity(st, sim)
+    st["fluidAcceleration"] = torch.zeros_like(st["fluidVelocity"])      # 6
+    grav.evaluate(st, sim)                                               # 7
+    mom.computeDpDt(st, sim)                                             # 8
+    sim.densityDiffusionModule.computeDensityDiffusion(st, sim)          # 9
+    pres.computePressure(st, sim)                                        # 10
+    pres.computePressureAcceleration(st, sim)
+    visc.evaluate(st, sim)                                               # 11
+    lam.computeLaminarViscosity(st, sim)                                 # 12
+    torch.cuda.synchronize()
+    p = S.Params(h=sc["h"], c0=c0, diffusion="deltaSPH", vmin=sc["vmin"], vmax=sc["vmax"], kinematic=0.01)
+    walls = oracle_walls(sc)
+    nb = S.search(torch.from_numpy(sc["pos"]), walls, sc["h"], sc["vmin"], sc["vmax"], torch.float64)
+    ref = {"x": torch.from_numpy(sc["pos"]).double(), "v": torch.from_numpy(sc["vel"]).double(),
+           "rho": torch.from_numpy(rho).double(), "area": torch.from_numpy(sc["area"]).double()}
+    acc, _, dpdt, ex = S.deltasph_rhs(ref, walls, nb, p, torch.float64)
+    assert rel(sim.boundaryModule.boundaryDensity.cpu(), ex["rho_b"]) < 1e-5
+    assert rel(st["fluidAcceleration"].cpu(), acc) < 5e-3
+    assert rel(st["dpdt"].cpu(), dpdt) < 5e-3
+
+
+def test_dfsph_timestep_with_walls_matches_reference_step(cuda):
+    import sph_torch as S
+    from pytorchsph_gb300 import modules as M
+    from pytorchsph_gb300 import workloads
+    sc = workloads.dam_break(30, 40, 0.01, (4.0, 2.0))
+    c0 = float(10 * np.sqrt(2 * 9.81 * sc["column_height"]))
+    dt = 5e-4
+    st = state(sc, cuda, sc["rho"])
+    st["dt"] = dt
+    cfg = config(sc, c0, "summation")
+    sim = Driver()
+    sim.neighborSearch = M.neighborSearchModule()
+    sim.boundaryModule = M.solidBoundaryModule()
+    dens, grav, dfsph, visc, lam = (M.densityModule(), M.gravityModule(), M.dfsphModule(), M.diffusionModule(),
+                                    M.laminarViscosityModule())
+    setup([sim.neighborSearch, sim.boundaryModule, dens, grav, dfsph, visc, lam], cfg, st)
+    t = lambda a: torch.as_tensor(np.asarray(a, np.float32), device=cuda).contiguous()
+    sim.boundaryModule.setWalls(t(sc["wall_pos"]), t(sc["ghost_pos"]), t(sc["wall_area"]))
+    sim.neighborSearch.search(st, sim)                                   # 2
+    sim.boundaryModule.boundaryNeighborhoodSearch(st, sim)               # 3
+    dens.evaluate(st, sim)                                               # 4
+    sim.boundaryModule.evalBoundaryDensity(st, sim)                      # 5
+    st["fluidAcceleration"] = torch.zeros_like(st["fluidVelocity"])      # 6
+    grav.evaluate(st, sim)                                               # 7
+    div_errors = dfsph.divergenceSolver(st, sim)                         # 8
+    st["fluidAcceleration"] += st["fluidPredAccel"]
+    dens_errors = dfsph.incompressibleSolver(st, sim)                    # 10
+    st["fluidAcceleration"] += st["fluidPredAccel"]
+    visc.evaluate(st, sim)                                               # 11
+    lam.computeLaminarViscosity(st, sim)                                 # 12
+    torch.cuda.synchronize()
+    p = S.Params(h=sc["h"], c0=c0, diffusion="MOG", vmin=sc["vmin"], vmax=sc["vmax"], kinematic=0.01)
+    walls = oracle_walls(sc)
+    walls.density_term = S.wall_density_term(walls, sc["h"], torch.float64)
+    nb = S.search(torch.from_numpy(sc["pos"]), walls, sc["h"], sc["vmin"], sc["vmax"], torch.float64)
+    ref = {"x": torch.from_numpy(sc["pos"]).double(), "v": torch.from_numpy(sc["vel"]).double(),
+           "rho": torch.from_numpy(sc["rho"]).double(), "area": torch.from_numpy(sc["area"]).double()}
+    acc, _, _, ex = S.dfsph_rhs(ref, walls, nb, p, dt, torch.float64)
+    assert len(div_errors) == len(ex["divergence_errors"])
+    assert len(dens_errors) == len(ex["density_errors"])
+    assert rel(sim.boundaryModule.boundaryDensity.cpu(), ex["rho_b"]) < 1e-5
+    assert rel(st["fluidAcceleration"].cpu(), acc) < 5e-3
