@@ -382,8 +382,9 @@ __global__ void __launch_bounds__(128, 8) k_batch_pass1(FluidView F, const float
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= F.n) return;
   const SceneDev& S = scenes[sid[i]];
-  const Pass1 o = pass1_body(i, F, xv, qv, W, S.g, S.P, S.coff);
-  if (S.P.diffusion == 2) {
+  const SphParams P = S.P;   // the fields the loop reads, in registers
+  const Pass1 o = pass1_body(i, F, xv, qv, W, S.g, P, S.coff);
+  if (P.diffusion == 2) {
     dpdt[i] = o.dpdt;
     acc[i] = make_float2(o.ax, o.ay);
     grad_rho[i] = o.grad_rho;
@@ -404,7 +405,8 @@ __global__ void __launch_bounds__(128) k_batch_diffusion(FluidView F, const floa
   if (i >= F.n) return;
   const SceneDev& S = scenes[sid[i]];
   if (S.P.diffusion != 2) return;
-  const float d = dpdt[i] + S.P.diff_k * diffusion_sum(i, F, qv, S.P, grad_rho);
+  const SphParams P = S.P;   // the fields the loop reads, in registers
+  const float d = dpdt[i] + P.diff_k * diffusion_sum(i, F, qv, P, grad_rho);
   const float2 a = acc[i];
   batch_update(i, F, a.x, a.y, d, S, xo, vo, ro, status);
 }
