@@ -53,6 +53,8 @@ def parse():
     ap.add_argument("--requests", type=int, default=1024)
     ap.add_argument("--trace-steps", type=int, default=1000)
     ap.add_argument("--no-trace", action="store_true", help="serving: skip the e2e and real-time trace runs")
+    ap.add_argument("--pairs", default="cells", choices=["cells", "csr"],
+                    help="serving: pairs from the cell rows, or a CSR neighbor list built every step")
     return ap.parse_args()
 
 
@@ -257,51 +259,44 @@ def serving_specs(n_requests, steps):
 
 
 def pass1_alg_bytes(batch):
-    """Algorithmic HBM bytes of one k_batch_pass1 launch: per particle its two 16-byte
-    neighbor records (read once; the other 27-odd reads of them are L1/L2 hits), key 4,
-    offsets 4, scene index 4 read, dpdt 4 + acc 8 + <grad rho> 8 written (64); 4 per CSR
-    column read; per wall position 8 + volume, density, pressure 12."""
-    P = int(batch.offsets[batch.n].item())
-    return batch.n * 64 + 4 * P + batch.nb * 20
+    """Algorithmic HBM bytes of one k_batch_pass1 launch over renormalized scenes.
+    Per particle: its two 16-byte neighbor records (read once; the other 27-odd reads of
+    them are L1/L2 hits), key 4, scene index 4 read, dpdt 4 + acc 8 + <grad rho> 8 written.
+    Pairs from the cell rows: the candidates' positions 8 read and three row masks 24
+    written (92), plus the cell table once.  CSR pairs: offsets 4 (64) and 4 per column.
+    Per wall: position 8 + volume, density, pressure 12."""
+    if batch.pairs == "csr":
+        P = int(batch.offsets[batch.n].item())
+        return batch.n * 64 + 4 * P + batch.nb * 20
+    return batch.n * 92 + (batch.cap + 2) * 4 + batch.nb * 20
 
 
 def phase_times(batch, reps=5):
     """Mean milliseconds of each phase of one batch step (eager, events between the calls;
     the step is run into scratch outputs so the batch state does not advance)."""
-    import ctypes
     import torch
     from pytorchsph_gb300 import _native as N
-    from pytorchsph_gb300.sim import FluidViewC
     acc = {}
-    xo = torch.empty_like(batch.a["x"])
-    vo = torch.empty_like(batch.a["v"])
-    ro = torch.empty_like(batch.a["rho"])
+    out = {"x": torch.empty_like(batch.a["x"]), "v": torch.empty_like(batch.a["v"]),
+           "rho": torch.empty_like(batch.a["rho"])}
+    names = ["sort+permute", "pair list", "walls+records", "pass1", "diffusion"]
     for _ in range(reps):
-        e = [torch.cuda.Event(enable_timing=True) for _ in range(7)]
+        e = [torch.cuda.Event(enable_timing=True) for _ in range(len(names) + 1)]
         torch.cuda.synchronize()
         e[0].record()
         batch._sort_permute()
         e[1].record()
-        batch._count()
+        batch._pair_list()
         e[2].record()
-        st = N.stream_ptr()
-        b = batch.b
-        N.call("sph_batch_nl_fill", N.ptr(b["x"]), N.ptr(b["sup"]), batch.n, N.ptr(batch.skeys),
-               N.ptr(batch.cell_start), N.ptr(batch.scenes), N.ptr(b["sid"]), N.ptr(batch.offsets), batch.pair_cap,
-               N.ptr(batch.cols), N.ptr(batch.status), st)
-        e[3].record()
-        fv = FluidViewC(N.ptr(b["x"]), N.ptr(b["v"]), N.ptr(b["rho"]), N.ptr(b["area"]), N.ptr(batch.skeys),
-                        N.ptr(batch.offsets), N.ptr(batch.cols), N.ptr(batch.cell_start), batch.n, batch.pair_cap)
         for k, mask in enumerate([N.SPH_PHASE_WALLS | N.SPH_PHASE_RECORDS, N.SPH_PHASE_PASS1,
                                   N.SPH_PHASE_DIFFUSION]):
-            N.call("sph_batch_deltasph_step", ctypes.byref(fv), ctypes.byref(batch.wall_view), N.ptr(batch.scenes),
-                   N.ptr(b["sid"]), N.ptr(batch.w["sid"]), N.ptr(batch.dpdt), N.ptr(batch.acc),
-                   N.ptr(batch.grad_rho), int(batch.any_renorm), N.ptr(xo), N.ptr(vo), N.ptr(ro),
-                   N.ptr(batch.status), mask, N.ptr(batch.forces_scratch), batch.forces_scratch.numel() * 8, st)
-            e[4 + k].record()
+            batch.forces(out, mask)
+            e[3 + k].record()
         torch.cuda.synchronize()
-        for k, name in enumerate(["sort+permute", "count+scan", "fill", "walls+records", "pass1", "diffusion"]):
+        for k, name in enumerate(names):
             acc[name] = acc.get(name, 0.0) + e[k].elapsed_time(e[k + 1]) / reps
+    if batch.pairs != "csr":
+        del acc["pair list"]
     return acc
 
 
@@ -315,7 +310,7 @@ def run_serving(args, dev, world, rank):
     budget = 60e9
 
     # (a) device-resident batch of every request: W warm-up + K timed batch steps
-    batch = SceneBatch(specs, dev)
+    batch = SceneBatch(specs, dev, pairs=args.pairs)
     batch.capture()
     for _ in range(max(args.warmup, 3)):
         batch.step()
@@ -348,7 +343,7 @@ def run_serving(args, dev, world, rank):
     pick = sorted(set(order[int(q * (len(order) - 1))] for q in np.linspace(0, 1, 16)))
     one = []
     for k in pick:
-        b1 = SceneBatch([specs[k]], dev)
+        b1 = SceneBatch([specs[k]], dev, pairs=args.pairs)
         b1.capture()
         for _ in range(3):
             b1.step()
@@ -372,7 +367,8 @@ def run_serving(args, dev, world, rank):
         # (c) end to end: every request queued at t = 0, continuous batching to completion
         reqs = [Request(t["rid"], 0.0, specs[k]) for k, t in enumerate(trace)]
         sync_ranks(world)
-        srv = Server(dev, budget_bytes=budget, rebuild_every=50, keep_final=True)   # final states to host
+        srv = Server(dev, budget_bytes=budget, rebuild_every=50, keep_final=True,   # final states to host
+                     pairs=args.pairs)
         wall = srv.run(reqs, time_scale=0.0, max_wall=600)
         sync_ranks(world)
         wall = max_over_ranks(wall, world)
@@ -391,7 +387,7 @@ def run_serving(args, dev, world, rank):
             s.dev = None
         # (d) real-time trace: Poisson arrivals at 50 / s
         reqs = [Request(t["rid"], t["arrival"], specs[k]) for k, t in enumerate(trace)]
-        srv = Server(dev, budget_bytes=budget, rebuild_every=20, keep_final=False)
+        srv = Server(dev, budget_bytes=budget, rebuild_every=20, keep_final=False, pairs=args.pairs)
         wall = srv.run(reqs, time_scale=1.0, max_wall=600)
         lat = srv.latency_percentiles((50, 99))
         ttc = [r.finished - r.arrival for r in reqs if r.finished >= 0 and r.error is None]
@@ -413,11 +409,13 @@ def run_serving(args, dev, world, rank):
                       "3-layer walls", "budget_gb": budget / 1e9,
             "batch_bytes": batch_bytes, "l2": f"state of {total_p} particles >> L2 (no flush needed)",
             "graph": "one CUDA graph per batch step", "parallelism": f"replicas{world}",
+            "pairs": "from the cell rows (no neighbor list)" if args.pairs == "cells" else "CSR list every step",
             "scene_generation_s": gen_s})
         line["phases_ms"] = {k: round(v, 4) for k, v in phases.items()}
         line["roofline"] = {"bound": "hbm", "kernel": "deltaSPH forces (k_batch_pass1)", "achieved": achieved,
                             "peak": peak, "unit": "GB/s", "frac": achieved / peak if achieved else None,
-                            "traffic": traffic_from_profiles("serving", "k_batch_pass1", total_p), "algorithmic_bytes": alg,
+                            "traffic": traffic_from_profiles("serving", f"k_batch_pass1[{args.pairs}]", total_p),
+                            "algorithmic_bytes": alg,
                             "peak_source": peak_src}
         line["serving"] = {"one_scene_gpu_path": {"value": one_scene_value, "unit": "particle-steps/s",
                                                   "sample": [{"n": n, "ms_per_step": t * 1e3} for n, t in one]},

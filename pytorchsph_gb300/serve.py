@@ -122,9 +122,17 @@ def upload_scenes(specs, device):
 
 
 class SceneBatch:
-    """A fixed set of scenes stepped together (deltaSPH, semi-implicit Euler)."""
+    """A fixed set of scenes stepped together (deltaSPH, semi-implicit Euler).
 
-    def __init__(self, specs, device=None, states=None, pair_headroom: float = 1.3):
+    pairs = "cells": the force passes take each particle's pairs straight from its cell rows
+    (no neighbor list; pass 1 keeps per-row bit masks for the diffusion pass).  pairs =
+    "csr": a CSR neighbor list is counted and filled every step first.  Both visit the
+    pairs in the same order and give the same sums."""
+
+    def __init__(self, specs, device=None, states=None, pair_headroom: float = 1.3, pairs: str = "cells"):
+        if pairs not in ("cells", "csr"):
+            raise ValueError("pairs must be 'cells' or 'csr'")
+        self.pairs = pairs
         self.lib = N.load()
         self.device = torch.device(device or torch.device("cuda", torch.cuda.current_device()))
         dev = self.device
@@ -199,9 +207,6 @@ class SceneBatch:
         self.hist = torch.zeros(self.cap + 1, dtype=torch.int32, device=dev)
         self.cs_scratch = torch.empty((self.lib.sph_counting_sort_scratch_bytes(n, self.cap) + 7) // 8,
                                       dtype=torch.int64, device=dev)
-        self.counts = torch.empty(n, dtype=torch.int32, device=dev)
-        self.offsets = torch.empty(n + 1, dtype=torch.int32, device=dev)
-        self.scan_scratch = torch.empty((self.lib.sph_scan_scratch_bytes(n) + 7) // 8, dtype=torch.int64, device=dev)
         self.dpdt = torch.empty(n, dtype=torch.float32, device=dev)
         self.acc = torch.empty((n, 2), dtype=torch.float32, device=dev)
         self.grad_rho = torch.empty((n, 2), dtype=torch.float32, device=dev) if self.any_renorm else None
@@ -210,12 +215,19 @@ class SceneBatch:
         # walls: concatenated, sorted once by (scene, cell)
         self.nb = sum(len(w) for w in wpos)
         self._setup_walls(wpos, wgh, war, wsid)
-        # pair capacity from a first count
-        self._sort_permute()
-        self._count()
-        P = int(self.offsets[n].item())
-        self.pair_cap = int(P * pair_headroom) + 1024
-        self.cols = torch.empty(self.pair_cap, dtype=torch.int32, device=dev)
+        self.counts = self.offsets = self.cols = None
+        self.pair_cap = 0
+        if pairs == "csr":
+            self.counts = torch.empty(n, dtype=torch.int32, device=dev)
+            self.offsets = torch.empty(n + 1, dtype=torch.int32, device=dev)
+            self.scan_scratch = torch.empty((self.lib.sph_scan_scratch_bytes(n) + 7) // 8, dtype=torch.int64,
+                                            device=dev)
+            # pair capacity from a first count
+            self._sort_permute()
+            self._count()
+            P = int(self.offsets[n].item())
+            self.pair_cap = int(P * pair_headroom) + 1024
+            self.cols = torch.empty(self.pair_cap, dtype=torch.int32, device=dev)
         self.graph = None
         self.steps_done = 0
 
@@ -279,29 +291,48 @@ class SceneBatch:
         N.call("sph_exclusive_scan_i32", N.ptr(self.counts), N.ptr(self.offsets), n, N.ptr(self.scan_scratch),
                self.scan_scratch.numel() * 8, st)
 
-    def step_kernels(self):
-        """The batch step as a fixed kernel sequence (no host synchronisation)."""
-        st = N.stream_ptr()
-        n = self.n
-        a, b = self.a, self.b
-        self._sort_permute()
+    def _pair_list(self):
+        """The CSR neighbor list of the sorted batch (pairs = "csr" only)."""
+        if self.pairs != "csr":
+            return
+        b = self.b
         self._count()
-        N.call("sph_batch_nl_fill", N.ptr(b["x"]), N.ptr(b["sup"]), n, N.ptr(self.skeys), N.ptr(self.cell_start),
-               N.ptr(self.scenes), N.ptr(b["sid"]), N.ptr(self.offsets), self.pair_cap, N.ptr(self.cols),
-               N.ptr(self.status), st)
-        fv = FluidViewC(N.ptr(b["x"]), N.ptr(b["v"]), N.ptr(b["rho"]), N.ptr(b["area"]), N.ptr(self.skeys),
-                        N.ptr(self.offsets), N.ptr(self.cols), N.ptr(self.cell_start), n, self.pair_cap)
+        N.call("sph_batch_nl_fill", N.ptr(b["x"]), N.ptr(b["sup"]), self.n, N.ptr(self.skeys),
+               N.ptr(self.cell_start), N.ptr(self.scenes), N.ptr(b["sid"]), N.ptr(self.offsets), self.pair_cap,
+               N.ptr(self.cols), N.ptr(self.status), N.stream_ptr())
+
+    def fluid_view(self):
+        """The sorted batch as the C ABI's fluid view (no CSR arrays with pairs = "cells")."""
+        b = self.b
+        return FluidViewC(N.ptr(b["x"]), N.ptr(b["v"]), N.ptr(b["rho"]), N.ptr(b["area"]), N.ptr(self.skeys),
+                          N.ptr(self.offsets), N.ptr(self.cols), N.ptr(self.cell_start), self.n, self.pair_cap)
+
+    def forces(self, out, phases=None):
+        """The launches of sph_batch_deltasph_step selected by `phases` (all by default),
+        writing the updated state to out["x"], out["v"], out["rho"]."""
+        b = self.b
+        fv = self.fluid_view()
         N.call("sph_batch_deltasph_step", ctypes.byref(fv), ctypes.byref(self.wall_view), N.ptr(self.scenes),
                N.ptr(b["sid"]), N.ptr(self.w["sid"]), N.ptr(self.dpdt), N.ptr(self.acc), N.ptr(self.grad_rho),
-               int(self.any_renorm), N.ptr(a["x"]), N.ptr(a["v"]), N.ptr(a["rho"]), N.ptr(self.status),
-               N.SPH_PHASE_ALL, N.ptr(self.forces_scratch), self.forces_scratch.numel() * 8, st)
+               int(self.any_renorm), N.ptr(out["x"]), N.ptr(out["v"]), N.ptr(out["rho"]), N.ptr(self.status),
+               N.SPH_PHASE_ALL if phases is None else phases, N.ptr(self.forces_scratch),
+               self.forces_scratch.numel() * 8, N.stream_ptr())
+
+    def step_kernels(self):
+        """The batch step as a fixed kernel sequence (no host synchronisation)."""
+        a, b = self.a, self.b
+        self._sort_permute()
+        self._pair_list()
+        self.forces(a)
         N.permute_arrays(None, [(b[k], a[k]) for k in ("area", "sup", "sid", "uid")])
 
     # kernels of this library launched by one batch step (for the bench's launch count): keys 1,
-    # counting sort (scan 3 + scatter + fix + fix_large) 6, permute 1, count 1, scan 3, fill 1,
-    # mdbc 1, records 1, pass1 + update 1 (+ diffusion + update 1 when renormalized), copy 1
+    # counting sort (scan 3 + scatter + fix + fix_large) 6, permute 1, [csr: count 1, scan 3,
+    # fill 1], mdbc 1, records 1, pass1 + update 1 (+ diffusion + update 1 when
+    # renormalized), copy 1
     def launches_per_step(self):
-        return 1 + 6 + 1 + 1 + 3 + 1 + (1 if self.nb else 0) + 1 + 1 + (1 if self.any_renorm else 0) + 1
+        csr = 1 + 3 + 1 if self.pairs == "csr" else 0
+        return 1 + 6 + 1 + csr + (1 if self.nb else 0) + 1 + 1 + (1 if self.any_renorm else 0) + 1
 
     def capture(self):
         """Capture one batch step into a CUDA graph (after a warm-up step)."""
@@ -336,7 +367,7 @@ class SceneBatch:
         f = self.flags() & ~allow
         if f:
             raise N.SPHError(f"batch step: {N.decode_flags(f)}")
-        if int(self.offsets[self.n].item()) > self.pair_cap:
+        if self.pairs == "csr" and int(self.offsets[self.n].item()) > self.pair_cap:
             raise N.SPHError("batch step: neighbor pair buffer too small")
 
     def escaped(self):
@@ -375,15 +406,19 @@ class SceneBatch:
         tot = 0
         for d in (self.a, self.b):
             tot += sum(t.numel() * t.element_size() for t in d.values())
-        tot += self.cols.numel() * 4 + (self.cap + 2) * 8 + self.n * 40
+        if self.cols is not None:
+            tot += self.cols.numel() * 4 + self.n * 8
+        tot += self.forces_scratch.numel() * 8 + (self.cap + 2) * 8 + self.n * 32
         return tot
 
 
-def estimate_bytes(scene) -> int:
-    """Device bytes one scene needs in a batch (state x2, sort, CSR at ~30 pairs/particle)."""
+def estimate_bytes(scene, pairs: str = "cells") -> int:
+    """Device bytes one scene needs in a batch: state x2, sort, force records and row masks,
+    and with pairs = "csr" the CSR list at ~30 pairs/particle."""
     n = len(scene["pos"])
     nb = len(scene.get("wall_pos", ()))
-    return n * (2 * 36 + 60 + 30 * 4 * 1.3) + nb * 60 + 4096
+    csr = 8 + 30 * 4 * 1.3 if pairs == "csr" else 0
+    return int(n * (2 * 36 + 32 + 56 + csr) + nb * 60 + 4096)
 
 
 # ----------------------------------------------------------------------------- continuous batching
@@ -412,13 +447,14 @@ class Server:
     with `Request.error` set; the other scenes, which share no data with it, carry on."""
 
     def __init__(self, device=None, budget_bytes: float = 60e9, rebuild_every: int = 20, use_graph: bool = True,
-                 keep_final: bool = True, pair_headroom: float = 1.3):
+                 keep_final: bool = True, pair_headroom: float = 1.3, pairs: str = "cells"):
         self.device = torch.device(device or torch.device("cuda", torch.cuda.current_device()))
         self.budget = budget_bytes
         self.rebuild_every = rebuild_every
         self.use_graph = use_graph
         self.keep_final = keep_final
         self.pair_headroom = pair_headroom
+        self.pairs = pairs
         self.live: list[Request] = []
         self.batch: SceneBatch | None = None
         self.particle_steps = 0
@@ -462,9 +498,9 @@ class Server:
                 else:
                     keep.append(r)
                     states.append(st)
-        used = sum(estimate_bytes(r.spec.scene) for r in keep)
+        used = sum(estimate_bytes(r.spec.scene, self.pairs) for r in keep)
         while queue and queue[0].arrival <= now:
-            need = estimate_bytes(queue[0].spec.scene)
+            need = estimate_bytes(queue[0].spec.scene, self.pairs)
             if used + need > self.budget and keep:
                 break
             r = queue.pop(0)
@@ -477,7 +513,7 @@ class Server:
         self._last_flags = 0
         if keep:
             self.batch = SceneBatch([r.spec for r in keep], self.device, states=states,
-                                    pair_headroom=self.pair_headroom)
+                                    pair_headroom=self.pair_headroom, pairs=self.pairs)
             self.rebuilds += 1
             if self.use_graph:
                 self.batch.capture()          # runs one step eagerly, then records it

@@ -1,7 +1,8 @@
 """Batched serving (pytorchsph_gb300.serve): every scene gives the same result alone and in
 any mix of scenes (bitwise: scenes share no data and each cell is ordered by particle id),
-a batch of one equals the single-scene engine, a captured CUDA graph equals eager launches,
-rebuilding the batch mid-run changes nothing, and the request loop completes a trace."""
+a batch of one equals the single-scene engine, pairs taken from the cell rows equal pairs
+from a CSR list, a captured CUDA graph equals eager launches, rebuilding the batch mid-run
+changes nothing, and the request loop completes a trace."""
 import numpy as np
 import pytest
 import torch
@@ -19,9 +20,9 @@ def spec(kind, n, shape, steps=5):
     return SceneSpec(sc, cfg, steps)
 
 
-def run_batch(specs, steps, dev, graph=False):
+def run_batch(specs, steps, dev, graph=False, pairs="cells"):
     from pytorchsph_gb300.serve import SceneBatch
-    b = SceneBatch(specs, dev)
+    b = SceneBatch(specs, dev, pairs=pairs)
     if graph:
         b.capture()
         steps -= 1
@@ -55,6 +56,18 @@ def test_batch_of_one_equals_single_scene_engine(cuda):
     s = sim.state()
     b = run_batch([A], 6, cuda)[0]
     assert same(s, b)
+
+
+def test_cell_pairs_equal_csr_pairs(cuda):
+    """Both pair sources visit the same pairs in the same order: bitwise equal states, for
+    renormalized and MOG scenes in one batch."""
+    import dataclasses
+    A, B = spec("dam_break", 3000, 1.2), spec("drop", 2600, 0.8)
+    C = spec("dam_break", 2500, 0.6)
+    C = dataclasses.replace(C, cfg=dataclasses.replace(C.cfg, density_diffusion="MOG"))
+    cells = run_batch([A, B, C], 6, cuda, pairs="cells")
+    csr = run_batch([A, B, C], 6, cuda, pairs="csr")
+    assert all(same(x, y) for x, y in zip(cells, csr))
 
 
 def test_graph_replay_equals_eager(cuda):
@@ -132,7 +145,7 @@ def test_pair_overflow_holds_the_step(cuda):
     from pytorchsph_gb300 import _native as N
     from pytorchsph_gb300.serve import SceneBatch
     A = spec("dam_break", 3000, 1.0)
-    b = SceneBatch([A], cuda, pair_headroom=0.5)
+    b = SceneBatch([A], cuda, pair_headroom=0.5, pairs="csr")
     before = b.scene_state(0)
     b.step()
     assert b.flags() & N.SPH_FLAG_PAIR_CAPACITY
@@ -147,7 +160,7 @@ def test_server_recovers_from_pair_overflow(cuda):
     from pytorchsph_gb300.serve import Request, Server
     A, B = spec("dam_break", 3000, 1.2, steps=5), spec("drop", 2600, 0.9, steps=7)
     reqs = [Request(0, 0.0, A), Request(1, 0.0, B)]
-    srv = Server(cuda, rebuild_every=4, pair_headroom=0.5)
+    srv = Server(cuda, rebuild_every=4, pair_headroom=0.5, pairs="csr")
     srv.run(reqs, time_scale=1.0, max_wall=120)
     assert srv.pair_overflows >= 1
     assert all(r.steps_done == r.spec.steps and r.error is None for r in reqs)
