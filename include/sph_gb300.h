@@ -273,7 +273,7 @@ sph_status_t sph_mdbc_wall_density(const sph_fluid_view* fluid, const sph_wall_v
  * artificial viscosity (diffusion.py:12-25) + laminar viscosity (laminar.py:12-27), each
  * with its wall part (solidBoundary.py:746-890).  Wall quantities must come from
  * sph_mdbc_wall_density.  scratch: sph_deltasph_scratch_bytes(n) bytes of device memory
- * (per-particle neighbor records). */
+ * (per-particle neighbor records, and the cell-row masks of sph_batch_deltasph_step). */
 size_t sph_deltasph_scratch_bytes(int64_t n);
 sph_status_t sph_deltasph_forces(const sph_fluid_view* fluid, const sph_wall_view* walls, const sph_grid* grid,
                                  const sph_params* params, float* dpdt, float* acc, float* L, float* grad_rho,
@@ -332,6 +332,12 @@ sph_status_t sph_batch_nl_fill(const float* xy, const float* sorted_support, int
  * the step is not applied: the outputs are the sorted inputs unchanged.  dpdt [n], acc
  * float2 [n] and grad_rho float2 [n] carry the renormalized scenes' first pass to their
  * diffusion pass (needed when any_renormalized); scratch as for sph_deltasph_forces.
+ * With fluid->offsets and fluid->cols both NULL no neighbor list is needed: the records
+ * launch also stores, per particle, the first candidate and a 64-bit accepted-candidate
+ * mask of each of its three cell rows (search_radius 1; other radii test their cell rows
+ * in the force passes), and both force passes visit those pairs, in the CSR fill's order
+ * (same sums).  Each scene's pair test then uses its own support (sph_params.support),
+ * which must be every particle's support.
  * `phases` selects the launches (SPH_PHASE_ALL for a step; single phases, in order, let a
  * caller time each kernel): walls = mDBC wall densities, records = per-particle neighbor
  * records, pass1 = first pair pass (+ update of scenes without deltaSPH diffusion),
