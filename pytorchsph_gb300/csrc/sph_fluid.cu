@@ -97,16 +97,16 @@ __device__ __forceinline__ void mdbc_body(int b, const FluidView& F, const WallV
 
 // ---------------------------------------------------------------------------- neighbor records
 // What neighbor j brings to every pair term, computed once per particle instead of once
-// per pair: xv = (x, y, vx, vy) and q = (rho_j, V_j = A_j / rho~_j, p_j = Tait(rho~_j),
-// m_j = rho_j V_j).  Two 16-byte loads per pair replace four scalar loads, a division and
-// the Tait power.
+// per pair: xv = (x, y, vx, vy) and q = (rho_j, V_j = A_j / rho~_j, p_j V_j with p_j =
+// Tait(rho~_j), m_j = rho_j V_j).  Two 16-byte loads per pair replace four scalar loads, a
+// division and the Tait power.
 __device__ __forceinline__ void prep_body(int i, const FluidView& F, const SphParams& P, float4* __restrict__ xv,
                                           float4* __restrict__ qv) {
   const float2 x = F.x[i], v = F.v[i];
   const float rt = F.rho[i];
   const float V = F.area[i] / rt, rho = rt * P.rho0;
   xv[i] = make_float4(x.x, x.y, v.x, v.y);
-  qv[i] = make_float4(rho, V, tait(rt, P), rho * V);
+  qv[i] = make_float4(rho, V, tait(rt, P) * V, rho * V);
 }
 
 // Pair geometry in the form the sums need: d = x_i - x_j, r2 = |d|^2 and the Wendland
@@ -132,42 +132,27 @@ __device__ __forceinline__ PairG pair_g(float xi, float yi, float xj, float yj, 
 // ---------------------------------------------------------------------------- cell-row pairs
 // The pairs of particle i straight from the cell table, without a CSR list: its candidates
 // are the contiguous sorted ranges of its 2r+1 cell rows (cells cx-r..cx+r of each row).
-// A range is tested in chunks of 64 candidates into a bit mask, and the accepted
+// A range is tested in segments of 32 candidates into a bit mask, and the accepted
 // candidates are visited in increasing index: the CSR fill's order, so every sum is the
 // same.  Visiting set bits keeps a warp's lanes together the way a CSR row does (a lane
 // runs the pair body only for its own neighbors).
 //
-// With r = 1 the records pass stores, per particle and row slot s (row cy - 1 + s), the
-// row's first candidate rows[s * n + i] and its mask masks[s * n + i] (empty row: 0), or,
-// for a row of 64 candidates or more, kLongRow | the row's end, re-tested by the force
-// passes.  The force passes read 36 bytes per particle instead of a CSR row.
-constexpr uint64_t kLongRow = 1ull << 63;
+// The records pass stores each particle's non-empty segments in order, at most
+// kMaxSegments: start seg_start[k * n + i] and mask seg_mask[k * n + i] for k < nseg[i]
+// (nseg[i] = -1 when there are more; the force passes then test its cell rows
+// themselves).  A force pass holds one segment and the next one, loaded ahead, so moving
+// on to the next segment costs a lane a register move.
+constexpr int kMaxSegments = 8;
 
-__device__ __forceinline__ uint64_t chunk_mask(const float2* __restrict__ x, int c, int e, float xi, float yi,
-                                               float thr) {
-  const int len = min(e - c, 64);
-  const int len_lo = min(len, 32);
-  uint32_t lo = 0, hi = 0;
-  for (int t = 0; t < len_lo; ++t) {
+__device__ __forceinline__ uint32_t segment_mask(const float2* __restrict__ x, int c, int e, float xi, float yi,
+                                                 float thr) {
+  const int len = min(e - c, 32);
+  uint32_t m = 0;
+  for (int t = 0; t < len; ++t) {
     const float2 pj = __ldg(x + c + t);
-    lo |= (uint32_t)(dist2_ref(xi, yi, pj.x, pj.y) <= thr) << t;
+    m |= (uint32_t)(dist2_ref(xi, yi, pj.x, pj.y) <= thr) << t;
   }
-  for (int t = 32; t < len; ++t) {
-    const float2 pj = __ldg(x + c + t);
-    hi |= (uint32_t)(dist2_ref(xi, yi, pj.x, pj.y) <= thr) << (t - 32);
-  }
-  return ((uint64_t)hi << 32) | lo;
-}
-
-// Visits c + t for the set bits t of m, in increasing order, below n.
-template <typename Fn>
-__device__ __forceinline__ void visit_mask(uint64_t m, int c, int n, Fn&& fn) {
-  while (m) {
-    const int j = c + __ffsll((long long)m) - 1;
-    if (j >= n) return;
-    m &= m - 1;
-    fn(j);
-  }
+  return m;
 }
 
 // Every row of the window, tested here (any r).
@@ -181,82 +166,89 @@ __device__ __forceinline__ void cell_pairs(const FluidView& F, const sph_grid& g
   for (int yy = y0; yy <= y1; ++yy) {
     const int row = yy * g.cells_x;
     const int b = __ldg(cs + row + x0), e = __ldg(cs + row + x1 + 1);
-    for (int c = b; c < e; c += 64) visit_mask(chunk_mask(F.x, c, e, xi, yi, thr), c, F.n, fn);
+    for (int c = b; c < e; c += 32) {
+      uint32_t w = segment_mask(F.x, c, e, xi, yi, thr);
+      while (w) {
+        const int j = c - 1 + __ffs(w);
+        w &= w - 1;
+        fn(j);
+      }
+    }
   }
 }
 
-// The three row slots of particle i (r = 1) for the force passes.
-__device__ __forceinline__ void row_masks_body(int i, const FluidView& F, const sph_grid& g, int coff, float thr,
-                                               int32_t* __restrict__ rows, uint64_t* __restrict__ masks) {
+// The segment list of particle i.
+__device__ __forceinline__ void segments_body(int i, const FluidView& F, const sph_grid& g, int coff, int r,
+                                              float thr, int32_t* __restrict__ nseg, int32_t* __restrict__ seg_start,
+                                              uint32_t* __restrict__ seg_mask) {
   int cx, cy;
   cell_of(F.keys[i] - (uint32_t)coff, g, &cx, &cy);
   const float2 xi = F.x[i];
-  const int x0 = max(cx - 1, 0), x1 = min(cx + 1, g.cells_x - 1);
-  const int32_t* cs = F.cell_start + coff;
-  for (int s = 0; s < 3; ++s) {
-    const int yy = cy - 1 + s;
-    int b = 0;
-    uint64_t m = 0;
-    if (x0 <= x1 && yy >= 0 && yy < g.cells_y) {
-      const int row = yy * g.cells_x;
-      b = __ldg(cs + row + x0);
-      const int e = __ldg(cs + row + x1 + 1);
-      if (e - b >= 64) m = kLongRow | (uint32_t)e;
-      else if (e > b) m = chunk_mask(F.x, b, e, xi.x, xi.y, thr);
-    }
-    rows[(size_t)s * F.n + i] = b;
-    masks[(size_t)s * F.n + i] = m;
-  }
-}
-
-// The bits of a stored row mask that can name a particle: none for a start outside
-// [0, n), none past index n - 1.
-__device__ __forceinline__ uint64_t clip_row(uint64_t m, int b, int n) {
-  if (b < 0 || b >= n) return 0;
-  return n - b < 64 ? m & ((1ull << (n - b)) - 1) : m;
-}
-
-// The pairs of particle i from its stored row slots.  One loop over the rows' six 32-bit
-// mask words (a lane moves on to its next word inside the loop), so a warp runs as many
-// pair bodies as its lane with the most neighbors, as over a CSR row; a long row sends the
-// particle through the row-by-row path.
-template <typename Fn>
-__device__ __forceinline__ void stored_pairs(int i, const FluidView& F, const int32_t* __restrict__ rows,
-                                             const uint64_t* __restrict__ masks, float xi, float yi, float thr,
-                                             Fn&& fn) {
   const size_t n = (size_t)F.n;
-  const int b0 = rows[i], b1 = rows[n + i], b2 = rows[2 * n + i];
-  uint64_t m0 = masks[i], m1 = masks[n + i], m2 = masks[2 * n + i];
-  if ((m0 | m1 | m2) & kLongRow) {
-#pragma unroll
-    for (int s = 0; s < 3; ++s) {
-      const int b = s == 0 ? b0 : (s == 1 ? b1 : b2);
-      const uint64_t m = s == 0 ? m0 : (s == 1 ? m1 : m2);
-      if (b < 0) continue;
-      if (m & kLongRow) {
-        const int e = min((int)(uint32_t)m, F.n);
-        for (int c = b; c < e; c += 64) visit_mask(chunk_mask(F.x, c, e, xi, yi, thr), c, F.n, fn);
-      } else {
-        visit_mask(m, b, F.n, fn);
+  int k = 0;
+  const int x0 = max(cx - r, 0), x1 = min(cx + r, g.cells_x - 1);
+  const int y0 = max(cy - r, 0), y1 = min(cy + r, g.cells_y - 1);
+  const int32_t* cs = F.cell_start + coff;
+  if (x0 <= x1) {
+    for (int yy = y0; yy <= y1; ++yy) {
+      const int row = yy * g.cells_x;
+      const int b = __ldg(cs + row + x0), e = __ldg(cs + row + x1 + 1);
+      for (int c = b; c < e; c += 32) {
+        const uint32_t w = segment_mask(F.x, c, e, xi.x, xi.y, thr);
+        if (w == 0) continue;
+        if (k < kMaxSegments) {
+          seg_start[k * n + i] = c;
+          seg_mask[k * n + i] = w;
+        }
+        ++k;
       }
     }
+  }
+  nseg[i] = k <= kMaxSegments ? k : -1;
+}
+
+// The bits of a stored segment that name a particle: none for a start outside [0, n),
+// none at index n or past it.
+__device__ __forceinline__ uint32_t clip_segment(uint32_t w, int b, int n) {
+  if ((unsigned)b >= (unsigned)n) return 0;
+  return n - b < 32 ? w & ((1u << (n - b)) - 1) : w;
+}
+
+// The pairs of particle i from its segment list (its cell rows when the list overflowed).
+template <typename Fn>
+__device__ __forceinline__ void stored_pairs(int i, const FluidView& F, const sph_grid& g, int coff, int r,
+                                             const int32_t* __restrict__ nseg, const int32_t* __restrict__ seg_start,
+                                             const uint32_t* __restrict__ seg_mask, float xi, float yi, float thr,
+                                             Fn&& fn) {
+  const int ns = nseg[i];
+  if (ns < 0 || ns > kMaxSegments) {
+    int cx, cy;
+    cell_of(F.keys[i] - (uint32_t)coff, g, &cx, &cy);
+    cell_pairs(F, g, r, coff, cx, cy, xi, yi, thr, fn);
     return;
   }
-  m0 = clip_row(m0, b0, F.n);
-  m1 = clip_row(m1, b1, F.n);
-  m2 = clip_row(m2, b2, F.n);
-  // word k: bits of row k / 2, candidates from base(k) = start + 32 (k & 1)
-  uint32_t w = (uint32_t)m0;
-  int base = b0 - 1, k = 0;   // __ffs counts from 1
+  if (ns == 0) return;
+  const size_t n = (size_t)F.n;
+  int b = seg_start[i];
+  uint32_t w = clip_segment(seg_mask[i], b, F.n);
+  int bn = 0;
+  uint32_t wn = 0;
+  if (ns > 1) {
+    bn = seg_start[n + i];
+    wn = seg_mask[n + i];
+  }
+  int k = 0;
   for (;;) {
     while (w == 0) {
-      if (k == 5) return;
-      ++k;
-      const uint64_t m = k < 2 ? m0 : (k < 4 ? m1 : m2);
-      w = (k & 1) ? (uint32_t)(m >> 32) : (uint32_t)m;
-      base = (k < 2 ? b0 : (k < 4 ? b1 : b2)) + ((k & 1) << 5) - 1;
+      if (++k >= ns) return;
+      b = bn;
+      w = clip_segment(wn, bn, F.n);
+      if (k + 1 < ns) {
+        bn = seg_start[(k + 1) * n + i];
+        wn = seg_mask[(k + 1) * n + i];
+      }
     }
-    const int j = base + __ffs(w);
+    const int j = b - 1 + __ffs(w);
     w &= w - 1;
     fn(j);
   }
@@ -273,59 +265,59 @@ struct Pass1 {
   float2 grad_rho;
 };
 
-// kCells: pairs from the stored row slots (cell rows tested here when r != 1) instead of
-// the CSR row.
+// Pairs from the segment lists S (kCells) instead of the CSR row.
+struct Segments {
+  const int32_t* nseg;
+  const int32_t* start;
+  const uint32_t* mask;
+};
+
 template <bool kCells>
 __device__ __forceinline__ Pass1 pass1_body(int i, const FluidView& F, const float4* __restrict__ xv,
                                             const float4* __restrict__ qv, const WallView& W, const sph_grid& g,
-                                            const SphParams& P, int coff, const int32_t* __restrict__ rows,
-                                            const uint64_t* __restrict__ masks) {
+                                            const SphParams& P, int coff, const Segments& S) {
   const float4 si = xv[i];
-  const float4 qi = qv[i];
-  const float rhoi = qi.x, pi = qi.z;
+  const float rhoi = qv[i].x, pi = tait(F.rho[i], P);
   const bool renorm = P.diffusion == 2;
-  const float mu2 = 2.0f * rhoi * P.kinematic;
+  const float mu8 = 4.0f * (2.0f * rhoi * P.kinematic);   // 4 (mu_i + mu_j), both rho_i nu
   float dp_f = 0.f, mog = 0.f;
   float pax = 0.f, pay = 0.f, vax = 0.f, vay = 0.f, lax = 0.f, lay = 0.f;
-  float l00 = 0.f, l01 = 0.f, l10 = 0.f, l11 = 0.f, gfx = 0.f, gfy = 0.f;
+  float l00 = 0.f, l01 = 0.f, l11 = 0.f, gfx = 0.f, gfy = 0.f;
   auto fluid_pair = [&](int j) {
     const float4 sj = __ldg(xv + j), qj = __ldg(qv + j);
-    const float rhoj = qj.x, Vj = qj.y, pj = qj.z, mj = qj.w;
+    const float rhoj = qj.x, Vj = qj.y, pVj = qj.z, mj = qj.w;
     const PairG e = pair_g(si.x, si.y, sj.x, sj.y, P);   // gradW = e.gd * d
     const float ux = sj.z - si.z, uy = sj.w - si.w;       // u_j - u_i
     const float ud = ux * e.dx + uy * e.dy;               // (u_j - u_i) . d
     const float ir2 = __fdividef(1.0f, e.r2 + P.eps);
     const float rg = -e.gd * e.r2;                        // (x_j - x_i) . gradW
     dp_f -= e.gd * ud * mj;
-    if (P.diffusion == 1) mog += 2.0f * (rhoj - rhoi) * ir2 * rg * Vj;
-    const float pf = (pi + pj) * Vj * e.gd;
+    if (P.diffusion == 1) mog += (rhoj - rhoi) * ir2 * rg * Vj;   // x 2 after the sum
+    const float pf = fmaf(pi, Vj, pVj) * e.gd;            // (p_i + p_j) V_j gd
     pax += pf * e.dx;
     pay += pf * e.dy;
     const float irs = __fdividef(1.0f, rhoi + rhoj);
-    const float vf = fminf(-ud, 0.f) * ir2 * mj * irs * e.gd;   // pi_ij, (u_j - u_i) . (x_j - x_i) = -ud
+    const float w = mj * irs * ir2;
+    const float vf = fminf(-ud, 0.f) * w * e.gd;          // pi_ij, (u_j - u_i) . (x_j - x_i) = -ud
     vax += vf * e.dx;
     vay += vf * e.dy;
-    const float term = 4.0f * mj * mu2 * rg * irs * irs * ir2;   // laminar: -term (u_i - u_j)
+    const float term = mu8 * rg * irs * w;                // laminar: -term (u_i - u_j)
     lax += term * ux;
     lay += term * uy;
     if (renorm) {
-      const float t = Vj * e.gd;                          // V_j (x_j - x_i) (x) gradW = -t d (x) d
+      // V_j (x_j - x_i) (x) gradW = -t d (x) d: symmetric, one off-diagonal sum
+      const float t = Vj * e.gd;
       const float tx = t * e.dx, ty = t * e.dy;
       l00 -= tx * e.dx;
       l01 -= tx * e.dy;
-      l10 -= ty * e.dx;
       l11 -= ty * e.dy;
-      const float s = 2.0f * (rhoj - rhoi) * t;
+      const float s = (rhoj - rhoi) * t;                  // x 2 after the sum
       gfx += s * e.dx;
       gfy += s * e.dy;
     }
   };
-  int cx = 0, cy = 0;
-  const bool direct = kCells && P.search_radius != 1;
-  if (direct || W.n > 0) cell_of(F.keys[i] - (uint32_t)coff, g, &cx, &cy);
   if constexpr (kCells) {
-    if (direct) cell_pairs(F, g, P.search_radius, coff, cx, cy, si.x, si.y, P.thr, fluid_pair);
-    else stored_pairs(i, F, rows, masks, si.x, si.y, P.thr, fluid_pair);
+    stored_pairs(i, F, g, coff, P.search_radius, S.nseg, S.start, S.mask, si.x, si.y, P.thr, fluid_pair);
   } else {
     const int k0 = F.offsets[i], k1 = row_end(F, i, k0);
     for (int k = k0; k < k1; ++k) fluid_pair(__ldg(F.cols + k));
@@ -333,6 +325,8 @@ __device__ __forceinline__ Pass1 pass1_body(int i, const FluidView& F, const flo
   float dp_w = 0.f, pwx = 0.f, pwy = 0.f, vwx = 0.f, vwy = 0.f;
   float w00 = 0.f, w01 = 0.f, w10 = 0.f, w11 = 0.f, gwx = 0.f, gwy = 0.f;
   if (W.n > 0) {
+    int cx, cy;
+    cell_of(F.keys[i] - (uint32_t)coff, g, &cx, &cy);
     const float thr = P.thr;
     for_each_wall(
         W, g, P.search_radius, cx, cy, si.x, si.y, thr,
@@ -366,7 +360,7 @@ __device__ __forceinline__ Pass1 pass1_body(int i, const FluidView& F, const flo
   }
   Pass1 o;
   o.dpdt = dp_f + dp_w;
-  if (P.diffusion == 1) o.dpdt += P.diff_k * mog;
+  if (P.diffusion == 1) o.dpdt += P.diff_k * (2.0f * mog);
   float ax, ay;
   if (P.point_source) {
     float dx = si.x - P.point_cx, dy = si.y - P.point_cy;
@@ -388,7 +382,9 @@ __device__ __forceinline__ Pass1 pass1_body(int i, const FluidView& F, const flo
   ay += P.visc_k * vay + P.visc_k * vwy;
   o.ax = ax + lax;
   o.ay = ay + lay;
-  o.L = make_float4(l00 + w00, l01 + w01, l10 + w10, l11 + w11);
+  o.L = make_float4(l00 + w00, l01 + w01, l01 + w10, l11 + w11);
+  gfx *= 2.0f;
+  gfy *= 2.0f;
   o.grad_rho = make_float2(0.f, 0.f);
   if (renorm) {
     const float4 Li = pinv2x2(o.L.x, o.L.y, o.L.z, o.L.w);
@@ -401,13 +397,11 @@ __device__ __forceinline__ Pass1 pass1_body(int i, const FluidView& F, const flo
 
 // D_i = sum_j [2 (rho_j - rho_i)/(|x_ji|^2 + eps) x_ji - (<grad rho>_i + <grad rho>_j)] . gradW_ij V_j
 // (the deltaSPH density diffusion before its h delta c0 factor).
-// kCells: pairs from the stored row slots (cell rows tested here when r != 1) instead of
-// the CSR row.
+// kCells: pairs from the segment lists instead of the CSR row.
 template <bool kCells>
 __device__ __forceinline__ float diffusion_sum(int i, const FluidView& F, const float4* __restrict__ qv,
                                                const SphParams& P, const float2* __restrict__ grad_rho,
-                                               const sph_grid& g, int coff, const int32_t* __restrict__ rows,
-                                               const uint64_t* __restrict__ masks) {
+                                               const sph_grid& g, int coff, const Segments& S) {
   const float2 xi = F.x[i], gi = grad_rho[i];
   const float rhoi = qv[i].x;
   float acc = 0.f;
@@ -421,13 +415,7 @@ __device__ __forceinline__ float diffusion_sum(int i, const FluidView& F, const 
     acc += e.gd * pd * qj.y;
   };
   if constexpr (kCells) {
-    if (P.search_radius != 1) {
-      int cx, cy;
-      cell_of(F.keys[i] - (uint32_t)coff, g, &cx, &cy);
-      cell_pairs(F, g, P.search_radius, coff, cx, cy, xi.x, xi.y, P.thr, pair);
-    } else {
-      stored_pairs(i, F, rows, masks, xi.x, xi.y, P.thr, pair);
-    }
+    stored_pairs(i, F, g, coff, P.search_radius, S.nseg, S.start, S.mask, xi.x, xi.y, P.thr, pair);
   } else {
     const int k0 = F.offsets[i], k1 = row_end(F, i, k0);
     for (int k = k0; k < k1; ++k) pair(__ldg(F.cols + k));
@@ -471,7 +459,7 @@ __global__ void __launch_bounds__(128) k_dsph_pass1(FluidView F, const float4* _
                                                     float4* __restrict__ Lout, float2* __restrict__ grad_rho) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= F.n) return;
-  const Pass1 o = pass1_body<false>(i, F, xv, qv, W, *gp, P, 0, nullptr, nullptr);
+  const Pass1 o = pass1_body<false>(i, F, xv, qv, W, *gp, P, 0, Segments{});
   dpdt[i] = o.dpdt;
   acc[i] = make_float2(o.ax, o.ay);
   if (Lout) Lout[i] = o.L;
@@ -482,7 +470,7 @@ __global__ void __launch_bounds__(128) k_dsph_diffusion(FluidView F, const float
                                                         const float2* __restrict__ grad_rho, float* __restrict__ dpdt) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= F.n) return;
-  dpdt[i] += P.diff_k * diffusion_sum<false>(i, F, qv, P, grad_rho, sph_grid{}, 0, nullptr, nullptr);
+  dpdt[i] += P.diff_k * diffusion_sum<false>(i, F, qv, P, grad_rho, sph_grid{}, 0, Segments{});
 }
 
 __global__ void k_sie(int n, const float2* __restrict__ x, const float2* __restrict__ v,
@@ -504,16 +492,16 @@ __global__ void __launch_bounds__(128) k_batch_mdbc(FluidView F, WallView W, con
   mdbc_body(b, F, W, S.g, S.P, S.coff);
 }
 
-// Neighbor records and, with pairs from the cell rows (rows != NULL), the row slots.
+// Neighbor records and, with pairs from the cell rows (nseg != NULL), the segment lists.
 __global__ void __launch_bounds__(256) k_batch_prep(FluidView F, const SceneDev* __restrict__ scenes,
                                                     const int32_t* __restrict__ sid, float4* __restrict__ xv,
-                                                    float4* __restrict__ qv, int32_t* __restrict__ rows,
-                                                    uint64_t* __restrict__ masks) {
+                                                    float4* __restrict__ qv, int32_t* __restrict__ nseg,
+                                                    int32_t* __restrict__ seg_start, uint32_t* __restrict__ seg_mask) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= F.n) return;
   const SceneDev& S = scenes[sid[i]];
   prep_body(i, F, S.P, xv, qv);
-  if (rows && S.P.search_radius == 1) row_masks_body(i, F, S.g, S.coff, S.P.thr, rows, masks);
+  if (nseg) segments_body(i, F, S.g, S.coff, S.P.search_radius, S.P.thr, nseg, seg_start, seg_mask);
 }
 
 // The update of one particle of a batch with its scene's dt.  If the neighbor list
@@ -541,15 +529,14 @@ __global__ void __launch_bounds__(128, 8) k_batch_pass1(FluidView F, const float
                                                      const SceneDev* __restrict__ scenes,
                                                      const int32_t* __restrict__ sid, float* __restrict__ dpdt,
                                                      float2* __restrict__ acc, float2* __restrict__ grad_rho,
-                                                     const int32_t* __restrict__ rows,
-                                                     const uint64_t* __restrict__ masks, float2* __restrict__ xo,
+                                                     const Segments seg, float2* __restrict__ xo,
                                                      float2* __restrict__ vo, float* __restrict__ ro,
                                                      int32_t* status) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= F.n) return;
   const SceneDev& S = scenes[sid[i]];
   const SphParams P = S.P;   // the fields the loop reads, in registers
-  const Pass1 o = pass1_body<kCells>(i, F, xv, qv, W, S.g, P, S.coff, rows, masks);
+  const Pass1 o = pass1_body<kCells>(i, F, xv, qv, W, S.g, P, S.coff, seg);
   if (P.diffusion == 2) {
     dpdt[i] = o.dpdt;
     acc[i] = make_float2(o.ax, o.ay);
@@ -563,9 +550,7 @@ template <bool kCells>
 __global__ void __launch_bounds__(128) k_batch_diffusion(FluidView F, const float4* __restrict__ qv,
                                                          const SceneDev* __restrict__ scenes,
                                                          const int32_t* __restrict__ sid,
-                                                         const float2* __restrict__ grad_rho,
-                                                         const int32_t* __restrict__ rows,
-                                                         const uint64_t* __restrict__ masks,
+                                                         const float2* __restrict__ grad_rho, const Segments seg,
                                                          const float* __restrict__ dpdt,
                                                          const float2* __restrict__ acc, float2* __restrict__ xo,
                                                          float2* __restrict__ vo, float* __restrict__ ro,
@@ -575,7 +560,7 @@ __global__ void __launch_bounds__(128) k_batch_diffusion(FluidView F, const floa
   const SceneDev& S = scenes[sid[i]];
   if (S.P.diffusion != 2) return;
   const SphParams P = S.P;   // the fields the loop reads, in registers
-  const float d = dpdt[i] + P.diff_k * diffusion_sum<kCells>(i, F, qv, P, grad_rho, S.g, S.coff, rows, masks);
+  const float d = dpdt[i] + P.diff_k * diffusion_sum<kCells>(i, F, qv, P, grad_rho, S.g, S.coff, seg);
   const float2 a = acc[i];
   batch_update(i, F, a.x, a.y, d, S, xo, vo, ro, status);
 }
@@ -676,25 +661,29 @@ sph_status_t sph_mdbc_wall_density(const sph_fluid_view* fluid, const sph_wall_v
   return SPH_OK;
 }
 
-// Neighbor records (two float4 per particle), then, for pairs from the cell rows, three row
-// masks and three row starts per particle.
-constexpr size_t kRecordBytes = 2 * sizeof(float4), kMaskBytes = 3 * (sizeof(uint64_t) + sizeof(int32_t));
+// Neighbor records (two float4 per particle), then, for pairs from the cell rows, the
+// segment lists: kMaxSegments masks and starts and a count per particle.
+constexpr size_t kRecordBytes = 2 * sizeof(float4),
+                 kMaskBytes = kMaxSegments * (sizeof(uint32_t) + sizeof(int32_t)) + sizeof(int32_t);
 size_t sph_deltasph_scratch_bytes(int64_t n) { return (size_t)(n > 0 ? n : 0) * (kRecordBytes + kMaskBytes) + 256; }
 
 }  // extern "C"
 
 // The neighbor records (xv, q) in caller scratch, 16-byte aligned.
 static bool records_from_scratch(void* scratch, size_t bytes, int64_t n, float4** xv, float4** qv,
-                                 uint64_t** masks = nullptr, int32_t** rows = nullptr) {
+                                 Segments* seg = nullptr) {
   if (!scratch) return false;
   const uintptr_t base = reinterpret_cast<uintptr_t>(scratch);
   const uintptr_t p = (base + 15) & ~(uintptr_t)15;
-  if ((p - base) + (size_t)n * (kRecordBytes + (masks ? kMaskBytes : 0)) > bytes) return false;
+  if ((p - base) + (size_t)n * (kRecordBytes + (seg ? kMaskBytes : 0)) > bytes) return false;
   *xv = reinterpret_cast<float4*>(p);
   *qv = *xv + n;
-  if (masks) {
-    *masks = reinterpret_cast<uint64_t*>(*qv + n);
-    *rows = reinterpret_cast<int32_t*>(*masks + 3 * n);
+  if (seg) {
+    uint32_t* m = reinterpret_cast<uint32_t*>(*qv + n);
+    int32_t* st = reinterpret_cast<int32_t*>(m + kMaxSegments * n);
+    seg->mask = m;
+    seg->start = st;
+    seg->nseg = st + kMaxSegments * n;
   }
   return true;
 }
@@ -760,16 +749,17 @@ sph_status_t sph_batch_deltasph_step(const sph_fluid_view* fluid, const sph_wall
   const int n = (int)fluid->n;
   if (n == 0) return SPH_OK;
   float4 *xv, *qv;
-  uint64_t* masks = nullptr;
-  int32_t* rows = nullptr;
-  SPH_REQUIRE(records_from_scratch(scratch, scratch_bytes, n, &xv, &qv, cells ? &masks : nullptr, &rows),
+  Segments seg{};
+  SPH_REQUIRE(records_from_scratch(scratch, scratch_bytes, n, &xv, &qv, cells ? &seg : nullptr),
               "batch_deltasph_step: scratch smaller than sph_deltasph_scratch_bytes(n)");
   cudaStream_t st = as_stream(stream);
   const FluidView F = to_fluid(fluid);
   const WallView W = to_walls(walls);
   const SceneDev* S = static_cast<const SceneDev*>(scenes);
   if (W.n > 0 && (phases & SPH_PHASE_WALLS)) k_batch_mdbc<<<grid_for(W.n, 128), 128, 0, st>>>(F, W, S, wall_sid);
-  if (phases & SPH_PHASE_RECORDS) k_batch_prep<<<grid_for(n, 256), 256, 0, st>>>(F, S, sid, xv, qv, rows, masks);
+  if (phases & SPH_PHASE_RECORDS)
+    k_batch_prep<<<grid_for(n, 256), 256, 0, st>>>(F, S, sid, xv, qv, const_cast<int32_t*>(seg.nseg),
+                                                   const_cast<int32_t*>(seg.start), const_cast<uint32_t*>(seg.mask));
   const int nb = grid_for(n, 128);
   float2* xo = reinterpret_cast<float2*>(x_out);
   float2* vo = reinterpret_cast<float2*>(v_out);
@@ -777,18 +767,17 @@ sph_status_t sph_batch_deltasph_step(const sph_fluid_view* fluid, const sph_wall
   const float2* ac = reinterpret_cast<const float2*>(acc);
   if (phases & SPH_PHASE_PASS1) {
     if (cells)
-      k_batch_pass1<true><<<nb, 128, 0, st>>>(F, xv, qv, W, S, sid, dpdt, reinterpret_cast<float2*>(acc), gr, rows,
-                                              masks, xo, vo, rho_out, status);
+      k_batch_pass1<true><<<nb, 128, 0, st>>>(F, xv, qv, W, S, sid, dpdt, reinterpret_cast<float2*>(acc), gr, seg,
+                                              xo, vo, rho_out, status);
     else
       k_batch_pass1<false><<<nb, 128, 0, st>>>(F, xv, qv, W, S, sid, dpdt, reinterpret_cast<float2*>(acc), gr,
-                                               nullptr, nullptr, xo, vo, rho_out, status);
+                                               Segments{}, xo, vo, rho_out, status);
   }
   if (any_renormalized && (phases & SPH_PHASE_DIFFUSION)) {
     if (cells)
-      k_batch_diffusion<true><<<nb, 128, 0, st>>>(F, qv, S, sid, gr, rows, masks, dpdt, ac, xo, vo, rho_out,
-                                                  status);
+      k_batch_diffusion<true><<<nb, 128, 0, st>>>(F, qv, S, sid, gr, seg, dpdt, ac, xo, vo, rho_out, status);
     else
-      k_batch_diffusion<false><<<nb, 128, 0, st>>>(F, qv, S, sid, gr, nullptr, nullptr, dpdt, ac, xo, vo, rho_out,
+      k_batch_diffusion<false><<<nb, 128, 0, st>>>(F, qv, S, sid, gr, Segments{}, dpdt, ac, xo, vo, rho_out,
                                                    status);
   }
   SPH_CHECK_LAUNCH("batch_deltasph_step");
