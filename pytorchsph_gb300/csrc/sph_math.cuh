@@ -126,27 +126,32 @@ __device__ __forceinline__ float4 pinv2x2(float a, float b, float c, float d) {
 __device__ inline void pinv3_solve(const double A[3][3], const double b[3], double x[3]) {
   // Well-conditioned A (Frobenius condition bound ||A|| ||A^-1|| below 1e5, far under the
   // 1/(3 FLT_EPSILON) at which a singular value would be dropped): pinv(A) = A^-1, applied
-  // through the adjugate.  This is the common case and costs ~100 double operations instead
+  // through the adjugate.  This is the common case and costs ~50 double operations instead
   // of the Jacobi sweeps (GB300's FP64 rate is low).
   {
-    const double c00 = A[1][1] * A[2][2] - A[1][2] * A[2][1], c01 = A[1][2] * A[2][0] - A[1][0] * A[2][2],
-                 c02 = A[1][0] * A[2][1] - A[1][1] * A[2][0];
-    const double c10 = A[0][2] * A[2][1] - A[0][1] * A[2][2], c11 = A[0][0] * A[2][2] - A[0][2] * A[2][0],
-                 c12 = A[0][1] * A[2][0] - A[0][0] * A[2][1];
-    const double c20 = A[0][1] * A[1][2] - A[0][2] * A[1][1], c21 = A[0][2] * A[1][0] - A[0][0] * A[1][2],
-                 c22 = A[0][0] * A[1][1] - A[0][1] * A[1][0];
-    const double det = A[0][0] * c00 + A[0][1] * c01 + A[0][2] * c02;
-    double na = 0.0;
+    // cofactors a*b - c*d as fma(a, b, -(c*d)): two double operations each
+    const auto cof = [](double a, double b, double c, double d) { return fma(a, b, -(c * d)); };
+    const double c00 = cof(A[1][1], A[2][2], A[1][2], A[2][1]), c01 = cof(A[1][2], A[2][0], A[1][0], A[2][2]),
+                 c02 = cof(A[1][0], A[2][1], A[1][1], A[2][0]);
+    const double c10 = cof(A[0][2], A[2][1], A[0][1], A[2][2]), c11 = cof(A[0][0], A[2][2], A[0][2], A[2][0]),
+                 c12 = cof(A[0][1], A[2][0], A[0][0], A[2][1]);
+    const double c20 = cof(A[0][1], A[1][2], A[0][2], A[1][1]), c21 = cof(A[0][2], A[1][0], A[0][0], A[1][2]),
+                 c22 = cof(A[0][0], A[1][1], A[0][1], A[1][0]);
+    const double det = fma(A[0][0], c00, fma(A[0][1], c01, A[0][2] * c02));
+    // The bound only decides between two exact-enough paths: its norms run in float.
+    float na = 0.f;
     for (int r = 0; r < 3; ++r)
-      for (int c = 0; c < 3; ++c) na += A[r][c] * A[r][c];
-    const double nc = c00 * c00 + c01 * c01 + c02 * c02 + c10 * c10 + c11 * c11 + c12 * c12 + c20 * c20 +
-                      c21 * c21 + c22 * c22;
+      for (int c = 0; c < 3; ++c) na += (float)A[r][c] * (float)A[r][c];
+    const float f00 = (float)c00, f01 = (float)c01, f02 = (float)c02, f10 = (float)c10, f11 = (float)c11,
+                f12 = (float)c12, f20 = (float)c20, f21 = (float)c21, f22 = (float)c22;
+    const float nc = f00 * f00 + f01 * f01 + f02 * f02 + f10 * f10 + f11 * f11 + f12 * f12 + f20 * f20 +
+                     f21 * f21 + f22 * f22;
     // ||A^-1||_F = ||adj A||_F / |det|
-    if (det != 0.0 && na * nc < 1e10 * det * det) {
+    if (det != 0.0 && (double)na * (double)nc < 1e10 * det * det) {
       const double id = 1.0 / det;  // A^-1 = adj(A) / det, adj(A)[r][c] = cofactor c_cr
-      x[0] = (c00 * b[0] + c10 * b[1] + c20 * b[2]) * id;
-      x[1] = (c01 * b[0] + c11 * b[1] + c21 * b[2]) * id;
-      x[2] = (c02 * b[0] + c12 * b[1] + c22 * b[2]) * id;
+      x[0] = fma(c00, b[0], fma(c10, b[1], c20 * b[2])) * id;
+      x[1] = fma(c01, b[0], fma(c11, b[1], c21 * b[2])) * id;
+      x[2] = fma(c02, b[0], fma(c12, b[1], c22 * b[2])) * id;
       return;
     }
   }
