@@ -9,7 +9,10 @@ Workloads (--workload):
                       upload, admission, batch rebuilds, final states read back) with every
                       request queued at t=0; `serving` adds the real-time trace's p50/p99
                       step latency and time-to-completion and the one-scene-at-a-time GPU path.
-  search_density_A/B  neighbor search + density over N = 2^20 particles.
+                      First the autotuner measures each scene-size bucket's cell ratio and
+                      lanes per particle (`tuning`; --no-tune: cells of h, one lane).
+  search_density_A/B  neighbor search + density over N = 2^20 particles (sort: the
+                      autotuner's pick for N unless --sort counting|radix).
   dambreak_deltasph   8,192-particle dam break, renormalized deltaSPH, 3-layer walls.
   dambreak_dfsph      262,144-particle dam break, DFSPH with walls, adaptive dt.
   diff_drop           16,384-particle oscillating drop, 200 float64 steps: forward + adjoint
@@ -48,11 +51,14 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="serving")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--sort", default="counting", choices=["counting", "radix"])
+    ap.add_argument("--sort", default="auto", choices=["auto", "counting", "radix"],
+                    help="search workloads: auto = the autotuner's pick for this N")
     ap.add_argument("--digit-bits", type=int, default=8)
     ap.add_argument("--requests", type=int, default=1024)
     ap.add_argument("--trace-steps", type=int, default=1000)
     ap.add_argument("--no-trace", action="store_true", help="serving: skip the e2e and real-time trace runs")
+    ap.add_argument("--no-tune", action="store_true",
+                    help="serving: one lane per particle and cells of h for every scene instead of the autotuner's picks")
     ap.add_argument("--pairs", default="cells", choices=["cells", "csr"],
                     help="serving: pairs from the cell rows, or a CSR neighbor list built every step")
     return ap.parse_args()
@@ -309,8 +315,22 @@ def run_serving(args, dev, world, rank):
     total_p = sum(len(s.scene["pos"]) for s in specs)
     budget = 60e9
 
+    # the autotuner's picks per scene-size bucket (cells of h / cell_ratio, lanes per particle),
+    # measured here: in a loaded batch of ~2M particles (the resident batch and the request
+    # loop) and for a scene stepped alone (the one-scene comparison path)
+    tuned, tune_s = {"loaded": None, "one_scene": None}, 0.0
+    if not args.no_tune and args.pairs == "cells":
+        from pytorchsph_gb300.tune import Autotuner, Tuning
+        t0 = time.perf_counter()
+        tuner = Autotuner(dev)
+        sizes = (2048, 8192, 32768, 131072)
+        tuned["loaded"] = Tuning(serving=tuner.tune_serving(sizes, batch_particles=1 << 21, steps=10))
+        tuned["one_scene"] = Tuning(serving=tuner.tune_serving(sizes, batch_particles=1, steps=20))
+        tune_s = time.perf_counter() - t0
+        torch.cuda.empty_cache()
+
     # (a) device-resident batch of every request: W warm-up + K timed batch steps
-    batch = SceneBatch(specs, dev, pairs=args.pairs)
+    batch = SceneBatch(specs, dev, pairs=args.pairs, tuning=tuned["loaded"])
     batch.capture()
     for _ in range(max(args.warmup, 3)):
         batch.step()
@@ -343,7 +363,7 @@ def run_serving(args, dev, world, rank):
     pick = sorted(set(order[int(q * (len(order) - 1))] for q in np.linspace(0, 1, 16)))
     one = []
     for k in pick:
-        b1 = SceneBatch([specs[k]], dev, pairs=args.pairs)
+        b1 = SceneBatch([specs[k]], dev, pairs=args.pairs, tuning=tuned["one_scene"])
         b1.capture()
         for _ in range(3):
             b1.step()
@@ -368,7 +388,7 @@ def run_serving(args, dev, world, rank):
         reqs = [Request(t["rid"], 0.0, specs[k]) for k, t in enumerate(trace)]
         sync_ranks(world)
         srv = Server(dev, budget_bytes=budget, rebuild_every=50, keep_final=True,   # final states to host
-                     pairs=args.pairs)
+                     pairs=args.pairs, tuning=tuned["loaded"])
         wall = srv.run(reqs, time_scale=0.0, max_wall=600)
         sync_ranks(world)
         wall = max_over_ranks(wall, world)
@@ -387,7 +407,8 @@ def run_serving(args, dev, world, rank):
             s.dev = None
         # (d) real-time trace: Poisson arrivals at 50 / s
         reqs = [Request(t["rid"], t["arrival"], specs[k]) for k, t in enumerate(trace)]
-        srv = Server(dev, budget_bytes=budget, rebuild_every=20, keep_final=False, pairs=args.pairs)
+        srv = Server(dev, budget_bytes=budget, rebuild_every=20, keep_final=False, pairs=args.pairs,
+                     tuning=tuned["loaded"])
         wall = srv.run(reqs, time_scale=1.0, max_wall=600)
         lat = srv.latency_percentiles((50, 99))
         ttc = [r.finished - r.arrival for r in reqs if r.finished >= 0 and r.error is None]
@@ -412,6 +433,12 @@ def run_serving(args, dev, world, rank):
             "pairs": "from the cell rows (no neighbor list)" if args.pairs == "cells" else "CSR list every step",
             "scene_generation_s": gen_s})
         line["phases_ms"] = {k: round(v, 4) for k, v in phases.items()}
+        if tuned["loaded"] is not None:
+            pick = lambda t: {str(b): {"cell_ratio": e["cell_ratio"], "tpp": e["tpp"],
+                                       "ms_per_step": {k: round(m["ms_per_step"], 4) for k, m in e["measured"].items()}}
+                              for b, e in t.serving.items()}
+            line["tuning"] = {"loaded_batch": pick(tuned["loaded"]), "one_scene": pick(tuned["one_scene"]),
+                              "candidates": "cell_ratio,tpp", "seconds": round(tune_s, 2)}
         line["roofline"] = {"bound": "hbm", "kernel": "deltaSPH forces (k_batch_pass1)", "achieved": achieved,
                             "peak": peak, "unit": "GB/s", "frac": achieved / peak if achieved else None,
                             "traffic": traffic_from_profiles("serving", f"k_batch_pass1[{args.pairs}]", total_p),
@@ -440,6 +467,12 @@ def run_search_density(args, dev, world, rank):
     h_pos, h_h, h_a = pin(pos), pin(h), pin(area)
     d_pos, d_h, d_a = h_pos.to(dev), h_h.to(dev), h_a.to(dev)
     support = float(h[0])
+    tuned = None
+    if args.sort == "auto":
+        from pytorchsph_gb300.tune import Autotuner, Tuning
+        t = Tuning(search=Autotuner(dev).tune_search(sizes=(n,)))
+        tuned = t.search
+        args.sort, args.digit_bits = t.search_config(n)["sort"], t.search_config(n)["digit_bits"]
     gs = GridSearch(dev, sort=args.sort, digit_bits=args.digit_bits)
     first = gs.run(d_pos, d_h, d_a, kernel_support=support, min_coord=vmin, max_coord=vmax)
     cells, P = first.cell_capacity, first.num_pairs
@@ -537,9 +570,14 @@ def run_search_density(args, dev, world, rank):
     if rank == 0:
         line = base_line(args, world, value, ms, "particles/s", {
             "workload": args.workload, "particles": n, "pairs": P, "cells": cells, "support": "3dx", "sort": args.sort,
+            "digit_bits": args.digit_bits if args.sort == "radix" else None,
+            "sort_chosen_by": "autotuner (measured in this run)" if tuned else "command line",
             "l2": "flushed between timed steps (flush not timed)", "graph": "one CUDA graph per step",
             "parallelism": f"replicas{world}"})
         line["phases_ms"] = {k: round(v, 5) for k, v in phases.items()}
+        if tuned:
+            line["tuning"] = {str(b): {k: (round(x["ms"], 4) if isinstance(x, dict) else x)
+                                       for k, x in e["measured"].items()} for b, e in tuned.items()}
         line["roofline"] = {"bound": "hbm", "kernel": kern, "achieved": achieved, "peak": peak, "unit": "GB/s",
                             "frac": achieved / peak if achieved else None,
                             "traffic": traffic_from_profiles(args.workload, kern, n), "algorithmic_bytes": alg,

@@ -338,6 +338,12 @@ sph_status_t sph_batch_nl_fill(const float* xy, const float* sorted_support, int
  * in the force passes), and both force passes visit those pairs, in the CSR fill's order
  * (same sums).  Each scene's pair test then uses its own support (sph_params.support),
  * which must be every particle's support.
+ * The force passes (pass1, diffusion) run over particle groups: group k is the sorted
+ * particles [group_begin[k], group_begin[k+1]) (host arrays; group_begin[0] = 0,
+ * group_begin[ngroups] = n, so a group holds whole scenes when it ends at scene bounds) with
+ * group_tpp[k] lanes per particle: 1, or 2 or 4 with pairs from the cell rows (each lane
+ * takes every 2nd or 4th segment; the lanes' sums are added by warp shuffles, so the
+ * summation order, not the pair set, depends on it).  ngroups = 0: one group, one lane.
  * `phases` selects the launches (SPH_PHASE_ALL for a step; single phases, in order, let a
  * caller time each kernel): walls = mDBC wall densities, records = per-particle neighbor
  * records, pass1 = first pair pass (+ update of scenes without deltaSPH diffusion),
@@ -350,7 +356,8 @@ sph_status_t sph_batch_nl_fill(const float* xy, const float* sorted_support, int
 sph_status_t sph_batch_deltasph_step(const sph_fluid_view* fluid, const sph_wall_view* walls, const void* scenes,
                                      const int32_t* sid, const int32_t* wall_sid, float* dpdt, float* acc,
                                      float* grad_rho, int32_t any_renormalized, float* x_out, float* v_out,
-                                     float* rho_out, int32_t* status, int32_t phases, void* scratch,
+                                     float* rho_out, int32_t* status, int32_t phases, int32_t ngroups,
+                                     const int64_t* group_begin, const int32_t* group_tpp, void* scratch,
                                      size_t scratch_bytes, void* stream);
 
 /* ---------------------------------------------------------------- Module terms (a9-a17) */

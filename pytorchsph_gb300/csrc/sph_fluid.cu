@@ -155,15 +155,16 @@ __device__ __forceinline__ uint32_t segment_mask(const float2* __restrict__ x, i
   return m;
 }
 
-// Every row of the window, tested here (any r).
-template <typename Fn>
+// Every row of the window, tested here (any r); with kTpp lanes per particle, lane `sub`
+// takes rows y0 + sub, y0 + sub + kTpp, ...
+template <int kTpp = 1, typename Fn>
 __device__ __forceinline__ void cell_pairs(const FluidView& F, const sph_grid& g, int r, int coff, int cx, int cy,
-                                           float xi, float yi, float thr, Fn&& fn) {
+                                           float xi, float yi, float thr, Fn&& fn, int sub = 0) {
   const int x0 = max(cx - r, 0), x1 = min(cx + r, g.cells_x - 1);
   if (x0 > x1) return;
   const int y0 = max(cy - r, 0), y1 = min(cy + r, g.cells_y - 1);
   const int32_t* cs = F.cell_start + coff;
-  for (int yy = y0; yy <= y1; ++yy) {
+  for (int yy = y0 + sub; yy <= y1; yy += kTpp) {
     const int row = yy * g.cells_x;
     const int b = __ldg(cs + row + x0), e = __ldg(cs + row + x1 + 1);
     for (int c = b; c < e; c += 32) {
@@ -215,43 +216,55 @@ __device__ __forceinline__ uint32_t clip_segment(uint32_t w, int b, int n) {
 }
 
 // The pairs of particle i from its segment list (its cell rows when the list overflowed).
-template <typename Fn>
+// With kTpp lanes per particle, lane `sub` takes segments sub, sub + kTpp, ... (rows, on the
+// overflow path); each lane holds its current segment and its next one, loaded ahead.
+template <int kTpp = 1, typename Fn>
 __device__ __forceinline__ void stored_pairs(int i, const FluidView& F, const sph_grid& g, int coff, int r,
                                              const int32_t* __restrict__ nseg, const int32_t* __restrict__ seg_start,
                                              const uint32_t* __restrict__ seg_mask, float xi, float yi, float thr,
-                                             Fn&& fn) {
+                                             Fn&& fn, int sub = 0) {
   const int ns = nseg[i];
   if (ns < 0 || ns > kMaxSegments) {
     int cx, cy;
     cell_of(F.keys[i] - (uint32_t)coff, g, &cx, &cy);
-    cell_pairs(F, g, r, coff, cx, cy, xi, yi, thr, fn);
+    cell_pairs<kTpp>(F, g, r, coff, cx, cy, xi, yi, thr, fn, sub);
     return;
   }
-  if (ns == 0) return;
+  if (ns <= sub) return;
   const size_t n = (size_t)F.n;
-  int b = seg_start[i];
-  uint32_t w = clip_segment(seg_mask[i], b, F.n);
+  int k = sub;
+  int b = seg_start[k * n + i];
+  uint32_t w = clip_segment(seg_mask[k * n + i], b, F.n);
   int bn = 0;
   uint32_t wn = 0;
-  if (ns > 1) {
-    bn = seg_start[n + i];
-    wn = seg_mask[n + i];
+  if (k + kTpp < ns) {
+    bn = seg_start[(k + kTpp) * n + i];
+    wn = seg_mask[(k + kTpp) * n + i];
   }
-  int k = 0;
   for (;;) {
     while (w == 0) {
-      if (++k >= ns) return;
+      k += kTpp;
+      if (k >= ns) return;
       b = bn;
       w = clip_segment(wn, bn, F.n);
-      if (k + 1 < ns) {
-        bn = seg_start[(k + 1) * n + i];
-        wn = seg_mask[(k + 1) * n + i];
+      if (k + kTpp < ns) {
+        bn = seg_start[(k + kTpp) * n + i];
+        wn = seg_mask[(k + kTpp) * n + i];
       }
     }
     const int j = b - 1 + __ffs(w);
     w &= w - 1;
     fn(j);
   }
+}
+
+// Sum of v over the kTpp consecutive lanes of one particle (every lane gets the sum; the
+// whole warp must take part).
+template <int kTpp>
+__device__ __forceinline__ float lane_sum(float v) {
+#pragma unroll
+  for (int o = 1; o < kTpp; o <<= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
 }
 
 // ---------------------------------------------------------------------------- pass 1
@@ -272,10 +285,14 @@ struct Segments {
   const uint32_t* mask;
 };
 
-template <bool kCells>
+// kTpp lanes per particle (kCells only): lane `sub` sums its share of the pairs, the lanes
+// add their sums, and lane 0 finishes (walls, gravity, L^+); the other lanes return a zero
+// record.  `live` false: a lane past the last particle, which only takes part in the sums.
+template <bool kCells, int kTpp = 1>
 __device__ __forceinline__ Pass1 pass1_body(int i, const FluidView& F, const float4* __restrict__ xv,
                                             const float4* __restrict__ qv, const WallView& W, const sph_grid& g,
-                                            const SphParams& P, int coff, const Segments& S) {
+                                            const SphParams& P, int coff, const Segments& S, int sub = 0,
+                                            bool live = true) {
   const float4 si = xv[i];
   const float rhoi = qv[i].x, pi = tait(F.rho[i], P);
   const bool renorm = P.diffusion == 2;
@@ -317,10 +334,28 @@ __device__ __forceinline__ Pass1 pass1_body(int i, const FluidView& F, const flo
     }
   };
   if constexpr (kCells) {
-    stored_pairs(i, F, g, coff, P.search_radius, S.nseg, S.start, S.mask, si.x, si.y, P.thr, fluid_pair);
+    if (live) stored_pairs<kTpp>(i, F, g, coff, P.search_radius, S.nseg, S.start, S.mask, si.x, si.y, P.thr,
+                                 fluid_pair, sub);
   } else {
+    static_assert(kTpp == 1, "CSR rows run one lane per particle");
     const int k0 = F.offsets[i], k1 = row_end(F, i, k0);
     for (int k = k0; k < k1; ++k) fluid_pair(__ldg(F.cols + k));
+  }
+  if constexpr (kTpp > 1) {
+    dp_f = lane_sum<kTpp>(dp_f);
+    mog = lane_sum<kTpp>(mog);
+    pax = lane_sum<kTpp>(pax);
+    pay = lane_sum<kTpp>(pay);
+    vax = lane_sum<kTpp>(vax);
+    vay = lane_sum<kTpp>(vay);
+    lax = lane_sum<kTpp>(lax);
+    lay = lane_sum<kTpp>(lay);
+    l00 = lane_sum<kTpp>(l00);
+    l01 = lane_sum<kTpp>(l01);
+    l11 = lane_sum<kTpp>(l11);
+    gfx = lane_sum<kTpp>(gfx);
+    gfy = lane_sum<kTpp>(gfy);
+    if (sub != 0 || !live) return Pass1{};
   }
   float dp_w = 0.f, pwx = 0.f, pwy = 0.f, vwx = 0.f, vwy = 0.f;
   float w00 = 0.f, w01 = 0.f, w10 = 0.f, w11 = 0.f, gwx = 0.f, gwy = 0.f;
@@ -398,10 +433,11 @@ __device__ __forceinline__ Pass1 pass1_body(int i, const FluidView& F, const flo
 // D_i = sum_j [2 (rho_j - rho_i)/(|x_ji|^2 + eps) x_ji - (<grad rho>_i + <grad rho>_j)] . gradW_ij V_j
 // (the deltaSPH density diffusion before its h delta c0 factor).
 // kCells: pairs from the segment lists instead of the CSR row.
-template <bool kCells>
+template <bool kCells, int kTpp = 1>
 __device__ __forceinline__ float diffusion_sum(int i, const FluidView& F, const float4* __restrict__ qv,
                                                const SphParams& P, const float2* __restrict__ grad_rho,
-                                               const sph_grid& g, int coff, const Segments& S) {
+                                               const sph_grid& g, int coff, const Segments& S, int sub = 0,
+                                               bool live = true) {
   const float2 xi = F.x[i], gi = grad_rho[i];
   const float rhoi = qv[i].x;
   float acc = 0.f;
@@ -415,12 +451,14 @@ __device__ __forceinline__ float diffusion_sum(int i, const FluidView& F, const 
     acc += e.gd * pd * qj.y;
   };
   if constexpr (kCells) {
-    stored_pairs(i, F, g, coff, P.search_radius, S.nseg, S.start, S.mask, xi.x, xi.y, P.thr, pair);
+    if (live) stored_pairs<kTpp>(i, F, g, coff, P.search_radius, S.nseg, S.start, S.mask, xi.x, xi.y, P.thr, pair,
+                                 sub);
   } else {
+    static_assert(kTpp == 1, "CSR rows run one lane per particle");
     const int k0 = F.offsets[i], k1 = row_end(F, i, k0);
     for (int k = k0; k < k1; ++k) pair(__ldg(F.cols + k));
   }
-  return acc;
+  return lane_sum<kTpp>(acc);
 }
 
 // semiImplicitEuler, src/simulationBase.py:647-652 with integrateValues :564-569, for one
@@ -519,11 +557,12 @@ __device__ __forceinline__ void batch_update(int i, const FluidView& F, float ax
   sie_apply(i, F.x[i], F.v[i], F.rho[i], make_float2(ax, ay), dpdt, S.dt, S.P.rho0, 1, xo, vo, ro, status);
 }
 
-// Pass 1 of every particle.  Particles of scenes without the deltaSPH density diffusion are
-// complete after it and are updated here; the others hand dpdt, acc and <grad rho> to
-// k_batch_diffusion, which finishes and updates them.  kCells: pairs from the cell rows,
-// their masks stored for the diffusion pass.
-template <bool kCells>
+// Pass 1 of the particles [p_lo, p_hi).  Particles of scenes without the deltaSPH density
+// diffusion are complete after it and are updated here; the others hand dpdt, acc and
+// <grad rho> to k_batch_diffusion, which finishes and updates them.  kCells: pairs from the
+// segment lists; kTpp lanes per particle (kCells only).  With kTpp > 1 no lane leaves
+// before the lane sums: lanes past p_hi take part with nothing to add.
+template <bool kCells, int kTpp>
 __global__ void __launch_bounds__(128, 8) k_batch_pass1(FluidView F, const float4* __restrict__ xv,
                                                      const float4* __restrict__ qv, WallView W,
                                                      const SceneDev* __restrict__ scenes,
@@ -531,12 +570,23 @@ __global__ void __launch_bounds__(128, 8) k_batch_pass1(FluidView F, const float
                                                      float2* __restrict__ acc, float2* __restrict__ grad_rho,
                                                      const Segments seg, float2* __restrict__ xo,
                                                      float2* __restrict__ vo, float* __restrict__ ro,
-                                                     int32_t* status) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= F.n) return;
+                                                     int32_t* status, int p_lo, int p_hi) {
+  int i, sub = 0;
+  bool live = true;
+  if constexpr (kTpp == 1) {
+    i = p_lo + (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    if (i >= p_hi) return;
+  } else {
+    const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t ii = p_lo + g / kTpp;
+    sub = (int)(g % kTpp);
+    live = ii < p_hi;
+    i = live ? (int)ii : p_lo;
+  }
   const SceneDev& S = scenes[sid[i]];
   const SphParams P = S.P;   // the fields the loop reads, in registers
-  const Pass1 o = pass1_body<kCells>(i, F, xv, qv, W, S.g, P, S.coff, seg);
+  const Pass1 o = pass1_body<kCells, kTpp>(i, F, xv, qv, W, S.g, P, S.coff, seg, sub, kTpp == 1 || live);
+  if (kTpp > 1 && (!live || sub != 0)) return;
   if (P.diffusion == 2) {
     dpdt[i] = o.dpdt;
     acc[i] = make_float2(o.ax, o.ay);
@@ -546,7 +596,7 @@ __global__ void __launch_bounds__(128, 8) k_batch_pass1(FluidView F, const float
   batch_update(i, F, o.ax, o.ay, o.dpdt, S, xo, vo, ro, status);
 }
 
-template <bool kCells>
+template <bool kCells, int kTpp>
 __global__ void __launch_bounds__(128) k_batch_diffusion(FluidView F, const float4* __restrict__ qv,
                                                          const SceneDev* __restrict__ scenes,
                                                          const int32_t* __restrict__ sid,
@@ -554,13 +604,26 @@ __global__ void __launch_bounds__(128) k_batch_diffusion(FluidView F, const floa
                                                          const float* __restrict__ dpdt,
                                                          const float2* __restrict__ acc, float2* __restrict__ xo,
                                                          float2* __restrict__ vo, float* __restrict__ ro,
-                                                         int32_t* status) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= F.n) return;
+                                                         int32_t* status, int p_lo, int p_hi) {
+  int i, sub = 0;
+  bool live = true;
+  if constexpr (kTpp == 1) {
+    i = p_lo + (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    if (i >= p_hi) return;
+  } else {
+    const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t ii = p_lo + g / kTpp;
+    sub = (int)(g % kTpp);
+    live = ii < p_hi;
+    i = live ? (int)ii : p_lo;
+  }
   const SceneDev& S = scenes[sid[i]];
-  if (S.P.diffusion != 2) return;
+  const bool act = live && S.P.diffusion == 2;   // the same on all lanes of a particle
+  if (kTpp == 1 && !act) return;
   const SphParams P = S.P;   // the fields the loop reads, in registers
-  const float d = dpdt[i] + P.diff_k * diffusion_sum<kCells>(i, F, qv, P, grad_rho, S.g, S.coff, seg);
+  const float sum = diffusion_sum<kCells, kTpp>(i, F, qv, P, grad_rho, S.g, S.coff, seg, sub, kTpp == 1 || act);
+  if (kTpp > 1 && (!act || sub != 0)) return;
+  const float d = dpdt[i] + P.diff_k * sum;
   const float2 a = acc[i];
   batch_update(i, F, a.x, a.y, d, S, xo, vo, ro, status);
 }
@@ -734,7 +797,8 @@ sph_status_t sph_integrate_semi_implicit_euler(int64_t n, const float* x, const 
 sph_status_t sph_batch_deltasph_step(const sph_fluid_view* fluid, const sph_wall_view* walls, const void* scenes,
                                      const int32_t* sid, const int32_t* wall_sid, float* dpdt, float* acc,
                                      float* grad_rho, int32_t any_renormalized, float* x_out, float* v_out,
-                                     float* rho_out, int32_t* status, int32_t phases, void* scratch,
+                                     float* rho_out, int32_t* status, int32_t phases, int32_t ngroups,
+                                     const int64_t* group_begin, const int32_t* group_tpp, void* scratch,
                                      size_t scratch_bytes, void* stream) {
   SPH_VIEW_CHECK(fluid);
   SPH_VIEW_CHECK(walls);
@@ -747,6 +811,19 @@ sph_status_t sph_batch_deltasph_step(const sph_fluid_view* fluid, const sph_wall
   SPH_REQUIRE(cells || (fluid->offsets && fluid->cols), "batch_deltasph_step: give both offsets and cols, or neither");
   SPH_REQUIRE(fluid->cell_start && fluid->keys, "batch_deltasph_step: bad arguments");
   const int n = (int)fluid->n;
+  // particle groups of the force passes: one group of one lane per particle by default
+  const int64_t all[2] = {0, n};
+  const int32_t one[1] = {1};
+  SPH_REQUIRE(ngroups >= 0 && (ngroups == 0 || (group_begin && group_tpp)), "batch_deltasph_step: bad groups");
+  const int ng = ngroups ? ngroups : 1;
+  const int64_t* gb = ngroups ? group_begin : all;
+  const int32_t* gt = ngroups ? group_tpp : one;
+  SPH_REQUIRE(gb[0] == 0 && gb[ng] == n, "batch_deltasph_step: the groups must cover [0, n)");
+  for (int k = 0; k < ng; ++k) {
+    SPH_REQUIRE(gb[k] <= gb[k + 1], "batch_deltasph_step: group bounds must not decrease");
+    SPH_REQUIRE(gt[k] == 1 || (cells && (gt[k] == 2 || gt[k] == 4)),
+                "batch_deltasph_step: lanes per particle must be 1 (2 or 4 with pairs from the cell rows)");
+  }
   if (n == 0) return SPH_OK;
   float4 *xv, *qv;
   Segments seg{};
@@ -760,25 +837,45 @@ sph_status_t sph_batch_deltasph_step(const sph_fluid_view* fluid, const sph_wall
   if (phases & SPH_PHASE_RECORDS)
     k_batch_prep<<<grid_for(n, 256), 256, 0, st>>>(F, S, sid, xv, qv, const_cast<int32_t*>(seg.nseg),
                                                    const_cast<int32_t*>(seg.start), const_cast<uint32_t*>(seg.mask));
-  const int nb = grid_for(n, 128);
   float2* xo = reinterpret_cast<float2*>(x_out);
   float2* vo = reinterpret_cast<float2*>(v_out);
   float2* gr = reinterpret_cast<float2*>(grad_rho);
-  const float2* ac = reinterpret_cast<const float2*>(acc);
-  if (phases & SPH_PHASE_PASS1) {
-    if (cells)
-      k_batch_pass1<true><<<nb, 128, 0, st>>>(F, xv, qv, W, S, sid, dpdt, reinterpret_cast<float2*>(acc), gr, seg,
-                                              xo, vo, rho_out, status);
-    else
-      k_batch_pass1<false><<<nb, 128, 0, st>>>(F, xv, qv, W, S, sid, dpdt, reinterpret_cast<float2*>(acc), gr,
-                                               Segments{}, xo, vo, rho_out, status);
+  float2* ac = reinterpret_cast<float2*>(acc);
+  for (int k = 0; k < ng; ++k) {
+    const int lo = (int)gb[k], hi = (int)gb[k + 1], t = gt[k];
+    if (hi <= lo) continue;
+    const int nb = grid_for((int64_t)(hi - lo) * t, 128);
+    if (phases & SPH_PHASE_PASS1) {
+      if (!cells)
+        k_batch_pass1<false, 1><<<nb, 128, 0, st>>>(F, xv, qv, W, S, sid, dpdt, ac, gr, Segments{}, xo, vo, rho_out,
+                                                    status, lo, hi);
+      else if (t == 1)
+        k_batch_pass1<true, 1><<<nb, 128, 0, st>>>(F, xv, qv, W, S, sid, dpdt, ac, gr, seg, xo, vo, rho_out, status,
+                                                   lo, hi);
+      else if (t == 2)
+        k_batch_pass1<true, 2><<<nb, 128, 0, st>>>(F, xv, qv, W, S, sid, dpdt, ac, gr, seg, xo, vo, rho_out, status,
+                                                   lo, hi);
+      else
+        k_batch_pass1<true, 4><<<nb, 128, 0, st>>>(F, xv, qv, W, S, sid, dpdt, ac, gr, seg, xo, vo, rho_out, status,
+                                                   lo, hi);
+    }
   }
-  if (any_renormalized && (phases & SPH_PHASE_DIFFUSION)) {
-    if (cells)
-      k_batch_diffusion<true><<<nb, 128, 0, st>>>(F, qv, S, sid, gr, seg, dpdt, ac, xo, vo, rho_out, status);
+  for (int k = 0; k < ng && any_renormalized && (phases & SPH_PHASE_DIFFUSION); ++k) {
+    const int lo = (int)gb[k], hi = (int)gb[k + 1], t = gt[k];
+    if (hi <= lo) continue;
+    const int nb = grid_for((int64_t)(hi - lo) * t, 128);
+    if (!cells)
+      k_batch_diffusion<false, 1><<<nb, 128, 0, st>>>(F, qv, S, sid, gr, Segments{}, dpdt, ac, xo, vo, rho_out,
+                                                      status, lo, hi);
+    else if (t == 1)
+      k_batch_diffusion<true, 1><<<nb, 128, 0, st>>>(F, qv, S, sid, gr, seg, dpdt, ac, xo, vo, rho_out, status, lo,
+                                                     hi);
+    else if (t == 2)
+      k_batch_diffusion<true, 2><<<nb, 128, 0, st>>>(F, qv, S, sid, gr, seg, dpdt, ac, xo, vo, rho_out, status, lo,
+                                                     hi);
     else
-      k_batch_diffusion<false><<<nb, 128, 0, st>>>(F, qv, S, sid, gr, Segments{}, dpdt, ac, xo, vo, rho_out,
-                                                   status);
+      k_batch_diffusion<true, 4><<<nb, 128, 0, st>>>(F, qv, S, sid, gr, seg, dpdt, ac, xo, vo, rho_out, status, lo,
+                                                     hi);
   }
   SPH_CHECK_LAUNCH("batch_deltasph_step");
   return SPH_OK;

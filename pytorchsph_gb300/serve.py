@@ -29,7 +29,7 @@ from .search import MAX_CELLS, Workspace
 from .sim import SimConfig, SphParamsC, FluidViewC, WallViewC, DIFFUSION
 
 
-def _params_for(cfg: SimConfig, h: float, cells: int) -> SphParamsC:
+def _params_for(cfg: SimConfig, h: float, cells: int, cell_ratio: int = 1) -> SphParamsC:
     P = SphParamsC()
     P.support = h
     P.rest_density = cfg.rest_density
@@ -44,7 +44,7 @@ def _params_for(cfg: SimConfig, h: float, cells: int) -> SphParamsC:
     P.point_center[0], P.point_center[1] = cfg.point_center
     P.density_diffusion = DIFFUSION[cfg.density_diffusion]
     P.boundary_diffusion = int(bool(cfg.boundary_diffusion))
-    P.search_radius = cfg.search_radius
+    P.search_radius = cfg.search_radius * cell_ratio     # cells of h / cell_ratio
     P.cell_capacity = cells
     return P
 
@@ -61,6 +61,8 @@ class SceneSpec:
     cfg: SimConfig
     steps: int = 1000
     name: str = ""
+    cell_ratio: int = 1      # grid cells of support / cell_ratio, searched cell_ratio cells out
+    tpp: int = 1             # lanes per particle in the force passes (1, 2, 4; pairs from cell rows)
     dev: dict | None = field(default=None, repr=False)   # device copies + grid, made once
 
     def on_device(self, device):
@@ -78,7 +80,8 @@ def upload_scenes(specs, device):
     """Device copies and grids of every spec not yet on `device`: one copy per field for all
     of them (from pinned host memory) and one grid launch (sph_grid_build_segments)."""
     device = torch.device(device)
-    todo = [sp for sp in specs if sp.dev is None or sp.dev["device"] != device]
+    todo = [sp for sp in specs if sp.dev is None or sp.dev["device"] != device or
+            sp.dev["cell_ratio"] != sp.cell_ratio]
     if not todo:
         return
     lib = N.load()
@@ -104,7 +107,18 @@ def upload_scenes(specs, device):
     vmax = torch.tensor(np.array([sp.scene["vmax"] for sp in todo], np.float32)).to(device)
     grids = torch.empty(S * 8, dtype=torch.int32, device=device)
     status = torch.zeros(1, dtype=torch.int32, device=device)
-    N.call("sph_grid_build_segments", N.ptr(dev_fields["pos"][0]), N.ptr(dev_fields["sup"][0]), N.ptr(seg), S,
+    # the grid's cell size is the largest support of the scene over its cell_ratio; the grid
+    # pads the domain by one cell below and two above, so the domain given to it grows by
+    # the difference to keep that padding one and two supports (walls lie in it)
+    cell_h = dev_fields["sup"][0]
+    if any(sp.cell_ratio != 1 for sp in todo):
+        inv = torch.tensor([1.0 / sp.cell_ratio for sp in todo], dtype=torch.float32, device=device)
+        cell_h = cell_h * torch.repeat_interleave(inv, torch.tensor(counts["n"], device=device))
+        grow = np.array([float(np.max(sp.scene["support"])) * (1.0 - 1.0 / sp.cell_ratio) for sp in todo],
+                        np.float32)[:, None]
+        vmin = vmin - torch.from_numpy(grow).to(device)
+        vmax = vmax + torch.from_numpy(2.0 * grow).to(device)
+    N.call("sph_grid_build_segments", N.ptr(dev_fields["pos"][0]), N.ptr(cell_h), N.ptr(seg), S,
            N.ptr(vmin), N.ptr(vmax), MAX_CELLS, N.ptr(grids), N.ptr(status), N.stream_ptr())
     flags = int(status.item())
     if flags:
@@ -112,7 +126,7 @@ def upload_scenes(specs, device):
     raw = grids.cpu().numpy().tobytes()
     offs = {name: np.concatenate([[0], np.cumsum(c)]) for name, (_, c) in dev_fields.items()}
     for s, sp in enumerate(todo):
-        d = {"device": device, "n": counts["n"][s], "nb": counts["nb"][s],
+        d = {"device": device, "n": counts["n"][s], "nb": counts["nb"][s], "cell_ratio": sp.cell_ratio,
              "grid": _Grid.from_buffer_copy(raw[32 * s:32 * (s + 1)])}
         for name, (t, _) in dev_fields.items():
             lo, hi = offs[name][s], offs[name][s + 1]
@@ -127,16 +141,37 @@ class SceneBatch:
     pairs = "cells": the force passes take each particle's pairs straight from its cell rows
     (no neighbor list; pass 1 keeps per-row bit masks for the diffusion pass).  pairs =
     "csr": a CSR neighbor list is counted and filled every step first.  Both visit the
-    pairs in the same order and give the same sums."""
+    pairs in the same order and give the same sums.
 
-    def __init__(self, specs, device=None, states=None, pair_headroom: float = 1.3, pairs: str = "cells"):
+    Each scene runs with its spec's cell_ratio and tpp (set from `tuning`, a
+    `tune.Tuning`, when given): the batch keeps its scenes grouped by tpp, and each group is
+    one particle range of the force passes.  Per-scene methods take the scenes' indices in
+    `specs` order."""
+
+    def __init__(self, specs, device=None, states=None, pair_headroom: float = 1.3, pairs: str = "cells",
+                 tuning=None):
         if pairs not in ("cells", "csr"):
             raise ValueError("pairs must be 'cells' or 'csr'")
         self.pairs = pairs
         self.lib = N.load()
         self.device = torch.device(device or torch.device("cuda", torch.cuda.current_device()))
         dev = self.device
-        self.specs = list(specs)
+        specs = list(specs)
+        if tuning is not None:
+            for sp in specs:
+                tuning.configure(sp)
+        for sp in specs:
+            if sp.tpp not in (1, 2, 4) or sp.cell_ratio not in (1, 2):
+                raise ValueError("tpp must be 1, 2 or 4 and cell_ratio 1 or 2")
+        lanes = [sp.tpp if pairs == "cells" else 1 for sp in specs]
+        # scenes grouped by lanes per particle (stable): _order[k] = the spec of batch scene k
+        self._order = sorted(range(len(specs)), key=lambda k: lanes[k])
+        self._slot = [0] * len(specs)
+        for k, e in enumerate(self._order):
+            self._slot[e] = k
+        self.specs = [specs[e] for e in self._order]
+        if states is not None:
+            states = [states[e] for e in self._order]
         S = len(self.specs)
         upload_scenes(self.specs, dev)
         rec = self.lib.sph_scene_bytes()
@@ -155,7 +190,7 @@ class SceneBatch:
             d = spec.on_device(dev)
             g = d["grid"]
             h = float(np.float32(spec.scene["support"][0]))
-            P = _params_for(cfg, h, g.num_cells)
+            P = _params_for(cfg, h, g.num_cells, spec.cell_ratio)
             buf = ctypes.create_string_buffer(rec)
             N.check(self.lib.sph_scene_encode(ctypes.byref(P), ctypes.byref(g), total_cells, cfg.dt, buf),
                     "scene_encode")
@@ -186,6 +221,20 @@ class SceneBatch:
                                          dtype=torch.int64, device=dev)
         self.n = self.p_off[-1]
         n = self.n
+        # force-pass groups: runs of scenes with the same lanes per particle
+        lanes_in = [lanes[e] for e in self._order]
+        begin, tpp = [0], []
+        for k in range(S):
+            if k == 0 or lanes_in[k] != lanes_in[k - 1]:
+                if k:
+                    begin.append(self.p_off[k])
+                tpp.append(lanes_in[k])
+        begin.append(n)
+        if not tpp:
+            begin, tpp = [0, n], [1]
+        self.groups = list(zip(begin[:-1], begin[1:], tpp))
+        self._group_begin = (ctypes.c_int64 * len(begin))(*begin)
+        self._group_tpp = (ctypes.c_int32 * len(tpp))(*tpp)
         # scene index and particle id of every particle; p_off_dev[sid] + uid is its slot in the
         # concatenation of the scenes in their own particle order
         counts = torch.tensor(np.diff(self.p_off), dtype=torch.int64, device=dev)
@@ -315,8 +364,9 @@ class SceneBatch:
         N.call("sph_batch_deltasph_step", ctypes.byref(fv), ctypes.byref(self.wall_view), N.ptr(self.scenes),
                N.ptr(b["sid"]), N.ptr(self.w["sid"]), N.ptr(self.dpdt), N.ptr(self.acc), N.ptr(self.grad_rho),
                int(self.any_renorm), N.ptr(out["x"]), N.ptr(out["v"]), N.ptr(out["rho"]), N.ptr(self.status),
-               N.SPH_PHASE_ALL if phases is None else phases, N.ptr(self.forces_scratch),
-               self.forces_scratch.numel() * 8, N.stream_ptr())
+               N.SPH_PHASE_ALL if phases is None else phases, len(self._group_tpp),
+               ctypes.cast(self._group_begin, ctypes.c_void_p), ctypes.cast(self._group_tpp, ctypes.c_void_p),
+               N.ptr(self.forces_scratch), self.forces_scratch.numel() * 8, N.stream_ptr())
 
     def step_kernels(self):
         """The batch step as a fixed kernel sequence (no host synchronisation)."""
@@ -328,11 +378,12 @@ class SceneBatch:
 
     # kernels of this library launched by one batch step (for the bench's launch count): keys 1,
     # counting sort (scan 3 + scatter + fix + fix_large) 6, permute 1, [csr: count 1, scan 3,
-    # fill 1], mdbc 1, records 1, pass1 + update 1 (+ diffusion + update 1 when
-    # renormalized), copy 1
+    # fill 1], mdbc 1, records 1, per particle group pass1 + update 1 (+ diffusion + update 1
+    # when renormalized), copy 1
     def launches_per_step(self):
         csr = 1 + 3 + 1 if self.pairs == "csr" else 0
-        return 1 + 6 + 1 + csr + (1 if self.nb else 0) + 1 + 1 + (1 if self.any_renorm else 0) + 1
+        groups = sum(1 for lo, hi, _ in self.groups if hi > lo)
+        return 1 + 6 + 1 + csr + (1 if self.nb else 0) + 1 + groups * (1 + (1 if self.any_renorm else 0)) + 1
 
     def capture(self):
         """Capture one batch step into a CUDA graph (after a warm-up step)."""
@@ -375,17 +426,20 @@ class SceneBatch:
         if not self.specs:
             return np.zeros(0, np.int64)
         cs = self.cell_start.long()
-        return (cs[self.outside_slot + 1] - cs[self.outside_slot]).cpu().numpy()
+        per_slot = (cs[self.outside_slot + 1] - cs[self.outside_slot]).cpu().numpy()
+        return per_slot[self._slot]
 
     def scene_finite(self, s: int) -> bool:
-        lo, hi = self.p_off[s], self.p_off[s + 1]
+        k = self._slot[s]
+        lo, hi = self.p_off[k], self.p_off[k + 1]
         return bool(torch.isfinite(self.a["x"][lo:hi]).all() and torch.isfinite(self.a["v"][lo:hi]).all()
                     and torch.isfinite(self.a["rho"][lo:hi]).all())
 
     # ------------------------------------------------------------------ output
     def states_device(self):
         """Positions, velocities and densities of every scene in its original particle order,
-        concatenated scene after scene (device; scene s is rows p_off[s]:p_off[s+1])."""
+        concatenated scene after scene in batch order (device; take a scene with
+        scene_state_device)."""
         dst = (self.p_off_dev[self.a["sid"].long()] + self.a["uid"].long()).to(torch.int32)
         out = {k: torch.empty_like(self.a[k]) for k in ("x", "v", "rho")}
         N.call("sph_invert_permutation", N.ptr(dst), self.n, N.ptr(self._inv), N.stream_ptr())
@@ -395,8 +449,9 @@ class SceneBatch:
     def scene_state_device(self, s: int, states=None):
         """Positions, velocities and densities of scene s in its original particle order (device)."""
         states = states or self.states_device()
-        lo, hi = self.p_off[s], self.p_off[s + 1]
-        return {k: v[lo:hi] for k, v in states.items()}
+        k = self._slot[s]
+        lo, hi = self.p_off[k], self.p_off[k + 1]
+        return {key: v[lo:hi] for key, v in states.items()}
 
     def scene_state(self, s: int):
         """Positions, velocities and densities of scene s in its original particle order (numpy)."""
@@ -447,7 +502,7 @@ class Server:
     with `Request.error` set; the other scenes, which share no data with it, carry on."""
 
     def __init__(self, device=None, budget_bytes: float = 60e9, rebuild_every: int = 20, use_graph: bool = True,
-                 keep_final: bool = True, pair_headroom: float = 1.3, pairs: str = "cells"):
+                 keep_final: bool = True, pair_headroom: float = 1.3, pairs: str = "cells", tuning=None):
         self.device = torch.device(device or torch.device("cuda", torch.cuda.current_device()))
         self.budget = budget_bytes
         self.rebuild_every = rebuild_every
@@ -455,6 +510,7 @@ class Server:
         self.keep_final = keep_final
         self.pair_headroom = pair_headroom
         self.pairs = pairs
+        self.tuning = tuning          # tune.Tuning: per-scene cell ratio and lanes by size
         self.live: list[Request] = []
         self.batch: SceneBatch | None = None
         self.particle_steps = 0
@@ -513,7 +569,7 @@ class Server:
         self._last_flags = 0
         if keep:
             self.batch = SceneBatch([r.spec for r in keep], self.device, states=states,
-                                    pair_headroom=self.pair_headroom, pairs=self.pairs)
+                                    pair_headroom=self.pair_headroom, pairs=self.pairs, tuning=self.tuning)
             self.rebuilds += 1
             if self.use_graph:
                 self.batch.capture()          # runs one step eagerly, then records it

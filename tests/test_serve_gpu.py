@@ -166,3 +166,54 @@ def test_server_recovers_from_pair_overflow(cuda):
     assert all(r.steps_done == r.spec.steps and r.error is None for r in reqs)
     for r in reqs:
         assert same(run_batch([r.spec], r.spec.steps, cuda)[0], r.final)
+
+
+def close(a, b, tol):
+    """Max |a - b| of each field within tol[field] of the field's largest magnitude."""
+    return all(np.abs(a[k].astype(np.float64) - b[k]).max() <= tol[k] * max(np.abs(b[k]).max(), 1e-30)
+               for k in ("x", "v", "rho"))
+
+
+# Another summation order moves a step by float32 rounding: positions and densities hardly,
+# velocities more, because pressure and wall terms are small remainders of large sums (one
+# float32 step is 2e-3 of max |v| from the float64 step on these dam breaks).
+REORDER_TOL = {"x": 1e-6, "v": 5e-3, "rho": 1e-5}
+
+
+def configured(spec, ratio, tpp):
+    import dataclasses
+    return dataclasses.replace(spec, cell_ratio=ratio, tpp=tpp, dev=None)
+
+
+def test_lanes_per_particle_and_cell_ratio_keep_the_pairs(cuda):
+    """Splitting a particle's segments over 2 or 4 lanes, or searching cells of h/2 two cells
+    out, visits the same pairs in another order: after 6 steps the states agree with one lane
+    and cells of h within float32 rounding (REORDER_TOL), and a configured scene is still
+    bitwise the same alone and in a mix of differently configured scenes."""
+    A, B = spec("dam_break", 3000, 1.2), spec("drop", 2600, 0.8)
+    base = run_batch([A, B], 6, cuda)
+    for ratio, tpp in ((1, 2), (1, 4), (2, 1), (2, 2)):
+        got = run_batch([configured(A, ratio, tpp), configured(B, ratio, tpp)], 6, cuda)
+        assert close(got[0], base[0], REORDER_TOL) and close(got[1], base[1], REORDER_TOL), (ratio, tpp)
+    A2, B4, C = configured(A, 2, 2), configured(B, 1, 4), spec("dam_break", 2500, 0.6)
+    mix = run_batch([C, B4, A2], 6, cuda, graph=True)
+    assert same(run_batch([A2], 6, cuda)[0], mix[2])
+    assert same(run_batch([B4], 6, cuda)[0], mix[1])
+    assert same(run_batch([C], 6, cuda)[0], mix[0])
+
+
+def test_autotuner_picks_a_measured_configuration(cuda):
+    from pytorchsph_gb300.serve import SceneBatch
+    from pytorchsph_gb300.tune import Autotuner, Tuning
+    tuner = Autotuner(cuda)
+    t = Tuning(serving=tuner.tune_serving(sizes=(2048,), batch_particles=8192, steps=2,
+                                          candidates=((1, 1), (2, 2))))
+    e = t.serving[11]
+    assert (e["cell_ratio"], e["tpp"]) in ((1, 1), (2, 2)) and len(e["measured"]) == 2
+    best = min(e["measured"].values(), key=lambda m: m["ms_per_step"])
+    assert e["measured"][f'{e["cell_ratio"]},{e["tpp"]}'] is best
+    A = spec("drop", 2600, 0.8)
+    b = SceneBatch([A], cuda, tuning=t)
+    assert (A.cell_ratio, A.tpp) == (e["cell_ratio"], e["tpp"])
+    b.step()
+    b.check()
