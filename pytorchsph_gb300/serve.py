@@ -3,7 +3,8 @@
 `SceneBatch` holds any number of independent scenes in one concatenated particle array
 (per-particle scene index, per-scene grid / parameters / dt in a device scene table,
 (scene, cell) sort keys) and advances all of them with one fixed sequence of kernels:
-keys -> counting sort -> permute -> CSR count / scan / fill -> mDBC + forces + update.
+keys -> counting sort -> permute -> mDBC beside neighbor records + segment lists -> pass 1
+-> diffusion + update (with pairs = "csr": a CSR count / scan / fill after the permute).
 Buffers are static, so one batch step can be captured once in a CUDA graph and replayed.
 Scenes never interact: each scene's particles sort into their own cell range and every
 kernel reads only its own scene's cells, so a scene gives the same bits alone and in any
@@ -139,7 +140,8 @@ class SceneBatch:
     """A fixed set of scenes stepped together (deltaSPH, semi-implicit Euler).
 
     pairs = "cells": the force passes take each particle's pairs straight from its cell rows
-    (no neighbor list; pass 1 keeps per-row bit masks for the diffusion pass).  pairs =
+    (no neighbor list; the records launch keeps each particle's accepted candidates as
+    segment bit masks for both force passes).  pairs =
     "csr": a CSR neighbor list is counted and filled every step first.  Both visit the
     pairs in the same order and give the same sums.
 
@@ -246,6 +248,11 @@ class SceneBatch:
         self.a = {"x": torch.cat(pos), "v": torch.cat(vel), "rho": torch.cat(rho), "area": torch.cat(area),
                   "sup": torch.cat(sup), "sid": sid, "uid": uid}
         self.b = {k: torch.empty_like(v) for k, v in self.a.items()}
+        # x, v, rho: unsorted state in a, sorted copy in b (the update writes a).  The static
+        # per-particle arrays alternate instead: the state's are in a (par 0) or b (par 1),
+        # the sort writes the other set, which becomes the state's after the step.
+        self.par = 0
+        self.s = None            # the sorted working set of the current step
         self._inv = torch.empty(n, dtype=torch.int32, device=dev)
         self.ws = Workspace(dev)
         self.status = torch.zeros(1, dtype=torch.int32, device=dev)
@@ -278,6 +285,7 @@ class SceneBatch:
             self.pair_cap = int(P * pair_headroom) + 1024
             self.cols = torch.empty(self.pair_cap, dtype=torch.int32, device=dev)
         self.graph = None
+        self._side = torch.cuda.Stream(dev)
         self.steps_done = 0
 
     def _setup_walls(self, wpos, wgh, war, wsid):
@@ -319,22 +327,35 @@ class SceneBatch:
         return out
 
     # ------------------------------------------------------------------ one batch step
+    AUX = ("area", "sup", "sid", "uid")
+
+    def _aux(self, which: int) -> dict:
+        return self.a if which == 0 else self.b
+
+    def state_arrays(self) -> dict:
+        """x, v, rho and the static per-particle arrays of the current (unsorted) state."""
+        cur = self._aux(self.par)
+        return {"x": self.a["x"], "v": self.a["v"], "rho": self.a["rho"], **{k: cur[k] for k in self.AUX}}
+
     def _sort_permute(self):
         st = N.stream_ptr()
         n = self.n
-        N.call("sph_batch_cell_keys", N.ptr(self.a["x"]), n, N.ptr(self.a["sid"]), N.ptr(self.scenes), self.cap,
+        cur, nxt = self._aux(self.par), self._aux(self.par ^ 1)
+        N.call("sph_batch_cell_keys", N.ptr(self.a["x"]), n, N.ptr(cur["sid"]), N.ptr(self.scenes), self.cap,
                N.ptr(self.keys), N.ptr(self.hist), N.ptr(self.status), st)
         # inside a cell, order by particle id: a scene's order never depends on its history
         # or on the other scenes of the batch
         N.call("sph_counting_sort_tie", N.ptr(self.keys), n, self.cap, N.ptr(self.hist), N.ptr(self.cell_start),
-               N.ptr(self.a["uid"]), N.ptr(self.order), N.ptr(self.skeys), N.ptr(self.status),
+               N.ptr(cur["uid"]), N.ptr(self.order), N.ptr(self.skeys), N.ptr(self.status),
                N.ptr(self.cs_scratch), self.cs_scratch.numel() * 8, st)
-        N.permute_arrays(self.order, [(self.a[k], self.b[k]) for k in self.a])
+        N.permute_arrays(self.order, [(self.a[k], self.b[k]) for k in ("x", "v", "rho")] +
+                         [(cur[k], nxt[k]) for k in self.AUX])
+        self.s = {"x": self.b["x"], "v": self.b["v"], "rho": self.b["rho"], **{k: nxt[k] for k in self.AUX}}
 
     def _count(self):
         st = N.stream_ptr()
         n = self.n
-        b = self.b
+        b = self.s
         N.call("sph_batch_nl_count", N.ptr(b["x"]), N.ptr(b["sup"]), n, N.ptr(self.skeys), N.ptr(self.cell_start),
                N.ptr(self.scenes), N.ptr(b["sid"]), N.ptr(self.counts), st)
         N.call("sph_exclusive_scan_i32", N.ptr(self.counts), N.ptr(self.offsets), n, N.ptr(self.scan_scratch),
@@ -344,7 +365,7 @@ class SceneBatch:
         """The CSR neighbor list of the sorted batch (pairs = "csr" only)."""
         if self.pairs != "csr":
             return
-        b = self.b
+        b = self.s
         self._count()
         N.call("sph_batch_nl_fill", N.ptr(b["x"]), N.ptr(b["sup"]), self.n, N.ptr(self.skeys),
                N.ptr(self.cell_start), N.ptr(self.scenes), N.ptr(b["sid"]), N.ptr(self.offsets), self.pair_cap,
@@ -352,14 +373,14 @@ class SceneBatch:
 
     def fluid_view(self):
         """The sorted batch as the C ABI's fluid view (no CSR arrays with pairs = "cells")."""
-        b = self.b
+        b = self.s
         return FluidViewC(N.ptr(b["x"]), N.ptr(b["v"]), N.ptr(b["rho"]), N.ptr(b["area"]), N.ptr(self.skeys),
                           N.ptr(self.offsets), N.ptr(self.cols), N.ptr(self.cell_start), self.n, self.pair_cap)
 
     def forces(self, out, phases=None):
         """The launches of sph_batch_deltasph_step selected by `phases` (all by default),
         writing the updated state to out["x"], out["v"], out["rho"]."""
-        b = self.b
+        b = self.s
         fv = self.fluid_view()
         N.call("sph_batch_deltasph_step", ctypes.byref(fv), ctypes.byref(self.wall_view), N.ptr(self.scenes),
                N.ptr(b["sid"]), N.ptr(self.w["sid"]), N.ptr(self.dpdt), N.ptr(self.acc), N.ptr(self.grad_rho),
@@ -369,21 +390,32 @@ class SceneBatch:
                N.ptr(self.forces_scratch), self.forces_scratch.numel() * 8, N.stream_ptr())
 
     def step_kernels(self):
-        """The batch step as a fixed kernel sequence (no host synchronisation)."""
-        a, b = self.a, self.b
+        """The batch step as a fixed kernel sequence (no host synchronisation).  The wall
+        densities (mDBC) run on a side stream beside the neighbor records: they read the
+        sorted fluid and write only the wall arrays, and pass 1 waits for both."""
+        a = self.a
         self._sort_permute()
         self._pair_list()
-        self.forces(a)
-        N.permute_arrays(None, [(b[k], a[k]) for k in ("area", "sup", "sid", "uid")])
+        if self.nb:
+            main = torch.cuda.current_stream()
+            self._side.wait_stream(main)
+            with torch.cuda.stream(self._side):
+                self.forces(a, N.SPH_PHASE_WALLS)
+            self.forces(a, N.SPH_PHASE_RECORDS)
+            main.wait_stream(self._side)
+            self.forces(a, N.SPH_PHASE_PASS1 | N.SPH_PHASE_DIFFUSION)
+        else:
+            self.forces(a)
+        self.par ^= 1             # the sorted static arrays are the state's now
 
     # kernels of this library launched by one batch step (for the bench's launch count): keys 1,
     # counting sort (scan 3 + scatter + fix + fix_large) 6, permute 1, [csr: count 1, scan 3,
     # fill 1], mdbc 1, records 1, per particle group pass1 + update 1 (+ diffusion + update 1
-    # when renormalized), copy 1
+    # when renormalized)
     def launches_per_step(self):
         csr = 1 + 3 + 1 if self.pairs == "csr" else 0
         groups = sum(1 for lo, hi, _ in self.groups if hi > lo)
-        return 1 + 6 + 1 + csr + (1 if self.nb else 0) + 1 + groups * (1 + (1 if self.any_renorm else 0)) + 1
+        return 1 + 6 + 1 + csr + (1 if self.nb else 0) + 1 + groups * (1 + (1 if self.any_renorm else 0))
 
     def capture(self):
         """Capture one batch step into a CUDA graph (after a warm-up step)."""
@@ -393,15 +425,22 @@ class SceneBatch:
             self.step_kernels()
         torch.cuda.current_stream().wait_stream(s)
         torch.cuda.synchronize()
-        self.graph = torch.cuda.CUDAGraph()
-        with torch.cuda.graph(self.graph):
-            self.step_kernels()
+        # one graph per parity of the static arrays; capturing runs nothing, so after the two
+        # captures the parity is the device state's again
+        graphs = [None, None]
+        for _ in range(2):
+            p = self.par
+            graphs[p] = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(graphs[p]):
+                self.step_kernels()
+        self.graph = graphs
         torch.cuda.synchronize()
         self.steps_done += 1
 
     def step(self):
         if self.graph is not None:
-            self.graph.replay()
+            self.graph[self.par].replay()
+            self.par ^= 1
         else:
             self.step_kernels()
         self.steps_done += 1
@@ -440,7 +479,8 @@ class SceneBatch:
         """Positions, velocities and densities of every scene in its original particle order,
         concatenated scene after scene in batch order (device; take a scene with
         scene_state_device)."""
-        dst = (self.p_off_dev[self.a["sid"].long()] + self.a["uid"].long()).to(torch.int32)
+        cur = self._aux(self.par)
+        dst = (self.p_off_dev[cur["sid"].long()] + cur["uid"].long()).to(torch.int32)
         out = {k: torch.empty_like(self.a[k]) for k in ("x", "v", "rho")}
         N.call("sph_invert_permutation", N.ptr(dst), self.n, N.ptr(self._inv), N.stream_ptr())
         N.permute_arrays(self._inv, [(self.a[k], out[k]) for k in ("x", "v", "rho")])
