@@ -241,7 +241,7 @@ __global__ void k_count_scatter(const uint32_t* __restrict__ keys, int64_t n, co
   tmp[slot] = (uint32_t)i;
 }
 
-constexpr int kSmallCell = 48;    // cells up to this size are sorted by one thread in registers
+constexpr int kSmallCell = 48;    // cells up to this size are ordered by ranking, one thread per particle
 constexpr int kBlockSortMax = 2048;  // larger cells: one block, bitonic sort in shared memory
 
 // Sort key inside a cell: the particle's index, or (tie[index], index) when a tie key is
@@ -250,36 +250,30 @@ __device__ __forceinline__ uint64_t cell_rank(uint32_t x, const uint32_t* __rest
   return tie ? (((uint64_t)__ldg(tie + x)) << 32) | x : (uint64_t)x;
 }
 
-// Per-cell fix-up: restore ascending (tie, index) order inside every cell, write the sorted
-// keys.  Cells larger than kSmallCell are queued for k_cell_fix_large.
-__global__ void __launch_bounds__(128) k_cell_fix(const int32_t* __restrict__ cell_start, int32_t ncell_slots,
+// Per-slot fix-up of ascending (tie, index) order inside every cell, and the sorted keys.
+// After the scatter, cell c's particles fill [cell_start[c], cell_start[c+1]) in atomic
+// order; the thread of slot t counts the cell's particles that rank below its own and
+// writes its particle to that place (k comparisons per particle, L1-resident).  Cells larger
+// than kSmallCell are queued for k_cell_fix_large by the thread of their first slot.
+__global__ void __launch_bounds__(256) k_cell_fix(const uint32_t* __restrict__ keys, int64_t n,
+                                                  const int32_t* __restrict__ cell_start,
                                                   const uint32_t* __restrict__ tmp, const uint32_t* __restrict__ tie,
                                                   uint32_t* __restrict__ order, uint32_t* __restrict__ sorted_keys,
                                                   int32_t* __restrict__ big_list, int32_t* __restrict__ big_count) {
-  int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= ncell_slots) return;
-  const int b = cell_start[c], e = cell_start[c + 1];
-  const int k = e - b;
-  if (k == 0) return;
-  for (int t = b; t < e; ++t) sorted_keys[t] = (uint32_t)c;
-  if (k <= kSmallCell) {
-    uint64_t v[kSmallCell];
-#pragma unroll 1
-    for (int t = 0; t < k; ++t) {
-      uint64_t x = cell_rank(tmp[b + t], tie);
-      int u = t;
-      while (u > 0 && v[u - 1] > x) {
-        v[u] = v[u - 1];
-        --u;
-      }
-      v[u] = x;
-    }
-#pragma unroll 1
-    for (int t = 0; t < k; ++t) order[b + t] = (uint32_t)(v[t] & 0xffffffffu);
-  } else {
-    int q = atomicAdd(big_count, 1);
-    big_list[q] = c;
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const uint32_t x = tmp[t];
+  const uint32_t c = __ldg(keys + x);
+  sorted_keys[t] = c;
+  const int b = __ldg(cell_start + c), e = __ldg(cell_start + c + 1);
+  if (e - b > kSmallCell) {
+    if (t == b) big_list[atomicAdd(big_count, 1)] = (int32_t)c;
+    return;
   }
+  const uint64_t mine = cell_rank(x, tie);
+  int rank = 0;
+  for (int u = b; u < e; ++u) rank += cell_rank(__ldg(tmp + u), tie) < mine;
+  order[b + rank] = x;
 }
 
 // One block per large cell: bitonic sort of up to kBlockSortMax entries in shared memory.
@@ -538,8 +532,8 @@ sph_status_t sph_counting_sort_tie(const uint32_t* keys, int64_t n, int32_t cell
   if (n == 0) return SPH_OK;
   cudaMemsetAsync(big_count, 0, sizeof(int32_t), st);
   k_count_scatter<<<grid_for(n, 256), 256, 0, st>>>(keys, n, cell_start, cell_count, tmp);
-  k_cell_fix<<<grid_for(slots, 128), 128, 0, st>>>(cell_start, (int32_t)slots, tmp, tie, order, sorted_keys,
-                                                   big_list, big_count);
+  k_cell_fix<<<grid_for(n, 256), 256, 0, st>>>(keys, n, cell_start, tmp, tie, order, sorted_keys, big_list,
+                                               big_count);
   k_cell_fix_large<<<kNumSMs, 512, 0, st>>>(cell_start, tmp, tie, order, big_list, big_count, status);
   SPH_CHECK_LAUNCH("counting_sort");
   return SPH_OK;
