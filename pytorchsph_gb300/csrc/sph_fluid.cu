@@ -422,7 +422,7 @@ __device__ __forceinline__ Pass1 pass1_body(int i, const FluidView& F, const flo
   gfy *= 2.0f;
   o.grad_rho = make_float2(0.f, 0.f);
   if (renorm) {
-    const float4 Li = pinv2x2(o.L.x, o.L.y, o.L.z, o.L.w);
+    const float4 Li = pinv2x2_fast(o.L.x, o.L.y, o.L.z, o.L.w);
     const float fx = Li.x * gfx + Li.y * gfy, fy = Li.z * gfx + Li.w * gfy;
     const float wx = Li.x * gwx + Li.y * gwy, wy = Li.z * gwx + Li.w * gwy;
     o.grad_rho = make_float2(-fx - wx, -fy - wy);

@@ -120,6 +120,25 @@ __device__ __forceinline__ float4 pinv2x2(float a, float b, float c, float d) {
   return make_float4(m00 * ct - m01 * st, m00 * st + m01 * ct, m10 * ct - m11 * st, m10 * st + m11 * ct);
 }
 
+// pinv2x2 of a well-conditioned M: there the pseudo-inverse is the inverse adj(M) / det, a
+// few operations instead of the closed form's atan2 / cos / sin.  With S1 = |M|_F^2 and
+// sigma_max^2 = (S1 + sqrt(S1^2 - 4 det^2)) / 2 (no cancellation), sigma_min^2 = det^2 /
+// sigma_max^2.  Taken when sigma_min > 0.1 sigma_max and sigma_min > 2e-5 (twice the 1e-5
+// cutoff): there the closed form in float32 is itself within ~1e-5 of the inverse (its small
+// singular value carries a relative error of ~FLT_EPSILON (sigma_max / sigma_min)^2).  Any
+// other M (free-surface particles, non-finite input) goes through pinv2x2.
+__device__ __forceinline__ float4 pinv2x2_fast(float a, float b, float c, float d) {
+  const float det = a * d - b * c;
+  const float S1 = a * a + b * b + c * c + d * d;
+  const float s1sq = 0.5f * (S1 + sqrtf(fmaxf(S1 * S1 - 4.0f * det * det, 0.0f)));
+  const float d2 = det * det;
+  if (d2 > 0.01f * s1sq * s1sq && d2 > 4e-10f * s1sq && isfinite(d2)) {
+    const float id = 1.0f / det;
+    return make_float4(d * id, -b * id, -c * id, a * id);
+  }
+  return pinv2x2(a, b, c, d);
+}
+
 // x = pinv(A) b for a 3x3 A in double (torch.linalg.pinv semantics: singular values below
 // 3 * FLT_EPSILON * sigma_max are dropped).  Eigen-decomposition of A^T A by cyclic Jacobi
 // rotations (at most 16 sweeps), then pinv(A) b = sum_k v_k ((A v_k) . b) / sigma_k^2.
