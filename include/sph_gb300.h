@@ -338,12 +338,12 @@ sph_status_t sph_batch_nl_fill(const float* xy, const float* sorted_support, int
  * in the force passes), and both force passes visit those pairs, in the CSR fill's order
  * (same sums).  Each scene's pair test then uses its own support (sph_params.support),
  * which must be every particle's support.
- * The force passes (pass1, diffusion) run over particle groups: group k is the sorted
- * particles [group_begin[k], group_begin[k+1]) (host arrays; group_begin[0] = 0,
- * group_begin[ngroups] = n, so a group holds whole scenes when it ends at scene bounds) with
- * group_tpp[k] lanes per particle: 1, or 2 or 4 with pairs from the cell rows (each lane
- * takes every 2nd or 4th segment; the lanes' sums are added by warp shuffles, so the
- * summation order, not the pair set, depends on it).  ngroups = 0: one group, one lane.
+ * The force passes (pass1, diffusion) run over `groups` (a host array of ngroups entries
+ * that tile [0, n) in order; a group holds whole scenes when its bounds are scene bounds):
+ * `tpp` lanes per particle (each lane takes every 2nd or 4th segment; the lanes' sums are
+ * added by warp shuffles, so the summation order, not the pair set, depends on it) and,
+ * when all its scenes share one, the diffusion `scheme`, which selects a kernel compiled for
+ * it.  ngroups = 0: one group, one lane, any schemes.
  * `phases` selects the launches (SPH_PHASE_ALL for a step; single phases, in order, let a
  * caller time each kernel): walls = mDBC wall densities, records = per-particle neighbor
  * records, pass1 = first pair pass (+ update of scenes without deltaSPH diffusion),
@@ -353,12 +353,19 @@ sph_status_t sph_batch_nl_fill(const float* xy, const float* sorted_support, int
 #define SPH_PHASE_PASS1 4
 #define SPH_PHASE_DIFFUSION 8
 #define SPH_PHASE_ALL 15
+/* A range of sorted particles that the force passes run over with one kernel variant. */
+typedef struct sph_force_group {
+  int64_t begin, end;  /* sorted particles [begin, end) */
+  int32_t tpp;         /* lanes per particle: 1, or 2 or 4 with pairs from the cell rows */
+  int32_t scheme;      /* the density diffusion of every scene in the range (0 none, 1 MOG,
+                          2 deltaSPH), or -1 when they differ */
+} sph_force_group;
 sph_status_t sph_batch_deltasph_step(const sph_fluid_view* fluid, const sph_wall_view* walls, const void* scenes,
                                      const int32_t* sid, const int32_t* wall_sid, float* dpdt, float* acc,
                                      float* grad_rho, int32_t any_renormalized, float* x_out, float* v_out,
                                      float* rho_out, int32_t* status, int32_t phases, int32_t ngroups,
-                                     const int64_t* group_begin, const int32_t* group_tpp, void* scratch,
-                                     size_t scratch_bytes, void* stream);
+                                     const sph_force_group* groups, void* scratch, size_t scratch_bytes,
+                                     void* stream);
 
 /* ---------------------------------------------------------------- Module terms (a9-a17) */
 

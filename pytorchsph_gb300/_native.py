@@ -69,7 +69,7 @@ SIGNATURES.update({  # batch of scenes
     "sph_batch_cell_keys": (_I32, [_P, _I64, _P, _P, _I32, _P, _P, _P, _P]),
     "sph_batch_nl_count": (_I32, [_P, _P, _I64, _P, _P, _P, _P, _P, _P]),
     "sph_batch_nl_fill": (_I32, [_P, _P, _I64, _P, _P, _P, _P, _P, _I64, _P, _P, _P]),
-    "sph_batch_deltasph_step": (_I32, [_P] * 8 + [_I32] + [_P] * 4 + [_I32, _I32, _P, _P, _P, _SZ, _P]),
+    "sph_batch_deltasph_step": (_I32, [_P] * 8 + [_I32] + [_P] * 4 + [_I32, _I32, _P, _P, _SZ, _P]),
 })
 
 SIGNATURES.update({  # Module-interface terms

@@ -288,14 +288,17 @@ struct Segments {
 // kTpp lanes per particle (kCells only): lane `sub` sums its share of the pairs, the lanes
 // add their sums, and lane 0 finishes (walls, gravity, L^+); the other lanes return a zero
 // record.  `live` false: a lane past the last particle, which only takes part in the sums.
-template <bool kCells, int kTpp = 1>
+// kScheme: the density diffusion (0 none, 1 MOG, 2 deltaSPH) fixed at compile time, or -1:
+// read from P.diffusion.
+template <bool kCells, int kTpp = 1, int kScheme = -1>
 __device__ __forceinline__ Pass1 pass1_body(int i, const FluidView& F, const float4* __restrict__ xv,
                                             const float4* __restrict__ qv, const WallView& W, const sph_grid& g,
                                             const SphParams& P, int coff, const Segments& S, int sub = 0,
                                             bool live = true) {
   const float4 si = xv[i];
   const float rhoi = qv[i].x, pi = tait(F.rho[i], P);
-  const bool renorm = P.diffusion == 2;
+  const int scheme = kScheme >= 0 ? kScheme : P.diffusion;
+  const bool renorm = scheme == 2;
   const float mu8 = 4.0f * (2.0f * rhoi * P.kinematic);   // 4 (mu_i + mu_j), both rho_i nu
   float dp_f = 0.f, mog = 0.f;
   float pax = 0.f, pay = 0.f, vax = 0.f, vay = 0.f, lax = 0.f, lay = 0.f;
@@ -309,7 +312,7 @@ __device__ __forceinline__ Pass1 pass1_body(int i, const FluidView& F, const flo
     const float ir2 = __fdividef(1.0f, e.r2 + P.eps);
     const float rg = -e.gd * e.r2;                        // (x_j - x_i) . gradW
     dp_f -= e.gd * ud * mj;
-    if (P.diffusion == 1) mog += (rhoj - rhoi) * ir2 * rg * Vj;   // x 2 after the sum
+    if (scheme == 1) mog += (rhoj - rhoi) * ir2 * rg * Vj;   // x 2 after the sum
     const float pf = fmaf(pi, Vj, pVj) * e.gd;            // (p_i + p_j) V_j gd
     pax += pf * e.dx;
     pay += pf * e.dy;
@@ -395,7 +398,7 @@ __device__ __forceinline__ Pass1 pass1_body(int i, const FluidView& F, const flo
   }
   Pass1 o;
   o.dpdt = dp_f + dp_w;
-  if (P.diffusion == 1) o.dpdt += P.diff_k * (2.0f * mog);
+  if (scheme == 1) o.dpdt += P.diff_k * (2.0f * mog);
   float ax, ay;
   if (P.point_source) {
     float dx = si.x - P.point_cx, dy = si.y - P.point_cy;
@@ -562,7 +565,7 @@ __device__ __forceinline__ void batch_update(int i, const FluidView& F, float ax
 // <grad rho> to k_batch_diffusion, which finishes and updates them.  kCells: pairs from the
 // segment lists; kTpp lanes per particle (kCells only).  With kTpp > 1 no lane leaves
 // before the lane sums: lanes past p_hi take part with nothing to add.
-template <bool kCells, int kTpp>
+template <bool kCells, int kTpp, int kScheme>
 __global__ void __launch_bounds__(128, 8) k_batch_pass1(FluidView F, const float4* __restrict__ xv,
                                                      const float4* __restrict__ qv, WallView W,
                                                      const SceneDev* __restrict__ scenes,
@@ -585,9 +588,9 @@ __global__ void __launch_bounds__(128, 8) k_batch_pass1(FluidView F, const float
   }
   const SceneDev& S = scenes[sid[i]];
   const SphParams P = S.P;   // the fields the loop reads, in registers
-  const Pass1 o = pass1_body<kCells, kTpp>(i, F, xv, qv, W, S.g, P, S.coff, seg, sub, kTpp == 1 || live);
+  const Pass1 o = pass1_body<kCells, kTpp, kScheme>(i, F, xv, qv, W, S.g, P, S.coff, seg, sub, kTpp == 1 || live);
   if (kTpp > 1 && (!live || sub != 0)) return;
-  if (P.diffusion == 2) {
+  if ((kScheme >= 0 ? kScheme : P.diffusion) == 2) {
     dpdt[i] = o.dpdt;
     acc[i] = make_float2(o.ax, o.ay);
     grad_rho[i] = o.grad_rho;
@@ -798,8 +801,8 @@ sph_status_t sph_batch_deltasph_step(const sph_fluid_view* fluid, const sph_wall
                                      const int32_t* sid, const int32_t* wall_sid, float* dpdt, float* acc,
                                      float* grad_rho, int32_t any_renormalized, float* x_out, float* v_out,
                                      float* rho_out, int32_t* status, int32_t phases, int32_t ngroups,
-                                     const int64_t* group_begin, const int32_t* group_tpp, void* scratch,
-                                     size_t scratch_bytes, void* stream) {
+                                     const sph_force_group* groups, void* scratch, size_t scratch_bytes,
+                                     void* stream) {
   SPH_VIEW_CHECK(fluid);
   SPH_VIEW_CHECK(walls);
   SPH_REQUIRE(scenes && sid && x_out && v_out && rho_out && status, "batch_deltasph_step: bad arguments");
@@ -811,18 +814,18 @@ sph_status_t sph_batch_deltasph_step(const sph_fluid_view* fluid, const sph_wall
   SPH_REQUIRE(cells || (fluid->offsets && fluid->cols), "batch_deltasph_step: give both offsets and cols, or neither");
   SPH_REQUIRE(fluid->cell_start && fluid->keys, "batch_deltasph_step: bad arguments");
   const int n = (int)fluid->n;
-  // particle groups of the force passes: one group of one lane per particle by default
-  const int64_t all[2] = {0, n};
-  const int32_t one[1] = {1};
-  SPH_REQUIRE(ngroups >= 0 && (ngroups == 0 || (group_begin && group_tpp)), "batch_deltasph_step: bad groups");
+  // force groups: by default one group, one lane per particle, any schemes
+  const sph_force_group all{0, n, 1, -1};
+  SPH_REQUIRE(ngroups >= 0 && (ngroups == 0 || groups), "batch_deltasph_step: bad groups");
   const int ng = ngroups ? ngroups : 1;
-  const int64_t* gb = ngroups ? group_begin : all;
-  const int32_t* gt = ngroups ? group_tpp : one;
-  SPH_REQUIRE(gb[0] == 0 && gb[ng] == n, "batch_deltasph_step: the groups must cover [0, n)");
+  const sph_force_group* G = ngroups ? groups : &all;
+  SPH_REQUIRE(G[0].begin == 0 && G[ng - 1].end == n, "batch_deltasph_step: the groups must tile [0, n)");
   for (int k = 0; k < ng; ++k) {
-    SPH_REQUIRE(gb[k] <= gb[k + 1], "batch_deltasph_step: group bounds must not decrease");
-    SPH_REQUIRE(gt[k] == 1 || (cells && (gt[k] == 2 || gt[k] == 4)),
+    SPH_REQUIRE(G[k].begin <= G[k].end && (k == 0 || G[k].begin == G[k - 1].end),
+                "batch_deltasph_step: the groups must tile [0, n) in order");
+    SPH_REQUIRE(G[k].tpp == 1 || (cells && (G[k].tpp == 2 || G[k].tpp == 4)),
                 "batch_deltasph_step: lanes per particle must be 1 (2 or 4 with pairs from the cell rows)");
+    SPH_REQUIRE(G[k].scheme >= -1 && G[k].scheme <= 2, "batch_deltasph_step: bad diffusion scheme");
   }
   if (n == 0) return SPH_OK;
   float4 *xv, *qv;
@@ -841,28 +844,38 @@ sph_status_t sph_batch_deltasph_step(const sph_fluid_view* fluid, const sph_wall
   float2* vo = reinterpret_cast<float2*>(v_out);
   float2* gr = reinterpret_cast<float2*>(grad_rho);
   float2* ac = reinterpret_cast<float2*>(acc);
-  for (int k = 0; k < ng; ++k) {
-    const int lo = (int)gb[k], hi = (int)gb[k + 1], t = gt[k];
-    if (hi <= lo) continue;
+  // kernel variants: CSR rows run one lane and read the scheme per scene; cell rows have 1, 2
+  // or 4 lanes and a scheme of MOG, deltaSPH or read per scene
+  auto pass1 = [&](int lo, int hi, int t, int scheme) {
     const int nb = grid_for((int64_t)(hi - lo) * t, 128);
-    if (phases & SPH_PHASE_PASS1) {
-      if (!cells)
-        k_batch_pass1<false, 1><<<nb, 128, 0, st>>>(F, xv, qv, W, S, sid, dpdt, ac, gr, Segments{}, xo, vo, rho_out,
-                                                    status, lo, hi);
-      else if (t == 1)
-        k_batch_pass1<true, 1><<<nb, 128, 0, st>>>(F, xv, qv, W, S, sid, dpdt, ac, gr, seg, xo, vo, rho_out, status,
-                                                   lo, hi);
-      else if (t == 2)
-        k_batch_pass1<true, 2><<<nb, 128, 0, st>>>(F, xv, qv, W, S, sid, dpdt, ac, gr, seg, xo, vo, rho_out, status,
-                                                   lo, hi);
-      else
-        k_batch_pass1<true, 4><<<nb, 128, 0, st>>>(F, xv, qv, W, S, sid, dpdt, ac, gr, seg, xo, vo, rho_out, status,
-                                                   lo, hi);
+#define SPH_PASS1(C, T, K)                                                                                  \
+  k_batch_pass1<C, T, K><<<nb, 128, 0, st>>>(F, xv, qv, W, S, sid, dpdt, ac, gr, C ? seg : Segments{}, xo, vo, \
+                                             rho_out, status, lo, hi)
+    if (!cells) {
+      SPH_PASS1(false, 1, -1);
+      return;
     }
-  }
+    const int k = scheme == 1 || scheme == 2 ? scheme : -1;
+    if (t == 1) {
+      if (k == 2) SPH_PASS1(true, 1, 2);
+      else if (k == 1) SPH_PASS1(true, 1, 1);
+      else SPH_PASS1(true, 1, -1);
+    } else if (t == 2) {
+      if (k == 2) SPH_PASS1(true, 2, 2);
+      else if (k == 1) SPH_PASS1(true, 2, 1);
+      else SPH_PASS1(true, 2, -1);
+    } else {
+      if (k == 2) SPH_PASS1(true, 4, 2);
+      else if (k == 1) SPH_PASS1(true, 4, 1);
+      else SPH_PASS1(true, 4, -1);
+    }
+#undef SPH_PASS1
+  };
+  for (int k = 0; k < ng && (phases & SPH_PHASE_PASS1); ++k)
+    if (G[k].end > G[k].begin) pass1((int)G[k].begin, (int)G[k].end, G[k].tpp, G[k].scheme);
   for (int k = 0; k < ng && any_renormalized && (phases & SPH_PHASE_DIFFUSION); ++k) {
-    const int lo = (int)gb[k], hi = (int)gb[k + 1], t = gt[k];
-    if (hi <= lo) continue;
+    const int lo = (int)G[k].begin, hi = (int)G[k].end, t = G[k].tpp;
+    if (hi <= lo || G[k].scheme == 0 || G[k].scheme == 1) continue;   // no deltaSPH scene in the group
     const int nb = grid_for((int64_t)(hi - lo) * t, 128);
     if (!cells)
       k_batch_diffusion<false, 1><<<nb, 128, 0, st>>>(F, qv, S, sid, gr, Segments{}, dpdt, ac, xo, vo, rho_out,

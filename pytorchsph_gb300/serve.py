@@ -50,6 +50,12 @@ def _params_for(cfg: SimConfig, h: float, cells: int, cell_ratio: int = 1) -> Sp
     return P
 
 
+class ForceGroupC(ctypes.Structure):
+    """sph_force_group: sorted particles [begin, end), lanes per particle, diffusion scheme."""
+    _fields_ = [("begin", ctypes.c_int64), ("end", ctypes.c_int64), ("tpp", ctypes.c_int32),
+                ("scheme", ctypes.c_int32)]
+
+
 class _Grid(ctypes.Structure):
     _fields_ = [("qmin", ctypes.c_float * 2), ("hmax", ctypes.c_float), ("hmax_threshold", ctypes.c_float),
                 ("cells_x", ctypes.c_int32), ("cells_y", ctypes.c_int32), ("num_cells", ctypes.c_int32),
@@ -146,9 +152,9 @@ class SceneBatch:
     pairs in the same order and give the same sums.
 
     Each scene runs with its spec's cell_ratio and tpp (set from `tuning`, a
-    `tune.Tuning`, when given): the batch keeps its scenes grouped by tpp, and each group is
-    one particle range of the force passes.  Per-scene methods take the scenes' indices in
-    `specs` order."""
+    `tune.Tuning`, when given): the batch keeps its scenes grouped by (tpp, density-diffusion
+    scheme), and each group is one particle range of the force passes with a kernel compiled
+    for its lanes and scheme.  Per-scene methods take the scenes' indices in `specs` order."""
 
     def __init__(self, specs, device=None, states=None, pair_headroom: float = 1.3, pairs: str = "cells",
                  tuning=None):
@@ -166,8 +172,9 @@ class SceneBatch:
             if sp.tpp not in (1, 2, 4) or sp.cell_ratio not in (1, 2):
                 raise ValueError("tpp must be 1, 2 or 4 and cell_ratio 1 or 2")
         lanes = [sp.tpp if pairs == "cells" else 1 for sp in specs]
-        # scenes grouped by lanes per particle (stable): _order[k] = the spec of batch scene k
-        self._order = sorted(range(len(specs)), key=lambda k: lanes[k])
+        schemes = [DIFFUSION[sp.cfg.density_diffusion] for sp in specs]
+        # scenes grouped by (lanes per particle, scheme), stable: _order[k] = the spec of batch scene k
+        self._order = sorted(range(len(specs)), key=lambda k: (lanes[k], schemes[k]))
         self._slot = [0] * len(specs)
         for k, e in enumerate(self._order):
             self._slot[e] = k
@@ -223,20 +230,17 @@ class SceneBatch:
                                          dtype=torch.int64, device=dev)
         self.n = self.p_off[-1]
         n = self.n
-        # force-pass groups: runs of scenes with the same lanes per particle
-        lanes_in = [lanes[e] for e in self._order]
-        begin, tpp = [0], []
+        # force-pass groups: runs of scenes with the same (lanes per particle, scheme)
+        kind = [(lanes[e], schemes[e]) for e in self._order]
+        self.groups = []                      # (begin, end, tpp, scheme)
         for k in range(S):
-            if k == 0 or lanes_in[k] != lanes_in[k - 1]:
-                if k:
-                    begin.append(self.p_off[k])
-                tpp.append(lanes_in[k])
-        begin.append(n)
-        if not tpp:
-            begin, tpp = [0, n], [1]
-        self.groups = list(zip(begin[:-1], begin[1:], tpp))
-        self._group_begin = (ctypes.c_int64 * len(begin))(*begin)
-        self._group_tpp = (ctypes.c_int32 * len(tpp))(*tpp)
+            if k == 0 or kind[k] != kind[k - 1]:
+                self.groups.append([self.p_off[k], self.p_off[k + 1], *kind[k]])
+            else:
+                self.groups[-1][1] = self.p_off[k + 1]
+        if not self.groups:
+            self.groups = [[0, n, 1, -1]]
+        self._groups_c = (ForceGroupC * len(self.groups))(*[ForceGroupC(*g) for g in self.groups])
         # scene index and particle id of every particle; p_off_dev[sid] + uid is its slot in the
         # concatenation of the scenes in their own particle order
         counts = torch.tensor(np.diff(self.p_off), dtype=torch.int64, device=dev)
@@ -385,9 +389,9 @@ class SceneBatch:
         N.call("sph_batch_deltasph_step", ctypes.byref(fv), ctypes.byref(self.wall_view), N.ptr(self.scenes),
                N.ptr(b["sid"]), N.ptr(self.w["sid"]), N.ptr(self.dpdt), N.ptr(self.acc), N.ptr(self.grad_rho),
                int(self.any_renorm), N.ptr(out["x"]), N.ptr(out["v"]), N.ptr(out["rho"]), N.ptr(self.status),
-               N.SPH_PHASE_ALL if phases is None else phases, len(self._group_tpp),
-               ctypes.cast(self._group_begin, ctypes.c_void_p), ctypes.cast(self._group_tpp, ctypes.c_void_p),
-               N.ptr(self.forces_scratch), self.forces_scratch.numel() * 8, N.stream_ptr())
+               N.SPH_PHASE_ALL if phases is None else phases, len(self._groups_c),
+               ctypes.cast(self._groups_c, ctypes.c_void_p), N.ptr(self.forces_scratch),
+               self.forces_scratch.numel() * 8, N.stream_ptr())
 
     def step_kernels(self):
         """The batch step as a fixed kernel sequence (no host synchronisation).  The wall
@@ -410,12 +414,13 @@ class SceneBatch:
 
     # kernels of this library launched by one batch step (for the bench's launch count): keys 1,
     # counting sort (scan 3 + scatter + fix + fix_large) 6, permute 1, [csr: count 1, scan 3,
-    # fill 1], mdbc 1, records 1, per particle group pass1 + update 1 (+ diffusion + update 1
-    # when renormalized)
+    # fill 1], mdbc 1, records 1, per force group pass1 + update 1 (+ diffusion + update 1 for
+    # a group with deltaSPH scenes)
     def launches_per_step(self):
         csr = 1 + 3 + 1 if self.pairs == "csr" else 0
-        groups = sum(1 for lo, hi, _ in self.groups if hi > lo)
-        return 1 + 6 + 1 + csr + (1 if self.nb else 0) + 1 + groups * (1 + (1 if self.any_renorm else 0))
+        p1 = sum(1 for lo, hi, _, _ in self.groups if hi > lo)
+        dif = sum(1 for lo, hi, _, k in self.groups if hi > lo and k not in (0, 1)) if self.any_renorm else 0
+        return 1 + 6 + 1 + csr + (1 if self.nb else 0) + 1 + p1 + dif
 
     def capture(self):
         """Capture one batch step into a CUDA graph (after a warm-up step)."""
