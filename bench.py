@@ -602,7 +602,12 @@ def run_dambreak(args, dev, world, rank):
         c0 = float(10 * np.sqrt(2 * 9.81 * sc["column_height"]))
         cfg = SimConfig(solver="deltaSPH", integration="semiImplicitEuler", dt=0.25 * sc["h"] / c0, c0=c0,
                         density_diffusion="deltaSPH")
-        b = SceneBatch([SceneSpec(sc, cfg, 500)], dev)
+        spec = SceneSpec(sc, cfg, 500)
+        tuned = None
+        if not args.no_tune:   # the autotuner's one-scene pick for this size
+            from pytorchsph_gb300.tune import Autotuner, Tuning
+            tuned = Tuning(serving=Autotuner(dev).tune_serving(sizes=(len(sc["pos"]),), batch_particles=1, steps=20))
+        b = SceneBatch([spec], dev, tuning=tuned)
         b.capture()
         for _ in range(max(args.warmup, 3)):
             b.step()
@@ -619,7 +624,9 @@ def run_dambreak(args, dev, world, rank):
         ms = max_over_ranks(st.elapsed_time(en) / args.steps, world)
         n, launches = b.n, b.launches_per_step()
         config = {"workload": args.workload, "particles": n, "walls": b.nb,
-                  "solver": "deltaSPH renormalized, semi-implicit Euler", "c0": c0, "graph": "one CUDA graph per step"}
+                  "solver": "deltaSPH renormalized, semi-implicit Euler", "c0": c0, "graph": "one CUDA graph per step",
+                  "cell_ratio": spec.cell_ratio, "lanes_per_particle": spec.tpp,
+                  "chosen_by": "autotuner (one scene, measured in this run)" if tuned else "defaults"}
         if rank == 0 and not args.no_cpu_baseline:
             t = cpu_deltasph_steps(sc, {"c0": c0, "dt": cfg.dt}, 2, "deltaSPH")
             cpu = {"value": n * 2 / t, "unit": "particle-steps/s", "cores": torch.get_num_threads(), "kind": "port",

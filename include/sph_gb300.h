@@ -541,6 +541,7 @@ typedef struct sph_dfsph_buffers {
   double* partials;         /* [sph_dfsph_partials_count()] */
   float* errors;            /* [max iterations + 1] error of every iteration */
   int32_t* iters;           /* [1] iterations run */
+  float* records;           /* [9 n], 16-byte aligned: per-particle pair records of the Jacobi sweeps */
 } sph_dfsph_buffers;
 
 size_t sph_dfsph_partials_count(void);

@@ -38,6 +38,10 @@ struct DfsphBufs {
   double* partials;   // [gridDim.x] block partial errors
   float* errors;      // [max_iters + 1] error history
   int32_t* iters;     // iteration count
+  // pair records of the Jacobi sweeps, one 16-byte gather per neighbor and phase:
+  float4* rec_p;      // (x, y, m = A rho0, p / (rho rho0)^2), its pressure part updated every sweep
+  float4* rec_a;      // (x, y, predicted pressure acceleration)
+  float* fdt;         // dt^2 A_act
 };
 
 // ---------------------------------------------------------------- densities
@@ -224,24 +228,30 @@ __global__ void __launch_bounds__(128) k_dfsph_wall_prepare(FluidView F, WallVie
 }
 
 // ---------------------------------------------------------------- solver phases
-// predicted pressure acceleration of fluid particle i (dfsph.py:25-42 + solidBoundary.py:310-403)
+// The spiky gradient of pair (i, j) as gs * d with d = x_i - x_j: spikyGrad = e kGS(q), e =
+// d / r, so gs = kGS(q) / r, from one reciprocal square root (0 when r < 1e-7, where the
+// reference's e is zero).
+__device__ __forceinline__ float spiky_gd(float r2, const SphParams& P) {
+  if (!(r2 >= 1e-14f)) return 0.f;
+  const float rs = rsqrtf(r2);
+  return kGS(r2 * rs * P.inv_h, P.c_s) * rs;
+}
+
+// predicted pressure acceleration of fluid particle i (dfsph.py:25-42 + solidBoundary.py:310-403),
+// the fluid pairs from the records rec_p = (x, y, m, p / rho^2)
 __device__ __forceinline__ float2 pressure_accel(const FluidView& F, const WallView& W, const sph_grid& g,
                                                  const SphParams& P, const DfsphBufs& B, int i, bool walls) {
-  const float2 xi = F.x[i];
-  const float ri = B.rho[i] * P.rho0;
-  const float ppi = B.p[i] / (ri * ri);
+  const float4 me = B.rec_p[i];
+  const float2 xi = make_float2(me.x, me.y);
+  const float ppi = me.w;
   float ax = 0.f, ay = 0.f;
   const int k0 = F.offsets[i], kn = row_end(F, i, k0);
   for (int k = k0; k < kn; ++k) {
-    const int j = __ldg(F.cols + k);
-    const float2 xj = __ldg(F.x + j);
-    const float rj = B.rho[j] * P.rho0;
-    const float ppj = B.p[j] / (rj * rj);
-    const Geo e = geo(xi.x, xi.y, xj.x, xj.y, P.inv_h);
-    const float gs = kGS(e.q, P.c_s);
-    const float f = -(__ldg(F.area + j) * P.rho0) * (ppi + ppj) * gs;
-    ax += f * e.ex;
-    ay += f * e.ey;
+    const float4 rj = __ldg(B.rec_p + __ldg(F.cols + k));
+    const float dx = xi.x - rj.x, dy = xi.y - rj.y;
+    const float f = -rj.z * (ppi + rj.w) * spiky_gd(dx * dx + dy * dy, P);
+    ax += f * dx;
+    ay += f * dy;
   }
   if (walls) {
     float wx = 0.f, wy = 0.f;
@@ -275,25 +285,37 @@ __global__ void __launch_bounds__(256) k_dfsph_solve(FluidView F, WallView W, co
   const int nthreads = gridDim.x * blockDim.x;
   const double count = (double)F.n + (walls ? (double)W.n : 0.0);
   __shared__ double s_part[8];
+  // the pair records: positions, masses and dt^2 A_act are fixed during the solve
+  for (int i = tid; i < F.n; i += nthreads) {
+    const float2 xi = F.x[i];
+    const float ri = B.rho[i] * P.rho0;
+    B.rec_p[i] = make_float4(xi.x, xi.y, F.area[i] * P.rho0, B.p[i] / (ri * ri));
+    B.fdt[i] = dt * dt * B.aact[i];
+  }
+  grid.sync();
   double err = 0.0;
   int it = 0;
   while ((it < min_iters || err > (double)thr_err) && it <= max_iters) {
     // phase A: predicted acceleration from the current pressures
-    for (int i = tid; i < F.n; i += nthreads) B.pa[i] = pressure_accel(F, W, g, P, B, i, walls);
+    for (int i = tid; i < F.n; i += nthreads) {
+      const float2 a = pressure_accel(F, W, g, P, B, i, walls);
+      B.pa[i] = a;
+      const float4 me = B.rec_p[i];
+      B.rec_a[i] = make_float4(me.x, me.y, a.x, a.y);
+    }
     grid.sync();
     // phase B: pressure sums, residuals, relaxed Jacobi updates, error partials
     double local = 0.0;
     for (int i = tid; i < F.n; i += nthreads) {
-      const float2 xi = F.x[i], pai = B.pa[i];
+      const float4 me = B.rec_a[i];
+      const float2 xi = make_float2(me.x, me.y), pai = make_float2(me.z, me.w);
       float ks = 0.f;
       const int k0 = F.offsets[i], kn = row_end(F, i, k0);
       for (int k = k0; k < kn; ++k) {
         const int j = __ldg(F.cols + k);
-        const float2 xj = __ldg(F.x + j), paj = B.pa[j];
-        const Geo e = geo(xi.x, xi.y, xj.x, xj.y, P.inv_h);
-        const float gs = kGS(e.q, P.c_s);
-        const float f = dt * dt * B.aact[j];
-        ks += f * ((pai.x - paj.x) * e.ex + (pai.y - paj.y) * e.ey) * gs;
+        const float4 rj = __ldg(B.rec_a + j);
+        const float dx = xi.x - rj.x, dy = xi.y - rj.y;
+        ks += __ldg(B.fdt + j) * ((pai.x - rj.z) * dx + (pai.y - rj.w) * dy) * spiky_gd(dx * dx + dy * dy, P);
       }
       if (walls) {
         float wks = 0.f;
@@ -313,6 +335,8 @@ __global__ void __launch_bounds__(256) k_dfsph_solve(FluidView F, WallView W, co
       if (density) pn = fmaxf(pn, 0.f);
       if (!isfinite(pn)) flag(status, SPH_FLAG_NONFINITE);
       B.p[i] = pn;
+      const float ri = B.rho[i] * P.rho0;
+      B.rec_p[i].w = pn / (ri * ri);
       local += (double)fmaxf(r, -thr_err);
     }
     if (walls) {
@@ -500,7 +524,8 @@ __global__ void k_dt_final(int nparts, const float* __restrict__ part, float h, 
 
 using namespace sph;
 
-static DfsphBufs to_bufs(const sph_dfsph_buffers* b) {
+// n: the fluid count, which places the pair records inside b->records.
+static DfsphBufs to_bufs(const sph_dfsph_buffers* b, int64_t n = 0) {
   DfsphBufs B;
   B.rho = b->rho;
   B.vol = b->volume;
@@ -521,6 +546,9 @@ static DfsphBufs to_bufs(const sph_dfsph_buffers* b) {
   B.partials = b->partials;
   B.errors = b->errors;
   B.iters = b->iters;
+  B.rec_p = b->records ? reinterpret_cast<float4*>(b->records) : nullptr;
+  B.rec_a = B.rec_p ? B.rec_p + n : nullptr;
+  B.fdt = B.rec_p ? b->records + 8 * n : nullptr;
   return B;
 }
 
@@ -567,10 +595,12 @@ sph_status_t sph_dfsph_solve(const sph_fluid_view* fluid, const sph_wall_view* w
   const int n = (int)fluid->n;
   if (n == 0) return SPH_OK;
   cudaStream_t st = as_stream(stream);
+  SPH_REQUIRE(bufs->records && (reinterpret_cast<uintptr_t>(bufs->records) & 15) == 0,
+              "dfsph_solve: records must be a 16-byte aligned array of 9 n floats");
   FluidView F = to_fluid(fluid);
   WallView W = to_walls(walls);
   SphParams P = to_params(params);
-  DfsphBufs B = to_bufs(bufs);
+  DfsphBufs B = to_bufs(bufs, n);
   k_dfsph_vstar<<<grid_for(n, 256), 256, 0, st>>>(n, F.v, reinterpret_cast<const float2*>(acc_in), dt, B.vstar);
   k_dfsph_prepare<<<grid_for(n, 128), 128, 0, st>>>(F, W, grid, P, B, dt, density);
   if (density && W.n > 0) k_dfsph_wall_prepare<<<grid_for(W.n, 128), 128, 0, st>>>(F, W, grid, P, B, dt);

@@ -53,7 +53,7 @@ class DfsphBuffersC(ctypes.Structure):
     _fields_ = [(k, ctypes.c_void_p) for k in (
         "rho", "volume", "actual_area", "vstar", "alpha", "source", "pressure", "pred_accel", "residual", "wall_rho",
         "wall_actual_area", "wall_alpha", "wall_source", "wall_pressure", "wall_residual", "wall_density_term",
-        "partials", "errors", "iters")]
+        "partials", "errors", "iters", "records")]
 
 
 
@@ -299,7 +299,7 @@ class Simulation:
              "wall_alpha": g("walpha", nb), "wall_source": g("wsrc", nb), "wall_pressure": g("wp", nb),
              "wall_residual": g("wres", nb), "wall_density_term": self.wall_term,
              "partials": g("partials", int(self.lib.sph_dfsph_partials_count()), torch.float64),
-             "errors": g("errors", maxit), "iters": g("iters", 1, torch.int32)}
+             "errors": g("errors", maxit), "iters": g("iters", 1, torch.int32), "records": g("records", 9 * n)}
         self.dfsph_arrays = b
         return DfsphBuffersC(*[N.ptr(b[k]) for k, _ in DfsphBuffersC._fields_])
 
