@@ -225,6 +225,22 @@ sph_status_t sph_nl_fill(const float* xy, const float* sorted_support, int64_t n
                          const int32_t* cell_start, const sph_grid* grid, int32_t cell_capacity,
                          int32_t search_radius, const int32_t* offsets, int64_t pair_capacity,
                          int32_t* cols, int32_t* status, void* stream);
+/* The same two passes with one candidate test per pair: sph_nl_count_segments tests the
+ * cell rows once, in segments of 32 candidates, and keeps each particle's accepted-candidate
+ * bit masks (at most 8 segments; more: its rows are scanned again by the fill) in
+ * seg_scratch (sph_nl_segments_scratch_bytes(n) bytes) besides counts and rho;
+ * sph_nl_fill_segments expands them into the CSR columns.  Same counts, rho, columns and
+ * order as sph_nl_count / sph_nl_fill. */
+size_t sph_nl_segments_scratch_bytes(int64_t n);
+sph_status_t sph_nl_count_segments(const float* xy, const float* sorted_support, const float* sorted_area, int64_t n,
+                                   const uint32_t* sorted_keys, const int32_t* cell_start, const sph_grid* grid,
+                                   int32_t cell_capacity, int32_t search_radius, float kernel_support,
+                                   int32_t* counts, float* rho, void* seg_scratch, size_t seg_bytes, void* stream);
+sph_status_t sph_nl_fill_segments(const float* xy, const float* sorted_support, int64_t n,
+                                  const uint32_t* sorted_keys, const int32_t* cell_start, const sph_grid* grid,
+                                  int32_t cell_capacity, int32_t search_radius, const int32_t* offsets,
+                                  int64_t pair_capacity, int32_t* cols, int32_t* status, const void* seg_scratch,
+                                  size_t seg_bytes, void* stream);
 /* out[order[s]] = in[s]: a sorted-order field back to original particle order. */
 sph_status_t sph_scatter_f32(const uint32_t* order, const float* in, int64_t n, float* out, void* stream);
 /* Materialise the reference's fluidNeighbors / fluidDistances / fluidRadialDistances

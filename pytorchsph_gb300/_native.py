@@ -46,6 +46,9 @@ SIGNATURES = {
     "sph_hash_map_build": (_I32, [_P, _I64, _I32, _I32, _P, _P, _P, _P, _P, _P, _SZ, _P]),
     "sph_nl_count": (_I32, [_P, _P, _P, _I64, _P, _P, _P, _I32, _I32, _F32, _P, _P, _P]),
     "sph_nl_fill": (_I32, [_P, _P, _I64, _P, _P, _P, _I32, _I32, _P, _I64, _P, _P, _P]),
+    "sph_nl_segments_scratch_bytes": (_SZ, [_I64]),
+    "sph_nl_count_segments": (_I32, [_P, _P, _P, _I64, _P, _P, _P, _I32, _I32, _F32, _P, _P, _P, _SZ, _P]),
+    "sph_nl_fill_segments": (_I32, [_P, _P, _I64, _P, _P, _P, _I32, _I32, _P, _I64, _P, _P, _P, _SZ, _P]),
     "sph_scatter_f32": (_I32, [_P, _P, _I64, _P, _P]),
     "sph_nl_to_coo": (_I32, [_P, _I64, _P, _P, _P, _P, _P, _F32, _F32, _P, _I64, _P, _P, _P]),
     "sph_scatter_counts": (_I32, [_P, _P, _I64, _P, _P]),

@@ -125,6 +125,94 @@ __global__ void __launch_bounds__(256) k_nl_fill(const float2* __restrict__ xy, 
   });
 }
 
+// One candidate pass for count, density and the CSR fill: particle s's cell rows are
+// tested in segments of 32 candidates (segment_mask); the non-empty segments are stored for
+// k_nl_fill_segments (nseg[s] = -1 when more than kMaxSegments), the count is their bit
+// count, and the density visits the set bits in order, the order of k_nl_count, so both
+// give the same sums.
+__global__ void __launch_bounds__(256) k_nl_segments(const float2* __restrict__ xy, const float* __restrict__ sh,
+                                                     const float* __restrict__ sa, int64_t n,
+                                                     const uint32_t* __restrict__ keys,
+                                                     const int32_t* __restrict__ cell_start,
+                                                     const sph_grid* __restrict__ gp, int32_t cap, int r,
+                                                     float inv_support, float c_w, int32_t* __restrict__ counts,
+                                                     float* __restrict__ rho, int32_t* __restrict__ nseg,
+                                                     int32_t* __restrict__ seg_start, uint32_t* __restrict__ seg_mask) {
+  const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  const sph_grid g = *gp;
+  const uint32_t key = keys[s];
+  int cnt = 0, k = 0;
+  float acc = 0.f;
+  if (grid_ok(g, cap) && key < (uint32_t)g.num_cells) {
+    const float2 pi = xy[s];
+    const float thr = grid_threshold(sh[s], g);
+    const int cx = (int)(key % (uint32_t)g.cells_x), cy = (int)(key / (uint32_t)g.cells_x);
+    const int x0 = max(cx - r, 0), x1 = min(cx + r, g.cells_x - 1);
+    const int y0 = max(cy - r, 0), y1 = min(cy + r, g.cells_y - 1);
+    for (int yy = y0; yy <= y1 && x0 <= x1; ++yy) {
+      const int row = yy * g.cells_x;
+      const int b = __ldg(cell_start + row + x0), e = __ldg(cell_start + row + x1 + 1);
+      for (int c = b; c < e; c += 32) {
+        uint32_t w = segment_mask(xy, c, e, pi.x, pi.y, thr);
+        if (w == 0) continue;
+        if (k < kMaxSegments) {
+          seg_start[(int64_t)k * n + s] = c;
+          seg_mask[(int64_t)k * n + s] = w;
+        }
+        ++k;
+        cnt += __popc(w);
+        while (rho && w) {
+          const int j = c - 1 + __ffs(w);
+          w &= w - 1;
+          const float2 pj = __ldg(xy + j);
+          acc += wendland(__fsqrt_rn(dist2_ref(pi.x, pi.y, pj.x, pj.y)) * inv_support, c_w) * __ldg(sa + j);
+        }
+      }
+    }
+  }
+  counts[s] = cnt;
+  if (rho) rho[s] = acc;
+  nseg[s] = k <= kMaxSegments ? k : -1;
+}
+
+// The CSR columns from the stored segments (no pair tests; the cell rows are scanned again
+// only for a particle whose segments did not fit).
+__global__ void __launch_bounds__(256) k_nl_fill_segments(const float2* __restrict__ xy,
+                                                          const float* __restrict__ sh, int64_t n,
+                                                          const uint32_t* __restrict__ keys,
+                                                          const int32_t* __restrict__ cell_start,
+                                                          const sph_grid* __restrict__ gp, int32_t cap, int r,
+                                                          const int32_t* __restrict__ offsets, int64_t pair_capacity,
+                                                          int32_t* __restrict__ cols, int32_t* status,
+                                                          const int32_t* __restrict__ nseg,
+                                                          const int32_t* __restrict__ seg_start,
+                                                          const uint32_t* __restrict__ seg_mask) {
+  const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const sph_grid g = *gp;
+  const uint32_t key = s < n ? keys[s] : 0xffffffffu;
+  const bool active = s < n && grid_ok(g, cap) && key < (uint32_t)g.num_cells;
+  const int ns = active ? nseg[s] : 0;
+  staged_fill(s, n, active, offsets, pair_capacity, cols, status, [&](auto&& emit) {
+    if (ns < 0 || ns > kMaxSegments) {
+      const float2 pi = xy[s];
+      const int cx = (int)(key % (uint32_t)g.cells_x), cy = (int)(key / (uint32_t)g.cells_x);
+      scan_candidates(xy, cell_start, g, r, cx, cy, pi.x, pi.y, grid_threshold(sh[s], g),
+                      [&](int j, float) { emit(j); });
+      return;
+    }
+    for (int k = 0; k < ns; ++k) {
+      const int c = seg_start[(int64_t)k * n + s];
+      uint32_t w = clip_segment(seg_mask[(int64_t)k * n + s], c, (int)n);
+      while (w) {
+        const int j = c - 1 + __ffs(w);
+        w &= w - 1;
+        emit(j);
+      }
+    }
+  });
+}
+
 // Query points (any order, e.g. wall or ghost particles) against the sorted grid, with
 // the query's own support in the predicate (dx = x_query - x_j): the pair set of
 // buildNeighborListUnsortedPerParticle, cppSrc/neighSearch.cpp:261-331.
@@ -301,6 +389,64 @@ sph_status_t sph_nl_count(const float* xy, const float* sorted_support, const fl
                                                                sorted_area, n, sorted_keys, cell_start, grid,
                                                                cell_capacity, search_radius, inv, cw, counts, rho);
   SPH_CHECK_LAUNCH("nl_count");
+  return SPH_OK;
+}
+
+size_t sph_nl_segments_scratch_bytes(int64_t n) {
+  return (size_t)(n > 0 ? n : 0) * (kMaxSegments * (sizeof(int32_t) + sizeof(uint32_t)) + sizeof(int32_t)) + 256;
+}
+
+// nseg [n], seg_start [kMaxSegments n], seg_mask [kMaxSegments n] inside the scratch.
+static bool segments_from_scratch(void* scratch, size_t bytes, int64_t n, int32_t** nseg, int32_t** start,
+                                  uint32_t** mask) {
+  if (!scratch || bytes < sph_nl_segments_scratch_bytes(n)) return false;
+  const uintptr_t p = (reinterpret_cast<uintptr_t>(scratch) + 15) & ~(uintptr_t)15;
+  *mask = reinterpret_cast<uint32_t*>(p);
+  *start = reinterpret_cast<int32_t*>(*mask + (size_t)kMaxSegments * n);
+  *nseg = *start + (size_t)kMaxSegments * n;
+  return true;
+}
+
+sph_status_t sph_nl_count_segments(const float* xy, const float* sorted_support, const float* sorted_area, int64_t n,
+                                   const uint32_t* sorted_keys, const int32_t* cell_start, const sph_grid* grid,
+                                   int32_t cell_capacity, int32_t search_radius, float kernel_support,
+                                   int32_t* counts, float* rho, void* seg_scratch, size_t seg_bytes, void* stream) {
+  SPH_REQUIRE(n >= 0 && n < ((int64_t)1 << 31) && xy && sorted_support && sorted_keys && cell_start && grid &&
+                  counts && search_radius >= 0,
+              "nl_count_segments: bad arguments");
+  SPH_REQUIRE(!rho || (kernel_support > 0.f && sorted_area),
+              "nl_count_segments: density needs kernel_support > 0 and areas");
+  int32_t *nseg, *start;
+  uint32_t* mask;
+  SPH_REQUIRE(segments_from_scratch(seg_scratch, seg_bytes, n, &nseg, &start, &mask),
+              "nl_count_segments: scratch smaller than sph_nl_segments_scratch_bytes(n)");
+  if (n == 0) return SPH_OK;
+  float inv = rho ? 1.0f / kernel_support : 0.f;
+  float cw = rho ? (float)(7.0 / 3.14159265358979323846) / (kernel_support * kernel_support) : 0.f;
+  k_nl_segments<<<grid_for(n, 256), 256, 0, as_stream(stream)>>>(
+      reinterpret_cast<const float2*>(xy), sorted_support, sorted_area, n, sorted_keys, cell_start, grid,
+      cell_capacity, search_radius, inv, cw, counts, rho, nseg, start, mask);
+  SPH_CHECK_LAUNCH("nl_count_segments");
+  return SPH_OK;
+}
+
+sph_status_t sph_nl_fill_segments(const float* xy, const float* sorted_support, int64_t n,
+                                  const uint32_t* sorted_keys, const int32_t* cell_start, const sph_grid* grid,
+                                  int32_t cell_capacity, int32_t search_radius, const int32_t* offsets,
+                                  int64_t pair_capacity, int32_t* cols, int32_t* status, const void* seg_scratch,
+                                  size_t seg_bytes, void* stream) {
+  SPH_REQUIRE(n >= 0 && n < ((int64_t)1 << 31) && xy && sorted_support && sorted_keys && cell_start && grid &&
+                  offsets && cols,
+              "nl_fill_segments: bad arguments");
+  int32_t *nseg, *start;
+  uint32_t* mask;
+  SPH_REQUIRE(segments_from_scratch(const_cast<void*>(seg_scratch), seg_bytes, n, &nseg, &start, &mask),
+              "nl_fill_segments: scratch smaller than sph_nl_segments_scratch_bytes(n)");
+  if (n == 0) return SPH_OK;
+  k_nl_fill_segments<<<grid_for(n, 256), 256, 0, as_stream(stream)>>>(
+      reinterpret_cast<const float2*>(xy), sorted_support, n, sorted_keys, cell_start, grid, cell_capacity,
+      search_radius, offsets, pair_capacity, cols, status, nseg, start, mask);
+  SPH_CHECK_LAUNCH("nl_fill_segments");
   return SPH_OK;
 }
 

@@ -142,19 +142,6 @@ __device__ __forceinline__ PairG pair_g(float xi, float yi, float xj, float yj, 
 // (nseg[i] = -1 when there are more; the force passes then test its cell rows
 // themselves).  A force pass holds one segment and the next one, loaded ahead, so moving
 // on to the next segment costs a lane a register move.
-constexpr int kMaxSegments = 8;
-
-__device__ __forceinline__ uint32_t segment_mask(const float2* __restrict__ x, int c, int e, float xi, float yi,
-                                                 float thr) {
-  const int len = min(e - c, 32);
-  uint32_t m = 0;
-  for (int t = 0; t < len; ++t) {
-    const float2 pj = __ldg(x + c + t);
-    m |= (uint32_t)(dist2_ref(xi, yi, pj.x, pj.y) <= thr) << t;
-  }
-  return m;
-}
-
 // Every row of the window, tested here (any r); with kTpp lanes per particle, lane `sub`
 // takes rows y0 + sub, y0 + sub + kTpp, ...
 template <int kTpp = 1, typename Fn>
@@ -206,13 +193,6 @@ __device__ __forceinline__ void segments_body(int i, const FluidView& F, const s
     }
   }
   nseg[i] = k <= kMaxSegments ? k : -1;
-}
-
-// The bits of a stored segment that name a particle: none for a start outside [0, n),
-// none at index n or past it.
-__device__ __forceinline__ uint32_t clip_segment(uint32_t w, int b, int n) {
-  if ((unsigned)b >= (unsigned)n) return 0;
-  return n - b < 32 ? w & ((1u << (n - b)) - 1) : w;
 }
 
 // The pairs of particle i from its segment list (its cell rows when the list overflowed).

@@ -241,6 +241,30 @@ __device__ __forceinline__ void for_each_wall(const WallView& W, const sph_grid&
   }
 }
 
+// ---------------------------------------------------------------- candidate segments
+// The candidates of a particle in one cell row are a contiguous sorted range; it is tested
+// in segments of 32 candidates into bit masks (bit t: candidate c + t passes the pair test),
+// and a particle keeps its non-empty segments, at most kMaxSegments, as (start, mask) pairs.
+constexpr int kMaxSegments = 8;
+
+__device__ __forceinline__ uint32_t segment_mask(const float2* __restrict__ x, int c, int e, float xi, float yi,
+                                                 float thr) {
+  const int len = min(e - c, 32);
+  uint32_t m = 0;
+  for (int t = 0; t < len; ++t) {
+    const float2 pj = __ldg(x + c + t);
+    m |= (uint32_t)(dist2_ref(xi, yi, pj.x, pj.y) <= thr) << t;
+  }
+  return m;
+}
+
+// The bits of a stored segment that name a particle: none for a start outside [0, n),
+// none at index n or past it.
+__device__ __forceinline__ uint32_t clip_segment(uint32_t w, int b, int n) {
+  if ((unsigned)b >= (unsigned)n) return 0;
+  return n - b < 32 ? w & ((1u << (n - b)) - 1) : w;
+}
+
 struct FluidView {
   const float2* x;
   const float2* v;

@@ -166,9 +166,12 @@ class GridSearch:
     """Hashed-grid neighbor search with CSR output, reusing its device workspace.
 
     sort = "counting" (one pass, the digit is the whole cell key) or "radix" (LSD radix
-    with `digit_bits` per pass); both give the (key, index) order of a stable sort."""
+    with `digit_bits` per pass); both give the (key, index) order of a stable sort.
+    segments = True: the count pass keeps each particle's accepted candidates as bit masks
+    and the fill expands them (one pair test per candidate instead of two); False: the fill
+    tests the candidates again.  Both give the same CSR."""
 
-    def __init__(self, device=None, sort: str = "counting", digit_bits: int = 8):
+    def __init__(self, device=None, sort: str = "counting", digit_bits: int = 8, segments: bool = True):
         if device is None:
             device = torch.device("cuda", torch.cuda.current_device())
         self.device = torch.device(device)
@@ -177,6 +180,7 @@ class GridSearch:
             raise ValueError(sort)
         self.sort = sort
         self.digit_bits = int(digit_bits)
+        self.segments = bool(segments)
 
     def grid(self, pos, support, min_coord=None, max_coord=None, cell_capacity=MAX_CELLS):
         """Compute the search grid on the device; returns the device grid bytes."""
@@ -261,8 +265,14 @@ class GridSearch:
         ks = float(kernel_support) if kernel_support is not None else 0.0
         if density and (ks <= 0 or area is None):
             raise N.SPHError("neighbor search: density needs kernel_support > 0 and areas")
-        N.call("sph_nl_count", N.ptr(xy), N.ptr(sh), N.ptr(sa), n, N.ptr(skeys), N.ptr(cell_start), N.ptr(grid), cap,
-               int(search_radius), ks, N.ptr(counts), N.ptr(rho), st)
+        if self.segments:   # one candidate test per pair: the fill expands the stored masks
+            seg = ws.bytes("segments", lib.sph_nl_segments_scratch_bytes(n))
+            N.call("sph_nl_count_segments", N.ptr(xy), N.ptr(sh), N.ptr(sa), n, N.ptr(skeys), N.ptr(cell_start),
+                   N.ptr(grid), cap, int(search_radius), ks, N.ptr(counts), N.ptr(rho), N.ptr(seg), seg.numel() * 8,
+                   st)
+        else:
+            N.call("sph_nl_count", N.ptr(xy), N.ptr(sh), N.ptr(sa), n, N.ptr(skeys), N.ptr(cell_start), N.ptr(grid),
+                   cap, int(search_radius), ks, N.ptr(counts), N.ptr(rho), st)
         mark("count")
         offsets = ws.get("offsets", n + 1)
         sc = ws.bytes("scan_scratch", lib.sph_scan_scratch_bytes(n))
@@ -271,8 +281,13 @@ class GridSearch:
         if pair_capacity is None:
             pair_capacity = int(offsets[n].item())
         cols = ws.get("cols", pair_capacity)
-        N.call("sph_nl_fill", N.ptr(xy), N.ptr(sh), n, N.ptr(skeys), N.ptr(cell_start), N.ptr(grid), cap,
-               int(search_radius), N.ptr(offsets), int(pair_capacity), N.ptr(cols), N.ptr(status), st)
+        if self.segments:
+            N.call("sph_nl_fill_segments", N.ptr(xy), N.ptr(sh), n, N.ptr(skeys), N.ptr(cell_start), N.ptr(grid), cap,
+                   int(search_radius), N.ptr(offsets), int(pair_capacity), N.ptr(cols), N.ptr(status), N.ptr(seg),
+                   seg.numel() * 8, st)
+        else:
+            N.call("sph_nl_fill", N.ptr(xy), N.ptr(sh), n, N.ptr(skeys), N.ptr(cell_start), N.ptr(grid), cap,
+                   int(search_radius), N.ptr(offsets), int(pair_capacity), N.ptr(cols), N.ptr(status), st)
         mark("fill")
         res = CSRNeighbors(n=n, order=order, keys=skeys, xy=xy, sh=sh, sa=sa, cell_start=cell_start, counts=counts,
                            offsets=offsets, cols=cols, rho=rho, grid=grid, status=status, cell_capacity=cap,

@@ -193,6 +193,27 @@ def test_sort_variants_agree(cuda):
     assert torch.equal(a.cols[:a.num_pairs], b.cols[:b.num_pairs])
 
 
+def test_segment_fill_equals_two_pass_fill(cuda):
+    """The count pass that keeps its accepted-candidate masks and the fill that expands them
+    give the same counts, density and CSR as the two-pass search that tests every candidate
+    twice, including particles with more than 8 segments (dense blob: up to ~300 neighbors,
+    so those rows are scanned again by the fill)."""
+    from pytorchsph_gb300.search import GridSearch
+    from pytorchsph_gb300 import workloads
+    dev = torch.device("cuda")
+    n = 1 << 16
+    pos = torch.from_numpy(workloads.gaussian_uniform_mix(n, 0.05, (0.5, 0.5), 3)).to(dev)
+    h = torch.full((n,), 0.012, device=dev)
+    area = torch.full((n,), 1.0 / n, device=dev)
+    kw = dict(kernel_support=0.012, min_coord=[0, 0], max_coord=[1, 1])
+    a = GridSearch(dev, segments=True).run(pos, h, area, **kw)
+    b = GridSearch(dev, segments=False).run(pos, h, area, **kw)
+    assert int(a.counts.max()) > 8 * 32
+    assert torch.equal(a.counts, b.counts) and torch.equal(a.offsets, b.offsets)
+    assert torch.equal(a.cols[:a.num_pairs], b.cols[:b.num_pairs])
+    assert torch.equal(a.rho, b.rho)
+
+
 def test_counting_sort_large_cells(cuda):
     """Cells above the per-thread sort limit (48) and the block limit (2048): the pair count
     stays exact, cells up to 2048 keep (key, index) order, bigger ones flag CELL_ORDER."""
