@@ -127,9 +127,10 @@ __global__ void __launch_bounds__(256) k_nl_fill(const float2* __restrict__ xy, 
 
 // One candidate pass for count, density and the CSR fill: particle s's cell rows are
 // tested in segments of 32 candidates (segment_mask); the non-empty segments are stored for
-// k_nl_fill_segments (nseg[s] = -1 when more than kMaxSegments), the count is their bit
-// count, and the density visits the set bits in order, the order of k_nl_count, so both
-// give the same sums.
+// k_nl_fill_segments, the count is their bit count, and the density visits the set bits in
+// order, the order of k_nl_count, so both give the same sums.  A particle with more than
+// kMaxSegments segments gets nseg[s] = -1 and goes on the dense list, whose rows
+// k_nl_fill_dense writes one warp per particle.
 __global__ void __launch_bounds__(256) k_nl_segments(const float2* __restrict__ xy, const float* __restrict__ sh,
                                                      const float* __restrict__ sa, int64_t n,
                                                      const uint32_t* __restrict__ keys,
@@ -137,7 +138,8 @@ __global__ void __launch_bounds__(256) k_nl_segments(const float2* __restrict__ 
                                                      const sph_grid* __restrict__ gp, int32_t cap, int r,
                                                      float inv_support, float c_w, int32_t* __restrict__ counts,
                                                      float* __restrict__ rho, int32_t* __restrict__ nseg,
-                                                     int32_t* __restrict__ seg_start, uint32_t* __restrict__ seg_mask) {
+                                                     int32_t* __restrict__ seg_start, uint32_t* __restrict__ seg_mask,
+                                                     int32_t* __restrict__ dense_list, int32_t* __restrict__ dense_count) {
   const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= n) return;
   const sph_grid g = *gp;
@@ -174,10 +176,12 @@ __global__ void __launch_bounds__(256) k_nl_segments(const float2* __restrict__ 
   counts[s] = cnt;
   if (rho) rho[s] = acc;
   nseg[s] = k <= kMaxSegments ? k : -1;
+  if (k > kMaxSegments) dense_list[atomicAdd(dense_count, 1)] = (int32_t)s;
 }
 
-// The CSR columns from the stored segments (no pair tests; the cell rows are scanned again
-// only for a particle whose segments did not fit).
+// The CSR columns from the stored segments (no pair tests).  Rows of the dense list are left
+// to k_nl_fill_dense, which runs after this kernel (a staged block may copy placeholder
+// entries over them first).
 __global__ void __launch_bounds__(256) k_nl_fill_segments(const float2* __restrict__ xy,
                                                           const float* __restrict__ sh, int64_t n,
                                                           const uint32_t* __restrict__ keys,
@@ -194,13 +198,7 @@ __global__ void __launch_bounds__(256) k_nl_fill_segments(const float2* __restri
   const bool active = s < n && grid_ok(g, cap) && key < (uint32_t)g.num_cells;
   const int ns = active ? nseg[s] : 0;
   staged_fill(s, n, active, offsets, pair_capacity, cols, status, [&](auto&& emit) {
-    if (ns < 0 || ns > kMaxSegments) {
-      const float2 pi = xy[s];
-      const int cx = (int)(key % (uint32_t)g.cells_x), cy = (int)(key / (uint32_t)g.cells_x);
-      scan_candidates(xy, cell_start, g, r, cx, cy, pi.x, pi.y, grid_threshold(sh[s], g),
-                      [&](int j, float) { emit(j); });
-      return;
-    }
+    if (ns < 0 || ns > kMaxSegments) return;   // a dense row
     for (int k = 0; k < ns; ++k) {
       const int c = seg_start[(int64_t)k * n + s];
       uint32_t w = clip_segment(seg_mask[(int64_t)k * n + s], c, (int)n);
@@ -211,6 +209,55 @@ __global__ void __launch_bounds__(256) k_nl_fill_segments(const float2* __restri
       }
     }
   });
+}
+
+// The rows of the dense list, one warp per particle: each sweep tests 32 candidates of a
+// cell row at once, and the accepted ones are written in order through a ballot, so the row
+// goes out in coalesced stores.  A row that does not fit the column buffer is skipped with
+// SPH_FLAG_PAIR_CAPACITY set.
+__global__ void __launch_bounds__(128) k_nl_fill_dense(const float2* __restrict__ xy, const float* __restrict__ sh,
+                                                       const uint32_t* __restrict__ keys,
+                                                       const int32_t* __restrict__ cell_start,
+                                                       const sph_grid* __restrict__ gp, int32_t cap, int r,
+                                                       const int32_t* __restrict__ offsets, int64_t pair_capacity,
+                                                       int32_t* __restrict__ cols, int32_t* status,
+                                                       const int32_t* __restrict__ dense_list,
+                                                       const int32_t* __restrict__ dense_count) {
+  const int lane = threadIdx.x & 31;
+  const int warps = gridDim.x * (blockDim.x >> 5);
+  const int nd = *dense_count;
+  const sph_grid g = *gp;
+  for (int q = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); q < nd; q += warps) {
+    const int s = dense_list[q];
+    int o = offsets[s];
+    const int end = offsets[s + 1];
+    if ((int64_t)end > pair_capacity || o < 0) {
+      if (lane == 0) flag(status, SPH_FLAG_PAIR_CAPACITY);
+      continue;
+    }
+    const uint32_t key = keys[s];
+    const float2 pi = xy[s];
+    const float thr = grid_threshold(sh[s], g);
+    const int cx = (int)(key % (uint32_t)g.cells_x), cy = (int)(key / (uint32_t)g.cells_x);
+    const int x0 = max(cx - r, 0), x1 = min(cx + r, g.cells_x - 1);
+    const int y0 = max(cy - r, 0), y1 = min(cy + r, g.cells_y - 1);
+    for (int yy = y0; yy <= y1 && x0 <= x1; ++yy) {
+      const int row = yy * g.cells_x;
+      const int b = __ldg(cell_start + row + x0), e = __ldg(cell_start + row + x1 + 1);
+      for (int c = b; c < e; c += 32) {
+        const int j = c + lane;
+        bool hit = false;
+        if (j < e) {
+          const float2 pj = __ldg(xy + j);
+          hit = dist2_ref(pi.x, pi.y, pj.x, pj.y) <= thr;
+        }
+        const uint32_t m = __ballot_sync(0xffffffffu, hit);
+        const int pos = o + __popc(m & ((1u << lane) - 1u));
+        if (hit && pos < end) cols[pos] = j;
+        o += __popc(m);
+      }
+    }
+  }
 }
 
 // Query points (any order, e.g. wall or ghost particles) against the sorted grid, with
@@ -393,17 +440,21 @@ sph_status_t sph_nl_count(const float* xy, const float* sorted_support, const fl
 }
 
 size_t sph_nl_segments_scratch_bytes(int64_t n) {
-  return (size_t)(n > 0 ? n : 0) * (kMaxSegments * (sizeof(int32_t) + sizeof(uint32_t)) + sizeof(int32_t)) + 256;
+  return (size_t)(n > 0 ? n : 0) * (kMaxSegments * (sizeof(int32_t) + sizeof(uint32_t)) + 2 * sizeof(int32_t)) +
+         256 + 16;
 }
 
-// nseg [n], seg_start [kMaxSegments n], seg_mask [kMaxSegments n] inside the scratch.
+// seg_mask [kMaxSegments n], seg_start [kMaxSegments n], nseg [n], the dense list [n] and its
+// count inside the scratch.
 static bool segments_from_scratch(void* scratch, size_t bytes, int64_t n, int32_t** nseg, int32_t** start,
-                                  uint32_t** mask) {
+                                  uint32_t** mask, int32_t** dense_list, int32_t** dense_count) {
   if (!scratch || bytes < sph_nl_segments_scratch_bytes(n)) return false;
   const uintptr_t p = (reinterpret_cast<uintptr_t>(scratch) + 15) & ~(uintptr_t)15;
   *mask = reinterpret_cast<uint32_t*>(p);
   *start = reinterpret_cast<int32_t*>(*mask + (size_t)kMaxSegments * n);
   *nseg = *start + (size_t)kMaxSegments * n;
+  *dense_list = *nseg + n;
+  *dense_count = *dense_list + n;
   return true;
 }
 
@@ -416,16 +467,17 @@ sph_status_t sph_nl_count_segments(const float* xy, const float* sorted_support,
               "nl_count_segments: bad arguments");
   SPH_REQUIRE(!rho || (kernel_support > 0.f && sorted_area),
               "nl_count_segments: density needs kernel_support > 0 and areas");
-  int32_t *nseg, *start;
+  int32_t *nseg, *start, *dense_list, *dense_count;
   uint32_t* mask;
-  SPH_REQUIRE(segments_from_scratch(seg_scratch, seg_bytes, n, &nseg, &start, &mask),
+  SPH_REQUIRE(segments_from_scratch(seg_scratch, seg_bytes, n, &nseg, &start, &mask, &dense_list, &dense_count),
               "nl_count_segments: scratch smaller than sph_nl_segments_scratch_bytes(n)");
   if (n == 0) return SPH_OK;
+  cudaMemsetAsync(dense_count, 0, sizeof(int32_t), as_stream(stream));
   float inv = rho ? 1.0f / kernel_support : 0.f;
   float cw = rho ? (float)(7.0 / 3.14159265358979323846) / (kernel_support * kernel_support) : 0.f;
   k_nl_segments<<<grid_for(n, 256), 256, 0, as_stream(stream)>>>(
       reinterpret_cast<const float2*>(xy), sorted_support, sorted_area, n, sorted_keys, cell_start, grid,
-      cell_capacity, search_radius, inv, cw, counts, rho, nseg, start, mask);
+      cell_capacity, search_radius, inv, cw, counts, rho, nseg, start, mask, dense_list, dense_count);
   SPH_CHECK_LAUNCH("nl_count_segments");
   return SPH_OK;
 }
@@ -438,14 +490,19 @@ sph_status_t sph_nl_fill_segments(const float* xy, const float* sorted_support, 
   SPH_REQUIRE(n >= 0 && n < ((int64_t)1 << 31) && xy && sorted_support && sorted_keys && cell_start && grid &&
                   offsets && cols,
               "nl_fill_segments: bad arguments");
-  int32_t *nseg, *start;
+  int32_t *nseg, *start, *dense_list, *dense_count;
   uint32_t* mask;
-  SPH_REQUIRE(segments_from_scratch(const_cast<void*>(seg_scratch), seg_bytes, n, &nseg, &start, &mask),
+  SPH_REQUIRE(segments_from_scratch(const_cast<void*>(seg_scratch), seg_bytes, n, &nseg, &start, &mask,
+                                    &dense_list, &dense_count),
               "nl_fill_segments: scratch smaller than sph_nl_segments_scratch_bytes(n)");
   if (n == 0) return SPH_OK;
-  k_nl_fill_segments<<<grid_for(n, 256), 256, 0, as_stream(stream)>>>(
-      reinterpret_cast<const float2*>(xy), sorted_support, n, sorted_keys, cell_start, grid, cell_capacity,
-      search_radius, offsets, pair_capacity, cols, status, nseg, start, mask);
+  cudaStream_t st = as_stream(stream);
+  k_nl_fill_segments<<<grid_for(n, 256), 256, 0, st>>>(reinterpret_cast<const float2*>(xy), sorted_support, n,
+                                                       sorted_keys, cell_start, grid, cell_capacity, search_radius,
+                                                       offsets, pair_capacity, cols, status, nseg, start, mask);
+  k_nl_fill_dense<<<kNumSMs * 8, 128, 0, st>>>(reinterpret_cast<const float2*>(xy), sorted_support, sorted_keys,
+                                               cell_start, grid, cell_capacity, search_radius, offsets, pair_capacity,
+                                               cols, status, dense_list, dense_count);
   SPH_CHECK_LAUNCH("nl_fill_segments");
   return SPH_OK;
 }
