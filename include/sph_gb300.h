@@ -347,7 +347,8 @@ sph_status_t sph_batch_nl_fill(const float* xy, const float* sorted_support, int
  * SPH_FLAG_PAIR_CAPACITY is set in *status when the update runs (the fill overflowed),
  * the step is not applied: the outputs are the sorted inputs unchanged.  dpdt [n], acc
  * float2 [n] and grad_rho float2 [n] carry the renormalized scenes' first pass to their
- * diffusion pass (needed when any_renormalized); scratch as for sph_deltasph_forces.
+ * diffusion pass (needed when any_renormalized; grad_rho then holds <grad rho> V, the part
+ * of the deltaSPH diffusion that needs the neighbors); scratch as for sph_deltasph_forces.
  * With fluid->offsets and fluid->cols both NULL no neighbor list is needed: the records
  * launch also stores, per particle, the first candidate and a 64-bit accepted-candidate
  * mask of each of its three cell rows (search_radius 1; other radii test their cell rows

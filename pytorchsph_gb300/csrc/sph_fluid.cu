@@ -252,10 +252,16 @@ __device__ __forceinline__ float lane_sum(float v) {
 // viscosity) and, for the deltaSPH scheme, the renormalization matrix L_i and the density
 // gradient <grad rho>_i = -L_i^+ sum_j 2 (rho_j - rho_i) V_j gradW_ij (+ walls), all in one
 // sweep over the row: L_i^+ is applied to the summed vector once instead of to every term.
+// For the deltaSPH scheme the diffusion D_i = sum_j psi_ij . gradW_ij V_j, psi_ij =
+// 2 (rho_j - rho_i) x_ji / (|x_ji|^2 + eps) - (<grad rho>_i + <grad rho>_j), is split: pass 1
+// sums the parts it can, ddiff = 2 sum_j (rho_j - rho_i) (x_ji . gradW) V_j / (|x_ji|^2 + eps)
+// - <grad rho>_i . sum_j V_j gradW_ij, and the diffusion pass subtracts
+// sum_j (<grad rho>_j V_j) . gradW_ij, the only part that needs the neighbors' gradients.
 struct Pass1 {
   float dpdt, ax, ay;
   float4 L;        // renormalization matrix, fluid + walls
   float2 grad_rho;
+  float ddiff;     // deltaSPH: the pass-1 part of D_i
 };
 
 // Pairs from the segment lists S (kCells) instead of the CSR row.
@@ -280,7 +286,7 @@ __device__ __forceinline__ Pass1 pass1_body(int i, const FluidView& F, const flo
   const int scheme = kScheme >= 0 ? kScheme : P.diffusion;
   const bool renorm = scheme == 2;
   const float mu8 = 4.0f * (2.0f * rhoi * P.kinematic);   // 4 (mu_i + mu_j), both rho_i nu
-  float dp_f = 0.f, mog = 0.f;
+  float dp_f = 0.f, mog = 0.f, bx = 0.f, by = 0.f;   // b = sum_j V_j gradW_ij (deltaSPH)
   float pax = 0.f, pay = 0.f, vax = 0.f, vay = 0.f, lax = 0.f, lay = 0.f;
   float l00 = 0.f, l01 = 0.f, l11 = 0.f, gfx = 0.f, gfy = 0.f;
   auto fluid_pair = [&](int j) {
@@ -292,7 +298,8 @@ __device__ __forceinline__ Pass1 pass1_body(int i, const FluidView& F, const flo
     const float ir2 = __fdividef(1.0f, e.r2 + P.eps);
     const float rg = -e.gd * e.r2;                        // (x_j - x_i) . gradW
     dp_f -= e.gd * ud * mj;
-    if (scheme == 1) mog += (rhoj - rhoi) * ir2 * rg * Vj;   // x 2 after the sum
+    // MOG diffusion; for deltaSPH the first part of its diffusion (x 2 after the sum)
+    if (scheme == 1 || scheme == 2) mog += (rhoj - rhoi) * ir2 * rg * Vj;
     const float pf = fmaf(pi, Vj, pVj) * e.gd;            // (p_i + p_j) V_j gd
     pax += pf * e.dx;
     pay += pf * e.dy;
@@ -311,6 +318,8 @@ __device__ __forceinline__ Pass1 pass1_body(int i, const FluidView& F, const flo
       l00 -= tx * e.dx;
       l01 -= tx * e.dy;
       l11 -= ty * e.dy;
+      bx += tx;
+      by += ty;
       const float s = (rhoj - rhoi) * t;                  // x 2 after the sum
       gfx += s * e.dx;
       gfy += s * e.dy;
@@ -338,6 +347,8 @@ __device__ __forceinline__ Pass1 pass1_body(int i, const FluidView& F, const flo
     l11 = lane_sum<kTpp>(l11);
     gfx = lane_sum<kTpp>(gfx);
     gfy = lane_sum<kTpp>(gfy);
+    bx = lane_sum<kTpp>(bx);
+    by = lane_sum<kTpp>(by);
     if (sub != 0 || !live) return Pass1{};
   }
   float dp_w = 0.f, pwx = 0.f, pwy = 0.f, vwx = 0.f, vwy = 0.f;
@@ -404,34 +415,40 @@ __device__ __forceinline__ Pass1 pass1_body(int i, const FluidView& F, const flo
   gfx *= 2.0f;
   gfy *= 2.0f;
   o.grad_rho = make_float2(0.f, 0.f);
+  o.ddiff = 0.f;
   if (renorm) {
     const float4 Li = pinv2x2_fast(o.L.x, o.L.y, o.L.z, o.L.w);
     const float fx = Li.x * gfx + Li.y * gfy, fy = Li.z * gfx + Li.w * gfy;
     const float wx = Li.x * gwx + Li.y * gwy, wy = Li.z * gwx + Li.w * gwy;
     o.grad_rho = make_float2(-fx - wx, -fy - wy);
+    o.ddiff = 2.0f * mog - (o.grad_rho.x * bx + o.grad_rho.y * by);
   }
   return o;
 }
 
 // D_i = sum_j [2 (rho_j - rho_i)/(|x_ji|^2 + eps) x_ji - (<grad rho>_i + <grad rho>_j)] . gradW_ij V_j
 // (the deltaSPH density diffusion before its h delta c0 factor).
-// kCells: pairs from the segment lists instead of the CSR row.
-template <bool kCells, int kTpp = 1>
+// sum_j (<grad rho>_j V_j) . gradW_ij, the part of the deltaSPH diffusion that needs the
+// neighbors' gradients.  kHoldsGV: gbuf holds <grad rho> V (the batch's pass 1 stores it
+// so); otherwise it holds <grad rho> and V_j comes from the neighbor record (the same
+// product, so both give the same bits).  kCells: pairs from the segment lists instead of the
+// CSR row.
+template <bool kCells, int kTpp = 1, bool kHoldsGV = true>
 __device__ __forceinline__ float diffusion_sum(int i, const FluidView& F, const float4* __restrict__ qv,
-                                               const SphParams& P, const float2* __restrict__ grad_rho,
+                                               const SphParams& P, const float2* __restrict__ gbuf,
                                                const sph_grid& g, int coff, const Segments& S, int sub = 0,
                                                bool live = true) {
-  const float2 xi = F.x[i], gi = grad_rho[i];
-  const float rhoi = qv[i].x;
+  const float2 xi = F.x[i];
   float acc = 0.f;
   auto pair = [&](int j) {
-    const float2 xj = __ldg(F.x + j), gj = __ldg(grad_rho + j);
-    const float4 qj = __ldg(qv + j);
+    const float2 xj = __ldg(F.x + j);
+    float2 gv = __ldg(gbuf + j);
+    if constexpr (!kHoldsGV) {
+      const float Vj = __ldg(qv + j).y;
+      gv = make_float2(gv.x * Vj, gv.y * Vj);
+    }
     const PairG e = pair_g(xi.x, xi.y, xj.x, xj.y, P);
-    const float s = 2.0f * (qj.x - rhoi) * __fdividef(1.0f, e.r2 + P.eps);
-    // psi . gradW with psi = s (x_j - x_i) - (g_i + g_j) and gradW = gd d
-    const float pd = -s * e.r2 - ((gi.x + gj.x) * e.dx + (gi.y + gj.y) * e.dy);
-    acc += e.gd * pd * qj.y;
+    acc += (gv.x * e.dx + gv.y * e.dy) * e.gd;
   };
   if constexpr (kCells) {
     if (live) stored_pairs<kTpp>(i, F, g, coff, P.search_radius, S.nseg, S.start, S.mask, xi.x, xi.y, P.thr, pair,
@@ -481,7 +498,7 @@ __global__ void __launch_bounds__(128) k_dsph_pass1(FluidView F, const float4* _
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= F.n) return;
   const Pass1 o = pass1_body<false>(i, F, xv, qv, W, *gp, P, 0, Segments{});
-  dpdt[i] = o.dpdt;
+  dpdt[i] = P.diffusion == 2 ? o.dpdt + P.diff_k * o.ddiff : o.dpdt;
   acc[i] = make_float2(o.ax, o.ay);
   if (Lout) Lout[i] = o.L;
   if (grad_rho) grad_rho[i] = o.grad_rho;
@@ -491,7 +508,7 @@ __global__ void __launch_bounds__(128) k_dsph_diffusion(FluidView F, const float
                                                         const float2* __restrict__ grad_rho, float* __restrict__ dpdt) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= F.n) return;
-  dpdt[i] += P.diff_k * diffusion_sum<false>(i, F, qv, P, grad_rho, sph_grid{}, 0, Segments{});
+  dpdt[i] -= P.diff_k * diffusion_sum<false, 1, false>(i, F, qv, P, grad_rho, sph_grid{}, 0, Segments{});
 }
 
 __global__ void k_sie(int n, const float2* __restrict__ x, const float2* __restrict__ v,
@@ -571,9 +588,10 @@ __global__ void __launch_bounds__(128, 8) k_batch_pass1(FluidView F, const float
   const Pass1 o = pass1_body<kCells, kTpp, kScheme>(i, F, xv, qv, W, S.g, P, S.coff, seg, sub, kTpp == 1 || live);
   if (kTpp > 1 && (!live || sub != 0)) return;
   if ((kScheme >= 0 ? kScheme : P.diffusion) == 2) {
-    dpdt[i] = o.dpdt;
+    dpdt[i] = o.dpdt + P.diff_k * o.ddiff;
     acc[i] = make_float2(o.ax, o.ay);
-    grad_rho[i] = o.grad_rho;
+    const float Vi = qv[i].y;
+    grad_rho[i] = make_float2(o.grad_rho.x * Vi, o.grad_rho.y * Vi);   // <grad rho> V for the diffusion pass
     return;
   }
   batch_update(i, F, o.ax, o.ay, o.dpdt, S, xo, vo, ro, status);
@@ -606,7 +624,7 @@ __global__ void __launch_bounds__(128) k_batch_diffusion(FluidView F, const floa
   const SphParams P = S.P;   // the fields the loop reads, in registers
   const float sum = diffusion_sum<kCells, kTpp>(i, F, qv, P, grad_rho, S.g, S.coff, seg, sub, kTpp == 1 || act);
   if (kTpp > 1 && (!act || sub != 0)) return;
-  const float d = dpdt[i] + P.diff_k * sum;
+  const float d = dpdt[i] - P.diff_k * sum;
   const float2 a = acc[i];
   batch_update(i, F, a.x, a.y, d, S, xo, vo, ro, status);
 }
