@@ -331,7 +331,11 @@ class SceneBatch:
         return out
 
     # ------------------------------------------------------------------ one batch step
-    AUX = ("area", "sup", "sid", "uid")
+    @property
+    def AUX(self):
+        """The static per-particle arrays that follow the sort: the sorted supports only
+        matter to the CSR search; with pairs from the cell rows the scene's support is used."""
+        return ("area", "sup", "sid", "uid") if self.pairs == "csr" else ("area", "sid", "uid")
 
     def _aux(self, which: int) -> dict:
         return self.a if which == 0 else self.b
