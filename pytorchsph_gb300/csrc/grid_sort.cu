@@ -178,6 +178,14 @@ __global__ void __launch_bounds__(kRedThreads) k_grid_segments(const float2* __r
                        cell_capacity, status);
 }
 
+// counter[key] += 1 for every lane, one atomic per distinct key of the warp: particles come
+// nearly sorted from the previous step, so a warp's lanes share a few cells and their
+// atomics would otherwise serialize.
+__device__ __forceinline__ void warp_count(int32_t* __restrict__ counter, uint32_t key) {
+  const unsigned peers = __match_any_sync(__activemask(), key);
+  if ((int)(threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(counter + key, __popc(peers));
+}
+
 __global__ void k_cell_keys(const float2* __restrict__ pos, int64_t n, const sph_grid* __restrict__ gp,
                             int32_t cell_capacity, uint32_t* __restrict__ keys, uint32_t* __restrict__ vals,
                             int32_t* __restrict__ cell_count, int32_t* status) {
@@ -198,7 +206,7 @@ __global__ void k_cell_keys(const float2* __restrict__ pos, int64_t n, const sph
   }
   keys[i] = key;
   if (vals) vals[i] = (uint32_t)i;
-  if (cell_count) atomicAdd(cell_count + key, 1);
+  if (cell_count) warp_count(cell_count, key);
 }
 
 // Batch of scenes: key = coff_s + ix + cells_x_s * iy with scene s's own grid.  Scene s owns
@@ -227,17 +235,23 @@ __global__ void k_batch_cell_keys(const float2* __restrict__ pos, int64_t n, con
       flag(status, SPH_FLAG_OUT_OF_GRID);
   }
   keys[i] = key;
-  atomicAdd(cell_count + key, 1);
+  warp_count(cell_count, key);
 }
 
-// Counting-sort scatter: slot = cell_start[key] + (remaining count of the cell) - 1.
+// Counting-sort scatter: slot = cell_start[key] + (remaining count of the cell) - 1, one
+// atomic per distinct key of the warp (the lanes of a key take consecutive slots).
 // Decrementing the histogram leaves it all zero for the next sort.
 __global__ void k_count_scatter(const uint32_t* __restrict__ keys, int64_t n, const int32_t* __restrict__ cell_start,
                                 int32_t* __restrict__ cell_count, uint32_t* __restrict__ tmp) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  uint32_t k = keys[i];
-  int slot = cell_start[k] + atomicSub(cell_count + k, 1) - 1;
+  const uint32_t k = keys[i];
+  const unsigned peers = __match_any_sync(__activemask(), k);
+  const int lane = (int)(threadIdx.x & 31), leader = __ffs(peers) - 1;
+  int left = 0;
+  if (lane == leader) left = atomicSub(cell_count + k, __popc(peers));
+  left = __shfl_sync(peers, left, leader);
+  const int slot = cell_start[k] + left - 1 - __popc(peers & ((1u << lane) - 1u));
   tmp[slot] = (uint32_t)i;
 }
 
