@@ -142,6 +142,25 @@ def upload_scenes(specs, device):
         sp.dev = d
 
 
+def scene_order(lanes, schemes):
+    """Batch order of the scenes: grouped by (lanes per particle, diffusion scheme), each
+    group in the given order.  Returns order[k] = the input index of batch scene k."""
+    return sorted(range(len(lanes)), key=lambda k: (lanes[k], schemes[k]))
+
+
+def force_groups(p_off, kinds):
+    """Force-pass groups of a batch whose scene k (in batch order) holds the particles
+    [p_off[k], p_off[k+1]) and has kind (lanes per particle, scheme): one [begin, end, tpp,
+    scheme] per run of equal kinds, tiling [0, p_off[-1]); one default group for no scenes."""
+    groups = []
+    for k, kind in enumerate(kinds):
+        if k == 0 or kind != kinds[k - 1]:
+            groups.append([p_off[k], p_off[k + 1], *kind])
+        else:
+            groups[-1][1] = p_off[k + 1]
+    return groups or [[0, p_off[-1] if p_off else 0, 1, -1]]
+
+
 class SceneBatch:
     """A fixed set of scenes stepped together (deltaSPH, semi-implicit Euler).
 
@@ -174,7 +193,7 @@ class SceneBatch:
         lanes = [sp.tpp if pairs == "cells" else 1 for sp in specs]
         schemes = [DIFFUSION[sp.cfg.density_diffusion] for sp in specs]
         # scenes grouped by (lanes per particle, scheme), stable: _order[k] = the spec of batch scene k
-        self._order = sorted(range(len(specs)), key=lambda k: (lanes[k], schemes[k]))
+        self._order = scene_order(lanes, schemes)
         self._slot = [0] * len(specs)
         for k, e in enumerate(self._order):
             self._slot[e] = k
@@ -230,16 +249,7 @@ class SceneBatch:
                                          dtype=torch.int64, device=dev)
         self.n = self.p_off[-1]
         n = self.n
-        # force-pass groups: runs of scenes with the same (lanes per particle, scheme)
-        kind = [(lanes[e], schemes[e]) for e in self._order]
-        self.groups = []                      # (begin, end, tpp, scheme)
-        for k in range(S):
-            if k == 0 or kind[k] != kind[k - 1]:
-                self.groups.append([self.p_off[k], self.p_off[k + 1], *kind[k]])
-            else:
-                self.groups[-1][1] = self.p_off[k + 1]
-        if not self.groups:
-            self.groups = [[0, n, 1, -1]]
+        self.groups = force_groups(self.p_off, [(lanes[e], schemes[e]) for e in self._order])
         self._groups_c = (ForceGroupC * len(self.groups))(*[ForceGroupC(*g) for g in self.groups])
         # scene index and particle id of every particle; p_off_dev[sid] + uid is its slot in the
         # concatenation of the scenes in their own particle order
