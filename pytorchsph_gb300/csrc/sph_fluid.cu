@@ -144,7 +144,9 @@ __device__ __forceinline__ PairG pair_g(float xi, float yi, float xj, float yj, 
 // on to the next segment costs a lane a register move.
 // Every row of the window, tested here (any r); with kTpp lanes per particle, lane `sub`
 // takes rows y0 + sub, y0 + sub + kTpp, ...
-template <int kTpp = 1, typename Fn>
+// kPaired: the candidate tests two at a time (segment_mask) or one at a time; the sums are
+// the same either way (which one a pass uses is a measured code-generation choice).
+template <int kTpp = 1, bool kPaired = false, typename Fn>
 __device__ __forceinline__ void cell_pairs(const FluidView& F, const sph_grid& g, int r, int coff, int cx, int cy,
                                            float xi, float yi, float thr, Fn&& fn, int sub = 0) {
   const int x0 = max(cx - r, 0), x1 = min(cx + r, g.cells_x - 1);
@@ -155,7 +157,7 @@ __device__ __forceinline__ void cell_pairs(const FluidView& F, const sph_grid& g
     const int row = yy * g.cells_x;
     const int b = __ldg(cs + row + x0), e = __ldg(cs + row + x1 + 1);
     for (int c = b; c < e; c += 32) {
-      uint32_t w = segment_mask(F.x, c, e, xi, yi, thr);
+      uint32_t w = kPaired ? segment_mask(F.x, c, e, xi, yi, thr) : segment_mask_scalar(F.x, c, e, xi, yi, thr);
       while (w) {
         const int j = c - 1 + __ffs(w);
         w &= w - 1;
@@ -198,7 +200,7 @@ __device__ __forceinline__ void segments_body(int i, const FluidView& F, const s
 // The pairs of particle i from its segment list (its cell rows when the list overflowed).
 // With kTpp lanes per particle, lane `sub` takes segments sub, sub + kTpp, ... (rows, on the
 // overflow path); each lane holds its current segment and its next one, loaded ahead.
-template <int kTpp = 1, typename Fn>
+template <int kTpp = 1, bool kPaired = false, typename Fn>
 __device__ __forceinline__ void stored_pairs(int i, const FluidView& F, const sph_grid& g, int coff, int r,
                                              const int32_t* __restrict__ nseg, const int32_t* __restrict__ seg_start,
                                              const uint32_t* __restrict__ seg_mask, float xi, float yi, float thr,
@@ -207,7 +209,7 @@ __device__ __forceinline__ void stored_pairs(int i, const FluidView& F, const sp
   if (ns < 0 || ns > kMaxSegments) {
     int cx, cy;
     cell_of(F.keys[i] - (uint32_t)coff, g, &cx, &cy);
-    cell_pairs<kTpp>(F, g, r, coff, cx, cy, xi, yi, thr, fn, sub);
+    cell_pairs<kTpp, kPaired>(F, g, r, coff, cx, cy, xi, yi, thr, fn, sub);
     return;
   }
   if (ns <= sub) return;
@@ -451,8 +453,8 @@ __device__ __forceinline__ float diffusion_sum(int i, const FluidView& F, const 
     acc += (gv.x * e.dx + gv.y * e.dy) * e.gd;
   };
   if constexpr (kCells) {
-    if (live) stored_pairs<kTpp>(i, F, g, coff, P.search_radius, S.nseg, S.start, S.mask, xi.x, xi.y, P.thr, pair,
-                                 sub);
+    if (live) stored_pairs<kTpp, true>(i, F, g, coff, P.search_radius, S.nseg, S.start, S.mask, xi.x, xi.y, P.thr,
+                                       pair, sub);
   } else {
     static_assert(kTpp == 1, "CSR rows run one lane per particle");
     const int k0 = F.offsets[i], k1 = row_end(F, i, k0);

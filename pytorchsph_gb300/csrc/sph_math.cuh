@@ -247,13 +247,38 @@ __device__ __forceinline__ void for_each_wall(const WallView& W, const sph_grid&
 // and a particle keeps its non-empty segments, at most kMaxSegments, as (start, mask) pairs.
 constexpr int kMaxSegments = 8;
 
-__device__ __forceinline__ uint32_t segment_mask(const float2* __restrict__ x, int c, int e, float xi, float yi,
-                                                 float thr) {
+// One candidate per step (the force passes' rare fallback for a particle whose segments
+// did not fit).
+__device__ __forceinline__ uint32_t segment_mask_scalar(const float2* __restrict__ x, int c, int e, float xi,
+                                                        float yi, float thr) {
   const int len = min(e - c, 32);
   uint32_t m = 0;
   for (int t = 0; t < len; ++t) {
     const float2 pj = __ldg(x + c + t);
     m |= (uint32_t)(dist2_ref(xi, yi, pj.x, pj.y) <= thr) << t;
+  }
+  return m;
+}
+
+// Two candidates per step with the paired float32 instructions (per component the same
+// round-to-nearest operations as dist2_ref: x_i - x_j as x_i + (-x_j), which IEEE
+// arithmetic makes identical, so the pair test is unchanged bit for bit).
+__device__ __forceinline__ uint32_t segment_mask(const float2* __restrict__ x, int c, int e, float xi, float yi,
+                                                 float thr) {
+  const int len = min(e - c, 32);
+  uint32_t m = 0;
+  const float2 qx = make_float2(xi, xi), qy = make_float2(yi, yi);
+  int t = 0;
+  for (; t + 1 < len; t += 2) {
+    const float2 a = __ldg(x + c + t), b = __ldg(x + c + t + 1);
+    const float2 dx = __fadd2_rn(qx, make_float2(-a.x, -b.x));
+    const float2 dy = __fadd2_rn(qy, make_float2(-a.y, -b.y));
+    const float2 v = __ffma2_rn(dx, dx, __fmul2_rn(dy, dy));
+    m |= ((uint32_t)(v.x <= thr) | ((uint32_t)(v.y <= thr) << 1)) << t;
+  }
+  if (t < len) {
+    const float2 a = __ldg(x + c + t);
+    m |= (uint32_t)(dist2_ref(xi, yi, a.x, a.y) <= thr) << t;
   }
   return m;
 }
