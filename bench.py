@@ -216,6 +216,38 @@ def cpu_baseline_serving(steps=3):
                       f"restated reference step (oracle/sph_torch.py, float32, torch CPU)"}
 
 
+def cpu_dfsph_steps(scene, steps):
+    """Seconds for `steps` DFSPH steps of the restated reference step (oracle/sph_torch.py,
+    float32, torch CPU, solid walls, the bench's solver settings and adaptive dt)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import torch
+    import sph_torch as S
+    p = S.Params(h=scene["h"], c0=float(10 * np.sqrt(2 * 9.81 * scene["column_height"])), kinematic=0.01,
+                 vmin=scene["vmin"], vmax=scene["vmax"], density_threshold=1e-4, divergence_threshold=1e-3,
+                 max_density_iters=100, max_divergence_iters=100)
+    walls = S.Walls(torch.from_numpy(scene["wall_pos"]), torch.from_numpy(scene["ghost_pos"]),
+                    torch.from_numpy(scene["wall_area"]))
+    walls.density_term = S.wall_density_term(walls, scene["h"], torch.float32)
+    st = {"x": torch.from_numpy(scene["pos"]), "v": torch.from_numpy(scene["vel"]),
+          "rho": torch.from_numpy(scene["rho"]), "area": torch.from_numpy(scene["area"])}
+    dt = 2e-4
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        new, _ = S.step(st, walls, p, dt, "semiImplicitEuler", "dfsph", torch.float32)
+        st = {"x": new["x"].float(), "v": new["v"], "rho": new["rho"], "area": st["area"]}
+        dt = S.update_dt(new, p, dt, 1e-6, 1e-3)
+    return time.perf_counter() - t0
+
+
+def serving_workload(args, world):
+    """The serving workload's description, the same in both arms."""
+    return {"workload": "serving", "requests": args.requests, "trace_steps": args.trace_steps,
+            "arrivals": "Poisson 50/s", "sizes": "log-uniform 2048-131072",
+            "mix": "50% dam break (aspect U[0.5,2]) / 50% oscillating drop (A U[0.5,2])",
+            "solver": "deltaSPH (renormalized density diffusion), semi-implicit Euler, dt = 0.1 h / c0, "
+                      "3-layer walls", "parallelism": f"replicas{world}"}
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -235,13 +267,45 @@ def run_reference(args):
         sample = f"full {args.workload} step x {args.steps} (sort + hash map + buildNeighborList + density)"
         unit, cores = "particles/s", threads
         config = {"workload": args.workload, "particles": len(pos)}
+    elif args.workload in ("dambreak_deltasph", "dambreak_dfsph"):
+        import torch
+        from pytorchsph_gb300 import workloads
+        torch.set_num_threads(threads)
+        steps = max(1, min(args.steps, 3))
+        if args.workload == "dambreak_deltasph":
+            sc = workloads.dam_break(64, 128, 0.01, (4.0, 2.0))
+            c0 = float(10 * np.sqrt(2 * 9.81 * sc["column_height"]))
+            params = {"c0": c0, "dt": 0.25 * sc["h"] / c0}
+            cpu_deltasph_steps(sc, params, 1, "deltaSPH")
+            t = cpu_deltasph_steps(sc, params, steps, "deltaSPH")
+            sample = f"{steps} steps of the same 8192-particle dam break (restated reference step, float32, torch CPU)"
+        else:   # the 262,144-particle block takes minutes per CPU step: a 64 x 64 block of the same tank
+            sc = workloads.dam_break(64, 64, 0.016, (4.096, 2.048))
+            t = cpu_dfsph_steps(sc, steps)
+            sample = (f"{steps} DFSPH steps of a {len(sc['pos'])}-particle block of the same tank (restated "
+                      f"reference step, float32, torch CPU)")
+        value, unit, cores = len(sc["pos"]) * steps / t, "particle-steps/s", torch.get_num_threads()
+        ms = 1e3 * t / steps
+        config = {"workload": args.workload}
+    elif args.workload == "diff_drop":
+        import torch
+        from pytorchsph_gb300 import workloads
+        torch.set_num_threads(threads)
+        start = workloads.oscillating_drop(16384, 0.5, 0.8)
+        dt, steps = 0.1 * start["h"] / 10.0, max(1, min(args.steps, 3))
+        cpu_autograd_drop(start, dt, 1)
+        t = cpu_autograd_drop(start, dt, steps)
+        value, unit, cores = len(start["pos"]) * steps / t, "particle-steps/s", torch.get_num_threads()
+        ms = 1e3 * t / steps
+        sample = f"forward + torch autograd backward of {steps} float64 steps of the drop (restated reference step)"
+        config = {"workload": "diff_drop"}
     else:
         import torch
         torch.set_num_threads(threads)
         cb = cpu_baseline_serving(steps=max(1, min(args.steps, 5)))
         value, unit, sample, cores = cb["value"], cb["unit"], cb["sample"], cb["cores"]
         ms = 2048 / value * 1e3
-        config = {"workload": args.workload}
+        config = serving_workload(args, world)
     line = base_line(args, world, value, ms, unit, config)
     line["impl"] = "reference"
     line["cpu_baseline"] = {"value": value, "unit": unit, "cores": cores, "kind": "port", "sample": sample}
@@ -423,13 +487,10 @@ def run_serving(args, dev, world, rank):
     cpu = cpu_baseline_serving() if rank == 0 and not args.no_cpu_baseline else None
     if rank == 0:
         line = base_line(args, world, value, ms, "particle-steps/s", {
-            "workload": "serving", "requests": len(specs), "trace_steps": args.trace_steps,
-            "particles_resident": total_p, "arrivals": "Poisson 50/s", "sizes": "log-uniform 2048-131072",
-            "mix": "50% dam break (aspect U[0.5,2]) / 50% oscillating drop (A U[0.5,2])",
-            "solver": "deltaSPH (renormalized density diffusion), semi-implicit Euler, dt = 0.1 h / c0, "
-                      "3-layer walls", "budget_gb": budget / 1e9,
+            **serving_workload(args, world), "requests": len(specs), "particles_resident": total_p,
+            "budget_gb": budget / 1e9,
             "batch_bytes": batch_bytes, "l2": f"state of {total_p} particles >> L2 (no flush needed)",
-            "graph": "one CUDA graph per batch step", "parallelism": f"replicas{world}",
+            "graph": "one CUDA graph per batch step",
             "pairs": "from the cell rows (no neighbor list)" if args.pairs == "cells" else "CSR list every step",
             "scene_generation_s": gen_s})
         line["phases_ms"] = {k: round(v, 4) for k, v in phases.items()}
@@ -654,6 +715,14 @@ def run_dambreak(args, dev, world, rank):
         config = {"workload": args.workload, "particles": n, "walls": sim.nb,
                   "solver": "DFSPH, divergence + density solves, semi-implicit Euler, adaptive dt",
                   "density_iters_last": int(sim.last["density_iters"].item())}
+        if rank == 0 and not args.no_cpu_baseline:
+            # the full block takes minutes per CPU step: a 64 x 64 block of the same tank
+            small = workloads.dam_break(64, 64, 0.016, (4.096, 2.048))
+            t = cpu_dfsph_steps(small, 2)
+            cpu = {"value": len(small["pos"]) * 2 / t, "unit": "particle-steps/s",
+                   "cores": torch.get_num_threads(), "kind": "port",
+                   "sample": f"2 DFSPH steps of a {len(small['pos'])}-particle block of the same tank with the "
+                             f"restated reference step (oracle/sph_torch.py, float32, torch CPU)"}
     value = n * world / (ms / 1e3)
     if rank == 0:
         line = base_line(args, world, value, ms, "particle-steps/s", config)
