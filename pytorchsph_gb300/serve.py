@@ -596,6 +596,12 @@ class Server:
             nonfinite = bool(self._read_flags() & N.SPH_FLAG_NONFINITE)
             escaped = self.batch.escaped()
             all_states = self.batch.states_device()
+            # final states to the host: one copy per field of the whole batch when the retiring
+            # requests hold a large part of it (many small copies cost more), else per request
+            host_states = None
+            retiring = sum(len(r.spec.scene["pos"]) for r in self.live if r.steps_done >= r.spec.steps)
+            if self.keep_final and retiring * 4 >= self.batch.n:
+                host_states = {k: v.cpu().numpy() for k, v in all_states.items()}
             for s, r in enumerate(self.live):
                 r.escaped = int(escaped[s])
                 if nonfinite and not self.batch.scene_finite(s):
@@ -607,7 +613,11 @@ class Server:
                 st = self.batch.scene_state_device(s, all_states)
                 if r.steps_done >= r.spec.steps:
                     r.finished = now
-                    if self.keep_final:
+                    if self.keep_final and host_states is not None:
+                        k0 = self.batch.p_off[self.batch._slot[s]]
+                        k1 = self.batch.p_off[self.batch._slot[s] + 1]
+                        r.final = {k: v[k0:k1].copy() for k, v in host_states.items()}
+                    elif self.keep_final:
                         r.final = {k: v.cpu().numpy() for k, v in st.items()}
                     r.spec.dev = None          # release the scene's device copies
                 else:
