@@ -129,6 +129,47 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_down(const int32_t* __res
   if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) out[n] = block_offsets[gridDim.x];
 }
 
+// Small scans in one launch: one block walks the tiles in order with a running carry
+// (n <= kSmallScanItems; the three-kernel scan costs two more launches, which dominate a
+// small scene's step).
+constexpr int64_t kSmallScanItems = 16 * (int64_t)kScanTile;
+
+template <typename TOut>
+__global__ void __launch_bounds__(kScanThreads) k_scan_small(const int32_t* __restrict__ in, TOut* __restrict__ out,
+                                                             int64_t n) {
+  __shared__ TOut sw[33];
+  __shared__ TOut tile[kScanTile];
+  TOut carry = 0;
+  for (int64_t base = 0; base < n; base += kScanTile) {
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+      const int64_t idx = base + (int64_t)k * kScanThreads + threadIdx.x;
+      tile[k * kScanThreads + threadIdx.x] = idx < n ? (TOut)in[idx] : TOut(0);
+    }
+    __syncthreads();
+    TOut local[kScanItems];
+    TOut sum = 0;
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+      local[k] = sum;
+      sum += tile[threadIdx.x * kScanItems + k];
+    }
+    TOut total;
+    const TOut ex = block_excl_scan<TOut>(sum, sw, &total) + carry;
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) tile[threadIdx.x * kScanItems + k] = ex + local[k];
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+      const int64_t idx = base + (int64_t)k * kScanThreads + threadIdx.x;
+      if (idx < n) out[idx] = tile[k * kScanThreads + threadIdx.x];
+    }
+    carry += total;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[n] = carry;
+}
+
 static int64_t scan_blocks(int64_t n) { return (n + kScanTile - 1) / kScanTile; }
 
 template <typename TOut>
@@ -145,6 +186,11 @@ static sph_status_t scan_impl(const int32_t* in, TOut* out, int64_t n, void* scr
   if (scratch_bytes < (size_t)(nb + 1) * sizeof(int64_t) || scratch == nullptr) {
     set_error_text("scan: scratch too small");
     return SPH_ERR_SCRATCH_TOO_SMALL;
+  }
+  if (n <= kSmallScanItems) {
+    k_scan_small<TOut><<<1, kScanThreads, 0, st>>>(in, out, n);
+    SPH_CHECK_LAUNCH("scan(small)");
+    return SPH_OK;
   }
   TOut* sums = reinterpret_cast<TOut*>(scratch);
   k_scan_reduce<TOut><<<(unsigned)nb, kScanThreads, 0, st>>>(in, n, sums);
