@@ -331,14 +331,20 @@ def serving_specs(n_requests, steps):
 def pass1_alg_bytes(batch):
     """Algorithmic HBM bytes of one k_batch_pass1 launch over renormalized scenes.
     Per particle: its two 16-byte neighbor records (read once; the other 27-odd reads of
-    them are L1/L2 hits), key 4, scene index 4 read, dpdt 4 + acc 8 + <grad rho> 8 written.
-    Pairs from the cell rows: the candidates' positions 8 read and three row masks 24
-    written (92), plus the cell table once.  CSR pairs: offsets 4 (64) and 4 per column.
-    Per wall: position 8 + volume, density, pressure 12."""
+    them are L1/L2 hits), relative density 4, key 4, scene index 4 read, dpdt 4 + acc 8 +
+    <grad rho> V 8 written.  Pairs from the cell rows: the segment count 4 and 8 per stored
+    segment (start, mask) read (68 per particle + 8 per segment).  CSR pairs: offsets 4 (64)
+    and 4 per column.  Per wall: position 8 + volume, density, pressure 12."""
+    import torch
     if batch.pairs == "csr":
         P = int(batch.offsets[batch.n].item())
         return batch.n * 64 + 4 * P + batch.nb * 20
-    return batch.n * 92 + (batch.cap + 2) * 4 + batch.nb * 20
+    # the segment counts sit after the records (32 n bytes) and the 8 n masks and 8 n starts
+    n = batch.n
+    words = batch.forces_scratch.view(torch.int32)
+    nseg = words[(32 * n + 64 * n) // 4:(32 * n + 64 * n) // 4 + n]
+    segments = int(torch.clamp(nseg, min=0).sum().item())
+    return n * 68 + 8 * segments + batch.nb * 20
 
 
 def phase_times(batch, reps=5):

@@ -289,7 +289,7 @@ sph_status_t sph_mdbc_wall_density(const sph_fluid_view* fluid, const sph_wall_v
  * artificial viscosity (diffusion.py:12-25) + laminar viscosity (laminar.py:12-27), each
  * with its wall part (solidBoundary.py:746-890).  Wall quantities must come from
  * sph_mdbc_wall_density.  scratch: sph_deltasph_scratch_bytes(n) bytes of device memory
- * (per-particle neighbor records, and the cell-row masks of sph_batch_deltasph_step). */
+ * (per-particle neighbor records, and the segment lists of sph_batch_deltasph_step). */
 size_t sph_deltasph_scratch_bytes(int64_t n);
 sph_status_t sph_deltasph_forces(const sph_fluid_view* fluid, const sph_wall_view* walls, const sph_grid* grid,
                                  const sph_params* params, float* dpdt, float* acc, float* L, float* grad_rho,
@@ -350,10 +350,10 @@ sph_status_t sph_batch_nl_fill(const float* xy, const float* sorted_support, int
  * diffusion pass (needed when any_renormalized; grad_rho then holds <grad rho> V, the part
  * of the deltaSPH diffusion that needs the neighbors); scratch as for sph_deltasph_forces.
  * With fluid->offsets and fluid->cols both NULL no neighbor list is needed: the records
- * launch also stores, per particle, the first candidate and a 64-bit accepted-candidate
- * mask of each of its three cell rows (search_radius 1; other radii test their cell rows
- * in the force passes), and both force passes visit those pairs, in the CSR fill's order
- * (same sums).  Each scene's pair test then uses its own support (sph_params.support),
+ * launch also tests each particle's cell rows in segments of 32 candidates and stores its
+ * non-empty segments (start, 32-bit accepted-candidate mask; at most 8, else the force
+ * passes test its rows themselves), and both force passes visit those pairs in the CSR
+ * fill's order (same sums).  Each scene's pair test then uses its own support (sph_params.support),
  * which must be every particle's support.
  * The force passes (pass1, diffusion) run over `groups` (a host array of ngroups entries
  * that tile [0, n) in order; a group holds whole scenes when its bounds are scene bounds):

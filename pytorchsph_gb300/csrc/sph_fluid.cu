@@ -1,8 +1,9 @@
-// deltaSPH right-hand side on sm_103a: one thread per fluid particle (cell-sorted order),
-// gathering over its CSR row and over the wall particles of the neighboring cells.  Every
-// sum is a gather into registers — no atomics, deterministic order: fluid neighbors in CSR
-// order, then walls, added to the fluid sum the way the reference adds its wall module's
-// result (`x += simulation.boundaryModule...`).
+// deltaSPH right-hand side on sm_103a: one thread (or 2 / 4 lanes) per fluid particle in
+// cell-sorted order, gathering over its pairs (a CSR row, or its segment list of accepted
+// candidates from the cell rows) and over the wall particles of the neighboring cells.
+// Every sum is a gather into registers — no atomics, deterministic order: fluid neighbors in
+// cell order, then walls, added to the fluid sum the way the reference adds its wall
+// module's result (`x += simulation.boundaryModule...`).
 //
 // Each kernel body takes its scene's grid, parameters and cell-table offset explicitly, so
 // the same code serves one scene (sph_* entry points) and a batch of independent scenes

@@ -529,7 +529,7 @@ class SceneBatch:
 
 
 def estimate_bytes(scene, pairs: str = "cells") -> int:
-    """Device bytes one scene needs in a batch: state x2, sort, force records and row masks,
+    """Device bytes one scene needs in a batch: state x2, sort, force records and segment lists,
     and with pairs = "csr" the CSR list at ~30 pairs/particle."""
     n = len(scene["pos"])
     nb = len(scene.get("wall_pos", ()))
