@@ -560,11 +560,15 @@ def run_search_density(args, dev, world, rank):
         marks("end")
         return r
 
+    # grid (bounds, final), keys, sort, gather, count, scan, fill, dense rows, scatter; a scan
+    # is one kernel (the zeroing of its tile words is a memset); counting sort: scan,
+    # scatter, in-cell fix of small and of large cells; radix: per digit histogram, scan,
+    # scatter, then the cell starts
     if args.sort == "counting":
-        sort_launches = 6
+        sort_launches = 4
     else:
-        sort_launches = ((N.load().sph_key_bits(cells) + args.digit_bits - 1) // args.digit_bits) * 5 + 1
-    launches_per_step = 2 + 1 + sort_launches + 1 + 1 + 3 + 1 + 1
+        sort_launches = ((N.load().sph_key_bits(cells) + args.digit_bits - 1) // args.digit_bits) * 3 + 1
+    launches_per_step = 2 + 1 + sort_launches + 1 + 1 + 1 + 1 + 1 + 1
     s = torch.cuda.Stream(dev)
     s.wait_stream(torch.cuda.current_stream())
     with torch.cuda.stream(s):

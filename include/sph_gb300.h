@@ -115,17 +115,22 @@ const char* sph_status_string(sph_status_t status);
 size_t sph_scan_scratch_bytes(int64_t n);
 /* out[k] = in[0] + ... + in[k-1] for k <= n (out has n+1 entries; out[n] = total).
  * Replaces torch::cumsum in cppSrc/neighSearch_cuda.cu:250 and the cumsums of
- * src/modules/neighborSearch.py:65,86. */
+ * src/modules/neighborSearch.py:65,86.  Above 8,192 items: one zeroing of the scratch and
+ * one single-pass launch (decoupled look-back); the scratch must not be shared by scans
+ * that overlap on the GPU. */
 sph_status_t sph_exclusive_scan_i32(const int32_t* in, int32_t* out, int64_t n, void* scratch,
                                     size_t scratch_bytes, void* stream);
 sph_status_t sph_exclusive_scan_i32_to_i64(const int32_t* in, int64_t* out, int64_t n, void* scratch,
                                            size_t scratch_bytes, void* stream);
+/* Look-back waits of the scans that gave up (each wait is bounded) since the library was
+ * loaded on the current device: 0 unless a scan's output is wrong.  Synchronous. */
+uint64_t sph_scan_timeouts(void);
 
 /* Allocation-free variant of sph_exclusive_scan_i32.  It has no counterpart in the
  * reference; it exists for callers that cannot allocate device memory: a host runtime
  * bound through this C ABI that only receives device pointers from another owner of
  * GPU memory, or code recording a CUDA graph, where cudaMalloc is not permitted.  The
- * scan's block sums live in a fixed 64 KiB array in the library's device memory (one per
+ * scan's tile words live in a fixed 64 KiB array in the library's device memory (one per
  * GPU, held until the process exits), so n is limited to
  * sph_exclusive_scan_i32_static_max_items() = 33,550,336; larger n is rejected with
  * SPH_ERR_INVALID_ARGUMENT.  Nothing in the array needs to start at zero.  The first call
@@ -227,7 +232,7 @@ sph_status_t sph_nl_fill(const float* xy, const float* sorted_support, int64_t n
                          int32_t* cols, int32_t* status, void* stream);
 /* The same two passes with one candidate test per pair: sph_nl_count_segments tests the
  * cell rows once, in segments of 32 candidates, and keeps each particle's accepted-candidate
- * bit masks (at most 8 segments; more: its rows are scanned again by the fill) in
+ * bit masks (at most 24 segments; more: its rows are scanned again by the fill) in
  * seg_scratch (sph_nl_segments_scratch_bytes(n) bytes) besides counts and rho;
  * sph_nl_fill_segments expands them into the CSR columns.  Same counts, rho, columns and
  * order as sph_nl_count / sph_nl_fill. */

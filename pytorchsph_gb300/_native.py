@@ -29,6 +29,7 @@ SIGNATURES = {
     "sph_scan_scratch_bytes": (_SZ, [_I64]),
     "sph_exclusive_scan_i32": (_I32, [_P, _P, _I64, _P, _SZ, _P]),
     "sph_exclusive_scan_i32_to_i64": (_I32, [_P, _P, _I64, _P, _SZ, _P]),
+    "sph_scan_timeouts": (ctypes.c_uint64, []),
     "sph_exclusive_scan_i32_static_max_items": (_I64, []),
     "sph_exclusive_scan_i32_static": (_I32, [_P, _P, _I64, _P]),
     "sph_radix_sort_scratch_bytes": (_SZ, [_I64, _I32]),

@@ -6,11 +6,34 @@
 // contiguous in the sorted order, so a particle scans 2r+1 contiguous index ranges.
 //
 // The pair test is the reference's sqrtf(fmaf(dx,dx,dy*dy)) < h_i in its square-root-free
-// exact form v <= F_i (sq_threshold); the square root is taken only for accepted pairs
-// that need the distance (density).
+// exact form v <= F_i (sq_threshold); the distance is taken only for accepted pairs that
+// need it (density).
 #include "sph_math.cuh"
 
 namespace sph {
+
+// Segments kept per particle by the one-scene search (the batch step's force passes keep
+// kMaxSegments): a particle with more goes on the dense list.  24 covers three cell rows of
+// up to 8 x 32 candidates each, ~9x the density of a jittered lattice at support 3 dx.
+constexpr int kSearchSegments = 24;
+
+// Density terms of the accepted candidates of one segment (the set bits of w, candidate
+// c-1+bit), added to acc in index order (the caller scales the sum by c_w).  Distance
+// r = v * rsqrt(max(v, 1e-30)): 0 for the particle itself, within a few ulp of sqrt(v)
+// otherwise.  W(q) / c_w = (1-q)^4 (1+4q), src/kernels.py:20-24.
+__device__ __forceinline__ void density_segment(const float2* __restrict__ xy, const float* __restrict__ sa, int c,
+                                                uint32_t w, float xi, float yi, float inv_support, float& acc) {
+  while (w) {
+    const int j = c - 1 + __ffs(w);
+    w &= w - 1;
+    const float2 pj = __ldg(xy + j);
+    const float v = dist2_ref(xi, yi, pj.x, pj.y);
+    const float q = v * (rsqrtf(fmaxf(v, 1e-30f)) * inv_support);
+    const float a = 1.f - q;
+    const float a2 = a * a;
+    acc += a2 * a2 * (1.f + 4.f * q) * __ldg(sa + j);
+  }
+}
 
 template <typename F>
 __device__ __forceinline__ void scan_candidates(const float2* __restrict__ xy, const int32_t* __restrict__ cell_start,
@@ -48,11 +71,19 @@ __global__ void __launch_bounds__(256) k_nl_count(const float2* __restrict__ xy,
     const float2 pi = xy[s];
     const float thr = grid_threshold(sh[s], g);
     const int cx = (int)(key % (uint32_t)g.cells_x), cy = (int)(key / (uint32_t)g.cells_x);
-    if (rho) {
-      scan_candidates(xy, cell_start, g, r, cx, cy, pi.x, pi.y, thr, [&](int j, float v) {
-        ++cnt;
-        acc += wendland(__fsqrt_rn(v) * inv_support, c_w) * __ldg(sa + j);
-      });
+    if (rho) {   // the candidates in segments of 32, as k_nl_segments, so both give the same sums
+      const int x0 = max(cx - r, 0), x1 = min(cx + r, g.cells_x - 1);
+      const int y0 = max(cy - r, 0), y1 = min(cy + r, g.cells_y - 1);
+      for (int yy = y0; yy <= y1 && x0 <= x1; ++yy) {
+        const int row = yy * g.cells_x;
+        const int b = __ldg(cell_start + row + x0), e = __ldg(cell_start + row + x1 + 1);
+        for (int c = b; c < e; c += 32) {
+          const uint32_t w = segment_mask(xy, c, e, pi.x, pi.y, thr);
+          cnt += __popc(w);
+          density_segment(xy, sa, c, w, pi.x, pi.y, inv_support, acc);
+        }
+      }
+      acc *= c_w;
     } else {
       scan_candidates(xy, cell_start, g, r, cx, cy, pi.x, pi.y, thr, [&](int, float) { ++cnt; });
     }
@@ -64,11 +95,13 @@ __global__ void __launch_bounds__(256) k_nl_count(const float2* __restrict__ xy,
 constexpr int kFillStage = 8192;  // CSR columns one 256-thread block builds in shared memory (32 KiB)
 
 // Writes the row [offsets[s], offsets[s+1]) of particle s with the columns `scan` emits.
-// The rows of one block are one contiguous span of cols.  When that span fits the stage
-// buffer (and the column buffer), the block builds it in shared memory and writes it out
-// with coalesced stores; otherwise every row is written in place, and a row that does not
-// fit the column buffer is skipped with SPH_FLAG_PAIR_CAPACITY set.  Every thread of the
-// block must call this (inactive ones with active = false): it holds a block barrier.
+// The rows of one block are one contiguous span of cols, written through a shared-memory
+// stage in windows of kFillStage columns: for each window the rows that reach into it emit
+// their columns that fall inside it (a row across a window edge is emitted once per window
+// it touches), and the block stores the window with coalesced stores.  A block whose span
+// ends past the column buffer writes its rows in place instead, and a row that does not
+// fit is skipped with SPH_FLAG_PAIR_CAPACITY set.  Every thread of the block must call
+// this (inactive ones with active = false): it holds block barriers.
 template <typename Scan>
 __device__ __forceinline__ void staged_fill(int64_t s, int64_t n, bool active, const int32_t* __restrict__ offsets,
                                             int64_t pair_capacity, int32_t* __restrict__ cols, int32_t* status,
@@ -76,30 +109,46 @@ __device__ __forceinline__ void staged_fill(int64_t s, int64_t n, bool active, c
   __shared__ int32_t stage[kFillStage];
   const int64_t b0 = (int64_t)blockIdx.x * blockDim.x;
   const int64_t b1 = min(b0 + (int64_t)blockDim.x, n);
-  const int32_t span0 = offsets[b0], span1 = offsets[b1];
-  const bool staged = span0 >= 0 && span1 >= span0 && span1 - span0 <= kFillStage &&
-                      (int64_t)span1 <= pair_capacity;  // the same in the whole block
-  if (active) {
-    // writes stay inside the row even if offsets disagree with the scan
-    if (staged) {
-      int32_t o = offsets[s] - span0;
-      const int32_t e = offsets[s + 1] - span0;
-      if (o >= 0) scan([&](int j) {
-        if (o < e) stage[o++] = j;
-      });
-    } else if ((int64_t)offsets[s + 1] <= pair_capacity) {
+  const int64_t span0 = offsets[b0], span1 = offsets[b1];
+  const bool staged = span0 >= 0 && span1 >= span0 && span1 <= pair_capacity;  // the same in the whole block
+  if (!staged) {
+    if (!active) return;
+    if ((int64_t)offsets[s + 1] <= pair_capacity) {
       int32_t o = offsets[s];
       const int32_t e = offsets[s + 1];
-      if (o >= 0) scan([&](int j) {
+      if (o >= 0) scan([&](int j) {   // writes stay inside the row even if offsets disagree with the scan
         if (o < e) cols[o++] = j;
       });
     } else {
       flag(status, SPH_FLAG_PAIR_CAPACITY);
     }
+    return;
   }
-  if (staged) {
+  if (span1 - span0 <= kFillStage) {   // one window
+    if (active) {
+      int32_t o = offsets[s] - (int32_t)span0;
+      const int32_t e = offsets[s + 1] - (int32_t)span0;
+      if (o >= 0) scan([&](int j) {
+        if (o < e) stage[o++] = j;
+      });
+    }
     __syncthreads();
-    for (int k = threadIdx.x; k < span1 - span0; k += blockDim.x) cols[span0 + k] = stage[k];
+    for (int k = threadIdx.x; k < (int)(span1 - span0); k += blockDim.x) cols[span0 + k] = stage[k];
+    return;
+  }
+  const int64_t r0 = active ? offsets[s] : 0, r1 = active ? offsets[s + 1] : 0;
+  for (int64_t w0 = span0; w0 < span1; w0 += kFillStage) {
+    const int64_t w1 = min(w0 + (int64_t)kFillStage, span1);
+    if (active && r0 < w1 && r1 > w0) {
+      int64_t o = r0;
+      scan([&](int j) {
+        if (o >= w0 && o < w1 && o < r1) stage[o - w0] = j;
+        ++o;
+      });
+    }
+    __syncthreads();
+    for (int64_t k = threadIdx.x; k < w1 - w0; k += blockDim.x) cols[w0 + k] = stage[k];
+    __syncthreads();
   }
 }
 
@@ -129,7 +178,7 @@ __global__ void __launch_bounds__(256) k_nl_fill(const float2* __restrict__ xy, 
 // tested in segments of 32 candidates (segment_mask); the non-empty segments are stored for
 // k_nl_fill_segments, the count is their bit count, and the density visits the set bits in
 // order, the order of k_nl_count, so both give the same sums.  A particle with more than
-// kMaxSegments segments gets nseg[s] = -1 and goes on the dense list, whose rows
+// kSearchSegments segments gets nseg[s] = -1 and goes on the dense list, whose rows
 // k_nl_fill_dense writes one warp per particle.
 __global__ void __launch_bounds__(256) k_nl_segments(const float2* __restrict__ xy, const float* __restrict__ sh,
                                                      const float* __restrict__ sa, int64_t n,
@@ -158,25 +207,20 @@ __global__ void __launch_bounds__(256) k_nl_segments(const float2* __restrict__ 
       for (int c = b; c < e; c += 32) {
         uint32_t w = segment_mask(xy, c, e, pi.x, pi.y, thr);
         if (w == 0) continue;
-        if (k < kMaxSegments) {
+        if (k < kSearchSegments) {
           seg_start[(int64_t)k * n + s] = c;
           seg_mask[(int64_t)k * n + s] = w;
         }
         ++k;
         cnt += __popc(w);
-        while (rho && w) {
-          const int j = c - 1 + __ffs(w);
-          w &= w - 1;
-          const float2 pj = __ldg(xy + j);
-          acc += wendland(__fsqrt_rn(dist2_ref(pi.x, pi.y, pj.x, pj.y)) * inv_support, c_w) * __ldg(sa + j);
-        }
+        if (rho) density_segment(xy, sa, c, w, pi.x, pi.y, inv_support, acc);
       }
     }
   }
   counts[s] = cnt;
-  if (rho) rho[s] = acc;
-  nseg[s] = k <= kMaxSegments ? k : -1;
-  if (k > kMaxSegments) dense_list[atomicAdd(dense_count, 1)] = (int32_t)s;
+  if (rho) rho[s] = acc * c_w;
+  nseg[s] = k <= kSearchSegments ? k : -1;
+  if (k > kSearchSegments) dense_list[atomicAdd(dense_count, 1)] = (int32_t)s;
 }
 
 // The CSR columns from the stored segments (no pair tests).  Rows of the dense list are left
@@ -197,8 +241,59 @@ __global__ void __launch_bounds__(256) k_nl_fill_segments(const float2* __restri
   const uint32_t key = s < n ? keys[s] : 0xffffffffu;
   const bool active = s < n && grid_ok(g, cap) && key < (uint32_t)g.num_cells;
   const int ns = active ? nseg[s] : 0;
+  const int64_t b0 = (int64_t)blockIdx.x * blockDim.x, b1 = min(b0 + (int64_t)blockDim.x, n);
+  const int64_t span0 = offsets[b0], span1 = offsets[b1];
+  if (span0 >= 0 && span1 - span0 > kFillStage && span1 <= pair_capacity) {   // the same in the whole block
+    // Rows too long for one stage: each warp writes its 32 rows one after another, the lanes
+    // taking one candidate bit each; lane k holds segment k of the row, and the exclusive
+    // scan of the segments' bit counts places them, so a segment goes out as one contiguous
+    // store of its accepted candidates.  The next row's segments are loaded while a row is
+    // written.
+    const int lane = threadIdx.x & 31;
+    const uint32_t below = (1u << lane) - 1u;
+    const int64_t r0 = active ? offsets[s] : 0, r1 = active ? offsets[s + 1] : 0;
+    auto load_row = [&](int t, int& nst, int& c, uint32_t& m) {
+      nst = __shfl_sync(0xffffffffu, ns, t);
+      const int64_t st = __shfl_sync(0xffffffffu, s, t);
+      c = 0;
+      m = 0;
+      if (nst > 0 && nst <= kSearchSegments && lane < nst) {
+        c = seg_start[(int64_t)lane * n + st];
+        m = seg_mask[(int64_t)lane * n + st];
+      }
+    };
+    int nst_next, c_next;
+    uint32_t m_next;
+    load_row(0, nst_next, c_next, m_next);
+    for (int t = 0; t < 32; ++t) {
+      const int nst = nst_next, c = c_next;
+      uint32_t m = m_next;
+      if (t + 1 < 32) load_row(t + 1, nst_next, c_next, m_next);
+      if (nst <= 0 || nst > kSearchSegments) continue;   // nothing, or a dense row
+      const int64_t o = __shfl_sync(0xffffffffu, r0, t), e = __shfl_sync(0xffffffffu, r1, t);
+      m = clip_segment(m, c, (int)n);
+      const int cnt = __popc(m);
+      int incl = cnt;
+#pragma unroll
+      for (int d = 1; d < 32; d <<= 1) {
+        const int v = __shfl_up_sync(0xffffffffu, incl, d);
+        if (lane >= d) incl += v;
+      }
+      const int excl = incl - cnt;
+      for (int k = 0; k < nst; ++k) {
+        const int ck = __shfl_sync(0xffffffffu, c, k);
+        const uint32_t mk = __shfl_sync(0xffffffffu, m, k);
+        const int bk = __shfl_sync(0xffffffffu, excl, k);
+        if ((mk >> lane) & 1u) {
+          const int64_t pos = o + bk + __popc(mk & below);
+          if (pos < e) cols[pos] = ck + lane;
+        }
+      }
+    }
+    return;
+  }
   staged_fill(s, n, active, offsets, pair_capacity, cols, status, [&](auto&& emit) {
-    if (ns < 0 || ns > kMaxSegments) return;   // a dense row
+    if (ns < 0 || ns > kSearchSegments) return;   // a dense row
     for (int k = 0; k < ns; ++k) {
       const int c = seg_start[(int64_t)k * n + s];
       uint32_t w = clip_segment(seg_mask[(int64_t)k * n + s], c, (int)n);
@@ -440,19 +535,19 @@ sph_status_t sph_nl_count(const float* xy, const float* sorted_support, const fl
 }
 
 size_t sph_nl_segments_scratch_bytes(int64_t n) {
-  return (size_t)(n > 0 ? n : 0) * (kMaxSegments * (sizeof(int32_t) + sizeof(uint32_t)) + 2 * sizeof(int32_t)) +
+  return (size_t)(n > 0 ? n : 0) * (kSearchSegments * (sizeof(int32_t) + sizeof(uint32_t)) + 2 * sizeof(int32_t)) +
          256 + 16;
 }
 
-// seg_mask [kMaxSegments n], seg_start [kMaxSegments n], nseg [n], the dense list [n] and its
+// seg_mask [kSearchSegments n], seg_start [kSearchSegments n], nseg [n], the dense list [n] and its
 // count inside the scratch.
 static bool segments_from_scratch(void* scratch, size_t bytes, int64_t n, int32_t** nseg, int32_t** start,
                                   uint32_t** mask, int32_t** dense_list, int32_t** dense_count) {
   if (!scratch || bytes < sph_nl_segments_scratch_bytes(n)) return false;
   const uintptr_t p = (reinterpret_cast<uintptr_t>(scratch) + 15) & ~(uintptr_t)15;
   *mask = reinterpret_cast<uint32_t*>(p);
-  *start = reinterpret_cast<int32_t*>(*mask + (size_t)kMaxSegments * n);
-  *nseg = *start + (size_t)kMaxSegments * n;
+  *start = reinterpret_cast<int32_t*>(*mask + (size_t)kSearchSegments * n);
+  *nseg = *start + (size_t)kSearchSegments * n;
   *dense_list = *nseg + n;
   *dense_count = *dense_list + n;
   return true;

@@ -1,6 +1,7 @@
 // Device-wide exclusive scan and stable LSD radix sort (sm_103a), plus the C-ABI error
-// plumbing.  Both primitives are reduce-then-scan designs: no block ever waits on
-// another block, so there is no inter-block spin and nothing can hang.
+// plumbing.  The scan is one pass with decoupled look-back: a block waits only for tiles
+// whose blocks are already running, and every wait is bounded.  The radix sort is
+// reduce-then-scan: its blocks never wait on one another.
 #include <cstdio>
 #include <cstring>
 #include <mutex>
@@ -20,6 +21,12 @@ void set_error_text(const char* text) { snprintf(g_err, sizeof(g_err), "%s", tex
 constexpr int kScanThreads = 256;
 constexpr int kScanItems = 16;
 constexpr int kScanTile = kScanThreads * kScanItems;  // 4096
+
+// Shared-memory index of tile item i, one pad word per 32: a thread's kScanItems
+// consecutive items (i = kScanItems * t + k) and a warp's coalesced column (i = 256 k + t)
+// then both fall in 32 distinct banks.
+__device__ __forceinline__ int tpad(int i) { return i + (i >> 5); }
+constexpr int kScanTilePadded = kScanTile + kScanTile / 32;
 
 template <typename T>
 __device__ __forceinline__ T warp_incl_scan(T v) {
@@ -53,98 +60,22 @@ __device__ __forceinline__ T block_excl_scan(T v, T* smem_warp, T* total) {
   return res;
 }
 
-template <typename TOut>
-__global__ void __launch_bounds__(kScanThreads) k_scan_reduce(const int32_t* __restrict__ in, int64_t n,
-                                                              TOut* __restrict__ block_sums) {
-  __shared__ TOut sw[33];
-  const int64_t base = (int64_t)blockIdx.x * kScanTile;
-  TOut s = 0;
-#pragma unroll
-  for (int k = 0; k < kScanItems; ++k) {
-    int64_t idx = base + (int64_t)k * kScanThreads + threadIdx.x;
-    if (idx < n) s += (TOut)in[idx];
-  }
-  TOut total;
-  block_excl_scan<TOut>(s, sw, &total);
-  if (threadIdx.x == 0) block_sums[blockIdx.x] = total;
-}
-
-// Single block: exclusive scan of block_sums in place (any count, chunked).
-template <typename TOut>
-__global__ void __launch_bounds__(1024) k_scan_sums(TOut* __restrict__ sums, int64_t nb) {
-  __shared__ TOut sw[33];
-  TOut carry = 0;
-  for (int64_t base = 0; base < nb; base += blockDim.x) {
-    int64_t idx = base + threadIdx.x;
-    TOut v = idx < nb ? sums[idx] : TOut(0);
-    TOut total;
-    TOut ex = block_excl_scan<TOut>(v, sw, &total);
-    if (idx < nb) sums[idx] = ex + carry;
-    carry += total;
-  }
-  if (threadIdx.x == 0) sums[nb] = carry;
-}
-
-// Each thread owns kScanItems consecutive items (blocked layout), so a tile is read in
-// two coalesced sweeps through shared memory.
-template <typename TOut>
-__global__ void __launch_bounds__(kScanThreads) k_scan_down(const int32_t* __restrict__ in, TOut* __restrict__ out,
-                                                            int64_t n, const TOut* __restrict__ block_offsets) {
-  __shared__ TOut sw[33];
-  __shared__ int32_t tile[kScanTile];
-  const int64_t base = (int64_t)blockIdx.x * kScanTile;
-#pragma unroll
-  for (int k = 0; k < kScanItems; ++k) {
-    int64_t idx = base + (int64_t)k * kScanThreads + threadIdx.x;
-    tile[k * kScanThreads + threadIdx.x] = idx < n ? in[idx] : 0;
-  }
-  __syncthreads();
-  TOut local[kScanItems];
-  TOut s = 0;
-#pragma unroll
-  for (int k = 0; k < kScanItems; ++k) {
-    local[k] = s;
-    s += (TOut)tile[threadIdx.x * kScanItems + k];
-  }
-  TOut total;
-  TOut ex = block_excl_scan<TOut>(s, sw, &total) + block_offsets[blockIdx.x];
-  __syncthreads();
-  TOut* otile = reinterpret_cast<TOut*>(tile);  // reuse only when sizeof(TOut)==4
-  if (sizeof(TOut) == 4) {
-#pragma unroll
-    for (int k = 0; k < kScanItems; ++k) otile[threadIdx.x * kScanItems + k] = ex + local[k];
-    __syncthreads();
-#pragma unroll
-    for (int k = 0; k < kScanItems; ++k) {
-      int64_t idx = base + (int64_t)k * kScanThreads + threadIdx.x;
-      if (idx < n) out[idx] = otile[k * kScanThreads + threadIdx.x];
-    }
-  } else {
-#pragma unroll
-    for (int k = 0; k < kScanItems; ++k) {
-      int64_t idx = base + (int64_t)threadIdx.x * kScanItems + k;
-      if (idx < n) out[idx] = ex + local[k];
-    }
-  }
-  if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) out[n] = block_offsets[gridDim.x];
-}
-
 // Small scans in one launch: one block walks the tiles in order with a running carry
-// (n <= kSmallScanItems; the three-kernel scan costs two more launches, which dominate a
-// small scene's step).
-constexpr int64_t kSmallScanItems = 16 * (int64_t)kScanTile;
+// (n <= kSmallScanItems; the look-back scan needs its tile words zeroed first, one more
+// operation in a small scene's step).
+constexpr int64_t kSmallScanItems = 2 * (int64_t)kScanTile;
 
 template <typename TOut>
 __global__ void __launch_bounds__(kScanThreads) k_scan_small(const int32_t* __restrict__ in, TOut* __restrict__ out,
                                                              int64_t n) {
   __shared__ TOut sw[33];
-  __shared__ TOut tile[kScanTile];
+  __shared__ TOut tile[kScanTilePadded];
   TOut carry = 0;
   for (int64_t base = 0; base < n; base += kScanTile) {
 #pragma unroll
     for (int k = 0; k < kScanItems; ++k) {
       const int64_t idx = base + (int64_t)k * kScanThreads + threadIdx.x;
-      tile[k * kScanThreads + threadIdx.x] = idx < n ? (TOut)in[idx] : TOut(0);
+      tile[tpad(k * kScanThreads + threadIdx.x)] = idx < n ? (TOut)in[idx] : TOut(0);
     }
     __syncthreads();
     TOut local[kScanItems];
@@ -152,17 +83,17 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_small(const int32_t* __re
 #pragma unroll
     for (int k = 0; k < kScanItems; ++k) {
       local[k] = sum;
-      sum += tile[threadIdx.x * kScanItems + k];
+      sum += tile[tpad(threadIdx.x * kScanItems + k)];
     }
     TOut total;
     const TOut ex = block_excl_scan<TOut>(sum, sw, &total) + carry;
 #pragma unroll
-    for (int k = 0; k < kScanItems; ++k) tile[threadIdx.x * kScanItems + k] = ex + local[k];
+    for (int k = 0; k < kScanItems; ++k) tile[tpad(threadIdx.x * kScanItems + k)] = ex + local[k];
     __syncthreads();
 #pragma unroll
     for (int k = 0; k < kScanItems; ++k) {
       const int64_t idx = base + (int64_t)k * kScanThreads + threadIdx.x;
-      if (idx < n) out[idx] = tile[k * kScanThreads + threadIdx.x];
+      if (idx < n) out[idx] = tile[tpad(k * kScanThreads + threadIdx.x)];
     }
     carry += total;
     __syncthreads();
@@ -171,6 +102,111 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_small(const int32_t* __re
 }
 
 static int64_t scan_blocks(int64_t n) { return (n + kScanTile - 1) / kScanTile; }
+
+// Single-pass scan by decoupled look-back (Merrill and Garland, "Single-pass Parallel Prefix
+// Scan with Decoupled Look-back", 2016).  A block takes the next tile by ticket, publishes
+// the tile's total, then warp 0 walks back over the tiles before it 32 at a time, adding
+// their totals until it meets a published inclusive prefix, and publishes its own.  Tile
+// words pack a 2-bit state (0 not ready, 1 total, 2 inclusive prefix) over a 62-bit
+// two's-complement value, so state and value are stored and loaded as one 64-bit word.
+// Tile t waits only for tiles with smaller tickets: their blocks are resident and publish
+// their totals before they wait on anything, so each wait ends.  Each poll loop is still
+// bounded (kLookbackPolls); a block that gives up counts a timeout in g_scan_timeouts
+// (read by sph_scan_timeouts) and leaves its output wrong rather than spin on.
+constexpr unsigned long long kTileTotal = 1ull << 62, kTilePrefix = 2ull << 62;
+constexpr unsigned long long kTileValue = (1ull << 62) - 1;
+constexpr int kLookbackPolls = 1 << 20;
+static __device__ unsigned long long g_scan_timeouts;
+
+__device__ __forceinline__ void tile_publish(unsigned long long* w, unsigned long long v) {
+  asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(w), "l"(v) : "memory");
+}
+
+__device__ __forceinline__ unsigned long long tile_peek(const unsigned long long* w) {
+  unsigned long long v;
+  asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(w) : "memory");
+  return v;
+}
+
+__device__ __forceinline__ unsigned long long tile_word(unsigned long long state, int64_t v) {
+  return state | ((unsigned long long)v & kTileValue);
+}
+
+__device__ __forceinline__ int64_t tile_value(unsigned long long w) { return (int64_t)(w << 2) >> 2; }
+
+// tiles: ntiles zeroed words and the ticket counter after them (zeroed).
+template <typename TOut>
+__global__ void __launch_bounds__(kScanThreads) k_scan_lookback(const int32_t* __restrict__ in, TOut* __restrict__ out,
+                                                                int64_t n, unsigned long long* tiles,
+                                                                int64_t ntiles) {
+  __shared__ TOut sw[33];
+  __shared__ TOut tile[kScanTilePadded];
+  __shared__ int64_t s_t;
+  __shared__ TOut s_prefix;
+  if (threadIdx.x == 0) s_t = (int64_t)atomicAdd(tiles + ntiles, 1ull);
+  __syncthreads();
+  const int64_t t = s_t;
+  const int64_t base = t * kScanTile;
+#pragma unroll
+  for (int k = 0; k < kScanItems; ++k) {
+    const int64_t idx = base + (int64_t)k * kScanThreads + threadIdx.x;
+    tile[tpad(k * kScanThreads + threadIdx.x)] = idx < n ? (TOut)in[idx] : TOut(0);
+  }
+  __syncthreads();
+  TOut local[kScanItems];
+  TOut sum = 0;
+#pragma unroll
+  for (int k = 0; k < kScanItems; ++k) {
+    local[k] = sum;
+    sum += tile[tpad(threadIdx.x * kScanItems + k)];
+  }
+  TOut total;
+  const TOut ex = block_excl_scan<TOut>(sum, sw, &total);
+  if (threadIdx.x < 32) {
+    const int lane = threadIdx.x;
+    if (lane == 0) tile_publish(tiles + t, tile_word(t == 0 ? kTilePrefix : kTileTotal, (int64_t)total));
+    TOut excl = 0;
+    if (t > 0) {
+      int64_t j = t - 1;   // the nearest tile of this window
+      int polls = 0;
+      while (true) {
+        const int64_t k = j - lane;
+        const unsigned long long w = k >= 0 ? tile_peek(tiles + k) : kTilePrefix;
+        const unsigned long long state = w & ~kTileValue;
+        const unsigned pre = __ballot_sync(0xffffffffu, state == kTilePrefix);
+        const unsigned pending = __ballot_sync(0xffffffffu, state == 0);
+        const unsigned upto = pre ? ((pre & (0u - pre)) << 1) - 1u : 0xffffffffu;   // lanes up to the first prefix
+        if (pending & upto) {
+          if (++polls > kLookbackPolls) {
+            if (lane == 0) atomicAdd(&g_scan_timeouts, 1ull);
+            break;
+          }
+          __nanosleep(64);
+          continue;
+        }
+        TOut v = ((upto >> lane) & 1u) ? (TOut)tile_value(w) : TOut(0);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        excl += v;
+        if (pre) break;
+        j -= 32;
+      }
+      if (lane == 0) tile_publish(tiles + t, tile_word(kTilePrefix, (int64_t)(excl + total)));
+    }
+    if (lane == 0) s_prefix = excl;
+  }
+  __syncthreads();
+  const TOut off = ex + s_prefix;
+#pragma unroll
+  for (int k = 0; k < kScanItems; ++k) tile[tpad(threadIdx.x * kScanItems + k)] = off + local[k];
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < kScanItems; ++k) {
+    const int64_t idx = base + (int64_t)k * kScanThreads + threadIdx.x;
+    if (idx < n) out[idx] = tile[tpad(k * kScanThreads + threadIdx.x)];
+  }
+  if (t == ntiles - 1 && threadIdx.x == 0) out[n] = s_prefix + total;
+}
 
 template <typename TOut>
 static sph_status_t scan_impl(const int32_t* in, TOut* out, int64_t n, void* scratch, size_t scratch_bytes,
@@ -183,26 +219,28 @@ static sph_status_t scan_impl(const int32_t* in, TOut* out, int64_t n, void* scr
     return SPH_OK;
   }
   int64_t nb = scan_blocks(n);
-  if (scratch_bytes < (size_t)(nb + 1) * sizeof(int64_t) || scratch == nullptr) {
+  // the tile words are 64-bit atomics: start them on an 8-byte boundary
+  const size_t skip = scratch ? (size_t)((8 - (reinterpret_cast<uintptr_t>(scratch) & 7)) & 7) : 0;
+  if (scratch == nullptr || scratch_bytes < skip + (size_t)(nb + 1) * sizeof(int64_t)) {
     set_error_text("scan: scratch too small");
     return SPH_ERR_SCRATCH_TOO_SMALL;
   }
+  scratch = static_cast<char*>(scratch) + skip;
   if (n <= kSmallScanItems) {
     k_scan_small<TOut><<<1, kScanThreads, 0, st>>>(in, out, n);
     SPH_CHECK_LAUNCH("scan(small)");
     return SPH_OK;
   }
-  TOut* sums = reinterpret_cast<TOut*>(scratch);
-  k_scan_reduce<TOut><<<(unsigned)nb, kScanThreads, 0, st>>>(in, n, sums);
-  k_scan_sums<TOut><<<1, 1024, 0, st>>>(sums, nb);
-  k_scan_down<TOut><<<(unsigned)nb, kScanThreads, 0, st>>>(in, out, n, sums);
+  unsigned long long* tiles = reinterpret_cast<unsigned long long*>(scratch);
+  cudaMemsetAsync(tiles, 0, (size_t)(nb + 1) * sizeof(unsigned long long), st);
+  k_scan_lookback<TOut><<<(unsigned)nb, kScanThreads, 0, st>>>(in, out, n, tiles, nb);
   SPH_CHECK_LAUNCH("scan");
   return SPH_OK;
 }
 
 // ------------------------------------------------------------------ allocation-free scan
-// Scratch for sph_exclusive_scan_i32_static: one int64 block sum per 4096-item tile plus
-// the total.  64 KiB of device memory in every GPU that loads this library, held until
+// Scratch for sph_exclusive_scan_i32_static: one 64-bit tile word per 4096-item tile plus
+// the ticket counter.  64 KiB of device memory in every GPU that loads this library, held until
 // the process exits.  It caps n at (kStaticScanSlots - 1) * kScanTile = 33,550,336 items.
 constexpr int kStaticScanSlots = 8192;
 static __device__ __align__(256) int64_t g_static_scan_scratch[kStaticScanSlots];
@@ -344,7 +382,13 @@ const char* sph_status_string(sph_status_t s) {
   }
 }
 
-size_t sph_scan_scratch_bytes(int64_t n) { return (size_t)(scan_blocks(n < 1 ? 1 : n) + 1) * sizeof(int64_t); }
+uint64_t sph_scan_timeouts(void) {
+  unsigned long long v = 0;
+  if (cudaMemcpyFromSymbol(&v, g_scan_timeouts, sizeof(v)) != cudaSuccess) return ~0ull;
+  return v;
+}
+
+size_t sph_scan_scratch_bytes(int64_t n) { return (size_t)(scan_blocks(n < 1 ? 1 : n) + 2) * sizeof(int64_t); }
 
 sph_status_t sph_exclusive_scan_i32(const int32_t* in, int32_t* out, int64_t n, void* scratch, size_t scratch_bytes,
                                     void* stream) {

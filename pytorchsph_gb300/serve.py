@@ -427,13 +427,13 @@ class SceneBatch:
         self.par ^= 1             # the sorted static arrays are the state's now
 
     # kernels of this library launched by one batch step (for the bench's launch count): keys 1,
-    # counting sort (scan 1 or 3 + scatter + fix + fix_large), permute 1, [csr: count 1, scan 1
-    # or 3, fill 1], mdbc 1, records 1, per force group pass1 + update 1 (+ diffusion + update 1
-    # for a group with deltaSPH scenes).  A scan of at most 65,536 items is one launch.
+    # counting sort (scan 1 + scatter + fix + fix_large), permute 1, [csr: count 1, scan 1,
+    # fill 1], mdbc 1, records 1, per force group pass1 + update 1 (+ diffusion + update 1 for
+    # a group with deltaSPH scenes).  A scan is one kernel (above 8,192 items its tile words
+    # are zeroed by a memset first, which is not a kernel).
     def launches_per_step(self):
-        scan = lambda items: 1 if items <= 65536 else 3
-        sort = scan(self.cap + 1) + 3
-        csr = 1 + scan(self.n) + 1 if self.pairs == "csr" else 0
+        sort = 1 + 3
+        csr = 1 + 1 + 1 if self.pairs == "csr" else 0
         p1 = sum(1 for lo, hi, _, _ in self.groups if hi > lo)
         dif = sum(1 for lo, hi, _, k in self.groups if hi > lo and k not in (0, 1)) if self.any_renorm else 0
         return 1 + sort + 1 + csr + (1 if self.nb else 0) + 1 + p1 + dif

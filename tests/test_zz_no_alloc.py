@@ -3,7 +3,7 @@
 Some callers of this library cannot allocate device memory: a host runtime that reaches
 the kernels through the C ABI and only receives device pointers from whoever owns the
 GPU memory, or code that is recording a CUDA graph (cudaMalloc is not allowed while a
-stream is being captured).  For them the scan keeps its block sums in a fixed 64 KiB
+stream is being captured).  For them the scan keeps its tile words in a fixed 64 KiB
 device array inside the library instead of caller-provided scratch.  This test calls it
 through the C ABI and checks it against the scratch-taking sph_exclusive_scan_i32 (an
 integer scan: results must be identical) on consecutive calls, and checks that sizes
