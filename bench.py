@@ -608,7 +608,14 @@ def run_search_density(args, dev, world, rank):
     phases = {k: v / args.steps for k, v in phase_acc.items()} if ok else {}
     dom = max(["count", "fill"], key=lambda k: phases.get(k, 0.0)) if phases else "fill"
     kern = {"count": "nl_count", "fill": "nl_fill"}[dom]
-    alg = n * 28 + 4 * (cells + 2) if kern == "nl_count" else n * 20 + 4 * P + 4 * (cells + 2)
+    # stored segments S: the nseg array follows the 24 n masks and 24 n starts in the scratch
+    seg_words = gs.ws._bufs["segments"].view(torch.int32)
+    nseg = seg_words[48 * n:49 * n]
+    S = int(torch.clamp(nseg, min=0).sum().item())
+    # count: position 8, support 4, area 4, key 4 read; count 4, density 4, nseg 4 written; 8 per
+    # stored segment; the cell table once.  fill: key 4, nseg 4, offset 4 read, 8 per segment
+    # read, 4 per column written.
+    alg = n * 32 + 8 * S + 4 * (cells + 2) if kern == "nl_count" else n * 12 + 8 * S + 4 * P
     peak, peak_src = hbm_peak()
     achieved = alg / (phases[dom] / 1e3) / 1e9 if phases else None
     e2e_ms = []
@@ -644,7 +651,7 @@ def run_search_density(args, dev, world, rank):
             "digit_bits": args.digit_bits if args.sort == "radix" else None,
             "sort_chosen_by": "autotuner (measured in this run)" if tuned else "command line",
             "l2": "flushed between timed steps (flush not timed)", "graph": "one CUDA graph per step",
-            "parallelism": f"replicas{world}"})
+            "parallelism": f"replicas{world}", "segments": S})
         line["phases_ms"] = {k: round(v, 5) for k, v in phases.items()}
         if tuned:
             line["tuning"] = {str(b): {k: (round(x["ms"], 4) if isinstance(x, dict) else x)

@@ -255,6 +255,7 @@ __global__ void k_count_scatter(const uint32_t* __restrict__ keys, int64_t n, co
   tmp[slot] = (uint32_t)i;
 }
 
+constexpr int kRankSortMax = 1024;   // large cells up to this size are ranked in shared memory
 constexpr int kSmallCell = 48;    // cells up to this size are ordered by ranking, one thread per particle
 constexpr int kBlockSortMax = 2048;  // larger cells: one block, bitonic sort in shared memory
 
@@ -290,9 +291,11 @@ __global__ void __launch_bounds__(256) k_cell_fix(const uint32_t* __restrict__ k
   order[b + rank] = x;
 }
 
-// One block per large cell: bitonic sort of up to kBlockSortMax entries in shared memory.
-// Bigger cells keep the atomic scatter order (their pair set is unchanged; only the
-// order inside that cell is not reproducible) and flag SPH_FLAG_CELL_ORDER.
+// One block per large cell, its (tie, index) ranks in shared memory: up to kRankSortMax
+// entries each thread counts the smaller ranks of its entries (one barrier); above that a
+// bitonic sort, up to kBlockSortMax entries.  Bigger cells keep the atomic scatter order
+// (their pair set is unchanged; only the order inside that cell is not reproducible) and
+// flag SPH_FLAG_CELL_ORDER.
 __global__ void __launch_bounds__(512) k_cell_fix_large(const int32_t* __restrict__ cell_start,
                                                         const uint32_t* __restrict__ tmp,
                                                         const uint32_t* __restrict__ tie,
@@ -308,6 +311,19 @@ __global__ void __launch_bounds__(512) k_cell_fix_large(const int32_t* __restric
     if (k > kBlockSortMax) {
       for (int t = threadIdx.x; t < k; t += blockDim.x) order[b + t] = tmp[b + t];
       if (threadIdx.x == 0) flag(status, SPH_FLAG_CELL_ORDER);
+      continue;
+    }
+    if (k <= kRankSortMax) {
+      for (int t = threadIdx.x; t < k; t += blockDim.x) s[t] = cell_rank(tmp[b + t], tie);
+      __syncthreads();
+      for (int t = threadIdx.x; t < k; t += blockDim.x) {
+        const uint64_t mine = s[t];
+        int rank = 0;
+#pragma unroll 4
+        for (int u = 0; u < k; ++u) rank += s[u] < mine;   // every lane reads the same word
+        order[b + rank] = (uint32_t)(mine & 0xffffffffu);
+      }
+      __syncthreads();
       continue;
     }
     int p2 = 1;
