@@ -115,7 +115,7 @@ const char* sph_status_string(sph_status_t status);
 size_t sph_scan_scratch_bytes(int64_t n);
 /* out[k] = in[0] + ... + in[k-1] for k <= n (out has n+1 entries; out[n] = total).
  * Replaces torch::cumsum in cppSrc/neighSearch_cuda.cu:250 and the cumsums of
- * src/modules/neighborSearch.py:65,86.  Above 8,192 items: one zeroing of the scratch and
+ * src/modules/neighborSearch.py:65,86.  Above 16,384 items: one zeroing of the scratch and
  * one single-pass launch (decoupled look-back); the scratch must not be shared by scans
  * that overlap on the GPU. */
 sph_status_t sph_exclusive_scan_i32(const int32_t* in, int32_t* out, int64_t n, void* scratch,

@@ -63,7 +63,7 @@ __device__ __forceinline__ T block_excl_scan(T v, T* smem_warp, T* total) {
 // Small scans in one launch: one block walks the tiles in order with a running carry
 // (n <= kSmallScanItems; the look-back scan needs its tile words zeroed first, one more
 // operation in a small scene's step).
-constexpr int64_t kSmallScanItems = 2 * (int64_t)kScanTile;
+constexpr int64_t kSmallScanItems = 4 * (int64_t)kScanTile;
 
 template <typename TOut>
 __global__ void __launch_bounds__(kScanThreads) k_scan_small(const int32_t* __restrict__ in, TOut* __restrict__ out,

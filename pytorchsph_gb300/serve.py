@@ -429,7 +429,7 @@ class SceneBatch:
     # kernels of this library launched by one batch step (for the bench's launch count): keys 1,
     # counting sort (scan 1 + scatter + fix + fix_large), permute 1, [csr: count 1, scan 1,
     # fill 1], mdbc 1, records 1, per force group pass1 + update 1 (+ diffusion + update 1 for
-    # a group with deltaSPH scenes).  A scan is one kernel (above 8,192 items its tile words
+    # a group with deltaSPH scenes).  A scan is one kernel (above 16,384 items its tile words
     # are zeroed by a memset first, which is not a kernel).
     def launches_per_step(self):
         sort = 1 + 3

@@ -1,5 +1,5 @@
 """The exclusive scans of the C ABI against torch.cumsum at sizes around the one-block
-path's limit (2 tiles of 4096) and the tile size, int32 and int64 outputs; the
+path's limit (4 tiles of 4096) and the tile size, int32 and int64 outputs; the
 single-pass look-back scan above that limit with negative items, an unaligned scratch
 pointer, replays of a captured CUDA graph, and no look-back wait that gave up."""
 import pytest
@@ -8,7 +8,7 @@ import torch
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("n", [1, 5, 4095, 4096, 4097, 8191, 8192, 8193, 3 * 4096 + 7, 65537, 300_001])
+@pytest.mark.parametrize("n", [1, 5, 4095, 4096, 4097, 8191, 8192, 8193, 3 * 4096 + 7, 16384, 16385, 65537, 300_001])
 def test_exclusive_scans_match_cumsum(cuda, n):
     from pytorchsph_gb300 import _native as N
     lib = N.load()
