@@ -191,6 +191,17 @@ sph_status_t sph_counting_sort(const uint32_t* keys, int64_t n, int32_t cell_cap
 sph_status_t sph_counting_sort_tie(const uint32_t* keys, int64_t n, int32_t cell_capacity, int32_t* cell_count,
                                    int32_t* cell_start, const uint32_t* tie, uint32_t* order, uint32_t* sorted_keys,
                                    int32_t* status, void* scratch, size_t scratch_bytes, void* stream);
+/* sph_counting_sort_tie that also moves `count` (at most 8) per-particle arrays into the
+ * sorted order, out[k][s] = in[k][order[s]], in the same launches: the in-cell fix writes
+ * each particle's rows where it places the particle (replaces the separate
+ * sph_permute_arrays pass; the gathers of src/modules/neighborSearch.py:51-53 applied to
+ * the whole state).  elem_bytes, in and out are host arrays of `count` entries (4-, 8- or 16-byte
+ * rows); in[k] and out[k] must not overlap. */
+sph_status_t sph_counting_sort_permute(const uint32_t* keys, int64_t n, int32_t cell_capacity, int32_t* cell_count,
+                                       int32_t* cell_start, const uint32_t* tie, uint32_t* order,
+                                       uint32_t* sorted_keys, int32_t count, const int32_t* elem_bytes,
+                                       const void* const* in, void* const* out, int32_t* status, void* scratch,
+                                       size_t scratch_bytes, void* stream);
 /* cell_start[c] = first sorted index whose key >= c, for c = 0..cell_capacity+1 (the cell
  * begin table after sph_radix_sort_pairs). */
 sph_status_t sph_cell_starts(const uint32_t* sorted_keys, int64_t n, int32_t cell_capacity,

@@ -68,6 +68,7 @@ SIGNATURES = {
 
 SIGNATURES.update({  # batch of scenes
     "sph_counting_sort_tie": (_I32, [_P, _I64, _I32, _P, _P, _P, _P, _P, _P, _P, _SZ, _P]),
+    "sph_counting_sort_permute": (_I32, [_P, _I64, _I32, _P, _P, _P, _P, _P, _I32, _P, _P, _P, _P, _P, _SZ, _P]),
     "sph_scene_bytes": (_SZ, []),
     "sph_scene_encode": (_I32, [_P, _P, _I32, _F32, _P]),
     "sph_batch_cell_keys": (_I32, [_P, _I64, _P, _P, _I32, _P, _P, _P, _P]),
@@ -191,15 +192,22 @@ def stream_ptr() -> int:
     return torch.cuda.current_stream().cuda_stream
 
 
-def permute_arrays(order, pairs):
-    """out[s] = in[order[s]] (a copy when order is None) for up to 8 (in, out) tensor pairs
-    of per-particle rows, in one kernel (sph_permute_arrays)."""
+def array_set(pairs):
+    """(count, row bytes, in pointers, out pointers) of (in, out) tensor pairs of per-particle
+    rows, as the C ABI's array-set arguments take them."""
     k = len(pairs)
-    n = pairs[0][0].shape[0] if k else 0
     row = lambda t: t.element_size() * (t.shape[1] if t.dim() == 2 else 1)
     eb = (ctypes.c_int32 * k)(*[row(t) for t, _ in pairs])
     ins = (ctypes.c_void_p * k)(*[t.data_ptr() for t, _ in pairs])
     outs = (ctypes.c_void_p * k)(*[o.data_ptr() for _, o in pairs])
+    return k, eb, ins, outs
+
+
+def permute_arrays(order, pairs):
+    """out[s] = in[order[s]] (a copy when order is None) for up to 8 (in, out) tensor pairs
+    of per-particle rows, in one kernel (sph_permute_arrays)."""
+    n = pairs[0][0].shape[0] if pairs else 0
+    k, eb, ins, outs = array_set(pairs)
     call("sph_permute_arrays", ptr(order), n, k, eb, ins, outs, stream_ptr())
 
 

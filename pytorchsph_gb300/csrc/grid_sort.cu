@@ -274,7 +274,8 @@ __global__ void __launch_bounds__(256) k_cell_fix(const uint32_t* __restrict__ k
                                                   const int32_t* __restrict__ cell_start,
                                                   const uint32_t* __restrict__ tmp, const uint32_t* __restrict__ tie,
                                                   uint32_t* __restrict__ order, uint32_t* __restrict__ sorted_keys,
-                                                  int32_t* __restrict__ big_list, int32_t* __restrict__ big_count) {
+                                                  int32_t* __restrict__ big_list, int32_t* __restrict__ big_count,
+                                                  const ArraySet rows) {
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n) return;
   const uint32_t x = tmp[t];
@@ -289,6 +290,7 @@ __global__ void __launch_bounds__(256) k_cell_fix(const uint32_t* __restrict__ k
   int rank = 0;
   for (int u = b; u < e; ++u) rank += cell_rank(__ldg(tmp + u), tie) < mine;
   order[b + rank] = x;
+  copy_rows(rows, b + rank, x);
 }
 
 // One block per large cell, its (tie, index) ranks in shared memory: up to kRankSortMax
@@ -301,7 +303,8 @@ __global__ void __launch_bounds__(512) k_cell_fix_large(const int32_t* __restric
                                                         const uint32_t* __restrict__ tie,
                                                         uint32_t* __restrict__ order,
                                                         const int32_t* __restrict__ big_list,
-                                                        const int32_t* __restrict__ big_count, int32_t* status) {
+                                                        const int32_t* __restrict__ big_count, int32_t* status,
+                                                        const ArraySet rows) {
   __shared__ uint64_t s[kBlockSortMax];
   const int nbig = *big_count;
   for (int q = blockIdx.x; q < nbig; q += gridDim.x) {
@@ -309,7 +312,10 @@ __global__ void __launch_bounds__(512) k_cell_fix_large(const int32_t* __restric
     const int b = cell_start[c], e = cell_start[c + 1];
     const int k = e - b;
     if (k > kBlockSortMax) {
-      for (int t = threadIdx.x; t < k; t += blockDim.x) order[b + t] = tmp[b + t];
+      for (int t = threadIdx.x; t < k; t += blockDim.x) {
+        order[b + t] = tmp[b + t];
+        copy_rows(rows, b + t, tmp[b + t]);
+      }
       if (threadIdx.x == 0) flag(status, SPH_FLAG_CELL_ORDER);
       continue;
     }
@@ -322,6 +328,7 @@ __global__ void __launch_bounds__(512) k_cell_fix_large(const int32_t* __restric
 #pragma unroll 4
         for (int u = 0; u < k; ++u) rank += s[u] < mine;   // every lane reads the same word
         order[b + rank] = (uint32_t)(mine & 0xffffffffu);
+        copy_rows(rows, b + rank, (uint32_t)(mine & 0xffffffffu));
       }
       __syncthreads();
       continue;
@@ -346,7 +353,10 @@ __global__ void __launch_bounds__(512) k_cell_fix_large(const int32_t* __restric
         __syncthreads();
       }
     }
-    for (int t = threadIdx.x; t < k; t += blockDim.x) order[b + t] = (uint32_t)(s[t] & 0xffffffffu);
+    for (int t = threadIdx.x; t < k; t += blockDim.x) {
+      order[b + t] = (uint32_t)(s[t] & 0xffffffffu);
+      copy_rows(rows, b + t, (uint32_t)(s[t] & 0xffffffffu));
+    }
     __syncthreads();
   }
 }
@@ -534,9 +544,10 @@ sph_status_t sph_counting_sort(const uint32_t* keys, int64_t n, int32_t cell_cap
                                scratch, scratch_bytes, stream);
 }
 
-sph_status_t sph_counting_sort_tie(const uint32_t* keys, int64_t n, int32_t cell_capacity, int32_t* cell_count,
-                                   int32_t* cell_start, const uint32_t* tie, uint32_t* order, uint32_t* sorted_keys,
-                                   int32_t* status, void* scratch, size_t scratch_bytes, void* stream) {
+static sph_status_t counting_sort_impl(const uint32_t* keys, int64_t n, int32_t cell_capacity, int32_t* cell_count,
+                                       int32_t* cell_start, const uint32_t* tie, uint32_t* order,
+                                       uint32_t* sorted_keys, const ArraySet& rows, int32_t* status, void* scratch,
+                                       size_t scratch_bytes, void* stream) {
   SPH_REQUIRE(n >= 0 && n < ((int64_t)1 << 31) && keys && cell_count && cell_start && order && sorted_keys &&
                   cell_capacity > 0,
               "counting_sort: bad arguments");
@@ -563,10 +574,31 @@ sph_status_t sph_counting_sort_tie(const uint32_t* keys, int64_t n, int32_t cell
   cudaMemsetAsync(big_count, 0, sizeof(int32_t), st);
   k_count_scatter<<<grid_for(n, 256), 256, 0, st>>>(keys, n, cell_start, cell_count, tmp);
   k_cell_fix<<<grid_for(n, 256), 256, 0, st>>>(keys, n, cell_start, tmp, tie, order, sorted_keys, big_list,
-                                               big_count);
-  k_cell_fix_large<<<kNumSMs, 512, 0, st>>>(cell_start, tmp, tie, order, big_list, big_count, status);
+                                               big_count, rows);
+  k_cell_fix_large<<<kNumSMs, 512, 0, st>>>(cell_start, tmp, tie, order, big_list, big_count, status, rows);
   SPH_CHECK_LAUNCH("counting_sort");
   return SPH_OK;
+}
+
+sph_status_t sph_counting_sort_tie(const uint32_t* keys, int64_t n, int32_t cell_capacity, int32_t* cell_count,
+                                   int32_t* cell_start, const uint32_t* tie, uint32_t* order, uint32_t* sorted_keys,
+                                   int32_t* status, void* scratch, size_t scratch_bytes, void* stream) {
+  ArraySet none;
+  array_set_from(0, nullptr, nullptr, nullptr, &none);
+  return counting_sort_impl(keys, n, cell_capacity, cell_count, cell_start, tie, order, sorted_keys, none, status,
+                            scratch, scratch_bytes, stream);
+}
+
+sph_status_t sph_counting_sort_permute(const uint32_t* keys, int64_t n, int32_t cell_capacity, int32_t* cell_count,
+                                       int32_t* cell_start, const uint32_t* tie, uint32_t* order,
+                                       uint32_t* sorted_keys, int32_t count, const int32_t* elem_bytes,
+                                       const void* const* in, void* const* out, int32_t* status, void* scratch,
+                                       size_t scratch_bytes, void* stream) {
+  ArraySet rows;
+  SPH_REQUIRE(array_set_from(count, elem_bytes, in, out, &rows),
+              "counting_sort_permute: at most 8 arrays, each with distinct in/out and 4, 8 or 16-byte rows");
+  return counting_sort_impl(keys, n, cell_capacity, cell_count, cell_start, tie, order, sorted_keys, rows, status,
+                            scratch, scratch_bytes, stream);
 }
 
 sph_status_t sph_cell_starts(const uint32_t* sorted_keys, int64_t n, int32_t cell_capacity, int32_t* cell_start,

@@ -105,6 +105,56 @@ __device__ __forceinline__ bool grid_ok(const sph_grid& g, int32_t cap) {
   return g.num_cells <= cap && g.cells_x > 0 && g.cells_y > 0;
 }
 
+// Up to kMaxArrays per-particle arrays moved together into a new order (4-, 8- or 16-byte
+// rows): the permute kernel and the counting sort's in-cell fix copy row src of every
+// in[k] to row dst of out[k].
+constexpr int kMaxArrays = 8;
+struct ArraySet {
+  const void* in[kMaxArrays];
+  void* out[kMaxArrays];
+  int32_t bytes[kMaxArrays];
+  int32_t count;
+};
+
+// The set from host arrays of `count` entries; false for a count above kMaxArrays, a
+// missing or shared in/out pointer, or a row size other than 4, 8 or 16 bytes.
+inline bool array_set_from(int32_t count, const int32_t* elem_bytes, const void* const* in, void* const* out,
+                           ArraySet* a) {
+  if (count < 0 || count > kMaxArrays || (count > 0 && (!elem_bytes || !in || !out))) return false;
+  a->count = count;
+  for (int k = 0; k < kMaxArrays; ++k) {
+    a->in[k] = nullptr;
+    a->out[k] = nullptr;
+    a->bytes[k] = 4;
+  }
+  for (int k = 0; k < count; ++k) {
+    if (!in[k] || !out[k] || in[k] == out[k] || (elem_bytes[k] != 4 && elem_bytes[k] != 8 && elem_bytes[k] != 16))
+      return false;
+    a->in[k] = in[k];
+    a->out[k] = out[k];
+    a->bytes[k] = elem_bytes[k];
+  }
+  return true;
+}
+
+__device__ __forceinline__ void copy_rows(const ArraySet& a, int64_t dst, int64_t src) {
+#pragma unroll
+  for (int k = 0; k < kMaxArrays; ++k) {
+    if (k >= a.count) break;
+    switch (a.bytes[k]) {
+      case 4:
+        static_cast<uint32_t*>(a.out[k])[dst] = static_cast<const uint32_t*>(a.in[k])[src];
+        break;
+      case 8:
+        static_cast<uint2*>(a.out[k])[dst] = static_cast<const uint2*>(a.in[k])[src];
+        break;
+      default:
+        static_cast<uint4*>(a.out[k])[dst] = static_cast<const uint4*>(a.in[k])[src];
+        break;
+    }
+  }
+}
+
 __device__ __forceinline__ void flag(int32_t* status, int32_t f) {
   if (status) atomicOr(status, f);
 }

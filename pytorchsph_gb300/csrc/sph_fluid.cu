@@ -681,33 +681,10 @@ __global__ void k_permute(const uint32_t* __restrict__ order, int n, const T* __
 
 // Up to kMaxArrays per-particle arrays gathered in one pass: out_k[s] = in_k[order[s]], or
 // a plain copy when order is null.  One launch reads order once instead of once per array.
-constexpr int kMaxArrays = 8;
-struct ArraySet {
-  const void* in[kMaxArrays];
-  void* out[kMaxArrays];
-  int32_t bytes[kMaxArrays];
-  int32_t count;
-};
-
 __global__ void __launch_bounds__(256) k_permute_arrays(const uint32_t* __restrict__ order, int n, ArraySet a) {
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= n) return;
-  const int src = order ? (int)order[s] : s;
-#pragma unroll
-  for (int k = 0; k < kMaxArrays; ++k) {
-    if (k >= a.count) break;
-    switch (a.bytes[k]) {
-      case 4:
-        static_cast<uint32_t*>(a.out[k])[s] = static_cast<const uint32_t*>(a.in[k])[src];
-        break;
-      case 8:
-        static_cast<uint2*>(a.out[k])[s] = static_cast<const uint2*>(a.in[k])[src];
-        break;
-      default:
-        static_cast<uint4*>(a.out[k])[s] = static_cast<const uint4*>(a.in[k])[src];
-        break;
-    }
-  }
+  copy_rows(a, s, order ? (int)order[s] : s);
 }
 
 }  // namespace sph
@@ -940,20 +917,8 @@ sph_status_t sph_permute_arrays(const uint32_t* order, int64_t n, int32_t count,
               "permute_arrays: bad arguments");
   if (n == 0 || count == 0) return SPH_OK;
   ArraySet a;
-  a.count = count;
-  for (int k = 0; k < kMaxArrays; ++k) {
-    a.in[k] = nullptr;
-    a.out[k] = nullptr;
-    a.bytes[k] = 4;
-  }
-  for (int k = 0; k < count; ++k) {
-    SPH_REQUIRE(in[k] && out[k] && in[k] != out[k] &&
-                    (elem_bytes[k] == 4 || elem_bytes[k] == 8 || elem_bytes[k] == 16),
-                "permute_arrays: each array needs distinct in/out and 4, 8 or 16-byte elements");
-    a.in[k] = in[k];
-    a.out[k] = out[k];
-    a.bytes[k] = elem_bytes[k];
-  }
+  SPH_REQUIRE(array_set_from(count, elem_bytes, in, out, &a),
+              "permute_arrays: each array needs distinct in/out and 4, 8 or 16-byte elements");
   k_permute_arrays<<<grid_for(n, 256), 256, 0, as_stream(stream)>>>(order, (int)n, a);
   SPH_CHECK_LAUNCH("permute_arrays");
   return SPH_OK;

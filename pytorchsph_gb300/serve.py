@@ -363,11 +363,12 @@ class SceneBatch:
                N.ptr(self.keys), N.ptr(self.hist), N.ptr(self.status), st)
         # inside a cell, order by particle id: a scene's order never depends on its history
         # or on the other scenes of the batch
-        N.call("sph_counting_sort_tie", N.ptr(self.keys), n, self.cap, N.ptr(self.hist), N.ptr(self.cell_start),
-               N.ptr(cur["uid"]), N.ptr(self.order), N.ptr(self.skeys), N.ptr(self.status),
+        # the state moves into the sorted order in the same launches
+        k, eb, ins, outs = N.array_set([(self.a[k], self.b[k]) for k in ("x", "v", "rho")] +
+                                       [(cur[k], nxt[k]) for k in self.AUX])
+        N.call("sph_counting_sort_permute", N.ptr(self.keys), n, self.cap, N.ptr(self.hist), N.ptr(self.cell_start),
+               N.ptr(cur["uid"]), N.ptr(self.order), N.ptr(self.skeys), k, eb, ins, outs, N.ptr(self.status),
                N.ptr(self.cs_scratch), self.cs_scratch.numel() * 8, st)
-        N.permute_arrays(self.order, [(self.a[k], self.b[k]) for k in ("x", "v", "rho")] +
-                         [(cur[k], nxt[k]) for k in self.AUX])
         self.s = {"x": self.b["x"], "v": self.b["v"], "rho": self.b["rho"], **{k: nxt[k] for k in self.AUX}}
 
     def _count(self):
@@ -427,16 +428,16 @@ class SceneBatch:
         self.par ^= 1             # the sorted static arrays are the state's now
 
     # kernels of this library launched by one batch step (for the bench's launch count): keys 1,
-    # counting sort (scan 1 + scatter + fix + fix_large), permute 1, [csr: count 1, scan 1,
-    # fill 1], mdbc 1, records 1, per force group pass1 + update 1 (+ diffusion + update 1 for
-    # a group with deltaSPH scenes).  A scan is one kernel (above 16,384 items its tile words
+    # counting sort with the state's permute (scan 1 + scatter + fix + fix_large), [csr: count
+    # 1, scan 1, fill 1], mdbc 1, records 1, per force group pass1 + update 1 (+ diffusion +
+    # update 1 for a group with deltaSPH scenes).  A scan is one kernel (above 16,384 items its tile words
     # are zeroed by a memset first, which is not a kernel).
     def launches_per_step(self):
         sort = 1 + 3
         csr = 1 + 1 + 1 if self.pairs == "csr" else 0
         p1 = sum(1 for lo, hi, _, _ in self.groups if hi > lo)
         dif = sum(1 for lo, hi, _, k in self.groups if hi > lo and k not in (0, 1)) if self.any_renorm else 0
-        return 1 + sort + 1 + csr + (1 if self.nb else 0) + 1 + p1 + dif
+        return 1 + sort + csr + (1 if self.nb else 0) + 1 + p1 + dif
 
     def capture(self):
         """Capture one batch step into a CUDA graph (after a warm-up step)."""
