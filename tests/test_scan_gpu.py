@@ -1,7 +1,7 @@
 """The exclusive scans of the C ABI against torch.cumsum at sizes around the one-block
 path's limit (4 tiles of 4096) and the tile size, int32 and int64 outputs; the
-single-pass look-back scan above that limit with negative items, an unaligned scratch
-pointer, replays of a captured CUDA graph, and no look-back wait that gave up."""
+single-pass look-back scan above that limit with negative items, unaligned scratch, input
+and output pointers, replays of a captured CUDA graph, and no look-back wait that gave up."""
 import pytest
 import torch
 
@@ -72,3 +72,20 @@ def test_lookback_scan_in_cuda_graph(cuda):
         torch.cuda.synchronize()
         assert torch.equal(out.long(), _cumsum(x))
     assert lib.sph_scan_timeouts() == 0
+
+
+def test_lookback_scan_unaligned_input_and_output(cuda):
+    """Input and output pointers 4 bytes past a 16-byte boundary: the same result."""
+    from pytorchsph_gb300 import _native as N
+    lib = N.load()
+    n = 1_000_001
+    g = torch.Generator().manual_seed(3)
+    xs = torch.randint(0, 100, (n + 1,), generator=g, dtype=torch.int32).to(cuda)
+    x = xs[1:]
+    ref = _cumsum(x)
+    o = torch.full((n + 2,), -1, dtype=torch.int32, device=cuda)
+    scratch = torch.empty((lib.sph_scan_scratch_bytes(n) + 7) // 8, dtype=torch.int64, device=cuda)
+    N.call("sph_exclusive_scan_i32", x.data_ptr(), o.data_ptr() + 4, n, N.ptr(scratch), scratch.numel() * 8,
+           N.stream_ptr())
+    torch.cuda.synchronize()
+    assert torch.equal(o[1:].long(), ref)
