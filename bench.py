@@ -608,10 +608,7 @@ def run_search_density(args, dev, world, rank):
     phases = {k: v / args.steps for k, v in phase_acc.items()} if ok else {}
     dom = max(["count", "fill"], key=lambda k: phases.get(k, 0.0)) if phases else "fill"
     kern = {"count": "nl_count", "fill": "nl_fill"}[dom]
-    # stored segments S: the nseg array follows the 24 n masks and 24 n starts in the scratch
-    seg_words = gs.ws._bufs["segments"].view(torch.int32)
-    nseg = seg_words[48 * n:49 * n]
-    S = int(torch.clamp(nseg, min=0).sum().item())
+    S = gs.stored_segments(n)
     # count: position 8, support 4, area 4, key 4 read; count 4, density 4, nseg 4 written; 8 per
     # stored segment; the cell table once.  fill: key 4, nseg 4, offset 4 read, 8 per segment
     # read, 4 per column written.

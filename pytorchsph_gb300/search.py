@@ -208,6 +208,13 @@ class GridSearch:
                              f"(domain / support ratio too large for the dense cell table)")
         return max(info["num_cells"], 1)
 
+    def stored_segments(self, n: int) -> int:
+        """Segments (start, 32-candidate mask) the last segment search of n particles kept,
+        summed over the particles (particles on the dense list count none).  The per-particle
+        counts follow the 24 n masks and 24 n starts in the segment scratch."""
+        words = self.ws.bytes("segments", N.load().sph_nl_segments_scratch_bytes(n)).view(torch.int32)
+        return int(torch.clamp(words[48 * n:49 * n], min=0).sum().item())
+
     def run(self, pos, support, area=None, kernel_support=None, min_coord=None, max_coord=None,
             search_radius: int = 1, cell_capacity: int | None = None, pair_capacity: int | None = None,
             density: bool = True, sync: bool = True, marks=None) -> CSRNeighbors:

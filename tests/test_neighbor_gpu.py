@@ -196,8 +196,8 @@ def test_sort_variants_agree(cuda):
 def test_segment_fill_equals_two_pass_fill(cuda):
     """The count pass that keeps its accepted-candidate masks and the fill that expands them
     give the same counts, density and CSR as the two-pass search that tests every candidate
-    twice, including particles with more than 8 segments (dense blob: up to ~300 neighbors,
-    so those rows are scanned again by the fill)."""
+    twice, including particles with more than 8 segments (blob: up to ~300 neighbors) and
+    blocks whose columns exceed the fill's shared-memory stage."""
     from pytorchsph_gb300.search import GridSearch
     from pytorchsph_gb300 import workloads
     dev = torch.device("cuda")
@@ -212,6 +212,49 @@ def test_segment_fill_equals_two_pass_fill(cuda):
     assert torch.equal(a.counts, b.counts) and torch.equal(a.offsets, b.offsets)
     assert torch.equal(a.cols[:a.num_pairs], b.cols[:b.num_pairs])
     assert torch.equal(a.rho, b.rho)
+
+
+def _host_segments(res, n):
+    """Non-empty 32-candidate segments of each particle's cell rows, counted on the host from
+    the CSR rows and the cell table (radius 1); particles with more than 24 count none."""
+    from pytorchsph_gb300.search import grid_from_bytes
+    g = grid_from_bytes(res.grid)
+    cx_n = g["cells_x"]
+    keys = res.keys[:n].long().cpu().numpy()
+    cs = res.cell_start.long().cpu().numpy()
+    off = res.offsets[:n + 1].long().cpu().numpy()
+    cols = res.cols[:res.num_pairs].long().cpu().numpy()
+    owner = np.repeat(np.arange(n), np.diff(off))
+    x0 = np.maximum(keys % cx_n - 1, 0)[owner]
+    row = keys[cols] // cx_n                        # the cell row of each neighbor
+    b = cs[row * cx_n + x0]
+    seg = (cols - b) // 32
+    code = np.unique((owner.astype(np.int64) * 4096 + row) * 4096 + seg)
+    per = np.bincount(code // (4096 * 4096), minlength=n)
+    return int(per[per <= 24].sum()), int((per > 24).sum())
+
+
+def test_dense_rows_and_stored_segments(cuda):
+    """A tight blob puts particles past the 24 kept segments (their rows go to the dense
+    warp-per-particle fill): the segment search still equals the two-pass search, and
+    stored_segments matches the segments counted on the host."""
+    from pytorchsph_gb300.search import GridSearch
+    from pytorchsph_gb300 import workloads
+    dev = torch.device("cuda")
+    n = 20000
+    pos = torch.from_numpy(workloads.gaussian_uniform_mix(n, 0.03, (0.5, 0.5), 4)).to(dev)
+    h = torch.full((n,), 0.012, device=dev)
+    area = torch.full((n,), 1.0 / n, device=dev)
+    kw = dict(kernel_support=0.012, min_coord=[0, 0], max_coord=[1, 1])
+    gs = GridSearch(dev, segments=True)
+    a = gs.run(pos, h, area, **kw)
+    b = GridSearch(dev, segments=False).run(pos, h, area, **kw)
+    assert torch.equal(a.counts, b.counts) and torch.equal(a.offsets, b.offsets)
+    assert torch.equal(a.cols[:a.num_pairs], b.cols[:b.num_pairs])
+    assert torch.equal(a.rho, b.rho)
+    kept, dense = _host_segments(a, n)
+    assert dense > 0
+    assert gs.stored_segments(n) == kept
 
 
 def test_counting_sort_large_cells(cuda):
