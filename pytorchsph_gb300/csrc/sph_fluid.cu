@@ -525,7 +525,7 @@ __global__ void k_sie(int n, const float2* __restrict__ x, const float2* __restr
 
 // ---------------------------------------------------------------------------- batch of scenes
 // scenes[sid[i]] gives particle i's grid, parameters, cell-table offset and time step.
-__global__ void __launch_bounds__(128) k_batch_mdbc(FluidView F, WallView W, const SceneDev* __restrict__ scenes,
+__global__ void __launch_bounds__(128, 8) k_batch_mdbc(FluidView F, WallView W, const SceneDev* __restrict__ scenes,
                                                     const int32_t* __restrict__ wsid) {
   int b = blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= W.n) return;

@@ -142,38 +142,9 @@ __device__ __forceinline__ float4 pinv2x2_fast(float a, float b, float c, float 
 // x = pinv(A) b for a 3x3 A in double (torch.linalg.pinv semantics: singular values below
 // 3 * FLT_EPSILON * sigma_max are dropped).  Eigen-decomposition of A^T A by cyclic Jacobi
 // rotations (at most 16 sweeps), then pinv(A) b = sum_k v_k ((A v_k) . b) / sigma_k^2.
-__device__ inline void pinv3_solve(const double A[3][3], const double b[3], double x[3]) {
-  // Well-conditioned A (Frobenius condition bound ||A|| ||A^-1|| below 1e5, far under the
-  // 1/(3 FLT_EPSILON) at which a singular value would be dropped): pinv(A) = A^-1, applied
-  // through the adjugate.  This is the common case and costs ~50 double operations instead
-  // of the Jacobi sweeps (GB300's FP64 rate is low).
-  {
-    // cofactors a*b - c*d as fma(a, b, -(c*d)): two double operations each
-    const auto cof = [](double a, double b, double c, double d) { return fma(a, b, -(c * d)); };
-    const double c00 = cof(A[1][1], A[2][2], A[1][2], A[2][1]), c01 = cof(A[1][2], A[2][0], A[1][0], A[2][2]),
-                 c02 = cof(A[1][0], A[2][1], A[1][1], A[2][0]);
-    const double c10 = cof(A[0][2], A[2][1], A[0][1], A[2][2]), c11 = cof(A[0][0], A[2][2], A[0][2], A[2][0]),
-                 c12 = cof(A[0][1], A[2][0], A[0][0], A[2][1]);
-    const double c20 = cof(A[0][1], A[1][2], A[0][2], A[1][1]), c21 = cof(A[0][2], A[1][0], A[0][0], A[1][2]),
-                 c22 = cof(A[0][0], A[1][1], A[0][1], A[1][0]);
-    const double det = fma(A[0][0], c00, fma(A[0][1], c01, A[0][2] * c02));
-    // The bound only decides between two exact-enough paths: its norms run in float.
-    float na = 0.f;
-    for (int r = 0; r < 3; ++r)
-      for (int c = 0; c < 3; ++c) na += (float)A[r][c] * (float)A[r][c];
-    const float f00 = (float)c00, f01 = (float)c01, f02 = (float)c02, f10 = (float)c10, f11 = (float)c11,
-                f12 = (float)c12, f20 = (float)c20, f21 = (float)c21, f22 = (float)c22;
-    const float nc = f00 * f00 + f01 * f01 + f02 * f02 + f10 * f10 + f11 * f11 + f12 * f12 + f20 * f20 +
-                     f21 * f21 + f22 * f22;
-    // ||A^-1||_F = ||adj A||_F / |det|
-    if (det != 0.0 && (double)na * (double)nc < 1e10 * det * det) {
-      const double id = 1.0 / det;  // A^-1 = adj(A) / det, adj(A)[r][c] = cofactor c_cr
-      x[0] = fma(c00, b[0], fma(c10, b[1], c20 * b[2])) * id;
-      x[1] = fma(c01, b[0], fma(c11, b[1], c21 * b[2])) * id;
-      x[2] = fma(c02, b[0], fma(c12, b[1], c22 * b[2])) * id;
-      return;
-    }
-  }
+// Kept out of line: its arrays would otherwise set the register count of every caller's
+// common path (pinv3_solve below).
+static __device__ __noinline__ void pinv3_solve_jacobi(const double A[3][3], const double b[3], double x[3]) {
   double S[3][3];
   for (int r = 0; r < 3; ++r)
     for (int c = 0; c < 3; ++c) S[r][c] = A[0][r] * A[0][c] + A[1][r] * A[1][c] + A[2][r] * A[2][c];
@@ -218,6 +189,41 @@ __device__ inline void pinv3_solve(const double A[3][3], const double b[3], doub
     double coef = (av[0] * b[0] + av[1] * b[1] + av[2] * b[2]) / (sig * sig);
     for (int r = 0; r < 3; ++r) x[r] += V[r][k] * coef;
   }
+}
+
+__device__ inline void pinv3_solve(const double A[3][3], const double b[3], double x[3]) {
+  // Well-conditioned A (Frobenius condition bound ||A|| ||A^-1|| below 1e5, far under the
+  // 1/(3 FLT_EPSILON) at which a singular value would be dropped): pinv(A) = A^-1, applied
+  // through the adjugate.  This is the common case and costs ~50 double operations instead
+  // of the Jacobi sweeps (GB300's FP64 rate is low).
+  {
+    // cofactors a*b - c*d as fma(a, b, -(c*d)): two double operations each
+    const auto cof = [](double a, double b, double c, double d) { return fma(a, b, -(c * d)); };
+    const double c00 = cof(A[1][1], A[2][2], A[1][2], A[2][1]), c01 = cof(A[1][2], A[2][0], A[1][0], A[2][2]),
+                 c02 = cof(A[1][0], A[2][1], A[1][1], A[2][0]);
+    const double c10 = cof(A[0][2], A[2][1], A[0][1], A[2][2]), c11 = cof(A[0][0], A[2][2], A[0][2], A[2][0]),
+                 c12 = cof(A[0][1], A[2][0], A[0][0], A[2][1]);
+    const double c20 = cof(A[0][1], A[1][2], A[0][2], A[1][1]), c21 = cof(A[0][2], A[1][0], A[0][0], A[1][2]),
+                 c22 = cof(A[0][0], A[1][1], A[0][1], A[1][0]);
+    const double det = fma(A[0][0], c00, fma(A[0][1], c01, A[0][2] * c02));
+    // The bound only decides between two exact-enough paths: its norms run in float.
+    float na = 0.f;
+    for (int r = 0; r < 3; ++r)
+      for (int c = 0; c < 3; ++c) na += (float)A[r][c] * (float)A[r][c];
+    const float f00 = (float)c00, f01 = (float)c01, f02 = (float)c02, f10 = (float)c10, f11 = (float)c11,
+                f12 = (float)c12, f20 = (float)c20, f21 = (float)c21, f22 = (float)c22;
+    const float nc = f00 * f00 + f01 * f01 + f02 * f02 + f10 * f10 + f11 * f11 + f12 * f12 + f20 * f20 +
+                     f21 * f21 + f22 * f22;
+    // ||A^-1||_F = ||adj A||_F / |det|
+    if (det != 0.0 && (double)na * (double)nc < 1e10 * det * det) {
+      const double id = 1.0 / det;  // A^-1 = adj(A) / det, adj(A)[r][c] = cofactor c_cr
+      x[0] = fma(c00, b[0], fma(c10, b[1], c20 * b[2])) * id;
+      x[1] = fma(c01, b[0], fma(c11, b[1], c21 * b[2])) * id;
+      x[2] = fma(c02, b[0], fma(c12, b[1], c22 * b[2])) * id;
+      return;
+    }
+  }
+  pinv3_solve_jacobi(A, b, x);
 }
 
 // Iterate the wall particles whose cell is within +-r of fluid cell (cx, cy) and that pass
