@@ -54,13 +54,17 @@ __device__ __forceinline__ void mdbc_body(int b, const FluidView& F, const WallV
           for (int j = j0; j < j1; ++j) {
             const float2 xj = F.x[j];
             if (!(dist2_ref(xg.x, xg.y, xj.x, xj.y) <= thr)) continue;
-            const Geo e = geo(xg.x, xg.y, xj.x, xj.y, P.inv_h);   // e = (x_g - x_j)/r
-            const float k = kW(e.q, P.c_w);
-            const float gw = kGW(e.q, P.c_g);
-            const float ggx = gw * e.ex, ggy = gw * e.ey;
+            // e = (x_g - x_j) / r from one rsqrt (zero below r = 1e-7, as the reference's e_ij)
+            const float dx = xg.x - xj.x, dy = xg.y - xj.y;
+            const float r2 = dx * dx + dy * dy;
+            const float ir = r2 >= 1e-14f ? rsqrtf(r2) : 0.f;
+            const float q = r2 * ir * P.inv_h;
+            const float k = kW(q, P.c_w);
+            const float gwr = kGW(q, P.c_g) * ir;
+            const float ggx = gwr * dx, ggy = gwr * dy;
             const float Aj = F.area[j];
             const float mass = Aj * P.rho0;
-            const float Vj = Aj / F.rho[j];
+            const float Vj = __fdividef(Aj, F.rho[j]);
             const float xx = xj.x - xg.x, xy = xj.y - xg.y;
             nom += mass * k;
             den += Vj * k;
