@@ -274,17 +274,21 @@ __device__ __forceinline__ uint32_t segment_mask(const float2* __restrict__ x, i
   const int len = min(e - c, 32);
   uint32_t m = 0;
   const float2 qx = make_float2(xi, xi), qy = make_float2(yi, yi);
-  int t = 0;
-  for (; t + 1 < len; t += 2) {
-    const float2 a = __ldg(x + c + t), b = __ldg(x + c + t + 1);
-    const float2 dx = __fadd2_rn(qx, make_float2(-a.x, -b.x));
-    const float2 dy = __fadd2_rn(qy, make_float2(-a.y, -b.y));
-    const float2 v = __ffma2_rn(dx, dx, __fmul2_rn(dy, dy));
-    m |= ((uint32_t)(v.x <= thr) | ((uint32_t)(v.y <= thr) << 1)) << t;
-  }
-  if (t < len) {
-    const float2 a = __ldg(x + c + t);
-    m |= (uint32_t)(dist2_ref(xi, yi, a.x, a.y) <= thr) << t;
+  // unrolled over the segment's 16 candidate pairs, each guarded by the length: every bit
+  // position is a constant, so a candidate costs its test and one predicated OR
+#pragma unroll
+  for (int t = 0; t < 32; t += 2) {
+    if (t + 1 < len) {
+      const float2 a = __ldg(x + c + t), b = __ldg(x + c + t + 1);
+      const float2 dx = __fadd2_rn(qx, make_float2(-a.x, -b.x));
+      const float2 dy = __fadd2_rn(qy, make_float2(-a.y, -b.y));
+      const float2 v = __ffma2_rn(dx, dx, __fmul2_rn(dy, dy));
+      if (v.x <= thr) m |= 1u << t;
+      if (v.y <= thr) m |= 2u << t;
+    } else if (t < len) {
+      const float2 a = __ldg(x + c + t);
+      if (dist2_ref(xi, yi, a.x, a.y) <= thr) m |= 1u << t;
+    }
   }
   return m;
 }
