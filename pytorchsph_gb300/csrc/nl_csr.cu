@@ -17,22 +17,40 @@ namespace sph {
 // up to 8 x 32 candidates each, ~9x the density of a jittered lattice at support 3 dx.
 constexpr int kSearchSegments = 24;
 
-// Density terms of the accepted candidates of one segment (the set bits of w, candidate
-// c-1+bit), added to acc in index order (the caller scales the sum by c_w).  Distance
-// r = v * rsqrt(max(v, 1e-30)): 0 for the particle itself, within a few ulp of sqrt(v)
-// otherwise.  W(q) / c_w = (1-q)^4 (1+4q), src/kernels.py:20-24.
-__device__ __forceinline__ void density_segment(const float2* __restrict__ xy, const float* __restrict__ sa, int c,
-                                                uint32_t w, float xi, float yi, float inv_support, float& acc) {
-  while (w) {
-    const int j = c - 1 + __ffs(w);
-    w &= w - 1;
-    const float2 pj = __ldg(xy + j);
-    const float v = dist2_ref(xi, yi, pj.x, pj.y);
-    const float q = v * (rsqrtf(fmaxf(v, 1e-30f)) * inv_support);
-    const float a = 1.f - q;
-    const float a2 = a * a;
-    acc += a2 * a2 * (1.f + 4.f * q) * __ldg(sa + j);
+// segment_mask with the density terms of the accepted candidates added to acc in index
+// order, in the same unrolled pass: the terms of a candidate pair are formed together on
+// the paired float32 instructions and only the accepted ones are added (the caller scales
+// the sum by c_w).  Distance r = v * rsqrt(max(v, 1e-30)): 0 for the particle itself,
+// within a few ulp of sqrt(v) otherwise.  W(q) / c_w = (1-q)^4 (1+4q), src/kernels.py:20-24.
+__device__ __forceinline__ uint32_t segment_mask_density(const float2* __restrict__ x, const float* __restrict__ sa,
+                                                         int c, int e, float xi, float yi, float thr,
+                                                         float inv_support, float& acc) {
+  const int len = min(e - c, 32);
+  uint32_t m = 0;
+  const float2 qx = make_float2(xi, xi), qy = make_float2(yi, yi), is2 = make_float2(inv_support, inv_support);
+#pragma unroll
+  for (int t = 0; t < 32; t += 2) {
+    if (t < len) {
+      const bool two = t + 1 < len;
+      const float2 a = __ldg(x + c + t), b = two ? __ldg(x + c + t + 1) : a;
+      const float2 dx = __fadd2_rn(qx, make_float2(-a.x, -b.x));
+      const float2 dy = __fadd2_rn(qy, make_float2(-a.y, -b.y));
+      const float2 v = __ffma2_rn(dx, dx, __fmul2_rn(dy, dy));
+      const bool in0 = v.x <= thr, in1 = two && v.y <= thr;
+      if (in0) m |= 1u << t;
+      if (in1) m |= 2u << t;
+      if (in0 || in1) {
+        const float2 rs = __fmul2_rn(make_float2(rsqrtf(fmaxf(v.x, 1e-30f)), rsqrtf(fmaxf(v.y, 1e-30f))), is2);
+        const float2 q = __fmul2_rn(v, rs);
+        const float2 am = __fadd2_rn(make_float2(1.f, 1.f), make_float2(-q.x, -q.y));
+        const float2 a2 = __fmul2_rn(am, am);
+        const float2 w = __fmul2_rn(__fmul2_rn(a2, a2), __ffma2_rn(make_float2(4.f, 4.f), q, make_float2(1.f, 1.f)));
+        if (in0) acc = fmaf(w.x, __ldg(sa + c + t), acc);
+        if (in1) acc = fmaf(w.y, __ldg(sa + c + t + 1), acc);
+      }
+    }
   }
+  return m;
 }
 
 template <typename F>
@@ -78,9 +96,7 @@ __global__ void __launch_bounds__(256) k_nl_count(const float2* __restrict__ xy,
         const int row = yy * g.cells_x;
         const int b = __ldg(cell_start + row + x0), e = __ldg(cell_start + row + x1 + 1);
         for (int c = b; c < e; c += 32) {
-          const uint32_t w = segment_mask(xy, c, e, pi.x, pi.y, thr);
-          cnt += __popc(w);
-          density_segment(xy, sa, c, w, pi.x, pi.y, inv_support, acc);
+          cnt += __popc(segment_mask_density(xy, sa, c, e, pi.x, pi.y, thr, inv_support, acc));
         }
       }
       acc *= c_w;
@@ -205,7 +221,8 @@ __global__ void __launch_bounds__(256) k_nl_segments(const float2* __restrict__ 
       const int row = yy * g.cells_x;
       const int b = __ldg(cell_start + row + x0), e = __ldg(cell_start + row + x1 + 1);
       for (int c = b; c < e; c += 32) {
-        uint32_t w = segment_mask(xy, c, e, pi.x, pi.y, thr);
+        uint32_t w = rho ? segment_mask_density(xy, sa, c, e, pi.x, pi.y, thr, inv_support, acc)
+                         : segment_mask(xy, c, e, pi.x, pi.y, thr);
         if (w == 0) continue;
         if (k < kSearchSegments) {
           seg_start[(int64_t)k * n + s] = c;
@@ -213,7 +230,6 @@ __global__ void __launch_bounds__(256) k_nl_segments(const float2* __restrict__ 
         }
         ++k;
         cnt += __popc(w);
-        if (rho) density_segment(xy, sa, c, w, pi.x, pi.y, inv_support, acc);
       }
     }
   }
