@@ -575,7 +575,7 @@ static sph_status_t counting_sort_impl(const uint32_t* keys, int64_t n, int32_t 
   k_count_scatter<<<grid_for(n, 256), 256, 0, st>>>(keys, n, cell_start, cell_count, tmp);
   k_cell_fix<<<grid_for(n, 256), 256, 0, st>>>(keys, n, cell_start, tmp, tie, order, sorted_keys, big_list,
                                                big_count, rows);
-  k_cell_fix_large<<<kNumSMs, 512, 0, st>>>(cell_start, tmp, tie, order, big_list, big_count, status, rows);
+  k_cell_fix_large<<<4 * kNumSMs, 512, 0, st>>>(cell_start, tmp, tie, order, big_list, big_count, status, rows);
   SPH_CHECK_LAUNCH("counting_sort");
   return SPH_OK;
 }
