@@ -127,16 +127,20 @@ sph_status_t sph_exclusive_scan_i32_to_i64(const int32_t* in, int64_t* out, int6
 uint64_t sph_scan_timeouts(void);
 
 /* Allocation-free variant of sph_exclusive_scan_i32.  It has no counterpart in the
- * reference; it exists for callers that cannot allocate device memory: a host runtime
- * bound through this C ABI that only receives device pointers from another owner of
- * GPU memory, or code recording a CUDA graph, where cudaMalloc is not permitted.  The
- * scan's tile words live in a fixed 64 KiB array in the library's device memory (one per
- * GPU, held until the process exits), so n is limited to
- * sph_exclusive_scan_i32_static_max_items() = 33,550,336; larger n is rejected with
- * SPH_ERR_INVALID_ARGUMENT.  Nothing in the array needs to start at zero.  The first call
- * on a device looks up the array's device address (cudaGetSymbolAddress) and should come
- * before any stream capture.  All calls share the one array: calls whose work overlaps on
- * the GPU (different streams, or different host threads) race and corrupt each other. */
+ * reference.  It exists for callers that cannot allocate device memory: a host runtime
+ * bound through this C ABI (a service written in another language) that only receives
+ * device pointers from the owner of GPU memory and has no allocator of its own, or a
+ * serving process whose whole device-memory budget is reserved up front in a pooled
+ * arena, where a further allocation would break the budget.  The scan's tile words live
+ * in a fixed 64 KiB array in the library's device memory (one per GPU, held until the
+ * process exits), so n is limited to sph_exclusive_scan_i32_static_max_items() =
+ * 33,550,336; larger n is rejected with SPH_ERR_INVALID_ARGUMENT and nothing runs.  The
+ * call clears the tile words it uses before the scan (a memset, no allocation).  The first
+ * call on a device looks up the array's device address (cudaGetSymbolAddress) and caches
+ * it; that first call should come before any stream capture, and the cached address does
+ * not survive cudaDeviceReset, so the entry point must not be used on a device after it
+ * was reset in the same process.  All calls share the one array: calls whose work overlaps
+ * on the GPU (different streams, or different host threads) race and corrupt each other. */
 int64_t sph_exclusive_scan_i32_static_max_items(void);
 sph_status_t sph_exclusive_scan_i32_static(const int32_t* in, int32_t* out, int64_t n, void* stream);
 
@@ -214,13 +218,15 @@ sph_status_t sph_gather_sorted(const uint32_t* order, int64_t n, const float* po
                                void* stream);
 
 /* constructHashMap (src/modules/neighborSearch.py:58-88) on the GPU from the sorted keys:
- * writes cell_indices/cum_cell(counts)/cell_span(begins) [C] in hash order and
- * hash_table [hash_len, 2]; *num_cells_out (host) receives C.  Synchronises once
- * (to learn C, like the reference's host-side shapes). */
+ * writes cell_indices/cum_cell(counts)/cell_span(begins) [C] in hash order (cells of one
+ * hash in increasing cell order, as a stable argsort of the hashes gives) and hash_table
+ * [hash_len, 2] = (first slot, cells in the bucket), (-1, 0) for an empty bucket.  The
+ * number of occupied cells C goes to *num_cells (device int32); the output arrays need room
+ * for n entries (C <= n).  Asynchronous: nothing waits on the host. */
 size_t sph_hash_map_scratch_bytes(int64_t n, int32_t hash_len);
 sph_status_t sph_hash_map_build(const uint32_t* sorted_keys, int64_t n, int32_t cells_x, int32_t hash_len,
                                 int32_t* hash_table, int32_t* cell_indices, int32_t* cum_cell,
-                                int32_t* cell_span, int64_t* num_cells_out, void* scratch,
+                                int32_t* cell_span, int32_t* num_cells, void* scratch,
                                 size_t scratch_bytes, void* stream);
 
 /* ---------------------------------------------------------------- native CSR search (a4, a5, a9) */

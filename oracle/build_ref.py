@@ -8,6 +8,8 @@ extension module written only into `oracle/_ref/` (git-ignored).
 
 The reference checkout only exists in the development container; on a machine without
 it this script reports that and returns None.  Nothing in the product imports this.
+This recipe is the one place that names where the checkout lies (`REF_ROOT`, overridden by
+the environment variable PYTORCHSPH_REFERENCE); the harness and the tests take it from here.
 """
 from __future__ import annotations
 

@@ -28,7 +28,8 @@ import os
 import sys
 import types
 
-REF_ROOT = os.environ.get("PYTORCHSPH_REFERENCE", "/root/reference")
+sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
+from build_ref import REF_ROOT  # noqa: E402  (the checkout's location is set in the build recipe)
 
 _loaded = None
 

@@ -39,7 +39,7 @@ def _modules():
 
 def base_config(scene, scheme="deltaSPH", diffusion="MOG", integration="semiImplicitEuler", dt=None, c0=None,
                 rho0=1000.0, alpha=0.01, delta=0.1, kinematic=0.001, gravity=9.81, point_source=False,
-                dfsph=None, cfl_fixed=True, boundary_diffusion=True):
+                point_center=(0.0, 0.0), dfsph=None, cfl_fixed=True, boundary_diffusion=True):
     dx = scene["dx"]
     h = np.float32(scene["h"])
     W, H = scene.get("tank", (None, None))
@@ -58,7 +58,7 @@ def base_config(scene, scheme="deltaSPH", diffusion="MOG", integration="semiImpl
         "integration": {"scheme": integration, "dt": dt},
         "fluid": {"restDensity": rho0, "c0": c0},
         "gravity": {"magnitude": gravity, "direction": [0, -1], "pointSource": point_source, "potentialField": True,
-                    "center": [0, 0]},
+                    "center": [float(point_center[0]), float(point_center[1])]},
         "timestep": {"fixed": cfl_fixed, "min": dt if cfl_fixed else 1e-6, "max": dt if cfl_fixed else 1e-2,
                      "CFLNumber": 0.4},
         "domain": {"min": [0.0, 0.0], "max": [W, H], "adjustDomain": False, "adjustParticle": False},

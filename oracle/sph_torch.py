@@ -157,6 +157,7 @@ class Params:
     gravity: tuple = (0.0, -9.81)
     point_source: bool = False          # gravity as -g (x - c) (potential field)
     point_magnitude: float = 1.0
+    point_center: tuple = (0.0, 0.0)   # gravity.center
     diffusion: str = "MOG"              # "MOG" | "deltaSPH"
     boundary_diffusion: bool = True
     vmin: np.ndarray = field(default_factory=lambda: np.zeros(2, np.float32))
@@ -247,11 +248,12 @@ def deltasph_rhs(st, walls, nb: Neighbors, p: Params, dtype):
     acc = torch.zeros((n, 2), dtype=dtype)
     # 7 gravity (gravity.py:46-57)
     if p.point_source:
-        dist = torch.linalg.norm(x, axis=1)
+        xc = x - torch.tensor(p.point_center, dtype=dtype)
+        dist = torch.linalg.norm(xc, axis=1)
         m = dist > 1e-7
         # the reference normalises in place where dist > 1e-7; torch.where keeps it
         # differentiable (same values)
-        diff = torch.where(m[:, None], x / torch.where(m, dist, torch.ones_like(dist))[:, None], x)
+        diff = torch.where(m[:, None], xc / torch.where(m, dist, torch.ones_like(dist))[:, None], xc)
         acc = acc - p.point_magnitude * diff * dist[:, None]
     else:
         acc = acc + torch.tensor(p.gravity, dtype=dtype)

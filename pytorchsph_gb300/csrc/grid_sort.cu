@@ -423,9 +423,13 @@ __global__ void k_cell_compact(const uint32_t* __restrict__ keys, int64_t n, con
   c_id[c] = (uint32_t)c;
 }
 
-__global__ void k_cell_emit(int64_t C, int64_t n, const uint32_t* __restrict__ c_id, const int32_t* __restrict__ c_lin,
-                            const int32_t* __restrict__ c_begin, int32_t* __restrict__ cell_indices,
-                            int32_t* __restrict__ cum_cell, int32_t* __restrict__ cell_span) {
+// The occupied-cell count C = num_cells[0] is read on the device (the total of the head scan),
+// so the map is built without a host round trip; launched over n >= C threads.
+__global__ void k_cell_emit(const int32_t* __restrict__ num_cells, int64_t n, const uint32_t* __restrict__ c_id,
+                            const int32_t* __restrict__ c_lin, const int32_t* __restrict__ c_begin,
+                            int32_t* __restrict__ cell_indices, int32_t* __restrict__ cum_cell,
+                            int32_t* __restrict__ cell_span) {
+  const int64_t C = *num_cells;
   int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= C) return;
   uint32_t c = c_id[k];
@@ -436,6 +440,16 @@ __global__ void k_cell_emit(int64_t C, int64_t n, const uint32_t* __restrict__ c
   cell_span[k] = b;
 }
 
+// Every slot of the hash-sort input starts as the sentinel hash L (above every real hash), so
+// the n-item sort puts the C occupied cells first, in (hash, cell) order, and the rest after.
+__global__ void k_hash_sentinel(uint32_t* __restrict__ c_hash, uint32_t* __restrict__ c_id, int64_t n, int32_t L) {
+  int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n) {
+    c_hash[k] = (uint32_t)L;
+    c_id[k] = (uint32_t)k;
+  }
+}
+
 __global__ void k_table_init(int32_t* __restrict__ table, int32_t L) {
   int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (b < L) {
@@ -444,7 +458,9 @@ __global__ void k_table_init(int32_t* __restrict__ table, int32_t L) {
   }
 }
 
-__global__ void k_table_fill(const uint32_t* __restrict__ sorted_hash, int64_t C, int32_t* __restrict__ table) {
+__global__ void k_table_fill(const uint32_t* __restrict__ sorted_hash, const int32_t* __restrict__ num_cells,
+                             int32_t* __restrict__ table) {
+  const int64_t C = *num_cells;
   int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= C) return;
   uint32_t hv = sorted_hash[k];
@@ -659,9 +675,9 @@ size_t sph_hash_map_scratch_bytes(int64_t n, int32_t hash_len) {
 
 sph_status_t sph_hash_map_build(const uint32_t* sorted_keys, int64_t n, int32_t cells_x, int32_t hash_len,
                                 int32_t* hash_table, int32_t* cell_indices, int32_t* cum_cell, int32_t* cell_span,
-                                int64_t* num_cells_out, void* scratch, size_t scratch_bytes, void* stream) {
-  SPH_REQUIRE(n > 0 && n < ((int64_t)1 << 31) && sorted_keys && cells_x > 0 && hash_len > 0 && hash_table &&
-                  cell_indices && cum_cell && cell_span && num_cells_out,
+                                int32_t* num_cells, void* scratch, size_t scratch_bytes, void* stream) {
+  SPH_REQUIRE(n > 0 && n < ((int64_t)1 << 31) && sorted_keys && cells_x > 0 && hash_len > 0 &&
+                  hash_len < 0x7fffffff && hash_table && cell_indices && cum_cell && cell_span && num_cells,
               "hash_map_build: bad arguments");
   if (!scratch || scratch_bytes < sph_hash_map_scratch_bytes(n, hash_len)) {
     set_error_text("hash_map_build: scratch too small");
@@ -689,24 +705,23 @@ sph_status_t sph_hash_map_build(const uint32_t* sorted_keys, int64_t n, int32_t 
   k_cell_heads<<<grid_for(n, 256), 256, 0, st>>>(sorted_keys, n, head);
   sph_status_t s = sph_exclusive_scan_i32(head, slot, n, scan_s, scan_b, stream);
   if (s != SPH_OK) return s;
-  int32_t C32 = 0;
-  cudaMemcpyAsync(&C32, slot + n, sizeof(int32_t), cudaMemcpyDeviceToHost, st);
+  k_hash_sentinel<<<grid_for(n, 256), 256, 0, st>>>(c_hash, c_id, n, hash_len);
   k_cell_compact<<<grid_for(n, 256), 256, 0, st>>>(sorted_keys, n, head, slot, cells_x, hash_len, c_lin, c_begin,
                                                    c_hash, c_id);
   SPH_CHECK_LAUNCH("hash_map_build(compact)");
-  cudaError_t e = cudaStreamSynchronize(st);
+  const int32_t* C = slot + n;  // occupied cells (the scan total), on the device
+  cudaError_t e = cudaMemcpyAsync(num_cells, C, sizeof(int32_t), cudaMemcpyDeviceToDevice, st);
   if (e != cudaSuccess) {
-    set_error("hash_map_build(sync)", e);
+    set_error("hash_map_build(count)", e);
     return SPH_ERR_CUDA;
   }
-  int64_t C = C32;
-  s = sph_radix_sort_pairs(c_hash, c_id, C, key_bits_for(hash_len > 1 ? hash_len - 1 : 1), 8, rs_s, rs_b, stream);
+  // stable sort of all n slots by hash, the sentinel L included in the key width
+  s = sph_radix_sort_pairs(c_hash, c_id, n, key_bits_for(hash_len), 8, rs_s, rs_b, stream);
   if (s != SPH_OK) return s;
-  k_cell_emit<<<grid_for(C, 256), 256, 0, st>>>(C, n, c_id, c_lin, c_begin, cell_indices, cum_cell, cell_span);
+  k_cell_emit<<<grid_for(n, 256), 256, 0, st>>>(C, n, c_id, c_lin, c_begin, cell_indices, cum_cell, cell_span);
   k_table_init<<<grid_for(hash_len, 256), 256, 0, st>>>(hash_table, hash_len);
-  k_table_fill<<<grid_for(C, 256), 256, 0, st>>>(c_hash, C, hash_table);
+  k_table_fill<<<grid_for(n, 256), 256, 0, st>>>(c_hash, C, hash_table);
   SPH_CHECK_LAUNCH("hash_map_build");
-  *num_cells_out = C;
   return SPH_OK;
 }
 

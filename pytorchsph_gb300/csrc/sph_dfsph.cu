@@ -9,6 +9,8 @@
 // max_iters, so every thread meets every barrier the same number of times.
 #include <cooperative_groups.h>
 
+#include <mutex>
+
 #include "sph_math.cuh"
 
 namespace cg = cooperative_groups;
@@ -552,7 +554,11 @@ static DfsphBufs to_bufs(const sph_dfsph_buffers* b, int64_t n = 0) {
   return B;
 }
 
-static int g_coop_blocks = 0;
+// Cooperative grid size of k_dfsph_solve per GPU (resident blocks x SMs), computed on the
+// first solve on that GPU; GPUs of one process may differ in SM count.
+constexpr int kCoopMaxDevices = 64;
+static int g_coop_blocks[kCoopMaxDevices] = {0};
+static std::mutex g_coop_mu;
 
 extern "C" {
 
@@ -605,19 +611,28 @@ sph_status_t sph_dfsph_solve(const sph_fluid_view* fluid, const sph_wall_view* w
   k_dfsph_prepare<<<grid_for(n, 128), 128, 0, st>>>(F, W, grid, P, B, dt, density);
   if (density && W.n > 0) k_dfsph_wall_prepare<<<grid_for(W.n, 128), 128, 0, st>>>(F, W, grid, P, B, dt);
   SPH_CHECK_LAUNCH("dfsph_solve(prepare)");
-  if (g_coop_blocks == 0) {
-    int per_sm = 0;
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_dfsph_solve, 256, 0);
-    if (e != cudaSuccess || per_sm < 1) {
-      set_error("dfsph_solve(occupancy)", e);
-      return SPH_ERR_CUDA;
-    }
-    int dev = 0, sms = kNumSMs;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    g_coop_blocks = std::min(per_sm, 8) * sms;
+  int dev = 0;
+  cudaError_t de = cudaGetDevice(&dev);
+  if (de != cudaSuccess || dev < 0 || dev >= kCoopMaxDevices) {
+    set_error("dfsph_solve(device)", de);
+    return SPH_ERR_CUDA;
   }
-  int blocks = std::min(g_coop_blocks, (int)sph_dfsph_partials_count());
+  int coop_blocks = 0;
+  {
+    std::lock_guard<std::mutex> lock(g_coop_mu);
+    if (g_coop_blocks[dev] == 0) {
+      int per_sm = 0, sms = 0;
+      cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_dfsph_solve, 256, 0);
+      if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+      if (e != cudaSuccess || per_sm < 1 || sms < 1) {
+        set_error("dfsph_solve(occupancy)", e);
+        return SPH_ERR_CUDA;
+      }
+      g_coop_blocks[dev] = std::min(per_sm, 8) * sms;
+    }
+    coop_blocks = g_coop_blocks[dev];
+  }
+  int blocks = std::min(coop_blocks, (int)sph_dfsph_partials_count());
   blocks = std::min(blocks, std::max(1, (n + 255) / 256));
   int density_i = density;
   int min_it = density ? params->min_density_iters : params->min_divergence_iters;

@@ -46,6 +46,11 @@ CASES = {
     "dsph_delta_sie": dict(seed=1, steps=3, kw=dict(scheme="deltaSPH", diffusion="deltaSPH",
                                                     integration="semiImplicitEuler")),
     "dsph_mog_rk4": dict(seed=2, steps=2, kw=dict(scheme="deltaSPH", diffusion="MOG", integration="RK4")),
+    # point-source body force (gravity.pointSource with potentialField, src/modules/gravity.py:46-57),
+    # the force of the oscillating drops, centred off the origin
+    "dsph_point_sie": dict(seed=4, steps=3, kw=dict(scheme="deltaSPH", diffusion="deltaSPH",
+                                                    integration="semiImplicitEuler", point_source=True,
+                                                    point_center=(0.08, 0.16))),
     "dfsph_sie": dict(seed=3, steps=3, kw=dict(scheme="dfsph", integration="semiImplicitEuler", dt=0.0005,
                                                kinematic=0.01, dfsph=DFSPH, cfl_fixed=False)),
 }
@@ -69,7 +74,10 @@ def main():
                       "diffusion": cfg["diffusion"]["densityScheme"], "integration": cfg["integration"]["scheme"],
                       "scheme": cfg["simulation"]["scheme"], "steps": c["steps"],
                       "dt_min": float(cfg["timestep"]["min"]), "dt_max": float(cfg["timestep"]["max"]),
-                      "fixed_dt": bool(cfg["timestep"]["fixed"])}
+                      "fixed_dt": bool(cfg["timestep"]["fixed"]),
+                      "point_source": bool(cfg["gravity"]["pointSource"]),
+                      "gravity_magnitude": float(cfg["gravity"]["magnitude"]),
+                      "point_center": [float(v) for v in cfg["gravity"]["center"]]}
         if "dfsph" in cfg:
             meta[name]["dfsph"] = {k: (float(v) if not isinstance(v, bool) else v) for k, v in cfg["dfsph"].items()}
         tag = "" if prec == "single" else "f64_"

@@ -106,6 +106,51 @@ def test_dropin_buildNeighborListCUDA(cuda, golden):
     assert np.array_equal(pairs_key(r.cpu().numpy(), cc.cpu().numpy()), ref)
 
 
+@pytest.mark.parametrize("case", CASES)
+def test_sortPositions_constructHashMap_match_reference(cuda, golden, case):
+    """sortPositions / constructHashMap / constructNeighborhoods(CUDA) of the GPU module mirror
+    (src/modules/neighborSearch.py:30-159) against the reference's own outputs.  Grid, sorted
+    keys and hash table bit for bit; the reference's argsort is not stable, so inside a cell
+    (and inside a hash bucket) only the members are compared, not their order."""
+    from pytorchsph_gb300 import neighborhoods as NH
+    g = golden
+    vmin, vmax = dom(g, case)
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+    pos, h = g[f"{case}/pos"], g[f"{case}/h"]
+    sp, ss, sli, si, cx, qmin, hmax = NH.sortPositions(
+        t(pos), t(h), 1.0, None if vmin is None else torch.from_numpy(vmin),
+        None if vmax is None else torch.from_numpy(vmax))
+    assert cx == int(g[f"{case}/si_cells_x"]) and np.float32(hmax) == g[f"{case}/si_hmax"]
+    assert np.array_equal(qmin.cpu().numpy(), g[f"{case}/si_qmin"])
+    lin = sli.cpu().numpy()
+    order = si.cpu().numpy()
+    assert np.array_equal(lin, g[f"{case}/si_sorted_lin"])
+    member = lambda a, o: np.sort(a.astype(np.int64) * (1 << 32) + o.astype(np.int64))
+    assert np.array_equal(member(lin, order), member(g[f"{case}/si_sorted_lin"], g[f"{case}/si_sort"]))
+    assert np.all((np.diff(lin) > 0) | (np.diff(order) > 0))      # stable inside a cell
+    assert np.array_equal(sp.cpu().numpy(), pos[order]) and np.array_equal(ss.cpu().numpy(), h[order])
+    L = int(g[f"{case}/hash_len"])
+    for _ in range(2):   # the second build reuses nothing of the first
+        table, ci, cum, span = NH.constructHashMap(sp, ss, sli, si, L, cx)
+        assert np.array_equal(table.cpu().numpy(), g[f"{case}/si_table"])
+        ci, cum, span = ci.cpu().numpy(), cum.cpu().numpy(), span.cpu().numpy()
+        gci = g[f"{case}/si_cell_indices"]
+        hsh = lambda c: ((c.astype(np.int64) % cx) * 3 + (c.astype(np.int64) // cx) * 5) % L
+        assert np.array_equal(hsh(ci), hsh(gci))                    # same bucket sequence
+        trip = lambda a, b, c: sorted(zip(a.tolist(), b.tolist(), c.tolist()))
+        assert trip(ci, cum, span) == trip(gci, g[f"{case}/si_cum_cell"], g[f"{case}/si_cell_span"])
+        for k in range(1, len(ci)):                                # cells of a bucket in increasing order
+            if hsh(ci[k:k + 1])[0] == hsh(ci[k - 1:k])[0]:
+                assert ci[k] > ci[k - 1]
+    ref = csr_key(g[f"{case}/offsets"], g[f"{case}/cols"])
+    dom_t = (None, None) if vmin is None else (torch.from_numpy(vmin), torch.from_numpy(vmax))
+    rows, cols, *_ = NH.constructNeighborhoods(t(pos), t(h), L, 1.0, *dom_t)
+    assert np.array_equal(pairs_key(rows.cpu().numpy(), cols.cpu().numpy()), ref)
+    i, j, *_ = NH.constructNeighborhoodsCUDA(t(pos), t(h), L, 1.0, *dom_t)
+    k = i.cpu().numpy() * (1 << 32) + j.cpu().numpy()
+    assert np.array_equal(k, ref) and np.all(np.diff(k) > 0)        # (i, j) order of the finalize
+
+
 def test_dropin_asymmetric(cuda, golden):
     from pytorchsph_gb300 import neighborSearch as NS
     g = golden

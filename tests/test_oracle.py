@@ -91,7 +91,7 @@ def test_predicate_spellings_differ_on_ties(golden):
         assert not np.array_equal(_csr_to_pairs(off, cols), ref)
 
 
-REF = os.environ.get("PYTORCHSPH_REFERENCE", "/root/reference")
+from build_ref import REF_ROOT as REF  # noqa: E402  (where the reference checkout lies, if anywhere)
 
 
 @pytest.mark.skipif(not os.path.exists(os.path.join(REF, "cppSrc", "neighSearch.cpp")),

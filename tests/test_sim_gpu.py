@@ -36,11 +36,12 @@ def sim_from_case(g, meta, name, dev):
                     min_density_iters=p.min_density_iters, max_density_iters=p.max_density_iters,
                     density_threshold=p.density_threshold, divergence_solver=p.divergence_solver,
                     min_divergence_iters=p.min_divergence_iters, max_divergence_iters=p.max_divergence_iters,
-                    divergence_threshold=p.divergence_threshold, omega_boundary=p.omega_boundary)
+                    divergence_threshold=p.divergence_threshold, omega_boundary=p.omega_boundary,
+                    point_source=p.point_source, point_magnitude=p.point_magnitude, point_center=p.point_center)
     return Simulation(scene, cfg, dev), m
 
 
-@pytest.mark.parametrize("name", ["dsph_mog_sie", "dsph_delta_sie", "dsph_mog_rk4", "dfsph_sie"])
+@pytest.mark.parametrize("name", ["dsph_mog_sie", "dsph_delta_sie", "dsph_mog_rk4", "dsph_point_sie", "dfsph_sie"])
 def test_steps_match_reference(cuda, name):
     g, meta = GC.load()
     sim, m = sim_from_case(g, meta, name, cuda)

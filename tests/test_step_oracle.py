@@ -23,7 +23,7 @@ def gold():
 F64 = {"deltaSPH": (1e-7, 1e-4), "dfsph": (1e-4, 1e-3)}
 
 
-@pytest.mark.parametrize("name", ["dsph_mog_sie", "dsph_delta_sie", "dsph_mog_rk4", "dfsph_sie"])
+@pytest.mark.parametrize("name", ["dsph_mog_sie", "dsph_delta_sie", "dsph_mog_rk4", "dsph_point_sie", "dfsph_sie"])
 def test_restatement_float64(gold, name):
     g, meta = gold
     solver = "dfsph" if meta[name]["scheme"] == "dfsph" else "deltaSPH"
@@ -48,7 +48,7 @@ def test_restatement_float64(gold, name):
         assert abs(dts[k] - float(g[f"{name}/f64_step{k - 1}_dt"])) <= 1e-12 * dts[k]
 
 
-@pytest.mark.parametrize("name", ["dsph_mog_sie", "dsph_delta_sie", "dfsph_sie"])
+@pytest.mark.parametrize("name", ["dsph_mog_sie", "dsph_delta_sie", "dsph_point_sie", "dfsph_sie"])
 def test_restatement_float32(gold, name):
     """float32 restatement vs the reference's float32 run: both carry float32 noise, which
     the wall pressure amplifies (p_b depends on rho_b - 1 ~ 3e-5)."""
