@@ -533,6 +533,80 @@ size_t sph_transpose_pairs_scratch_bytes(int64_t n);
 sph_status_t sph_transpose_pairs(const int64_t* cols, int64_t num_pairs, int64_t n, int32_t* col_offsets,
                                  int32_t* pairs, void* scratch, size_t scratch_bytes, void* stream);
 
+/* ---------------------------------------------------------------- delta+ surface detection and shifting (f3) */
+
+/* The surface detection and particle shifting of src/modules/deltaPlus.py
+ * (deltaPlusModule.detectSurface :242-245 = computeNormalizationmatrix :116-130,
+ * computeFluidNormal :132-163, detectFluidSurface :165-205; shift :247-251 =
+ * computeShiftAmount :81-115, adjustShiftingAmount :207-240) over the reference's own pair
+ * lists.  Fluid arrays in original order; pairs as the Module interface holds them:
+ *   fluid pairs fluidNeighbors (i, j), i-ordered, e_ij = (x_i - x_j) / r, q = r / h;
+ *   wall pairs boundaryToFluidNeighbors (b, f), b-ordered, e = (x_b - x_f) / r, and the same
+ *   pairs grouped by fluid particle (sph_transpose_pairs);
+ *   wall-wall pairs boundaryToBoundaryNeighbors (b, c), b-ordered, with the reference's
+ *   boundaryToBoundaryNeighborDistances e = (x_c - x_b) / r (the opposite sign of
+ *   fluidDistances, solidBoundary.py:180-191, 624-634). */
+typedef struct sph_surface_in {
+  const int32_t* offsets;            /* [n+1] fluid pair rows */
+  const int64_t* cols;               /* [P] j */
+  const float* dist;                 /* float2 [P] e_ij */
+  const float* radial;               /* [P] q_ij */
+  const int32_t* wall_offsets;       /* [nb+1] wall pair rows */
+  const int64_t* wall_rows;          /* [Pb] b */
+  const int64_t* wall_cols;          /* [Pb] f */
+  const float* wall_dist;            /* float2 [Pb] (x_b - x_f) / r */
+  const float* wall_radial;          /* [Pb] */
+  const int32_t* fluid_wall_offsets; /* [n+1] wall pairs grouped by fluid particle */
+  const int32_t* fluid_wall_pairs;   /* [Pb] pair indices, ascending per fluid particle */
+  const int32_t* ww_offsets;         /* [nb+1] wall-wall pair rows */
+  const int64_t* ww_cols;            /* [Pw] c */
+  const float* ww_dist;              /* float2 [Pw] (x_c - x_b) / r */
+  const float* ww_radial;            /* [Pw] */
+  const float* pos;                  /* float2 [n] fluidPosition */
+  const float* vel;                  /* float2 [n] fluidVelocity */
+  const float* rho;                  /* [n] fluidDensity (relative) */
+  const float* area;                 /* [n] fluidArea */
+  const float* volume;               /* [n] fluidVolume */
+  const float* matrix;               /* float4 [count] a 2x2 matrix per row (SPH_SURF_PINV_EIG) */
+  const float* L;                    /* float4 [n] fluidL (pseudo-inverted normalization matrix) */
+  const float* lambda;               /* [n] fluidLambda */
+  const float* normal;               /* float2 [n] fluidNormal */
+  const float* mask;                 /* [n] angle mask (SPH_SURF_CLASSIFY) / fluidSurfaceMask (adjust) */
+  const float* shift;                /* float2 [n] shiftAmount (SPH_SURF_SHIFT_ADJUST) */
+  const float* wall_pos;             /* float2 [nb] boundaryPositions */
+  const float* wall_area;            /* [nb] boundaryVolume (the wall particle's area) */
+  const float* wall_rho;             /* [nb] boundaryDensity (relative) */
+  const float* wall_volume;          /* [nb] boundaryVolume / boundaryDensity */
+  const float* wall_lambda;          /* [nb] the walls' eigVals[:, 1] */
+  float packing;                     /* particle.packing: k0 = W(packing) of the shift */
+  float cfl;                         /* shift CFL (1.5 in the reference) */
+  int64_t n, nb;                     /* fluid and wall particles (SPH_SURF_PINV_EIG: n rows) */
+} sph_surface_in;
+
+#define SPH_SURF_PINV_EIG 0            /* out float4 [n] = pinv2x2(matrix), out2 float2 [n] = its eigVals
+                                          (singular values, larger first; src/util.py:386-433) */
+#define SPH_SURF_WALL_NORMALIZATION 1  /* out float4 [nb] = the wall's own normalization matrix:
+                                          wall->fluid pairs + wall-wall pairs (solidBoundary.py:679-693) */
+#define SPH_SURF_NORMAL 2              /* out float2 [n] lambdaGrad, out2 float2 [n] fluidNormal
+                                          (deltaPlus.py:132-163; the wall part takes the wall's volume as
+                                          fluidArea[b] / fluidDensity[b], as the reference indexes it: every
+                                          wall index in the pairs must be below n) */
+#define SPH_SURF_ANGLE_MASK 3          /* out [n] 1 where arccos(max dot) > pi/6 and lambda < 0.6, else 0;
+                                          out2 float2 [n] (angleMin, angleMax) of the fluid pairs, or NULL
+                                          (deltaPlus.py:165-188) */
+#define SPH_SURF_CLASSIFY 4            /* out [n] fluidSurfaceMask: 0 surface, 1 near surface (2/3 where
+                                          lambda < 0.5), 2 bulk (deltaPlus.py:189-205) */
+#define SPH_SURF_SHIFT 5               /* out float2 [n] shiftAmount = -cfl Ma 4 h^2 (fluid + wall sums),
+                                          Ma = max |v| / c0; out2 = device scratch of sph_surface_scratch_bytes()
+                                          (deltaPlus.py:81-115) */
+#define SPH_SURF_SHIFT_ADJUST 6        /* out float2 [n] fluidUpdate (length capped at 0.05 h, projected on
+                                          the tangent where mask < 1.5, zero where mask < 0.5); out2 [n] the
+                                          updated fluidSurfaceMask (deltaPlus.py:207-240) */
+size_t sph_surface_scratch_bytes(void);
+/* One step of the delta+ module; params gives support, c0.  Asynchronous. */
+sph_status_t sph_surface_term(int32_t term, const sph_surface_in* in, const sph_params* params, float* out,
+                              float* out2, void* stream);
+
 /* ---------------------------------------------------------------- differentiable rollouts */
 
 /* A free fluid (no walls) stepped by the deltaSPH right-hand side (src/deltaSPH.py:146-200:

@@ -489,3 +489,127 @@ def update_dt(state, p: Params, dt, dt_min, dt_max, cfl=0.4, scheme="dfsph"):
             m = min(m, vdt)
     target = m if m > dt_min else dt_min
     return min(max(target, dt * 0.5), dt * 1.05)
+
+
+# ----------------------------------------------------------------- delta+ (src/modules/deltaPlus.py)
+def eigvals2x2(M):
+    """The eigVals pinv2x2 returns (src/util.py:408-431): singular values (o1, o2), swapped
+    where |o2| > |o1|."""
+    a, b, c, d = M[:, 0, 0], M[:, 0, 1], M[:, 1, 0], M[:, 1, 1]
+    S1 = a ** 2 + b ** 2 + c ** 2 + d ** 2
+    S2 = torch.sqrt((a ** 2 + b ** 2 - c ** 2 - d ** 2) ** 2 + 4 * (a * c + b * d) ** 2)
+    e = torch.stack([torch.sqrt((S1 + S2) / 2), torch.sqrt((S1 - S2) / 2)], 1)
+    swap = torch.abs(e[:, 1]) > torch.abs(e[:, 0])
+    e[swap] = torch.flip(e[swap], [1])
+    return e
+
+
+def _scatter_fill0(vals, idx, n, reduce):
+    """torch_scatter max / min: the reduction over each index, 0 where an index has none."""
+    out = torch.zeros(n, dtype=vals.dtype)
+    return out.scatter_reduce(0, idx, vals, reduce=reduce, include_self=False)
+
+
+def surface_detect(fl, wl, ww, h, dtype):
+    """detectSurface (deltaPlus.py:242-245): the normalization matrix (fluid pairs plus the
+    wall part, densityDiffusion.py:30-44, solidBoundary.py:676-694) with pinv2x2, the walls'
+    own matrices, the lambda gradient and normal (:132-163) and the surface mask (:165-205).
+    fl: fluid state and pairs {x, rho, area, volume, i, j, e, q}; wl: wall pairs and arrays
+    {bb, bf, e (x_b - x_f)/r, q, x, area, rho}; ww: wall-wall pairs {i, j, e (x_j - x_i)/r, q}
+    in the reference's sign.  Returns a dict with the reference's state names."""
+    T = lambda a: a.to(dtype)
+    x, rho, area, vol = T(fl["x"]), T(fl["rho"]), T(fl["area"]), T(fl["volume"])
+    i, j, e, q = fl["i"], fl["j"], T(fl["e"]), T(fl["q"])
+    n = x.shape[0]
+    bb, bf, be, bq = wl["bb"], wl["bf"], T(wl["e"]), T(wl["q"])
+    xb, Ab, rhob = T(wl["x"]), T(wl["area"]), T(wl["rho"])
+    nb = xb.shape[0]
+    rho0 = wl.get("rho0", 1000.0)
+    Vb = Ab * rho0 / rhob / rho0              # self.fluidVolume of solidBoundary.py:678
+
+    def norm_matrix(ii, jj, ri, rj, Vj, dist, qq, num):   # computeNormalizationMatrix
+        g = gradW(qq, dist, h)
+        term = torch.einsum('nu,nv->nuv', rj[jj] - ri[ii], g) * Vj[jj][:, None, None]
+        return ssum(term, ii, num)
+
+    M = norm_matrix(i, j, x, x, vol, e, q, n)
+    # walls' own matrices: wall -> fluid pairs, then the wall-wall pairs (solidBoundary.py:679-692)
+    Mb = norm_matrix(bb, bf, xb, x, vol, be, bq, nb)
+    Mb = Mb + norm_matrix(ww["i"], ww["j"], xb, xb, Vb, T(ww["e"]), T(ww["q"]), nb)
+    eig_b = eigvals2x2(Mb)
+    # fluid side of the wall part: fluid i = bf, j = bb, distances -e
+    M = M + norm_matrix(bf, bb, x, xb, Vb, -be, bq, n)
+    L = pinv2x2(M)
+    eig = eigvals2x2(M)
+    lam = eig[:, 1]
+    # lambda gradient and normal (deltaPlus.py:132-163)
+    g = gradW(q, e, h)
+    corr = torch.bmm(L[i], g[:, :, None])[:, :, 0]
+    term = -((area[j] / rho[j]) * (lam[j] - lam[i]))[:, None] * corr
+    lg = ssum(term, i, n)
+    gb = gradW(bq, -be, h)
+    corr = torch.bmm(L[bf], gb[:, :, None])[:, :, 0]
+    term = -((area[bb] / rho[bb]) * (eig_b[:, 1][bb] - lam[bf]))[:, None] * corr   # the reference's fluidArea[bb]
+    lg = lg + ssum(term, bf, n)
+    eps = h ** 2 * 0.1
+    normal = lg / (torch.linalg.norm(lg, dim=1) + eps)[:, None]
+    # surface mask (deltaPlus.py:165-205)
+    m = i != j
+    ii, jj = i[m], j[m]
+    dots = torch.einsum('nd,nd->n', -e[m], normal[ii])
+    sc = _scatter_fill0(dots, ii, n, "amax")
+    angle_min = torch.arccos(_scatter_fill0(dots, ii, n, "amin"))
+    angle_max = torch.arccos(sc)
+    dots = torch.einsum('nd,nd->n', be, normal[bf])
+    sc = torch.arccos(torch.max(sc, _scatter_fill0(dots, bf, n, "amax")))
+    mask = torch.zeros_like(sc)
+    mask[torch.logical_and(sc > math.pi / 6, lam < 0.6)] = 1
+    mask2 = _scatter_fill0(mask[jj], ii, n, "amax")
+    final = torch.zeros_like(sc)
+    final[mask2 > 0] = 2 / 3
+    final[mask > 0] = 1
+    zero, surf, bulk = final > 0.7, torch.logical_and(lam >= 0.5, final > 0.), final < 0.1
+    surface = final.clone()
+    surface[surf] = 1
+    surface[zero] = 0
+    surface[bulk] = 2
+    return {"normalizationMatrix": M, "fluidL": L, "eigVals": eig, "fluidLambda": lam, "lambdaGrad": lg,
+            "fluidNormal": normal, "angleMin": angle_min, "angleMax": angle_max, "fluidSurfaceMask": surface,
+            "boundaryNormalizationMatrix": Mb, "boundaryEigVals": eig_b}
+
+
+def shift(fl, wl, normal, surface, h, c0, packing, dtype, cfl=1.5):
+    """shift (deltaPlus.py:247-251): computeShiftAmount (:81-115) and adjustShiftingAmount
+    (:207-240).  Returns (shiftAmount before the adjustment, fluidUpdate, fluidSurfaceMask)."""
+    T = lambda a: a.to(dtype)
+    v, rho, area = T(fl["v"]), T(fl["rho"]), T(fl["area"])
+    i, j, e, q = fl["i"], fl["j"], T(fl["e"]), T(fl["q"])
+    n = v.shape[0]
+    bb, bf, be, bq = wl["bb"], wl["bf"], T(wl["e"]), T(wl["q"])
+    Ab, rhob = T(wl["area"]), T(wl["rho"])
+    Ma = torch.max(torch.linalg.norm(v, dim=1)) / c0
+    k0 = W(torch.tensor(packing, dtype=dtype), h)
+    R, npow = 0.2, 4
+    coef = -cfl * Ma * (4 * h ** 2)
+    kt = 1 + R * torch.pow(W(q, h) / k0, npow)
+    term = (kt * area[j] / (rho[i] + rho[j]))[:, None] * gradW(q, e, h)
+    s = coef * ssum(term, i, n)
+    kt = 1 + R * torch.pow(W(bq, h) / k0, npow)
+    term = (kt * Ab[bb] / (rho[bf] + rhob[bb]))[:, None] * gradW(bq, -be, h)
+    s = s + coef * ssum(term, bf, n)
+    raw = s.clone()
+    ln = torch.linalg.norm(s, axis=1)
+    big = ln > h * 0.05
+    s[big] = s[big] / ln[big, None] * h * 0.05
+    nrm, surf = T(normal), T(surface)
+    outer = torch.einsum('nu,nv->nuv', nrm, nrm)
+    eye = torch.eye(2, dtype=dtype)
+    ns = torch.matmul(eye - outer, s.unsqueeze(2))[:, :, 0]
+    zero, sr, bulk = surf < 0.5, surf < 1.5, surf > 1.5
+    s[sr] = ns[sr]
+    s[zero] = 0
+    mask = surf.clone()
+    mask[sr] = 1
+    mask[zero] = 0
+    mask[bulk] = 2
+    return raw, s, mask

@@ -84,6 +84,8 @@ SIGNATURES.update({  # Module-interface terms
     "sph_wall_term": (_I32, [_I32, _P, _P, _P, _I32, _P]),
     "sph_transpose_pairs_scratch_bytes": (_SZ, [_I64]),
     "sph_transpose_pairs": (_I32, [_P, _I64, _I64, _P, _P, _P, _SZ, _P]),
+    "sph_surface_scratch_bytes": (_SZ, []),
+    "sph_surface_term": (_I32, [_I32, _P, _P, _P, _P, _P]),
     "sph_pair_geometry": (_I32, [_P, _P, _I64, _P, _P, _P, _F32, _P, _P, _P]),
 })
 

@@ -368,7 +368,7 @@ using namespace sph;
 
 extern "C" {
 
-int32_t sph_abi_version(void) { return 1; }
+int32_t sph_abi_version(void) { return 2; }
 
 const char* sph_last_error(void) { return sph::g_err; }
 

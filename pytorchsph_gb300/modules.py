@@ -373,11 +373,7 @@ class densityDiffusionModule(_SummationModule):
     def computeNormalizationMatrices(self, simulationState, simulation):
         self.normalizationMatrix = pair_term("normalization", simulationState, self.P)
         self.normalizationMatrix += simulation.boundaryModule.computeNormalizationMatrices(simulationState, simulation)
-        n = self.normalizationMatrix.shape[0]
-        L = torch.empty((n, 4), dtype=torch.float32, device=self.normalizationMatrix.device)
-        particle_op("pinv2x2", self.normalizationMatrix.reshape(n, 4), None, self.P, L)
-        self.fluidL = L.view(n, 2, 2)
-        self.eigVals = None   # the singular values are not computed (nothing on the path reads them)
+        self.fluidL, self.eigVals = pinv2x2(self.normalizationMatrix, self.P)
 
     def computeRenormalizedDensityGradient(self, simulationState, simulation):
         n = self.fluidL.shape[0]
@@ -555,6 +551,63 @@ def wall_term(term, pairs, P, n, nb, out=None, accumulate=False, dt=0.0, **array
     return out
 
 
+class SurfaceC(ctypes.Structure):
+    """sph_surface_in (include/sph_gb300.h)."""
+    _fields_ = [(k, ctypes.c_void_p) for k in (
+        "offsets", "cols", "dist", "radial", "wall_offsets", "wall_rows", "wall_cols", "wall_dist", "wall_radial",
+        "fluid_wall_offsets", "fluid_wall_pairs", "ww_offsets", "ww_cols", "ww_dist", "ww_radial", "pos", "vel",
+        "rho", "area", "volume", "matrix", "L", "lambda_", "normal", "mask", "shift", "wall_pos", "wall_area",
+        "wall_rho", "wall_volume", "wall_lambda")] + [
+        ("packing", ctypes.c_float), ("cfl", ctypes.c_float), ("n", ctypes.c_int64), ("nb", ctypes.c_int64)]
+
+
+SURF = {"pinv_eig": 0, "wall_normalization": 1, "normal": 2, "angle_mask": 3, "classify": 4, "shift": 5,
+        "shift_adjust": 6}
+
+
+def surface_term(term, P, n, nb=0, out=None, out2=None, fluid=None, walls=None, wall_walls=None, packing=0.0,
+                 cfl=1.5, **arrays):
+    """One call of sph_surface_term.  fluid: the state whose fluidNeighbors / distances give
+    the fluid pairs; walls: a _WallPairs (wall -> fluid); wall_walls: (offsets, cols, dist,
+    radial) of the wall-wall pairs; arrays: the named per-particle arrays."""
+    keep = []
+    ptr = {}
+    if fluid is not None:
+        off = row_offsets(fluid)
+        cols = fluid['fluidNeighbors'][1].contiguous()
+        keep += [off, cols]
+        ptr.update(offsets=N.ptr(off), cols=N.ptr(cols), dist=N.ptr(_f32(fluid['fluidDistances'])),
+                   radial=N.ptr(_f32(fluid['fluidRadialDistances'])))
+    if walls is not None:
+        ptr.update(wall_offsets=N.ptr(walls.woff), wall_rows=N.ptr(walls.rows), wall_cols=N.ptr(walls.cols),
+                   wall_dist=N.ptr(walls.dist), wall_radial=N.ptr(walls.radial), fluid_wall_offsets=N.ptr(walls.foff),
+                   fluid_wall_pairs=N.ptr(walls.fpairs))
+    if wall_walls is not None:
+        wo, wc, wd, wr = wall_walls
+        ptr.update(ww_offsets=N.ptr(wo), ww_cols=N.ptr(wc), ww_dist=N.ptr(_f32(wd)), ww_radial=N.ptr(_f32(wr)))
+    for k, v in arrays.items():
+        name = "lambda_" if k in ("lambda", "lambda_") else k
+        if name not in [f[0] for f in SurfaceC._fields_]:
+            raise N.SPHError(f"surface_term: unknown array {k}")
+        t = _f32(v.reshape(-1) if v is not None else None)
+        keep.append(t)
+        ptr[name] = N.ptr(t)
+    inp = SurfaceC(**ptr, packing=float(packing), cfl=float(cfl), n=int(n), nb=int(nb))
+    N.call("sph_surface_term", SURF[term], ctypes.byref(inp), ctypes.byref(P), N.ptr(out), N.ptr(out2),
+           N.stream_ptr())
+    return out, out2
+
+
+def pinv2x2(M, P):
+    """(pinv2x2(M) [n,2,2], its eigVals [n,2]) of src/util.py:386-433 for matrices M [n,2,2]."""
+    n = M.shape[0]
+    dev = M.device
+    L = torch.empty((n, 2, 2), dtype=torch.float32, device=dev)
+    eig = torch.empty((n, 2), dtype=torch.float32, device=dev)
+    surface_term("pinv_eig", P, n, out=L, out2=eig, matrix=M.contiguous())
+    return L, eig
+
+
 class solidBoundaryModule(BoundaryModule):
     """src/modules/solidBoundary.py on GPU kernels: ghost-particle solid walls with mDBC wall
     densities and the PBSPH pressure scheme (deltaSPH: continuity, L, <grad rho>, pressure
@@ -622,6 +675,19 @@ class solidBoundaryModule(BoundaryModule):
         res = GridSearch(dev).run(self.boundaryPositions, self.boundarySupport, self.boundaryVolume,
                                   kernel_support=float(self.support))
         self.boundaryDensityTerm = res.density()
+        # the wall-wall pair lists of solidBoundary.py:180-191 from the same search, with the
+        # reference's sign of the distances, (x_col - x_row) / r
+        nbrs, dist, radial = res.to_coo()
+        self.boundaryToBoundaryNeighbors = nbrs
+        self.boundaryToBoundaryNeighborDistances = (-dist).contiguous()
+        self.boundaryToBoundaryNeighborRadialDistances = radial
+        ww_off = torch.empty(self.numPtcls + 1, dtype=torch.int32, device=dev)
+        rows = nbrs[0].contiguous()
+        N.call("sph_row_offsets", N.ptr(rows), rows.shape[0], self.numPtcls, N.ptr(ww_off), N.stream_ptr())
+        self._ww = (ww_off, nbrs[1].contiguous(), self.boundaryToBoundaryNeighborDistances, radial)
+        self.normalizationMatrix = None
+        self.fluidL = None
+        self.eigVals = None
 
     def resetState(self, simulationState):
         for k in ("boundaryPressure", "boundaryPressure2", "boundaryActualArea", "boundaryPredictedVelocity",
@@ -688,9 +754,17 @@ class solidBoundaryModule(BoundaryModule):
                          wall_rho=self.boundaryDensity)
 
     def computeNormalizationMatrices(self, simulationState, simulation):
+        """solidBoundary.py:676-694: the walls' own matrices (wall -> fluid and wall -> wall
+        pairs) with their pseudo-inverses and singular values, and the fluid's wall part."""
         st = simulationState
         n = st['fluidPosition'].shape[0]
         self.fluidVolume = self._wall_volume()
+        M = torch.empty((self.numPtcls, 2, 2), dtype=torch.float32, device=self.boundaryPositions.device)
+        surface_term("wall_normalization", self.P, n, self.numPtcls, out=M, walls=self._bf, wall_walls=self._ww,
+                     pos=st['fluidPosition'], volume=st['fluidVolume'], wall_pos=self.boundaryPositions,
+                     wall_volume=self.fluidVolume)
+        self.normalizationMatrix = M
+        self.fluidL, self.eigVals = pinv2x2(M, self.P)
         out = self._sum("normalization", st, pos=st['fluidPosition'], wall_pos=self.boundaryPositions,
                         wall_volume=self.fluidVolume)
         return out.view(n, 2, 2)
@@ -912,3 +986,129 @@ class dfsphModule(Module):
 
     def divergenceSolver(self, simulationState, simulation):
         return self.DFSPH(simulationState, simulation, False)
+
+
+# ----------------------------------------------------------------------------- delta+ surface / shifting
+class deltaPlusModule(Module):
+    """src/modules/deltaPlus.py:36-251 on GPU kernels (sph_surface_term): surface detection
+    (normalization matrix with its singular values, the lambda gradient and the fluid normal,
+    the angle test and the surface classification) and the delta+ particle shift.
+
+    What the reference does and this keeps: the wall part of the lambda gradient takes the wall
+    particle's volume as fluidArea[b] / fluidDensity[b], indexing the fluid arrays with the
+    wall index (deltaPlus.py:150), so a wall index at or above the fluid count raises
+    IndexError as it does there; the shift evaluates W at the packing ratio for its k0
+    (deltaPlus.py:90), which the reference can only evaluate once the ratio is a tensor."""
+
+    def __init__(self):
+        super().__init__('densityInterpolation', 'Evaluates density at the current timestep')
+
+    def exportState(self, simulationState, simulation, grp, mask):
+        if simulation.config['shifting']['enabled']:
+            grp.create_dataset('fluidShifting', data=simulationState['fluidUpdate'].detach().cpu().numpy())
+
+    def initialize(self, simulationConfig, simulationState):
+        cfg = simulationConfig
+        self.support = cfg['particle']['support']
+        self.packing = cfg['particle']['packing']
+        self.restDensity = cfg['fluid']['restDensity']
+        self.scheme = cfg['diffusion']['densityScheme']
+        self.alpha = cfg['diffusion']['alpha']
+        self.delta = cfg['diffusion']['delta']
+        self.c0 = _c0(cfg)
+        self.eps = self.support ** 2 * 0.1
+        self.dtype = cfg['compute']['precision']
+        self.device = cfg['compute']['device']
+        self.P = _params(self.support, self.restDensity, self.c0, alpha=self.alpha, delta=self.delta)
+
+    @staticmethod
+    def _walls(simulation, n):
+        bm = getattr(simulation, 'boundaryModule', None)
+        if bm is None or not getattr(bm, 'active', False) or getattr(bm, '_bf', None) is None:
+            return None, None, 0
+        return bm, bm._bf, bm.numPtcls
+
+    def computeShiftAmount(self, simulationState, simulation):
+        st = simulationState
+        n = st['fluidPosition'].shape[0]
+        cfg = getattr(simulation, 'config', None)
+        c0 = cfg['fluid']['c0'] if cfg else self.c0
+        packing = cfg['particle']['packing'] if cfg else self.packing
+        bm, walls, nb = self._walls(simulation, n)
+        P = _params(self.support, self.restDensity, c0)
+        out = torch.empty((n, 2), dtype=torch.float32, device=st['fluidPosition'].device)
+        scratch = torch.empty((N.load().sph_surface_scratch_bytes() + 3) // 4, dtype=torch.float32, device=out.device)
+        surface_term("shift", P, n, nb, out=out, out2=scratch, fluid=st, walls=walls, packing=packing, cfl=1.5,
+                     vel=st['fluidVelocity'], area=st['fluidArea'], rho=st['fluidDensity'],
+                     wall_area=bm.boundaryVolume if bm else None, wall_rho=bm.boundaryDensity if bm else None)
+        st['shiftAmount'] = out
+
+    def computeNormalizationmatrix(self, simulationState, simulation):
+        st = simulationState
+        if 'fluidL' in st:
+            self.normalizationMatrix = st['normalizationMatrix']
+            self.fluidL = st['fluidL']
+            self.eigVals = st['eigVals']
+        else:
+            M = pair_term("normalization", st, self.P)
+            bm = getattr(simulation, 'boundaryModule', None)
+            if bm is not None and getattr(bm, 'active', False):
+                M += bm.computeNormalizationMatrices(st, simulation)
+            st['normalizationMatrix'] = M
+            st['fluidL'], st['eigVals'] = pinv2x2(M, self.P)
+        st['fluidLambda'] = st['eigVals'][:, 1]
+
+    def computeFluidNormal(self, simulationState, simulation):
+        st = simulationState
+        n = st['fluidPosition'].shape[0]
+        bm, walls, nb = self._walls(simulation, n)
+        if walls is not None and walls.rows.numel() > 0 and int(walls.rows.max()) >= n:
+            # fluidArea[bb] of deltaPlus.py:150 with a wall index past the fluid arrays
+            raise IndexError(f"index {int(walls.rows.max())} is out of bounds for dimension 0 with size {n}")
+        dev = st['fluidPosition'].device
+        grad = torch.empty((n, 2), dtype=torch.float32, device=dev)
+        normal = torch.empty((n, 2), dtype=torch.float32, device=dev)
+        surface_term("normal", self.P, n, nb, out=grad, out2=normal, fluid=st, walls=walls, area=st['fluidArea'],
+                     rho=st['fluidDensity'], L=st['fluidL'].contiguous(), lambda_=st['fluidLambda'].contiguous(),
+                     wall_lambda=bm.eigVals[:, 1].contiguous() if bm is not None else None)
+        st['lambdaGrad'] = grad
+        st['fluidNormal'] = normal
+
+    def detectFluidSurface(self, simulationState, simulation):
+        st = simulationState
+        n = st['fluidPosition'].shape[0]
+        bm, walls, nb = self._walls(simulation, n)
+        dev = st['fluidPosition'].device
+        lam = st['fluidLambda'].contiguous()
+        mask = torch.empty(n, dtype=torch.float32, device=dev)
+        angles = torch.empty((n, 2), dtype=torch.float32, device=dev)
+        surface_term("angle_mask", self.P, n, nb, out=mask, out2=angles, fluid=st, walls=walls,
+                     normal=st['fluidNormal'], lambda_=lam)
+        st['angleMin'] = angles[:, 0]
+        st['angleMax'] = angles[:, 1]
+        surf = torch.empty(n, dtype=torch.float32, device=dev)
+        surface_term("classify", self.P, n, nb, out=surf, fluid=st, mask=mask, lambda_=lam)
+        st['fluidSurfaceMask'] = surf
+
+    def adjustShiftingAmount(self, simulationState, simulation):
+        st = simulationState
+        n = st['fluidPosition'].shape[0]
+        dev = st['fluidPosition'].device
+        update = torch.empty((n, 2), dtype=torch.float32, device=dev)
+        mask = torch.empty(n, dtype=torch.float32, device=dev)
+        surface_term("shift_adjust", self.P, n, out=update, out2=mask, shift=st['shiftAmount'],
+                     mask=st['fluidSurfaceMask'], normal=st['fluidNormal'])
+        st['shiftAmount'] = update       # the reference adjusts shiftAmount in place
+        st['fluidUpdate'] = update
+        st['fluidSurfaceMask'] = mask
+
+    def detectSurface(self, simulationState, simulation):
+        self.computeNormalizationmatrix(simulationState, simulation)
+        self.computeFluidNormal(simulationState, simulation)
+        self.detectFluidSurface(simulationState, simulation)
+
+    def shift(self, simulationState, simulation):
+        if 'fluidSurfaceMask' not in simulationState:
+            self.detectSurface(simulationState, simulation)
+        self.computeShiftAmount(simulationState, simulation)
+        self.adjustShiftingAmount(simulationState, simulation)
