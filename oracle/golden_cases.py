@@ -35,7 +35,8 @@ def case(g, meta, name):
                  omega_boundary=float(df.get("relaxedJacobiOmega", 0.5)),
                  point_source=bool(m.get("point_source", False)),
                  point_magnitude=float(m.get("gravity_magnitude", 9.81)),
-                 point_center=tuple(m.get("point_center", (0.0, 0.0))))
+                 point_center=tuple(m.get("point_center", (0.0, 0.0))),
+                 boundary_pressure=m.get("boundary_pressure", "PBSPH"))
     walls = S.Walls(torch.from_numpy(sc("wall_pos")), torch.from_numpy(sc("ghost_pos")), torch.from_numpy(sc("wall_area")))
     state = {"x": torch.from_numpy(sc("pos")), "v": torch.from_numpy(sc("vel")), "rho": torch.from_numpy(sc("rho")),
              "area": torch.from_numpy(sc("area"))}

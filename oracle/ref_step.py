@@ -39,7 +39,8 @@ def _modules():
 
 def base_config(scene, scheme="deltaSPH", diffusion="MOG", integration="semiImplicitEuler", dt=None, c0=None,
                 rho0=1000.0, alpha=0.01, delta=0.1, kinematic=0.001, gravity=9.81, point_source=False,
-                point_center=(0.0, 0.0), dfsph=None, cfl_fixed=True, boundary_diffusion=True):
+                point_center=(0.0, 0.0), dfsph=None, cfl_fixed=True, boundary_diffusion=True,
+                boundary_pressure="PBSPH"):
     dx = scene["dx"]
     h = np.float32(scene["h"])
     W, H = scene.get("tank", (None, None))
@@ -52,7 +53,7 @@ def base_config(scene, scheme="deltaSPH", diffusion="MOG", integration="semiImpl
         "particle": {"radius": radius},
         "simulation": {"scheme": scheme, "boundaryScheme": "solid", "verbose": False,
                        "densityScheme": "continuum" if scheme != "dfsph" else "summation", "mode": "default"},
-        "pressure": {"fluidPressureTerm": "TaitEOS", "boundaryPressureTerm": "PBSPH", "gamma": 7.0},
+        "pressure": {"fluidPressureTerm": "TaitEOS", "boundaryPressureTerm": boundary_pressure, "gamma": 7.0},
         "diffusion": {"velocityScheme": "deltaSPH", "densityScheme": diffusion, "alpha": alpha, "delta": delta,
                       "kinematic": kinematic, "boundaryDiffusion": boundary_diffusion},
         "integration": {"scheme": integration, "dt": dt},
@@ -117,6 +118,41 @@ class _Float32Search:
         return call
 
 
+def _precompute_mls_renamed(util):
+    """precomputeMLS (src/util.py:332-384) with its local `kernel` renamed.
+
+    The reference assigns `kernel = kernel(radialDistances, support)` inside the function that
+    calls the module-level `kernel` (:357), so every call raises UnboundLocalError and the
+    ghostMLS / deltaMLS wall pressures cannot run.  This recompiles the reference's own source
+    with every use of that local (not the call) renamed; nothing else changes."""
+    import ast
+    import inspect
+    import textwrap
+    tree = ast.parse(textwrap.dedent(inspect.getsource(util.precomputeMLS)))
+    fn = tree.body[0]
+    fn.decorator_list = []
+    called = {id(c.func) for c in ast.walk(fn) if isinstance(c, ast.Call) and isinstance(c.func, ast.Name)}
+    for node in ast.walk(fn):
+        if isinstance(node, ast.Name) and node.id == "kernel" and id(node) not in called:
+            node.id = "kernelValue"
+    out = {}
+    exec(compile(ast.fix_missing_locations(tree), util.__file__, "exec"), util.__dict__, out)
+    return out["precomputeMLS"]
+
+
+class _FluidVolumeView:
+    """solidBoundary.py:782 reads `self.deltaSPH.fluidVolume`, an attribute nothing in the
+    reference sets (MLSPressure raises AttributeError there); the harness points it at the
+    state's fluidVolume, the fluid's area that evalMLSBoundaries is given right after (:802)."""
+
+    def __init__(self, sim):
+        self.sim = sim
+
+    @property
+    def fluidVolume(self):
+        return self.sim.simulationState["fluidVolume"]
+
+
 def make_simulation(scene, precision="single", **kw):
     """A reference simulation object around `scene`, initialised like initializeSimulation.
     precision="double" runs the reference's own summations in float64."""
@@ -167,6 +203,8 @@ def make_simulation(scene, precision="single", **kw):
         return w.astype(np.float64), torch.from_numpy(g).to(dtype)
 
     R.solidBoundary.samplePolygon = sample_polygon
+    if cfg["pressure"]["boundaryPressureTerm"] in ("ghostMLS", "deltaMLS"):
+        R.solidBoundary.precomputeMLS = _precompute_mls_renamed(R.util)
 
     n = len(scene["pos"])
     T = lambda a: torch.from_numpy(a.copy()).to(dtype)
@@ -192,6 +230,8 @@ def make_simulation(scene, precision="single", **kw):
     sim.simulationState = sim.setupSimulationState(sim.perennialState)
     # walls must be exactly the scene's (the reference keeps its own copies)
     bm = sim.boundaryModule
+    if cfg["pressure"]["boundaryPressureTerm"] == "MLSPressure":
+        bm.deltaSPH = _FluidVolumeView(sim)
     assert np.array_equal(bm.boundaryPositions.to(torch.float32).numpy(), scene["wall_pos"])
     return sim
 

@@ -100,8 +100,11 @@ class Neighbors:
     gf: Pairs | None          # ghost g -> fluid f (rows = g)
 
 
-def search(x32, walls, h, vmin, vmax, dtype):
-    """Pairs with the reference's exact search (the C oracle, pinned to cppSrc/neighSearch.cpp)."""
+def search(x32, walls, h, vmin, vmax, dtype, ghost_from_walls=False):
+    """Pairs with the reference's exact search (the C oracle, pinned to cppSrc/neighSearch.cpp).
+    ghost_from_walls: the ghost pair list is queried from the wall positions, as
+    boundaryNeighborhoodSearch does for the deltaMLS and MLSPressure wall pressures
+    (solidBoundary.py:639-640)."""
     xs = x32.detach().to(torch.float32).numpy()
     hs = np.full(len(xs), np.float32(h), np.float32)
     si = ns.SortInfo(xs, hs, vmin, vmax)
@@ -115,9 +118,10 @@ def search(x32, walls, h, vmin, vmax, dtype):
         rb, cb = ns.nl_query(si, walls.x.numpy(), hb)
         rb, cb = canonical(rb, cb)
         bf = make_pairs(walls.x.to(dtype), X, rb, cb, h, dtype)
-        rg, cg = ns.nl_query(si, walls.xg.numpy(), hb)
+        xq = walls.x if ghost_from_walls else walls.xg
+        rg, cg = ns.nl_query(si, xq.numpy(), hb)
         rg, cg = canonical(rg, cg)
-        gf = make_pairs(walls.xg.to(dtype), X, rg, cg, h, dtype)
+        gf = make_pairs(xq.to(dtype), X, rg, cg, h, dtype)
     return Neighbors(ff, bf, gf)
 
 
@@ -158,6 +162,7 @@ class Params:
     point_source: bool = False          # gravity as -g (x - c) (potential field)
     point_magnitude: float = 1.0
     point_center: tuple = (0.0, 0.0)   # gravity.center
+    boundary_pressure: str = "PBSPH"    # pressure.boundaryPressureTerm: PBSPH | ghostMLS | deltaMLS | MLSPressure
     diffusion: str = "MOG"              # "MOG" | "deltaSPH"
     boundary_diffusion: bool = True
     vmin: np.ndarray = field(default_factory=lambda: np.zeros(2, np.float32))
@@ -222,6 +227,61 @@ def mdbc_density(walls, st, nb: Neighbors, p: Params, dtype):
     return torch.clamp(rho_b, min=1)
 
 
+def mls_pressure(xq, st, P: Pairs, pf, p: Params, nb: int):
+    """precomputeMLS (src/util.py:332-384) and the wall pressure sum of solidBoundary.py:787-790:
+    M_b = sum_j 2 b_j b_j^T V_j W_j with b_j = (1, x_j - x_q), V_j = A_j / (rho~_j rho0);
+    p_b = sum_j (pinv(M_b) e1 . b_j) W_j V_j p_j."""
+    i, j = P.i, P.j
+    x, A, rt = st["x"], st["area"], st["rho"]
+    k = W(P.q, p.h)
+    bij = torch.cat([torch.ones((i.shape[0], 1), dtype=x.dtype), x[j] - xq[i]], 1)
+    V = (A / (rt * p.rho0))[j]
+    M = ssum(2 * torch.einsum("nu,nv->nuv", bij, bij) * (V * k)[:, None, None], i, nb)
+    Me1 = torch.linalg.pinv(M)[:, :, 0]
+    pg = torch.einsum("nd,nd->n", Me1[i], bij) * k * V
+    return ssum(pg * pf[j], i, nb)
+
+
+def mls_boundary_pressure(xb, st, P: Pairs, pf, p: Params, nb: int):
+    """prepareMLSBoundaries + evalMLSBoundaries (src/util.py:283-330), clamped at 0
+    (solidBoundary.py:802-803), with fluidVolume as the fluid's area."""
+    i, j = P.i, P.j
+    x, V = st["x"], st["volume"]
+    k = W(P.q, p.h) * V[j]
+    nom = ssum(k[:, None] * x[j], i, nb)
+    den = ssum(k, i, nb)
+    d = xb.clone()
+    m = den > 1e-9
+    d[m] = nom[m] / den[m, None]
+    xbar = x[j] - d[i]
+    M1 = torch.linalg.pinv(ssum(torch.einsum("nu,nv->nuv", xbar, xbar) * k[:, None, None], i, nb))
+    vec = xbar * k[:, None]
+    bbar = torch.cat([torch.ones((nb, 1), dtype=x.dtype), xb - d], 1)
+    vsum = ssum(vec * pf[j, None], i, nb)
+    alpha = ssum(pf[j] * k, i, nb)
+    s = ssum(k, i, nb)
+    ms = s > 1e-6
+    alpha[ms] = alpha[ms] / s[ms]
+    c = torch.cat([alpha[:, None], torch.matmul(M1, vsum.unsqueeze(2))[:, :, 0]], 1)
+    return torch.clamp(torch.einsum("nu,nu->n", bbar, c), min=0)
+
+
+def wall_pressure(walls, st, nb: Neighbors, rho_b, p: Params, dtype):
+    """solidBoundaryModule.computePressure (solidBoundary.py:772-808): PBSPH = Tait of the mDBC
+    density; ghostMLS / deltaMLS = MLS interpolation of the fluid pressure at the ghost / wall
+    positions; MLSPressure = the Shepard-centred linear MLS fit."""
+    scheme = p.boundary_pressure
+    if scheme == "PBSPH":
+        return tait(rho_b, p)
+    pf = tait(st["rho"], p)
+    if scheme in ("ghostMLS", "deltaMLS"):
+        xq = (walls.xg if scheme == "ghostMLS" else walls.x).to(dtype)
+        return mls_pressure(xq, st, nb.gf, pf, p, walls.n)
+    if scheme == "MLSPressure":
+        return mls_boundary_pressure(walls.x.to(dtype), st, nb.gf, pf, p, walls.n)
+    raise ValueError(scheme)
+
+
 def deltasph_rhs(st, walls, nb: Neighbors, p: Params, dtype):
     """deltaSPHSimulation.timestep, src/deltaSPH.py:146-200, solid walls, continuum density.
     Returns (acceleration, velocity, dpdt, extras)."""
@@ -239,7 +299,7 @@ def deltasph_rhs(st, walls, nb: Neighbors, p: Params, dtype):
     if have_walls:
         rho_b = mdbc_density(walls, st, nb, p, dtype)
         Vb = walls.area.to(dtype) / rho_b
-        pb = tait(rho_b, p)                                                 # solidBoundary.py:802-804 (PBSPH)
+        pb = wall_pressure(walls, st, nb, rho_b, p, dtype)                 # solidBoundary.py:772-808
         B = nb.bf
         bb, bf = B.i, B.j
         gb = gradW(B.q, -B.e, h)                                            # fluid side: e = (x_f - x_b)/r
@@ -442,7 +502,8 @@ def step(state, walls, p: Params, dt, scheme="semiImplicitEuler", solver="deltaS
     A = state["area"].to(dtype)
 
     def rhs(x, v, r):
-        nb = search(x.to(torch.float32), walls, p.h, p.vmin, p.vmax, dtype)
+        nb = search(x.to(torch.float32), walls, p.h, p.vmin, p.vmax, dtype,
+                    ghost_from_walls=p.boundary_pressure in ("deltaMLS", "MLSPressure"))
         st = {"x": x, "v": v, "rho": r, "area": A}
         if solver == "dfsph":
             a, vel, dp, ex = dfsph_rhs(st, walls, nb, p, dt, dtype)

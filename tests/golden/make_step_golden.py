@@ -51,6 +51,15 @@ CASES = {
     "dsph_point_sie": dict(seed=4, steps=3, kw=dict(scheme="deltaSPH", diffusion="deltaSPH",
                                                     integration="semiImplicitEuler", point_source=True,
                                                     point_center=(0.08, 0.16))),
+    # MLS wall pressures (solidBoundary.py:772-808, src/util.py:283-384); the harness patches
+    # of oracle/ref_step.py make them run
+    "dsph_ghostmls_sie": dict(seed=6, steps=2, kw=dict(scheme="deltaSPH", diffusion="deltaSPH",
+                                                       integration="semiImplicitEuler", boundary_pressure="ghostMLS")),
+    "dsph_deltamls_sie": dict(seed=7, steps=2, kw=dict(scheme="deltaSPH", diffusion="deltaSPH",
+                                                       integration="semiImplicitEuler", boundary_pressure="deltaMLS")),
+    "dsph_mlspressure_sie": dict(seed=8, steps=2, kw=dict(scheme="deltaSPH", diffusion="deltaSPH",
+                                                          integration="semiImplicitEuler",
+                                                          boundary_pressure="MLSPressure")),
     "dfsph_sie": dict(seed=3, steps=3, kw=dict(scheme="dfsph", integration="semiImplicitEuler", dt=0.0005,
                                                kinematic=0.01, dfsph=DFSPH, cfl_fixed=False)),
 }
@@ -77,7 +86,8 @@ def main():
                       "fixed_dt": bool(cfg["timestep"]["fixed"]),
                       "point_source": bool(cfg["gravity"]["pointSource"]),
                       "gravity_magnitude": float(cfg["gravity"]["magnitude"]),
-                      "point_center": [float(v) for v in cfg["gravity"]["center"]]}
+                      "point_center": [float(v) for v in cfg["gravity"]["center"]],
+                      "boundary_pressure": cfg["pressure"]["boundaryPressureTerm"]}
         if "dfsph" in cfg:
             meta[name]["dfsph"] = {k: (float(v) if not isinstance(v, bool) else v) for k, v in cfg["dfsph"].items()}
         tag = "" if prec == "single" else "f64_"
