@@ -525,6 +525,15 @@ typedef struct sph_wall_terms_in {
 #define SPH_BWALL_DFSPH_ALPHA 22           /* [nb]  boundaryAlpha (:443-479) */
 #define SPH_BWALL_DFSPH_SOURCE 23          /* [nb]  boundarySource, density solve (:481-520) */
 #define SPH_BWALL_DFSPH_PRESSURE_SUM 24    /* [nb]  boundary kernel sum (:405-441) */
+/* wall pressures of the MLS schemes (solidBoundary.py:772-808) over the ghost pair list
+ * (ghostToFluidNeighbors; for deltaMLS / MLSPressure queried from the wall positions,
+ * :639-640), fluid pressure in `pressure`: */
+#define SPH_BWALL_GHOST_MLS_PRESSURE 25    /* [nb]  ghostMLS: precomputeMLS at the ghost (src/util.py:332-384),
+                                              p_b = sum_j (pinv(M_b) e1 . b_j) W_j V_j p_j, b_j = (1, x_j - x_g),
+                                              M_b = sum_j 2 b_j b_j^T V_j W_j, V_j = A_j / (rho~_j rho0) */
+#define SPH_BWALL_DELTA_MLS_PRESSURE 26    /* [nb]  deltaMLS: the same at the wall position */
+#define SPH_BWALL_MLS_PRESSURE 27          /* [nb]  MLSPressure: prepareMLSBoundaries + evalMLSBoundaries
+                                              (src/util.py:283-330) with V_j = volume, clamped at 0 */
 sph_status_t sph_wall_term(int32_t term, const sph_wall_terms_in* in, const sph_params* params, float* out,
                            int32_t accumulate, void* stream);
 /* Pairs grouped by column (fluid particle): col_offsets [n+1], pairs [num_pairs] = pair
@@ -578,6 +587,8 @@ typedef struct sph_surface_in {
   const float* wall_rho;             /* [nb] boundaryDensity (relative) */
   const float* wall_volume;          /* [nb] boundaryVolume / boundaryDensity */
   const float* wall_lambda;          /* [nb] the walls' eigVals[:, 1] */
+  const float* pressure;             /* [n] fluid pressure (pressureModule.pressure) */
+  const float* wall_pressure;        /* [nb] wall pressure */
   float packing;                     /* particle.packing: k0 = W(packing) of the shift */
   float cfl;                         /* shift CFL (1.5 in the reference) */
   int64_t n, nb;                     /* fluid and wall particles (SPH_SURF_PINV_EIG: n rows) */
@@ -602,6 +613,11 @@ typedef struct sph_surface_in {
 #define SPH_SURF_SHIFT_ADJUST 6        /* out float2 [n] fluidUpdate (length capped at 0.05 h, projected on
                                           the tangent where mask < 1.5, zero where mask < 0.5); out2 [n] the
                                           updated fluidSurfaceMask (deltaPlus.py:207-240) */
+#define SPH_SURF_PRESSURE_ACCEL 7      /* out float2 [n] computePressureAccelDeltaPlus over the fluid pairs
+                                          (pressure.py:31-51): -1/rho_i sum_j p_ij V_j gradW_ij with
+                                          p_ij = p_i + p_j where p_i >= 0 or mask_i < 1.5, else p_j - p_i */
+#define SPH_SURF_WALL_PRESSURE_ACCEL 8 /* out float2 [n] the same over the wall pairs with the wall
+                                          pressure and wall volume (solidBoundary.py:876-884) */
 size_t sph_surface_scratch_bytes(void);
 /* One step of the delta+ module; params gives support, c0.  Asynchronous. */
 sph_status_t sph_surface_term(int32_t term, const sph_surface_in* in, const sph_params* params, float* out,

@@ -50,6 +50,8 @@ struct SurfIn {
   const float* wrho;
   const float* wvol;
   const float* wlambda;
+  const float* pressure;
+  const float* wpressure;
   float packing, cfl;
   int n, nb;
 };
@@ -342,6 +344,44 @@ __global__ void k_surf_shift_adjust(SurfIn in, SphParams P, float2* __restrict__
   mask_out[i] = nm;
 }
 
+// computePressureAccelDeltaPlus (pressure.py:31-51): the pressure term switches to p_j - p_i
+// where p_i < 0 inside the bulk (mask_i >= 1.5), to avoid tensile instability there.  kWall:
+// over the wall pairs of particle i (e_fb = -e_bf, the wall's pressure and volume), as
+// solidBoundary.py:876-884 calls it with (bf, bb).
+template <bool kWall>
+__global__ void __launch_bounds__(128) k_surf_pressure_accel(SurfIn in, SphParams P, float2* __restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= in.n) return;
+  const float pi = in.pressure[i];
+  const bool plus = pi >= 0.f || in.mask[i] < 1.5f;
+  float sx = 0.f, sy = 0.f;
+  if (!kWall) {
+    for (int k = in.off[i], k1 = in.off[i + 1]; k < k1; ++k) {
+      const int j = (int)in.cols[k];
+      const float2 e = in.dist[k];
+      const float gw = kGW(in.radial[k], P.c_g);
+      const float pj = in.pressure[j];
+      const float c = (plus ? pi + pj : pj - pi) * in.volume[j];
+      sx += c * (e.x * gw);
+      sy += c * (e.y * gw);
+    }
+  } else if (in.fwoff) {
+    for (int t = in.fwoff[i], t1 = in.fwoff[i + 1]; t < t1; ++t) {
+      const int k = in.fwpairs[t];
+      const int b = (int)in.wrows[k];
+      if ((unsigned)b >= (unsigned)in.nb) continue;
+      const float2 e = in.wdist[k];
+      const float gw = kGW(in.wradial[k], P.c_g);
+      const float pb = in.wpressure[b];
+      const float c = (plus ? pi + pb : pb - pi) * in.wvol[b];
+      sx += c * (-e.x * gw);
+      sy += c * (-e.y * gw);
+    }
+  }
+  const float ir = -1.0f / (in.rho[i] * P.rho0);
+  out[i] = make_float2(ir * sx, ir * sy);
+}
+
 }  // namespace sph
 
 using namespace sph;
@@ -379,6 +419,8 @@ static SurfIn to_surf(const sph_surface_in* in) {
   t.wrho = in->wall_rho;
   t.wvol = in->wall_volume;
   t.wlambda = in->wall_lambda;
+  t.pressure = in->pressure;
+  t.wpressure = in->wall_pressure;
   t.packing = in->packing;
   t.cfl = in->cfl;
   t.n = (int)in->n;
@@ -419,6 +461,12 @@ sph_status_t sph_surface_term(int32_t term, const sph_surface_in* in, const sph_
            params->c0 > 0.f;
       break;
     case SPH_SURF_SHIFT_ADJUST: ok = out2 && in->shift && in->mask && in->normal; break;
+    case SPH_SURF_PRESSURE_ACCEL:
+      ok = in->offsets && in->cols && in->dist && in->radial && in->pressure && in->mask && in->volume && in->rho;
+      break;
+    case SPH_SURF_WALL_PRESSURE_ACCEL:
+      ok = in->pressure && in->mask && in->rho && (!walls || (in->wall_pressure && in->wall_volume));
+      break;
     default:
       set_error_text("surface_term: unknown term");
       return SPH_ERR_INVALID_ARGUMENT;
@@ -463,6 +511,12 @@ sph_status_t sph_surface_term(int32_t term, const sph_surface_in* in, const sph_
     case SPH_SURF_SHIFT_ADJUST:
       if (in->n)
         k_surf_shift_adjust<<<grid_for(in->n, 256), 256, 0, st>>>(t, P, reinterpret_cast<float2*>(out), out2);
+      break;
+    case SPH_SURF_PRESSURE_ACCEL:
+      if (in->n) k_surf_pressure_accel<false><<<nbf, 128, 0, st>>>(t, P, reinterpret_cast<float2*>(out));
+      break;
+    case SPH_SURF_WALL_PRESSURE_ACCEL:
+      if (in->n) k_surf_pressure_accel<true><<<nbf, 128, 0, st>>>(t, P, reinterpret_cast<float2*>(out));
       break;
   }
   SPH_CHECK_LAUNCH("surface_term");

@@ -239,6 +239,124 @@ __global__ void __launch_bounds__(128) k_wall_side_term(WallTermIn in, SphParams
   }
 }
 
+// Pseudo-inverse of the symmetric 2x2 matrix [[a, b], [b, d]] with torch.linalg.pinv's
+// default cut-off for float32 input (singular values at or below 2 FLT_EPSILON sigma_max are
+// dropped), in double: (o00, o01, o11).
+__device__ inline void pinv_sym2(double a, double b, double d, double o[3]) {
+  o[0] = o[1] = o[2] = 0.0;
+  const double h = 0.5 * (a + d);
+  const double r = sqrt(0.25 * (a - d) * (a - d) + b * b);
+  const double l[2] = {h + r, h - r};
+  const double smax = fmax(fabs(l[0]), fabs(l[1]));
+  const double tol = 2.0 * 1.1920928955078125e-07 * smax;
+  // eigenvector of l[0]: the larger of (l0 - d, b) and (b, l0 - a); the other one is orthogonal
+  double vx = l[0] - d, vy = b;
+  const double ux = b, uy = l[0] - a;
+  if (ux * ux + uy * uy > vx * vx + vy * vy) {
+    vx = ux;
+    vy = uy;
+  }
+  double nv = sqrt(vx * vx + vy * vy);
+  if (!(nv > 0.0)) {   // b == 0 and a == d: any basis
+    vx = 1.0;
+    vy = 0.0;
+    nv = 1.0;
+  }
+  vx /= nv;
+  vy /= nv;
+  const double ev[2][2] = {{vx, vy}, {-vy, vx}};
+  for (int k = 0; k < 2; ++k) {
+    if (!(fabs(l[k]) > tol)) continue;
+    const double il = 1.0 / l[k];
+    o[0] += il * ev[k][0] * ev[k][0];
+    o[1] += il * ev[k][0] * ev[k][1];
+    o[2] += il * ev[k][1] * ev[k][1];
+  }
+}
+
+// Wall pressures of the MLS schemes, wall b over its ghost pair list (solidBoundary.py:772-808).
+// The moment sums run in float in pair order, as the reference's float32 scatters do; the
+// small systems are solved in double with torch.linalg.pinv's cut-off (pinv3_solve,
+// pinv_sym2).  Walls whose fluid neighbors lie almost on a line give ill-conditioned systems:
+// there the reference's own float32 and float64 runs disagree by more than the pressure.
+template <int kTerm>
+__global__ void __launch_bounds__(128) k_wall_mls_pressure(WallTermIn in, SphParams P, float* __restrict__ out) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= in.nb) return;
+  const int k0 = in.woff[b], k1 = in.woff[b + 1];
+  if (kTerm == SPH_BWALL_MLS_PRESSURE) {
+    // prepareMLSBoundaries: Shepard centre d of the neighbors (weights W_j V_j), then the
+    // centred moment matrix; evalMLSBoundaries: p_b = alpha + (x_b - d) . pinv(M) sum_j xbar_j k_j p_j
+    const float2 xb = in.wpos[b];
+    float nx = 0.f, ny = 0.f, den = 0.f;
+    for (int k = k0; k < k1; ++k) {
+      const int f = (int)in.cols[k];
+      if ((unsigned)f >= (unsigned)in.n) continue;
+      const float kk = kW(in.radial[k], P.c_w) * in.volume[f];
+      const float2 xf = in.pos[f];
+      nx += kk * xf.x;
+      ny += kk * xf.y;
+      den += kk;
+    }
+    const float2 d = den > 1e-9f ? make_float2(nx / den, ny / den) : xb;
+    float m00 = 0.f, m01 = 0.f, m11 = 0.f, vx = 0.f, vy = 0.f, ap = 0.f, as = 0.f;
+    for (int k = k0; k < k1; ++k) {
+      const int f = (int)in.cols[k];
+      if ((unsigned)f >= (unsigned)in.n) continue;
+      const float kk = kW(in.radial[k], P.c_w) * in.volume[f];
+      const float2 xf = in.pos[f];
+      const float bx = xf.x - d.x, by = xf.y - d.y;
+      const float pf = in.pressure[f];
+      m00 += bx * bx * kk;
+      m01 += bx * by * kk;
+      m11 += by * by * kk;
+      vx += bx * kk * pf;
+      vy += by * kk * pf;
+      ap += pf * kk;
+      as += kk;
+    }
+    double Mi[3];
+    pinv_sym2(m00, m01, m11, Mi);
+    const double alpha = as > 1e-6f ? (double)(ap / as) : (double)ap;
+    const double cx = Mi[0] * vx + Mi[1] * vy, cy = Mi[1] * vx + Mi[2] * vy;
+    const double pb = alpha + ((double)xb.x - d.x) * cx + ((double)xb.y - d.y) * cy;
+    out[b] = pb < 0.0 ? 0.f : (float)pb;
+    return;
+  }
+  // precomputeMLS at the ghost (ghostMLS) or the wall position (deltaMLS)
+  const float2 xq = kTerm == SPH_BWALL_GHOST_MLS_PRESSURE ? in.wghost[b] : in.wpos[b];
+  float m00 = 0.f, m01 = 0.f, m02 = 0.f, m11 = 0.f, m12 = 0.f, m22 = 0.f;
+  for (int k = k0; k < k1; ++k) {
+    const int f = (int)in.cols[k];
+    if ((unsigned)f >= (unsigned)in.n) continue;
+    const float t = in.area[f] / (in.rho[f] * P.rho0) * kW(in.radial[k], P.c_w);
+    const float2 xf = in.pos[f];
+    const float dx = xf.x - xq.x, dy = xf.y - xq.y;
+    m00 += 2.0f * t;
+    m01 += 2.0f * dx * t;
+    m02 += 2.0f * dy * t;
+    m11 += 2.0f * (dx * dx) * t;
+    m12 += 2.0f * (dx * dy) * t;
+    m22 += 2.0f * (dy * dy) * t;
+  }
+  const double A[3][3] = {{m00, m01, m02}, {m01, m11, m12}, {m02, m12, m22}};
+  const double e1[3] = {1.0, 0.0, 0.0};
+  double c[3];
+  pinv3_solve(A, e1, c);
+  float s = 0.f;
+  for (int k = k0; k < k1; ++k) {
+    const int f = (int)in.cols[k];
+    if ((unsigned)f >= (unsigned)in.n) continue;
+    const float w = kW(in.radial[k], P.c_w);
+    const float V = in.area[f] / (in.rho[f] * P.rho0);
+    const float2 xf = in.pos[f];
+    const float dx = xf.x - xq.x, dy = xf.y - xq.y;
+    const float pg = (float)(c[0] + c[1] * dx + c[2] * dy) * w * V;
+    s += pg * in.pressure[f];
+  }
+  out[b] = s;
+}
+
 // Stable grouping of pairs by column: counts, offsets, scatter, then every row restored to
 // ascending pair order (rows are short: the walls within h of one particle).
 __global__ void k_pair_col_count(const int64_t* __restrict__ cols, int64_t P, int64_t n,
@@ -378,6 +496,9 @@ sph_status_t sph_wall_term(int32_t term, const sph_wall_terms_in* in, const sph_
     case SPH_BWALL_DFSPH_ALPHA: ok = in->actual_area && in->area && in->wall_actual_area; break;
     case SPH_BWALL_DFSPH_SOURCE: ok = in->actual_area && in->pred_vel && in->wall_rho; break;
     case SPH_BWALL_DFSPH_PRESSURE_SUM: ok = in->actual_area && in->pred_accel; break;
+    case SPH_BWALL_GHOST_MLS_PRESSURE: ok = in->pos && in->area && in->rho && in->pressure && in->wall_ghost; break;
+    case SPH_BWALL_DELTA_MLS_PRESSURE: ok = in->pos && in->area && in->rho && in->pressure && in->wall_pos; break;
+    case SPH_BWALL_MLS_PRESSURE: ok = in->pos && in->volume && in->pressure && in->wall_pos; break;
     default: break;
   }
   SPH_REQUIRE(ok, "wall_term: an array this term reads is missing");
@@ -409,6 +530,14 @@ sph_status_t sph_wall_term(int32_t term, const sph_wall_terms_in* in, const sph_
     SPH_WB(SPH_BWALL_DFSPH_ALPHA)
     SPH_WB(SPH_BWALL_DFSPH_SOURCE)
     SPH_WB(SPH_BWALL_DFSPH_PRESSURE_SUM)
+#define SPH_WM(T) \
+  case T:         \
+    if (in->nb) k_wall_mls_pressure<T><<<nbw, 128, 0, st>>>(t, P, out); \
+    break;
+    SPH_WM(SPH_BWALL_GHOST_MLS_PRESSURE)
+    SPH_WM(SPH_BWALL_DELTA_MLS_PRESSURE)
+    SPH_WM(SPH_BWALL_MLS_PRESSURE)
+#undef SPH_WM
 #undef SPH_WF
 #undef SPH_WB
     default:

@@ -134,7 +134,8 @@ TERM = {"density": 0, "divergence": 1, "mog": 2, "normalization": 3, "renormaliz
         "dfsph_source": 10, "dfsph_pressure_sum": 11, "dfsph_accel": 12}
 WALL = {"density": 0, "dpdt": 1, "normalization": 2, "renormalized_gradient": 3, "pressure_accel": 4,
         "velocity_diffusion": 5, "dfsph_alpha": 6, "dfsph_source": 7, "dfsph_pressure_sum": 8, "dfsph_accel": 9,
-        "b_density": 20, "b_mdbc": 21, "b_dfsph_alpha": 22, "b_dfsph_source": 23, "b_dfsph_pressure_sum": 24}
+        "b_density": 20, "b_mdbc": 21, "b_dfsph_alpha": 22, "b_dfsph_source": 23, "b_dfsph_pressure_sum": 24,
+        "b_ghost_mls_pressure": 25, "b_delta_mls_pressure": 26, "b_mls_pressure": 27}
 WALL_WIDTH = {"density": 1, "dpdt": 1, "normalization": 4, "renormalized_gradient": 2, "pressure_accel": 2,
               "velocity_diffusion": 2, "dfsph_alpha": 4, "dfsph_source": 1, "dfsph_pressure_sum": 1,
               "dfsph_accel": 2}
@@ -428,9 +429,14 @@ class pressureModule(_SummationModule):
         return self.pressure
 
     def computePressureAcceleration(self, simulationState, simulation):
-        if self.simulationScheme == 'deltaPlus':
-            raise N.SPHError("pressureModule: the deltaPlus pressure term is not on this path")
-        self.pressureAccel = pair_term("pressure_accel", simulationState, self.P, pressure=self.pressure)
+        st = simulationState
+        if self.simulationScheme == 'deltaPlus':     # computePressureAccelDeltaPlus (pressure.py:31-51)
+            n = st['fluidPosition'].shape[0]
+            self.pressureAccel = torch.empty((n, 2), dtype=torch.float32, device=st['fluidPosition'].device)
+            surface_term("pressure_accel", self.P, n, out=self.pressureAccel, fluid=st, pressure=self.pressure,
+                         mask=st['fluidSurfaceMask'], volume=st['fluidVolume'], rho=st['fluidDensity'])
+        else:
+            self.pressureAccel = pair_term("pressure_accel", st, self.P, pressure=self.pressure)
         self.pressureAccel += simulation.boundaryModule.computePressureAcceleration(simulationState, simulation)
         simulationState['fluidAcceleration'] += self.pressureAccel
         simulation.sync(simulationState['fluidAcceleration'])
@@ -557,12 +563,12 @@ class SurfaceC(ctypes.Structure):
         "offsets", "cols", "dist", "radial", "wall_offsets", "wall_rows", "wall_cols", "wall_dist", "wall_radial",
         "fluid_wall_offsets", "fluid_wall_pairs", "ww_offsets", "ww_cols", "ww_dist", "ww_radial", "pos", "vel",
         "rho", "area", "volume", "matrix", "L", "lambda_", "normal", "mask", "shift", "wall_pos", "wall_area",
-        "wall_rho", "wall_volume", "wall_lambda")] + [
+        "wall_rho", "wall_volume", "wall_lambda", "pressure", "wall_pressure")] + [
         ("packing", ctypes.c_float), ("cfl", ctypes.c_float), ("n", ctypes.c_int64), ("nb", ctypes.c_int64)]
 
 
 SURF = {"pinv_eig": 0, "wall_normalization": 1, "normal": 2, "angle_mask": 3, "classify": 4, "shift": 5,
-        "shift_adjust": 6}
+        "shift_adjust": 6, "pressure_accel": 7, "wall_pressure_accel": 8}
 
 
 def surface_term(term, P, n, nb=0, out=None, out2=None, fluid=None, walls=None, wall_walls=None, packing=0.0,
@@ -651,8 +657,10 @@ class solidBoundaryModule(BoundaryModule):
         self.c0 = _c0(cfg)
         self.eps = self.support ** 2 * 0.1
         self.restDensity = cfg['fluid']['restDensity']
-        if self.boundaryPressureScheme != 'PBSPH' or self.fluidPressureScheme != 'TaitEOS':
-            raise N.SPHError("solidBoundaryModule: the PBSPH boundary pressure with TaitEOS runs on this path")
+        if self.boundaryPressureScheme not in ('PBSPH', 'ghostMLS', 'deltaMLS', 'MLSPressure') or \
+                self.fluidPressureScheme != 'TaitEOS':
+            raise N.SPHError("solidBoundaryModule: the PBSPH, ghostMLS, deltaMLS and MLSPressure boundary pressures "
+                             "with TaitEOS run on this path")
         self.P = _params(self.support, self.restDensity, self.c0, self.gamma, self.alpha, self.delta)
 
     def setWalls(self, positions, ghostPositions, volumes):
@@ -706,10 +714,13 @@ class solidBoundaryModule(BoundaryModule):
         (self.boundaryToFluidNeighbors, self.boundaryToFluidNeighborDistances,
          self.boundaryToFluidNeighborRadialDistances) = ns.searchExisting(
             self.boundaryPositions, self.boundarySupport, simulationState, simulation)
+        # the ghost pair list; the deltaMLS and MLSPressure wall pressures query it from the wall
+        # positions instead (solidBoundary.py:639-640), and mDBC then uses those pairs too
+        query = self.boundaryPositions if self.boundaryPressureScheme in ('deltaMLS', 'MLSPressure') \
+            else self.boundaryGhostPositions
         (self.ghostToFluidNeighbors, self.ghostToFluidNeighborDistances,
          self.ghostToFluidNeighborRadialDistances) = ns.searchExisting(
-            self.boundaryGhostPositions, self.boundarySupport * self.MLSscale, simulationState, simulation,
-            searchRadius=self.MLSscale)
+            query, self.boundarySupport * self.MLSscale, simulationState, simulation, searchRadius=self.MLSscale)
         self._bf = _WallPairs(self.boundaryToFluidNeighbors, self.boundaryToFluidNeighborDistances,
                               self.boundaryToFluidNeighborRadialDistances, self.numPtcls, n)
         self._gf = _WallPairs(self.ghostToFluidNeighbors, self.ghostToFluidNeighborDistances,
@@ -777,7 +788,22 @@ class solidBoundaryModule(BoundaryModule):
                          wall_volume=self._wall_volume())
 
     def computePressure(self, simulationState, simulation):
-        self.pressure = particle_op("tait", self.boundaryDensity, None, self.P, torch.empty_like(self.boundaryDensity))
+        """solidBoundary.py:772-808: PBSPH = Tait of the mDBC density; the MLS schemes
+        interpolate the fluid pressure (pressureModule.pressure) at the ghost / wall position."""
+        st = simulationState
+        scheme = self.boundaryPressureScheme
+        if scheme == 'PBSPH':
+            self.pressure = particle_op("tait", self.boundaryDensity, None, self.P,
+                                        torch.empty_like(self.boundaryDensity))
+        elif scheme in ('ghostMLS', 'deltaMLS'):
+            self.pressure = self._sum("b_ghost_mls_pressure" if scheme == 'ghostMLS' else "b_delta_mls_pressure", st,
+                                      pairs=self._gf, pos=st['fluidPosition'], area=st['fluidArea'],
+                                      rho=st['fluidDensity'], pressure=simulation.pressureModule.pressure,
+                                      wall_pos=self.boundaryPositions, wall_ghost=self.boundaryGhostPositions)
+        else:
+            self.pressure = self._sum("b_mls_pressure", st, pairs=self._gf, pos=st['fluidPosition'],
+                                      volume=st['fluidVolume'], pressure=simulation.pressureModule.pressure,
+                                      wall_pos=self.boundaryPositions)
         return self.pressure
 
     def computeVelocityDiffusion(self, simulationState, simulation):
@@ -789,6 +815,13 @@ class solidBoundaryModule(BoundaryModule):
     def computePressureAcceleration(self, simulationState, simulation):
         st = simulationState
         self.fluidVolume = self._wall_volume()
+        if self.simulationScheme == 'deltaPlus':     # computePressureAccelDeltaPlus (solidBoundary.py:876-884)
+            n = st['fluidPosition'].shape[0]
+            out = torch.empty((n, 2), dtype=torch.float32, device=st['fluidPosition'].device)
+            surface_term("wall_pressure_accel", self.P, n, self.numPtcls, out=out, walls=self._bf,
+                         pressure=simulation.pressureModule.pressure, wall_pressure=self.pressure,
+                         mask=st['fluidSurfaceMask'], rho=st['fluidDensity'], wall_volume=self.fluidVolume)
+            return out
         return self._sum("pressure_accel", st, rho=st['fluidDensity'], pressure=st['fluidPressure'],
                          wall_pressure=self.pressure, wall_volume=self.fluidVolume)
 

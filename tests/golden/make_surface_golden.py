@@ -9,7 +9,9 @@ perturbed dam-break block and records, in float32 and float64:
     normalization matrix and eigVals);
   * shift: with shifting.enabled the inputs of the first shift call (after the step's
     integration and the new search) and its outputs (shiftAmount before the adjustment,
-    fluidUpdate and fluidSurfaceMask after it).
+    fluidUpdate and fluidSurfaceMask after it);
+  * step: the acceleration, dpdt and wall pressure of the first right-hand side, whose
+    pressure term is the delta+ one (computePressureAccelDeltaPlus, pressure.py:31-51).
 The scene has more fluid particles than wall particles: computeFluidNormal indexes the fluid
 arrays with wall indices (deltaPlus.py:150) and raises otherwise.
 The reference's computeShiftAmount evaluates kernel(packing, support) on a Python float, which
@@ -105,6 +107,17 @@ def run(prec, shifting):
     sm.computeShiftAmount = amount
     sm.shift = shift
     sim.config["shifting"]["enabled"] = shifting
+    orig_timestep = sim.timestep
+
+    def timestep():
+        res = orig_timestep()
+        if "step" not in cap:   # the first right-hand side (deltaPlus pressure term, pressure.py:31-51)
+            st = sim.simulationState
+            cap["step"] = {"out_fluidAcceleration": _np(st["fluidAcceleration"]), "out_dpdt": _np(st["dpdt"]),
+                           "out_boundaryPressure": _np(bm.pressure)}
+        return res
+
+    sim.timestep = timestep
     sim.integrate()
     cfg = sim.config
     meta = {"h": float(sc["h"]), "dx": sc["dx"], "tank": sc["tank"], "c0": float(cfg["fluid"]["c0"]),
@@ -124,7 +137,7 @@ def main():
         meta = m
         for k in ("pos", "vel", "rho", "area", "wall_pos", "ghost_pos", "wall_area", "vmin", "vmax"):
             out[f"scene_{k}"] = sc[k]
-        for part in ("surface", "shift"):
+        for part in ("surface", "shift", "step"):
             for k, v in cap[part].items():
                 if tag and part == "surface" and k.startswith("in_") and not k.startswith("in_boundary"):
                     continue          # the same values as the float32 run's (the first evaluation)

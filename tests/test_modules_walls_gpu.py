@@ -156,3 +156,71 @@ def test_dfsph_timestep_with_walls_matches_reference_step(cuda):
     assert len(dens_errors) == len(ex["density_errors"])
     assert rel(sim.boundaryModule.boundaryDensity.cpu(), ex["rho_b"]) < 1e-5
     assert rel(st["fluidAcceleration"].cpu(), acc) < 5e-3
+
+
+@pytest.mark.parametrize("name", ["dsph_ghostmls_sie", "dsph_deltamls_sie", "dsph_mlspressure_sie"])
+def test_mls_wall_pressures_match_reference(cuda, name):
+    """The MLS wall pressures of solidBoundaryModule.computePressure (ghostMLS, deltaMLS,
+    MLSPressure; solidBoundary.py:772-808), driven in the reference's timestep order on a golden
+    step case, against the reference's own first step (tests/golden/step_golden.npz).
+    Compared on the walls whose MLS system is well conditioned (at least 10 or at most 2 fluid
+    neighbors): on walls with 3-9 neighbors nearly on a line the reference's own float32 and
+    float64 runs differ by more than the pressure itself.  Accelerations are compared on the
+    fluid particles that see no such wall."""
+    import golden_cases as GC
+    from pytorchsph_gb300 import modules as M
+    g, meta = GC.load()
+    m = meta[name]
+    sc = {k: g[f"{name}/scene_{k}"] for k in ("pos", "vel", "rho", "area", "wall_pos", "ghost_pos", "wall_area",
+                                               "vmin", "vmax")}
+    sc["h"] = m["h"]
+    sc["support"] = np.full(len(sc["pos"]), np.float32(m["h"]), np.float32)
+    st = state(sc, cuda, sc["rho"])
+    cfg = config(sc, m["c0"], "continuum")
+    cfg["pressure"]["boundaryPressureTerm"] = m["boundary_pressure"]
+    cfg["diffusion"]["kinematic"] = m["kinematic"]
+    sim = Driver()
+    sim.neighborSearch = M.neighborSearchModule()
+    sim.boundaryModule = M.solidBoundaryModule()
+    sim.densityDiffusionModule = M.densityDiffusionModule()
+    sim.pressureModule = M.pressureModule()
+    dens, grav, mom, visc, lam = (M.densityModule(), M.gravityModule(), M.momentumModule(), M.diffusionModule(),
+                                  M.laminarViscosityModule())
+    pres = sim.pressureModule
+    setup([sim.neighborSearch, sim.boundaryModule, sim.densityDiffusionModule, dens, grav, mom, pres, visc, lam],
+          cfg, st)
+    t = lambda a: torch.as_tensor(np.asarray(a, np.float32), device=cuda).contiguous()
+    sim.boundaryModule.setWalls(t(sc["wall_pos"]), t(sc["ghost_pos"]), t(sc["wall_area"]))
+    sim.neighborSearch.search(st, sim)
+    sim.boundaryModule.boundaryNeighborhoodSearch(st, sim)
+    dens.evaluate(st, sim)
+    sim.boundaryModule.evalBoundaryDensity(st, sim)
+    st["fluidAcceleration"] = torch.zeros_like(st["fluidVelocity"])
+    grav.evaluate(st, sim)
+    mom.computeDpDt(st, sim)
+    sim.densityDiffusionModule.computeDensityDiffusion(st, sim)
+    pres.computePressure(st, sim)
+    pres.computePressureAcceleration(st, sim)
+    visc.evaluate(st, sim)
+    lam.computeLaminarViscosity(st, sim)
+    torch.cuda.synchronize()
+    bm = sim.boundaryModule
+    gp = bm.ghostToFluidNeighbors.cpu().numpy()
+    cnt = np.bincount(gp[0], minlength=bm.numPtcls)
+    good = (cnt >= 10) | (cnt <= 2)
+    ref32 = g[f"{name}/step0_boundaryPressure"]
+    ref64 = g[f"{name}/f64_step0_boundaryPressure"]
+    pb = bm.pressure.cpu().numpy().astype(np.float64)
+    scale = np.abs(ref64[good]).max()
+    assert np.abs(pb[good] - ref32[good]).max() <= 1e-4 * scale
+    assert np.abs(pb[good] - ref64[good]).max() <= 1e-4 * scale
+    assert rel(bm.boundaryDensity.cpu(), g[f"{name}/f64_step0_boundaryDensity"]) < 1e-5
+    # fluid particles whose wall pairs all touch well-conditioned walls
+    bf = bm.boundaryToFluidNeighbors.cpu().numpy()
+    bad_fluid = np.zeros(len(sc["pos"]), bool)
+    bad_fluid[bf[1][~good[bf[0]]]] = True
+    a = st["fluidAcceleration"].cpu().numpy().astype(np.float64)
+    a64 = g[f"{name}/f64_step0_fluidAcceleration"]
+    ok = ~bad_fluid
+    assert ok.sum() > 0.8 * len(ok)
+    assert np.abs(a[ok] - a64[ok]).max() <= 5e-3 * np.abs(a64[ok]).max()

@@ -185,3 +185,58 @@ def test_wall_index_past_fluid_raises(cuda, gold):
     dp.computeNormalizationmatrix(st, sim)
     with pytest.raises(IndexError):
         dp.computeFluidNormal(st, sim)
+
+
+def test_deltaplus_timestep_matches_reference(cuda, gold):
+    """The deltaSPH timestep with the delta+ module (src/deltaSPH.py:146-200 with
+    simulation.scheme = 'deltaPlus': surface detection at step 5 and the surface-switched
+    pressure term computePressureAccelDeltaPlus, pressure.py:31-51, fluid and wall parts),
+    driven through the Module interface from the neighbor search on, against the reference's
+    first right-hand side: the error against the reference's float64 run at most 3x its float32
+    run's own error plus 1e-6 of the maximum."""
+    from pytorchsph_gb300 import modules as M
+    g, m = gold
+    t = lambda a: torch.as_tensor(np.ascontiguousarray(a), device=cuda)
+    _, sim, dp = _setup(g, m, "surface", cuda)
+    cfg = sim.config
+    cfg["gravity"] = {"magnitude": 9.81, "direction": [0.0, -1.0], "pointSource": False, "potentialField": True,
+                      "center": [0.0, 0.0]}
+    pos = g["scene_pos"]
+    n = len(pos)
+    st = {"fluidPosition": t(pos), "fluidVelocity": t(g["scene_vel"]), "fluidDensity": t(g["scene_rho"]),
+          "fluidArea": t(g["scene_area"]), "fluidSupport": torch.full((n,), float(np.float32(m["h"])), device=cuda),
+          "numParticles": n, "fluidRestDensity": torch.full((n,), m["rho0"], device=cuda)}
+    sim.neighborSearch = M.neighborSearchModule()
+    bm = M.solidBoundaryModule()
+    sim.boundaryModule = bm
+    sim.densityDiffusionModule = M.densityDiffusionModule()
+    sim.pressureModule = M.pressureModule()
+    mods = [sim.neighborSearch, bm, sim.densityDiffusionModule, sim.pressureModule, M.densityModule(),
+            M.gravityModule(), M.momentumModule(), M.diffusionModule(), M.laminarViscosityModule(), dp]
+    for mod in mods:
+        for p in mod.getParameters() or []:
+            p.parseConfig(cfg)
+        mod.initialize(cfg, st)
+        mod.resetState(st)
+    dens, grav, mom, visc, lam = mods[4:9]
+    bm.setWalls(t(g["scene_wall_pos"]), t(g["scene_ghost_pos"]), t(g["scene_wall_area"]))
+    sim.neighborSearch.search(st, sim)                                   # 2
+    bm.boundaryNeighborhoodSearch(st, sim)                               # 3
+    dens.evaluate(st, sim)                                               # 4
+    bm.evalBoundaryDensity(st, sim)
+    dp.detectSurface(st, sim)                                            # 5
+    st["fluidAcceleration"] = torch.zeros_like(st["fluidVelocity"])      # 6
+    grav.evaluate(st, sim)                                               # 7
+    mom.computeDpDt(st, sim)                                             # 8
+    sim.densityDiffusionModule.computeDensityDiffusion(st, sim)          # 9
+    sim.pressureModule.computePressure(st, sim)                          # 10
+    sim.pressureModule.computePressureAcceleration(st, sim)
+    visc.evaluate(st, sim)                                               # 11
+    lam.computeLaminarViscosity(st, sim)                                 # 12
+    torch.cuda.synchronize()
+    assert np.array_equal(st["fluidSurfaceMask"].cpu().numpy(), g["surface/out_fluidSurfaceMask"])
+    for key, field in (("fluidAcceleration", "fluidAcceleration"), ("dpdt", "dpdt")):
+        e_gpu = rel(st[field], g[f"f64_step/out_{key}"])
+        e_ref = rel(g[f"step/out_{key}"], g[f"f64_step/out_{key}"])
+        assert e_gpu <= 3 * e_ref + 1e-6, (key, e_gpu, e_ref)
+        assert rel(st[field], g[f"step/out_{key}"]) < 2e-2, key
