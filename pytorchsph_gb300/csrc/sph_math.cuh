@@ -206,16 +206,28 @@ __device__ inline void pinv3_solve(const double A[3][3], const double b[3], doub
     const double c20 = cof(A[0][1], A[1][2], A[0][2], A[1][1]), c21 = cof(A[0][2], A[1][0], A[0][0], A[1][2]),
                  c22 = cof(A[0][0], A[1][1], A[0][1], A[1][0]);
     const double det = fma(A[0][0], c00, fma(A[0][1], c01, A[0][2] * c02));
-    // The bound only decides between two exact-enough paths: its norms run in float.
+    // The bound only decides between two exact-enough paths: its norms run in float, on A
+    // scaled by its largest entry (cofactors by its square, det by its cube), so that the
+    // squares neither underflow nor overflow whatever the matrix's scale (MLS moment
+    // matrices with volumes A / rho0 have entries near 1e-12).
+    double amax = 0.0;
+    for (int r = 0; r < 3; ++r)
+      for (int c = 0; c < 3; ++c) amax = fmax(amax, fabs(A[r][c]));
+    const double is = amax > 0.0 ? 1.0 / amax : 0.0, is2 = is * is;
     float na = 0.f;
     for (int r = 0; r < 3; ++r)
-      for (int c = 0; c < 3; ++c) na += (float)A[r][c] * (float)A[r][c];
-    const float f00 = (float)c00, f01 = (float)c01, f02 = (float)c02, f10 = (float)c10, f11 = (float)c11,
-                f12 = (float)c12, f20 = (float)c20, f21 = (float)c21, f22 = (float)c22;
+      for (int c = 0; c < 3; ++c) {
+        const float v = (float)(A[r][c] * is);
+        na += v * v;
+      }
+    const float f00 = (float)(c00 * is2), f01 = (float)(c01 * is2), f02 = (float)(c02 * is2),
+                f10 = (float)(c10 * is2), f11 = (float)(c11 * is2), f12 = (float)(c12 * is2),
+                f20 = (float)(c20 * is2), f21 = (float)(c21 * is2), f22 = (float)(c22 * is2);
     const float nc = f00 * f00 + f01 * f01 + f02 * f02 + f10 * f10 + f11 * f11 + f12 * f12 + f20 * f20 +
                      f21 * f21 + f22 * f22;
-    // ||A^-1||_F = ||adj A||_F / |det|
-    if (det != 0.0 && (double)na * (double)nc < 1e10 * det * det) {
+    const double ds = det * is2 * is;
+    // ||A^-1||_F = ||adj A||_F / |det|, all three scaled alike
+    if (det != 0.0 && amax > 0.0 && (double)na * (double)nc < 1e10 * ds * ds) {
       const double id = 1.0 / det;  // A^-1 = adj(A) / det, adj(A)[r][c] = cofactor c_cr
       x[0] = fma(c00, b[0], fma(c10, b[1], c20 * b[2])) * id;
       x[1] = fma(c01, b[0], fma(c11, b[1], c21 * b[2])) * id;

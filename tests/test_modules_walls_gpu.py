@@ -163,10 +163,11 @@ def test_mls_wall_pressures_match_reference(cuda, name):
     """The MLS wall pressures of solidBoundaryModule.computePressure (ghostMLS, deltaMLS,
     MLSPressure; solidBoundary.py:772-808), driven in the reference's timestep order on a golden
     step case, against the reference's own first step (tests/golden/step_golden.npz).
-    Compared on the walls whose MLS system is well conditioned (at least 10 or at most 2 fluid
-    neighbors): on walls with 3-9 neighbors nearly on a line the reference's own float32 and
-    float64 runs differ by more than the pressure itself.  Accelerations are compared on the
-    fluid particles that see no such wall."""
+    Compared on the walls whose MLS system is well conditioned, taken as the walls where the
+    reference's own float32 and float64 pressures agree to 1e-5 (plus 1e-3 Pa): walls whose
+    few fluid neighbors lie nearly on a line give ill-conditioned systems, and there the
+    reference disagrees with itself by more than the pressure.  Accelerations are compared on
+    the fluid particles that see no ill-conditioned wall."""
     import golden_cases as GC
     from pytorchsph_gb300 import modules as M
     g, meta = GC.load()
@@ -205,13 +206,12 @@ def test_mls_wall_pressures_match_reference(cuda, name):
     lam.computeLaminarViscosity(st, sim)
     torch.cuda.synchronize()
     bm = sim.boundaryModule
-    gp = bm.ghostToFluidNeighbors.cpu().numpy()
-    cnt = np.bincount(gp[0], minlength=bm.numPtcls)
-    good = (cnt >= 10) | (cnt <= 2)
     ref32 = g[f"{name}/step0_boundaryPressure"]
     ref64 = g[f"{name}/f64_step0_boundaryPressure"]
+    good = np.abs(ref32 - ref64) <= 1e-5 * np.abs(ref64) + 1e-3
     pb = bm.pressure.cpu().numpy().astype(np.float64)
     scale = np.abs(ref64[good]).max()
+    assert good.sum() > 0.7 * len(good)
     assert np.abs(pb[good] - ref32[good]).max() <= 1e-4 * scale
     assert np.abs(pb[good] - ref64[good]).max() <= 1e-4 * scale
     assert rel(bm.boundaryDensity.cpu(), g[f"{name}/f64_step0_boundaryDensity"]) < 1e-5
