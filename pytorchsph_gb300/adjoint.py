@@ -10,6 +10,10 @@ backwards, recomputing each checkpoint segment's states forward first.  Scalars 
 (default) or float32; the search always sees float32 positions, as the reference's does.
 
 Gradients are with respect to the initial velocity field and the artificial viscosity alpha.
+`DropRolloutFunction` puts the rollout behind torch.autograd: its forward records every
+step's neighbor list and a checkpoint every `checkpoint_every` steps, and its backward
+recomputes each segment's states from its checkpoint with the recorded lists (no search)
+and runs the adjoint kernels backwards.
 """
 from __future__ import annotations
 
@@ -83,26 +87,30 @@ class DropRollout:
         self.steps_run += 1
         return off, cols
 
-    def rollout(self, v0, alpha, steps, checkpoints=False):
-        """Final positions after `steps` steps from (x0, v0, rho0); with checkpoints, also the
-        states at every `checkpoint_every`-th step."""
+    def rollout(self, v0, alpha, steps, checkpoints=False, record_pairs=False):
+        """Final positions after `steps` steps from (x0, v0, rho0) and the checkpoints (the states
+        at every `checkpoint_every`-th step, when asked for); with record_pairs also the list of
+        every step's (offsets, columns)."""
         x = self.x0.clone()
         v = v0.to(self.dtype).reshape(self.n, 2).clone()
         rho = self.rho0.clone()
         ck = {}
+        pairs = []
         for k in range(steps):
             if checkpoints and k % self.every == 0:
                 ck[k] = (x.clone(), v.clone(), rho.clone())
-            self.step(x, v, rho, alpha)
-        return x, ck
+            pr = self.step(x, v, rho, alpha)
+            if record_pairs:
+                pairs.append(pr)
+        return (x, ck, pairs) if record_pairs else (x, ck)
 
     # ------------------------------------------------------------------ adjoint
-    def loss_and_grad(self, v0, alpha, target, steps):
-        """Loss mean_i |x_T,i - target_i|^2 and its gradients with respect to v0 [n, 2] and alpha."""
-        xT, ck = self.rollout(v0, alpha, steps, checkpoints=True)
-        diff = xT - target.to(self.dtype)
-        loss = float((diff * diff).sum().item()) / self.n
-        lx = (2.0 / self.n) * diff
+    def vjp(self, ck, alpha, steps, grad_x, pairs=None):
+        """Vector-Jacobian product of the rollout: given d(objective)/d(x_T) = grad_x [n, 2],
+        returns (d/d v0 [n, 2], d/d alpha).  Each checkpoint segment's states are recomputed
+        forward from its checkpoint, with the recorded pair lists when given (else searched
+        again), and the adjoint kernels run the segment's steps backwards."""
+        lx = grad_x.to(self.dtype).reshape(self.n, 2).contiguous().clone()
         lv = torch.zeros_like(lx)
         lr = torch.zeros_like(self.rho0)
         nx, nv, nr = torch.empty_like(lx), torch.empty_like(lv), torch.empty_like(lr)
@@ -115,8 +123,8 @@ class DropRollout:
             seg = []
             for k in range(s0, s1):          # recompute the segment's states
                 state = (x.clone(), v.clone(), rho.clone())
-                pairs = self.step(x, v, rho, alpha)
-                seg.append((state, pairs))
+                pr = self.step(x, v, rho, alpha, pairs[k] if pairs is not None else None)
+                seg.append((state, pr))
             for (xs, vs, rs), (off, cols) in reversed(seg):
                 N.call("sph_drop_adjoint", int(self.fp64), self.n, N.ptr(off), N.ptr(cols), N.ptr(xs), N.ptr(vs),
                        N.ptr(rs), N.ptr(self.area), ctypes.byref(self.P), self.dt, N.ptr(lx), N.ptr(lv), N.ptr(lr),
@@ -125,9 +133,51 @@ class DropRollout:
                 lx, nx = nx, lx
                 lv, nv = nv, lv
                 lr, nr = nr, lr
-        return loss, lv, float(dalpha.sum().item())
+        return lv, dalpha.sum()
+
+    def loss_and_grad(self, v0, alpha, target, steps):
+        """Loss mean_i |x_T,i - target_i|^2 and its gradients with respect to v0 [n, 2] and alpha."""
+        xT, ck, pairs = self.rollout(v0, alpha, steps, checkpoints=True, record_pairs=True)
+        diff = xT - target.to(self.dtype)
+        loss = float((diff * diff).sum().item()) / self.n
+        lv, da = self.vjp(ck, alpha, steps, (2.0 / self.n) * diff, pairs)
+        return loss, lv, float(da.item())
 
     def loss(self, v0, alpha, target, steps):
         xT, _ = self.rollout(v0, alpha, steps)
         d = xT - target.to(self.dtype)
         return float((d * d).sum().item()) / self.n
+
+
+class DropRolloutFunction(torch.autograd.Function):
+    """Final positions x_T [n, 2] of a `steps`-step DropRollout as a differentiable function of
+    the initial velocities v0 [n, 2] and the artificial viscosity alpha (0-d tensor).
+
+    Forward: the GPU rollout, recording each step's neighbor list and a checkpoint every
+    `rollout.every` steps.  Backward: DropRollout.vjp with the recorded lists (the adjoint
+    kernels of sph_drop_adjoint).  The rollout's precision (float32 or float64) is the
+    rollout's; gradients come back in the inputs' dtypes."""
+
+    @staticmethod
+    def forward(ctx, v0, alpha, rollout, steps):
+        a = float(alpha)
+        xT, ck, pairs = rollout.rollout(v0.detach(), a, int(steps), checkpoints=True, record_pairs=True)
+        ctx.rollout, ctx.ck, ctx.pairs, ctx.alpha, ctx.steps = rollout, ck, pairs, a, int(steps)
+        ctx.v_dtype, ctx.a_dtype = v0.dtype, (alpha.dtype if isinstance(alpha, torch.Tensor) else torch.float64)
+        ctx.a_device = alpha.device if isinstance(alpha, torch.Tensor) else v0.device
+        return xT
+
+    @staticmethod
+    def backward(ctx, grad_x):
+        gv, ga = ctx.rollout.vjp(ctx.ck, ctx.alpha, ctx.steps, grad_x, ctx.pairs)
+        ctx.ck = ctx.pairs = None
+        gv = gv.to(ctx.v_dtype) if ctx.needs_input_grad[0] else None
+        ga = ga.to(device=ctx.a_device, dtype=ctx.a_dtype) if ctx.needs_input_grad[1] else None
+        return gv, ga, None, None
+
+
+def drop_rollout(rollout: DropRollout, v0: torch.Tensor, alpha, steps: int) -> torch.Tensor:
+    """x_T = DropRolloutFunction.apply(v0, alpha, rollout, steps)."""
+    if not isinstance(alpha, torch.Tensor):
+        alpha = torch.tensor(float(alpha), dtype=torch.float64, device=v0.device)
+    return DropRolloutFunction.apply(v0, alpha, rollout, steps)
