@@ -623,6 +623,41 @@ size_t sph_surface_scratch_bytes(void);
 sph_status_t sph_surface_term(int32_t term, const sph_surface_in* in, const sph_params* params, float* out,
                               float* out2, void* stream);
 
+/* ---------------------------------------------------------------- periodic boundaries (f4) */
+
+/* createGhostParticlesKernel (src/modules/periodicBC.py:23-103) on the GPU: the ghost copies
+ * of the particles within `band` (= buffer * support) of the domain edges, in the reference's
+ * order: categories x+, x- (periodic_x), y+, y- (periodic_y), then x+y+, x+y-, x-y+, x-y-
+ * (both), each in increasing particle index.  indices [capacity] (int64) and offsets float2
+ * [capacity] (the position offset of each copy, -+(max - min) in float32) receive the
+ * concatenated lists, counts [8] (device) the length of each category (0 for a disabled
+ * one); more than `capacity` copies flags SPH_FLAG_PAIR_CAPACITY.  domain_min / domain_max
+ * are host float[2]. */
+size_t sph_periodic_ghosts_scratch_bytes(int64_t n);
+sph_status_t sph_periodic_ghosts(const float* pos, int64_t n, const float* domain_min, const float* domain_max,
+                                 float band, int32_t periodic_x, int32_t periodic_y, int64_t capacity,
+                                 int64_t* indices, float* offsets, int32_t* counts, int32_t* status, void* scratch,
+                                 size_t scratch_bytes, void* stream);
+/* Periodic neighbor search without ghost copies: a cell grid of cells >= cell_size tiling the
+ * box [domain_min, domain_max) exactly (at least three cells along a periodic direction),
+ * neighbor cells wrapped around periodic edges, and a neighbor seen through an edge tested at
+ * its image position (x_j +- (max - min), rounded to float32 as the reference's ghost
+ * positions are) with the reference predicate sqrtf(fmaf(dx,dx,dy*dy)) < support_i.  The
+ * pairs are the reference's pairs of real particles against real particles and ghosts
+ * (createGhostParticlesKernel + its search), each ghost replaced by its particle: rows /
+ * cols int64 in (i, j) order and codes int8 = (sx + 1) | (sy + 1) << 2 with s the image
+ * shift in units of the box length.  Two passes with the same arguments: count writes
+ * offsets [n+1] (int64), fill the `capacity` pairs. */
+size_t sph_nl_periodic_scratch_bytes(int64_t n, const float* domain_min, const float* domain_max, float cell_size);
+sph_status_t sph_nl_periodic_count(const float* pos, const float* support, int64_t n, const float* domain_min,
+                                   const float* domain_max, float cell_size, int32_t periodic_x, int32_t periodic_y,
+                                   int64_t* offsets, int32_t* status, void* scratch, size_t scratch_bytes,
+                                   void* stream);
+sph_status_t sph_nl_periodic_fill(const float* pos, const float* support, int64_t n, const float* domain_min,
+                                  const float* domain_max, float cell_size, int32_t periodic_x, int32_t periodic_y,
+                                  const int64_t* offsets, int64_t capacity, int64_t* rows, int64_t* cols,
+                                  int8_t* codes, int32_t* status, void* scratch, size_t scratch_bytes, void* stream);
+
 /* ---------------------------------------------------------------- differentiable rollouts */
 
 /* A free fluid (no walls) stepped by the deltaSPH right-hand side (src/deltaSPH.py:146-200:

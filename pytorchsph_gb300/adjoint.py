@@ -170,7 +170,6 @@ class DropRolloutFunction(torch.autograd.Function):
     @staticmethod
     def backward(ctx, grad_x):
         gv, ga = ctx.rollout.vjp(ctx.ck, ctx.alpha, ctx.steps, grad_x, ctx.pairs)
-        ctx.ck = ctx.pairs = None
         gv = gv.to(ctx.v_dtype) if ctx.needs_input_grad[0] else None
         ga = ga.to(device=ctx.a_device, dtype=ctx.a_dtype) if ctx.needs_input_grad[1] else None
         return gv, ga, None, None

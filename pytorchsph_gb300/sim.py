@@ -128,7 +128,7 @@ class Simulation:
         self.support_arr = torch.full((n,), h, dtype=torch.float32, device=dev)
         self.status = torch.zeros(1, dtype=torch.int32, device=dev)
         self.dt = torch.tensor([cfg.dt], dtype=torch.float32, device=dev)
-        self.time = 0.0
+        self.time = torch.zeros(1, dtype=torch.float64, device=dev)   # simulated time, kept on the device
         self.steps = 0
         # grid (constant: given domain, uniform support)
         self.grid = torch.empty(8, dtype=torch.int32, device=dev)
@@ -221,6 +221,9 @@ class Simulation:
                           "area": z(0), "cell_start": torch.zeros(self.cap + 2, dtype=torch.int32, device=dev),
                           "rho": z(0), "volume": z(0), "pressure": z(0), "order": None}
         else:
+            self.scene_walls = {"pos": np.ascontiguousarray(scene["wall_pos"], np.float32),
+                                "ghost": np.ascontiguousarray(scene["ghost_pos"], np.float32),
+                                "area": np.ascontiguousarray(scene["wall_area"], np.float32)}
             wx = torch.as_tensor(np.ascontiguousarray(scene["wall_pos"], np.float32), device=dev)
             order, _, cs = self._sort_keys(wx, nb, "w_")
             self.walls = {"x": self._permute(order, wx),
@@ -345,6 +348,7 @@ class Simulation:
             N.call("sph_integrate_semi_implicit_euler", n, N.ptr(self.arr["x"]), N.ptr(vel), N.ptr(self.arr["rho"]),
                    N.ptr(acc), N.ptr(dpdt), N.ptr(self.dt), c.rest_density, int(cont), N.ptr(xo), N.ptr(vo),
                    N.ptr(ro), N.ptr(self.status), st)
+            self.last["eval"] = {"x": self.arr["x"], "v": self.arr["v"], "rho": self.arr["rho"]}
             self.arr["x"], self.arr["v"], self.arr["rho"] = xo, vo, ro
             self.last["acc_final"] = acc
         elif c.integration == "RK4":
@@ -374,12 +378,15 @@ class Simulation:
             N.call("sph_rk_axpy", n, N.ptr(e["x0"]), N.ptr(e["v0"]), N.ptr(e["r0"]), N.ptr(e["su"]), N.ptr(e["sa"]),
                    N.ptr(e["sd"]), N.ptr(self.dt), 1.0 / 6.0, c.rest_density, N.ptr(xo), N.ptr(vo), N.ptr(ro),
                    N.ptr(self.status), st)
+            self.last["eval"] = {"x": self.arr["x"], "v": self.arr["v"], "rho": self.arr["rho"]}
             self.arr["x"], self.arr["v"], self.arr["rho"] = xo, vo, ro
             self.last["acc_final"] = e["sa"]
             self.extra = {}
         else:
             raise N.SPHError(f"integration scheme {c.integration!r} is not on the GB300 path")
+        self.time += self.dt
         if not c.fixed_dt:
+            self.last["dt_used"] = self.dt.clone()
             sc = self.ws.bytes("dt_scratch", self.lib.sph_dt_scratch_bytes())
             N.call("sph_update_dt", n, N.ptr(self.arr["v"]), N.ptr(self.last["acc_final"]), self.h, c.kinematic, c.cfl,
                    c.c0, int(c.solver in ("deltaSPH", "deltaPlus")), c.dt_min, c.dt_max, N.ptr(self.dt), N.ptr(sc),
@@ -394,6 +401,82 @@ class Simulation:
             raise N.SPHError(f"simulation step: {N.decode_flags(f)}")
         if self.cols is not None and int(self.offsets[self.n].item()) > self.pair_cap:
             raise N.SPHError("neighbor pair buffer too small")
+
+    # ------------------------------------------------------------------ export
+    def export_fields(self) -> dict:
+        """The arrays of the reference's per-step export group (src/simulationBase.py:742-772,
+        solidBoundary.py:263) after the last step, as device tensors in the engine's row order
+        with the UID of each row (int32); issued on the current stream, no host wait.
+        fluidPosition / fluidVelocity are the new state, finalPosition / finalVelocity /
+        fluidDensity the state the last right-hand side was evaluated at, as the reference
+        writes its perennial and simulation states."""
+        if "eval" not in self.last:
+            raise N.SPHError("export_fields: no step has run yet")
+        st = N.stream_ptr()
+        n = self.n
+        c = self.cfg
+        ev = self.last["eval"]
+        f = {"UID": self.arr["uid"], "fluidPosition": self.arr["x"], "fluidVelocity": self.arr["v"],
+             "finalPosition": ev["x"], "finalVelocity": ev["v"], "fluidArea": self.arr["area"],
+             "fluidDensity": ev["rho"], "fluidSupport": self.support_arr, "fluidAcceleration": self.last["acc_final"]}
+        if isinstance(self.last.get("pressure"), torch.Tensor):
+            f["fluidPressure"] = self.last["pressure"]
+        else:
+            p = torch.empty(n, dtype=torch.float32, device=self.device)
+            N.call("sph_particle_op", 0, n, N.ptr(ev["rho"]), None, _ref(self.params), N.ptr(p), 0, st)
+            f["fluidPressure"] = p
+        if c.point_source:
+            g = torch.zeros((n, 2), dtype=torch.float32, device=self.device)
+            N.call("sph_particle_op", 3, n, N.ptr(ev["x"]), None, _ref(self.params), N.ptr(g), 1, st)
+            f["fluidGravity"] = g
+        if c.solver != "dfsph" and isinstance(self.last.get("dpdt"), torch.Tensor):
+            f["fluidDpdt"] = self.last["dpdt"]
+        if self.nb:
+            src = self.dfsph_arrays["wall_rho"] if c.solver == "dfsph" else self.walls["rho"]
+            wr = torch.empty(self.nb, dtype=torch.float32, device=self.device)
+            N.call("sph_scatter_f32", N.ptr(self.walls["order"]), N.ptr(src), self.nb, N.ptr(wr), st)
+            f["boundaryDensity"] = wr
+        return f
+
+    def export_attributes(self) -> dict:
+        """Root attributes of the reference's export file (src/simulationBase.py:452-481) that
+        this engine's configuration determines."""
+        c = self.cfg
+        a = {"simulationScheme": c.solver, "boundaryScheme": "solid",
+             "densityScheme": "summation" if c.solver == "dfsph" else "continuum", "EOSgamma": c.gamma,
+             "fluidPressureTerm": "TaitEOS", "boundaryPressureTerm": "PBSPH", "shiftingScheme": "deltaPlus",
+             "shiftingEnabled": False, "defaultKernel": "wendland2", "device": str(self.device),
+             "floatprecision": "single", "restDensity": c.rest_density, "c0": c.c0, "support": self.h,
+             "velocityDiffusionScheme": "deltaSPH", "densityDiffusionScheme": c.density_diffusion,
+             "alphaDiffusion": c.alpha, "deltaDiffusion": c.delta, "kinematicDiffusion": c.kinematic,
+             "staticBoundary": True, "initialDt": c.dt, "integrationScheme": c.integration, "fixedDt": c.fixed_dt}
+        if not c.point_source:
+            a["fluidGravity"] = list(c.gravity)
+        return a
+
+    def boundary_information(self) -> dict:
+        """The static wall arrays of the reference's boundaryInformation group
+        (src/simulationBase.py:483-491) in the scene's wall order; boundaryNormals point from
+        each wall particle to its mirrored ghost, into the fluid."""
+        if not self.nb:
+            return {}
+        w = self.scene_walls
+        d = w["ghost"].astype(np.float64) - w["pos"].astype(np.float64)
+        nrm = d / np.maximum(np.linalg.norm(d, axis=1, keepdims=True), 1e-30)
+        return {"boundaryPosition": w["pos"], "boundaryVelocity": np.zeros_like(w["pos"]),
+                "boundarySupport": np.full(self.nb, np.float32(self.h), np.float32),
+                "boundaryRestDensity": np.full(self.nb, np.float32(self.cfg.rest_density), np.float32),
+                "boundaryArea": w["area"], "boundaryNormals": nrm.astype(np.float32),
+                "boundaryBodyAssociation": np.zeros(self.nb, np.int64)}
+
+    def export(self, exporter) -> bool:
+        """Queue this step's export group on a pytorchsph_gb300.export.SnapshotExporter: the
+        arrays of export_fields() and the attributes time, timestep and dt (the dt the step
+        used), all copied from the device without a host wait."""
+        f = self.export_fields()
+        f["@time"] = self.time.clone()
+        f["@dt"] = self.last.get("dt_used", self.dt).clone()
+        return exporter.submit(f, timestep=self.steps)
 
     # ------------------------------------------------------------------ output
     def _orig(self, t):

@@ -133,7 +133,7 @@ def test_autograd_function_matches_adjoint_and_gradcheck(cuda):
     loss = ((xT - target) ** 2).sum() / r.n
     loss.backward()
     L, gv, ga = r.loss_and_grad(v0.detach(), 0.015, target, steps)
-    assert float(loss) == L
+    assert float(loss.detach()) == L
     assert torch.equal(v0.grad, gv) and float(alpha.grad) == ga
     # gradcheck on a smaller drop (pair sets do not change under its perturbations)
     sc2, dt2 = drop(120, 1.0)
