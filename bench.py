@@ -204,39 +204,38 @@ def cpu_deltasph_steps(scene, params, steps, diffusion="MOG"):
     return time.perf_counter() - t0
 
 
-def cpu_baseline_serving(steps=3):
+def cpu_baseline_serving(n_requests=1024, steps=2, sizes=(2048, 16384, 131072)):
+    """The restated reference step (oracle/sph_torch.py, float32, torch CPU, every host thread)
+    timed on requests spanning the trace's sizes, for both scene kinds (dam break with walls,
+    drop without), then a log-log fit of seconds per step against particle count per kind,
+    applied to every request of the trace: the CPU's particle-steps/s on the trace's own size
+    and kind mix, and its milliseconds to advance every request by one step."""
     import torch
     from pytorchsph_gb300 import workloads
-    sc, p = workloads.make_request_scene({"kind": "dam_break", "n": 2048, "shape": 1.0})
-    cpu_deltasph_steps(sc, p, 1, p["diffusion"])
-    t = cpu_deltasph_steps(sc, p, steps, p["diffusion"])
-    n = len(sc["pos"])
-    return {"value": n * steps / t, "unit": "particle-steps/s", "cores": torch.get_num_threads(), "kind": "port",
-            "sample": f"{steps} semi-implicit-Euler deltaSPH steps of a {n}-particle dam-break request with the "
-                      f"restated reference step (oracle/sph_torch.py, float32, torch CPU)"}
-
-
-def cpu_dfsph_steps(scene, steps):
-    """Seconds for `steps` DFSPH steps of the restated reference step (oracle/sph_torch.py,
-    float32, torch CPU, solid walls, the bench's solver settings and adaptive dt)."""
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import torch
-    import sph_torch as S
-    p = S.Params(h=scene["h"], c0=float(10 * np.sqrt(2 * 9.81 * scene["column_height"])), kinematic=0.01,
-                 vmin=scene["vmin"], vmax=scene["vmax"], density_threshold=1e-4, divergence_threshold=1e-3,
-                 max_density_iters=100, max_divergence_iters=100)
-    walls = S.Walls(torch.from_numpy(scene["wall_pos"]), torch.from_numpy(scene["ghost_pos"]),
-                    torch.from_numpy(scene["wall_area"]))
-    walls.density_term = S.wall_density_term(walls, scene["h"], torch.float32)
-    st = {"x": torch.from_numpy(scene["pos"]), "v": torch.from_numpy(scene["vel"]),
-          "rho": torch.from_numpy(scene["rho"]), "area": torch.from_numpy(scene["area"])}
-    dt = 2e-4
-    t0 = time.perf_counter()
-    for _ in range(steps):
-        new, _ = S.step(st, walls, p, dt, "semiImplicitEuler", "dfsph", torch.float32)
-        st = {"x": new["x"].float(), "v": new["v"], "rho": new["rho"], "area": st["area"]}
-        dt = S.update_dt(new, p, dt, 1e-6, 1e-3)
-    return time.perf_counter() - t0
+    meas = {}
+    for kind in ("dam_break", "drop"):
+        pts = []
+        for n in sizes:
+            sc, p = workloads.make_request_scene({"kind": kind, "n": n, "shape": 1.0})
+            cpu_deltasph_steps(sc, p, 1, p["diffusion"])
+            t = cpu_deltasph_steps(sc, p, steps, p["diffusion"]) / steps
+            pts.append((len(sc["pos"]), t))
+        meas[kind] = pts
+    fit = {}
+    for kind, pts in meas.items():
+        ln = np.log([q[0] for q in pts])
+        lt = np.log([q[1] for q in pts])
+        fit[kind] = np.polyfit(ln, lt, 1)
+    trace = workloads.serving_trace(n_requests, 50.0, 2048, 131072, 1, seed=0)
+    tot_n = float(sum(r["n"] for r in trace))
+    tot_s = float(sum(np.exp(np.polyval(fit[r["kind"]], np.log(r["n"]))) for r in trace))
+    samples = "; ".join(f"{k}: " + ", ".join(f"{n} particles {1e3 * t:.1f} ms" for n, t in v) for k, v in meas.items())
+    return {"value": tot_n / tot_s, "unit": "particle-steps/s", "cores": torch.get_num_threads(), "kind": "port",
+            "ms_per_trace_step": 1e3 * tot_s,
+            "sample": f"{steps} semi-implicit-Euler deltaSPH steps (restated reference step, float32, torch CPU) "
+                      f"of requests of {', '.join(str(n) for n in sizes)} particles per scene kind ({samples}); "
+                      f"seconds per step fitted log-log in the particle count per kind and summed over the "
+                      f"{n_requests}-request trace"}
 
 
 def serving_workload(args, world):
@@ -302,9 +301,9 @@ def run_reference(args):
     else:
         import torch
         torch.set_num_threads(threads)
-        cb = cpu_baseline_serving(steps=max(1, min(args.steps, 5)))
+        cb = cpu_baseline_serving(args.requests, steps=max(1, min(args.steps, 2)))
         value, unit, sample, cores = cb["value"], cb["unit"], cb["sample"], cb["cores"]
-        ms = 2048 / value * 1e3
+        ms = cb["ms_per_trace_step"]
         config = serving_workload(args, world)
     line = base_line(args, world, value, ms, unit, config)
     line["impl"] = "reference"
@@ -490,7 +489,7 @@ def run_serving(args, dev, world, rank):
                     "requests_completed": len(ttc), "requests_failed": len(srv.failed),
                     "rebuilds": srv.rebuilds, "rebuild_s": srv.rebuild_seconds}
 
-    cpu = cpu_baseline_serving() if rank == 0 and not args.no_cpu_baseline else None
+    cpu = cpu_baseline_serving(args.requests) if rank == 0 and not args.no_cpu_baseline else None
     if rank == 0:
         line = base_line(args, world, value, ms, "particle-steps/s", {
             **serving_workload(args, world), "requests": len(specs), "particles_resident": total_p,

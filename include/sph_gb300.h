@@ -185,7 +185,8 @@ int32_t sph_key_bits(int32_t cell_capacity);
  * [cell_start[c], cell_start[c+1])); order[s] = original index of sorted particle s,
  * ordered by (key, index) exactly as a stable sort; sorted_keys[s] = its key.  Leaves
  * cell_count zeroed.  Cells of more than 2048 particles keep an unreproducible inner
- * order and flag SPH_FLAG_CELL_ORDER. */
+ * order and flag SPH_FLAG_CELL_ORDER.  The sentinel cell (key cell_capacity) is not ordered:
+ * its particles keep the scatter's order. */
 size_t sph_counting_sort_scratch_bytes(int64_t n, int32_t cell_capacity);
 sph_status_t sph_counting_sort(const uint32_t* keys, int64_t n, int32_t cell_capacity, int32_t* cell_count,
                                int32_t* cell_start, uint32_t* order, uint32_t* sorted_keys, int32_t* status,
@@ -352,7 +353,9 @@ sph_status_t sph_scene_encode(const sph_params* params, const sph_grid* grid_hos
                               void* out_host);
 /* (scene, cell) keys + per-cell histogram for sph_counting_sort; cell_capacity = the total
  * slot count, sum over scenes of num_cells_s + 1.  Sets SPH_FLAG_OUT_OF_GRID /
- * SPH_FLAG_NONFINITE for particles put in their scene's outside slot. */
+ * SPH_FLAG_NONFINITE for particles put in their scene's outside slot.  A particle with a
+ * negative scene index (a free slot of a pooled batch) gets the sentinel key cell_capacity,
+ * without a flag, and the batch kernels skip it. */
 sph_status_t sph_batch_cell_keys(const float* pos, int64_t n, const int32_t* sid, const void* scenes,
                                  int32_t cell_capacity, uint32_t* keys, int32_t* cell_count, int32_t* status,
                                  void* stream);
@@ -541,6 +544,20 @@ sph_status_t sph_wall_term(int32_t term, const sph_wall_terms_in* in, const sph_
 size_t sph_transpose_pairs_scratch_bytes(int64_t n);
 sph_status_t sph_transpose_pairs(const int64_t* cols, int64_t num_pairs, int64_t n, int32_t* col_offsets,
                                  int32_t* pairs, void* scratch, size_t scratch_bytes, void* stream);
+
+/* Pooled serving arena (continuous batching without rebuilding the batch): fixed-capacity
+ * particle arrays whose free slots carry scene index -1.  No reference counterpart: the
+ * reference steps one scene at a time. */
+/* sid[begin + k] = scene, uid[begin + k] = k for k < count (a newly admitted scene). */
+sph_status_t sph_arena_set_ids(int32_t* sid, int32_t* uid, int64_t begin, int64_t count, int32_t scene,
+                               void* stream);
+/* Scene `scene`'s x (float2), v (float2), rho in its own particle order: out[uid[i]] = in[i] for
+ * every i < n with sid[i] == scene. */
+sph_status_t sph_arena_extract(const float* x, const float* v, const float* rho, const int32_t* sid,
+                               const int32_t* uid, int64_t n, int32_t scene, float* x_out, float* v_out,
+                               float* rho_out, void* stream);
+/* sid[i] = -1 for every i < n with sid[i] == scene (its particles leave the batch at the next sort). */
+sph_status_t sph_arena_retire(int32_t* sid, int64_t n, int32_t scene, void* stream);
 
 /* ---------------------------------------------------------------- delta+ surface detection and shifting (f3) */
 

@@ -85,6 +85,9 @@ SIGNATURES.update({  # Module-interface terms
     "sph_transpose_pairs_scratch_bytes": (_SZ, [_I64]),
     "sph_transpose_pairs": (_I32, [_P, _I64, _I64, _P, _P, _P, _SZ, _P]),
     "sph_surface_scratch_bytes": (_SZ, []),
+    "sph_arena_set_ids": (_I32, [_P, _P, _I64, _I64, _I32, _P]),
+    "sph_arena_extract": (_I32, [_P, _P, _P, _P, _P, _I64, _I32, _P, _P, _P, _P]),
+    "sph_arena_retire": (_I32, [_P, _I64, _I32, _P]),
     "sph_periodic_ghosts_scratch_bytes": (_SZ, [_I64]),
     "sph_periodic_ghosts": (_I32, [_P, _I64, _P, _P, _F32, _I32, _I32, _I64, _P, _P, _P, _P, _P, _SZ, _P]),
     "sph_nl_periodic_scratch_bytes": (_SZ, [_I64, _P, _P, _F32]),

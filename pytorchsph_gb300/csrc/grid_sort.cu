@@ -219,12 +219,16 @@ __global__ void k_batch_cell_keys(const float2* __restrict__ pos, int64_t n, con
                                   uint32_t* __restrict__ keys, int32_t* __restrict__ cell_count, int32_t* status) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  const SceneDev& S = scenes[sid[i]];
+  // a particle of no scene (scene index < 0: a free or retired slot of a pooled batch) goes to
+  // the sentinel cell after every scene's cells, without a flag
+  const int32_t s = sid[i];
+  const SceneDev& S = scenes[s < 0 ? 0 : s];
   const sph_grid& g = S.g;
   float2 p = pos[i];
-  const bool fits = S.coff >= 0 && S.coff + g.num_cells < cell_capacity;
+  const bool fits = s >= 0 && S.coff >= 0 && S.coff + g.num_cells < cell_capacity;
   uint32_t key = fits ? (uint32_t)(S.coff + g.num_cells) : (uint32_t)cell_capacity;
-  if (!isfinite(p.x) || !isfinite(p.y)) {
+  if (s < 0) {
+  } else if (!isfinite(p.x) || !isfinite(p.y)) {
     flag(status, SPH_FLAG_NONFINITE);
   } else {
     int ix = cell_coord(p.x, g.qmin[0], g.hmax);
@@ -270,17 +274,24 @@ __device__ __forceinline__ uint64_t cell_rank(uint32_t x, const uint32_t* __rest
 // order; the thread of slot t counts the cell's particles that rank below its own and
 // writes its particle to that place (k comparisons per particle, L1-resident).  Cells larger
 // than kSmallCell are queued for k_cell_fix_large by the thread of their first slot.
+// The sentinel cell (the key cell_capacity: particles outside every grid, or of no scene in
+// a pooled batch) keeps the scatter order: nothing reads its order.
 __global__ void __launch_bounds__(256) k_cell_fix(const uint32_t* __restrict__ keys, int64_t n,
                                                   const int32_t* __restrict__ cell_start,
                                                   const uint32_t* __restrict__ tmp, const uint32_t* __restrict__ tie,
                                                   uint32_t* __restrict__ order, uint32_t* __restrict__ sorted_keys,
                                                   int32_t* __restrict__ big_list, int32_t* __restrict__ big_count,
-                                                  const ArraySet rows) {
+                                                  const ArraySet rows, uint32_t sentinel) {
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n) return;
   const uint32_t x = tmp[t];
   const uint32_t c = __ldg(keys + x);
   sorted_keys[t] = c;
+  if (c == sentinel) {
+    order[t] = x;
+    copy_rows(rows, t, x);
+    return;
+  }
   const int b = __ldg(cell_start + c), e = __ldg(cell_start + c + 1);
   if (e - b > kSmallCell) {
     if (t == b) big_list[atomicAdd(big_count, 1)] = (int32_t)c;
@@ -590,7 +601,7 @@ static sph_status_t counting_sort_impl(const uint32_t* keys, int64_t n, int32_t 
   cudaMemsetAsync(big_count, 0, sizeof(int32_t), st);
   k_count_scatter<<<grid_for(n, 256), 256, 0, st>>>(keys, n, cell_start, cell_count, tmp);
   k_cell_fix<<<grid_for(n, 256), 256, 0, st>>>(keys, n, cell_start, tmp, tie, order, sorted_keys, big_list,
-                                               big_count, rows);
+                                               big_count, rows, (uint32_t)cell_capacity);
   k_cell_fix_large<<<4 * kNumSMs, 512, 0, st>>>(cell_start, tmp, tie, order, big_list, big_count, status, rows);
   SPH_CHECK_LAUNCH("counting_sort");
   return SPH_OK;

@@ -532,7 +532,7 @@ __global__ void k_sie(int n, const float2* __restrict__ x, const float2* __restr
 __global__ void __launch_bounds__(128, 8) k_batch_mdbc(FluidView F, WallView W, const SceneDev* __restrict__ scenes,
                                                     const int32_t* __restrict__ wsid) {
   int b = blockIdx.x * blockDim.x + threadIdx.x;
-  if (b >= W.n) return;
+  if (b >= W.n || wsid[b] < 0) return;   // wall of no scene (free slot of a pooled batch)
   const SceneDev& S = scenes[wsid[b]];
   mdbc_body(b, F, W, S.g, S.P, S.coff);
 }
@@ -543,7 +543,7 @@ __global__ void __launch_bounds__(256) k_batch_prep(FluidView F, const SceneDev*
                                                     float4* __restrict__ qv, int32_t* __restrict__ nseg,
                                                     int32_t* __restrict__ seg_start, uint32_t* __restrict__ seg_mask) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= F.n) return;
+  if (i >= F.n || sid[i] < 0) return;   // particle of no scene: never anyone's neighbor
   const SceneDev& S = scenes[sid[i]];
   prep_body(i, F, S.P, xv, qv);
   if (nseg) segments_body(i, F, S.g, S.coff, S.P.search_radius, S.P.thr, nseg, seg_start, seg_mask);
@@ -582,15 +582,16 @@ __global__ void __launch_bounds__(128, 8) k_batch_pass1(FluidView F, const float
   bool live = true;
   if constexpr (kTpp == 1) {
     i = p_lo + (int)(blockIdx.x * blockDim.x + threadIdx.x);
-    if (i >= p_hi) return;
+    if (i >= p_hi || sid[i] < 0) return;
   } else {
     const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int64_t ii = p_lo + g / kTpp;
     sub = (int)(g % kTpp);
     live = ii < p_hi;
     i = live ? (int)ii : p_lo;
+    live = live && sid[i] >= 0;   // a particle of no scene takes part in the lane sums only
   }
-  const SceneDev& S = scenes[sid[i]];
+  const SceneDev& S = scenes[sid[i] < 0 ? 0 : sid[i]];
   const SphParams P = S.P;   // the fields the loop reads, in registers
   const Pass1 o = pass1_body<kCells, kTpp, kScheme>(i, F, xv, qv, W, S.g, P, S.coff, seg, sub, kTpp == 1 || live);
   if (kTpp > 1 && (!live || sub != 0)) return;
@@ -617,15 +618,16 @@ __global__ void __launch_bounds__(128) k_batch_diffusion(FluidView F, const floa
   bool live = true;
   if constexpr (kTpp == 1) {
     i = p_lo + (int)(blockIdx.x * blockDim.x + threadIdx.x);
-    if (i >= p_hi) return;
+    if (i >= p_hi || sid[i] < 0) return;
   } else {
     const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int64_t ii = p_lo + g / kTpp;
     sub = (int)(g % kTpp);
     live = ii < p_hi;
     i = live ? (int)ii : p_lo;
+    live = live && sid[i] >= 0;
   }
-  const SceneDev& S = scenes[sid[i]];
+  const SceneDev& S = scenes[sid[i] < 0 ? 0 : sid[i]];
   const bool act = live && S.P.diffusion == 2;   // the same on all lanes of a particle
   if (kTpp == 1 && !act) return;
   const SphParams P = S.P;   // the fields the loop reads, in registers

@@ -529,6 +529,250 @@ class SceneBatch:
         return tot
 
 
+class ArenaFull(Exception):
+    """The arena has no room for a scene (particles, walls, cells or slots)."""
+
+
+class SceneArena(SceneBatch):
+    """A pooled arena of fixed capacity for continuous batching: scenes are admitted into free
+    particle slots and retired from them between steps, without rebuilding the batch or
+    re-capturing its CUDA graphs.
+
+    The arrays of SceneBatch are allocated for `particles` particles, `walls` wall particles,
+    `cells` cell slots and `slots` scenes.  A slot of no scene carries scene index -1: the sort
+    sends it to the sentinel cell after every scene's cells and the batch kernels skip it, so
+    every step compacts the live scenes to the front of the sorted arrays.  Admission writes
+    the scene's particles after the occupied ones, its static arrays, its scene-table entry
+    and a cell range (first fit; the live scenes' ranges are packed again when no gap fits,
+    which changes no result), and re-sorts the walls; retirement reads the scene's state out
+    in its own particle order and marks its particles free.  Every scene runs with the arena's
+    lanes per particle `tpp` and density-diffusion kernel `scheme` (-1: read per scene); pairs
+    come from the cell rows.  A scene gives the same bits in the arena as alone."""
+
+    def __init__(self, device=None, particles: int = 1 << 20, walls: int = 1 << 16, cells: int = 1 << 20,
+                 slots: int = 256, tpp: int = 1, scheme: int = -1):
+        if tpp not in (1, 2, 4) or scheme not in (-1, 0, 1, 2):
+            raise ValueError("tpp must be 1, 2 or 4 and scheme -1, 0, 1 or 2")
+        self.pairs = "cells"
+        self.lib = N.load()
+        self.device = torch.device(device or torch.device("cuda", torch.cuda.current_device()))
+        dev = self.device
+        self.N, self.WC, self.C, self.S = int(particles), int(walls), int(cells), int(slots)
+        if self.C + 1 >= MAX_CELLS:
+            raise N.SPHError("arena cell tables too large")
+        self.tpp, self.scheme = tpp, scheme
+        self.rec = self.lib.sph_scene_bytes()
+        self.scenes = torch.zeros(self.S * self.rec, dtype=torch.uint8, device=dev)
+        self.cap = self.C
+        self.n = self.N
+        n = self.N
+        f2 = lambda m: torch.zeros((m, 2), dtype=torch.float32, device=dev)
+        f1 = lambda m: torch.zeros(m, dtype=torch.float32, device=dev)
+        i1 = lambda m, v=0: torch.full((m,), v, dtype=torch.int32, device=dev)
+        self.a = {"x": f2(n), "v": f2(n), "rho": f1(n) + 1.0, "area": f1(n), "sup": f1(n), "sid": i1(n, -1),
+                  "uid": i1(n)}
+        self.b = {k: v.clone() for k, v in self.a.items()}
+        self.par = 0
+        self.s = None
+        self._inv = i1(n)
+        self.ws = Workspace(dev)
+        self.status = i1(1)
+        self.keys, self.order, self.skeys = i1(n), i1(n), i1(n)
+        self.cell_start = i1(self.C + 2)
+        self.hist = i1(self.C + 1)
+        self.cs_scratch = torch.empty((self.lib.sph_counting_sort_scratch_bytes(n, self.C) + 7) // 8,
+                                      dtype=torch.int64, device=dev)
+        self.dpdt, self.acc = f1(n), f2(n)
+        self.any_renorm = scheme in (-1, 2)
+        self.grad_rho = f2(n) if self.any_renorm else None
+        self.forces_scratch = torch.empty((self.lib.sph_deltasph_scratch_bytes(n) + 7) // 8, dtype=torch.int64,
+                                          device=dev)
+        self.groups = [[0, n, tpp, scheme]]
+        self._groups_c = (ForceGroupC * 1)(ForceGroupC(0, n, tpp, scheme))
+        # walls: an unsorted staging list (live walls first) and the sorted arrays the graph reads
+        W = self.WC
+        self.nb = W
+        self.ws_w = {"x": f2(W), "ghost": f2(W), "area": f1(W), "sid": i1(W, -1), "uid": i1(W)}
+        self.w = {"x": f2(W), "ghost": f2(W), "area": f1(W), "sid": i1(W, -1), "cell_start": i1(self.C + 2),
+                  "rho": f1(W) + 1.0, "vol": f1(W), "p": f1(W), "order": i1(W)}
+        self._wkeys, self._wskeys, self._whist = i1(W), i1(W), i1(self.C + 1)
+        self._wcs = torch.empty((self.lib.sph_counting_sort_scratch_bytes(W, self.C) + 7) // 8, dtype=torch.int64,
+                                device=dev)
+        self.wall_view = WallViewC(N.ptr(self.w["x"]), N.ptr(self.w["ghost"]), N.ptr(self.w["area"]),
+                                   N.ptr(self.w["cell_start"]), W, N.ptr(self.w["rho"]), N.ptr(self.w["vol"]),
+                                   N.ptr(self.w["p"]))
+        self.counts = self.offsets = self.cols = None
+        self.pair_cap = 0
+        self.graph = None
+        self._side = torch.cuda.Stream(dev)
+        self.steps_done = 0
+        # host bookkeeping
+        self.slots = {}                    # slot -> dict(spec, n, nb, coff, ncells, grid)
+        self.free_slots = list(range(self.S))
+        self.occupied = 0                  # particle slots in use (live + retired before the next sort)
+        self.live_n = 0
+        self.walls_n = 0
+        self.specs = []
+        self._staging = []
+        self._sort_walls()
+
+    # ------------------------------------------------------------------ bookkeeping
+    def _alloc_cells(self, size):
+        used = sorted((d["coff"], d["ncells"]) for d in self.slots.values())
+        at = 0
+        for c, k in used:
+            if c - at >= size:
+                return at
+            at = c + k
+        if self.C - at >= size:
+            return at
+        if self.C - sum(k for _, k in used) >= size:   # pack the live scenes' ranges, then append
+            self._pack_cells()
+            return sum(k for _, k in used)
+        return None
+
+    def _pack_cells(self):
+        at = 0
+        for slot in sorted(self.slots, key=lambda t: self.slots[t]["coff"]):
+            d = self.slots[slot]
+            d["coff"] = at
+            self._write_scene(slot)
+            at += d["ncells"]
+        self._sort_walls()
+
+    def _write_scene(self, slot):
+        d = self.slots[slot]
+        sp = d["spec"]
+        h = float(np.float32(sp.scene["support"][0]))
+        P = _params_for(sp.cfg, h, d["grid"].num_cells, sp.cell_ratio)
+        buf = ctypes.create_string_buffer(self.rec)
+        N.check(self.lib.sph_scene_encode(ctypes.byref(P), ctypes.byref(d["grid"]), d["coff"], sp.cfg.dt, buf),
+                "scene_encode")
+        # through pinned memory, so the host does not wait for the queued steps; the staging row
+        # is kept until an event after the copy has passed
+        row = torch.frombuffer(bytearray(buf.raw), dtype=torch.uint8).pin_memory()
+        self.scenes[slot * self.rec:(slot + 1) * self.rec].copy_(row, non_blocking=True)
+        ev = torch.cuda.Event()
+        ev.record()
+        self._staging = [(e, t) for e, t in self._staging if not e.query()] + [(ev, row)]
+
+    def _sort_walls(self):
+        """Sort the staging walls by (scene, cell) into the arrays the batch kernels read; the
+        staging list becomes the sorted one (live walls first)."""
+        st = N.stream_ptr()
+        W = self.WC
+        s = self.ws_w
+        N.call("sph_batch_cell_keys", N.ptr(s["x"]), W, N.ptr(s["sid"]), N.ptr(self.scenes), self.C,
+               N.ptr(self._wkeys), N.ptr(self._whist), N.ptr(self.status), st)
+        N.call("sph_counting_sort", N.ptr(self._wkeys), W, self.C, N.ptr(self._whist), N.ptr(self.w["cell_start"]),
+               N.ptr(self.w["order"]), N.ptr(self._wskeys), N.ptr(self.status), N.ptr(self._wcs),
+               self._wcs.numel() * 8, st)
+        for k in ("x", "ghost", "area", "sid"):
+            self._perm(self.w["order"], s[k], out=self.w[k])
+            s[k].copy_(self.w[k])
+
+    def fits(self, spec) -> bool:
+        n = len(spec.scene["pos"])
+        nb = len(spec.scene.get("wall_pos", ()))
+        return bool(self.free_slots) and self.occupied + n <= self.N and self.walls_n + nb <= self.WC
+
+    # ------------------------------------------------------------------ admission / retirement
+    def admit(self, spec, state=None) -> int:
+        """Put a scene into the arena between steps; returns its slot.  Raises ArenaFull when
+        its particles, walls, cells or a slot do not fit.  `state` (x, v, rho device or host
+        arrays in the scene's particle order) continues a scene instead of starting it."""
+        cfg = spec.cfg
+        if cfg.solver != "deltaSPH" or cfg.integration != "semiImplicitEuler":
+            raise N.SPHError("batched serving runs deltaSPH with semi-implicit Euler")
+        if self.scheme >= 0 and DIFFUSION[cfg.density_diffusion] != self.scheme:
+            raise N.SPHError("the scene's density diffusion is not the arena's")
+        spec.tpp = self.tpp
+        d = spec.on_device(self.device)
+        n, nb = d["n"], d["nb"]
+        if not self.fits(spec):
+            raise ArenaFull("no room for the scene's particles, walls or a slot")
+        ncells = d["grid"].num_cells + 1
+        coff = self._alloc_cells(ncells)
+        if coff is None:
+            raise ArenaFull("no room in the cell tables")
+        slot = self.free_slots.pop(0)
+        self.slots[slot] = {"spec": spec, "n": n, "nb": nb, "coff": coff, "ncells": ncells, "grid": d["grid"]}
+        self._write_scene(slot)
+        st = N.stream_ptr()
+        lo, hi = self.occupied, self.occupied + n
+        cur = self._aux(self.par)
+        as_dev = lambda t: torch.as_tensor(t, dtype=torch.float32, device=self.device)
+        self.a["x"][lo:hi].copy_(as_dev(state["x"]).reshape(n, 2) if state else d["pos"])
+        self.a["v"][lo:hi].copy_(as_dev(state["v"]).reshape(n, 2) if state else d["vel"])
+        self.a["rho"][lo:hi].copy_(as_dev(state["rho"]) if state else d["rho"])
+        cur["area"][lo:hi].copy_(d["area"])
+        N.call("sph_arena_set_ids", N.ptr(cur["sid"]), N.ptr(cur["uid"]), lo, n, slot, st)
+        self.occupied = hi
+        self.live_n += n
+        if nb:
+            w0, w1 = self.walls_n, self.walls_n + nb
+            self.ws_w["x"][w0:w1].copy_(d["wall_pos"])
+            self.ws_w["ghost"][w0:w1].copy_(d["ghost_pos"])
+            self.ws_w["area"][w0:w1].copy_(d["wall_area"])
+            N.call("sph_arena_set_ids", N.ptr(self.ws_w["sid"]), N.ptr(self.ws_w["uid"]), w0, nb, slot, st)
+            self.walls_n = w1
+            self._sort_walls()
+        self.specs = [self.slots[k]["spec"] for k in sorted(self.slots)]
+        return slot
+
+    def scene_state_device(self, slot, states=None):
+        """x, v, rho of the scene in `slot` in its own particle order (device, fresh tensors)."""
+        d = self.slots[slot]
+        n = d["n"]
+        cur = self._aux(self.par)
+        out = {"x": torch.empty((n, 2), dtype=torch.float32, device=self.device),
+               "v": torch.empty((n, 2), dtype=torch.float32, device=self.device),
+               "rho": torch.empty(n, dtype=torch.float32, device=self.device)}
+        N.call("sph_arena_extract", N.ptr(self.a["x"]), N.ptr(self.a["v"]), N.ptr(self.a["rho"]), N.ptr(cur["sid"]),
+               N.ptr(cur["uid"]), self.N, slot, N.ptr(out["x"]), N.ptr(out["v"]), N.ptr(out["rho"]), N.stream_ptr())
+        return out
+
+    def scene_state(self, slot):
+        return {k: v.cpu().numpy() for k, v in self.scene_state_device(slot).items()}
+
+    def scene_finite(self, slot) -> bool:
+        s = self.scene_state_device(slot)
+        return bool(all(torch.isfinite(t).all() for t in s.values()))
+
+    def retire(self, slot):
+        """Take the scene in `slot` out of the arena; returns its final x, v, rho (device)."""
+        out = self.scene_state_device(slot)
+        d = self.slots.pop(slot)
+        st = N.stream_ptr()
+        N.call("sph_arena_retire", N.ptr(self._aux(self.par)["sid"]), self.N, slot, st)
+        if d["nb"]:
+            N.call("sph_arena_retire", N.ptr(self.ws_w["sid"]), self.WC, slot, st)
+            self.walls_n -= d["nb"]
+            self._sort_walls()
+        self.live_n -= d["n"]
+        self.free_slots.append(slot)
+        self.free_slots.sort()
+        self.specs = [self.slots[k]["spec"] for k in sorted(self.slots)]
+        return out
+
+    def step(self):
+        super().step()
+        self.occupied = self.live_n    # the sort moved every free slot behind the live scenes
+
+    def capture(self):
+        super().capture()              # one step run eagerly, then the graphs recorded
+        self.occupied = self.live_n
+
+    def escaped(self):
+        """Per live slot, how many of its particles were outside its grid at the last sort."""
+        cs = self.cell_start.long()
+        return {slot: int(cs[d["coff"] + d["ncells"]] - cs[d["coff"] + d["ncells"] - 1])
+                for slot, d in self.slots.items()}
+
+    def launches_per_step(self):
+        return 1 + 4 + 1 + 1 + 1 + (1 if self.any_renorm else 0)
+
+
 def estimate_bytes(scene, pairs: str = "cells") -> int:
     """Device bytes one scene needs in a batch: state x2, sort, force records and segment lists,
     and with pairs = "csr" the CSR list at ~30 pairs/particle."""
@@ -539,6 +783,10 @@ def estimate_bytes(scene, pairs: str = "cells") -> int:
 
 
 # ----------------------------------------------------------------------------- continuous batching
+def _timing_event():
+    return torch.cuda.Event(enable_timing=True)
+
+
 @dataclass
 class Request:
     rid: int
@@ -550,6 +798,7 @@ class Request:
     final: dict | None = None
     escaped: int = 0            # particles outside the scene's grid at its last step
     error: str | None = None    # set when the request was retired without completing
+    slot: int = -1              # its slot in the server's arena while live (pooled serving)
 
 
 class Server:
@@ -564,7 +813,8 @@ class Server:
     with `Request.error` set; the other scenes, which share no data with it, carry on."""
 
     def __init__(self, device=None, budget_bytes: float = 60e9, rebuild_every: int = 20, use_graph: bool = True,
-                 keep_final: bool = True, pair_headroom: float = 1.3, pairs: str = "cells", tuning=None):
+                 keep_final: bool = True, pair_headroom: float = 1.3, pairs: str = "cells", tuning=None,
+                 pooled: bool = True):
         self.device = torch.device(device or torch.device("cuda", torch.cuda.current_device()))
         self.budget = budget_bytes
         self.rebuild_every = rebuild_every
@@ -584,6 +834,11 @@ class Server:
         self.rebuild_seconds = 0.0
         self._flags = torch.zeros(1, dtype=torch.int32, pin_memory=True)
         self._last_flags = 0
+        # pooled: the scenes live in a SceneArena (admission and retirement write free slots, the
+        # CUDA graph is captured again only when the arena grows); else the batch is rebuilt
+        self.pooled = pooled and pairs == "cells" and use_graph
+        self.arena: SceneArena | None = None
+        self.arena_grows = 0
 
     def _read_flags(self) -> int:
         """Wait for the batch's work and read its status word (4 bytes over a pinned buffer)."""
@@ -667,12 +922,150 @@ class Server:
         return bool(f & (N.SPH_FLAG_PAIR_CAPACITY | N.SPH_FLAG_NONFINITE)) or \
             any(r.steps_done >= r.spec.steps for r in self.live)
 
+    # ------------------------------------------------------------------ pooled serving
+    def _arena_kind(self, specs):
+        schemes = {DIFFUSION[sp.cfg.density_diffusion] for sp in specs}
+        return schemes.pop() if len(schemes) == 1 else -1
+
+    def _grow(self, need_specs):
+        """A larger arena holding the live scenes (their states carried over) and room for
+        `need_specs`; the one place the batch is rebuilt and its graph captured again."""
+        t = time.perf_counter()
+        live_specs = [r.spec for r in self.live]
+        allsp = live_specs + list(need_specs)
+        n = sum(len(sp.scene["pos"]) for sp in allsp)
+        nb = sum(len(sp.scene.get("wall_pos", ())) for sp in allsp)
+        cells = sum(sp.dev["grid"].num_cells + 1 for sp in allsp)
+        old = self.arena
+        grow = lambda need, cur, lo: max(lo, int(need * 1.5), cur)
+        new = SceneArena(self.device, particles=grow(n, old.N if old else 0, 1 << 16),
+                         walls=grow(nb, old.WC if old else 0, 1 << 12), cells=grow(cells, old.C if old else 0, 1 << 16),
+                         slots=max(256, 2 * len(allsp), old.S if old else 0), tpp=self._tpp,
+                         scheme=self._scheme)
+        for r in self.live:
+            st = old.retire(r.slot)
+            r.slot = new.admit(r.spec, state=st)
+        self.arena = new
+        self.arena_grows += 1
+        self.rebuilds += 1
+        self.rebuild_seconds += time.perf_counter() - t
+
+    def _admit_pooled(self, queue, now):
+        arrived = []
+        used = sum(estimate_bytes(r.spec.scene, self.pairs) for r in self.live)
+        while queue and queue[0].arrival <= now:
+            need = estimate_bytes(queue[0].spec.scene, self.pairs)
+            if used + need > self.budget and (self.live or arrived):
+                break
+            arrived.append(queue.pop(0))
+            used += need
+        if not arrived:
+            return False
+        t = time.perf_counter()
+        for r in arrived:
+            if self.tuning is not None:
+                self.tuning.configure(r.spec)
+            r.spec.tpp = self._tpp
+        upload_scenes([r.spec for r in arrived], self.device)   # one upload and grid launch
+        for k, r in enumerate(arrived):
+            try:
+                if self.arena is None:
+                    raise ArenaFull("no arena yet")
+                r.slot = self.arena.admit(r.spec)
+            except ArenaFull:
+                self._grow([q.spec for q in arrived[k:]])
+                r.slot = self.arena.admit(r.spec)
+            r.admitted = now
+            self.live.append(r)
+        self.admit_seconds += time.perf_counter() - t
+        return True
+
+    def _retire_pooled(self, r, now, error=None):
+        st = self.arena.retire(r.slot)
+        r.finished = now
+        if error:
+            r.error = error
+            self.failed.append(r)
+        elif self.keep_final:
+            host = {k: torch.empty(v.shape, dtype=v.dtype, pin_memory=True) for k, v in st.items()}
+            for k in st:
+                host[k].copy_(st[k], non_blocking=True)
+            r.final = host                     # numpy after the run's last synchronisation
+        r.spec.dev = None
+        self.live.remove(r)
+
+    def _run_pooled(self, queue, t0, max_wall):
+        self._scheme = self._arena_kind([r.spec for r in queue])
+        self._tpp = 1
+        self.admit_seconds = 0.0
+        flags = torch.zeros(2, dtype=torch.int32, pin_memory=True)
+        done = [None, None]          # event after each of the last two steps' status copies
+        timed = []                   # (start event, end event, live scenes) per step
+        k = 0
+        while queue or self.live:
+            now = time.perf_counter() - t0
+            if now > max_wall:
+                break
+            e0 = _timing_event()
+            e0.record()
+            self._admit_pooled(queue, now)
+            if not self.live:
+                if queue:
+                    time.sleep(max(0.0, min(queue[0].arrival - (time.perf_counter() - t0), 0.01)))
+                continue
+            a = self.arena
+            if a.graph is None:
+                a.capture()          # runs one step eagerly, then records the step's graphs
+            else:
+                a.step()
+            # the status word of this step to pinned memory, then cleared for the next one
+            flags[k % 2:k % 2 + 1].copy_(a.status, non_blocking=True)
+            ev = torch.cuda.Event()
+            ev.record()
+            a.status.zero_()
+            e1 = _timing_event()
+            e1.record()
+            timed.append((e0, e1, len(self.live)))
+            done[k % 2] = ev
+            n_live = a.live_n
+            for r in list(self.live):
+                r.steps_done += 1
+            self.particle_steps += n_live
+            self.batch_steps += 1
+            now = time.perf_counter() - t0
+            for r in [r for r in self.live if r.steps_done >= r.spec.steps]:
+                self._retire_pooled(r, now)
+            # the previous step's status (its work is done once this step has been queued)
+            prev = done[(k - 1) % 2] if k else None
+            if prev is not None:
+                prev.synchronize()
+                f = int(flags[(k - 1) % 2])
+                self._last_flags = f
+                if f & N.SPH_FLAG_NONFINITE:
+                    torch.cuda.synchronize()
+                    for r in list(self.live):
+                        if not a.scene_finite(r.slot):
+                            self._retire_pooled(r, time.perf_counter() - t0, error="non-finite state")
+            k += 1
+        torch.cuda.synchronize()
+        for r in self.requests_all:
+            if isinstance(r.final, dict) and r.final and isinstance(next(iter(r.final.values())), torch.Tensor):
+                r.final = {kk: v.numpy() for kk, v in r.final.items()}
+        for e0, e1, nl in timed:
+            self.step_latency.append((e0.elapsed_time(e1) / 1e3, nl))
+        if self.arena is not None:
+            self.arena.check()
+        return time.perf_counter() - t0
+
     def run(self, requests, time_scale: float = 1.0, max_wall: float = 600.0):
         """Serve `requests` (arrival times scaled by time_scale); returns the wall seconds."""
         queue = sorted(requests, key=lambda r: r.arrival)
         for r in queue:
             r.arrival *= time_scale
         t0 = time.perf_counter()
+        if self.pooled:
+            self.requests_all = list(queue)
+            return self._run_pooled(queue, t0, max_wall)
         since = 0
         while queue or self.live:
             now = time.perf_counter() - t0
