@@ -238,6 +238,29 @@ def cpu_baseline_serving(n_requests=1024, steps=2, sizes=(2048, 16384, 131072)):
                       f"{n_requests}-request trace"}
 
 
+def cpu_dfsph_steps(scene, steps):
+    """Seconds for `steps` DFSPH steps of the restated reference step (oracle/sph_torch.py,
+    float32, torch CPU, solid walls, the bench's solver settings and adaptive dt)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import torch
+    import sph_torch as S
+    p = S.Params(h=scene["h"], c0=float(10 * np.sqrt(2 * 9.81 * scene["column_height"])), kinematic=0.01,
+                 vmin=scene["vmin"], vmax=scene["vmax"], density_threshold=1e-4, divergence_threshold=1e-3,
+                 max_density_iters=100, max_divergence_iters=100)
+    walls = S.Walls(torch.from_numpy(scene["wall_pos"]), torch.from_numpy(scene["ghost_pos"]),
+                    torch.from_numpy(scene["wall_area"]))
+    walls.density_term = S.wall_density_term(walls, scene["h"], torch.float32)
+    st = {"x": torch.from_numpy(scene["pos"]), "v": torch.from_numpy(scene["vel"]),
+          "rho": torch.from_numpy(scene["rho"]), "area": torch.from_numpy(scene["area"])}
+    dt = 2e-4
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        new, _ = S.step(st, walls, p, dt, "semiImplicitEuler", "dfsph", torch.float32)
+        st = {"x": new["x"].float(), "v": new["v"], "rho": new["rho"], "area": st["area"]}
+        dt = S.update_dt(new, p, dt, 1e-6, 1e-3)
+    return time.perf_counter() - t0
+
+
 def served_accuracy(spec, req, final):
     """Relative density error (max and mean over particles) and position error (max, in
     supports) of a served request's final state against the float64 restated reference step
@@ -358,19 +381,21 @@ def pass1_alg_bytes(batch):
     """Algorithmic HBM bytes of one k_batch_pass1 launch over renormalized scenes.
     Per particle: its two 16-byte neighbor records (read once; the other 27-odd reads of
     them are L1/L2 hits), relative density 4, key 4, scene index 4 read, dpdt 4 + acc 8 +
-    <grad rho> V 8 written.  Pairs from the cell rows: the segment count 4 and 8 per stored
-    segment (start, mask) read (68 per particle + 8 per segment).  CSR pairs: offsets 4 (64)
+    <grad rho> V 8 written.  Pairs from the cell rows: the pair count 4 and the list's words
+    read, 4 bytes per two pairs (68 per particle + 2 per pair).  CSR pairs: offsets 4 (64)
     and 4 per column.  Per wall: position 8 + volume, density, pressure 12."""
+    import ctypes
     import torch
+    from pytorchsph_gb300 import _native as N
     if batch.pairs == "csr":
         P = int(batch.offsets[batch.n].item())
         return batch.n * 64 + 4 * P + batch.nb * 20
-    # the segment counts sit after the records (32 n bytes) and the 8 n masks and 8 n starts
     n = batch.n
-    words = batch.forces_scratch.view(torch.int32)
-    nseg = words[(32 * n + 64 * n) // 4:(32 * n + 64 * n) // 4 + n]
-    segments = int(torch.clamp(nseg, min=0).sum().item())
-    return n * 68 + 8 * segments + batch.nb * 20
+    wo, co, mp = ctypes.c_size_t(), ctypes.c_size_t(), ctypes.c_int32()
+    N.call("sph_deltasph_pair_lists", n, ctypes.byref(wo), ctypes.byref(co), ctypes.byref(mp))
+    counts = batch.forces_scratch.view(torch.int32)[co.value // 4:co.value // 4 + n]
+    words = int(((torch.clamp(counts, min=0) + 1) // 2).sum().item())
+    return n * 68 + 4 * words + batch.nb * 20
 
 
 def phase_times(batch, reps=5):

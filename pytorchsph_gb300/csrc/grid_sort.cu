@@ -186,6 +186,22 @@ __device__ __forceinline__ void warp_count(int32_t* __restrict__ counter, uint32
   if ((int)(threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(counter + key, __popc(peers));
 }
 
+// As warp_count for the lanes with `in`, except that the sentinel key takes one atomic per
+// block: the sentinel cell can hold millions of particles (the free slots of a pooled
+// batch), and one atomic per warp on its single counter would serialize.  Every thread of
+// the block calls it (blocks of a multiple of 32 threads).
+__device__ __forceinline__ void block_count(int32_t* __restrict__ counter, uint32_t key, bool in, uint32_t sentinel) {
+  __shared__ int s_n;
+  if (threadIdx.x == 0) s_n = 0;
+  __syncthreads();
+  const bool sent = in && key == sentinel;
+  if (in && !sent) warp_count(counter, key);
+  const unsigned b = __ballot_sync(0xffffffffu, sent);
+  if ((threadIdx.x & 31) == 0 && b) atomicAdd(&s_n, __popc(b));
+  __syncthreads();
+  if (threadIdx.x == 0 && s_n) atomicAdd(counter + sentinel, s_n);
+}
+
 __global__ void k_cell_keys(const float2* __restrict__ pos, int64_t n, const sph_grid* __restrict__ gp,
                             int32_t cell_capacity, uint32_t* __restrict__ keys, uint32_t* __restrict__ vals,
                             int32_t* __restrict__ cell_count, int32_t* status) {
@@ -217,46 +233,65 @@ __global__ void k_cell_keys(const float2* __restrict__ pos, int64_t n, const sph
 __global__ void k_batch_cell_keys(const float2* __restrict__ pos, int64_t n, const int32_t* __restrict__ sid,
                                   const SceneDev* __restrict__ scenes, int32_t cell_capacity,
                                   uint32_t* __restrict__ keys, int32_t* __restrict__ cell_count, int32_t* status) {
-  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  // a particle of no scene (scene index < 0: a free or retired slot of a pooled batch) goes to
-  // the sentinel cell after every scene's cells, without a flag
-  const int32_t s = sid[i];
-  const SceneDev& S = scenes[s < 0 ? 0 : s];
-  const sph_grid& g = S.g;
-  float2 p = pos[i];
-  const bool fits = s >= 0 && S.coff >= 0 && S.coff + g.num_cells < cell_capacity;
-  uint32_t key = fits ? (uint32_t)(S.coff + g.num_cells) : (uint32_t)cell_capacity;
-  if (s < 0) {
-  } else if (!isfinite(p.x) || !isfinite(p.y)) {
-    flag(status, SPH_FLAG_NONFINITE);
-  } else {
-    int ix = cell_coord(p.x, g.qmin[0], g.hmax);
-    int iy = cell_coord(p.y, g.qmin[1], g.hmax);
-    if (ix >= 0 && iy >= 0 && ix < g.cells_x && iy < g.cells_y && fits)
-      key = (uint32_t)(S.coff + ix + g.cells_x * iy);
-    else
-      flag(status, SPH_FLAG_OUT_OF_GRID);
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const bool in = i < n;   // no early exit: the whole block takes part in block_count
+  uint32_t key = (uint32_t)cell_capacity;
+  if (in) {
+    // a particle of no scene (scene index < 0: a free or retired slot of a pooled batch) goes
+    // to the sentinel cell after every scene's cells, without a flag
+    const int32_t s = sid[i];
+    const SceneDev& S = scenes[s < 0 ? 0 : s];
+    const sph_grid& g = S.g;
+    const float2 p = pos[i];
+    const bool fits = s >= 0 && S.coff >= 0 && S.coff + g.num_cells < cell_capacity;
+    if (fits) key = (uint32_t)(S.coff + g.num_cells);
+    if (s < 0) {
+    } else if (!isfinite(p.x) || !isfinite(p.y)) {
+      flag(status, SPH_FLAG_NONFINITE);
+    } else {
+      int ix = cell_coord(p.x, g.qmin[0], g.hmax);
+      int iy = cell_coord(p.y, g.qmin[1], g.hmax);
+      if (ix >= 0 && iy >= 0 && ix < g.cells_x && iy < g.cells_y && fits)
+        key = (uint32_t)(S.coff + ix + g.cells_x * iy);
+      else
+        flag(status, SPH_FLAG_OUT_OF_GRID);
+    }
+    keys[i] = key;
   }
-  keys[i] = key;
-  warp_count(cell_count, key);
+  block_count(cell_count, key, in, (uint32_t)cell_capacity);
 }
 
 // Counting-sort scatter: slot = cell_start[key] + (remaining count of the cell) - 1, one
-// atomic per distinct key of the warp (the lanes of a key take consecutive slots).
-// Decrementing the histogram leaves it all zero for the next sort.
+// atomic per distinct key of the warp (the lanes of a key take consecutive slots); the
+// sentinel key takes one atomic per block (block_count).  Decrementing the histogram leaves
+// it all zero for the next sort.
 __global__ void k_count_scatter(const uint32_t* __restrict__ keys, int64_t n, const int32_t* __restrict__ cell_start,
-                                int32_t* __restrict__ cell_count, uint32_t* __restrict__ tmp) {
-  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const uint32_t k = keys[i];
-  const unsigned peers = __match_any_sync(__activemask(), k);
-  const int lane = (int)(threadIdx.x & 31), leader = __ffs(peers) - 1;
-  int left = 0;
-  if (lane == leader) left = atomicSub(cell_count + k, __popc(peers));
-  left = __shfl_sync(peers, left, leader);
-  const int slot = cell_start[k] + left - 1 - __popc(peers & ((1u << lane) - 1u));
-  tmp[slot] = (uint32_t)i;
+                                int32_t* __restrict__ cell_count, uint32_t* __restrict__ tmp, uint32_t sentinel) {
+  __shared__ int s_n, s_left;
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const bool in = i < n;   // no early exit: the whole block takes part in the sentinel slots
+  const uint32_t k = in ? keys[i] : 0u;
+  const bool sent = in && k == sentinel;
+  const int lane = (int)(threadIdx.x & 31);
+  if (in && !sent) {
+    const unsigned peers = __match_any_sync(__activemask(), k);
+    const int leader = __ffs(peers) - 1;
+    int left = 0;
+    if (lane == leader) left = atomicSub(cell_count + k, __popc(peers));
+    left = __shfl_sync(peers, left, leader);
+    const int slot = cell_start[k] + left - 1 - __popc(peers & ((1u << lane) - 1u));
+    tmp[slot] = (uint32_t)i;
+  }
+  if (threadIdx.x == 0) s_n = 0;
+  __syncthreads();
+  const unsigned b = __ballot_sync(0xffffffffu, sent);
+  int base = 0;
+  if (lane == 0 && b) base = atomicAdd(&s_n, __popc(b));
+  base = __shfl_sync(0xffffffffu, base, 0);
+  __syncthreads();
+  if (threadIdx.x == 0 && s_n) s_left = atomicSub(cell_count + sentinel, s_n);
+  __syncthreads();
+  if (sent) tmp[cell_start[sentinel] + s_left - 1 - base - __popc(b & ((1u << lane) - 1u))] = (uint32_t)i;
 }
 
 constexpr int kRankSortMax = 1024;   // large cells up to this size are ranked in shared memory
@@ -599,7 +634,7 @@ static sph_status_t counting_sort_impl(const uint32_t* keys, int64_t n, int32_t 
   if (s != SPH_OK) return s;
   if (n == 0) return SPH_OK;
   cudaMemsetAsync(big_count, 0, sizeof(int32_t), st);
-  k_count_scatter<<<grid_for(n, 256), 256, 0, st>>>(keys, n, cell_start, cell_count, tmp);
+  k_count_scatter<<<grid_for(n, 256), 256, 0, st>>>(keys, n, cell_start, cell_count, tmp, (uint32_t)cell_capacity);
   k_cell_fix<<<grid_for(n, 256), 256, 0, st>>>(keys, n, cell_start, tmp, tie, order, sorted_keys, big_list,
                                                big_count, rows, (uint32_t)cell_capacity);
   k_cell_fix_large<<<4 * kNumSMs, 512, 0, st>>>(cell_start, tmp, tie, order, big_list, big_count, status, rows);

@@ -261,13 +261,14 @@ __device__ __forceinline__ float2 pressure_accel(const FluidView& F, const WallV
     cell_of(F.keys[i], g, &cx, &cy);
     const float thr = P.thr;
     for_each_wall(W, g, P.search_radius, cx, cy, xi.x, xi.y, thr, [&](int b, float2 xb) {
-      const Geo e = geo(xb.x, xb.y, xi.x, xi.y, P.inv_h);   // spiky(e_bf), used negated
-      const float gs = kGS(e.q, P.c_s);
+      // spiky(e_bf) = gd (x_b - x_f), used negated
+      const float dx = xb.x - xi.x, dy = xb.y - xi.y;
+      const float gd = spiky_gd(dx * dx + dy * dy, P);
       const float rb = B.wrho[b] * P.rho0;
       const float pb = B.wp[b] / (rb * rb);
-      const float f = -(W.area[b] * P.rho0) * (ppi + pb) * (-gs);
-      wx += f * e.ex;
-      wy += f * e.ey;
+      const float f = (W.area[b] * P.rho0) * (ppi + pb) * gd;
+      wx += f * dx;
+      wy += f * dy;
     });
     ax += wx;
     ay += wy;
@@ -325,9 +326,9 @@ __global__ void __launch_bounds__(256, 8) k_dfsph_solve(FluidView F, WallView W,
         cell_of(F.keys[i], g, &cx, &cy);
         const float thr = P.thr;
         for_each_wall(W, g, P.search_radius, cx, cy, xi.x, xi.y, thr, [&](int b, float2 xb) {
-          const Geo e = geo(xb.x, xb.y, xi.x, xi.y, P.inv_h);
-          const float gs = kGS(e.q, P.c_s);
-          wks += dt * dt * B.waact[b] * (pai.x * (-gs * e.ex) + pai.y * (-gs * e.ey));
+          const float dx = xb.x - xi.x, dy = xb.y - xi.y;
+          const float gd = spiky_gd(dx * dx + dy * dy, P);
+          wks -= dt * dt * B.waact[b] * gd * (pai.x * dx + pai.y * dy);
         });
         ks += wks;
       }
@@ -358,10 +359,10 @@ __global__ void __launch_bounds__(256, 8) k_dfsph_solve(FluidView F, WallView W,
               for (int j = F.cell_start[row + x0]; j < F.cell_start[row + x1 + 1]; ++j) {
                 const float2 xj = F.x[j];
                 if (!(dist2_ref(xb.x, xb.y, xj.x, xj.y) <= thr)) continue;
-                const Geo e = geo(xb.x, xb.y, xj.x, xj.y, P.inv_h);
-                const float gs = kGS(e.q, P.c_s);
+                const float dx = xb.x - xj.x, dy = xb.y - xj.y;
+                const float gd = spiky_gd(dx * dx + dy * dy, P);
                 const float2 paj = B.pa[j];
-                bks += dt * dt * B.aact[j] * (paj.x * (-gs * e.ex) + paj.y * (-gs * e.ey));
+                bks -= dt * dt * B.aact[j] * gd * (paj.x * dx + paj.y * dy);
               }
             }
         }

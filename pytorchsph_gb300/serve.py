@@ -3,7 +3,7 @@
 `SceneBatch` holds any number of independent scenes in one concatenated particle array
 (per-particle scene index, per-scene grid / parameters / dt in a device scene table,
 (scene, cell) sort keys) and advances all of them with one fixed sequence of kernels:
-keys -> counting sort -> permute -> mDBC beside neighbor records + segment lists -> pass 1
+keys -> counting sort -> permute -> mDBC beside neighbor records + pair lists -> pass 1
 -> diffusion + update (with pairs = "csr": a CSR count / scan / fill after the permute).
 Buffers are static, so one batch step can be captured once in a CUDA graph and replayed.
 Scenes never interact: each scene's particles sort into their own cell range and every
@@ -165,8 +165,8 @@ class SceneBatch:
     """A fixed set of scenes stepped together (deltaSPH, semi-implicit Euler).
 
     pairs = "cells": the force passes take each particle's pairs straight from its cell rows
-    (no neighbor list; the records launch keeps each particle's accepted candidates as
-    segment bit masks for both force passes).  pairs =
+    (no neighbor list; the records launch tests the cell rows and keeps each particle's
+    accepted candidates as 16-bit index offsets for both force passes).  pairs =
     "csr": a CSR neighbor list is counted and filled every step first.  Both visit the
     pairs in the same order and give the same sums.
 
@@ -544,8 +544,9 @@ class SceneArena(SceneBatch):
     every step compacts the live scenes to the front of the sorted arrays.  Admission writes
     the scene's particles after the occupied ones, its static arrays, its scene-table entry
     and a cell range (first fit; the live scenes' ranges are packed again when no gap fits,
-    which changes no result), and re-sorts the walls; retirement reads the scene's state out
-    in its own particle order and marks its particles free.  Every scene runs with the arena's
+    which changes no result) and its walls; retirement reads the scene's state out in its own
+    particle order and marks its particles and walls free.  The walls are sorted again once
+    before the next step, however many scenes came or went.  Every scene runs with the arena's
     lanes per particle `tpp` and density-diffusion kernel `scheme` (-1: read per scene); pairs
     come from the cell rows.  A scene gives the same bits in the arena as alone."""
 
@@ -614,6 +615,7 @@ class SceneArena(SceneBatch):
         self.walls_n = 0
         self.specs = []
         self._staging = []
+        self._walls_dirty = False     # walls admitted or retired since the last wall sort
         self._sort_walls()
 
     # ------------------------------------------------------------------ bookkeeping
@@ -638,7 +640,7 @@ class SceneArena(SceneBatch):
             d["coff"] = at
             self._write_scene(slot)
             at += d["ncells"]
-        self._sort_walls()
+        self._walls_dirty = True
 
     def _write_scene(self, slot):
         d = self.slots[slot]
@@ -716,7 +718,7 @@ class SceneArena(SceneBatch):
             self.ws_w["area"][w0:w1].copy_(d["wall_area"])
             N.call("sph_arena_set_ids", N.ptr(self.ws_w["sid"]), N.ptr(self.ws_w["uid"]), w0, nb, slot, st)
             self.walls_n = w1
-            self._sort_walls()
+            self._walls_dirty = True
         self.specs = [self.slots[k]["spec"] for k in sorted(self.slots)]
         return slot
 
@@ -748,18 +750,26 @@ class SceneArena(SceneBatch):
         if d["nb"]:
             N.call("sph_arena_retire", N.ptr(self.ws_w["sid"]), self.WC, slot, st)
             self.walls_n -= d["nb"]
-            self._sort_walls()
+            self._walls_dirty = True
         self.live_n -= d["n"]
         self.free_slots.append(slot)
         self.free_slots.sort()
         self.specs = [self.slots[k]["spec"] for k in sorted(self.slots)]
         return out
 
+    def _walls_ready(self):
+        # one wall sort for all the admissions and retirements since the last step
+        if self._walls_dirty:
+            self._sort_walls()
+            self._walls_dirty = False
+
     def step(self):
+        self._walls_ready()
         super().step()
         self.occupied = self.live_n    # the sort moved every free slot behind the live scenes
 
     def capture(self):
+        self._walls_ready()
         super().capture()              # one step run eagerly, then the graphs recorded
         self.occupied = self.live_n
 
@@ -774,12 +784,13 @@ class SceneArena(SceneBatch):
 
 
 def estimate_bytes(scene, pairs: str = "cells") -> int:
-    """Device bytes one scene needs in a batch: state x2, sort, force records and segment lists,
-    and with pairs = "csr" the CSR list at ~30 pairs/particle."""
+    """Device bytes one scene needs in a batch: state x2, sort, force records and pair lists
+    (32 words and a count per particle), and with pairs = "csr" the CSR list at ~30
+    pairs/particle."""
     n = len(scene["pos"])
     nb = len(scene.get("wall_pos", ()))
     csr = 8 + 30 * 4 * 1.3 if pairs == "csr" else 0
-    return int(n * (2 * 36 + 32 + 56 + csr) + nb * 60 + 4096)
+    return int(n * (2 * 36 + 32 + 132 + csr) + nb * 60 + 4096)
 
 
 # ----------------------------------------------------------------------------- continuous batching
