@@ -381,8 +381,8 @@ def pass1_alg_bytes(batch):
     """Algorithmic HBM bytes of one k_batch_pass1 launch over renormalized scenes.
     Per particle: its two 16-byte neighbor records (read once; the other 27-odd reads of
     them are L1/L2 hits), relative density 4, key 4, scene index 4 read, dpdt 4 + acc 8 +
-    <grad rho> V 8 written.  Pairs from the cell rows: the pair count 4 and the list's words
-    read, 4 bytes per two pairs (68 per particle + 2 per pair).  CSR pairs: offsets 4 (64)
+    <grad rho> V 8 written.  Pairs from the cell rows: the segment count 4 and 8 per stored
+    segment (start, mask) read (68 per particle + 8 per segment).  CSR pairs: offsets 4 (64)
     and 4 per column.  Per wall: position 8 + volume, density, pressure 12."""
     import ctypes
     import torch
@@ -391,11 +391,12 @@ def pass1_alg_bytes(batch):
         P = int(batch.offsets[batch.n].item())
         return batch.n * 64 + 4 * P + batch.nb * 20
     n = batch.n
-    wo, co, mp = ctypes.c_size_t(), ctypes.c_size_t(), ctypes.c_int32()
-    N.call("sph_deltasph_pair_lists", n, ctypes.byref(wo), ctypes.byref(co), ctypes.byref(mp))
-    counts = batch.forces_scratch.view(torch.int32)[co.value // 4:co.value // 4 + n]
-    words = int(((torch.clamp(counts, min=0) + 1) // 2).sum().item())
-    return n * 68 + 4 * words + batch.nb * 20
+    mo, so, co, ms = ctypes.c_size_t(), ctypes.c_size_t(), ctypes.c_size_t(), ctypes.c_int32()
+    N.call("sph_deltasph_segment_lists", n, ctypes.byref(mo), ctypes.byref(so), ctypes.byref(co), ctypes.byref(ms))
+    # the scratch tensor is 256-byte aligned, so its first 16-byte boundary is its start
+    nseg = batch.forces_scratch.view(torch.int32)[co.value // 4:co.value // 4 + n]
+    segments = int(torch.clamp(nseg, min=0).sum().item())
+    return n * 68 + 8 * segments + batch.nb * 20
 
 
 def phase_times(batch, reps=5):

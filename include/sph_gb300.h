@@ -312,14 +312,15 @@ sph_status_t sph_mdbc_wall_density(const sph_fluid_view* fluid, const sph_wall_v
  * artificial viscosity (diffusion.py:12-25) + laminar viscosity (laminar.py:12-27), each
  * with its wall part (solidBoundary.py:746-890).  Wall quantities must come from
  * sph_mdbc_wall_density.  scratch: sph_deltasph_scratch_bytes(n) bytes of device memory
- * (per-particle neighbor records, and the pair lists of sph_batch_deltasph_step). */
+ * (per-particle neighbor records, and the segment lists of sph_batch_deltasph_step). */
 size_t sph_deltasph_scratch_bytes(int64_t n);
-/* Where sph_batch_deltasph_step keeps its pair lists in a 256-byte-aligned scratch of n
- * particles: byte offsets of the offset words (max_pairs / 2 uint32 per particle, word m of
- * particle i at index m * n + i, low half the earlier pair, each half the int16 j - i) and
- * of the int32 pair counts (-1: the particle's list did not fit).  For callers that count
- * pairs (bytes moved per step) without a host copy of the search. */
-sph_status_t sph_deltasph_pair_lists(int64_t n, size_t* words_offset, size_t* counts_offset, int32_t* max_pairs);
+/* Where sph_batch_deltasph_step keeps its segment lists in a scratch of n particles (byte
+ * offsets from the scratch's first 16-byte boundary): the uint32 accepted-candidate masks
+ * and the int32 segment starts (segment k of particle i at index k * n + i, k <
+ * max_segments) and the int32 segment counts (-1: the particle's segments did not fit).
+ * For callers that count the bytes a step moves without a host copy of the search. */
+sph_status_t sph_deltasph_segment_lists(int64_t n, size_t* masks_offset, size_t* starts_offset,
+                                        size_t* counts_offset, int32_t* max_segments);
 sph_status_t sph_deltasph_forces(const sph_fluid_view* fluid, const sph_wall_view* walls, const sph_grid* grid,
                                  const sph_params* params, float* dpdt, float* acc, float* L, float* grad_rho,
                                  void* scratch, size_t scratch_bytes, void* stream);
@@ -382,13 +383,13 @@ sph_status_t sph_batch_nl_fill(const float* xy, const float* sorted_support, int
  * of the deltaSPH diffusion that needs the neighbors); scratch as for sph_deltasph_forces.
  * With fluid->offsets and fluid->cols both NULL no neighbor list is needed: the records
  * launch also tests each particle's cell rows in segments of 32 candidates and stores its
- * pairs as 16-bit offsets j - i (at most 64, else the force passes test its rows
- * themselves; sph_deltasph_pair_lists), and both force passes visit those pairs in the CSR
- * fill's order (same sums).  Each scene's pair test then uses its own support (sph_params.support),
+ * non-empty segments (start, 32-bit accepted-candidate mask; at most 8, else the force
+ * passes test its rows themselves; sph_deltasph_segment_lists), and both force passes visit
+ * those pairs in the CSR fill's order (same sums).  Each scene's pair test then uses its own support (sph_params.support),
  * which must be every particle's support.
  * The force passes (pass1, diffusion) run over `groups` (a host array of ngroups entries
  * that tile [0, n) in order; a group holds whole scenes when its bounds are scene bounds):
- * `tpp` lanes per particle (each lane takes every 2nd or 4th pair; the lanes' sums are
+ * `tpp` lanes per particle (each lane takes every 2nd or 4th segment; the lanes' sums are
  * added by warp shuffles, so the summation order, not the pair set, depends on it) and,
  * when all its scenes share one, the diffusion `scheme`, which selects a kernel compiled for
  * it.  ngroups = 0: one group, one lane, any schemes.

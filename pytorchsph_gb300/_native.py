@@ -107,7 +107,7 @@ SIGNATURES.update({  # differentiable rollouts
 SIGNATURES.update({  # simulation kernels
     "sph_mdbc_wall_density": (_I32, [_P] * 5),
     "sph_deltasph_scratch_bytes": (_SZ, [_I64]),
-    "sph_deltasph_pair_lists": (_I32, [_I64, _P, _P, _P]),
+    "sph_deltasph_segment_lists": (_I32, [_I64, _P, _P, _P, _P]),
     "sph_deltasph_forces": (_I32, [_P] * 8 + [_P, _SZ, _P]),
     "sph_integrate_semi_implicit_euler": (_I32, [_I64] + [_P] * 6 +
                                           [_F32, _I32] + [_P] * 5),

@@ -1,6 +1,6 @@
 // deltaSPH right-hand side on sm_103a: one thread (or 2 / 4 lanes) per fluid particle in
-// cell-sorted order, gathering over its pairs (a CSR row, or its list of 16-bit pair offsets
-// built from the cell rows) and over the wall particles of the neighboring cells.
+// cell-sorted order, gathering over its pairs (a CSR row, or its segment list of accepted
+// candidates from the cell rows) and over the wall particles of the neighboring cells.
 // Every sum is a gather into registers — no atomics, deterministic order: fluid neighbors in
 // cell order, then walls, added to the fluid sum the way the reference adds its wall
 // module's result (`x += simulation.boundaryModule...`).
@@ -142,22 +142,11 @@ __device__ __forceinline__ PairG pair_g(float xi, float yi, float xj, float yj, 
 // same.  Visiting set bits keeps a warp's lanes together the way a CSR row does (a lane
 // runs the pair body only for its own neighbors).
 //
-// The records pass stores each particle's pairs as a list of 16-bit offsets j - i, in
-// increasing j (the CSR fill's order, so every sum is the same): kMaxPairs at most, two to a
-// 32-bit word, word m of particle i at words[m * n + i] (slot-major: a warp's loads of one
-// word index are coalesced), and the count npair[i] (-1 when the list did not fit: more
-// than kMaxPairs pairs, or an offset beyond 16 bits; the force passes then test its cell
-// rows themselves).  A force pass walks a list with one counter: per pair a shift, a sign
-// extension and an add, where walking stored bit masks took a find-first-set, a mask update
-// and, at every segment's end, a divergent branch to the next segment.
-constexpr int kMaxPairs = 64;
-constexpr int kPairWords = kMaxPairs / 2;
-
-struct PairLists {
-  const int32_t* npair;
-  const uint32_t* words;
-};
-
+// The records pass stores each particle's non-empty segments in order, at most
+// kMaxSegments: start seg_start[k * n + i] and mask seg_mask[k * n + i] for k < nseg[i]
+// (nseg[i] = -1 when there are more; the force passes then test its cell rows
+// themselves).  A force pass holds one segment and the next one, loaded ahead, so moving
+// on to the next segment costs a lane a register move.
 // Every row of the window, tested here (any r); with kTpp lanes per particle, lane `sub`
 // takes rows y0 + sub, y0 + sub + kTpp, ...
 // kPaired: the candidate tests two at a time (segment_mask) or one at a time; the sums are
@@ -183,17 +172,15 @@ __device__ __forceinline__ void cell_pairs(const FluidView& F, const sph_grid& g
   }
 }
 
-// The pair list of particle i: its cell rows tested in segments of 32 candidates, the accepted
-// candidates stored as offsets.
-__device__ __forceinline__ void pairs_body(int i, const FluidView& F, const sph_grid& g, int coff, int r, float thr,
-                                           int32_t* __restrict__ npair, uint32_t* __restrict__ words) {
+// The segment list of particle i.
+__device__ __forceinline__ void segments_body(int i, const FluidView& F, const sph_grid& g, int coff, int r,
+                                              float thr, int32_t* __restrict__ nseg, int32_t* __restrict__ seg_start,
+                                              uint32_t* __restrict__ seg_mask) {
   int cx, cy;
   cell_of(F.keys[i] - (uint32_t)coff, g, &cx, &cy);
   const float2 xi = F.x[i];
   const size_t n = (size_t)F.n;
   int k = 0;
-  bool fits = true;
-  uint32_t low = 0;
   const int x0 = max(cx - r, 0), x1 = min(cx + r, g.cells_x - 1);
   const int y0 = max(cy - r, 0), y1 = min(cy + r, g.cells_y - 1);
   const int32_t* cs = F.cell_start + coff;
@@ -202,63 +189,59 @@ __device__ __forceinline__ void pairs_body(int i, const FluidView& F, const sph_
       const int row = yy * g.cells_x;
       const int b = __ldg(cs + row + x0), e = __ldg(cs + row + x1 + 1);
       for (int c = b; c < e; c += 32) {
-        uint32_t w = segment_mask(F.x, c, e, xi.x, xi.y, thr);
-        while (w) {
-          const int d = c - 1 + __ffs(w) - i;
-          w &= w - 1;
-          fits = fits && d >= -32768 && d <= 32767;
-          if (k < kMaxPairs) {
-            const uint32_t h = (uint32_t)d & 0xffffu;
-            if (k & 1)
-              words[(size_t)(k >> 1) * n + i] = low | (h << 16);
-            else
-              low = h;
-          }
-          ++k;
+        const uint32_t w = segment_mask(F.x, c, e, xi.x, xi.y, thr);
+        if (w == 0) continue;
+        if (k < kMaxSegments) {
+          seg_start[k * n + i] = c;
+          seg_mask[k * n + i] = w;
         }
+        ++k;
       }
     }
   }
-  if ((k & 1) && k <= kMaxPairs) words[(size_t)(k >> 1) * n + i] = low;
-  npair[i] = fits && k <= kMaxPairs ? k : -1;
+  nseg[i] = k <= kMaxSegments ? k : -1;
 }
 
-// The pairs of particle i from its pair list (its cell rows when the list did not fit).  One
-// lane: each word is loaded two pairs ahead of its use.  kTpp lanes: lane `sub` takes pairs
-// sub, sub + kTpp, ...  Every index is clamped to [0, n) (the lists are written in the same
-// step from the same sorted arrays, so the clamp never changes one).
+// The pairs of particle i from its segment list (its cell rows when the list overflowed).
+// With kTpp lanes per particle, lane `sub` takes segments sub, sub + kTpp, ... (rows, on the
+// overflow path); each lane holds its current segment and its next one, loaded ahead.
 template <int kTpp = 1, bool kPaired = false, typename Fn>
 __device__ __forceinline__ void stored_pairs(int i, const FluidView& F, const sph_grid& g, int coff, int r,
-                                             const PairLists& L, float xi, float yi, float thr, Fn&& fn,
-                                             int sub = 0) {
-  const int np = L.npair[i];
-  if (np < 0 || np > kMaxPairs) {
+                                             const int32_t* __restrict__ nseg, const int32_t* __restrict__ seg_start,
+                                             const uint32_t* __restrict__ seg_mask, float xi, float yi, float thr,
+                                             Fn&& fn, int sub = 0) {
+  const int ns = nseg[i];
+  if (ns < 0 || ns > kMaxSegments) {
     int cx, cy;
     cell_of(F.keys[i] - (uint32_t)coff, g, &cx, &cy);
     cell_pairs<kTpp, kPaired>(F, g, r, coff, cx, cy, xi, yi, thr, fn, sub);
     return;
   }
+  if (ns <= sub) return;
   const size_t n = (size_t)F.n;
-  const unsigned last = (unsigned)F.n - 1u;
-  const uint32_t* __restrict__ w = L.words + i;
-  if constexpr (kTpp == 1) {
-    uint32_t cur = 0, next = np > 0 ? __ldg(w) : 0u;
-    for (int k = 0; k < np; ++k) {
-      if ((k & 1) == 0) {
-        cur = next;
-        if (k + 2 < np) next = __ldg(w + (size_t)((k >> 1) + 1) * n);
-      } else {
-        cur >>= 16;
+  int k = sub;
+  int b = seg_start[k * n + i];
+  uint32_t w = clip_segment(seg_mask[k * n + i], b, F.n);
+  int bn = 0;
+  uint32_t wn = 0;
+  if (k + kTpp < ns) {
+    bn = seg_start[(k + kTpp) * n + i];
+    wn = seg_mask[(k + kTpp) * n + i];
+  }
+  for (;;) {
+    while (w == 0) {
+      k += kTpp;
+      if (k >= ns) return;
+      b = bn;
+      w = clip_segment(wn, bn, F.n);
+      if (k + kTpp < ns) {
+        bn = seg_start[(k + kTpp) * n + i];
+        wn = seg_mask[(k + kTpp) * n + i];
       }
-      const int j = i + (int)(int16_t)(cur & 0xffffu);
-      fn((int)min((unsigned)j, last));
     }
-  } else {
-    for (int k = sub; k < np; k += kTpp) {
-      const uint32_t v = __ldg(w + (size_t)(k >> 1) * n);
-      const int j = i + (int)(int16_t)((k & 1) ? v >> 16 : v & 0xffffu);
-      fn((int)min((unsigned)j, last));
-    }
+    const int j = b - 1 + __ffs(w);
+    w &= w - 1;
+    fn(j);
   }
 }
 
@@ -288,6 +271,13 @@ struct Pass1 {
   float ddiff;     // deltaSPH: the pass-1 part of D_i
 };
 
+// Pairs from the segment lists S (kCells) instead of the CSR row.
+struct Segments {
+  const int32_t* nseg;
+  const int32_t* start;
+  const uint32_t* mask;
+};
+
 // kTpp lanes per particle (kCells only): lane `sub` sums its share of the pairs, the lanes
 // add their sums, and lane 0 finishes (walls, gravity, L^+); the other lanes return a zero
 // record.  `live` false: a lane past the last particle, which only takes part in the sums.
@@ -296,7 +286,7 @@ struct Pass1 {
 template <bool kCells, int kTpp = 1, int kScheme = -1>
 __device__ __forceinline__ Pass1 pass1_body(int i, const FluidView& F, const float4* __restrict__ xv,
                                             const float4* __restrict__ qv, const WallView& W, const sph_grid& g,
-                                            const SphParams& P, int coff, const PairLists& S, int sub = 0,
+                                            const SphParams& P, int coff, const Segments& S, int sub = 0,
                                             bool live = true) {
   const float4 si = xv[i];
   const float rhoi = qv[i].x, pi = tait(F.rho[i], P);
@@ -343,7 +333,8 @@ __device__ __forceinline__ Pass1 pass1_body(int i, const FluidView& F, const flo
     }
   };
   if constexpr (kCells) {
-    if (live) stored_pairs<kTpp>(i, F, g, coff, P.search_radius, S, si.x, si.y, P.thr, fluid_pair, sub);
+    if (live) stored_pairs<kTpp>(i, F, g, coff, P.search_radius, S.nseg, S.start, S.mask, si.x, si.y, P.thr,
+                                 fluid_pair, sub);
   } else {
     static_assert(kTpp == 1, "CSR rows run one lane per particle");
     const int k0 = F.offsets[i], k1 = row_end(F, i, k0);
@@ -452,7 +443,7 @@ __device__ __forceinline__ Pass1 pass1_body(int i, const FluidView& F, const flo
 template <bool kCells, int kTpp = 1, bool kHoldsGV = true>
 __device__ __forceinline__ float diffusion_sum(int i, const FluidView& F, const float4* __restrict__ qv,
                                                const SphParams& P, const float2* __restrict__ gbuf,
-                                               const sph_grid& g, int coff, const PairLists& S, int sub = 0,
+                                               const sph_grid& g, int coff, const Segments& S, int sub = 0,
                                                bool live = true) {
   const float2 xi = F.x[i];
   float acc = 0.f;
@@ -467,7 +458,8 @@ __device__ __forceinline__ float diffusion_sum(int i, const FluidView& F, const 
     acc += (gv.x * e.dx + gv.y * e.dy) * e.gd;
   };
   if constexpr (kCells) {
-    if (live) stored_pairs<kTpp, true>(i, F, g, coff, P.search_radius, S, xi.x, xi.y, P.thr, pair, sub);
+    if (live) stored_pairs<kTpp, true>(i, F, g, coff, P.search_radius, S.nseg, S.start, S.mask, xi.x, xi.y, P.thr,
+                                       pair, sub);
   } else {
     static_assert(kTpp == 1, "CSR rows run one lane per particle");
     const int k0 = F.offsets[i], k1 = row_end(F, i, k0);
@@ -512,7 +504,7 @@ __global__ void __launch_bounds__(128) k_dsph_pass1(FluidView F, const float4* _
                                                     float4* __restrict__ Lout, float2* __restrict__ grad_rho) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= F.n) return;
-  const Pass1 o = pass1_body<false>(i, F, xv, qv, W, *gp, P, 0, PairLists{});
+  const Pass1 o = pass1_body<false>(i, F, xv, qv, W, *gp, P, 0, Segments{});
   dpdt[i] = P.diffusion == 2 ? o.dpdt + P.diff_k * o.ddiff : o.dpdt;
   acc[i] = make_float2(o.ax, o.ay);
   if (Lout) Lout[i] = o.L;
@@ -523,7 +515,7 @@ __global__ void __launch_bounds__(128) k_dsph_diffusion(FluidView F, const float
                                                         const float2* __restrict__ grad_rho, float* __restrict__ dpdt) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= F.n) return;
-  dpdt[i] -= P.diff_k * diffusion_sum<false, 1, false>(i, F, qv, P, grad_rho, sph_grid{}, 0, PairLists{});
+  dpdt[i] -= P.diff_k * diffusion_sum<false, 1, false>(i, F, qv, P, grad_rho, sph_grid{}, 0, Segments{});
 }
 
 __global__ void k_sie(int n, const float2* __restrict__ x, const float2* __restrict__ v,
@@ -545,16 +537,16 @@ __global__ void __launch_bounds__(128, 8) k_batch_mdbc(FluidView F, WallView W, 
   mdbc_body(b, F, W, S.g, S.P, S.coff);
 }
 
-// Neighbor records and, with pairs from the cell rows (npair != NULL), the pair lists.
+// Neighbor records and, with pairs from the cell rows (nseg != NULL), the segment lists.
 __global__ void __launch_bounds__(256) k_batch_prep(FluidView F, const SceneDev* __restrict__ scenes,
                                                     const int32_t* __restrict__ sid, float4* __restrict__ xv,
-                                                    float4* __restrict__ qv, int32_t* __restrict__ npair,
-                                                    uint32_t* __restrict__ words) {
+                                                    float4* __restrict__ qv, int32_t* __restrict__ nseg,
+                                                    int32_t* __restrict__ seg_start, uint32_t* __restrict__ seg_mask) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= F.n || sid[i] < 0) return;   // particle of no scene: never anyone's neighbor
   const SceneDev& S = scenes[sid[i]];
   prep_body(i, F, S.P, xv, qv);
-  if (npair) pairs_body(i, F, S.g, S.coff, S.P.search_radius, S.P.thr, npair, words);
+  if (nseg) segments_body(i, F, S.g, S.coff, S.P.search_radius, S.P.thr, nseg, seg_start, seg_mask);
 }
 
 // The update of one particle of a batch with its scene's dt.  If the neighbor list
@@ -583,7 +575,7 @@ __global__ void __launch_bounds__(128, 8) k_batch_pass1(FluidView F, const float
                                                      const SceneDev* __restrict__ scenes,
                                                      const int32_t* __restrict__ sid, float* __restrict__ dpdt,
                                                      float2* __restrict__ acc, float2* __restrict__ grad_rho,
-                                                     const PairLists seg, float2* __restrict__ xo,
+                                                     const Segments seg, float2* __restrict__ xo,
                                                      float2* __restrict__ vo, float* __restrict__ ro,
                                                      int32_t* status, int p_lo, int p_hi) {
   int i, sub = 0;
@@ -617,7 +609,7 @@ template <bool kCells, int kTpp>
 __global__ void __launch_bounds__(128) k_batch_diffusion(FluidView F, const float4* __restrict__ qv,
                                                          const SceneDev* __restrict__ scenes,
                                                          const int32_t* __restrict__ sid,
-                                                         const float2* __restrict__ grad_rho, const PairLists seg,
+                                                         const float2* __restrict__ grad_rho, const Segments seg,
                                                          const float* __restrict__ dpdt,
                                                          const float2* __restrict__ acc, float2* __restrict__ xo,
                                                          float2* __restrict__ vo, float* __restrict__ ro,
@@ -719,36 +711,40 @@ sph_status_t sph_mdbc_wall_density(const sph_fluid_view* fluid, const sph_wall_v
   return SPH_OK;
 }
 
-// Neighbor records (two float4 per particle), then, for pairs from the cell rows, the pair
-// lists: kPairWords words of two offsets and a count per particle.
-constexpr size_t kRecordBytes = 2 * sizeof(float4), kListBytes = kPairWords * sizeof(uint32_t) + sizeof(int32_t);
-size_t sph_deltasph_scratch_bytes(int64_t n) { return (size_t)(n > 0 ? n : 0) * (kRecordBytes + kListBytes) + 256; }
+// Neighbor records (two float4 per particle), then, for pairs from the cell rows, the
+// segment lists: kMaxSegments masks and starts and a count per particle.
+constexpr size_t kRecordBytes = 2 * sizeof(float4),
+                 kMaskBytes = kMaxSegments * (sizeof(uint32_t) + sizeof(int32_t)) + sizeof(int32_t);
+size_t sph_deltasph_scratch_bytes(int64_t n) { return (size_t)(n > 0 ? n : 0) * (kRecordBytes + kMaskBytes) + 256; }
 
-sph_status_t sph_deltasph_pair_lists(int64_t n, size_t* words_offset, size_t* counts_offset, int32_t* max_pairs) {
-  SPH_REQUIRE(n >= 0 && words_offset && counts_offset && max_pairs, "deltasph_pair_lists: bad arguments");
-  *words_offset = (size_t)n * kRecordBytes;
-  *counts_offset = (size_t)n * (kRecordBytes + kPairWords * sizeof(uint32_t));
-  *max_pairs = kMaxPairs;
+sph_status_t sph_deltasph_segment_lists(int64_t n, size_t* masks_offset, size_t* starts_offset,
+                                        size_t* counts_offset, int32_t* max_segments) {
+  SPH_REQUIRE(n >= 0 && masks_offset && starts_offset && counts_offset && max_segments,
+              "deltasph_segment_lists: bad arguments");
+  *masks_offset = (size_t)n * kRecordBytes;
+  *starts_offset = *masks_offset + (size_t)n * kMaxSegments * sizeof(uint32_t);
+  *counts_offset = *starts_offset + (size_t)n * kMaxSegments * sizeof(int32_t);
+  *max_segments = kMaxSegments;
   return SPH_OK;
 }
 
 }  // extern "C"
 
 // The neighbor records (xv, q) in caller scratch, 16-byte aligned.
-// The pair lists follow at the offsets sph_deltasph_pair_lists reports (scratch 256-byte
-// aligned, as torch and cudaMalloc give it).
 static bool records_from_scratch(void* scratch, size_t bytes, int64_t n, float4** xv, float4** qv,
-                                 PairLists* lists = nullptr) {
+                                 Segments* seg = nullptr) {
   if (!scratch) return false;
   const uintptr_t base = reinterpret_cast<uintptr_t>(scratch);
   const uintptr_t p = (base + 15) & ~(uintptr_t)15;
-  if ((p - base) + (size_t)n * (kRecordBytes + (lists ? kListBytes : 0)) > bytes) return false;
+  if ((p - base) + (size_t)n * (kRecordBytes + (seg ? kMaskBytes : 0)) > bytes) return false;
   *xv = reinterpret_cast<float4*>(p);
   *qv = *xv + n;
-  if (lists) {
-    const uint32_t* w = reinterpret_cast<const uint32_t*>(*qv + n);
-    lists->words = w;
-    lists->npair = reinterpret_cast<const int32_t*>(w + (size_t)kPairWords * n);
+  if (seg) {
+    uint32_t* m = reinterpret_cast<uint32_t*>(*qv + n);
+    int32_t* st = reinterpret_cast<int32_t*>(m + kMaxSegments * n);
+    seg->mask = m;
+    seg->start = st;
+    seg->nseg = st + kMaxSegments * n;
   }
   return true;
 }
@@ -828,7 +824,7 @@ sph_status_t sph_batch_deltasph_step(const sph_fluid_view* fluid, const sph_wall
   }
   if (n == 0) return SPH_OK;
   float4 *xv, *qv;
-  PairLists seg{};
+  Segments seg{};
   SPH_REQUIRE(records_from_scratch(scratch, scratch_bytes, n, &xv, &qv, cells ? &seg : nullptr),
               "batch_deltasph_step: scratch smaller than sph_deltasph_scratch_bytes(n)");
   cudaStream_t st = as_stream(stream);
@@ -837,8 +833,8 @@ sph_status_t sph_batch_deltasph_step(const sph_fluid_view* fluid, const sph_wall
   const SceneDev* S = static_cast<const SceneDev*>(scenes);
   if (W.n > 0 && (phases & SPH_PHASE_WALLS)) k_batch_mdbc<<<grid_for(W.n, 128), 128, 0, st>>>(F, W, S, wall_sid);
   if (phases & SPH_PHASE_RECORDS)
-    k_batch_prep<<<grid_for(n, 256), 256, 0, st>>>(F, S, sid, xv, qv, const_cast<int32_t*>(seg.npair),
-                                                   const_cast<uint32_t*>(seg.words));
+    k_batch_prep<<<grid_for(n, 256), 256, 0, st>>>(F, S, sid, xv, qv, const_cast<int32_t*>(seg.nseg),
+                                                   const_cast<int32_t*>(seg.start), const_cast<uint32_t*>(seg.mask));
   float2* xo = reinterpret_cast<float2*>(x_out);
   float2* vo = reinterpret_cast<float2*>(v_out);
   float2* gr = reinterpret_cast<float2*>(grad_rho);
@@ -848,7 +844,7 @@ sph_status_t sph_batch_deltasph_step(const sph_fluid_view* fluid, const sph_wall
   auto pass1 = [&](int lo, int hi, int t, int scheme) {
     const int nb = grid_for((int64_t)(hi - lo) * t, 128);
 #define SPH_PASS1(C, T, K)                                                                                  \
-  k_batch_pass1<C, T, K><<<nb, 128, 0, st>>>(F, xv, qv, W, S, sid, dpdt, ac, gr, C ? seg : PairLists{}, xo, vo, \
+  k_batch_pass1<C, T, K><<<nb, 128, 0, st>>>(F, xv, qv, W, S, sid, dpdt, ac, gr, C ? seg : Segments{}, xo, vo, \
                                              rho_out, status, lo, hi)
     if (!cells) {
       SPH_PASS1(false, 1, -1);
@@ -877,7 +873,7 @@ sph_status_t sph_batch_deltasph_step(const sph_fluid_view* fluid, const sph_wall
     if (hi <= lo || G[k].scheme == 0 || G[k].scheme == 1) continue;   // no deltaSPH scene in the group
     const int nb = grid_for((int64_t)(hi - lo) * t, 128);
     if (!cells)
-      k_batch_diffusion<false, 1><<<nb, 128, 0, st>>>(F, qv, S, sid, gr, PairLists{}, dpdt, ac, xo, vo, rho_out,
+      k_batch_diffusion<false, 1><<<nb, 128, 0, st>>>(F, qv, S, sid, gr, Segments{}, dpdt, ac, xo, vo, rho_out,
                                                       status, lo, hi);
     else if (t == 1)
       k_batch_diffusion<true, 1><<<nb, 128, 0, st>>>(F, qv, S, sid, gr, seg, dpdt, ac, xo, vo, rho_out, status, lo,

@@ -3,7 +3,7 @@
 `SceneBatch` holds any number of independent scenes in one concatenated particle array
 (per-particle scene index, per-scene grid / parameters / dt in a device scene table,
 (scene, cell) sort keys) and advances all of them with one fixed sequence of kernels:
-keys -> counting sort -> permute -> mDBC beside neighbor records + pair lists -> pass 1
+keys -> counting sort -> permute -> mDBC beside neighbor records + segment lists -> pass 1
 -> diffusion + update (with pairs = "csr": a CSR count / scan / fill after the permute).
 Buffers are static, so one batch step can be captured once in a CUDA graph and replayed.
 Scenes never interact: each scene's particles sort into their own cell range and every
@@ -165,8 +165,8 @@ class SceneBatch:
     """A fixed set of scenes stepped together (deltaSPH, semi-implicit Euler).
 
     pairs = "cells": the force passes take each particle's pairs straight from its cell rows
-    (no neighbor list; the records launch tests the cell rows and keeps each particle's
-    accepted candidates as 16-bit index offsets for both force passes).  pairs =
+    (no neighbor list; the records launch keeps each particle's accepted candidates as
+    segment bit masks for both force passes).  pairs =
     "csr": a CSR neighbor list is counted and filled every step first.  Both visit the
     pairs in the same order and give the same sums.
 
@@ -784,13 +784,12 @@ class SceneArena(SceneBatch):
 
 
 def estimate_bytes(scene, pairs: str = "cells") -> int:
-    """Device bytes one scene needs in a batch: state x2, sort, force records and pair lists
-    (32 words and a count per particle), and with pairs = "csr" the CSR list at ~30
-    pairs/particle."""
+    """Device bytes one scene needs in a batch: state x2, sort, force records and segment lists,
+    and with pairs = "csr" the CSR list at ~30 pairs/particle."""
     n = len(scene["pos"])
     nb = len(scene.get("wall_pos", ()))
     csr = 8 + 30 * 4 * 1.3 if pairs == "csr" else 0
-    return int(n * (2 * 36 + 32 + 132 + csr) + nb * 60 + 4096)
+    return int(n * (2 * 36 + 32 + 68 + csr) + nb * 60 + 4096)
 
 
 # ----------------------------------------------------------------------------- continuous batching
@@ -938,19 +937,28 @@ class Server:
         schemes = {DIFFUSION[sp.cfg.density_diffusion] for sp in specs}
         return schemes.pop() if len(schemes) == 1 else -1
 
-    def _grow(self, need_specs):
+    def _grow(self, need_specs, queue=()):
         """A larger arena holding the live scenes (their states carried over) and room for
-        `need_specs`; the one place the batch is rebuilt and its graph captured again."""
+        `need_specs`; the one place the batch is rebuilt and its graph captured again.  It is
+        sized at 1.5x the need for the arrivals still to come, but no larger than what the
+        requests still queued could add: every slot costs sort work each step, used or not."""
         t = time.perf_counter()
         live_specs = [r.spec for r in self.live]
         allsp = live_specs + list(need_specs)
         n = sum(len(sp.scene["pos"]) for sp in allsp)
         nb = sum(len(sp.scene.get("wall_pos", ())) for sp in allsp)
         cells = sum(sp.dev["grid"].num_cells + 1 for sp in allsp)
+        # a queued scene's cells are unknown before its upload: bounded by its particles over
+        # the fewest particles per cell among the scenes at hand, plus its outside slot
+        ppc = min(len(sp.scene["pos"]) / max(sp.dev["grid"].num_cells, 1) for sp in allsp)
+        more = {"n": sum(len(r.spec.scene["pos"]) for r in queue),
+                "nb": sum(len(r.spec.scene.get("wall_pos", ())) for r in queue),
+                "c": sum(int(len(r.spec.scene["pos"]) / max(ppc, 1e-3)) + 1 for r in queue)}
         old = self.arena
-        grow = lambda need, cur, lo: max(lo, int(need * 1.5), cur)
-        new = SceneArena(self.device, particles=grow(n, old.N if old else 0, 1 << 16),
-                         walls=grow(nb, old.WC if old else 0, 1 << 12), cells=grow(cells, old.C if old else 0, 1 << 16),
+        grow = lambda need, cur, lo, key: max(lo, min(int(need * 1.5), need + more[key]), cur)
+        new = SceneArena(self.device, particles=grow(n, old.N if old else 0, 1 << 16, "n"),
+                         walls=grow(nb, old.WC if old else 0, 1 << 12, "nb"),
+                         cells=grow(cells, old.C if old else 0, 1 << 16, "c"),
                          slots=max(256, 2 * len(allsp), old.S if old else 0), tpp=self._tpp,
                          scheme=self._scheme)
         for r in self.live:
@@ -984,7 +992,7 @@ class Server:
                     raise ArenaFull("no arena yet")
                 r.slot = self.arena.admit(r.spec)
             except ArenaFull:
-                self._grow([q.spec for q in arrived[k:]])
+                self._grow([q.spec for q in arrived[k:]], queue)
                 r.slot = self.arena.admit(r.spec)
             r.admitted = now
             self.live.append(r)

@@ -3,8 +3,8 @@
 Knobs:
   * serving batch (per scene, `SceneSpec.cell_ratio` / `SceneSpec.tpp`): the cell size as
     a fraction of the support (cells of h / cell_ratio searched cell_ratio cells out: fewer
-    candidates per particle, more cell rows), and the lanes per particle of the force
-    passes (1, 2 or 4: a particle's pairs dealt to the lanes, sums added by warp
+    candidates per particle, more segments), and the lanes per particle of the force
+    passes (1, 2 or 4: a particle's segments split over the lanes, sums added by warp
     shuffles).  A scene's configuration depends only on its particle count, so a scene's
     result is the same alone and in any mix of scenes.
   * one-scene neighbor search (`GridSearch`): counting sort, or LSD radix sort and its

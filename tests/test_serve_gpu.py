@@ -70,10 +70,11 @@ def test_cell_pairs_equal_csr_pairs(cuda):
     assert all(same(x, y) for x, y in zip(cells, csr))
 
 
-def test_pair_list_overflow_takes_the_cell_rows(cuda):
-    """Particles with more pairs than a pair list holds (a dam-break block compressed to 0.6
-    of its spacing: ~75 neighbors each) take their pairs from the cell rows in both force
-    passes: bitwise the states of the CSR list, with the drop beside it unaffected."""
+def test_segment_overflow_takes_the_cell_rows(cuda):
+    """Particles with more non-empty segments than a segment list holds (a dam-break block
+    compressed to 0.45 of its spacing: ~140 neighbors, over 8 segments of 32 candidates)
+    take their pairs from the cell rows in both force passes: bitwise the states of the CSR
+    list, with the drop beside it unaffected."""
     import ctypes
     import dataclasses
     from pytorchsph_gb300 import _native as N
@@ -81,21 +82,22 @@ def test_pair_list_overflow_takes_the_cell_rows(cuda):
     A = spec("dam_break", 3000, 1.0)
     sc = dict(A.scene)
     lo = sc["pos"].min(0)
-    sc["pos"] = (lo + (sc["pos"] - lo) * 0.6).astype(np.float32)
+    sc["pos"] = (lo + (sc["pos"] - lo) * 0.45).astype(np.float32)
     A = dataclasses.replace(A, scene=sc)
     B = spec("drop", 2500, 1.0)
     b = SceneBatch([A, B], cuda, pairs="cells")
-    for _ in range(4):
+    for _ in range(3):
         b.step()
     b.check()
-    wo, co, mp = ctypes.c_size_t(), ctypes.c_size_t(), ctypes.c_int32()
-    N.call("sph_deltasph_pair_lists", b.n, ctypes.byref(wo), ctypes.byref(co), ctypes.byref(mp))
+    mo, so, co, ms = ctypes.c_size_t(), ctypes.c_size_t(), ctypes.c_size_t(), ctypes.c_int32()
+    N.call("sph_deltasph_segment_lists", b.n, ctypes.byref(mo), ctypes.byref(so), ctypes.byref(co),
+           ctypes.byref(ms))
     counts = b.forces_scratch.view(torch.int32)[co.value // 4:co.value // 4 + b.n].cpu().numpy()
-    assert (counts == -1).sum() > 1000 and counts.max() <= mp.value
+    assert (counts == -1).sum() > 500 and counts.max() <= ms.value
     cells = [b.scene_state(s) for s in range(2)]
-    csr = run_batch([A, B], 4, cuda, pairs="csr")
+    csr = run_batch([A, B], 3, cuda, pairs="csr")
     assert all(same(x, y) for x, y in zip(cells, csr))
-    assert same(cells[1], run_batch([B], 4, cuda)[0])
+    assert same(cells[1], run_batch([B], 3, cuda)[0])
 
 
 def test_graph_replay_equals_eager(cuda):
