@@ -720,10 +720,18 @@ def run_search_density(args, dev, world, rank):
         if tuned:
             line["tuning"] = {str(b): {k: (round(x["ms"], 4) if isinstance(x, dict) else x)
                                        for k, x in e["measured"].items()} for b, e in tuned.items()}
+        # the whole step against the search + density byte budget of the workload: per
+        # particle 16 key generation, 60 sort (three 8-bit radix passes of 20), 28 reorder,
+        # 12 cell table, 8 count, 8 scan, 8 fill read, 4 offsets, 4 density (148), plus 4 per
+        # pair written as a CSR column and 4 read back by an unfused density pass
+        step_alg = n * 148 + 8 * P
+        step_gbs = step_alg / (ms / 1e3) / 1e9
         line["roofline"] = {"bound": "hbm", "kernel": kern, "achieved": achieved, "peak": peak, "unit": "GB/s",
                             "frac": achieved / peak if achieved else None,
                             "traffic": traffic_from_profiles(args.workload, kern, n), "algorithmic_bytes": alg,
-                            "peak_source": peak_src}
+                            "peak_source": peak_src,
+                            "step": {"algorithmic_bytes": step_alg, "achieved": step_gbs, "frac": step_gbs / peak,
+                                     "unit": "GB/s", "bytes": "148 per particle + 8 per pair"}}
         line["e2e"] = {"value": n * world / (statistics.mean(e2e_ms) / 1e3), "unit": "particles/s",
                        "h2d_bytes_per_step": 16 * n, "d2h_bytes_per_step": 4 * n + 4}
         line["gpu_launches"] = launches_per_step * args.steps

@@ -18,6 +18,7 @@ time-to-completion.
 """
 from __future__ import annotations
 
+import bisect
 import ctypes
 import time
 from dataclasses import dataclass, field
@@ -614,12 +615,19 @@ class SceneArena(SceneBatch):
         self.live_n = 0
         self.walls_n = 0
         self.specs = []
-        self._staging = []
+        self._rows_host = torch.zeros(self.S * self.rec, dtype=torch.uint8, pin_memory=True)
+        self._row_events = [None] * self.S
+        self._cell_top = 0            # end of the highest cell range handed out
         self._walls_dirty = False     # walls admitted or retired since the last wall sort
         self._sort_walls()
 
     # ------------------------------------------------------------------ bookkeeping
     def _alloc_cells(self, size):
+        # behind the highest range when it fits (no scan of the live ranges), else first fit
+        top = self._cell_top
+        if self.C - top >= size:
+            self._cell_top = top + size
+            return top
         used = sorted((d["coff"], d["ncells"]) for d in self.slots.values())
         at = 0
         for c, k in used:
@@ -630,7 +638,9 @@ class SceneArena(SceneBatch):
             return at
         if self.C - sum(k for _, k in used) >= size:   # pack the live scenes' ranges, then append
             self._pack_cells()
-            return sum(k for _, k in used)
+            at = sum(k for _, k in used)
+            self._cell_top = at + size
+            return at
         return None
 
     def _pack_cells(self):
@@ -640,6 +650,7 @@ class SceneArena(SceneBatch):
             d["coff"] = at
             self._write_scene(slot)
             at += d["ncells"]
+        self._cell_top = at
         self._walls_dirty = True
 
     def _write_scene(self, slot):
@@ -647,16 +658,19 @@ class SceneArena(SceneBatch):
         sp = d["spec"]
         h = float(np.float32(sp.scene["support"][0]))
         P = _params_for(sp.cfg, h, d["grid"].num_cells, sp.cell_ratio)
-        buf = ctypes.create_string_buffer(self.rec)
+        # through the slot's row of a pinned staging table, so the host does not wait for the
+        # queued steps; a row is rewritten only after the event behind its last copy
+        ev = self._row_events[slot]
+        if ev is not None:
+            ev.synchronize()
+        row = self._rows_host[slot * self.rec:(slot + 1) * self.rec]
+        buf = (ctypes.c_char * self.rec).from_address(row.data_ptr())
         N.check(self.lib.sph_scene_encode(ctypes.byref(P), ctypes.byref(d["grid"]), d["coff"], sp.cfg.dt, buf),
                 "scene_encode")
-        # through pinned memory, so the host does not wait for the queued steps; the staging row
-        # is kept until an event after the copy has passed
-        row = torch.frombuffer(bytearray(buf.raw), dtype=torch.uint8).pin_memory()
         self.scenes[slot * self.rec:(slot + 1) * self.rec].copy_(row, non_blocking=True)
         ev = torch.cuda.Event()
         ev.record()
-        self._staging = [(e, t) for e, t in self._staging if not e.query()] + [(ev, row)]
+        self._row_events[slot] = ev
 
     def _sort_walls(self):
         """Sort the staging walls by (scene, cell) into the arrays the batch kernels read; the
@@ -719,7 +733,7 @@ class SceneArena(SceneBatch):
             N.call("sph_arena_set_ids", N.ptr(self.ws_w["sid"]), N.ptr(self.ws_w["uid"]), w0, nb, slot, st)
             self.walls_n = w1
             self._walls_dirty = True
-        self.specs = [self.slots[k]["spec"] for k in sorted(self.slots)]
+        self._specs = None
         return slot
 
     def scene_state_device(self, slot, states=None):
@@ -752,10 +766,20 @@ class SceneArena(SceneBatch):
             self.walls_n -= d["nb"]
             self._walls_dirty = True
         self.live_n -= d["n"]
-        self.free_slots.append(slot)
-        self.free_slots.sort()
-        self.specs = [self.slots[k]["spec"] for k in sorted(self.slots)]
+        bisect.insort(self.free_slots, slot)
+        self._specs = None
         return out
+
+    @property
+    def specs(self):
+        """The live scenes' specs in slot order (built when asked for)."""
+        if self._specs is None:
+            self._specs = [self.slots[k]["spec"] for k in sorted(self.slots)]
+        return self._specs
+
+    @specs.setter
+    def specs(self, value):
+        self._specs = list(value)
 
     def _walls_ready(self):
         # one wall sort for all the admissions and retirements since the last step
@@ -795,6 +819,27 @@ def estimate_bytes(scene, pairs: str = "cells") -> int:
 # ----------------------------------------------------------------------------- continuous batching
 def _timing_event():
     return torch.cuda.Event(enable_timing=True)
+
+
+class _PinnedPool:
+    """Pinned host memory handed out as views of large chunks: one page-locking allocation per
+    chunk instead of one per array (page-locking costs far more than the copy it enables).  A
+    chunk stays allocated while any view of it is alive."""
+
+    def __init__(self, chunk_bytes: int = 1 << 26):
+        self.chunk = int(chunk_bytes)
+        self.cur = None
+        self.off = 0
+
+    def take(self, shape, dtype):
+        nbytes = int(np.prod(shape)) * torch.empty(0, dtype=dtype).element_size()
+        step = (nbytes + 255) & ~255
+        if self.cur is None or self.off + step > self.cur.numel():
+            self.cur = torch.empty(max(self.chunk, step), dtype=torch.uint8, pin_memory=True)
+            self.off = 0
+        v = self.cur[self.off:self.off + nbytes].view(dtype).view(tuple(shape))
+        self.off += step
+        return v
 
 
 @dataclass
@@ -1006,7 +1051,7 @@ class Server:
             r.error = error
             self.failed.append(r)
         elif self.keep_final:
-            host = {k: torch.empty(v.shape, dtype=v.dtype, pin_memory=True) for k, v in st.items()}
+            host = {k: self._pinned.take(v.shape, v.dtype) for k, v in st.items()}
             for k in st:
                 host[k].copy_(st[k], non_blocking=True)
             r.final = host                     # numpy after the run's last synchronisation
@@ -1017,6 +1062,7 @@ class Server:
         self._scheme = self._arena_kind([r.spec for r in queue])
         self._tpp = 1
         self.admit_seconds = 0.0
+        self._pinned = _PinnedPool()
         flags = torch.zeros(2, dtype=torch.int32, pin_memory=True)
         done = [None, None]          # event after each of the last two steps' status copies
         timed = []                   # (start event, end event, live scenes) per step
