@@ -629,13 +629,14 @@ def run_search_density(args, dev, world, rank):
 
     # grid (bounds, final), keys, sort, gather, count, scan, fill, dense rows, scatter; a scan
     # is one kernel (the zeroing of its tile words is a memset); counting sort: scan,
-    # scatter, in-cell fix of small and of large cells; radix: per digit histogram, scan,
-    # scatter, then the cell starts
+    # scatter, in-cell fix of small and of large cells, which also gather the positions,
+    # supports and areas; radix: per digit histogram, scan, scatter, then the cell starts
+    # and the gather
     if args.sort == "counting":
         sort_launches = 4
     else:
-        sort_launches = ((N.load().sph_key_bits(cells) + args.digit_bits - 1) // args.digit_bits) * 3 + 1
-    launches_per_step = 2 + 1 + sort_launches + 1 + 1 + 1 + 1 + 1 + 1
+        sort_launches = ((N.load().sph_key_bits(cells) + args.digit_bits - 1) // args.digit_bits) * 3 + 1 + 1
+    launches_per_step = 2 + 1 + sort_launches + 1 + 1 + 1 + 1 + 1
     s = torch.cuda.Stream(dev)
     s.wait_stream(torch.cuda.current_stream())
     with torch.cuda.stream(s):
@@ -797,6 +798,25 @@ def run_dambreak(args, dev, world, rank):
             transient.append(sim.last["density_iters"])
         transient = [int(t.item()) for t in transient]
         torch.cuda.synchronize()
+
+        def timed(k):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            for _ in range(k):
+                sim.step(sync=False)
+            b.record()
+            b.synchronize()
+            return a.elapsed_time(b) / k
+
+        eager_ms = timed(5)           # host-issued launches, for comparison
+        try:
+            sim.capture()             # the whole step as one CUDA graph
+            graph = "one CUDA graph per step (cooperative solves inside)"
+            for _ in range(3):
+                sim.step(sync=False)
+        except Exception as e:        # eager launches then
+            graph = f"eager launches (capture failed: {e})"
+        torch.cuda.synchronize()
         with ClockSampler(dev.index or 0) as clk:
             st, en = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             sync_ranks(world)
@@ -812,7 +832,8 @@ def run_dambreak(args, dev, world, rank):
                   "solver": "DFSPH, divergence + density solves, semi-implicit Euler, adaptive dt",
                   "density_iters_last": int(sim.last["density_iters"].item()),
                   "warmup_steps_density_iters": transient,
-                  "timed_steps": "after the start-up transient (the warm-up steps above)"}
+                  "timed_steps": "after the start-up transient (the warm-up steps above)",
+                  "graph": graph, "eager_ms_per_step": eager_ms}
         if rank == 0 and not args.no_cpu_baseline:
             # the full block takes minutes per CPU step: a 64 x 64 block of the same tank
             small = workloads.dam_break(64, 64, 0.016, (4.096, 2.048))

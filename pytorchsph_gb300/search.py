@@ -250,8 +250,14 @@ class GridSearch:
                    N.ptr(status), st)
             mark("keys")
             cs = ws.bytes("cs_scratch", lib.sph_counting_sort_scratch_bytes(n, cap))
-            N.call("sph_counting_sort", N.ptr(keys), n, cap, N.ptr(cell_count), N.ptr(cell_start), N.ptr(order),
-                   N.ptr(skeys), N.ptr(status), N.ptr(cs), cs.numel() * 8, st)
+            # positions, supports and areas move into the sorted order in the sort's own launches
+            xy = ws.get("xy", 2 * n, torch.float32).view(n, 2)
+            sh = ws.get("sorted_support", n, torch.float32)
+            sa = ws.get("sorted_area", n, torch.float32) if area is not None else None
+            rows = [(pos, xy), (support, sh)] + ([(area, sa)] if area is not None else [])
+            k, eb, ins, outs = N.array_set(rows)
+            N.call("sph_counting_sort_permute", N.ptr(keys), n, cap, N.ptr(cell_count), N.ptr(cell_start), None,
+                   N.ptr(order), N.ptr(skeys), k, eb, ins, outs, N.ptr(status), N.ptr(cs), cs.numel() * 8, st)
         else:
             N.call("sph_cell_keys", N.ptr(pos), n, N.ptr(grid), cap, N.ptr(skeys), N.ptr(order), None,
                    N.ptr(status), st)
@@ -261,11 +267,12 @@ class GridSearch:
                    N.ptr(rs), rs.numel() * 8, st)
             N.call("sph_cell_starts", N.ptr(skeys), n, cap, N.ptr(cell_start), st)
         mark("sort")
-        xy = ws.get("xy", 2 * n, torch.float32).view(n, 2)
-        sh = ws.get("sorted_support", n, torch.float32)
-        sa = ws.get("sorted_area", n, torch.float32) if area is not None else None
-        N.call("sph_gather_sorted", N.ptr(order), n, N.ptr(pos), N.ptr(support), N.ptr(area), N.ptr(xy), N.ptr(sh),
-               N.ptr(sa), st)
+        if self.sort != "counting":
+            xy = ws.get("xy", 2 * n, torch.float32).view(n, 2)
+            sh = ws.get("sorted_support", n, torch.float32)
+            sa = ws.get("sorted_area", n, torch.float32) if area is not None else None
+            N.call("sph_gather_sorted", N.ptr(order), n, N.ptr(pos), N.ptr(support), N.ptr(area), N.ptr(xy),
+                   N.ptr(sh), N.ptr(sa), st)
         mark("gather")
         counts = ws.get("counts", n)
         rho = ws.get("rho", n, torch.float32) if density else None

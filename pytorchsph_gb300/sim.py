@@ -142,6 +142,7 @@ class Simulation:
         self.cols = None
         self.extra = {}
         self.last = {}
+        self.graph = None
 
     # ------------------------------------------------------------------ set-up
     def _grid_capacity(self):
@@ -334,8 +335,40 @@ class Simulation:
         return acc, self.arr["v"], None
 
     # ------------------------------------------------------------------ integration
+    def capture(self):
+        """Record one step() in a CUDA graph; every later step() replays it (one launch of
+        the whole step instead of ~20 host calls).  The state arrays become fixed device
+        buffers: the recorded step ends by copying its new state into them.  Needs one eager
+        step first (it sizes the neighbor buffer; a step that overflows it raises at check())."""
+        if self.cols is None:
+            raise N.SPHError("capture: run one step first")
+        torch.cuda.synchronize(self.device)
+        inputs = dict(self.arr)
+        g = torch.cuda.CUDAGraph()
+        steps, last = self.steps, self.last
+        try:
+            with torch.cuda.graph(g):
+                self._step_kernels()
+                for k, t in inputs.items():
+                    t.copy_(self.arr[k])
+        except Exception:
+            self.arr, self.last = inputs, last
+            raise
+        self.arr = inputs
+        self.steps = steps
+        self.graph = g
+
     def step(self, sync=True):
         """One integrate() (src/simulationBase.py:632-782)."""
+        if self.graph is not None:
+            self.graph.replay()
+        else:
+            self._step_kernels(sync)   # sync: the neighbor buffer grows to the step's pair count
+        self.steps += 1
+        if sync:
+            self.check()
+
+    def _step_kernels(self, sync=False):
         st = N.stream_ptr()
         n = self.n
         c = self.cfg
@@ -391,9 +424,6 @@ class Simulation:
             N.call("sph_update_dt", n, N.ptr(self.arr["v"]), N.ptr(self.last["acc_final"]), self.h, c.kinematic, c.cfl,
                    c.c0, int(c.solver in ("deltaSPH", "deltaPlus")), c.dt_min, c.dt_max, N.ptr(self.dt), N.ptr(sc),
                    sc.numel() * 8, st)
-        self.steps += 1
-        if sync:
-            self.check()
 
     def check(self):
         f = int(self.status.item())

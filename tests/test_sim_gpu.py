@@ -94,3 +94,35 @@ def test_dam_break_against_float64_oracle(cuda, diffusion):
     assert rel(s["x"], new["x"].numpy()) < 1e-6
     assert rel(s["rho"], new["rho"].numpy()) < 1e-5
     assert rel(s["v"], new["v"].numpy()) < 1e-2
+
+
+@pytest.mark.parametrize("solver", ["deltaSPH", "dfsph"])
+def test_captured_step_equals_eager(cuda, solver):
+    """Simulation.capture records one step in a CUDA graph (the DFSPH solves are cooperative
+    launches inside it); replaying it gives bitwise the eager steps' state, time step,
+    simulated time and iteration counts."""
+    from pytorchsph_gb300 import workloads
+    from pytorchsph_gb300.sim import Simulation, SimConfig
+    sc = workloads.dam_break(48, 64, 0.01, (1.6, 1.0))
+    c0 = float(10 * np.sqrt(2 * 9.81 * sc["column_height"]))
+    if solver == "dfsph":
+        cfg = SimConfig(solver="dfsph", integration="semiImplicitEuler", dt=2e-4, c0=c0, kinematic=0.01,
+                        fixed_dt=False, dt_min=1e-6, dt_max=1e-3)
+    else:
+        cfg = SimConfig(solver="deltaSPH", integration="semiImplicitEuler", dt=0.25 * sc["h"] / c0, c0=c0,
+                        density_diffusion="deltaSPH")
+    a, b = Simulation(sc, cfg, cuda), Simulation(sc, cfg, cuda)
+    for _ in range(2):
+        a.step()
+        b.step()
+    b.capture()
+    for _ in range(6):
+        a.step()
+        b.step()
+    sa, sb = a.state(), b.state()
+    for k in ("x", "v", "rho"):
+        assert np.array_equal(sa[k], sb[k]), k
+    assert float(a.dt.item()) == float(b.dt.item()) and float(a.time.item()) == float(b.time.item())
+    assert a.steps == b.steps == 8
+    if solver == "dfsph":
+        assert int(a.last["density_iters"].item()) == int(b.last["density_iters"].item())
