@@ -393,7 +393,7 @@ def pass1_alg_bytes(batch):
     n = batch.n
     mo, so, co, ms = ctypes.c_size_t(), ctypes.c_size_t(), ctypes.c_size_t(), ctypes.c_int32()
     N.call("sph_deltasph_segment_lists", n, ctypes.byref(mo), ctypes.byref(so), ctypes.byref(co), ctypes.byref(ms))
-    # the scratch tensor is 256-byte aligned, so its first 16-byte boundary is its start
+    # the scratch tensor is 256-byte aligned, so its first 32-byte boundary is its start
     nseg = batch.forces_scratch.view(torch.int32)[co.value // 4:co.value // 4 + n]
     segments = int(torch.clamp(nseg, min=0).sum().item())
     return n * 68 + 8 * segments + batch.nb * 20

@@ -315,7 +315,7 @@ sph_status_t sph_mdbc_wall_density(const sph_fluid_view* fluid, const sph_wall_v
  * (per-particle neighbor records, and the segment lists of sph_batch_deltasph_step). */
 size_t sph_deltasph_scratch_bytes(int64_t n);
 /* Where sph_batch_deltasph_step keeps its segment lists in a scratch of n particles (byte
- * offsets from the scratch's first 16-byte boundary): the uint32 accepted-candidate masks
+ * offsets from the scratch's first 32-byte boundary): the uint32 accepted-candidate masks
  * and the int32 segment starts (segment k of particle i at index k * n + i, k <
  * max_segments) and the int32 segment counts (-1: the particle's segments did not fit).
  * For callers that count the bytes a step moves without a host copy of the search. */

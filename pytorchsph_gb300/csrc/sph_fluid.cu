@@ -105,13 +105,18 @@ __device__ __forceinline__ void mdbc_body(int b, const FluidView& F, const WallV
 // per pair: xv = (x, y, vx, vy) and q = (rho_j, V_j = A_j / rho~_j, p_j V_j with p_j =
 // Tait(rho~_j), m_j = rho_j V_j).  Two 16-byte loads per pair replace four scalar loads, a
 // division and the Tait power.
-__device__ __forceinline__ void prep_body(int i, const FluidView& F, const SphParams& P, float4* __restrict__ xv,
-                                          float4* __restrict__ qv) {
+// Both float4 of a particle sit in one 32-byte record, so a pair's two loads share one
+// 32-byte sector and one address.
+struct __align__(32) Rec {
+  float4 xv, q;
+};
+
+__device__ __forceinline__ void prep_body(int i, const FluidView& F, const SphParams& P, Rec* __restrict__ rec) {
   const float2 x = F.x[i], v = F.v[i];
   const float rt = F.rho[i];
   const float V = F.area[i] / rt, rho = rt * P.rho0;
-  xv[i] = make_float4(x.x, x.y, v.x, v.y);
-  qv[i] = make_float4(rho, V, tait(rt, P) * V, rho * V);
+  rec[i].xv = make_float4(x.x, x.y, v.x, v.y);
+  rec[i].q = make_float4(rho, V, tait(rt, P) * V, rho * V);
 }
 
 // Pair geometry in the form the sums need: d = x_i - x_j, r2 = |d|^2 and the Wendland
@@ -284,12 +289,12 @@ struct Segments {
 // kScheme: the density diffusion (0 none, 1 MOG, 2 deltaSPH) fixed at compile time, or -1:
 // read from P.diffusion.
 template <bool kCells, int kTpp = 1, int kScheme = -1>
-__device__ __forceinline__ Pass1 pass1_body(int i, const FluidView& F, const float4* __restrict__ xv,
-                                            const float4* __restrict__ qv, const WallView& W, const sph_grid& g,
+__device__ __forceinline__ Pass1 pass1_body(int i, const FluidView& F, const Rec* __restrict__ rec,
+                                            const WallView& W, const sph_grid& g,
                                             const SphParams& P, int coff, const Segments& S, int sub = 0,
                                             bool live = true) {
-  const float4 si = xv[i];
-  const float rhoi = qv[i].x, pi = tait(F.rho[i], P);
+  const float4 si = rec[i].xv;
+  const float rhoi = rec[i].q.x, pi = tait(F.rho[i], P);
   const int scheme = kScheme >= 0 ? kScheme : P.diffusion;
   const bool renorm = scheme == 2;
   const float mu8 = 4.0f * (2.0f * rhoi * P.kinematic);   // 4 (mu_i + mu_j), both rho_i nu
@@ -297,7 +302,7 @@ __device__ __forceinline__ Pass1 pass1_body(int i, const FluidView& F, const flo
   float pax = 0.f, pay = 0.f, vax = 0.f, vay = 0.f, lax = 0.f, lay = 0.f;
   float l00 = 0.f, l01 = 0.f, l11 = 0.f, gfx = 0.f, gfy = 0.f;
   auto fluid_pair = [&](int j) {
-    const float4 sj = __ldg(xv + j), qj = __ldg(qv + j);
+    const float4 sj = __ldg(&rec[j].xv), qj = __ldg(&rec[j].q);
     const float rhoj = qj.x, Vj = qj.y, pVj = qj.z, mj = qj.w;
     const PairG e = pair_g(si.x, si.y, sj.x, sj.y, P);   // gradW = e.gd * d
     const float ux = sj.z - si.z, uy = sj.w - si.w;       // u_j - u_i
@@ -441,7 +446,7 @@ __device__ __forceinline__ Pass1 pass1_body(int i, const FluidView& F, const flo
 // product, so both give the same bits).  kCells: pairs from the segment lists instead of the
 // CSR row.
 template <bool kCells, int kTpp = 1, bool kHoldsGV = true>
-__device__ __forceinline__ float diffusion_sum(int i, const FluidView& F, const float4* __restrict__ qv,
+__device__ __forceinline__ float diffusion_sum(int i, const FluidView& F, const Rec* __restrict__ rec,
                                                const SphParams& P, const float2* __restrict__ gbuf,
                                                const sph_grid& g, int coff, const Segments& S, int sub = 0,
                                                bool live = true) {
@@ -451,7 +456,7 @@ __device__ __forceinline__ float diffusion_sum(int i, const FluidView& F, const 
     const float2 xj = __ldg(F.x + j);
     float2 gv = __ldg(gbuf + j);
     if constexpr (!kHoldsGV) {
-      const float Vj = __ldg(qv + j).y;
+      const float Vj = __ldg(&rec[j].q.y);
       gv = make_float2(gv.x * Vj, gv.y * Vj);
     }
     const PairG e = pair_g(xi.x, xi.y, xj.x, xj.y, P);
@@ -490,32 +495,30 @@ __global__ void __launch_bounds__(128) k_mdbc(FluidView F, WallView W, const sph
   mdbc_body(b, F, W, *gp, P, 0);
 }
 
-__global__ void __launch_bounds__(256) k_prep(FluidView F, SphParams P, float4* __restrict__ xv,
-                                              float4* __restrict__ qv) {
+__global__ void __launch_bounds__(256) k_prep(FluidView F, SphParams P, Rec* __restrict__ rec) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= F.n) return;
-  prep_body(i, F, P, xv, qv);
+  prep_body(i, F, P, rec);
 }
 
-__global__ void __launch_bounds__(128) k_dsph_pass1(FluidView F, const float4* __restrict__ xv,
-                                                    const float4* __restrict__ qv, WallView W,
+__global__ void __launch_bounds__(128) k_dsph_pass1(FluidView F, const Rec* __restrict__ rec, WallView W,
                                                     const sph_grid* __restrict__ gp, SphParams P,
                                                     float* __restrict__ dpdt, float2* __restrict__ acc,
                                                     float4* __restrict__ Lout, float2* __restrict__ grad_rho) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= F.n) return;
-  const Pass1 o = pass1_body<false>(i, F, xv, qv, W, *gp, P, 0, Segments{});
+  const Pass1 o = pass1_body<false>(i, F, rec, W, *gp, P, 0, Segments{});
   dpdt[i] = P.diffusion == 2 ? o.dpdt + P.diff_k * o.ddiff : o.dpdt;
   acc[i] = make_float2(o.ax, o.ay);
   if (Lout) Lout[i] = o.L;
   if (grad_rho) grad_rho[i] = o.grad_rho;
 }
 
-__global__ void __launch_bounds__(128) k_dsph_diffusion(FluidView F, const float4* __restrict__ qv, SphParams P,
+__global__ void __launch_bounds__(128) k_dsph_diffusion(FluidView F, const Rec* __restrict__ rec, SphParams P,
                                                         const float2* __restrict__ grad_rho, float* __restrict__ dpdt) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= F.n) return;
-  dpdt[i] -= P.diff_k * diffusion_sum<false, 1, false>(i, F, qv, P, grad_rho, sph_grid{}, 0, Segments{});
+  dpdt[i] -= P.diff_k * diffusion_sum<false, 1, false>(i, F, rec, P, grad_rho, sph_grid{}, 0, Segments{});
 }
 
 __global__ void k_sie(int n, const float2* __restrict__ x, const float2* __restrict__ v,
@@ -539,13 +542,13 @@ __global__ void __launch_bounds__(128, 8) k_batch_mdbc(FluidView F, WallView W, 
 
 // Neighbor records and, with pairs from the cell rows (nseg != NULL), the segment lists.
 __global__ void __launch_bounds__(256) k_batch_prep(FluidView F, const SceneDev* __restrict__ scenes,
-                                                    const int32_t* __restrict__ sid, float4* __restrict__ xv,
-                                                    float4* __restrict__ qv, int32_t* __restrict__ nseg,
+                                                    const int32_t* __restrict__ sid, Rec* __restrict__ rec,
+                                                    int32_t* __restrict__ nseg,
                                                     int32_t* __restrict__ seg_start, uint32_t* __restrict__ seg_mask) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= F.n || sid[i] < 0) return;   // particle of no scene: never anyone's neighbor
   const SceneDev& S = scenes[sid[i]];
-  prep_body(i, F, S.P, xv, qv);
+  prep_body(i, F, S.P, rec);
   if (nseg) segments_body(i, F, S.g, S.coff, S.P.search_radius, S.P.thr, nseg, seg_start, seg_mask);
 }
 
@@ -570,8 +573,7 @@ __device__ __forceinline__ void batch_update(int i, const FluidView& F, float ax
 // segment lists; kTpp lanes per particle (kCells only).  With kTpp > 1 no lane leaves
 // before the lane sums: lanes past p_hi take part with nothing to add.
 template <bool kCells, int kTpp, int kScheme>
-__global__ void __launch_bounds__(128, 8) k_batch_pass1(FluidView F, const float4* __restrict__ xv,
-                                                     const float4* __restrict__ qv, WallView W,
+__global__ void __launch_bounds__(128, 8) k_batch_pass1(FluidView F, const Rec* __restrict__ rec, WallView W,
                                                      const SceneDev* __restrict__ scenes,
                                                      const int32_t* __restrict__ sid, float* __restrict__ dpdt,
                                                      float2* __restrict__ acc, float2* __restrict__ grad_rho,
@@ -593,12 +595,12 @@ __global__ void __launch_bounds__(128, 8) k_batch_pass1(FluidView F, const float
   }
   const SceneDev& S = scenes[sid[i] < 0 ? 0 : sid[i]];
   const SphParams P = S.P;   // the fields the loop reads, in registers
-  const Pass1 o = pass1_body<kCells, kTpp, kScheme>(i, F, xv, qv, W, S.g, P, S.coff, seg, sub, kTpp == 1 || live);
+  const Pass1 o = pass1_body<kCells, kTpp, kScheme>(i, F, rec, W, S.g, P, S.coff, seg, sub, kTpp == 1 || live);
   if (kTpp > 1 && (!live || sub != 0)) return;
   if ((kScheme >= 0 ? kScheme : P.diffusion) == 2) {
     dpdt[i] = o.dpdt + P.diff_k * o.ddiff;
     acc[i] = make_float2(o.ax, o.ay);
-    const float Vi = qv[i].y;
+    const float Vi = rec[i].q.y;
     grad_rho[i] = make_float2(o.grad_rho.x * Vi, o.grad_rho.y * Vi);   // <grad rho> V for the diffusion pass
     return;
   }
@@ -606,7 +608,7 @@ __global__ void __launch_bounds__(128, 8) k_batch_pass1(FluidView F, const float
 }
 
 template <bool kCells, int kTpp>
-__global__ void __launch_bounds__(128) k_batch_diffusion(FluidView F, const float4* __restrict__ qv,
+__global__ void __launch_bounds__(128) k_batch_diffusion(FluidView F, const Rec* __restrict__ rec,
                                                          const SceneDev* __restrict__ scenes,
                                                          const int32_t* __restrict__ sid,
                                                          const float2* __restrict__ grad_rho, const Segments seg,
@@ -631,7 +633,7 @@ __global__ void __launch_bounds__(128) k_batch_diffusion(FluidView F, const floa
   const bool act = live && S.P.diffusion == 2;   // the same on all lanes of a particle
   if (kTpp == 1 && !act) return;
   const SphParams P = S.P;   // the fields the loop reads, in registers
-  const float sum = diffusion_sum<kCells, kTpp>(i, F, qv, P, grad_rho, S.g, S.coff, seg, sub, kTpp == 1 || act);
+  const float sum = diffusion_sum<kCells, kTpp>(i, F, rec, P, grad_rho, S.g, S.coff, seg, sub, kTpp == 1 || act);
   if (kTpp > 1 && (!act || sub != 0)) return;
   const float d = dpdt[i] - P.diff_k * sum;
   const float2 a = acc[i];
@@ -716,6 +718,7 @@ sph_status_t sph_mdbc_wall_density(const sph_fluid_view* fluid, const sph_wall_v
 constexpr size_t kRecordBytes = 2 * sizeof(float4),
                  kMaskBytes = kMaxSegments * (sizeof(uint32_t) + sizeof(int32_t)) + sizeof(int32_t);
 size_t sph_deltasph_scratch_bytes(int64_t n) { return (size_t)(n > 0 ? n : 0) * (kRecordBytes + kMaskBytes) + 256; }
+static_assert(sizeof(Rec) == kRecordBytes, "a neighbor record is two float4");
 
 sph_status_t sph_deltasph_segment_lists(int64_t n, size_t* masks_offset, size_t* starts_offset,
                                         size_t* counts_offset, int32_t* max_segments) {
@@ -730,17 +733,15 @@ sph_status_t sph_deltasph_segment_lists(int64_t n, size_t* masks_offset, size_t*
 
 }  // extern "C"
 
-// The neighbor records (xv, q) in caller scratch, 16-byte aligned.
-static bool records_from_scratch(void* scratch, size_t bytes, int64_t n, float4** xv, float4** qv,
-                                 Segments* seg = nullptr) {
+// The neighbor records in caller scratch, 32-byte aligned.
+static bool records_from_scratch(void* scratch, size_t bytes, int64_t n, Rec** rec, Segments* seg = nullptr) {
   if (!scratch) return false;
   const uintptr_t base = reinterpret_cast<uintptr_t>(scratch);
-  const uintptr_t p = (base + 15) & ~(uintptr_t)15;
+  const uintptr_t p = (base + 31) & ~(uintptr_t)31;
   if ((p - base) + (size_t)n * (kRecordBytes + (seg ? kMaskBytes : 0)) > bytes) return false;
-  *xv = reinterpret_cast<float4*>(p);
-  *qv = *xv + n;
+  *rec = reinterpret_cast<Rec*>(p);
   if (seg) {
-    uint32_t* m = reinterpret_cast<uint32_t*>(*qv + n);
+    uint32_t* m = reinterpret_cast<uint32_t*>(*rec + n);
     int32_t* st = reinterpret_cast<int32_t*>(m + kMaxSegments * n);
     seg->mask = m;
     seg->start = st;
@@ -759,19 +760,19 @@ sph_status_t sph_deltasph_forces(const sph_fluid_view* fluid, const sph_wall_vie
   SPH_REQUIRE(grid && params && dpdt && acc && params->support > 0.f, "deltasph_forces: bad arguments");
   SPH_REQUIRE(params->density_diffusion != 2 || grad_rho, "deltasph_forces: deltaSPH diffusion needs grad_rho");
   if (fluid->n == 0) return SPH_OK;
-  float4 *xv, *qv;
-  SPH_REQUIRE(records_from_scratch(scratch, scratch_bytes, fluid->n, &xv, &qv),
+  Rec* rec;
+  SPH_REQUIRE(records_from_scratch(scratch, scratch_bytes, fluid->n, &rec),
               "deltasph_forces: scratch smaller than sph_deltasph_scratch_bytes(n)");
   cudaStream_t st = as_stream(stream);
   const FluidView F = to_fluid(fluid);
   const WallView W = to_walls(walls);
   const SphParams P = to_params(params);
   const int nb = grid_for(fluid->n, 128);
-  k_prep<<<grid_for(fluid->n, 256), 256, 0, st>>>(F, P, xv, qv);
-  k_dsph_pass1<<<nb, 128, 0, st>>>(F, xv, qv, W, grid, P, dpdt, reinterpret_cast<float2*>(acc),
+  k_prep<<<grid_for(fluid->n, 256), 256, 0, st>>>(F, P, rec);
+  k_dsph_pass1<<<nb, 128, 0, st>>>(F, rec, W, grid, P, dpdt, reinterpret_cast<float2*>(acc),
                                    reinterpret_cast<float4*>(L), reinterpret_cast<float2*>(grad_rho));
   if (P.diffusion == 2)
-    k_dsph_diffusion<<<nb, 128, 0, st>>>(F, qv, P, reinterpret_cast<const float2*>(grad_rho), dpdt);
+    k_dsph_diffusion<<<nb, 128, 0, st>>>(F, rec, P, reinterpret_cast<const float2*>(grad_rho), dpdt);
   SPH_CHECK_LAUNCH("deltasph_forces");
   return SPH_OK;
 }
@@ -823,9 +824,9 @@ sph_status_t sph_batch_deltasph_step(const sph_fluid_view* fluid, const sph_wall
     SPH_REQUIRE(G[k].scheme >= -1 && G[k].scheme <= 2, "batch_deltasph_step: bad diffusion scheme");
   }
   if (n == 0) return SPH_OK;
-  float4 *xv, *qv;
+  Rec* rec;
   Segments seg{};
-  SPH_REQUIRE(records_from_scratch(scratch, scratch_bytes, n, &xv, &qv, cells ? &seg : nullptr),
+  SPH_REQUIRE(records_from_scratch(scratch, scratch_bytes, n, &rec, cells ? &seg : nullptr),
               "batch_deltasph_step: scratch smaller than sph_deltasph_scratch_bytes(n)");
   cudaStream_t st = as_stream(stream);
   const FluidView F = to_fluid(fluid);
@@ -833,7 +834,7 @@ sph_status_t sph_batch_deltasph_step(const sph_fluid_view* fluid, const sph_wall
   const SceneDev* S = static_cast<const SceneDev*>(scenes);
   if (W.n > 0 && (phases & SPH_PHASE_WALLS)) k_batch_mdbc<<<grid_for(W.n, 128), 128, 0, st>>>(F, W, S, wall_sid);
   if (phases & SPH_PHASE_RECORDS)
-    k_batch_prep<<<grid_for(n, 256), 256, 0, st>>>(F, S, sid, xv, qv, const_cast<int32_t*>(seg.nseg),
+    k_batch_prep<<<grid_for(n, 256), 256, 0, st>>>(F, S, sid, rec, const_cast<int32_t*>(seg.nseg),
                                                    const_cast<int32_t*>(seg.start), const_cast<uint32_t*>(seg.mask));
   float2* xo = reinterpret_cast<float2*>(x_out);
   float2* vo = reinterpret_cast<float2*>(v_out);
@@ -844,7 +845,7 @@ sph_status_t sph_batch_deltasph_step(const sph_fluid_view* fluid, const sph_wall
   auto pass1 = [&](int lo, int hi, int t, int scheme) {
     const int nb = grid_for((int64_t)(hi - lo) * t, 128);
 #define SPH_PASS1(C, T, K)                                                                                  \
-  k_batch_pass1<C, T, K><<<nb, 128, 0, st>>>(F, xv, qv, W, S, sid, dpdt, ac, gr, C ? seg : Segments{}, xo, vo, \
+  k_batch_pass1<C, T, K><<<nb, 128, 0, st>>>(F, rec, W, S, sid, dpdt, ac, gr, C ? seg : Segments{}, xo, vo, \
                                              rho_out, status, lo, hi)
     if (!cells) {
       SPH_PASS1(false, 1, -1);
@@ -873,16 +874,16 @@ sph_status_t sph_batch_deltasph_step(const sph_fluid_view* fluid, const sph_wall
     if (hi <= lo || G[k].scheme == 0 || G[k].scheme == 1) continue;   // no deltaSPH scene in the group
     const int nb = grid_for((int64_t)(hi - lo) * t, 128);
     if (!cells)
-      k_batch_diffusion<false, 1><<<nb, 128, 0, st>>>(F, qv, S, sid, gr, Segments{}, dpdt, ac, xo, vo, rho_out,
+      k_batch_diffusion<false, 1><<<nb, 128, 0, st>>>(F, rec, S, sid, gr, Segments{}, dpdt, ac, xo, vo, rho_out,
                                                       status, lo, hi);
     else if (t == 1)
-      k_batch_diffusion<true, 1><<<nb, 128, 0, st>>>(F, qv, S, sid, gr, seg, dpdt, ac, xo, vo, rho_out, status, lo,
+      k_batch_diffusion<true, 1><<<nb, 128, 0, st>>>(F, rec, S, sid, gr, seg, dpdt, ac, xo, vo, rho_out, status, lo,
                                                      hi);
     else if (t == 2)
-      k_batch_diffusion<true, 2><<<nb, 128, 0, st>>>(F, qv, S, sid, gr, seg, dpdt, ac, xo, vo, rho_out, status, lo,
+      k_batch_diffusion<true, 2><<<nb, 128, 0, st>>>(F, rec, S, sid, gr, seg, dpdt, ac, xo, vo, rho_out, status, lo,
                                                      hi);
     else
-      k_batch_diffusion<true, 4><<<nb, 128, 0, st>>>(F, qv, S, sid, gr, seg, dpdt, ac, xo, vo, rho_out, status, lo,
+      k_batch_diffusion<true, 4><<<nb, 128, 0, st>>>(F, rec, S, sid, gr, seg, dpdt, ac, xo, vo, rho_out, status, lo,
                                                      hi);
   }
   SPH_CHECK_LAUNCH("batch_deltasph_step");

@@ -136,10 +136,12 @@ def upload_scenes(specs, device):
     for s, sp in enumerate(todo):
         d = {"device": device, "n": counts["n"][s], "nb": counts["nb"][s], "cell_ratio": sp.cell_ratio,
              "grid": _Grid.from_buffer_copy(raw[32 * s:32 * (s + 1)])}
+        d["src"] = {}
         for name, (t, _) in dev_fields.items():
             lo, hi = offs[name][s], offs[name][s + 1]
             if hi > lo:
                 d[name] = t[lo:hi]
+                d["src"][name] = (t, int(lo), int(hi))   # rows of one upload buffer
         sp.dev = d
 
 
@@ -653,13 +655,13 @@ class SceneArena(SceneBatch):
         self._cell_top = at
         self._walls_dirty = True
 
-    def _write_scene(self, slot):
+    def _encode_row(self, slot):
+        """The slot's scene-table row, into its row of the pinned staging table (a mirror of
+        the device table); a row is rewritten only after the event behind its last copy."""
         d = self.slots[slot]
         sp = d["spec"]
         h = float(np.float32(sp.scene["support"][0]))
         P = _params_for(sp.cfg, h, d["grid"].num_cells, sp.cell_ratio)
-        # through the slot's row of a pinned staging table, so the host does not wait for the
-        # queued steps; a row is rewritten only after the event behind its last copy
         ev = self._row_events[slot]
         if ev is not None:
             ev.synchronize()
@@ -667,10 +669,20 @@ class SceneArena(SceneBatch):
         buf = (ctypes.c_char * self.rec).from_address(row.data_ptr())
         N.check(self.lib.sph_scene_encode(ctypes.byref(P), ctypes.byref(d["grid"]), d["coff"], sp.cfg.dt, buf),
                 "scene_encode")
-        self.scenes[slot * self.rec:(slot + 1) * self.rec].copy_(row, non_blocking=True)
+
+    def _copy_rows(self, lo, hi):
+        """Rows [lo, hi) of the staging table to the device table, behind the queued steps (no
+        host wait); rows in between that did not change are copied unchanged."""
+        a, b = lo * self.rec, hi * self.rec
+        self.scenes[a:b].copy_(self._rows_host[a:b], non_blocking=True)
         ev = torch.cuda.Event()
         ev.record()
-        self._row_events[slot] = ev
+        for k in range(lo, hi):
+            self._row_events[k] = ev
+
+    def _write_scene(self, slot):
+        self._encode_row(slot)
+        self._copy_rows(slot, slot + 1)
 
     def _sort_walls(self):
         """Sort the staging walls by (scene, cell) into the arrays the batch kernels read; the
@@ -735,6 +747,82 @@ class SceneArena(SceneBatch):
             self._walls_dirty = True
         self._specs = None
         return slot
+
+    _PARTICLE_FIELDS = (("pos", "x"), ("vel", "v"), ("rho", "rho"), ("area", "area"))
+    _WALL_FIELDS = (("wall_pos", "x"), ("ghost_pos", "ghost"), ("wall_area", "area"))
+
+    def admit_many(self, specs):
+        """admit() for several new scenes at once: the bookkeeping per scene, then one copy per
+        field for each run of scenes that were uploaded side by side (upload_scenes), one
+        copy of their scene-table rows, and the id stamps.  Returns their slots, or None
+        (admitting none) when they do not all fit behind the occupied particles, walls and
+        cell ranges; admit() one by one then finds gaps or raises ArenaFull."""
+        if not specs:
+            return []
+        for sp in specs:
+            cfg = sp.cfg
+            if cfg.solver != "deltaSPH" or cfg.integration != "semiImplicitEuler":
+                raise N.SPHError("batched serving runs deltaSPH with semi-implicit Euler")
+            if self.scheme >= 0 and DIFFUSION[cfg.density_diffusion] != self.scheme:
+                raise N.SPHError("the scene's density diffusion is not the arena's")
+            sp.tpp = self.tpp
+        upload_scenes(specs, self.device)
+        ds = [sp.dev for sp in specs]
+        n_tot = sum(d["n"] for d in ds)
+        nb_tot = sum(d["nb"] for d in ds)
+        cells = [d["grid"].num_cells + 1 for d in ds]
+        if (len(self.free_slots) < len(specs) or self.occupied + n_tot > self.N or
+                self.walls_n + nb_tot > self.WC or self.C - self._cell_top < sum(cells)):
+            return None
+        slots = self.free_slots[:len(specs)]
+        del self.free_slots[:len(specs)]
+        for sp, d, slot, nc in zip(specs, ds, slots, cells):
+            self.slots[slot] = {"spec": sp, "n": d["n"], "nb": d["nb"], "coff": self._cell_top, "ncells": nc,
+                                "grid": d["grid"]}
+            self._cell_top += nc
+            self._encode_row(slot)
+        self._copy_rows(min(slots), max(slots) + 1)
+        st = N.stream_ptr()
+        cur = self._aux(self.par)
+        p, w = self.occupied, self.walls_n
+        for d, slot in zip(ds, slots):
+            N.call("sph_arena_set_ids", N.ptr(cur["sid"]), N.ptr(cur["uid"]), p, d["n"], slot, st)
+            if d["nb"]:
+                N.call("sph_arena_set_ids", N.ptr(self.ws_w["sid"]), N.ptr(self.ws_w["uid"]), w, d["nb"], slot, st)
+            p += d["n"]
+            w += d["nb"]
+        dst = {"x": self.a["x"], "v": self.a["v"], "rho": self.a["rho"], "area": cur["area"]}
+        self._copy_runs(ds, self._PARTICLE_FIELDS, dst, self.occupied)
+        if nb_tot:
+            self._copy_runs(ds, self._WALL_FIELDS, self.ws_w, self.walls_n)
+            self._walls_dirty = True
+        self.occupied = p
+        self.live_n += n_tot
+        self.walls_n = w
+        self._specs = None
+        return slots
+
+    @staticmethod
+    def _copy_runs(ds, fields, dst, start):
+        """dst[name][start + ...] <- the scenes' rows of each field in order, one copy per run
+        of scenes whose rows lie side by side in one upload buffer."""
+        for name, key in fields:
+            at = start
+            run = None            # [buffer, lo, hi, dst offset]
+            for d in ds:
+                src = d["src"].get(name)
+                if src is None:
+                    continue
+                t, lo, hi = src
+                if run is not None and run[0] is t and run[2] == lo:
+                    run[2] = hi
+                else:
+                    if run is not None:
+                        dst[key][run[3]:run[3] + run[2] - run[1]].copy_(run[0][run[1]:run[2]])
+                    run = [t, lo, hi, at]
+                at += hi - lo
+            if run is not None:
+                dst[key][run[3]:run[3] + run[2] - run[1]].copy_(run[0][run[1]:run[2]])
 
     def scene_state_device(self, slot, states=None):
         """x, v, rho of the scene in `slot` in its own particle order (device, fresh tensors)."""
@@ -1015,8 +1103,10 @@ class Server:
         self.rebuild_seconds += time.perf_counter() - t
 
     def _admit_pooled(self, queue, now):
+        if not queue or queue[0].arrival > now:
+            return False
         arrived = []
-        used = sum(estimate_bytes(r.spec.scene, self.pairs) for r in self.live)
+        used = self._used_bytes
         while queue and queue[0].arrival <= now:
             need = estimate_bytes(queue[0].spec.scene, self.pairs)
             if used + need > self.budget and (self.live or arrived):
@@ -1031,21 +1121,40 @@ class Server:
                 self.tuning.configure(r.spec)
             r.spec.tpp = self._tpp
         upload_scenes([r.spec for r in arrived], self.device)   # one upload and grid launch
-        for k, r in enumerate(arrived):
-            try:
-                if self.arena is None:
-                    raise ArenaFull("no arena yet")
-                r.slot = self.arena.admit(r.spec)
-            except ArenaFull:
-                self._grow([q.spec for q in arrived[k:]], queue)
-                r.slot = self.arena.admit(r.spec)
+
+        def admitted(r, slot):
+            r.slot = slot
             r.admitted = now
             self.live.append(r)
+            self._used_bytes += estimate_bytes(r.spec.scene, self.pairs)
+
+        # all behind the occupied slots at once when they fit, else one by one (gaps, packing)
+        # and a larger arena when those run out
+        slots = self.arena.admit_many([r.spec for r in arrived]) if self.arena is not None else None
+        if slots is not None:
+            for r, slot in zip(arrived, slots):
+                admitted(r, slot)
+        else:
+            for k, r in enumerate(arrived):
+                try:
+                    if self.arena is None:
+                        raise ArenaFull("no arena yet")
+                    admitted(r, self.arena.admit(r.spec))
+                except ArenaFull:
+                    self._grow([q.spec for q in arrived[k:]], queue)   # moves the live scenes over
+                    rest = arrived[k:]
+                    slots = self.arena.admit_many([q.spec for q in rest])
+                    if slots is None:
+                        slots = [self.arena.admit(q.spec) for q in rest]
+                    for q, slot in zip(rest, slots):
+                        admitted(q, slot)
+                    break
         self.admit_seconds += time.perf_counter() - t
         return True
 
     def _retire_pooled(self, r, now, error=None):
         st = self.arena.retire(r.slot)
+        self._used_bytes -= estimate_bytes(r.spec.scene, self.pairs)
         r.finished = now
         if error:
             r.error = error
@@ -1063,6 +1172,7 @@ class Server:
         self._tpp = 1
         self.admit_seconds = 0.0
         self._pinned = _PinnedPool()
+        self._used_bytes = 0
         flags = torch.zeros(2, dtype=torch.int32, pin_memory=True)
         done = [None, None]          # event after each of the last two steps' status copies
         timed = []                   # (start event, end event, live scenes) per step

@@ -98,3 +98,24 @@ def test_pooled_server_grows_and_matches_alone(cuda):
         assert same(run_batch([r.spec], r.spec.steps, cuda)[0], r.final)
     p = srv.latency_percentiles()
     assert p[50] is not None and p[99] >= p[50] > 0
+
+
+def test_admit_many_equals_one_by_one(cuda):
+    """Admitting several scenes in one call (one copy per field for scenes uploaded side by
+    side) gives bitwise the states of admitting them one by one; when they do not all fit it
+    admits none and says so."""
+    A, B, C = spec("dam_break", 2600, 0.9), spec("drop", 2300, 1.3), spec("dam_break", 3100, 1.6)
+    a1 = arena(cuda)
+    s1 = a1.admit_many([A, B, C])
+    assert s1 is not None and len(set(s1)) == 3
+    stepper(a1)(4)
+    a1.check()
+    for x in (A, B, C):
+        x.dev = None                  # upload again, one scene at a time
+    a2 = arena(cuda)
+    s2 = [a2.admit(x) for x in (A, B, C)]
+    stepper(a2)(4)
+    for p, q in zip(s1, s2):
+        assert same(a1.scene_state(p), a2.scene_state(q))
+    small = arena(cuda, particles=6000)
+    assert small.admit_many([A, B, C]) is None and not small.slots and small.occupied == 0
