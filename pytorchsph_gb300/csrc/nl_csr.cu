@@ -40,7 +40,7 @@ __device__ __forceinline__ uint32_t segment_mask_density(const float2* __restric
       if (in0) m |= 1u << t;
       if (in1) m |= 2u << t;
       if (in0 || in1) {
-        const float2 rs = __fmul2_rn(make_float2(rsqrtf(fmaxf(v.x, 1e-30f)), rsqrtf(fmaxf(v.y, 1e-30f))), is2);
+        const float2 rs = __fmul2_rn(make_float2(rsqrt_normal(fmaxf(v.x, 1e-30f)), rsqrt_normal(fmaxf(v.y, 1e-30f))), is2);
         const float2 q = __fmul2_rn(v, rs);
         const float2 am = __fadd2_rn(make_float2(1.f, 1.f), make_float2(-q.x, -q.y));
         const float2 a2 = __fmul2_rn(am, am);

@@ -235,7 +235,7 @@ __global__ void __launch_bounds__(128) k_dfsph_wall_prepare(FluidView F, WallVie
 // reference's e is zero).
 __device__ __forceinline__ float spiky_gd(float r2, const SphParams& P) {
   if (!(r2 >= 1e-14f)) return 0.f;
-  const float rs = rsqrtf(r2);
+  const float rs = rsqrt_normal(r2);
   return kGS(r2 * rs * P.inv_h, P.c_s) * rs;
 }
 

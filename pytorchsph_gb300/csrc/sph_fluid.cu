@@ -57,14 +57,14 @@ __device__ __forceinline__ void mdbc_body(int b, const FluidView& F, const WallV
             // e = (x_g - x_j) / r from one rsqrt (zero below r = 1e-7, as the reference's e_ij)
             const float dx = xg.x - xj.x, dy = xg.y - xj.y;
             const float r2 = dx * dx + dy * dy;
-            const float ir = r2 >= 1e-14f ? rsqrtf(r2) : 0.f;
+            const float ir = r2 >= 1e-14f ? rsqrt_normal(r2) : 0.f;
             const float q = r2 * ir * P.inv_h;
             const float k = kW(q, P.c_w);
             const float gwr = kGW(q, P.c_g) * ir;
             const float ggx = gwr * dx, ggy = gwr * dy;
             const float Aj = F.area[j];
             const float mass = Aj * P.rho0;
-            const float Vj = __fdividef(Aj, F.rho[j]);
+            const float Vj = Aj * rcp_normal(F.rho[j]);
             const float xx = xj.x - xg.x, xy = xj.y - xg.y;
             nom += mass * k;
             den += Vj * k;
@@ -133,7 +133,7 @@ __device__ __forceinline__ PairG pair_g(float xi, float yi, float xj, float yj, 
   g.dy = yi - yj;
   g.r2 = g.dx * g.dx + g.dy * g.dy;
   const bool apart = g.r2 >= 1e-14f;
-  const float r = apart ? g.r2 * rsqrtf(g.r2) : 0.f;
+  const float r = apart ? g.r2 * rsqrt_normal(g.r2) : 0.f;
   const float a = 1.0f - r * P.inv_h;
   g.gd = apart ? P.gk * (a * a * a) : 0.f;
   return g;
@@ -307,7 +307,7 @@ __device__ __forceinline__ Pass1 pass1_body(int i, const FluidView& F, const Rec
     const PairG e = pair_g(si.x, si.y, sj.x, sj.y, P);   // gradW = e.gd * d
     const float ux = sj.z - si.z, uy = sj.w - si.w;       // u_j - u_i
     const float ud = ux * e.dx + uy * e.dy;               // (u_j - u_i) . d
-    const float ir2 = __fdividef(1.0f, e.r2 + P.eps);
+    const float ir2 = rcp_normal(e.r2 + P.eps);
     const float rg = -e.gd * e.r2;                        // (x_j - x_i) . gradW
     dp_f -= e.gd * ud * mj;
     // MOG diffusion; for deltaSPH the first part of its diffusion (x 2 after the sum)
@@ -315,7 +315,7 @@ __device__ __forceinline__ Pass1 pass1_body(int i, const FluidView& F, const Rec
     const float pf = fmaf(pi, Vj, pVj) * e.gd;            // (p_i + p_j) V_j gd
     pax += pf * e.dx;
     pay += pf * e.dy;
-    const float irs = __fdividef(1.0f, rhoi + rhoj);
+    const float irs = rcp_normal(rhoi + rhoj);
     const float w = mj * irs * ir2;
     const float vf = fminf(-ud, 0.f) * w * e.gd;          // pi_ij, (u_j - u_i) . (x_j - x_i) = -ud
     vax += vf * e.dx;
@@ -380,8 +380,8 @@ __device__ __forceinline__ Pass1 pass1_body(int i, const FluidView& F, const Rec
           pwx += pf * e.dx;
           pwy += pf * e.dy;
           if (P.boundary_diffusion) {
-            const float vf = fminf(-ud, 0.f) * __fdividef(1.0f, e.r2 + P.eps) * Vb * rhob *
-                             __fdividef(1.0f, rhoi + rhob) * e.gd;
+            const float vf = fminf(-ud, 0.f) * rcp_normal(e.r2 + P.eps) * Vb * rhob *
+                             rcp_normal(rhoi + rhob) * e.gd;
             vwx += vf * e.dx;
             vwy += vf * e.dy;
           }

@@ -60,6 +60,22 @@ __device__ __forceinline__ float kGS(float q, float c_s) {
   return -c_s * a * a;
 }
 
+// Approximate reciprocal square root and reciprocal of a positive NORMAL float (every caller
+// passes a value >= 1e-30): the same hardware approximation as rsqrtf(x) and
+// __fdividef(1, x), in their .ftz forms, which skip the scaling that the default forms wrap
+// around it for subnormal inputs.  For normal inputs the results are the same.
+__device__ __forceinline__ float rsqrt_normal(float x) {
+  float r;
+  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+
+__device__ __forceinline__ float rcp_normal(float x) {
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+
 struct Geo {
   float dx, dy;   // x_row - x_col
   float r, q;
