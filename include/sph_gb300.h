@@ -565,6 +565,15 @@ sph_status_t sph_arena_extract(const float* x, const float* v, const float* rho,
                                float* rho_out, void* stream);
 /* sid[i] = -1 for every i < n with sid[i] == scene (its particles leave the batch at the next sort). */
 sph_status_t sph_arena_retire(int32_t* sid, int64_t n, int32_t scene, void* stream);
+/* Several scenes of a pooled batch in one pass over its n slots: for every slot table entry s
+ * (0 <= s < nslots) with row0[s] >= 0, the particles of scene s go to the output rows
+ * row0[s] + particle id (ids >= rows[s] are skipped), and with `retire` their slots are
+ * freed (scene index -1).  x_out, v_out, rho_out all NULL: retire only (x, v, rho, uid may
+ * then be NULL).  row0 [nslots] int64 and rows [nslots] int32 are device arrays. */
+sph_status_t sph_arena_extract_many(const float* x, const float* v, const float* rho, int32_t* sid,
+                                    const int32_t* uid, int64_t n, const int64_t* row0, const int32_t* rows,
+                                    int32_t nslots, float* x_out, float* v_out, float* rho_out, int32_t retire,
+                                    void* stream);
 
 /* ---------------------------------------------------------------- delta+ surface detection and shifting (f3) */
 

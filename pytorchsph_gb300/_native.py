@@ -87,6 +87,7 @@ SIGNATURES.update({  # Module-interface terms
     "sph_surface_scratch_bytes": (_SZ, []),
     "sph_arena_set_ids": (_I32, [_P, _P, _I64, _I64, _I32, _P]),
     "sph_arena_extract": (_I32, [_P, _P, _P, _P, _P, _I64, _I32, _P, _P, _P, _P]),
+    "sph_arena_extract_many": (_I32, [_P, _P, _P, _P, _P, _I64, _P, _P, _I32, _P, _P, _P, _I32, _P]),
     "sph_arena_retire": (_I32, [_P, _I64, _I32, _P]),
     "sph_periodic_ghosts_scratch_bytes": (_SZ, [_I64]),
     "sph_periodic_ghosts": (_I32, [_P, _I64, _P, _P, _F32, _I32, _I32, _I64, _P, _P, _P, _P, _P, _SZ, _P]),

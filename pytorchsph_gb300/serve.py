@@ -84,18 +84,61 @@ _FIELDS = (("pos", "pos", 2, "n"), ("vel", "vel", 2, "n"), ("rho", "rho", 1, "n"
            ("wall_area", "wall_area", 1, "nb"))
 
 
-def upload_scenes(specs, device):
+def _pinned(a, dtype):
+    t = torch.empty(a.shape, dtype=dtype, pin_memory=True)
+    t.numpy()[...] = a
+    return t
+
+
+class PendingUpload:
+    """Scenes whose arrays and grid launch are queued on the device (upload_scenes with
+    wait=False).  finish() waits for the event behind the grids' copy back to pinned host
+    memory (long done when called a step later), checks the status and gives each spec its
+    `dev` entry."""
+
+    def __init__(self, todo, device, counts, dev_fields, grids_host, status_host, event, keep):
+        self.todo, self.device, self.counts, self.dev_fields = todo, device, counts, dev_fields
+        self.grids_host, self.status_host, self.event, self._keep = grids_host, status_host, event, keep
+
+    def ready(self) -> bool:
+        return self.event is None or self.event.query()
+
+    def finish(self):
+        if self.event is not None:
+            self.event.synchronize()
+        self._keep = None
+        flags = int(self.status_host[0])
+        if flags:
+            raise N.SPHError(f"scene grids: {N.decode_flags(flags)}")
+        raw = self.grids_host.numpy().tobytes()
+        offs = {name: np.concatenate([[0], np.cumsum(c)]) for name, (_, c) in self.dev_fields.items()}
+        for s, sp in enumerate(self.todo):
+            d = {"device": self.device, "n": self.counts["n"][s], "nb": self.counts["nb"][s],
+                 "cell_ratio": sp.cell_ratio, "grid": _Grid.from_buffer_copy(raw[32 * s:32 * (s + 1)])}
+            d["src"] = {}
+            for name, (t, _) in self.dev_fields.items():
+                lo, hi = offs[name][s], offs[name][s + 1]
+                if hi > lo:
+                    d[name] = t[lo:hi]
+                    d["src"][name] = (t, int(lo), int(hi))   # rows of one upload buffer
+            sp.dev = d
+
+
+def upload_scenes(specs, device, wait: bool = True):
     """Device copies and grids of every spec not yet on `device`: one copy per field for all
-    of them (from pinned host memory) and one grid launch (sph_grid_build_segments)."""
+    of them (from pinned host memory) and one grid launch (sph_grid_build_segments).  Every
+    host-to-device copy comes from pinned memory and the grids come back through pinned
+    memory behind an event, so with wait=False nothing here waits for the device: the
+    returned PendingUpload is finished later (None when every spec was on the device)."""
     device = torch.device(device)
     todo = [sp for sp in specs if sp.dev is None or sp.dev["device"] != device or
             sp.dev["cell_ratio"] != sp.cell_ratio]
     if not todo:
-        return
-    lib = N.load()
+        return None
     counts = {"n": [len(sp.scene["pos"]) for sp in todo],
               "nb": [len(sp.scene.get("wall_pos", ())) for sp in todo]}
     dev_fields = {}
+    keep = []                     # pinned sources, alive until the copies have run
     for name, key, width, cnt in _FIELDS:
         c = counts[cnt]
         total = sum(c)
@@ -109,40 +152,39 @@ def upload_scenes(specs, device):
                 hv[o:o + k] = np.asarray(sp.scene[key], np.float32).reshape(hv[o:o + k].shape)
                 o += k
         dev_fields[name] = (host.to(device, non_blocking=True), c)
+        keep.append(host)
     S = len(todo)
-    seg = torch.tensor(np.concatenate([[0], np.cumsum(counts["n"])]), dtype=torch.int64).to(device)
-    vmin = torch.tensor(np.array([sp.scene["vmin"] for sp in todo], np.float32)).to(device)
-    vmax = torch.tensor(np.array([sp.scene["vmax"] for sp in todo], np.float32)).to(device)
-    grids = torch.empty(S * 8, dtype=torch.int32, device=device)
-    status = torch.zeros(1, dtype=torch.int32, device=device)
     # the grid's cell size is the largest support of the scene over its cell_ratio; the grid
     # pads the domain by one cell below and two above, so the domain given to it grows by
     # the difference to keep that padding one and two supports (walls lie in it)
+    grow = np.array([float(np.max(sp.scene["support"])) * (1.0 - 1.0 / sp.cell_ratio) for sp in todo],
+                    np.float32)[:, None]
+    small = [_pinned(np.concatenate([[0], np.cumsum(counts["n"])]).astype(np.int64), torch.int64),
+             _pinned(np.array([sp.scene["vmin"] for sp in todo], np.float32) - grow, torch.float32),
+             _pinned(np.array([sp.scene["vmax"] for sp in todo], np.float32) + 2.0 * grow, torch.float32)]
+    keep += small
+    seg, vmin, vmax = (t.to(device, non_blocking=True) for t in small)
+    grids = torch.empty(S * 8, dtype=torch.int32, device=device)
+    status = torch.zeros(1, dtype=torch.int32, device=device)
     cell_h = dev_fields["sup"][0]
     if any(sp.cell_ratio != 1 for sp in todo):
-        inv = torch.tensor([1.0 / sp.cell_ratio for sp in todo], dtype=torch.float32, device=device)
-        cell_h = cell_h * torch.repeat_interleave(inv, torch.tensor(counts["n"], device=device))
-        grow = np.array([float(np.max(sp.scene["support"])) * (1.0 - 1.0 / sp.cell_ratio) for sp in todo],
-                        np.float32)[:, None]
-        vmin = vmin - torch.from_numpy(grow).to(device)
-        vmax = vmax + torch.from_numpy(2.0 * grow).to(device)
+        per = _pinned(np.repeat(np.array([1.0 / sp.cell_ratio for sp in todo], np.float32), counts["n"]),
+                      torch.float32)
+        keep.append(per)
+        cell_h = cell_h * per.to(device, non_blocking=True)
     N.call("sph_grid_build_segments", N.ptr(dev_fields["pos"][0]), N.ptr(cell_h), N.ptr(seg), S,
            N.ptr(vmin), N.ptr(vmax), MAX_CELLS, N.ptr(grids), N.ptr(status), N.stream_ptr())
-    flags = int(status.item())
-    if flags:
-        raise N.SPHError(f"scene grids: {N.decode_flags(flags)}")
-    raw = grids.cpu().numpy().tobytes()
-    offs = {name: np.concatenate([[0], np.cumsum(c)]) for name, (_, c) in dev_fields.items()}
-    for s, sp in enumerate(todo):
-        d = {"device": device, "n": counts["n"][s], "nb": counts["nb"][s], "cell_ratio": sp.cell_ratio,
-             "grid": _Grid.from_buffer_copy(raw[32 * s:32 * (s + 1)])}
-        d["src"] = {}
-        for name, (t, _) in dev_fields.items():
-            lo, hi = offs[name][s], offs[name][s + 1]
-            if hi > lo:
-                d[name] = t[lo:hi]
-                d["src"][name] = (t, int(lo), int(hi))   # rows of one upload buffer
-        sp.dev = d
+    grids_host = torch.empty(S * 8, dtype=torch.int32, pin_memory=True)
+    status_host = torch.empty(1, dtype=torch.int32, pin_memory=True)
+    grids_host.copy_(grids, non_blocking=True)
+    status_host.copy_(status, non_blocking=True)
+    ev = torch.cuda.Event()
+    ev.record()
+    pending = PendingUpload(todo, device, counts, dev_fields, grids_host, status_host, ev,
+                            keep + [seg, vmin, vmax, grids, status, cell_h])
+    if wait:
+        pending.finish()
+    return pending
 
 
 def scene_order(lanes, schemes):
@@ -875,6 +917,46 @@ class SceneArena(SceneBatch):
             self._sort_walls()
             self._walls_dirty = False
 
+    def retire_many(self, slots):
+        """retire() for several scenes at once: one pass over the particle slots extracts their
+        states and frees them (one more frees their walls).  Returns (rows, (x, v, rho)):
+        rows[slot] = (first row, count) of that scene in the three device buffers, each in
+        the scene's own particle order."""
+        if not slots:
+            return {}, None
+        dev = self.device
+        row0 = np.full(self.S, -1, np.int64)
+        nrows = np.zeros(self.S, np.int32)
+        wrow0 = np.full(self.S, -1, np.int64)
+        rows, at = {}, 0
+        for sl in slots:
+            d = self.slots[sl]
+            row0[sl], nrows[sl] = at, d["n"]
+            rows[sl] = (at, d["n"])
+            at += d["n"]
+            if d["nb"]:
+                wrow0[sl] = 0
+        t_row0, t_rows, t_wrow0 = (_pinned(a, dt).to(dev, non_blocking=True) for a, dt in
+                                   ((row0, torch.int64), (nrows, torch.int32), (wrow0, torch.int64)))
+        out = (torch.empty((at, 2), dtype=torch.float32, device=dev), torch.empty((at, 2), dtype=torch.float32, device=dev),
+               torch.empty(at, dtype=torch.float32, device=dev))
+        st = N.stream_ptr()
+        cur = self._aux(self.par)
+        N.call("sph_arena_extract_many", N.ptr(self.a["x"]), N.ptr(self.a["v"]), N.ptr(self.a["rho"]),
+               N.ptr(cur["sid"]), N.ptr(cur["uid"]), self.N, N.ptr(t_row0), N.ptr(t_rows), self.S, N.ptr(out[0]),
+               N.ptr(out[1]), N.ptr(out[2]), 1, st)
+        if (wrow0 >= 0).any():
+            N.call("sph_arena_extract_many", None, None, None, N.ptr(self.ws_w["sid"]), None, self.WC, N.ptr(t_wrow0),
+                   N.ptr(t_rows), self.S, None, None, None, 1, st)
+            self._walls_dirty = True
+        for sl in slots:
+            d = self.slots.pop(sl)
+            self.walls_n -= d["nb"]
+            self.live_n -= d["n"]
+            bisect.insort(self.free_slots, sl)
+        self._specs = None
+        return rows, out
+
     def step(self):
         self._walls_ready()
         super().step()
@@ -1103,30 +1185,41 @@ class Server:
         self.rebuild_seconds += time.perf_counter() - t
 
     def _admit_pooled(self, queue, now):
-        if not queue or queue[0].arrival > now:
-            return False
+        """Admit the requests staged one step ago, then stage the ones that have arrived: their
+        upload and grid launch are queued now and finished at the next step, so the host
+        never waits for the step in flight."""
+        t = time.perf_counter()
+        admitted_any = False
+        staged, self._staged = self._staged, []
+        for pending, reqs in staged:
+            if pending is not None:
+                pending.finish()
+            self._admit_staged(reqs, queue, now)
+            admitted_any = True
         arrived = []
         used = self._used_bytes
         while queue and queue[0].arrival <= now:
             need = estimate_bytes(queue[0].spec.scene, self.pairs)
-            if used + need > self.budget and (self.live or arrived):
+            if used + need > self.budget and (self.live or arrived or staged):
                 break
             arrived.append(queue.pop(0))
             used += need
-        if not arrived:
-            return False
-        t = time.perf_counter()
-        for r in arrived:
-            if self.tuning is not None:
-                self.tuning.configure(r.spec)
-            r.spec.tpp = self._tpp
-        upload_scenes([r.spec for r in arrived], self.device)   # one upload and grid launch
+        if arrived:
+            for r in arrived:
+                if self.tuning is not None:
+                    self.tuning.configure(r.spec)
+                r.spec.tpp = self._tpp
+            self._used_bytes = used
+            # one upload and grid launch for all of them, finished at the next step
+            self._staged.append((upload_scenes([r.spec for r in arrived], self.device, wait=False), arrived))
+        self.admit_seconds += time.perf_counter() - t
+        return admitted_any
 
+    def _admit_staged(self, arrived, queue, now):
         def admitted(r, slot):
             r.slot = slot
             r.admitted = now
             self.live.append(r)
-            self._used_bytes += estimate_bytes(r.spec.scene, self.pairs)
 
         # all behind the occupied slots at once when they fit, else one by one (gaps, packing)
         # and a larger arena when those run out
@@ -1134,23 +1227,40 @@ class Server:
         if slots is not None:
             for r, slot in zip(arrived, slots):
                 admitted(r, slot)
-        else:
-            for k, r in enumerate(arrived):
-                try:
-                    if self.arena is None:
-                        raise ArenaFull("no arena yet")
-                    admitted(r, self.arena.admit(r.spec))
-                except ArenaFull:
-                    self._grow([q.spec for q in arrived[k:]], queue)   # moves the live scenes over
-                    rest = arrived[k:]
-                    slots = self.arena.admit_many([q.spec for q in rest])
-                    if slots is None:
-                        slots = [self.arena.admit(q.spec) for q in rest]
-                    for q, slot in zip(rest, slots):
-                        admitted(q, slot)
-                    break
-        self.admit_seconds += time.perf_counter() - t
-        return True
+            return
+        for k, r in enumerate(arrived):
+            try:
+                if self.arena is None:
+                    raise ArenaFull("no arena yet")
+                admitted(r, self.arena.admit(r.spec))
+            except ArenaFull:
+                self._grow([q.spec for q in arrived[k:]], queue)   # moves the live scenes over
+                rest = arrived[k:]
+                slots = self.arena.admit_many([q.spec for q in rest])
+                if slots is None:
+                    slots = [self.arena.admit(q.spec) for q in rest]
+                for q, slot in zip(rest, slots):
+                    admitted(q, slot)
+                return
+
+    def _retire_pooled_many(self, reqs, now):
+        """The requests that completed this step, retired together (one extract pass; with
+        keep_final one pinned block and one copy per field for all their final states)."""
+        rows, out = self.arena.retire_many([r.slot for r in reqs])
+        host = None
+        if self.keep_final:
+            host = [self._pinned.take(t.shape, t.dtype) for t in out]
+            for h, t in zip(host, out):
+                h.copy_(t, non_blocking=True)
+        for r in reqs:
+            self._used_bytes -= estimate_bytes(r.spec.scene, self.pairs)
+            r.finished = now
+            if host is not None:
+                a, n = rows[r.slot]
+                r.final = {"x": host[0][a:a + n], "v": host[1][a:a + n], "rho": host[2][a:a + n]}
+            r.spec.dev = None
+        gone = {id(r) for r in reqs}
+        self.live = [r for r in self.live if id(r) not in gone]
 
     def _retire_pooled(self, r, now, error=None):
         st = self.arena.retire(r.slot)
@@ -1173,11 +1283,12 @@ class Server:
         self.admit_seconds = 0.0
         self._pinned = _PinnedPool()
         self._used_bytes = 0
+        self._staged = []             # (pending upload, requests) admitted at the next step
         flags = torch.zeros(2, dtype=torch.int32, pin_memory=True)
         done = [None, None]          # event after each of the last two steps' status copies
         timed = []                   # (start event, end event, live scenes) per step
         k = 0
-        while queue or self.live:
+        while queue or self.live or self._staged:
             now = time.perf_counter() - t0
             if now > max_wall:
                 break
@@ -1185,7 +1296,7 @@ class Server:
             e0.record()
             self._admit_pooled(queue, now)
             if not self.live:
-                if queue:
+                if queue and not self._staged:
                     time.sleep(max(0.0, min(queue[0].arrival - (time.perf_counter() - t0), 0.01)))
                 continue
             a = self.arena
@@ -1208,8 +1319,9 @@ class Server:
             self.particle_steps += n_live
             self.batch_steps += 1
             now = time.perf_counter() - t0
-            for r in [r for r in self.live if r.steps_done >= r.spec.steps]:
-                self._retire_pooled(r, now)
+            finished = [r for r in self.live if r.steps_done >= r.spec.steps]
+            if finished:
+                self._retire_pooled_many(finished, now)
             # the previous step's status (its work is done once this step has been queued)
             prev = done[(k - 1) % 2] if k else None
             if prev is not None:

@@ -119,3 +119,27 @@ def test_admit_many_equals_one_by_one(cuda):
         assert same(a1.scene_state(p), a2.scene_state(q))
     small = arena(cuda, particles=6000)
     assert small.admit_many([A, B, C]) is None and not small.slots and small.occupied == 0
+
+
+def test_retire_many_equals_retire(cuda):
+    """Retiring several scenes in one pass gives each its state in its own particle order, as
+    retire() does, and frees their particles, walls and slots; the scene left behind is
+    unaffected."""
+    A, B, C = spec("dam_break", 2600, 1.1), spec("drop", 2300, 0.9), spec("dam_break", 2900, 1.4)
+    a1, a2 = arena(cuda), arena(cuda)
+    s1 = [a1.admit(x) for x in (A, B, C)]
+    s2 = [a2.admit(x) for x in (A, B, C)]
+    stepper(a1)(3)
+    stepper(a2)(3)
+    one = {sl: {k: v.cpu().numpy() for k, v in a1.retire(sl).items()} for sl in (s1[0], s1[2])}
+    rows, out = a2.retire_many([s2[0], s2[2]])
+    for sl1, sl2 in ((s1[0], s2[0]), (s1[2], s2[2])):
+        r0, n = rows[sl2]
+        got = {"x": out[0][r0:r0 + n].cpu().numpy(), "v": out[1][r0:r0 + n].cpu().numpy(),
+               "rho": out[2][r0:r0 + n].cpu().numpy()}
+        assert same(got, one[sl1])
+    assert sorted(a2.slots) == [s2[1]] and a2.live_n == a1.live_n and a2.walls_n == a1.walls_n
+    stepper(a1)(2)
+    stepper(a2)(2)
+    a2.check()
+    assert same(a1.scene_state(s1[1]), a2.scene_state(s2[1]))
