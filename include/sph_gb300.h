@@ -762,7 +762,8 @@ sph_status_t sph_dfsph_solve(const sph_fluid_view* fluid, const sph_wall_view* w
                              const sph_params* params, const sph_dfsph_buffers* bufs, const float* acc_in,
                              const float* dt, int32_t density, int32_t* status, void* stream);
 /* DFSPH steps 11-12 (src/dfsph.py:187-194): acc += artificial viscosity (with walls) +
- * laminar viscosity, with V = A / fluid-only density and rho incl. walls. */
+ * laminar viscosity, with V = A / fluid-only density and rho incl. walls.  Uses
+ * bufs->records as scratch for its pair records. */
 sph_status_t sph_dfsph_viscosity(const sph_fluid_view* fluid, const sph_wall_view* walls, const sph_grid* grid,
                                  const sph_params* params, const sph_dfsph_buffers* bufs, float* acc, void* stream);
 /* a += b (float2 [n]); a = (x, y) (float2 [n]). */

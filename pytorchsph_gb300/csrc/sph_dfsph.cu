@@ -128,13 +128,44 @@ __global__ void __launch_bounds__(128) k_wall_wall_term(WallView W, const sph_gr
 }
 
 // ---------------------------------------------------------------- solver set-up
-__global__ void k_dfsph_vstar(int n, const float2* __restrict__ v, const float2* __restrict__ acc,
-                              const float* __restrict__ dt_ptr, float2* __restrict__ vstar) {
+// The spiky gradient of pair (i, j) as gs * d with d = x_i - x_j: spikyGrad = e kGS(q), e =
+// d / r, so gs = kGS(q) / r, from one reciprocal square root (0 when r < 1e-7, where the
+// reference's e is zero).
+__device__ __forceinline__ float spiky_gd(float r2, const SphParams& P) {
+  if (!(r2 >= 1e-14f)) return 0.f;
+  const float rs = rsqrt_normal(r2);
+  return kGS(r2 * rs * P.inv_h, P.c_s) * rs;
+}
+
+// The Wendland gradient the same way: gradW = e kGW(q) = gw * d.
+__device__ __forceinline__ float wendland_gd(float r2, const SphParams& P) {
+  if (!(r2 >= 1e-14f)) return 0.f;
+  const float rs = rsqrt_normal(r2);
+  return kGW(r2 * rs * P.inv_h, P.c_g) * rs;
+}
+
+// v* = v + dt a, and the pair records of the preparation pass: rec_a = (x, y, v*),
+// rec_p = (A_act, A_act^2 / (A rho0)) (both rewritten by the solve before it reads them).
+__global__ void k_dfsph_vstar(FluidView F, SphParams P, DfsphBufs B, const float2* __restrict__ acc,
+                              const float* __restrict__ dt_ptr) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
+  if (i >= F.n) return;
   const float dt = *dt_ptr;
-  const float2 a = acc[i], u = v[i];
-  vstar[i] = make_float2(u.x + dt * a.x, u.y + dt * a.y);
+  const float2 a = acc[i], u = F.v[i], x = F.x[i];
+  const float2 vs = make_float2(u.x + dt * a.x, u.y + dt * a.y);
+  B.vstar[i] = vs;
+  B.rec_a[i] = make_float4(x.x, x.y, vs.x, vs.y);
+  const float aa = B.aact[i];
+  B.rec_p[i] = make_float4(aa, aa * aa / (F.area[i] * P.rho0), 0.f, 0.f);
+}
+
+// The pair records of the viscosity pass: rec_a = (x, y, v), rec_p = (V, rho rho0).
+__global__ void k_dfsph_visc_records(FluidView F, SphParams P, DfsphBufs B) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= F.n) return;
+  const float2 x = F.x[i], u = F.v[i];
+  B.rec_a[i] = make_float4(x.x, x.y, u.x, u.y);
+  B.rec_p[i] = make_float4(B.vol[i], B.rho[i] * P.rho0, 0.f, 0.f);
 }
 
 // alpha (dfsph.py:58-83 + solidBoundary.py:443-479) and source (dfsph.py:85-100, 154-161 +
@@ -145,21 +176,23 @@ __global__ void __launch_bounds__(128) k_dfsph_prepare(FluidView F, WallView W, 
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= F.n) return;
   const float dt = *dt_ptr;
-  const float2 xi = F.x[i];
-  const float2 vi = B.vstar[i];
+  const float4 me = B.rec_a[i];
+  const float2 xi = make_float2(me.x, me.y);
+  const float2 vi = make_float2(me.z, me.w);
   float k1x = 0.f, k1y = 0.f, k2 = 0.f, src = 0.f;
   const int k0 = F.offsets[i], kn = row_end(F, i, k0);
   for (int k = k0; k < kn; ++k) {
     const int j = __ldg(F.cols + k);
-    const float2 xj = __ldg(F.x + j), vj = __ldg(B.vstar + j);
-    const float aj = __ldg(B.aact + j), Aj = __ldg(F.area + j);
-    const Geo e = geo(xi.x, xi.y, xj.x, xj.y, P.inv_h);
-    const float gs = kGS(e.q, P.c_s);
-    const float gx = gs * e.ex, gy = gs * e.ey;
+    const float4 rj = __ldg(B.rec_a + j);
+    const float2 qj = __ldg(reinterpret_cast<const float2*>(B.rec_p + j));   // (A_act, A_act^2 / m)
+    const float dx = xi.x - rj.x, dy = xi.y - rj.y;
+    const float gd = spiky_gd(dx * dx + dy * dy, P);
+    const float gx = gd * dx, gy = gd * dy;
+    const float aj = qj.x;
     k1x += aj * gx;
     k1y += aj * gy;
-    k2 += (aj * aj / (Aj * P.rho0)) * (gx * gx + gy * gy);
-    src += -dt * aj * ((vi.x - vj.x) * gx + (vi.y - vj.y) * gy);
+    k2 += qj.y * (gx * gx + gy * gy);
+    src += -dt * aj * ((vi.x - rj.z) * gx + (vi.y - rj.w) * gy);
   }
   float w1x = 0.f, w1y = 0.f, w2 = 0.f, wsrc = 0.f;
   if (density && W.n > 0) {
@@ -230,14 +263,6 @@ __global__ void __launch_bounds__(128) k_dfsph_wall_prepare(FluidView F, WallVie
 }
 
 // ---------------------------------------------------------------- solver phases
-// The spiky gradient of pair (i, j) as gs * d with d = x_i - x_j: spikyGrad = e kGS(q), e =
-// d / r, so gs = kGS(q) / r, from one reciprocal square root (0 when r < 1e-7, where the
-// reference's e is zero).
-__device__ __forceinline__ float spiky_gd(float r2, const SphParams& P) {
-  if (!(r2 >= 1e-14f)) return 0.f;
-  const float rs = rsqrt_normal(r2);
-  return kGS(r2 * rs * P.inv_h, P.c_s) * rs;
-}
 
 // predicted pressure acceleration of fluid particle i (dfsph.py:25-42 + solidBoundary.py:310-403),
 // the fluid pairs from the records rec_p = (x, y, m, p / rho^2)
@@ -409,19 +434,23 @@ __global__ void __launch_bounds__(128) k_dfsph_viscosity(FluidView F, WallView W
                                                          SphParams P, DfsphBufs B, float2* __restrict__ acc) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= F.n) return;
-  const float2 xi = F.x[i], vi = F.v[i];
+  const float4 me = B.rec_a[i];
+  const float2 xi = make_float2(me.x, me.y), vi = make_float2(me.z, me.w);
   const float rhoi = B.rho[i] * P.rho0;
   float vax = 0.f, vay = 0.f, lax = 0.f, lay = 0.f;
   const int k0 = F.offsets[i], kn = row_end(F, i, k0);
   for (int k = k0; k < kn; ++k) {
     const int j = __ldg(F.cols + k);
-    const float2 xj = __ldg(F.x + j), vj = __ldg(F.v + j);
-    const float Vj = __ldg(B.vol + j), rhoj = __ldg(B.rho + j) * P.rho0;
-    const Geo e = geo(xi.x, xi.y, xj.x, xj.y, P.inv_h);
-    const float gw = kGW(e.q, P.c_g);
-    const float gx = gw * e.ex, gy = gw * e.ey;
+    const float4 rj = __ldg(B.rec_a + j);
+    const float2 qj = __ldg(reinterpret_cast<const float2*>(B.rec_p + j));   // (V, rho rho0)
+    const float2 vj = make_float2(rj.z, rj.w);
+    const float Vj = qj.x, rhoj = qj.y;
+    const float dx = xi.x - rj.x, dy = xi.y - rj.y;
+    const float d2 = dx * dx + dy * dy;
+    const float gd = wendland_gd(d2, P);
+    const float gx = gd * dx, gy = gd * dy;
     const float ux = vj.x - vi.x, uy = vj.y - vi.y;
-    const float rx = -e.dx, ry = -e.dy;
+    const float rx = -dx, ry = -dy;
     const float r2 = rx * rx + ry * ry + P.eps;
     const float pij = fminf(ux * rx + uy * ry, 0.f) / r2;
     const float vf = pij * Vj * rhoj / (rhoi + rhoj);
@@ -608,7 +637,7 @@ sph_status_t sph_dfsph_solve(const sph_fluid_view* fluid, const sph_wall_view* w
   WallView W = to_walls(walls);
   SphParams P = to_params(params);
   DfsphBufs B = to_bufs(bufs, n);
-  k_dfsph_vstar<<<grid_for(n, 256), 256, 0, st>>>(n, F.v, reinterpret_cast<const float2*>(acc_in), dt, B.vstar);
+  k_dfsph_vstar<<<grid_for(n, 256), 256, 0, st>>>(F, P, B, reinterpret_cast<const float2*>(acc_in), dt);
   k_dfsph_prepare<<<grid_for(n, 128), 128, 0, st>>>(F, W, grid, P, B, dt, density);
   if (density && W.n > 0) k_dfsph_wall_prepare<<<grid_for(W.n, 128), 128, 0, st>>>(F, W, grid, P, B, dt);
   SPH_CHECK_LAUNCH("dfsph_solve(prepare)");
@@ -657,8 +686,15 @@ sph_status_t sph_dfsph_viscosity(const sph_fluid_view* fluid, const sph_wall_vie
   SPH_VIEW_CHECK(walls);
   SPH_REQUIRE(grid && params && bufs && acc, "dfsph_viscosity: bad arguments");
   if (fluid->n == 0) return SPH_OK;
-  k_dfsph_viscosity<<<grid_for(fluid->n, 128), 128, 0, as_stream(stream)>>>(
-      to_fluid(fluid), to_walls(walls), grid, to_params(params), to_bufs(bufs), reinterpret_cast<float2*>(acc));
+  SPH_REQUIRE(bufs->records && (reinterpret_cast<uintptr_t>(bufs->records) & 15) == 0,
+              "dfsph_viscosity: records must be a 16-byte aligned array of 9 n floats");
+  const FluidView F = to_fluid(fluid);
+  const SphParams P = to_params(params);
+  const DfsphBufs B = to_bufs(bufs, fluid->n);
+  cudaStream_t st = as_stream(stream);
+  k_dfsph_visc_records<<<grid_for(fluid->n, 256), 256, 0, st>>>(F, P, B);
+  k_dfsph_viscosity<<<grid_for(fluid->n, 128), 128, 0, st>>>(F, to_walls(walls), grid, P, B,
+                                                             reinterpret_cast<float2*>(acc));
   SPH_CHECK_LAUNCH("dfsph_viscosity");
   return SPH_OK;
 }
