@@ -573,7 +573,7 @@ __device__ __forceinline__ void batch_update(int i, const FluidView& F, float ax
 // segment lists; kTpp lanes per particle (kCells only).  With kTpp > 1 no lane leaves
 // before the lane sums: lanes past p_hi take part with nothing to add.
 template <bool kCells, int kTpp, int kScheme>
-__global__ void __launch_bounds__(128, 8) k_batch_pass1(FluidView F, const Rec* __restrict__ rec, WallView W,
+__global__ void __launch_bounds__(128, 9) k_batch_pass1(FluidView F, const Rec* __restrict__ rec, WallView W,
                                                      const SceneDev* __restrict__ scenes,
                                                      const int32_t* __restrict__ sid, float* __restrict__ dpdt,
                                                      float2* __restrict__ acc, float2* __restrict__ grad_rho,
