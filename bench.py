@@ -876,10 +876,11 @@ def cpu_autograd_drop(sc, dt, steps):
 
 
 def run_diff_drop(args, dev, world, rank):
-    """Differentiable drop: 16,384-particle disc, 200 float64 steps, loss against a target
-    rollout (A = 1.0, alpha = 0.02) from A = 0.8, alpha = 0.01; gradient with respect to v0 and
-    alpha by the GPU adjoint with checkpoints every 20 steps, checked against central finite
-    differences (float64, eps 1e-4) on 64 seeded velocity components and on alpha."""
+    """Differentiable drop (config 5): 16,384-particle disc, 200-step rollout in float32
+    forward and adjoint, loss against a target rollout (A = 1.0, alpha = 0.02) from A = 0.8,
+    alpha = 0.01; gradient with respect to v0 and alpha by the GPU adjoint with checkpoints
+    every 20 steps, checked against float64 central finite differences (eps 1e-4) on 64
+    seeded velocity components and on alpha.  The float64 rollout's time is reported beside."""
     import torch
     from pytorchsph_gb300 import workloads
     from pytorchsph_gb300.adjoint import DropRollout
@@ -887,9 +888,10 @@ def run_diff_drop(args, dev, world, rank):
     start = workloads.oscillating_drop(16384, 0.5, 0.8)
     tgt = workloads.oscillating_drop(16384, 0.5, 1.0)
     dt = 0.1 * start["h"] / 10.0
-    r = DropRollout(start, 10.0, dt, checkpoint_every=20, device=dev)
-    target, _ = r.rollout(torch.as_tensor(tgt["vel"], dtype=torch.float64, device=dev), 0.02, steps)
-    v0 = torch.as_tensor(start["vel"], dtype=torch.float64, device=dev)
+    r64 = DropRollout(start, 10.0, dt, fp64=True, checkpoint_every=20, device=dev)
+    r = DropRollout(start, 10.0, dt, fp64=False, checkpoint_every=20, device=dev)
+    target, _ = r64.rollout(torch.as_tensor(tgt["vel"], dtype=torch.float64, device=dev), 0.02, steps)
+    v0 = torch.as_tensor(start["vel"], dtype=torch.float32, device=dev)
     for _ in range(max(args.warmup, 3)):
         r.loss_and_grad(v0, 0.01, target, steps)
     torch.cuda.synchronize()
@@ -907,19 +909,25 @@ def run_diff_drop(args, dev, world, rank):
     r.loss(v0, 0.01, target, steps)
     torch.cuda.synchronize()
     fwd_ms = (time.perf_counter() - t0) * 1e3
-    # finite differences
+    v64 = v0.double()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    r64.loss_and_grad(v64, 0.01, target, steps)
+    torch.cuda.synchronize()
+    f64_ms = (time.perf_counter() - t0) * 1e3
+    # float64 central finite differences
     rng = np.random.default_rng(0)
-    idx = rng.choice(v0.numel(), 64, replace=False)
+    idx = rng.choice(v64.numel(), 64, replace=False)
     eps = 1e-4
     fd, ad = [], []
     for k in idx:
-        e = torch.zeros(v0.numel(), dtype=torch.float64, device=dev)
+        e = torch.zeros(v64.numel(), dtype=torch.float64, device=dev)
         e[int(k)] = eps
-        e = e.reshape(v0.shape)
-        fd.append((r.loss(v0 + e, 0.01, target, steps) - r.loss(v0 - e, 0.01, target, steps)) / (2 * eps))
+        e = e.reshape(v64.shape)
+        fd.append((r64.loss(v64 + e, 0.01, target, steps) - r64.loss(v64 - e, 0.01, target, steps)) / (2 * eps))
         ad.append(float(gv.reshape(-1)[int(k)]))
     fd, ad = np.array(fd), np.array(ad)
-    fa = (r.loss(v0, 0.01 + eps, target, steps) - r.loss(v0, 0.01 - eps, target, steps)) / (2 * eps)
+    fa = (r64.loss(v64, 0.01 + eps, target, steps) - r64.loss(v64, 0.01 - eps, target, steps)) / (2 * eps)
     n = r.n
     value = n * steps * world / (ms / 1e3)
     cpu = None
@@ -934,10 +942,11 @@ def run_diff_drop(args, dev, world, rank):
     if rank == 0:
         line = base_line(args, world, value, ms, "particle-steps/s", {
             "workload": "diff_drop", "particles": n, "rollout_steps": steps, "checkpoint_every": 20,
-            "dtype": "f64", "loss": "mean |x_T - x*_T|^2", "target": "A = 1.0, alpha = 0.02",
+            "dtype": "f32", "loss": "mean |x_T - x*_T|^2", "target": "A = 1.0, alpha = 0.02",
             "start": "A = 0.8, alpha = 0.01", "dt": "0.1 h / c0", "density_diffusion": "MOG",
             "unit_of_work": "one forward + adjoint of the 200-step rollout per timed step"})
-        line["dtype"] = "f64"
+        line["dtype"] = "f32"
+        line["float64_forward_adjoint_ms"] = f64_ms
         line["gradient_check"] = {
             "components": 64, "eps": eps,
             "max_abs_err_over_max_fd": float(np.abs(ad - fd).max() / max(np.abs(fd).max(), 1e-300)),
@@ -946,9 +955,9 @@ def run_diff_drop(args, dev, world, rank):
             "loss": loss}
         line["forward_ms"] = fwd_ms
         peak, peak_src = hbm_peak()
-        line["roofline"] = {"bound": "hbm", "kernel": "k_drop_adjoint (float64)", "achieved": None, "peak": peak,
+        line["roofline"] = {"bound": "hbm", "kernel": "k_drop_adjoint (float32)", "achieved": None, "peak": peak,
                             "unit": "GB/s", "frac": None, "traffic": None, "peak_source": peak_src,
-                            "note": "the float64 dual-number pair products bound this kernel, not HBM"}
+                            "note": "the dual-number pair products bound this kernel, not HBM"}
         line["e2e"] = {"value": None, "unit": "particle-steps/s", "h2d_bytes_per_step": None,
                        "d2h_bytes_per_step": None}
         line["gpu_launches"] = None

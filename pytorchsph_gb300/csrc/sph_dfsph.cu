@@ -301,7 +301,7 @@ __device__ __forceinline__ float2 pressure_accel(const FluidView& F, const WallV
   return make_float2(ax, ay);
 }
 
-__global__ void __launch_bounds__(256, 8) k_dfsph_solve(FluidView F, WallView W, const sph_grid* __restrict__ gp,
+__global__ void __launch_bounds__(256, 4) k_dfsph_solve(FluidView F, WallView W, const sph_grid* __restrict__ gp,
                                                      SphParams P, DfsphBufs B, const float* __restrict__ dt_ptr,
                                                      int density, int min_iters, int max_iters, float thr_err,
                                                      float omega_f, float omega_b, int32_t* status) {

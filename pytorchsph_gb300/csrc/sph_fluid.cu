@@ -194,7 +194,8 @@ __device__ __forceinline__ void segments_body(int i, const FluidView& F, const s
       const int row = yy * g.cells_x;
       const int b = __ldg(cs + row + x0), e = __ldg(cs + row + x1 + 1);
       for (int c = b; c < e; c += 32) {
-        const uint32_t w = segment_mask(F.x, c, e, xi.x, xi.y, thr);
+        const uint32_t w = c + 32 <= F.n ? segment_mask_full(F.x, c, e, xi.x, xi.y, thr)
+                                         : segment_mask(F.x, c, e, xi.x, xi.y, thr);
         if (w == 0) continue;
         if (k < kMaxSegments) {
           seg_start[k * n + i] = c;

@@ -321,6 +321,26 @@ __device__ __forceinline__ uint32_t segment_mask(const float2* __restrict__ x, i
   return m;
 }
 
+// segment_mask when c + 32 <= n (the array's length): every candidate load is in bounds, so
+// all 32 candidates are tested without per-pair guards (all loads can be in flight
+// together) and the bits past the range are cleared; the bits inside it are segment_mask's.
+__device__ __forceinline__ uint32_t segment_mask_full(const float2* __restrict__ x, int c, int e, float xi,
+                                                      float yi, float thr) {
+  const int len = min(e - c, 32);
+  uint32_t m = 0;
+  const float2 qx = make_float2(xi, xi), qy = make_float2(yi, yi);
+#pragma unroll
+  for (int t = 0; t < 32; t += 2) {
+    const float2 a = __ldg(x + c + t), b = __ldg(x + c + t + 1);
+    const float2 dx = __fadd2_rn(qx, make_float2(-a.x, -b.x));
+    const float2 dy = __fadd2_rn(qy, make_float2(-a.y, -b.y));
+    const float2 v = __ffma2_rn(dx, dx, __fmul2_rn(dy, dy));
+    if (v.x <= thr) m |= 1u << t;
+    if (v.y <= thr) m |= 2u << t;
+  }
+  return len >= 32 ? m : m & ((1u << len) - 1u);
+}
+
 // The bits of a stored segment that name a particle: none for a start outside [0, n),
 // none at index n or past it.
 __device__ __forceinline__ uint32_t clip_segment(uint32_t w, int b, int n) {
