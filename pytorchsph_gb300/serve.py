@@ -139,12 +139,19 @@ def upload_scenes(specs, device, wait: bool = True):
               "nb": [len(sp.scene.get("wall_pos", ())) for sp in todo]}
     dev_fields = {}
     keep = []                     # pinned sources, alive until the copies have run
+    # a large upload (a burst of arrivals) goes from pageable memory: on this host a copy
+    # from pageable memory runs about as fast as from pinned memory, and page-locking a
+    # fresh buffer of hundreds of MB costs far more than the copy; small uploads use torch's
+    # cached pinned blocks and stay asynchronous
+    big = sum(counts["n"]) * 24 + sum(counts["nb"]) * 20 > (64 << 20)
     for name, key, width, cnt in _FIELDS:
         c = counts[cnt]
         total = sum(c)
         if total == 0:
             continue
-        host = torch.empty((total, width) if width > 1 else (total,), dtype=torch.float32, pin_memory=True)
+        shape = (total, width) if width > 1 else (total,)
+        host = torch.from_numpy(np.empty(shape, np.float32)) if big else torch.empty(shape, dtype=torch.float32,
+                                                                                       pin_memory=True)
         hv = host.numpy()
         o = 0
         for sp, k in zip(todo, c):
