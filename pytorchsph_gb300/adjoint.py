@@ -30,7 +30,8 @@ from .sim import SphParamsC
 class DropRollout:
     def __init__(self, scene: dict, c0: float, dt: float, kinematic: float = 0.001, delta: float = 0.1,
                  rest_density: float = 1000.0, gravity=(0.0, 0.0), point_source: bool = True,
-                 point_magnitude: float = 1.0, fp64: bool = True, checkpoint_every: int = 20, device=None):
+                 point_magnitude: float = 1.0, fp64: bool = True, checkpoint_every: int = 20, device=None,
+                 point_center=(0.0, 0.0)):
         self.dev = torch.device(device or torch.device("cuda", torch.cuda.current_device()))
         self.fp64 = bool(fp64)
         self.dtype = torch.float64 if fp64 else torch.float32
@@ -56,6 +57,7 @@ class DropRollout:
         P.gravity[0], P.gravity[1] = gravity
         P.point_source = int(point_source)
         P.point_magnitude = point_magnitude
+        P.point_center[0], P.point_center[1] = point_center
         P.density_diffusion = 1            # MOG
         self.search = GridSearch(self.dev)
         self.acc = torch.empty((self.n, 2), dtype=self.dtype, device=self.dev)

@@ -176,3 +176,29 @@ def test_float32_adjoint_at_drop_scale_matches_float64_differences(cuda):
     assert rel(ad, fd) < 1e-3, rel(ad, fd)
     fa = (r64.loss(v64, 0.01 + eps, target, steps) - r64.loss(v64, 0.01 - eps, target, steps)) / (2 * eps)
     assert abs(float(alpha.grad) - fa) <= 1e-3 * abs(fa), (float(alpha.grad), fa)
+
+
+def test_adjoint_matches_reference_finite_differences(cuda):
+    """The GPU adjoint (float64) against the reference's own gradient: central finite
+    differences (eps 1e-4) of the reference's forward rollout, 40 steps of a ~550-particle
+    drop moved into a 3 x 3 tank whose walls stay out of reach
+    (tests/golden/drop_fd_golden.npz, made by make_drop_fd_golden.py; the reference's step
+    does not run under torch autograd).  The GPU forward reproduces the reference's final
+    positions and loss, and its gradient the 16 velocity components and alpha."""
+    import os
+    from pytorchsph_gb300.adjoint import DropRollout
+    g = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "drop_fd_golden.npz"))
+    c, tank = float(g["center"]), float(g["tank"])
+    sc = {"pos": g["pos"], "rho": g["rho"], "area": g["area"], "support": g["support"],
+          "vmin": np.zeros(2, np.float32), "vmax": np.full(2, tank, np.float32)}
+    r = DropRollout(sc, 10.0, float(g["dt"]), fp64=True, checkpoint_every=10, device=cuda, point_center=(c, c))
+    steps = int(g["steps"])
+    v0 = torch.as_tensor(g["vel"], dtype=torch.float64, device=cuda)
+    target = torch.as_tensor(g["target"], dtype=torch.float64, device=cuda)
+    xT, _ = r.rollout(v0, 0.01, steps)
+    assert np.abs(xT.cpu().numpy() - g["x_final"]).max() < 1e-10
+    loss, gv, ga = r.loss_and_grad(v0, 0.01, target, steps)
+    assert abs(loss - float(g["loss"])) <= 1e-6 * float(g["loss"])
+    ad = gv.reshape(-1).cpu().numpy()[g["idx"]]
+    assert rel(ad, g["fd"]) < 1e-4, rel(ad, g["fd"])
+    assert abs(ga - float(g["fd_alpha"])) <= 1e-4 * abs(float(g["fd_alpha"])), (ga, float(g["fd_alpha"]))
