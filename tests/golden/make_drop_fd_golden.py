@@ -61,7 +61,9 @@ def rollout(sc, v0, alpha, dt):
     sim.simulationState = sim.setupSimulationState(sim.perennialState)
     for _ in range(STEPS):
         sim.integrate()
-    return sim.perennialState["fluidPosition"].detach().numpy().astype(np.float64)
+    # integrateValues (src/simulationBase.py:563-568) writes the new state into
+    # simulationState; perennialState keeps the state the step started from
+    return sim.simulationState["fluidPosition"].detach().numpy().astype(np.float64)
 
 
 def main():
