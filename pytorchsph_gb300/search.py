@@ -104,6 +104,8 @@ class CSRNeighbors:
     def to_original(self, field: torch.Tensor) -> torch.Tensor:
         """A sorted-order float32 field back in original particle order."""
         out = torch.empty(self.n, dtype=torch.float32, device=self.order.device)
+        if self.n == 0:
+            return out
         N.call("sph_scatter_f32", N.ptr(self.order), N.ptr(field), self.n, N.ptr(out), N.stream_ptr())
         return out
 
@@ -117,6 +119,10 @@ class CSRNeighbors:
         self.check()
         P = self.num_pairs
         dev = self.order.device
+        if self.n == 0:
+            return (torch.empty((2, 0), dtype=torch.int64, device=dev),
+                    torch.empty((0, 2), dtype=torch.float32, device=dev) if distances else None,
+                    torch.empty(0, dtype=torch.float32, device=dev) if distances else None)
         st = N.stream_ptr()
         cnt_orig = torch.empty(self.n, dtype=torch.int32, device=dev)
         N.call("sph_scatter_counts", N.ptr(self.order), N.ptr(self.counts), self.n, N.ptr(cnt_orig), st)
@@ -233,6 +239,15 @@ class GridSearch:
             raise N.SPHError("neighbor search: at most 2^31-2 particles")
         st = N.stream_ptr()
         ws = self.ws
+        if n == 0:   # no particles: an empty result (no grid to build)
+            dev = pos.device
+            i32 = lambda m: torch.zeros(m, dtype=torch.int32, device=dev)
+            f32 = lambda m: torch.zeros(m, dtype=torch.float32, device=dev)
+            return CSRNeighbors(n=0, order=i32(0), keys=i32(0), xy=f32(0).view(0, 2), sh=f32(0),
+                                sa=f32(0) if area is not None else None, cell_start=i32(2), counts=i32(0),
+                                offsets=i32(1), cols=i32(0), rho=f32(0) if density else None, grid=None,
+                                status=i32(1), cell_capacity=0, pair_capacity=0, kernel_support=kernel_support,
+                                search_radius=int(search_radius))
         if cell_capacity is None:
             cell_capacity = self.auto_cell_capacity(pos, support, min_coord, max_coord)
         cap = int(cell_capacity)

@@ -61,3 +61,9 @@ def test_degenerate_layouts_match_oracle(cuda, layout):
     rho = res.density().cpu().numpy()
     ref = ns.density(off, cols, pos, area, float(h), use_double=True)
     assert np.abs(rho - ref).max() <= 1e-5 * np.abs(ref).max()
+
+
+def test_no_particles_density(cuda):
+    pos = np.zeros((0, 2), np.float32)
+    res, _ = run(pos, np.zeros(0, np.float32), np.zeros(2, np.float32), np.ones(2, np.float32))
+    assert res.density().numel() == 0
