@@ -600,10 +600,13 @@ class SceneArena(SceneBatch):
     particle order and marks its particles and walls free.  The walls are sorted again once
     before the next step, however many scenes came or went.  Every scene runs with the arena's
     lanes per particle `tpp` and density-diffusion kernel `scheme` (-1: read per scene); pairs
-    come from the cell rows.  A scene gives the same bits in the arena as alone."""
+    come from the cell rows.  A step processes only the occupied slots rounded up to a
+    multiple of `extent_quantum` (by default the larger of 2^17 and a sixteenth of the
+    capacity), with a captured graph per extent, so an arena sized for a peak load steps a
+    light load at the light load's cost.  A scene gives the same bits in the arena as alone."""
 
     def __init__(self, device=None, particles: int = 1 << 20, walls: int = 1 << 16, cells: int = 1 << 20,
-                 slots: int = 256, tpp: int = 1, scheme: int = -1):
+                 slots: int = 256, tpp: int = 1, scheme: int = -1, extent_quantum: int | None = None):
         if tpp not in (1, 2, 4) or scheme not in (-1, 0, 1, 2):
             raise ValueError("tpp must be 1, 2 or 4 and scheme -1, 0, 1 or 2")
         self.pairs = "cells"
@@ -619,6 +622,8 @@ class SceneArena(SceneBatch):
         self.cap = self.C
         self.n = self.N
         n = self.N
+        self._quantum = int(extent_quantum) if extent_quantum else max(1 << 17, -(-self.N // 16))
+        self._graphs = {}
         f2 = lambda m: torch.zeros((m, 2), dtype=torch.float32, device=dev)
         f1 = lambda m: torch.zeros(m, dtype=torch.float32, device=dev)
         i1 = lambda m, v=0: torch.full((m,), v, dtype=torch.int32, device=dev)
@@ -777,6 +782,8 @@ class SceneArena(SceneBatch):
         self._write_scene(slot)
         st = N.stream_ptr()
         lo, hi = self.occupied, self.occupied + n
+        if hi > self.n:
+            self._set_extent(self._extent_for(hi))   # before the scene's slots are written
         cur = self._aux(self.par)
         as_dev = lambda t: torch.as_tensor(t, dtype=torch.float32, device=self.device)
         self.a["x"][lo:hi].copy_(as_dev(state["x"]).reshape(n, 2) if state else d["pos"])
@@ -823,6 +830,8 @@ class SceneArena(SceneBatch):
         if (len(self.free_slots) < len(specs) or self.occupied + n_tot > self.N or
                 self.walls_n + nb_tot > self.WC or self.C - self._cell_top < sum(cells)):
             return None
+        if self.occupied + n_tot > self.n:
+            self._set_extent(self._extent_for(self.occupied + n_tot))   # before any slot is written
         slots = self.free_slots[:len(specs)]
         del self.free_slots[:len(specs)]
         for sp, d, slot, nc in zip(specs, ds, slots, cells):
@@ -882,7 +891,7 @@ class SceneArena(SceneBatch):
                "v": torch.empty((n, 2), dtype=torch.float32, device=self.device),
                "rho": torch.empty(n, dtype=torch.float32, device=self.device)}
         N.call("sph_arena_extract", N.ptr(self.a["x"]), N.ptr(self.a["v"]), N.ptr(self.a["rho"]), N.ptr(cur["sid"]),
-               N.ptr(cur["uid"]), self.N, slot, N.ptr(out["x"]), N.ptr(out["v"]), N.ptr(out["rho"]), N.stream_ptr())
+               N.ptr(cur["uid"]), self.n, slot, N.ptr(out["x"]), N.ptr(out["v"]), N.ptr(out["rho"]), N.stream_ptr())
         return out
 
     def scene_state(self, slot):
@@ -897,7 +906,7 @@ class SceneArena(SceneBatch):
         out = self.scene_state_device(slot)
         d = self.slots.pop(slot)
         st = N.stream_ptr()
-        N.call("sph_arena_retire", N.ptr(self._aux(self.par)["sid"]), self.N, slot, st)
+        N.call("sph_arena_retire", N.ptr(self._aux(self.par)["sid"]), self.n, slot, st)
         if d["nb"]:
             N.call("sph_arena_retire", N.ptr(self.ws_w["sid"]), self.WC, slot, st)
             self.walls_n -= d["nb"]
@@ -923,6 +932,39 @@ class SceneArena(SceneBatch):
         if self._walls_dirty:
             self._sort_walls()
             self._walls_dirty = False
+
+    # ------------------------------------------------------------------ active extent
+    # A step processes the slots [0, n) only, n the occupied slots rounded up to a multiple of
+    # the extent quantum: the sort keeps the live scenes in front, so free capacity behind the
+    # extent costs nothing.  Each extent has its own pair of captured graphs (cached).  Slots
+    # that join the extent are first marked free in both copies of the static arrays (stale
+    # scene indices may linger there from an earlier, larger extent); nothing reads a slot
+    # outside the extent.
+    def _extent_for(self, occupied: int) -> int:
+        q = self._quantum
+        return min(self.N, max(q, -(-occupied // q) * q))
+
+    def _set_extent(self, n: int):
+        if n == self.n:
+            return
+        if n > self.n:
+            for which in (0, 1):
+                self._aux(which)["sid"][self.n:n].fill_(-1)
+        self.n = n
+        self.groups = [[0, n, self.tpp, self.scheme]]
+        self._groups_c = (ForceGroupC * 1)(ForceGroupC(0, n, self.tpp, self.scheme))
+        self.graph = self._graphs.get(n)
+
+    def _capture_extent(self):
+        """Both parities' graphs of a step over the current extent (capturing runs nothing)."""
+        graphs = [None, None]
+        for _ in range(2):
+            p = self.par
+            graphs[p] = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(graphs[p]):
+                self.step_kernels()
+        self.graph = graphs
+        self._graphs[self.n] = graphs
 
     def retire_many(self, slots):
         """retire() for several scenes at once: one pass over the particle slots extracts their
@@ -950,7 +992,7 @@ class SceneArena(SceneBatch):
         st = N.stream_ptr()
         cur = self._aux(self.par)
         N.call("sph_arena_extract_many", N.ptr(self.a["x"]), N.ptr(self.a["v"]), N.ptr(self.a["rho"]),
-               N.ptr(cur["sid"]), N.ptr(cur["uid"]), self.N, N.ptr(t_row0), N.ptr(t_rows), self.S, N.ptr(out[0]),
+               N.ptr(cur["sid"]), N.ptr(cur["uid"]), self.n, N.ptr(t_row0), N.ptr(t_rows), self.S, N.ptr(out[0]),
                N.ptr(out[1]), N.ptr(out[2]), 1, st)
         if (wrow0 >= 0).any():
             N.call("sph_arena_extract_many", None, None, None, N.ptr(self.ws_w["sid"]), None, self.WC, N.ptr(t_wrow0),
@@ -966,12 +1008,17 @@ class SceneArena(SceneBatch):
 
     def step(self):
         self._walls_ready()
+        self._set_extent(self._extent_for(self.occupied))   # shrinks after retirements
+        if self.graph is None and self._graphs:
+            self._capture_extent()     # a new extent of an arena already captured once
         super().step()
         self.occupied = self.live_n    # the sort moved every free slot behind the live scenes
 
     def capture(self):
         self._walls_ready()
+        self._set_extent(self._extent_for(self.occupied))
         super().capture()              # one step run eagerly, then the graphs recorded
+        self._graphs[self.n] = self.graph
         self.occupied = self.live_n
 
     def escaped(self):

@@ -143,3 +143,30 @@ def test_retire_many_equals_retire(cuda):
     stepper(a2)(2)
     a2.check()
     assert same(a1.scene_state(s1[1]), a2.scene_state(s2[1]))
+
+
+def test_extent_shrinks_and_grows_without_changing_results(cuda):
+    """With a small extent quantum the arena steps only its occupied slots: retiring scenes
+    shrinks the extent, admitting grows it again over slots that an earlier extent left
+    stale; every scene still equals the scene run alone."""
+    A, B, C = spec("dam_break", 3000, 1.2), spec("drop", 2600, 0.8), spec("dam_break", 4200, 1.5)
+    D, E = spec("drop", 2400, 1.4), spec("dam_break", 2800, 0.9)
+    a = arena(cuda, extent_quantum=2048)
+    go = stepper(a)
+    sa, sb, sc = a.admit(A), a.admit(B), a.admit(C)
+    go(2)
+    n_full = a.n
+    assert n_full == 10240 and len(a._graphs) == 1
+    final_b = {k: v.cpu().numpy() for k, v in a.retire(sb).items()}
+    final_c = {k: v.cpu().numpy() for k, v in a.retire(sc).items()}
+    go(2)                                  # A alone: the extent shrinks to 4096
+    assert a.n == 4096
+    sd, se = a.admit(D), a.admit(E)        # grows over slots that held B and C
+    go(3)
+    a.check()
+    assert a.n == 8192 and len(a._graphs) == 3   # extents 10240, 4096, 8192
+    assert same(run_batch([A], 7, cuda)[0], a.scene_state(sa))
+    assert same(run_batch([B], 2, cuda)[0], final_b)
+    assert same(run_batch([C], 2, cuda)[0], final_c)
+    assert same(run_batch([D], 3, cuda)[0], a.scene_state(sd))
+    assert same(run_batch([E], 3, cuda)[0], a.scene_state(se))
