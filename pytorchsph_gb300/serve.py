@@ -602,8 +602,9 @@ class SceneArena(SceneBatch):
     lanes per particle `tpp` and density-diffusion kernel `scheme` (-1: read per scene); pairs
     come from the cell rows.  A step processes only the occupied slots rounded up to a
     multiple of `extent_quantum` (by default the larger of 2^17 and a sixteenth of the
-    capacity), with a captured graph per extent, so an arena sized for a peak load steps a
-    light load at the light load's cost.  A scene gives the same bits in the arena as alone."""
+    capacity), and sorts into the cell slots up to the highest live scene's, rounded the same
+    way, with a captured graph per extent, so an arena sized for a peak load steps a light
+    load at the light load's cost.  A scene gives the same bits in the arena as alone."""
 
     def __init__(self, device=None, particles: int = 1 << 20, walls: int = 1 << 16, cells: int = 1 << 20,
                  slots: int = 256, tpp: int = 1, scheme: int = -1, extent_quantum: int | None = None):
@@ -623,6 +624,7 @@ class SceneArena(SceneBatch):
         self.n = self.N
         n = self.N
         self._quantum = int(extent_quantum) if extent_quantum else max(1 << 17, -(-self.N // 16))
+        self._cell_quantum = int(extent_quantum) if extent_quantum else max(1 << 17, -(-self.C // 16))
         self._graphs = {}
         f2 = lambda m: torch.zeros((m, 2), dtype=torch.float32, device=dev)
         f1 = lambda m: torch.zeros(m, dtype=torch.float32, device=dev)
@@ -944,16 +946,25 @@ class SceneArena(SceneBatch):
         q = self._quantum
         return min(self.N, max(q, -(-occupied // q) * q))
 
-    def _set_extent(self, n: int):
-        if n == self.n:
+    def _cell_extent(self) -> int:
+        """The cell slots a step sorts into: up to the end of the highest live cell range,
+        rounded up to the cell quantum (the sentinel cell of free slots sits right behind)."""
+        end = max((d["coff"] + d["ncells"] for d in self.slots.values()), default=0)
+        q = self._cell_quantum
+        return min(self.C, max(q, -(-end // q) * q))
+
+    def _set_extent(self, n: int, cap: int | None = None):
+        cap = self.cap if cap is None else cap
+        if n == self.n and cap == self.cap:
             return
         if n > self.n:
             for which in (0, 1):
                 self._aux(which)["sid"][self.n:n].fill_(-1)
         self.n = n
+        self.cap = cap   # the histogram past it is zero (every sort leaves it so) and unread
         self.groups = [[0, n, self.tpp, self.scheme]]
         self._groups_c = (ForceGroupC * 1)(ForceGroupC(0, n, self.tpp, self.scheme))
-        self.graph = self._graphs.get(n)
+        self.graph = self._graphs.get((n, cap))
 
     def _capture_extent(self):
         """Both parities' graphs of a step over the current extent (capturing runs nothing)."""
@@ -964,7 +975,7 @@ class SceneArena(SceneBatch):
             with torch.cuda.graph(graphs[p]):
                 self.step_kernels()
         self.graph = graphs
-        self._graphs[self.n] = graphs
+        self._graphs[(self.n, self.cap)] = graphs
 
     def retire_many(self, slots):
         """retire() for several scenes at once: one pass over the particle slots extracts their
@@ -1008,7 +1019,7 @@ class SceneArena(SceneBatch):
 
     def step(self):
         self._walls_ready()
-        self._set_extent(self._extent_for(self.occupied))   # shrinks after retirements
+        self._set_extent(self._extent_for(self.occupied), self._cell_extent())   # shrinks after retirements
         if self.graph is None and self._graphs:
             self._capture_extent()     # a new extent of an arena already captured once
         super().step()
@@ -1016,9 +1027,9 @@ class SceneArena(SceneBatch):
 
     def capture(self):
         self._walls_ready()
-        self._set_extent(self._extent_for(self.occupied))
+        self._set_extent(self._extent_for(self.occupied), self._cell_extent())
         super().capture()              # one step run eagerly, then the graphs recorded
-        self._graphs[self.n] = self.graph
+        self._graphs[(self.n, self.cap)] = self.graph
         self.occupied = self.live_n
 
     def escaped(self):

@@ -155,8 +155,7 @@ def test_extent_shrinks_and_grows_without_changing_results(cuda):
     go = stepper(a)
     sa, sb, sc = a.admit(A), a.admit(B), a.admit(C)
     go(2)
-    n_full = a.n
-    assert n_full == 10240 and len(a._graphs) == 1
+    assert a.n == 10240 and len(a._graphs) == 1
     final_b = {k: v.cpu().numpy() for k, v in a.retire(sb).items()}
     final_c = {k: v.cpu().numpy() for k, v in a.retire(sc).items()}
     go(2)                                  # A alone: the extent shrinks to 4096
@@ -164,7 +163,7 @@ def test_extent_shrinks_and_grows_without_changing_results(cuda):
     sd, se = a.admit(D), a.admit(E)        # grows over slots that held B and C
     go(3)
     a.check()
-    assert a.n == 8192 and len(a._graphs) == 3   # extents 10240, 4096, 8192
+    assert a.n == 8192 and len(a._graphs) >= 3   # particle extents 10240, 4096, 8192
     assert same(run_batch([A], 7, cuda)[0], a.scene_state(sa))
     assert same(run_batch([B], 2, cuda)[0], final_b)
     assert same(run_batch([C], 2, cuda)[0], final_c)
