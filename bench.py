@@ -54,6 +54,8 @@ def parse():
     ap.add_argument("--sort", default="auto", choices=["auto", "counting", "radix"],
                     help="search workloads: auto = the autotuner's pick for this N")
     ap.add_argument("--digit-bits", type=int, default=8)
+    ap.add_argument("--cell-ratio", type=int, default=1,
+                    help="search workloads with --sort counting|radix: grid cells of h / cell_ratio")
     ap.add_argument("--requests", type=int, default=1024)
     ap.add_argument("--trace-steps", type=int, default=1000)
     ap.add_argument("--no-trace", action="store_true", help="serving: skip the e2e and real-time trace runs")
@@ -604,10 +606,12 @@ def run_search_density(args, dev, world, rank):
     tuned = None
     if args.sort == "auto":
         from pytorchsph_gb300.tune import Autotuner, Tuning
-        t = Tuning(search=Autotuner(dev).tune_search(sizes=(n,)))
+        t = Tuning(search=Autotuner(dev).tune_search(
+            data=(d_pos, d_h, d_a, dict(kernel_support=support, min_coord=vmin, max_coord=vmax))))
         tuned = t.search
-        args.sort, args.digit_bits = t.search_config(n)["sort"], t.search_config(n)["digit_bits"]
-    gs = GridSearch(dev, sort=args.sort, digit_bits=args.digit_bits)
+        cfg = t.search_config(n)
+        args.sort, args.digit_bits, args.cell_ratio = cfg["sort"], cfg["digit_bits"], cfg["cell_ratio"]
+    gs = GridSearch(dev, sort=args.sort, digit_bits=args.digit_bits, cell_ratio=args.cell_ratio)
     first = gs.run(d_pos, d_h, d_a, kernel_support=support, min_coord=vmin, max_coord=vmax)
     cells, P = first.cell_capacity, first.num_pairs
     pair_cap = int(P * 1.05) + 1024
@@ -714,7 +718,7 @@ def run_search_density(args, dev, world, rank):
         line = base_line(args, world, value, ms, "particles/s", {
             "workload": args.workload, "particles": n, "pairs": P, "cells": cells, "support": "3dx", "sort": args.sort,
             "digit_bits": args.digit_bits if args.sort == "radix" else None,
-            "sort_chosen_by": "autotuner (measured in this run)" if tuned else "command line",
+            "cell_ratio": args.cell_ratio, "sort_chosen_by": "autotuner (measured on this workload in this run)" if tuned else "command line",
             "l2": "flushed between timed steps (flush not timed)", "graph": "one CUDA graph per step",
             "parallelism": f"replicas{world}", "segments": S})
         line["phases_ms"] = {k: round(v, 5) for k, v in phases.items()}

@@ -41,16 +41,18 @@ typedef int32_t sph_status_t;
 
 /* Uniform search grid, the device-side form of what sortPositions computes
  * (src/modules/neighborSearch.py:30-55): cell size hmax, origin qmin,
- * cell (ix, iy) = ceil((x - qmin) / hmax), linear id ix + cells_x * iy. */
+ * cell (ix, iy) = ceil((x - qmin) / hmax), linear id ix + cells_x * iy.
+ * sph_grid_build_ratio makes cells of max(support) / ratio: hmax is then the cell size and
+ * threshold_support the largest support. */
 typedef struct sph_grid {
   float qmin[2];
   float hmax;
   float hmax_threshold;  /* set by sph_grid_build: the pair test's square-root-free threshold
-                            for support hmax (0 = not set) */
+                            for support threshold_support (0 = not set) */
   int32_t cells_x;
   int32_t cells_y;
   int32_t num_cells;
-  int32_t reserved2;
+  float threshold_support;  /* the support hmax_threshold belongs to (0: hmax) */
 } sph_grid;
 
 /* Physical and numerical parameters of the summations (one scene). */
@@ -170,6 +172,14 @@ size_t sph_grid_scratch_bytes(int64_t n);
 sph_status_t sph_grid_build(const float* pos, const float* support, int64_t n, const float* min_coord,
                             const float* max_coord, int32_t cell_capacity, sph_grid* grid,
                             int32_t* status, void* scratch, size_t scratch_bytes, void* stream);
+/* The grid of sph_grid_build (same qmin and the same padded extent) with cells of
+ * hmax / cell_ratio, 1 <= cell_ratio <= 8: searched cell_ratio cells out, it gives the
+ * same pair sets with fewer candidates per particle.  The pairs of a row come in the order
+ * of the finer cells.  No counterpart in the reference (its grid is the ratio-1 one). */
+sph_status_t sph_grid_build_ratio(const float* pos, const float* support, int64_t n, const float* min_coord,
+                                  const float* max_coord, int32_t cell_ratio, int32_t cell_capacity,
+                                  sph_grid* grid, int32_t* status, void* scratch, size_t scratch_bytes,
+                                  void* stream);
 /* keys[i] = linear cell id of pos[i] (the linearIndices of neighborSearch.py:46-47);
  * vals[i] = i when vals != NULL; cell_count[key] += 1 when cell_count != NULL (a zeroed
  * int32 [cell_capacity+1] histogram for sph_counting_sort).

@@ -36,6 +36,7 @@ SIGNATURES = {
     "sph_radix_sort_pairs": (_I32, [_P, _P, _I64, _I32, _I32, _P, _SZ, _P]),
     "sph_grid_scratch_bytes": (_SZ, [_I64]),
     "sph_grid_build": (_I32, [_P, _P, _I64, _P, _P, _I32, _P, _P, _P, _SZ, _P]),
+    "sph_grid_build_ratio": (_I32, [_P, _P, _I64, _P, _P, _I32, _I32, _P, _P, _P, _SZ, _P]),
     "sph_grid_build_segments": (_I32, [_P, _P, _P, _I32, _P, _P, _I32, _P, _P, _P]),
     "sph_cell_keys": (_I32, [_P, _I64, _P, _I32, _P, _P, _P, _P, _P]),
     "sph_counting_sort_scratch_bytes": (_SZ, [_I64, _I32]),

@@ -64,13 +64,13 @@ __global__ void __launch_bounds__(kRedThreads) k_bounds_partial(const float2* __
 }
 
 __device__ sph_grid make_grid(const Bounds& b, int has_min, float min_x, float min_y, int has_max, float max_x,
-                              float max_y, int32_t cell_capacity, int32_t* status);
+                              float max_y, int32_t cell_capacity, int32_t* status, int ratio);
 
 // Grid of sortPositions, src/modules/neighborSearch.py:34-46, all in float32:
 // qMin = minCoord - hMax*1.0, qMax = maxCoord + 2*hMax*1.0, cells = ceil((qMax-qMin)/hMax).
 __global__ void k_bounds_final(const Bounds* __restrict__ part, int nparts, int has_min, float min_x, float min_y,
                                int has_max, float max_x, float max_y, int32_t cell_capacity, sph_grid* grid,
-                               int32_t* status) {
+                               int32_t* status, int ratio) {
   __shared__ Bounds sb[32];
   Bounds b{-INFINITY, INFINITY, INFINITY, -INFINITY, -INFINITY, 0};
   for (int k = threadIdx.x; k < nparts; k += 32) {
@@ -93,26 +93,27 @@ __global__ void k_bounds_final(const Bounds* __restrict__ part, int nparts, int 
     b.mxy = fmaxf(b.mxy, sb[k].mxy);
     b.nonfinite |= sb[k].nonfinite;
   }
-  *grid = make_grid(b, has_min, min_x, min_y, has_max, max_x, max_y, cell_capacity, status);
+  *grid = make_grid(b, has_min, min_x, min_y, has_max, max_x, max_y, cell_capacity, status, ratio);
 }
 
 // The grid of one particle set from its bounds (thread-local).
 __device__ sph_grid make_grid(const Bounds& b, int has_min, float min_x, float min_y, int has_max, float max_x,
-                              float max_y, int32_t cell_capacity, int32_t* status) {
+                              float max_y, int32_t cell_capacity, int32_t* status, int ratio) {
   float hs = __fmul_rn(b.hmax, 1.0f);
   float two_hs = __fmul_rn(__fmul_rn(2.0f, b.hmax), 1.0f);
   float qmin_x = __fsub_rn(has_min ? min_x : b.mnx, hs);
   float qmin_y = __fsub_rn(has_min ? min_y : b.mny, hs);
   float qmax_x = __fadd_rn(has_max ? max_x : b.mxx, two_hs);
   float qmax_y = __fadd_rn(has_max ? max_y : b.mxy, two_hs);
-  float ex = __fdiv_rn(__fsub_rn(qmax_x, qmin_x), hs);
-  float ey = __fdiv_rn(__fsub_rn(qmax_y, qmin_y), hs);
+  const float cell = ratio > 1 ? __fdiv_rn(hs, (float)ratio) : hs;
+  float ex = __fdiv_rn(__fsub_rn(qmax_x, qmin_x), cell);
+  float ey = __fdiv_rn(__fsub_rn(qmax_y, qmin_y), cell);
   sph_grid g;
   g.qmin[0] = qmin_x;
   g.qmin[1] = qmin_y;
-  g.hmax = b.hmax;
+  g.hmax = cell;
   g.hmax_threshold = sq_threshold(b.hmax);
-  g.reserved2 = 0;
+  g.threshold_support = b.hmax;
   bool ok = b.nonfinite == 0 && b.hmax > 0.f && isfinite(ex) && isfinite(ey) && ex < 2.0e9f && ey < 2.0e9f;
   int cx = ok ? (int)ceilf(ex) : 0;
   int cy = ok ? (int)ceilf(ey) : 0;
@@ -175,7 +176,7 @@ __global__ void __launch_bounds__(kRedThreads) k_grid_segments(const float2* __r
   grids[s] = make_grid(b, min_coords != nullptr, min_coords ? min_coords[2 * s] : 0.f,
                        min_coords ? min_coords[2 * s + 1] : 0.f, max_coords != nullptr,
                        max_coords ? max_coords[2 * s] : 0.f, max_coords ? max_coords[2 * s + 1] : 0.f,
-                       cell_capacity, status);
+                       cell_capacity, status, 1);
 }
 
 // counter[key] += 1 for every lane, one atomic per distinct key of the warp: particles come
@@ -534,7 +535,15 @@ size_t sph_grid_scratch_bytes(int64_t) { return (size_t)(2 * kNumSMs) * sizeof(B
 sph_status_t sph_grid_build(const float* pos, const float* support, int64_t n, const float* min_coord,
                             const float* max_coord, int32_t cell_capacity, sph_grid* grid, int32_t* status,
                             void* scratch, size_t scratch_bytes, void* stream) {
-  SPH_REQUIRE(n > 0 && pos && support && grid && cell_capacity > 0 && cell_capacity < 0x7ffffffe,
+  return sph_grid_build_ratio(pos, support, n, min_coord, max_coord, 1, cell_capacity, grid, status, scratch,
+                              scratch_bytes, stream);
+}
+
+sph_status_t sph_grid_build_ratio(const float* pos, const float* support, int64_t n, const float* min_coord,
+                                  const float* max_coord, int32_t cell_ratio, int32_t cell_capacity, sph_grid* grid,
+                                  int32_t* status, void* scratch, size_t scratch_bytes, void* stream) {
+  SPH_REQUIRE(n > 0 && pos && support && grid && cell_capacity > 0 && cell_capacity < 0x7ffffffe &&
+                  cell_ratio >= 1 && cell_ratio <= 8,
               "grid_build: bad arguments");
   if (!scratch || scratch_bytes < sph_grid_scratch_bytes(n)) {
     set_error_text("grid_build: scratch too small");
@@ -547,7 +556,7 @@ sph_status_t sph_grid_build(const float* pos, const float* support, int64_t n, c
   k_bounds_final<<<1, 32, 0, st>>>(part, nparts, min_coord != nullptr, min_coord ? min_coord[0] : 0.f,
                                    min_coord ? min_coord[1] : 0.f, max_coord != nullptr,
                                    max_coord ? max_coord[0] : 0.f, max_coord ? max_coord[1] : 0.f, cell_capacity,
-                                   grid, status);
+                                   grid, status, (int)cell_ratio);
   SPH_CHECK_LAUNCH("grid_build");
   return SPH_OK;
 }

@@ -73,9 +73,11 @@ __host__ __device__ __forceinline__ float sq_threshold(float h) {
 }
 
 // sq_threshold(h) for a query of support h in grid g: the grid carries the value for its
-// cell size hmax (the common support), computed once by sph_grid_build.
+// largest support (threshold_support, or the cell size hmax when that is 0), computed once
+// by sph_grid_build.
 __device__ __forceinline__ float grid_threshold(float h, const sph_grid& g) {
-  return (h == g.hmax && g.hmax_threshold > 0.f) ? g.hmax_threshold : sq_threshold(h);
+  const float hs = g.threshold_support > 0.f ? g.threshold_support : g.hmax;
+  return (h == hs && g.hmax_threshold > 0.f) ? g.hmax_threshold : sq_threshold(h);
 }
 
 // Reference predicate with the distance: true iff sqrtf(fmaf(dx,dx,dy*dy)) < h_i.

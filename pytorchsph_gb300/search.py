@@ -175,9 +175,13 @@ class GridSearch:
     with `digit_bits` per pass); both give the (key, index) order of a stable sort.
     segments = True: the count pass keeps each particle's accepted candidates as bit masks
     and the fill expands them (one pair test per candidate instead of two); False: the fill
-    tests the candidates again.  Both give the same CSR."""
+    tests the candidates again.  Both give the same CSR.
+    cell_ratio > 1: grid cells of max(support) / cell_ratio, searched cell_ratio times
+    search_radius cells out; the same pair set from fewer candidates, each row's pairs in
+    the order of the finer cells."""
 
-    def __init__(self, device=None, sort: str = "counting", digit_bits: int = 8, segments: bool = True):
+    def __init__(self, device=None, sort: str = "counting", digit_bits: int = 8, segments: bool = True,
+                 cell_ratio: int = 1):
         if device is None:
             device = torch.device("cuda", torch.cuda.current_device())
         self.device = torch.device(device)
@@ -187,6 +191,9 @@ class GridSearch:
         self.sort = sort
         self.digit_bits = int(digit_bits)
         self.segments = bool(segments)
+        if not 1 <= int(cell_ratio) <= 8:
+            raise ValueError(cell_ratio)
+        self.cell_ratio = int(cell_ratio)
 
     def grid(self, pos, support, min_coord=None, max_coord=None, cell_capacity=MAX_CELLS):
         """Compute the search grid on the device; returns the device grid bytes."""
@@ -195,8 +202,9 @@ class GridSearch:
         grid = self.ws.get("grid", 8, torch.int32)
         status = self.ws.get("status", 1, torch.int32)
         scratch = self.ws.bytes("grid_scratch", lib.sph_grid_scratch_bytes(n))
-        N.call("sph_grid_build", N.ptr(pos), N.ptr(support), n, _f2(min_coord), _f2(max_coord), int(cell_capacity),
-               N.ptr(grid), N.ptr(status), N.ptr(scratch), scratch.numel() * 8, N.stream_ptr())
+        N.call("sph_grid_build_ratio", N.ptr(pos), N.ptr(support), n, _f2(min_coord), _f2(max_coord),
+               self.cell_ratio, int(cell_capacity), N.ptr(grid), N.ptr(status), N.ptr(scratch), scratch.numel() * 8,
+               N.stream_ptr())
         return grid
 
     def auto_cell_capacity(self, pos, support, min_coord=None, max_coord=None) -> int:
@@ -239,6 +247,7 @@ class GridSearch:
             raise N.SPHError("neighbor search: at most 2^31-2 particles")
         st = N.stream_ptr()
         ws = self.ws
+        search_radius = int(search_radius) * self.cell_ratio   # in cells of the (finer) grid
         if n == 0:   # no particles: an empty result (no grid to build)
             dev = pos.device
             i32 = lambda m: torch.zeros(m, dtype=torch.int32, device=dev)

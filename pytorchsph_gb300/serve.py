@@ -60,7 +60,7 @@ class ForceGroupC(ctypes.Structure):
 class _Grid(ctypes.Structure):
     _fields_ = [("qmin", ctypes.c_float * 2), ("hmax", ctypes.c_float), ("hmax_threshold", ctypes.c_float),
                 ("cells_x", ctypes.c_int32), ("cells_y", ctypes.c_int32), ("num_cells", ctypes.c_int32),
-                ("reserved2", ctypes.c_int32)]
+                ("threshold_support", ctypes.c_float)]
 
 
 @dataclass

@@ -8,7 +8,7 @@ Knobs:
     shuffles).  A scene's configuration depends only on its particle count, so a scene's
     result is the same alone and in any mix of scenes.
   * one-scene neighbor search (`GridSearch`): counting sort, or LSD radix sort and its
-    digit width.
+    digit width, and the cell size (cells of h or of h / 2; the same pair set either way).
 
 A bucket is floor(log2 N).  `Autotuner.tune_serving` times, for each bucket's size, a
 loaded batch (about `batch_particles` particles of scenes of that size, half dam breaks,
@@ -26,7 +26,8 @@ import numpy as np
 import torch
 
 SERVING_CANDIDATES = ((1, 1), (1, 2), (1, 4), (2, 1), (2, 2), (2, 4))   # (cell_ratio, tpp)
-SEARCH_CANDIDATES = (("counting", 0), ("radix", 4), ("radix", 6), ("radix", 8))
+SEARCH_CANDIDATES = (("counting", 0, 1), ("counting", 0, 2), ("radix", 4, 1), ("radix", 6, 1), ("radix", 8, 1),
+                     ("radix", 8, 2))   # (sort, digit bits, cell ratio)
 
 
 def bucket(n: int) -> int:
@@ -45,7 +46,7 @@ def _nearest(table: dict, n: int):
 class Tuning:
     """Chosen configuration per size bucket (and what each candidate measured)."""
     serving: dict = field(default_factory=dict)   # bucket -> {"cell_ratio", "tpp", "measured": {...}}
-    search: dict = field(default_factory=dict)    # bucket -> {"sort", "digit_bits", "measured": {...}}
+    search: dict = field(default_factory=dict)    # bucket -> {"sort", "digit_bits", "cell_ratio", "measured"}
     device: str = ""
 
     def scene_config(self, n: int) -> dict:
@@ -59,8 +60,9 @@ class Tuning:
 
     def search_config(self, n: int) -> dict:
         e = _nearest(self.search, n)
-        return {"sort": "counting", "digit_bits": 8} if e is None else {"sort": e["sort"],
-                                                                          "digit_bits": e["digit_bits"]}
+        if e is None:
+            return {"sort": "counting", "digit_bits": 8, "cell_ratio": 1}
+        return {"sort": e["sort"], "digit_bits": e["digit_bits"], "cell_ratio": int(e.get("cell_ratio", 1))}
 
     def to_json(self) -> dict:
         return {"device": self.device, "serving": {str(k): v for k, v in self.serving.items()},
@@ -140,22 +142,29 @@ class Autotuner:
             torch.cuda.empty_cache()
         return out
 
-    def tune_search(self, sizes=(1 << 16, 1 << 18, 1 << 20), steps: int = 5, candidates=SEARCH_CANDIDATES) -> dict:
-        """bucket -> the fastest sort for GridSearch.run (+ density) on a jittered lattice."""
+    def tune_search(self, sizes=(1 << 16, 1 << 18, 1 << 20), steps: int = 5, candidates=SEARCH_CANDIDATES,
+                    data=None) -> dict:
+        """bucket -> the fastest configuration of GridSearch.run (+ density) on a jittered
+        lattice of each size, or on `data` = (pos, support, area, run keywords) when given
+        (the caller's own particles: one bucket)."""
         from .search import GridSearch
         out = {}
-        for size in sizes:
-            side = int(round(math.sqrt(size)))
-            dx = 1.0 / side
-            g = torch.Generator().manual_seed(0)
-            ij = torch.stack(torch.meshgrid(torch.arange(side), torch.arange(side), indexing="ij"), -1).reshape(-1, 2)
-            pos = ((ij.float() + 0.5) * dx + (torch.rand(ij.shape, generator=g) - 0.5) * 0.2 * dx).to(self.device)
-            h = torch.full((pos.shape[0],), 3 * dx, dtype=torch.float32, device=self.device)
-            area = torch.full_like(h, dx * dx)
-            measured = {}
-            for sort, bits in candidates:
-                gs = GridSearch(self.device, sort=sort, digit_bits=bits or 8)
+        for size in (sizes if data is None else (int(data[0].shape[0]),)):
+            if data is None:
+                side = int(round(math.sqrt(size)))
+                dx = 1.0 / side
+                g = torch.Generator().manual_seed(0)
+                ij = torch.stack(torch.meshgrid(torch.arange(side), torch.arange(side), indexing="ij"),
+                                 -1).reshape(-1, 2)
+                pos = ((ij.float() + 0.5) * dx + (torch.rand(ij.shape, generator=g) - 0.5) * 0.2 * dx).to(self.device)
+                h = torch.full((pos.shape[0],), 3 * dx, dtype=torch.float32, device=self.device)
+                area = torch.full_like(h, dx * dx)
                 kw = dict(kernel_support=3 * dx, min_coord=(0.0, 0.0), max_coord=(1.0, 1.0))
+            else:
+                pos, h, area, kw = data
+            measured = {}
+            for sort, bits, ratio in candidates:
+                gs = GridSearch(self.device, sort=sort, digit_bits=bits or 8, cell_ratio=ratio)
                 res = gs.run(pos, h, area, **kw)
                 cap, pcap = res.cell_capacity, int(res.num_pairs * 1.05) + 1024
                 for _ in range(2):
@@ -168,11 +177,11 @@ class Autotuner:
                 en.record()
                 torch.cuda.synchronize()
                 ms = st.elapsed_time(en) / steps
-                measured[f"{sort},{bits}"] = {"ms": ms, "particles_per_s": pos.shape[0] / (ms / 1e3)}
+                measured[f"{sort},{bits},{ratio}"] = {"ms": ms, "particles_per_s": pos.shape[0] / (ms / 1e3)}
             best = min(measured, key=lambda k: measured[k]["ms"])
-            sort, bits = best.split(",")
+            sort, bits, ratio = best.split(",")
             out[bucket(size)] = {"size": int(pos.shape[0]), "sort": sort, "digit_bits": int(bits) or 8,
-                                 "measured": measured}
+                                 "cell_ratio": int(ratio), "measured": measured}
         return out
 
     def tune(self, serving_sizes=(2048, 8192, 32768, 131072), search_sizes=(1 << 16, 1 << 18, 1 << 20),

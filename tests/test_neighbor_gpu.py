@@ -28,19 +28,22 @@ def dom(g, c):
 def run_native(pos, h, area, support, vmin, vmax, **kw):
     from pytorchsph_gb300.search import GridSearch
     dev = torch.device("cuda")
-    gs = GridSearch(dev, **{k: v for k, v in kw.items() if k in ("digit_bits", "sort")})
+    gs = GridSearch(dev, **{k: v for k, v in kw.items() if k in ("digit_bits", "sort", "cell_ratio")})
     res = gs.run(torch.from_numpy(pos).to(dev), torch.from_numpy(h).to(dev), torch.from_numpy(area).to(dev),
                  kernel_support=float(support), min_coord=vmin, max_coord=vmax)
     return res
 
 
 @pytest.mark.parametrize("case", CASES)
-@pytest.mark.parametrize("sort,digit_bits", [("counting", 8), ("radix", 8), ("radix", 5)])
-def test_native_csr_pairs_bit_exact(cuda, golden, case, sort, digit_bits):
+@pytest.mark.parametrize("sort,digit_bits,cell_ratio", [("counting", 8, 1), ("radix", 8, 1), ("radix", 5, 1),
+                                                        ("counting", 8, 2), ("radix", 8, 3)])
+def test_native_csr_pairs_bit_exact(cuda, golden, case, sort, digit_bits, cell_ratio):
+    """The pair set of every golden case, for each sort and for grids of cells of h and of
+    h / 2, h / 3 (searched 2 and 3 cells out)."""
     g = golden
     vmin, vmax = dom(g, case)
     res = run_native(g[f"{case}/pos"], g[f"{case}/h"], g[f"{case}/area"], g[f"{case}/support"], vmin, vmax,
-                     digit_bits=digit_bits, sort=sort)
+                     digit_bits=digit_bits, sort=sort, cell_ratio=cell_ratio)
     pairs, dist, radial = res.to_coo()
     got = pairs_key(pairs[0].cpu().numpy(), pairs[1].cpu().numpy())
     assert np.array_equal(got, csr_key(g[f"{case}/offsets"], g[f"{case}/cols"]))
@@ -51,10 +54,12 @@ def test_native_csr_pairs_bit_exact(cuda, golden, case, sort, digit_bits):
 
 
 @pytest.mark.parametrize("case", ["lattice", "mix", "ties", "edges"])
-def test_fused_density_matches_reference(cuda, golden, case):
+@pytest.mark.parametrize("cell_ratio", [1, 2])
+def test_fused_density_matches_reference(cuda, golden, case, cell_ratio):
     g = golden
     vmin, vmax = dom(g, case)
-    res = run_native(g[f"{case}/pos"], g[f"{case}/h"], g[f"{case}/area"], g[f"{case}/support"], vmin, vmax)
+    res = run_native(g[f"{case}/pos"], g[f"{case}/h"], g[f"{case}/area"], g[f"{case}/support"], vmin, vmax,
+                     cell_ratio=cell_ratio)
     rho = res.density().cpu().numpy().astype(np.float64)
     ref64 = g[f"{case}/rho64"]
     ref32 = g[f"{case}/rho32"]
@@ -258,6 +263,31 @@ def test_segment_fill_equals_two_pass_fill(cuda):
     assert torch.equal(a.counts, b.counts) and torch.equal(a.offsets, b.offsets)
     assert torch.equal(a.cols[:a.num_pairs], b.cols[:b.num_pairs])
     assert torch.equal(a.rho, b.rho)
+
+
+@pytest.mark.parametrize("cell_ratio", [2, 3])
+def test_finer_cells_give_the_same_pairs(cuda, cell_ratio):
+    """Grids of cells of h / 2 and h / 3 (searched 2 and 3 cells out): the same (i, j) pair
+    list as cells of h, with ragged supports and a clustered blob; densities differ only by
+    summation order; the two-pass fill agrees."""
+    from pytorchsph_gb300.search import GridSearch
+    from pytorchsph_gb300 import workloads
+    dev = torch.device("cuda")
+    n = 40000
+    rng = np.random.default_rng(11)
+    pos = torch.from_numpy(workloads.gaussian_uniform_mix(n, 0.05, (0.5, 0.5), 9)).to(dev)
+    h = torch.from_numpy(rng.uniform(0.006, 0.012, n).astype(np.float32)).to(dev)
+    area = torch.full((n,), 1.0 / n, device=dev)
+    kw = dict(kernel_support=0.012, min_coord=[0, 0], max_coord=[1, 1])
+    a = GridSearch(dev).run(pos, h, area, **kw)
+    b = GridSearch(dev, cell_ratio=cell_ratio).run(pos, h, area, **kw)
+    c = GridSearch(dev, cell_ratio=cell_ratio, segments=False).run(pos, h, area, **kw)
+    pa, pb = a.to_coo(distances=False)[0], b.to_coo(distances=False)[0]
+    assert a.num_pairs == b.num_pairs and torch.equal(pa, pb)
+    assert torch.equal(b.counts, c.counts) and torch.equal(b.cols[:b.num_pairs], c.cols[:c.num_pairs])
+    assert torch.equal(b.rho, c.rho)
+    ra, rb = a.density(), b.density()   # float32 sums of up to ~300 terms in another order
+    assert float((ra - rb).abs().max()) <= 1e-5 * float(ra.abs().max())
 
 
 def _host_segments(res, n):

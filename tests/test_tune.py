@@ -13,9 +13,9 @@ def test_buckets_and_nearest_lookup():
     assert t.scene_config(10000) == {"cell_ratio": 2, "tpp": 4}     # bucket 13: 11 and 15 tie, lower wins
     assert t.scene_config(20000) == {"cell_ratio": 1, "tpp": 1}
     assert t.scene_config(10 ** 7) == {"cell_ratio": 1, "tpp": 1}
-    assert t.search_config(1 << 16) == {"sort": "radix", "digit_bits": 6}
+    assert t.search_config(1 << 16) == {"sort": "radix", "digit_bits": 6, "cell_ratio": 1}
     assert Tuning().scene_config(5000) == {"cell_ratio": 1, "tpp": 1}
-    assert Tuning().search_config(5000) == {"sort": "counting", "digit_bits": 8}
+    assert Tuning().search_config(5000) == {"sort": "counting", "digit_bits": 8, "cell_ratio": 1}
 
 
 def test_configure_sets_spec_fields_and_json_round_trip(tmp_path):
