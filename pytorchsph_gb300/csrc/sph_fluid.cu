@@ -311,17 +311,18 @@ __device__ __forceinline__ Pass1 pass1_body(int i, const FluidView& F, const Rec
     const float ir2 = rcp_normal(e.r2 + P.eps);
     const float rg = -e.gd * e.r2;                        // (x_j - x_i) . gradW
     dp_f -= e.gd * ud * mj;
-    // MOG diffusion; for deltaSPH the first part of its diffusion (x 2 after the sum)
-    if (scheme == 1 || scheme == 2) mog += (rhoj - rhoi) * ir2 * rg * Vj;
+    // MOG diffusion (for deltaSPH the first part of its diffusion, formed below from the
+    // renormalization product): (rho_j - rho_i) V_j (x_j - x_i) . gradW / (r^2 + eps), x 2 after the sum
+    if (scheme == 1) mog += (rhoj - rhoi) * ir2 * rg * Vj;
     const float pf = fmaf(pi, Vj, pVj) * e.gd;            // (p_i + p_j) V_j gd
     pax += pf * e.dx;
     pay += pf * e.dy;
     const float irs = rcp_normal(rhoi + rhoj);
-    const float w = mj * irs * ir2;
-    const float vf = fminf(-ud, 0.f) * w * e.gd;          // pi_ij, (u_j - u_i) . (x_j - x_i) = -ud
+    const float wg = mj * irs * ir2 * e.gd;
+    const float vf = fminf(-ud, 0.f) * wg;                // pi_ij, (u_j - u_i) . (x_j - x_i) = -ud
     vax += vf * e.dx;
     vay += vf * e.dy;
-    const float term = mu8 * rg * irs * w;                // laminar: -term (u_i - u_j)
+    const float term = e.r2 * irs * wg;                   // laminar: mu8 term (u_j - u_i), mu8 after the sum
     lax += term * ux;
     lay += term * uy;
     if (renorm) {
@@ -336,6 +337,7 @@ __device__ __forceinline__ Pass1 pass1_body(int i, const FluidView& F, const Rec
       const float s = (rhoj - rhoi) * t;                  // x 2 after the sum
       gfx += s * e.dx;
       gfy += s * e.dy;
+      mog -= s * (e.r2 * ir2);                            // (rho_j - rho_i) V_j (-gd r^2) / (r^2 + eps)
     }
   };
   if constexpr (kCells) {
@@ -422,8 +424,8 @@ __device__ __forceinline__ Pass1 pass1_body(int i, const FluidView& F, const Rec
   ay += ir * pay + ir * pwy;
   ax += P.visc_k * vax + P.visc_k * vwx;
   ay += P.visc_k * vay + P.visc_k * vwy;
-  o.ax = ax + lax;
-  o.ay = ay + lay;
+  o.ax = ax - mu8 * lax;
+  o.ay = ay - mu8 * lay;
   o.L = make_float4(l00 + w00, l01 + w01, l01 + w10, l11 + w11);
   gfx *= 2.0f;
   gfy *= 2.0f;
