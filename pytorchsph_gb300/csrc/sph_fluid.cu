@@ -133,9 +133,9 @@ __device__ __forceinline__ PairG pair_g(float xi, float yi, float xj, float yj, 
   g.dy = yi - yj;
   g.r2 = g.dx * g.dx + g.dy * g.dy;
   const bool apart = g.r2 >= 1e-14f;
-  const float r = apart ? g.r2 * rsqrt_normal(g.r2) : 0.f;
-  const float a = 1.0f - r * P.inv_h;
-  g.gd = apart ? P.gk * (a * a * a) : 0.f;
+  const float r = g.r2 * rsqrt_normal(g.r2);   // NaN at r2 = 0, dropped by the select
+  const float a = apart ? 1.0f - r * P.inv_h : 0.f;
+  g.gd = P.gk * (a * a * a);
   return g;
 }
 
@@ -310,7 +310,8 @@ __device__ __forceinline__ Pass1 pass1_body(int i, const FluidView& F, const Rec
     const float ud = ux * e.dx + uy * e.dy;               // (u_j - u_i) . d
     const float ir2 = rcp_normal(e.r2 + P.eps);
     const float rg = -e.gd * e.r2;                        // (x_j - x_i) . gradW
-    dp_f -= e.gd * ud * mj;
+    const float mg = mj * e.gd;
+    dp_f -= mg * ud;
     // MOG diffusion (for deltaSPH the first part of its diffusion, formed below from the
     // renormalization product): (rho_j - rho_i) V_j (x_j - x_i) . gradW / (r^2 + eps), x 2 after the sum
     if (scheme == 1) mog += (rhoj - rhoi) * ir2 * rg * Vj;
@@ -318,7 +319,7 @@ __device__ __forceinline__ Pass1 pass1_body(int i, const FluidView& F, const Rec
     pax += pf * e.dx;
     pay += pf * e.dy;
     const float irs = rcp_normal(rhoi + rhoj);
-    const float wg = mj * irs * ir2 * e.gd;
+    const float wg = mg * (irs * ir2);
     const float vf = fminf(-ud, 0.f) * wg;                // pi_ij, (u_j - u_i) . (x_j - x_i) = -ud
     vax += vf * e.dx;
     vay += vf * e.dy;
