@@ -127,6 +127,9 @@ struct PairG {
   float dx, dy, r2, gd;
 };
 
+// kScaled = false: gd without its constant factor gk (a sum that is linear in gd takes gk
+// once at the end).
+template <bool kScaled = true>
 __device__ __forceinline__ PairG pair_g(float xi, float yi, float xj, float yj, const SphParams& P) {
   PairG g;
   g.dx = xi - xj;
@@ -135,7 +138,7 @@ __device__ __forceinline__ PairG pair_g(float xi, float yi, float xj, float yj, 
   const bool apart = g.r2 >= 1e-14f;
   const float r = g.r2 * rsqrt_normal(g.r2);   // NaN at r2 = 0, dropped by the select
   const float a = apart ? 1.0f - r * P.inv_h : 0.f;
-  g.gd = P.gk * (a * a * a);
+  g.gd = kScaled ? P.gk * (a * a * a) : a * a * a;
   return g;
 }
 
@@ -463,7 +466,7 @@ __device__ __forceinline__ float diffusion_sum(int i, const FluidView& F, const 
       const float Vj = __ldg(&rec[j].q.y);
       gv = make_float2(gv.x * Vj, gv.y * Vj);
     }
-    const PairG e = pair_g(xi.x, xi.y, xj.x, xj.y, P);
+    const PairG e = pair_g<false>(xi.x, xi.y, xj.x, xj.y, P);   // gk after the sum
     acc += (gv.x * e.dx + gv.y * e.dy) * e.gd;
   };
   if constexpr (kCells) {
@@ -474,7 +477,7 @@ __device__ __forceinline__ float diffusion_sum(int i, const FluidView& F, const 
     const int k0 = F.offsets[i], k1 = row_end(F, i, k0);
     for (int k = k0; k < k1; ++k) pair(__ldg(F.cols + k));
   }
-  return lane_sum<kTpp>(acc);
+  return lane_sum<kTpp>(acc) * P.gk;
 }
 
 // semiImplicitEuler, src/simulationBase.py:647-652 with integrateValues :564-569, for one
