@@ -30,3 +30,16 @@ def test_configure_sets_spec_fields_and_json_round_trip(tmp_path):
     t.save(str(p))
     u = Tuning.load(str(p))
     assert u.serving == t.serving and u.device == "GB300"
+
+
+def test_search_cell_ratio_round_trip(tmp_path):
+    """A search bucket tuned to cells of h/2 keeps its ratio through JSON; a table written
+    before the ratio was a knob reads as cells of h."""
+    t = Tuning(search={20: {"sort": "counting", "digit_bits": 8, "cell_ratio": 2,
+                            "measured": {"counting,0,2": {"ms": 0.49}}},
+                       16: {"sort": "radix", "digit_bits": 8}})
+    p = tmp_path / "tuning.json"
+    t.save(str(p))
+    u = Tuning.load(str(p))
+    assert u.search_config(1 << 20) == {"sort": "counting", "digit_bits": 8, "cell_ratio": 2}
+    assert u.search_config(1 << 16) == {"sort": "radix", "digit_bits": 8, "cell_ratio": 1}
