@@ -75,7 +75,8 @@ class CSRNeighbors:
         self._rank = None
 
     # n, order, keys, xy, sh, sa, cell_start, counts, offsets, cols, rho, grid, status,
-    # cell_capacity, pair_capacity, kernel_support, search_radius
+    # cell_capacity, pair_capacity, kernel_support, search_radius (in cells of the grid),
+    # cell_ratio (cells per support)
 
     @property
     def num_pairs(self) -> int:
@@ -142,8 +143,9 @@ class CSRNeighbors:
               original_indices: bool = True):
         """Pairs of arbitrary query points against this grid (searchExisting,
         src/modules/neighborSearch.py:231-252): rows = query index, cols = particle index
-        (original order by default), predicate |x_q - x_j| < support_q."""
-        r = self.search_radius if search_radius is None else int(search_radius)
+        (original order by default), predicate |x_q - x_j| < support_q.  search_radius counts
+        supports, as in GridSearch.run (the grid's cells are support / cell_ratio)."""
+        r = self.search_radius if search_radius is None else int(search_radius) * getattr(self, "cell_ratio", 1)
         m = qpos.shape[0]
         dev = self.order.device
         st = N.stream_ptr()
@@ -256,7 +258,7 @@ class GridSearch:
                                 sa=f32(0) if area is not None else None, cell_start=i32(2), counts=i32(0),
                                 offsets=i32(1), cols=i32(0), rho=f32(0) if density else None, grid=None,
                                 status=i32(1), cell_capacity=0, pair_capacity=0, kernel_support=kernel_support,
-                                search_radius=int(search_radius))
+                                search_radius=int(search_radius), cell_ratio=self.cell_ratio)
         if cell_capacity is None:
             cell_capacity = self.auto_cell_capacity(pos, support, min_coord, max_coord)
         cap = int(cell_capacity)
@@ -330,7 +332,7 @@ class GridSearch:
         res = CSRNeighbors(n=n, order=order, keys=skeys, xy=xy, sh=sh, sa=sa, cell_start=cell_start, counts=counts,
                            offsets=offsets, cols=cols, rho=rho, grid=grid, status=status, cell_capacity=cap,
                            pair_capacity=int(pair_capacity), kernel_support=kernel_support,
-                           search_radius=int(search_radius))
+                           search_radius=int(search_radius), cell_ratio=self.cell_ratio)
         if sync:
             res.check()
         return res

@@ -288,6 +288,16 @@ def test_finer_cells_give_the_same_pairs(cuda, cell_ratio):
     assert torch.equal(b.rho, c.rho)
     ra, rb = a.density(), b.density()   # float32 sums of up to ~300 terms in another order
     assert float((ra - rb).abs().max()) <= 1e-5 * float(ra.abs().max())
+    # queries against the finer grid (searchExisting): the same pairs, with the radius in
+    # supports whether given or taken from the search
+    q = torch.rand(3000, 2, device=dev)
+    hq = torch.full((3000,), 0.01, device=dev)
+    def pairs(res, **kw):
+        r, c = res.query(q, hq, **kw)
+        return np.unique(r.long().cpu().numpy() * n + c.long().cpu().numpy())
+    ref = pairs(a)
+    assert len(ref) > 0
+    assert np.array_equal(pairs(b), ref) and np.array_equal(pairs(b, search_radius=1), ref)
 
 
 def _host_segments(res, n):
