@@ -668,6 +668,7 @@ class SceneArena(SceneBatch):
         self.steps_done = 0
         # host bookkeeping
         self.slots = {}                    # slot -> dict(spec, n, nb, coff, ncells, grid)
+        self._cell_end = None              # end of the highest live cell range (None: recount)
         self.free_slots = list(range(self.S))
         self.occupied = 0                  # particle slots in use (live + retired before the next sort)
         self.live_n = 0
@@ -709,6 +710,7 @@ class SceneArena(SceneBatch):
             self._write_scene(slot)
             at += d["ncells"]
         self._cell_top = at
+        self._cell_end = None
         self._walls_dirty = True
 
     def _encode_row(self, slot):
@@ -781,6 +783,7 @@ class SceneArena(SceneBatch):
             raise ArenaFull("no room in the cell tables")
         slot = self.free_slots.pop(0)
         self.slots[slot] = {"spec": spec, "n": n, "nb": nb, "coff": coff, "ncells": ncells, "grid": d["grid"]}
+        self._cell_end = None
         self._write_scene(slot)
         st = N.stream_ptr()
         lo, hi = self.occupied, self.occupied + n
@@ -841,6 +844,7 @@ class SceneArena(SceneBatch):
                                 "grid": d["grid"]}
             self._cell_top += nc
             self._encode_row(slot)
+        self._cell_end = None
         self._copy_rows(min(slots), max(slots) + 1)
         st = N.stream_ptr()
         cur = self._aux(self.par)
@@ -907,6 +911,7 @@ class SceneArena(SceneBatch):
         """Take the scene in `slot` out of the arena; returns its final x, v, rho (device)."""
         out = self.scene_state_device(slot)
         d = self.slots.pop(slot)
+        self._cell_end = None
         st = N.stream_ptr()
         N.call("sph_arena_retire", N.ptr(self._aux(self.par)["sid"]), self.n, slot, st)
         if d["nb"]:
@@ -949,7 +954,9 @@ class SceneArena(SceneBatch):
     def _cell_extent(self) -> int:
         """The cell slots a step sorts into: up to the end of the highest live cell range,
         rounded up to the cell quantum (the sentinel cell of free slots sits right behind)."""
-        end = max((d["coff"] + d["ncells"] for d in self.slots.values()), default=0)
+        if self._cell_end is None:   # recounted only after admissions and retirements
+            self._cell_end = max((d["coff"] + d["ncells"] for d in self.slots.values()), default=0)
+        end = self._cell_end
         q = self._cell_quantum
         return min(self.C, max(q, -(-end // q) * q))
 
@@ -1011,6 +1018,7 @@ class SceneArena(SceneBatch):
             self._walls_dirty = True
         for sl in slots:
             d = self.slots.pop(sl)
+            self._cell_end = None
             self.walls_n -= d["nb"]
             self.live_n -= d["n"]
             bisect.insort(self.free_slots, sl)
